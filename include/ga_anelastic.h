@@ -1,0 +1,216 @@
+/*
+ * ga_anelastic.h - C ABI of the GB300 anelastic dynamical core.
+ *
+ * The reference model (michaeldiaz0/Model) has no plugin layer: its per-step
+ * "operator API" is a set of global C++ functions that read and write global
+ * arrays.  This header replaces that surface with a context object.  Each
+ * entry point below names the reference function (file:line) it stands in for.
+ *
+ * Conventions
+ *   - 3-D fields are double precision on the host side, laid out [i][j][k]
+ *     with k fastest, exactly as the reference's INDEX(i,j,k) =
+ *     i*NY*NZ + j*NZ + k (include/model.h:50).
+ *   - Every prognostic field keeps the reference's three rotation buffers
+ *     (current, forecast "P", start-of-step "M"; solver.cpp:229-263,
+ *     microphysics.cpp:642-669).  Slots are addressed with GA_SLOT_*.
+ *   - The library owns all device memory.  Host pointers are borrowed for the
+ *     duration of a call only.  Calls are synchronous (they return after the
+ *     GPU work has finished) unless the name ends in _async.
+ *   - Every entry point returns GA_OK (0) or a negative GA_ERR_* code.  The
+ *     reference prints and calls exit(0) instead (kessler.cpp:83-88); this
+ *     library never exits the process.  ga_last_error() gives the text of the
+ *     most recent error on the calling thread.
+ *   - One context per host thread.  A context is bound to one CUDA device and
+ *     one CUDA stream, created by ga_create.
+ */
+#ifndef GA_ANELASTIC_H
+#define GA_ANELASTIC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GA_ABI_VERSION 1
+
+/* ---- status codes ------------------------------------------------------ */
+#define GA_OK               0
+#define GA_ERR_ARG         -1   /* bad argument (null pointer, bad id, size) */
+#define GA_ERR_CUDA        -2   /* a CUDA runtime call failed                 */
+#define GA_ERR_NOMEM       -3   /* device allocation failed                   */
+#define GA_ERR_CONFIG      -4   /* configuration rejected (grid too small...) */
+#define GA_ERR_NONFINITE   -5   /* NaN/Inf found by ga_check_finite           */
+#define GA_ERR_KESSLER     -6   /* evaporation E>100, where the reference
+                                   calls exit(0) (kessler.cpp:83-88)          */
+#define GA_ERR_UNSUPPORTED -7   /* option not built in this library           */
+
+/* ---- precision of a context ------------------------------------------- */
+#define GA_PREC_F64 0   /* FP64 storage and arithmetic: the parity path     */
+#define GA_PREC_F32 1   /* FP32 storage and arithmetic with FP64 islands    */
+
+/* ---- field ids ---------------------------------------------------------- */
+/* prognostic fields (three rotation slots each) */
+#define GA_U      0   /* us/ups/ums     model.h:63-65   */
+#define GA_V      1   /* vs/vps/vms                      */
+#define GA_W      2   /* ws/wps/wms                      */
+#define GA_TH     3   /* ths/thps/thms                   */
+#define GA_QV     4   /* qvs/qvps/qvms  microphysics.h:18 */
+#define GA_QC     5   /* qcs/qcps/qcms                   */
+#define GA_QR     6   /* qrs/qrps/qrms                   */
+#define GA_NPROG  7
+/* single-buffer fields */
+#define GA_PI     7   /* pis: perturbation Exner pressure (diagnostic)       */
+#define GA_UBAR   8   /* m_ubar .. m_pbar: basic state (model.h:84-91)       */
+#define GA_VBAR   9
+#define GA_WBAR  10
+#define GA_THBAR 11
+#define GA_QBAR  12
+#define GA_PBAR  13
+#define GA_VT    14   /* vts: rain fall speed (microphysics.h:24)            */
+#define GA_NFIELDS 15
+/* 2-D field: accumulated rain accRain[NX][NY] (microphysics.h:25)           */
+#define GA_ACCRAIN 15
+
+/* rotation slots */
+#define GA_SLOT_CUR 0  /* us  : middle of the RK stage                        */
+#define GA_SLOT_P   1  /* ups : forecast value                                */
+#define GA_SLOT_M   2  /* ums : value at the beginning of the step            */
+
+/* ---- per-operator entry ids for ga_op ---------------------------------- */
+#define GA_OP_SIGN_CELLS        0  /* compute_sign_cells        fluxes.cpp:316  (no-op: signs are taken on the fly) */
+#define GA_OP_ADVECT_UVW        1  /* advect_uvw_velocity       advection.cpp:304 (+ buoyancy overwrite :329-337) */
+#define GA_OP_SOLVE_PRESSURE    2  /* solve_pressure            pressure.cpp:142 */
+#define GA_OP_PROJECT           3  /* gradient loop of integrate_non_hydro  solver.cpp:120-135 */
+#define GA_OP_INTEGRATE_NON_HYDRO 4 /* integrate_non_hydro      solver.cpp:87    */
+#define GA_OP_ADVECT_THETA      5  /* advect_theta              advection.cpp:349 */
+#define GA_OP_ADVECT_MICRO      6  /* advect_microphysics_cell  advection.cpp:451 */
+#define GA_OP_ZERO_MOISTURE     7  /* zero_moisture             microphysics.cpp:675 */
+#define GA_OP_BC                8  /* apply_boundary_condition  boundaries.cpp:119 */
+#define GA_OP_BC_MICRO          9  /* apply_boundary_condition_microphysics boundaries.cpp:200 */
+#define GA_OP_KESSLER          10  /* run_microphysics -> run_kessler_microphysics microphysics.cpp:97, kessler.cpp:25 */
+#define GA_OP_RAYLEIGH         11  /* rayleigh_damping          damping.cpp:1148 */
+#define GA_OP_ADVANCE_INNER    12  /* advance_inner + microphysics_advance_inner solver.cpp:241, microphysics.cpp:642 */
+#define GA_OP_ADVANCE_OUTER    13  /* advance_outer + microphysics_advance       solver.cpp:254, microphysics.cpp:657 */
+#define GA_OP_COUNT            14
+
+/*
+ * Runtime configuration: the subset of the reference's struct input_params
+ * (include/stdafx.h:126-203) that the step reads, after initialize_globals
+ * (initializer.cpp:160-245) has copied it into globals.  The compile-time
+ * choices of the reference build (5th/3rd order advection, non-hydrostatic,
+ * nonlinear, stretched-grid code path) are fixed in the kernels.
+ */
+typedef struct ga_config {
+    int    nx, ny, nz;              /* NX, NY, NZ                                   */
+    double dx, dy, dz, dt;          /* grid spacing (m) and time step (s)           */
+    int    microphysics_option;     /* 0 none, 1 Kessler (2 = ice: unsupported)     */
+    int    rain_fallout;            /* 1 Eulerian, 2 semi-Lagrangian (PPM)          */
+    int    periodic_ew_boundaries;  /* 0 sponge on all sides, 1 periodic east-west  */
+    int    boundary_width_north;    /* jnbuffer  (boundaries.cpp:23-26)             */
+    int    boundary_width_south;    /* jsbuffer                                     */
+    int    boundary_width_east;     /* iebuffer                                     */
+    int    boundary_width_west;     /* iwbuffer                                     */
+    int    rayleigh_damping_z;      /* raydampheight: first damped level            */
+    int    precision;               /* GA_PREC_F64 or GA_PREC_F32                   */
+    int    device;                  /* CUDA device ordinal                           */
+} ga_config;
+
+/*
+ * Vertical columns and the other small arrays the step reads.  The caller
+ * fills them (ga_columns_build does it from tb/qb exactly as the reference's
+ * initialize_vertical_basic_state2, initializer.cpp:858-928) and the library
+ * copies them.  All arrays are double.
+ */
+typedef struct ga_columns {
+    const double *zu, *zw;            /* [NZ] unstretched heights (initializer.cpp:840-849) */
+    const double *zsu, *zsw;          /* [NZ] stretched heights (stretched_grid :1340)      */
+    const double *mu, *mw;            /* [NZ] grid-stretching factors                       */
+    const double *rhou, *rhow;        /* [NZ] base-state density at u and w levels          */
+    const double *one_d_rhou, *one_d_rhow;
+    const double *tb, *tbv, *tbw, *qb, *pib;   /* [NZ] base-state theta, theta_v, q, Exner */
+    const double *f;                  /* [NY] Coriolis parameter (initializer.cpp:826)      */
+} ga_columns;
+
+/* Owned storage for a ga_columns, filled by ga_columns_build. */
+typedef struct ga_column_store {
+    double zu[512], zw[512], zsu[512], zsw[512], mu[512], mw[512];
+    double rhou[512], rhow[512], one_d_rhou[512], one_d_rhow[512];
+    double tb[512], tbv[512], tbw[512], qb[512], pib[512];
+} ga_column_store;
+
+typedef struct ga_ctx ga_ctx;
+
+/* ---- library ----------------------------------------------------------- */
+int         ga_abi_version(void);
+const char *ga_last_error(void);
+
+/*
+ * Build the vertical column arrays from the base-state theta tb[NZ] and
+ * humidity qb[NZ] profiles.  Replaces setup_vertical_height_levels
+ * (initializer.cpp:840), stretched_grid (:1340) and
+ * initialize_vertical_basic_state2 (:858-928), including their in-place edits
+ * of tb/qb (tb[0]=tb[1] etc.).  height_lowest_level is the reference input of
+ * the same name.  Host-only; needs no GPU.
+ */
+int ga_columns_build(int nz, double dz, double height_lowest_level,
+                     const double *tb_in, const double *qb_in,
+                     ga_column_store *out);
+
+/*
+ * Coriolis parameter f[j] for a domain whose south-west corner is given by the
+ * reference's corner_lat input: setup_coordinates(0,-89.462997)
+ * (initializer.cpp:1948-1967) then initialize_coriolis_parameter (:826-833).
+ * Host-only.
+ */
+int ga_coriolis_build(int ny, double dy, double corner_lat, double *f_out);
+
+/* ---- context ------------------------------------------------------------ */
+/* Replaces initialize_serial's solver set-up: initialize_pressure_solver
+ * (pressure.cpp:99), init_boundaries (boundaries.cpp:44), init_microphysics
+ * (microphysics.cpp:41).  Allocates every device buffer (zeroed, as the
+ * reference's calloc) and precomputes the spectral and sponge tables. */
+int ga_create(const ga_config *cfg, const ga_columns *cols, ga_ctx **out);
+int ga_destroy(ga_ctx *ctx);
+
+/* Copy one field between host and device.  For prognostic fields `slot` picks
+ * the rotation buffer; for the others it is ignored.  n must equal NX*NY*NZ
+ * (NX*NY for GA_ACCRAIN).  Values are converted to/from FP32 for FP32
+ * contexts. */
+int ga_set_field(ga_ctx *ctx, int field, int slot, const double *host, size_t n);
+int ga_get_field(ga_ctx *ctx, int field, int slot, double *host, size_t n);
+
+/* Advance nsteps full RK3 steps: nsteps calls of s_integrate_rk3
+ * (driver_serial.cpp:178-286), each followed by the counter updates of
+ * s_run_model (bigcounter++, mtime += dt; driver_serial.cpp:366-369). */
+int ga_step(ga_ctx *ctx, int nsteps);
+/* Same, queued on the context's stream without a final synchronize. */
+int ga_step_async(ga_ctx *ctx, int nsteps);
+int ga_synchronize(ga_ctx *ctx);
+
+/* Run a single operator (GA_OP_*) with RK fraction `step`, for per-operator
+ * parity tests.  Mirrors calling the reference global function directly. */
+int ga_op(ga_ctx *ctx, int op, double step);
+
+/* Number of completed steps (reference: bigcounter) and model time (mtime). */
+int ga_get_counters(ga_ctx *ctx, long long *bigcounter, double *mtime);
+
+/* Scan the prognostic forecast buffers for NaN/Inf on the device.
+ * Returns GA_OK or GA_ERR_NONFINITE.  The reference has no such check. */
+int ga_check_finite(ga_ctx *ctx);
+
+/* Number of kernel launches issued by this context since creation. */
+long long ga_launch_count(ga_ctx *ctx);
+
+/* CUDA stream the context runs on (a cudaStream_t, as void*). */
+void *ga_stream(ga_ctx *ctx);
+
+/* Device pointer of a field buffer (FP64 or FP32 per the precision), for
+ * callers that keep state resident on the GPU. */
+void *ga_field_device_ptr(ga_ctx *ctx, int field, int slot);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GA_ANELASTIC_H */

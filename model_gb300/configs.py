@@ -1,0 +1,290 @@
+"""Seeded synthetic initial states for the benchmark and test workloads.
+
+The reference initialises from NetCDF files written by its Python tools
+(initialize.py:52-111, sample_initializations.py:371-492); no such file ships
+with it and NetCDF is not available here, so these generators build the same
+kinds of state in memory: a horizontally uniform basic state from an analytic
+sounding (theta, humidity, wind profiles), and a perturbation (warm bubble,
+line thermal, vortex) plus seeded uniform noise.  Values are produced once on
+the host and fed bit-identically to the CPU oracle and to the GPU.
+
+Random numbers come from splitmix64 (integer arithmetic, so identical on every
+platform), seeded with 1000 + workload id (+ 7919 * member for ensembles).
+
+Layout of every 3-D array: [i][j][k], k fastest (reference INDEX, model.h:50).
+"""
+from __future__ import annotations
+
+import dataclasses
+import math
+
+import numpy as np
+
+# physical constants of the reference (include/model.h:248-259)
+RD = 287.0
+CP = 1004.0
+P0 = 100000.0
+GRAV = 9.8
+PRESSFC = 100200.0
+
+_SM_GAMMA = np.uint64(0x9E3779B97F4A7C15)
+_SM_M1 = np.uint64(0xBF58476D1CE4E5B9)
+_SM_M2 = np.uint64(0x94D049BB133111EB)
+
+
+def splitmix_uniform(seed: int, n: int) -> np.ndarray:
+    """n doubles uniform in [0, 1) from the splitmix64 stream of `seed`."""
+    with np.errstate(over="ignore"):
+        idx = np.arange(1, n + 1, dtype=np.uint64)
+        z = np.uint64(seed & 0xFFFFFFFFFFFFFFFF) + idx * _SM_GAMMA
+        z = (z ^ (z >> np.uint64(30))) * _SM_M1
+        z = (z ^ (z >> np.uint64(27))) * _SM_M2
+        z = z ^ (z >> np.uint64(31))
+    return (z >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0)
+
+
+@dataclasses.dataclass
+class Workload:
+    """One initial state plus the runtime settings the step reads."""
+
+    name: str
+    nx: int
+    ny: int
+    nz: int
+    dx: float
+    dy: float
+    dz: float
+    dt: float
+    nsteps: int
+    microphysics_option: int = 0
+    rain_fallout: int = 1
+    periodic_ew_boundaries: int = 0
+    boundary_width_north: int = 5
+    boundary_width_south: int = 5
+    boundary_width_east: int = 5
+    boundary_width_west: int = 5
+    rayleigh_damping_z: int = -1  # default NZ - 5
+    height_lowest_level: float = -1.0  # default dz (uniform grid)
+    corner_lat: float = 120.0
+    fields: dict = dataclasses.field(default_factory=dict)
+
+    def __post_init__(self):
+        if self.rayleigh_damping_z < 0:
+            self.rayleigh_damping_z = self.nz - 5
+        if self.height_lowest_level < 0:
+            self.height_lowest_level = self.dz
+
+    @property
+    def points(self) -> int:
+        return self.nx * self.ny * self.nz
+
+    def settings(self) -> dict:
+        keys = ("nx", "ny", "nz", "dx", "dy", "dz", "dt", "microphysics_option", "rain_fallout",
+                "periodic_ew_boundaries", "boundary_width_north", "boundary_width_south",
+                "boundary_width_east", "boundary_width_west", "rayleigh_damping_z",
+                "height_lowest_level", "corner_lat")
+        return {k: getattr(self, k) for k in keys}
+
+
+# ---------------------------------------------------------------------------
+# soundings
+# ---------------------------------------------------------------------------
+def _levels(nz: int, dz: float) -> np.ndarray:
+    """Heights of the scalar levels of the uniform grid: zu[k] = (k-0.5) dz
+    (initializer.cpp:843)."""
+    return (np.arange(nz, dtype=np.float64) - 0.5) * dz
+
+
+def _exner_profile(theta_v: np.ndarray, zu: np.ndarray) -> np.ndarray:
+    """Hydrostatic Exner function on the scalar levels, integrated upward
+    from the surface value (same recurrence as initializer.cpp:887-893)."""
+    nz = zu.size
+    pib = np.zeros(nz)
+    pisfc = (PRESSFC / P0) ** (RD / CP)
+    pib[1] = pisfc - GRAV * zu[1] / (CP * theta_v[1])
+    pib[0] = pisfc + GRAV * (0 - zu[0]) / (CP * theta_v[0])
+    for k in range(2, nz):
+        pib[k] = pib[k - 1] - GRAV * (zu[k] - zu[k - 1]) / (CP * 0.5 * (theta_v[k] + theta_v[k - 1]))
+    return pib
+
+
+def _qvsat(temperature, pressure):
+    esl = 611.2 * np.exp(17.67 * (temperature - 273.15) / (temperature - 29.65))
+    return 0.62197 * esl / (pressure - esl)
+
+
+def thunderstorm_sounding(nz: int, dz: float, u_top: float = 15.0, shear_depth: float = 6000.0):
+    """Weisman-Klemp style sounding: theta 300 K at the surface rising as
+    (z/12 km)^1.25 to 343 K at a 12 km tropopause, isothermal (213 K) above
+    (shape of sample_initializations.py:422-427); relative humidity 0.95 at
+    the surface falling linearly to 0.25 at 12 km, vapour capped at 14 g/kg;
+    u rising linearly from 0 to u_top over shear_depth, constant above."""
+    zu = _levels(nz, dz)
+    z = np.maximum(zu, 0.0)
+    ztr, ttr, tsurf, temptr = 12000.0, 343.0, 300.0, 213.0
+    theta = np.where(z < ztr, tsurf + (ttr - tsurf) * (z / ztr) ** 1.25,
+                     ttr * np.exp(GRAV * (z - ztr) / (CP * temptr)))
+    rh = np.where(z < ztr, 0.95 - (0.95 - 0.25) * z / ztr, 0.25)
+    qv = np.zeros(nz)
+    for _ in range(4):  # fixed point: Exner depends on theta_v
+        pib = _exner_profile(theta * (1.0 + 0.61 * qv), zu)
+        temp = theta * pib
+        pres = P0 * pib ** (CP / RD)
+        qv = np.minimum(rh * _qvsat(temp, pres), 0.014)
+    ubar = u_top * np.minimum(z / shear_depth, 1.0)
+    return theta, qv, ubar
+
+
+def stable_sounding(nz: int, dz: float, theta0: float = 300.0, bv: float = 0.01):
+    """Constant Brunt-Vaisala frequency: theta = theta0 exp(N^2 z / g)."""
+    z = np.maximum(_levels(nz, dz), 0.0)
+    return theta0 * np.exp(bv * bv * z / GRAV)
+
+
+def _grid_xyz(nx, ny, nz, dx, dy, dz):
+    x = (np.arange(nx) + 0.5) * dx
+    y = (np.arange(ny) + 0.5) * dy
+    z = _levels(nz, dz)
+    return x, y, z
+
+
+def _basic_state(wl: Workload, theta_col, qv_col, u_col):
+    n3 = (wl.nx, wl.ny, wl.nz)
+    f = wl.fields
+    f["tb_in"] = np.array(theta_col, dtype=np.float64)
+    f["qb_in"] = np.array(qv_col, dtype=np.float64)
+    f["ubar"] = np.broadcast_to(u_col, n3).copy()
+    f["vbar"] = np.zeros(n3)
+    f["wbar"] = np.zeros(n3)
+    f["thbar"] = np.zeros(n3)
+    f["qbar"] = np.zeros(n3)
+    # basic-state Exner pressure, full value (PBAR, model.h:91): the 1-D
+    # profile of the column builder broadcast horizontally
+    tb = np.array(theta_col, dtype=np.float64)
+    qb = np.array(qv_col, dtype=np.float64)
+    tb[0], tb[-1], qb[0], qb[-1] = tb[1], tb[-2], qb[1], qb[-2]
+    pib = _exner_profile(tb * (1.0 + 0.61 * qb), _levels(wl.nz, wl.dz))
+    pib[0], pib[-1] = pib[1], pib[-2]
+    f["pbar"] = np.broadcast_to(pib, n3).copy()
+
+
+def _zero_perturbation(wl: Workload):
+    n3 = (wl.nx, wl.ny, wl.nz)
+    for k in ("u", "v", "w", "th", "qv", "qc", "qr"):
+        wl.fields[k] = np.zeros(n3)
+
+
+def _add_noise(wl: Workload, seed: int, amp: float):
+    """U(-amp, amp) on theta' at every interior level k = 1..NZ-2."""
+    r = splitmix_uniform(seed, wl.points).reshape(wl.nx, wl.ny, wl.nz)
+    noise = amp * (2.0 * r - 1.0)
+    noise[:, :, 0] = 0.0
+    noise[:, :, -1] = 0.0
+    wl.fields["th"] += noise
+
+
+# ---------------------------------------------------------------------------
+# workloads
+# ---------------------------------------------------------------------------
+def dry_bubble(nx=64, ny=64, nz=40, dx=500.0, dz=250.0, dt=2.0, nsteps=100, seed=1001,
+               amp=2.0, radius=2000.0, zc=2000.0, noise=0.01) -> Workload:
+    """Dry warm bubble: basic state at rest, theta 300 K at the surface with
+    N = 0.01 1/s; theta' = amp exp(-r^2/radius^2) centred at (domain centre,
+    zc) plus U(+-noise) everywhere."""
+    wl = Workload("dry_bubble", nx, ny, nz, dx, dx, dz, dt, nsteps, microphysics_option=0)
+    _basic_state(wl, stable_sounding(nz, dz), np.zeros(nz), np.zeros(nz))
+    _zero_perturbation(wl)
+    x, y, z = _grid_xyz(nx, ny, nz, dx, dx, dz)
+    xc, yc = 0.5 * nx * dx, 0.5 * ny * dx
+    r2 = ((x[:, None, None] - xc) ** 2 + (y[None, :, None] - yc) ** 2
+          + (z[None, None, :] - zc) ** 2) / radius ** 2
+    wl.fields["th"] += amp * np.exp(-r2)
+    _add_noise(wl, seed, noise)
+    return wl
+
+
+def thunderstorm(nx=128, ny=128, nz=48, dx=1000.0, dz=400.0, dt=4.0, nsteps=600, seed=1002,
+                 amp=3.0, rh=10000.0, rz=1500.0, zc=1500.0, noise=0.05, u_top=15.0,
+                 shear_depth=6000.0, rain_fallout=1, name="thunderstorm") -> Workload:
+    """Kessler moist thunderstorm: thunderstorm_sounding basic state; theta'
+    = amp * (1 + cos(pi r))/2 for r <= 1 with r the distance from (domain
+    centre, zc) scaled by rh horizontally and rz vertically (shape of
+    sample_initializations.py:349-362), plus U(+-noise)."""
+    wl = Workload(name, nx, ny, nz, dx, dx, dz, dt, nsteps, microphysics_option=1,
+                  rain_fallout=rain_fallout)
+    th, qv, u = thunderstorm_sounding(nz, dz, u_top, shear_depth)
+    _basic_state(wl, th, qv, u)
+    _zero_perturbation(wl)
+    x, y, z = _grid_xyz(nx, ny, nz, dx, dx, dz)
+    xc, yc = 0.5 * nx * dx, 0.5 * ny * dx
+    r = np.sqrt(((x[:, None, None] - xc) / rh) ** 2 + ((y[None, :, None] - yc) / rh) ** 2
+                + ((z[None, None, :] - zc) / rz) ** 2)
+    wl.fields["th"] += np.where(r <= 1.0, amp * 0.5 * (1.0 + np.cos(math.pi * r)), 0.0)
+    _add_noise(wl, seed, noise)
+    return wl
+
+
+def squall_line(nx=512, ny=512, nz=64, dx=1000.0, dz=300.0, dt=3.0, nsteps=400, seed=1005,
+                amp=2.0, half_width=5000.0, depth=3000.0, mod=0.15) -> Workload:
+    """Squall line: thunderstorm sounding with 0 -> 20 m/s shear over 0-2.5 km;
+    a line thermal of amp K with a half-cosine of half-width `half_width`
+    across x, extending along y with a seeded, y-smoothed +-mod amplitude
+    modulation, and a half-cosine in z up to `depth`."""
+    wl = Workload("squall_line", nx, ny, nz, dx, dx, dz, dt, nsteps, microphysics_option=1)
+    th, qv, u = thunderstorm_sounding(nz, dz, 20.0, 2500.0)
+    _basic_state(wl, th, qv, u)
+    _zero_perturbation(wl)
+    x, y, z = _grid_xyz(nx, ny, nz, dx, dx, dz)
+    x0 = 0.5 * nx * dx
+    xi = 2.0 * splitmix_uniform(seed, ny) - 1.0
+    kern = np.ones(9) / 9.0
+    xi = np.convolve(np.pad(xi, 4, mode="wrap"), kern, mode="valid")
+    xi = xi / max(np.abs(xi).max(), 1e-12)
+    sx = 0.5 * (1.0 + np.cos(math.pi * np.minimum(np.abs(x - x0) / half_width, 1.0)))
+    sz = np.where((z > 0) & (z < depth), 0.5 * (1.0 + np.cos(math.pi * (z / depth - 0.5) * 2.0)) , 0.0)
+    wl.fields["th"] += (amp * (1.0 + mod * xi)[None, :, None]) * sx[:, None, None] * sz[None, None, :]
+    _add_noise(wl, seed + 1, 0.01)
+    return wl
+
+
+def moist_blob(nx=24, ny=22, nz=16, dx=1000.0, dz=500.0, dt=4.0, nsteps=3, seed=2001,
+               rain_fallout=1, periodic=0, qc=1.5e-3, qr=2.0e-3) -> Workload:
+    """Small moist test case that exercises every Kessler branch from the
+    first step: a warm, cloudy, rainy blob (theta' 2 K, qc and qr set) in the
+    thunderstorm sounding, with seeded noise on all perturbation fields."""
+    wl = Workload("moist_blob", nx, ny, nz, dx, dx, dz, dt, nsteps, microphysics_option=1,
+                  rain_fallout=rain_fallout, periodic_ew_boundaries=periodic,
+                  boundary_width_north=3, boundary_width_south=3, boundary_width_east=3,
+                  boundary_width_west=3)
+    th, qv, u = thunderstorm_sounding(nz, dz, 12.0, 4000.0)
+    _basic_state(wl, th, qv, u)
+    _zero_perturbation(wl)
+    x, y, z = _grid_xyz(nx, ny, nz, dx, dx, dz)
+    xc, yc = 0.5 * nx * dx, 0.5 * ny * dx
+    r = np.sqrt(((x[:, None, None] - xc) / (0.3 * nx * dx)) ** 2
+                + ((y[None, :, None] - yc) / (0.3 * ny * dx)) ** 2
+                + ((z[None, None, :] - 2500.0) / 2000.0) ** 2)
+    blob = np.where(r <= 1.0, 0.5 * (1.0 + np.cos(math.pi * r)), 0.0)
+    f = wl.fields
+    n3 = (nx, ny, nz)
+    rnd = [2.0 * splitmix_uniform(seed + s, wl.points).reshape(n3) - 1.0 for s in range(6)]
+    f["th"] += 2.0 * blob + 0.3 * rnd[0]
+    f["u"] += 2.0 * rnd[1]
+    f["v"] += 2.0 * rnd[2]
+    f["w"] += 0.5 * rnd[3] * blob
+    f["qv"] += 1.0e-3 * blob
+    f["qc"] += qc * blob * (1.0 + 0.5 * rnd[4])
+    f["qr"] += qr * blob * (1.0 + 0.5 * rnd[5])
+    return wl
+
+
+WORKLOADS = {
+    "dry_bubble": dry_bubble,
+    "thunderstorm": thunderstorm,
+    "squall_line": squall_line,
+    "moist_blob": moist_blob,
+}
+
+
+def make(name: str, **kw) -> Workload:
+    return WORKLOADS[name](**kw)

@@ -1,0 +1,37 @@
+#!/bin/bash
+# Builds the reference's serial step (PARALLEL 0) as a CPU oracle into
+# oracle/_ref/, from the reference's own sources where they lie.
+#   usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
+# Only include/stdafx.h is copied into the build folder, with PARALLEL set to
+# 0 as the serial Makefile path expects; every other reference file is
+# compiled in place, unmodified.  main.cpp and files.cpp are replaced by
+# oracle/ref/ref_harness.cpp (in-memory initial state, bundle dump) and FFTW3
+# by oracle/ref/fftw_shim.cpp.  g++ -O3 as in the reference Makefile; no FMA
+# contraction, so x86 and Arm hosts compute the same values.
+# TEST INFRASTRUCTURE: the output is never shipped or called by the library.
+set -euo pipefail
+REF=${1:-/root/reference}
+HERE=$(cd "$(dirname "$0")" && pwd)
+OUT="$HERE/_ref"
+if [ ! -f "$REF/source/pressure.cpp" ]; then
+    echo "reference sources not found under $REF" >&2
+    exit 3
+fi
+mkdir -p "$OUT/include" "$OUT/obj"
+sed 's/^#define PARALLEL 1/#define PARALLEL 0/' "$REF/include/stdafx.h" > "$OUT/include/stdafx.h"
+grep -q '^#define PARALLEL 0' "$OUT/include/stdafx.h"
+CXXFLAGS="-O3 -ffp-contract=off -w -I$OUT/include -I$HERE/ref/shim -I$REF/include"
+SRCS="solver initializer data_initializer interpolate fluxes pressure advection turbulence damping
+      boundaries util Heating kessler rutledge microphysics energy trajectory laplacian
+      process_input driver_serial"
+pids=()
+for s in $SRCS; do
+    g++ $CXXFLAGS -c "$REF/source/$s.cpp" -o "$OUT/obj/$s.o" & pids+=($!)
+done
+g++ $CXXFLAGS -c "$HERE/ref/ref_harness.cpp" -o "$OUT/obj/ref_harness.o" & pids+=($!)
+g++ $CXXFLAGS -c "$HERE/ref/fftw_shim.cpp" -o "$OUT/obj/fftw_shim.o" & pids+=($!)
+g++ $CXXFLAGS -c "$HERE/ref/files_stub.cpp" -o "$OUT/obj/files_stub.o" & pids+=($!)
+gcc -O3 -ffp-contract=off -c "$HERE/ora_fft.c" -o "$OUT/obj/ora_fft.o" & pids+=($!)
+for p in "${pids[@]}"; do wait "$p"; done
+g++ -o "$OUT/ref_harness" "$OUT"/obj/*.o -lm
+echo "built $OUT/ref_harness"

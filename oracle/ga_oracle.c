@@ -1,0 +1,1139 @@
+/*
+ * ga_oracle.c - CPU restatement (FP64) of the reference's per-step dynamical
+ * core: s_integrate_rk3 (source/driver_serial.cpp:178-286) and everything it
+ * calls on the non-hydrostatic, nonlinear, serial path.
+ *
+ * TEST INFRASTRUCTURE, NOT PRODUCT CODE: the parity oracle and the CPU
+ * baseline.  Built with -ffp-contract=off so no multiply-add is fused.
+ *
+ * Structure (own design, not the reference's): instead of sweeping YZ slabs of
+ * "cell" structs and carrying the west face over from the previous column,
+ * every face flux is a pure function of the current fields, evaluated where a
+ * tendency needs it.  The arithmetic inside each face and tendency keeps the
+ * reference expression's evaluation order, so the values are identical.
+ * Index helpers: IX(i,j,k) = (i*NY + j)*NZ + k, the reference's INDEX.
+ */
+#include "ga_oracle.h"
+#include "ora_fft.h"
+
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* physical constants: include/model.h:248-259 */
+static const double Rd = 287.0, cp = 1004, cv = 717, p0 = 100000, grav = 9.8, Lv = 2.5e6;
+static const double trigpi = 3.14159265358979324;
+static const double pressfc = 100200;
+static const double fc = 7.292e-5;
+static const double meters_per_degree = 111000;
+/* interpolation weights: fluxes.cpp:247-251 */
+static const double onetwelfth = 1.0 / 12.0;
+static const double seventwelfth = 7.0 / 12.0;
+static const double thirtyseven60ths = 37.0 / 60.0;
+static const double two15ths = 2.0 / 15.0;
+static const double one60ths = 1.0 / 60.0;
+static const double minvar = 1.0e-12; /* kessler.cpp:5 */
+
+enum { F_U, F_V, F_W, F_TH, F_QV, F_QC, F_QR };
+
+struct ora_state {
+    ga_config c;
+    int NX, NY, NZ;
+    long N;
+    double dx, dy, dz, dt, dtx, dty, dtz, one_d_dx, one_d_dy, one_d_dz;
+    double *zu, *zw, *zsu, *zsw, *mu, *mw, *rhou, *rhow, *one_d_rhou, *one_d_rhow;
+    double *tb, *tbv, *tbw, *qb, *pib, *f;
+    double *buf[GA_NPROG][3];
+    double *cur[GA_NPROG], *P[GA_NPROG], *M[GA_NPROG];
+    double *pi, *bar[6], *vt, *accrain;
+    /* pressure solver */
+    int ni, nj, nk, ioff;
+    double *hcoef;  /* (cos kx + cos ly) - 2, per (p,q) */
+    double *acoef, *ccoef, *vcoef;
+    double *spec;   /* complex [k][p][q] */
+    double *specw;  /* work */
+    ora_fft_plan fi, fj;
+    /* sponge */
+    double *east_coeff, *west_coeff, *north_coeff, *south_coeff;
+    int eb, ee, wb, we, nb, ne, sb, se;
+    /* rayleigh */
+    int raylevel;
+    double *ray_u, *ray_w;
+    /* PPM remap scratch; qp_edges persists between calls as in the reference */
+    double *qp_edges, *qn_edges, *mono;
+    double *za, *qa, *qd, *ve;
+    long long bigcounter;
+    double mtime;
+    int err;
+};
+
+#define IX(i, j, k) (((long)(i) * S->NY + (j)) * S->NZ + (k))
+#define IX2(i, j) ((long)(i) * S->NY + (j))
+
+static inline double sgn(double x) { return x > 0 ? 1.0 : -1.0; } /* signof, fluxes.cpp:295-311 */
+
+/* INTERP_5TH_EAST of fluxes.cpp:110-122 with the 6-point stencil passed as
+ * a(-2) .. a(+3) around the face between a0 and a1. */
+static inline double face5(double am2, double am1, double a0, double a1, double a2, double a3,
+                           double sign)
+{
+    double c6 = thirtyseven60ths * (a1 + a0) - two15ths * (a2 + am1) + one60ths * (a3 + am2);
+    double u5 = -(a3 - am2) + 5.0 * (a2 - am1) - 10.0 * (a1 - a0);
+    return c6 + one60ths * sign * u5;
+}
+
+/* INTERP_3RD_TOP of fluxes.cpp:131-136: 4-point stencil a(-1)..a(+2) */
+static inline double face3(double am1, double a0, double a1, double a2, double sign)
+{
+    double c4 = seventwelfth * (a1 + a0) - onetwelfth * (a2 + am1);
+    double u3 = (a2 - am1) - 3.0 * (a1 - a0);
+    return c4 + onetwelfth * sign * u3;
+}
+
+/* stencil fetch helpers along i, j, k */
+#define SI(a, i, j, k)                                                                        \
+    a[IX((i)-2, j, k)], a[IX((i)-1, j, k)], a[IX(i, j, k)], a[IX((i) + 1, j, k)],           \
+        a[IX((i) + 2, j, k)], a[IX((i) + 3, j, k)]
+#define SJ(a, i, j, k)                                                                        \
+    a[IX(i, (j)-2, k)], a[IX(i, (j)-1, k)], a[IX(i, j, k)], a[IX(i, (j) + 1, k)],           \
+        a[IX(i, (j) + 2, k)], a[IX(i, (j) + 3, k)]
+#define SK(a, i, j, k) a[IX(i, j, (k)-1)], a[IX(i, j, k)], a[IX(i, j, (k) + 1)], a[IX(i, j, (k) + 2)]
+
+/* ------------------------------------------------------------------------
+ * Momentum face fluxes: interpolate_velocity (fluxes.cpp:1384-1592),
+ * advecting_velocity (:1109-1164), compute_fluxes (:582-627).
+ * ---------------------------------------------------------------------- */
+static double u_east(const ora_state *S, int i, int j, int k)
+{
+    const double *U = S->cur[F_U], *UB = S->bar[0];
+    double ua = 0.5 * (U[IX(i + 1, j, k)] + U[IX(i, j, k)]);
+    double uba = 0.5 * (UB[IX(i + 1, j, k)] + UB[IX(i, j, k)]);
+    double ue = face5(SI(U, i, j, k), sgn(uba + ua));
+    double ube = face5(SI(UB, i, j, k), sgn(ua));
+    return ua * ube + (uba + ua) * ue;
+}
+static double u_north(const ora_state *S, int i, int j, int k)
+{
+    const double *U = S->cur[F_U], *UB = S->bar[0], *V = S->cur[F_V], *VB = S->bar[1];
+    double va = 0.5 * (V[IX(i, j + 1, k)] + V[IX(i - 1, j + 1, k)]);
+    double vba = 0.5 * (VB[IX(i, j + 1, k)] + VB[IX(i - 1, j + 1, k)]);
+    double un = face5(SJ(U, i, j, k), sgn(vba + va));
+    double ubn = face5(SJ(UB, i, j, k), sgn(va));
+    return va * ubn + (vba + va) * un;
+}
+static double u_top(const ora_state *S, int i, int j, int k)
+{
+    if (k == 0) return 0.0; /* compute_fluxes :591 */
+    const double *U = S->cur[F_U], *UB = S->bar[0], *W = S->cur[F_W], *WB = S->bar[2];
+    double wa = 0.5 * (W[IX(i, j, k + 1)] + W[IX(i - 1, j, k + 1)]);
+    double wba = 0.5 * (WB[IX(i, j, k + 1)] + WB[IX(i - 1, j, k + 1)]);
+    double ut, ubt;
+    if (k == 1 || k == S->NZ - 2) { /* interpolate_velocity_vertical_2nd :1170 */
+        ut = 0.5 * (U[IX(i, j, k + 1)] + U[IX(i, j, k)]);
+        ubt = 0.5 * (UB[IX(i, j, k + 1)] + UB[IX(i, j, k)]);
+    } else {
+        ut = face3(SK(U, i, j, k), sgn(wba + wa));
+        ubt = face3(SK(UB, i, j, k), sgn(wa));
+    }
+    return wa * ubt + (wba + wa) * ut;
+}
+static double v_east(const ora_state *S, int i, int j, int k)
+{
+    const double *U = S->cur[F_U], *UB = S->bar[0], *V = S->cur[F_V], *VB = S->bar[1];
+    double ua = 0.5 * (U[IX(i + 1, j, k)] + U[IX(i + 1, j - 1, k)]);
+    double uba = 0.5 * (UB[IX(i + 1, j, k)] + UB[IX(i + 1, j - 1, k)]);
+    double ve = face5(SI(V, i, j, k), sgn(uba + ua));
+    double vbe = face5(SI(VB, i, j, k), sgn(ua));
+    return ua * vbe + (uba + ua) * ve;
+}
+static double v_north(const ora_state *S, int i, int j, int k)
+{
+    const double *V = S->cur[F_V], *VB = S->bar[1];
+    double va = 0.5 * (V[IX(i, j + 1, k)] + V[IX(i, j, k)]);
+    double vba = 0.5 * (VB[IX(i, j + 1, k)] + VB[IX(i, j, k)]);
+    double vn = face5(SJ(V, i, j, k), sgn(vba + va));
+    double vbn = face5(SJ(VB, i, j, k), sgn(va));
+    return va * vbn + (vba + va) * vn;
+}
+static double v_top(const ora_state *S, int i, int j, int k)
+{
+    if (k == 0) return 0.0;
+    const double *V = S->cur[F_V], *VB = S->bar[1], *W = S->cur[F_W], *WB = S->bar[2];
+    double wa = 0.5 * (W[IX(i, j, k + 1)] + W[IX(i, j - 1, k + 1)]);
+    double wba = 0.5 * (WB[IX(i, j, k + 1)] + WB[IX(i, j - 1, k + 1)]);
+    double vt, vbt;
+    if (k == 1 || k == S->NZ - 2) {
+        vt = 0.5 * (V[IX(i, j, k + 1)] + V[IX(i, j, k)]);
+        vbt = 0.5 * (VB[IX(i, j, k + 1)] + VB[IX(i, j, k)]);
+    } else {
+        vt = face3(SK(V, i, j, k), sgn(wba + wa));
+        vbt = face3(SK(VB, i, j, k), sgn(wa));
+    }
+    return wa * vbt + (wba + wa) * vt;
+}
+
+/* advect_uvw_velocity (advection.cpp:304-339) with u_tend_cell (:73-94) and
+ * v_tend_cell (:101-122).  The WCELL flux tendency written at :323 is
+ * overwritten by the buoyancy loop (:329-337) before anyone reads it, so only
+ * the buoyancy update is restated. */
+static void op_advect_uvw(ora_state *S, double step)
+{
+    const int NX = S->NX, NY = S->NY, NZ = S->NZ;
+    const double *U = S->cur[F_U], *V = S->cur[F_V];
+    const double *rhow = S->rhow, *one_d_rhou = S->one_d_rhou;
+    for (int i = 3; i < NX - 3; i++)
+        for (int j = 3; j < NY - 3; j++)
+            for (int k = 1; k < NZ - 1; k++) {
+                double DTZ = S->dtz * S->mu[k];
+                double ov_u = 0.25 * (V[IX(i, j, k)] + V[IX(i, j + 1, k)] + V[IX(i - 1, j, k)] +
+                                      V[IX(i - 1, j + 1, k)]);
+                double ut = -S->dtx * (u_east(S, i, j, k) - u_east(S, i - 1, j, k)) -
+                            S->dty * (u_north(S, i, j, k) - u_north(S, i, j - 1, k)) -
+                            DTZ * (rhow[k + 1] * u_top(S, i, j, k) - rhow[k] * u_top(S, i, j, k - 1)) *
+                                one_d_rhou[k] +
+                            S->dt * S->f[j] * ov_u;
+                S->P[F_U][IX(i, j, k)] = S->M[F_U][IX(i, j, k)] + step * ut;
+
+                double ov_v = 0.25 * (U[IX(i, j, k)] + U[IX(i + 1, j, k)] + U[IX(i, j - 1, k)] +
+                                      U[IX(i + 1, j - 1, k)]);
+                double vt = -S->dtx * (v_east(S, i, j, k) - v_east(S, i - 1, j, k)) -
+                            S->dty * (v_north(S, i, j, k) - v_north(S, i, j - 1, k)) -
+                            DTZ * (rhow[k + 1] * v_top(S, i, j, k) - rhow[k] * v_top(S, i, j, k - 1)) *
+                                one_d_rhou[k] -
+                            S->dt * S->f[j] * ov_v;
+                S->P[F_V][IX(i, j, k)] = S->M[F_V][IX(i, j, k)] + step * vt;
+            }
+    /* buoyancy: advection.cpp:329-337 with buoyancy_dry / buoyancy_warm_micro (:42-52) */
+    const double *TH = S->cur[F_TH], *tbv = S->tbv;
+    const int moist = S->c.microphysics_option != 0;
+    for (int i = 3; i < NX - 3; i++)
+        for (int j = 3; j < NY - 3; j++)
+            for (int k = 2; k < NZ - 1; k++) {
+                double b0, b1;
+                if (!moist) {
+                    b0 = TH[IX(i, j, k)] / tbv[k];
+                    b1 = TH[IX(i, j, k - 1)] / tbv[k - 1];
+                } else {
+                    const double *QV = S->cur[F_QV], *QC = S->cur[F_QC], *QR = S->cur[F_QR];
+                    b0 = TH[IX(i, j, k)] / tbv[k] + 0.61 * QV[IX(i, j, k)] - QC[IX(i, j, k)] -
+                         QR[IX(i, j, k)];
+                    b1 = TH[IX(i, j, k - 1)] / tbv[k - 1] + 0.61 * QV[IX(i, j, k - 1)] -
+                         QC[IX(i, j, k - 1)] - QR[IX(i, j, k - 1)];
+                }
+                S->P[F_W][IX(i, j, k)] = S->M[F_W][IX(i, j, k)] + step * S->dt * grav * 0.5 * (b0 + b1);
+            }
+}
+
+/* ------------------------------------------------------------------------
+ * Scalar face fluxes with a basic state: interpolate_scalar(s,sb,...)
+ * (fluxes.cpp:797-867), compute_fluxes_scalar (:632-654); the signs are those
+ * of compute_sign_cells (:316-341) taken directly from the current winds.
+ * Returned: perturbation-flux + basic-state-flux (the sum is commutative, so
+ * the order of compute_fluxes_moisture :740-770 gives the same value).
+ * ---------------------------------------------------------------------- */
+static double s_east(const ora_state *S, const double *s, const double *sb, int i, int j, int k)
+{
+    const double *U = S->cur[F_U], *UB = S->bar[0];
+    double u1 = U[IX(i + 1, j, k)];
+    double ut = UB[IX(i + 1, j, k)] + u1;
+    double se = face5(SI(s, i, j, k), sgn(ut));
+    if (!sb) return ut * se;
+    double be = face5(SI(sb, i, j, k), sgn(u1));
+    return u1 * be + ut * se;
+}
+static double s_north(const ora_state *S, const double *s, const double *sb, int i, int j, int k)
+{
+    const double *V = S->cur[F_V], *VB = S->bar[1];
+    double v1 = V[IX(i, j + 1, k)];
+    double vt = VB[IX(i, j + 1, k)] + v1;
+    double sn = face5(SJ(s, i, j, k), sgn(vt));
+    if (!sb) return vt * sn;
+    double bn = face5(SJ(sb, i, j, k), sgn(v1));
+    return v1 * bn + vt * sn;
+}
+static double s_top(const ora_state *S, const double *s, const double *sb, int i, int j, int k)
+{
+    if (k == 0) return 0.0;
+    const double *W = S->cur[F_W], *WB = S->bar[2];
+    double w1 = W[IX(i, j, k + 1)];
+    double wt = WB[IX(i, j, k + 1)] + w1;
+    double st, bt = 0.0;
+    if (k == 1 || k == S->NZ - 2) {
+        st = 0.5 * (s[IX(i, j, k + 1)] + s[IX(i, j, k)]);
+        if (sb) bt = 0.5 * (sb[IX(i, j, k + 1)] + sb[IX(i, j, k)]);
+    } else {
+        st = face3(SK(s, i, j, k), sgn(wt));
+        if (sb) bt = face3(SK(sb, i, j, k), sgn(w1));
+    }
+    if (!sb) return wt * st;
+    return w1 * bt + wt * st;
+}
+/* rain: interpolate_scalar_with_fallspeed (fluxes.cpp:953-1032) and the qr
+ * fluxes of compute_fluxes_moisture (:719-784), incl. the bottom outflow */
+static double r_top(const ora_state *S, const double *s, int i, int j, int k)
+{
+    const double *W = S->cur[F_W], *WB = S->bar[2], *VT = S->vt;
+    if (k == 0) {
+        double s0 = 0.5 * (s[IX(i, j, 0)] + s[IX(i, j, 1)]);
+        return -0.5 * (VT[IX(i, j, 1)] + VT[IX(i, j, 0)]) * s0;
+    }
+    double wb = WB[IX(i, j, k + 1)] + W[IX(i, j, k + 1)];
+    double wf = wb - 0.5 * (VT[IX(i, j, k)] + VT[IX(i, j, k + 1)]);
+    double st;
+    if (k == 1 || k == S->NZ - 2)
+        st = 0.5 * (s[IX(i, j, k + 1)] + s[IX(i, j, k)]);
+    else
+        st = face3(SK(s, i, j, k), sgn(wf));
+    return wf * st;
+}
+
+/* tendency of a flux-form scalar: theta_tend_cell / qv_tend_cell (advection.cpp
+ * :152-168, :197-213) with Z_ADVECT_BASE (:16-18) when base != NULL */
+static double s_tend(const ora_state *S, const double *s, const double *sb, const double *base,
+                     int i, int j, int k)
+{
+    const double *rhow = S->rhow, *one_d_rhou = S->one_d_rhou;
+    double DTZ = S->dtz * S->mu[k];
+    double t = -S->dtx * (s_east(S, s, sb, i, j, k) - s_east(S, s, sb, i - 1, j, k)) -
+               S->dty * (s_north(S, s, sb, i, j, k) - s_north(S, s, sb, i, j - 1, k)) -
+               DTZ * (rhow[k + 1] * s_top(S, s, sb, i, j, k) - rhow[k] * s_top(S, s, sb, i, j, k - 1)) *
+                   one_d_rhou[k];
+    if (base) {
+        const double *W = S->cur[F_W];
+        double zab = 0.50 *
+                     (rhow[k + 1] * W[IX(i, j, k + 1)] * (base[k + 1] - base[k]) +
+                      rhow[k] * W[IX(i, j, k)] * (base[k] - base[k - 1])) *
+                     one_d_rhou[k];
+        t = t - DTZ * zab;
+    }
+    return t;
+}
+
+static void op_advect_theta(ora_state *S, double step) /* advection.cpp:349-373 */
+{
+    for (int i = 3; i < S->NX - 3; i++)
+        for (int j = 3; j < S->NY - 3; j++)
+            for (int k = 1; k < S->NZ - 1; k++)
+                S->P[F_TH][IX(i, j, k)] =
+                    S->M[F_TH][IX(i, j, k)] +
+                    step * s_tend(S, S->cur[F_TH], S->bar[3], S->tb, i, j, k);
+}
+
+/* calculate_rain_fall_speed_kessler (kessler.cpp:222-252) over [il,ih)x[jl,jh) */
+static void fall_speed(ora_state *S, const double *qr, int il, int ih, int jl, int jh)
+{
+    double *vt = S->vt;
+    for (int i = il; i < ih; i++)
+        for (int j = jl; j < jh; j++)
+            for (int k = 1; k < S->NZ - 1; k++) {
+                vt[IX(i, j, k)] = 0.0;
+                if (qr[IX(i, j, k)] > minvar) {
+                    double qrr = fmax(qr[IX(i, j, k)] * 0.001 * S->rhou[k], 0.0);
+                    double vtden = sqrt(S->rhou[1] / S->rhou[k]);
+                    vt[IX(i, j, k)] = 36.34 * (pow(qrr, 0.1364)) * vtden;
+                }
+            }
+    for (int i = il; i < ih; i++)
+        for (int j = jl; j < jh; j++) vt[IX(i, j, 0)] = vt[IX(i, j, 1)];
+}
+
+static void op_advect_micro(ora_state *S, double step) /* advection.cpp:451-498 */
+{
+    const int NX = S->NX, NY = S->NY, NZ = S->NZ;
+    if (S->c.rain_fallout == 1) fall_speed(S, S->cur[F_QR], 3, NX - 3, 3, NY - 3);
+    const double *rhow = S->rhow, *one_d_rhou = S->one_d_rhou;
+    const double *QC = S->cur[F_QC], *QR = S->cur[F_QR];
+    for (int i = 3; i < NX - 3; i++)
+        for (int j = 3; j < NY - 3; j++)
+            for (int k = 1; k < NZ - 1; k++) {
+                long ix = IX(i, j, k);
+                S->P[F_QV][ix] =
+                    S->M[F_QV][ix] + step * s_tend(S, S->cur[F_QV], S->bar[4], S->qb, i, j, k);
+                S->P[F_QC][ix] = S->M[F_QC][ix] + step * s_tend(S, QC, NULL, NULL, i, j, k);
+                double DTZ = S->dtz * S->mu[k];
+                double tr = -S->dtx * (s_east(S, QR, NULL, i, j, k) - s_east(S, QR, NULL, i - 1, j, k)) -
+                            S->dty * (s_north(S, QR, NULL, i, j, k) - s_north(S, QR, NULL, i, j - 1, k)) -
+                            DTZ * (rhow[k + 1] * r_top(S, QR, i, j, k) - rhow[k] * r_top(S, QR, i, j, k - 1)) *
+                                one_d_rhou[k];
+                S->P[F_QR][ix] = S->M[F_QR][ix] + step * tr;
+            }
+}
+
+static void op_zero_moisture(ora_state *S) /* microphysics.cpp:675-700 */
+{
+    double *qc = S->P[F_QC], *qr = S->P[F_QR], *qv = S->P[F_QV];
+    for (long n = 0; n < S->N; n++)
+        if (qc[n] < 0) qc[n] = 0;
+    for (long n = 0; n < S->N; n++)
+        if (qr[n] < 0) qr[n] = 0;
+    for (int i = 1; i < S->NX - 1; i++)
+        for (int j = 1; j < S->NY - 1; j++)
+            for (int k = 1; k < S->NZ - 1; k++) {
+                long ix = IX(i, j, k);
+                if (qv[ix] + S->bar[4][ix] + S->qb[k] < 0) qv[ix] = -(S->bar[4][ix] + S->qb[k]);
+            }
+}
+
+/* ------------------------------------------------------------------------
+ * Pressure: solve_pressure (pressure.cpp:142-224, serial non-hydrostatic
+ * branch :187-208), divergence3d (:1340-1381) / divergence3d_periodic
+ * (:1390-1424), poisson_fft3d (:805-893), init_fft3d (:724-797).
+ * ---------------------------------------------------------------------- */
+static void mirror(ora_state *S, double *s) /* mirror_boundaries, boundaries.cpp:363-379 */
+{
+    const int NX = S->NX, NY = S->NY, NZ = S->NZ;
+    for (int k = 1; k < NZ - 1; k++) {
+        for (int j = 0; j < NY; j++) {
+            s[IX(0, j, k)] = s[IX(1, j, k)];
+            s[IX(NX - 1, j, k)] = s[IX(NX - 2, j, k)];
+        }
+        for (int i = 0; i < NX; i++) {
+            s[IX(i, 0, k)] = s[IX(i, 1, k)];
+            s[IX(i, NY - 1, k)] = s[IX(i, NY - 2, k)];
+        }
+    }
+}
+static void periodic_ew(ora_state *S, double *v) /* boundaries.cpp:562-574 */
+{
+    const int NX = S->NX;
+    for (int k = 0; k < S->NZ; k++)
+        for (int j = 0; j < S->NY; j++) {
+            v[IX(0, j, k)] = v[IX(NX - 6, j, k)];
+            v[IX(1, j, k)] = v[IX(NX - 5, j, k)];
+            v[IX(2, j, k)] = v[IX(NX - 4, j, k)];
+            v[IX(NX - 3, j, k)] = v[IX(3, j, k)];
+            v[IX(NX - 2, j, k)] = v[IX(4, j, k)];
+            v[IX(NX - 1, j, k)] = v[IX(5, j, k)];
+        }
+}
+
+#define SP(p, q, k) (S->spec + 2 * (((long)(k) * S->ni + (p)) * S->nj + (q)))
+
+static void poisson(ora_state *S, double step)
+{
+    const int NX = S->NX, NY = S->NY, NZ = S->NZ;
+    const int ni = S->ni, nj = S->nj, nk = S->nk;
+    const double *UP = S->P[F_U], *VP = S->P[F_V], *WP = S->P[F_W];
+    const double *rhou = S->rhou, *rhow = S->rhow;
+    /* divergence tendency into the real part; imaginary part zero */
+    memset(S->spec, 0, sizeof(double) * 2 * (size_t)ni * nj * nk);
+    int il, ih, jl = 1, jh = NY - 1, off;
+    if (!S->c.periodic_ew_boundaries) { il = 1; ih = NX - 1; off = 0; }
+    else { il = 3; ih = NX - 3; off = 3; }
+    for (int i = il; i < ih; i++)
+        for (int j = jl; j < jh; j++)
+            for (int k = 1; k < NZ - 1; k++) {
+                double d = rhou[k] * (UP[IX(i + 1, j, k)] - UP[IX(i, j, k)]) * S->one_d_dx +
+                           rhou[k] * (VP[IX(i, j + 1, k)] - VP[IX(i, j, k)]) * S->one_d_dy +
+                           (rhow[k + 1] * WP[IX(i, j, k + 1)] - rhow[k] * WP[IX(i, j, k)]) *
+                               (S->one_d_dz * S->mu[k]);
+                d /= (step * S->dt);
+                SP(i - off, j, k)[0] = d;
+            }
+    for (int k = 1; k < NZ - 1; k++) {
+        if (!S->c.periodic_ew_boundaries)
+            for (int j = 0; j < NY; j++) {
+                SP(0, j, k)[0] = SP(1, j, k)[0];
+                SP(NX - 1, j, k)[0] = SP(NX - 2, j, k)[0];
+            }
+        for (int i = 0; i < ni; i++) {
+            SP(i, 0, k)[0] = SP(i, 1, k)[0];
+            SP(i, NY - 1, k)[0] = SP(i, NY - 2, k)[0];
+        }
+    }
+    /* the copies to levels 0 and NZ-1 (:1372-1380) feed transforms whose
+     * results are never read back, so those two levels are skipped */
+    const double size2d = (double)(ni * nj);
+    for (int k = 1; k < nk - 1; k++) {
+        ora_fft_2d(&S->fi, &S->fj, -1, SP(0, 0, k), S->specw);
+        memcpy(SP(0, 0, k), S->specw, sizeof(double) * 2 * (size_t)ni * nj);
+    }
+    for (int k = 1; k < nk - 1; k++)
+        for (int p = 0; p < ni; p++)
+            for (int q = 0; q < nj; q++) {
+                SP(p, q, k)[0] /= size2d;
+                SP(p, q, k)[1] /= size2d;
+            }
+    /* Thomas algorithm per (p,q) (pressure.cpp:834-871); the diagonal
+     * B(p,q,k) of init_fft3d's stretched branch (:778-792) */
+    double *F = (double *)malloc(sizeof(double) * nk);
+    const double dx2 = S->dx * S->dx;
+    for (int p = 0; p < ni; p++)
+        for (int q = 0; q < nj; q++) {
+            double h = S->hcoef[(long)p * nj + q];
+            double z = 1.0 / (rhou[1] * 2.0 * h / dx2 - S->vcoef[1]);
+            F[1] = S->ccoef[1] * z;
+            SP(p, q, 1)[0] = SP(p, q, 1)[0] * z;
+            SP(p, q, 1)[1] = SP(p, q, 1)[1] * z;
+            for (int k = 2; k < nk - 1; k++) {
+                double b = rhou[k] * 2.0 * h / dx2 - S->vcoef[k];
+                z = 1.0 / (b - S->acoef[k] * F[k - 1]);
+                F[k] = S->ccoef[k] * z;
+                SP(p, q, k)[0] = (SP(p, q, k)[0] - S->acoef[k] * SP(p, q, k - 1)[0]) * z;
+                SP(p, q, k)[1] = (SP(p, q, k)[1] - S->acoef[k] * SP(p, q, k - 1)[1]) * z;
+            }
+            if (p == 0 && q == 0) { /* mean mode gauge (:858-859), T3 */
+                SP(0, 0, NZ - 2)[0] = 0;
+                SP(0, 0, NZ - 2)[1] = 0;
+            }
+            for (int k = NZ - 3; k >= 1; k--) {
+                SP(p, q, k)[0] -= F[k] * SP(p, q, k + 1)[0];
+                SP(p, q, k)[1] -= F[k] * SP(p, q, k + 1)[1];
+            }
+        }
+    free(F);
+    for (int k = 1; k < nk - 1; k++) {
+        ora_fft_2d(&S->fi, &S->fj, +1, SP(0, 0, k), S->specw);
+        memcpy(SP(0, 0, k), S->specw, sizeof(double) * 2 * (size_t)ni * nj);
+    }
+    double *PI = S->pi;
+    for (int i = 0; i < ni; i++)
+        for (int j = 0; j < nj; j++) {
+            PI[IX(i + off, j, 0)] = SP(i, j, 1)[0];
+            for (int k = 1; k < nk - 1; k++) PI[IX(i + off, j, k)] = SP(i, j, k)[0];
+            PI[IX(i + off, j, NZ - 1)] = SP(i, j, NZ - 2)[0];
+        }
+}
+
+static void op_solve_pressure(ora_state *S, double step)
+{
+    if (!S->c.periodic_ew_boundaries) {
+        mirror(S, S->P[F_U]);
+        mirror(S, S->P[F_V]);
+        mirror(S, S->P[F_W]);
+        poisson(S, step);
+        mirror(S, S->pi);
+    } else {
+        periodic_ew(S, S->P[F_U]);
+        periodic_ew(S, S->P[F_V]);
+        periodic_ew(S, S->P[F_W]);
+        poisson(S, step);
+        periodic_ew(S, S->pi);
+    }
+}
+
+static void op_project(ora_state *S, double step) /* solver.cpp:120-135 */
+{
+    double *UP = S->P[F_U], *VP = S->P[F_V], *WP = S->P[F_W];
+    const double *PI = S->pi;
+    for (int i = 1; i < S->NX - 1; i++)
+        for (int j = 1; j < S->NY - 1; j++) {
+            UP[IX(i, j, 1)] -= step * (S->dtx * (PI[IX(i, j, 1)] - PI[IX(i - 1, j, 1)]));
+            VP[IX(i, j, 1)] -= step * (S->dty * (PI[IX(i, j, 1)] - PI[IX(i, j - 1, 1)]));
+            for (int k = 2; k < S->NZ - 1; k++) {
+                UP[IX(i, j, k)] -= step * (S->dtx * (PI[IX(i, j, k)] - PI[IX(i - 1, j, k)]));
+                VP[IX(i, j, k)] -= step * (S->dty * (PI[IX(i, j, k)] - PI[IX(i, j - 1, k)]));
+                WP[IX(i, j, k)] -= step * ((S->dtz * S->mw[k]) * (PI[IX(i, j, k)] - PI[IX(i, j, k - 1)]));
+            }
+        }
+}
+
+/* ------------------------------------------------------------------------
+ * Boundary conditions: boundaries.cpp:119-284, 304-326, 436-498.
+ * ---------------------------------------------------------------------- */
+static void sponge(ora_state *S, double *v, int ns_only)
+{
+    const int NX = S->NX, NY = S->NY, NZ = S->NZ;
+    if (!ns_only) {
+        for (int i = S->eb; i < S->ee; i++)
+            for (int j = 1; j < NY; j++)
+                for (int k = 1; k < NZ; k++) v[IX(i, j, k)] -= S->east_coeff[i - S->eb] * v[IX(i, j, k)];
+        for (int i = S->wb; i < S->we; i++)
+            for (int j = 1; j < NY; j++)
+                for (int k = 1; k < NZ; k++) v[IX(i, j, k)] -= S->west_coeff[i - S->wb] * v[IX(i, j, k)];
+    }
+    for (int i = 1; i < NX; i++)
+        for (int j = S->sb; j < S->se; j++)
+            for (int k = 1; k < NZ; k++) v[IX(i, j, k)] -= S->south_coeff[j - S->sb] * v[IX(i, j, k)];
+    for (int i = 1; i < NX; i++)
+        for (int j = S->nb; j < S->ne; j++)
+            for (int k = 1; k < NZ; k++) v[IX(i, j, k)] -= S->north_coeff[j - S->nb] * v[IX(i, j, k)];
+}
+static void upper_lower(ora_state *S, double *v)
+{
+    for (int i = 1; i < S->NX; i++)
+        for (int j = 1; j < S->NY; j++) {
+            v[IX(i, j, 0)] = v[IX(i, j, 1)];
+            v[IX(i, j, S->NZ - 1)] = v[IX(i, j, S->NZ - 2)];
+        }
+}
+static void upper_lower_zero(ora_state *S, double *v)
+{
+    for (int i = 1; i < S->NX; i++)
+        for (int j = 1; j < S->NY; j++) {
+            v[IX(i, j, 0)] = 0;
+            v[IX(i, j, 1)] = 0;
+            v[IX(i, j, S->NZ - 1)] = 0;
+        }
+}
+
+static void op_bc(ora_state *S)
+{
+    const int per = S->c.periodic_ew_boundaries;
+    if (!per) {
+        sponge(S, S->P[F_U], 0);
+        sponge(S, S->P[F_V], 0);
+        sponge(S, S->P[F_TH], 0);
+        upper_lower(S, S->P[F_U]);
+        upper_lower(S, S->P[F_V]);
+        upper_lower(S, S->P[F_TH]);
+        sponge(S, S->P[F_W], 0);
+        upper_lower_zero(S, S->P[F_W]);
+    } else {
+        sponge(S, S->P[F_U], 1);
+        sponge(S, S->P[F_V], 1);
+        sponge(S, S->P[F_TH], 1);
+        periodic_ew(S, S->P[F_U]);
+        periodic_ew(S, S->P[F_V]);
+        periodic_ew(S, S->pi);
+        periodic_ew(S, S->P[F_TH]);
+        upper_lower(S, S->P[F_U]);
+        upper_lower(S, S->P[F_V]);
+        upper_lower(S, S->P[F_TH]);
+        sponge(S, S->P[F_W], 1);
+        periodic_ew(S, S->P[F_W]);
+        upper_lower_zero(S, S->P[F_W]);
+    }
+}
+
+static void op_bc_micro(ora_state *S)
+{
+    const int per = S->c.periodic_ew_boundaries;
+    const int f3[3] = {F_QV, F_QC, F_QR};
+    for (int n = 0; n < 3; n++) sponge(S, S->P[f3[n]], per);
+    if (per)
+        for (int n = 0; n < 3; n++) periodic_ew(S, S->P[f3[n]]);
+    for (int n = 0; n < 3; n++) upper_lower(S, S->P[f3[n]]);
+}
+
+static void op_rayleigh(ora_state *S) /* damping.cpp:1148-1177 */
+{
+    for (int k = S->raylevel; k < S->NZ; k++) {
+        double cu = S->ray_u[k], cw = S->ray_w[k];
+        for (int i = 1; i < S->NX - 1; i++)
+            for (int j = 1; j < S->NY - 1; j++) {
+                long ix = IX(i, j, k);
+                S->P[F_U][ix] -= cu * S->P[F_U][ix];
+                S->P[F_V][ix] -= cu * S->P[F_V][ix];
+                S->P[F_W][ix] -= cw * S->P[F_W][ix];
+                S->P[F_TH][ix] -= cu * S->P[F_TH][ix];
+            }
+    }
+}
+
+/* ------------------------------------------------------------------------
+ * Kessler warm rain: run_kessler_microphysics (kessler.cpp:25-213).
+ * ---------------------------------------------------------------------- */
+static void kessler_points(ora_state *S)
+{
+    const double cpRd = cp / Rd;
+    double *THP = S->P[F_TH], *QVP = S->P[F_QV], *QCP = S->P[F_QC], *QRP = S->P[F_QR];
+    const double *THBAR = S->bar[3], *QBAR = S->bar[4], *PBAR = S->bar[5], *PI = S->pi;
+    const double dt = S->dt;
+    for (int i = 1; i < S->NX - 1; i++)
+        for (int j = 1; j < S->NY - 1; j++)
+            for (int k = 1; k < S->NZ - 1; k++) {
+                long ix = IX(i, j, k);
+                const double rhou = S->rhou[k];
+                double theta = THP[ix] + THBAR[ix] + S->tb[k];
+                double pressure = PI[ix] / (cp * S->tbv[k]) + PBAR[ix];
+                double vapor = QVP[ix] + QBAR[ix] + S->qb[k];
+                double temperature = theta * pressure;
+                double pd = p0 * pow(pressure, cpRd);
+                double A, B, E, esl, qvsat;
+                if (QCP[ix] > 1.0e-3) A = 0.001 * (QCP[ix] - 1.0e-3) * dt;
+                else A = 0;
+                if (QRP[ix] > minvar) B = rhou * 2.2 * QCP[ix] * pow(QRP[ix], 0.875) * dt;
+                else B = 0;
+                if (QRP[ix] > minvar) {
+                    esl = 611.2 * exp(17.67 * (temperature - 273.15) / (temperature - 29.65));
+                    qvsat = 0.62197 * esl / (pd - esl);
+                    double cvent = 1.6 + 30.3922 * pow(rhou * QRP[ix], 0.2046);
+                    E = (1.0 / rhou) *
+                        (((1.0 - vapor / qvsat) * cvent * pow(rhou * QRP[ix], 0.525)) /
+                         (2.03e4 + 9.58e6 / (pd * qvsat))) *
+                        dt;
+                    E = fmin(QRP[ix], E);
+                    E = fmax(E, 0.0);
+                    if (E > 100) S->err = GA_ERR_KESSLER;
+                } else
+                    E = 0;
+                QVP[ix] += E;
+                double total_convert = fmin(A + B, QCP[ix]);
+                QCP[ix] -= total_convert;
+                QRP[ix] += (total_convert - E);
+                double de = (Lv / (cp * pressure)) * E;
+                THP[ix] -= de;
+                /* saturation adjustment (:119-176) */
+                theta = THP[ix] + THBAR[ix] + S->tb[k];
+                vapor = QVP[ix] + QBAR[ix] + S->qb[k];
+                temperature = theta * pressure;
+                esl = 611.2 * exp(17.67 * (temperature - 273.15) / (temperature - 29.65));
+                qvsat = 0.62197 * esl / (pd - esl);
+                const double f = 17.67 * (273.15 - 29.65) * Lv / cp;
+                /* pow(x,2) is folded to x*x by the reference's compiler */
+                double tm = temperature - 29.65;
+                double phi = pd / (pd - esl) * qvsat * f / (tm * tm);
+                double C = 0.0;
+                if (vapor > qvsat) C = (vapor - qvsat) / (1.0 + phi);
+                else if (vapor < qvsat && QCP[ix] > 0) C = -fmin(QCP[ix], (qvsat - vapor) / (1.0 + phi));
+                QCP[ix] += C;
+                QVP[ix] -= C;
+                double dc = (Lv / (cp * pressure)) * C;
+                THP[ix] += dc;
+            }
+}
+
+/* PPM semi-Lagrangian fallout: hydrometeor_fallout (microphysics.cpp:210-292),
+ * piecewise_parabolic_interp (:516-579), calculate_edge_values (:590-637),
+ * integrate_parabolic (:339-350), below_surface_rainfall (:355-370). */
+static double integrate_parabolic(const double *zin, const double *qin, int p, double zl, double zh,
+                                  const double *qp, const double *qn)
+{
+    double t0 = (zl - zin[p]) / (zin[p + 1] - zin[p]);
+    double t1 = (zh - zin[p]) / (zin[p + 1] - zin[p]);
+    double high = (qp[p] + qn[p] - 2.0 * qin[p]) * t1 * t1 * t1 -
+                  (qp[p] + 2.0 * qn[p] - 3.0 * qin[p]) * t1 * t1 + qn[p] * t1;
+    double low = (qp[p] + qn[p] - 2.0 * qin[p]) * t0 * t0 * t0 -
+                 (qp[p] + 2.0 * qn[p] - 3.0 * qin[p]) * t0 * t0 + qn[p] * t0;
+    return high - low;
+}
+static void edge_values(ora_state *S, const double *zin, const double *qin, int n)
+{
+    double *qp = S->qp_edges, *qn = S->qn_edges, *mono = S->mono;
+    for (int k = 1; k < n - 1; k++) {
+        double dq = 0.25 * (qin[k + 1] - qin[k - 1]);
+        double dmax = fmax(qin[k + 1], fmax(qin[k], qin[k - 1])) - qin[k];
+        double dmin = qin[k] - fmin(qin[k + 1], fmin(qin[k], qin[k - 1]));
+        mono[k] = sgn(dq) * fmin(fabs(dq), fmin(dmax, dmin));
+    }
+    mono[0] = mono[1];
+    mono[n - 1] = mono[n - 2];
+    for (int k = 1; k < n - 1; k++) {
+        qn[k] = (qin[k - 1] * (zin[k + 1] - zin[k]) + qin[k] * (zin[k] - zin[k - 1])) /
+                    (zin[k + 1] - zin[k - 1]) -
+                (mono[k] - mono[k - 1]) / 3.0;
+        qp[k - 1] = qn[k];
+    }
+    /* qp[n-2] is not set above: it keeps the value of the previous call */
+    qp[n - 1] = qin[n - 1];
+    qp[0] = qin[0];
+    qn[n - 1] = qin[n - 1];
+    qn[0] = qin[0];
+    for (int k = 0; k < n; k++) {
+        qn[k] = qin[k] - sgn(mono[k]) * fmin(fabs(2.0 * mono[k]), fabs(qn[k] - qin[k]));
+        qp[k] = qin[k] + sgn(mono[k]) * fmin(fabs(2.0 * mono[k]), fabs(qp[k] - qin[k]));
+    }
+}
+static double ppm_remap(ora_state *S, const double *zin, const double *zout, const double *qin,
+                        double *qout, int n)
+{
+    memset(qout, 0, sizeof(double) * n);
+    int hn = 1;
+    /* the reference accumulates into an uninitialised local here; 0 is used */
+    double rainfall = 0.0;
+    for (int j = 1; j < n - 2; j++)
+        if (zin[j] < 0 && zin[j + 1] < 0) {
+            rainfall += qin[j] * (zin[j + 1] - zin[j]);
+            hn = j + 1;
+        }
+    edge_values(S, zin, qin, n);
+    const double *qp = S->qp_edges, *qn = S->qn_edges;
+    if (zin[hn] < 0)
+        rainfall += integrate_parabolic(zin, qin, hn, zin[hn], 0, qp, qn) * -zin[hn] *
+                    ((zin[hn + 1] - zin[hn]) / -zin[hn]);
+    for (int i = 0; i < n - 1; i++)
+        for (int j = 0; j < n - 1; j++) {
+            double scale = (zin[j + 1] - zin[j]) / (zout[i + 1] - zout[i]);
+            if (zout[i] < zin[j] && zout[i + 1] < zin[j + 1] && zout[i + 1] > zin[j])
+                qout[i] = qout[i] + integrate_parabolic(zin, qin, j, zin[j], zout[i + 1], qp, qn) * scale;
+            if (zout[i] < zin[j + 1] && zout[i + 1] > zin[j + 1] && zout[i] > zin[j])
+                qout[i] = qout[i] + integrate_parabolic(zin, qin, j, zout[i], zin[j + 1], qp, qn) * scale;
+            if (zout[i] >= zin[j] && zout[i + 1] <= zin[j + 1])
+                qout[i] = qout[i] + integrate_parabolic(zin, qin, j, zout[i], zout[i + 1], qp, qn) * scale;
+            if (zout[i] < zin[j] && zout[i + 1] > zin[j + 1])
+                qout[i] = qout[i] + integrate_parabolic(zin, qin, j, zin[j], zin[j + 1], qp, qn) * scale;
+        }
+    return rainfall;
+}
+static void fallout(ora_state *S)
+{
+    const int NZ = S->NZ;
+    double *var = S->P[F_QR];
+    const double *vel = S->vt, *ZW = S->zsw;
+    const double DeCFL0 = 0.05, dt = S->dt;
+    double *ZA = S->za, *QA = S->qa, *QD = S->qd, *Ve = S->ve;
+    for (int k = 0; k < NZ; k++) { ZA[k] = ZW[k]; Ve[k] = 0; QD[k] = 0; QA[k] = 0; }
+    for (int i = 1; i < S->NX - 1; i++)
+        for (int j = 1; j < S->NY - 1; j++) {
+            int has = 0;
+            for (int k = 1; k < NZ; k++)
+                if (var[IX(i, j, k)] > minvar) { has = 1; break; }
+            if (!has) continue;
+            for (int k = 1; k < NZ; k++) Ve[k] = 0.5 * (vel[IX(i, j, k)] + vel[IX(i, j, k - 1)]);
+            Ve[0] = Ve[1];
+            for (int k = NZ - 2; k >= 0; k--) {
+                double dzu = ZW[k + 1] - ZW[k];
+                double decfl = (Ve[k + 1] - Ve[k]) * dt / dzu;
+                if (decfl >= DeCFL0) Ve[k] = Ve[k + 1] - DeCFL0 * dzu / dt;
+            }
+            for (int k = 0; k < NZ - 1; k++) ZA[k] = ZW[k] - dt * Ve[k];
+            for (int k = 0; k < NZ - 1; k++)
+                QA[k] = S->rhou[k] * var[IX(i, j, k)] * (ZW[k + 1] - ZW[k]) / (ZA[k + 1] - ZA[k]);
+            S->accrain[IX2(i, j)] += ppm_remap(S, ZA, ZW, QA, QD, NZ);
+            for (int k = 0; k < NZ; k++) var[IX(i, j, k)] = QD[k] * S->one_d_rhou[k];
+        }
+}
+
+static void op_kessler(ora_state *S) /* run_microphysics(1,NX-1,1,NY-1) */
+{
+    if (S->c.microphysics_option != 1) return;
+    kessler_points(S);
+    if (S->c.rain_fallout == 2) {
+        fall_speed(S, S->P[F_QR], 1, S->NX - 1, 1, S->NY - 1);
+        fallout(S);
+        memset(S->vt, 0, sizeof(double) * S->N);
+    } else {
+        /* precip_rate (microphysics.cpp:143-160) */
+        for (int i = 1; i < S->NX - 1; i++)
+            for (int j = 1; j < S->NY - 1; j++)
+                S->accrain[IX2(i, j)] += S->rhow[1] * 0.5 *
+                                         (S->vt[IX(i, j, 0)] + S->vt[IX(i, j, 1)]) * 0.5 *
+                                         (S->P[F_QR][IX(i, j, 0)] + S->P[F_QR][IX(i, j, 1)]) * S->dt;
+    }
+}
+
+/* ------------------------------------------------------------------------
+ * Buffer rotation: solver.cpp:229-263, microphysics.cpp:642-669.
+ * ---------------------------------------------------------------------- */
+static void swap_f(ora_state *S, int f)
+{
+    double *t = S->cur[f];
+    S->cur[f] = S->P[f];
+    S->P[f] = t;
+}
+static void advance_inner(ora_state *S)
+{
+    for (int f = 0; f < 4; f++) swap_f(S, f);
+}
+static void micro_advance_inner(ora_state *S)
+{
+    for (int f = 4; f < 7; f++) swap_f(S, f);
+}
+static void advance_outer(ora_state *S)
+{
+    for (int f = 0; f < 4; f++) memcpy(S->M[f], S->P[f], sizeof(double) * S->N);
+    advance_inner(S);
+}
+static void micro_advance(ora_state *S)
+{
+    for (int f = 4; f < 7; f++) memcpy(S->M[f], S->P[f], sizeof(double) * S->N);
+    micro_advance_inner(S);
+}
+
+static void integrate_non_hydro(ora_state *S, double step) /* solver.cpp:87-138 */
+{
+    op_advect_uvw(S, step);
+    op_solve_pressure(S, step);
+    op_project(S, step);
+}
+
+static void rk3_step(ora_state *S) /* driver_serial.cpp:178-286 */
+{
+    static const double steps[3] = {1. / 3., 0.5, 1.0};
+    const int micro = S->c.microphysics_option != 0;
+    for (int s = 0; s < 3; s++) {
+        integrate_non_hydro(S, steps[s]);
+        op_advect_theta(S, steps[s]);
+        if (micro) {
+            op_advect_micro(S, steps[s]);
+            op_zero_moisture(S);
+        }
+        op_bc(S);
+        if (micro) {
+            op_bc_micro(S);
+            if (s < 2) micro_advance_inner(S);
+        }
+        if (s < 2) advance_inner(S);
+    }
+    if (micro) {
+        op_kessler(S);
+        op_bc_micro(S);
+        micro_advance(S);
+    }
+    op_bc(S);
+    op_rayleigh(S);
+    advance_outer(S);
+    S->mtime += S->dt; /* s_run_model :366-369 */
+    S->bigcounter++;
+}
+
+/* ------------------------------------------------------------------------
+ * Column builders: setup_vertical_height_levels (initializer.cpp:840-849),
+ * stretched_grid (:1340-1385), initialize_vertical_basic_state2 (:858-928),
+ * setup_coordinates (:1948-1967), initialize_coriolis_parameter (:826-833).
+ * ---------------------------------------------------------------------- */
+int ora_columns_build(int NZ, double dz, double z0, const double *tb_in, const double *qb_in,
+                      ga_column_store *o)
+{
+    if (NZ < 6 || NZ > 512) return GA_ERR_ARG;
+    memset(o, 0, sizeof(*o));
+    for (int k = 0; k < NZ; k++) {
+        o->zu[k] = ((double)k - 0.5) * dz;
+        o->zw[k] = ((double)k - 1) * dz;
+    }
+    const int lev = 1, nt = NZ - 1;
+    const double dzp = dz;
+    double c2 = (1 - z0 / (dzp * lev)) / ((nt - 1) * dzp - dzp * lev);
+    double c1 = z0 / (dzp * lev) - c2 * dzp * lev;
+    for (int i = 0; i <= nt; i++) {
+        double fullLev = ((double)i - 1.0) * dzp;
+        double halfLev = ((double)i - 0.5) * dzp;
+        o->zsw[i] = (c1 + c2 * fullLev) * fullLev;
+        o->mw[i] = 1 / (c1 + 2 * c2 * fullLev);
+        o->zsu[i] = (c1 + c2 * halfLev) * halfLev;
+        o->mu[i] = 1 / (c1 + 2 * c2 * halfLev);
+    }
+    double *tb = o->tb, *qb = o->qb, *tbw = o->tbw, *tbv = o->tbv, *pib = o->pib;
+    double *rhou = o->rhou, *rhow = o->rhow, *zsu = o->zsu;
+    for (int k = 0; k < NZ; k++) { tb[k] = tb_in[k]; qb[k] = qb_in[k]; }
+    tb[0] = tb[1];
+    tb[NZ - 1] = tb[NZ - 2];
+    qb[0] = qb[1];
+    qb[NZ - 1] = qb[NZ - 2];
+    tbw[0] = 0.5 * (tb[0] + tb[1]);
+    for (int k = 1; k < NZ; k++) tbw[k] = 0.5 * (tb[k] + tb[k - 1]);
+    for (int k = 0; k < NZ; k++) tbv[k] = tb[k] * (1.0 + 0.61 * qb[k]);
+    double pisfc = pow((pressfc / p0), (Rd / cp));
+    pib[1] = pisfc - grav * (zsu[1] - 0) / (cp * tbv[1]);
+    pib[0] = pisfc + grav * (0 - zsu[0]) / (cp * tbv[0]);
+    for (int k = 2; k < NZ; k++) pib[k] = pib[k - 1] - grav * (zsu[k] - zsu[k - 1]) / (cp * (0.5 * (tbv[k] + tbv[k - 1])));
+    for (int k = 0; k < NZ; k++) rhou[k] = p0 * pow(pib[k], (cv / Rd)) / (Rd * tbv[k]);
+    rhow[1] = pressfc / (Rd * tbw[1]);
+    for (int k = 1; k < NZ; k++) rhow[k] = 0.5 * (rhou[k] + rhou[k - 1]);
+    tbv[0] = tbv[1];
+    tbv[NZ - 1] = tbv[NZ - 2];
+    tbw[0] = tbw[1];
+    tbw[NZ - 1] = tbw[NZ - 2];
+    pib[0] = pib[1];
+    pib[NZ - 1] = pib[NZ - 2];
+    rhow[0] = rhow[1];
+    for (int k = 0; k < NZ; k++) {
+        o->one_d_rhow[k] = 1. / rhow[k];
+        o->one_d_rhou[k] = 1. / rhou[k];
+    }
+    return GA_OK;
+}
+
+int ora_coriolis_build(int NY, double dy, double corner_lat, double *f)
+{
+    double lat = -89.462997 + corner_lat + dy / meters_per_degree;
+    for (int j = 0; j < NY; j++) {
+        if (j > 0) lat = lat + dy / meters_per_degree;
+        f[j] = 2 * fc * sin(lat * trigpi / 180.);
+    }
+    return GA_OK;
+}
+
+/* ------------------------------------------------------------------------
+ * State management
+ * ---------------------------------------------------------------------- */
+static double cos_profile(double pl, double ph, double frac, double shift) /* util.cpp:740-749 */
+{
+    if (frac >= 0 && frac <= 1.0) return cos(pl * 2 * trigpi + (ph - pl) * 2 * trigpi * frac) + shift;
+    return 0;
+}
+
+static double *dup_col(const double *src, int n)
+{
+    double *d = (double *)calloc((size_t)n, sizeof(double));
+    if (src) memcpy(d, src, sizeof(double) * n);
+    return d;
+}
+
+ora_state *ora_create(const ga_config *cfg, const ga_columns *cols)
+{
+    if (!cfg || !cols) return NULL;
+    if (cfg->nx < 12 || cfg->ny < 12 || cfg->nz < 6 || cfg->nz > 512) return NULL;
+    ora_state *S = (ora_state *)calloc(1, sizeof(ora_state));
+    S->c = *cfg;
+    const int NX = cfg->nx, NY = cfg->ny, NZ = cfg->nz;
+    S->NX = NX; S->NY = NY; S->NZ = NZ;
+    S->N = (long)NX * NY * NZ;
+    S->dx = cfg->dx; S->dy = cfg->dy; S->dz = cfg->dz; S->dt = cfg->dt;
+    S->dtx = S->dt / S->dx; S->dty = S->dt / S->dy; S->dtz = S->dt / S->dz;
+    S->one_d_dx = 1.0 / S->dx; S->one_d_dy = 1.0 / S->dy; S->one_d_dz = 1.0 / S->dz;
+    S->zu = dup_col(cols->zu, NZ); S->zw = dup_col(cols->zw, NZ);
+    S->zsu = dup_col(cols->zsu, NZ); S->zsw = dup_col(cols->zsw, NZ);
+    S->mu = dup_col(cols->mu, NZ); S->mw = dup_col(cols->mw, NZ);
+    S->rhou = dup_col(cols->rhou, NZ); S->rhow = dup_col(cols->rhow, NZ);
+    S->one_d_rhou = dup_col(cols->one_d_rhou, NZ); S->one_d_rhow = dup_col(cols->one_d_rhow, NZ);
+    S->tb = dup_col(cols->tb, NZ); S->tbv = dup_col(cols->tbv, NZ); S->tbw = dup_col(cols->tbw, NZ);
+    S->qb = dup_col(cols->qb, NZ); S->pib = dup_col(cols->pib, NZ);
+    S->f = dup_col(cols->f, NY);
+    for (int f = 0; f < GA_NPROG; f++) {
+        for (int s = 0; s < 3; s++) S->buf[f][s] = (double *)calloc((size_t)S->N, sizeof(double));
+        S->cur[f] = S->buf[f][0];
+        S->P[f] = S->buf[f][1];
+        S->M[f] = S->buf[f][2];
+    }
+    S->pi = (double *)calloc((size_t)S->N, sizeof(double));
+    for (int b = 0; b < 6; b++) S->bar[b] = (double *)calloc((size_t)S->N, sizeof(double));
+    S->vt = (double *)calloc((size_t)S->N, sizeof(double));
+    S->accrain = (double *)calloc((size_t)NX * NY, sizeof(double));
+    /* pressure solver set-up: initialize_pressure_solver (pressure.cpp:99-134) */
+    S->ni = cfg->periodic_ew_boundaries ? NX - 6 : NX;
+    S->nj = NY;
+    S->nk = NZ;
+    const int ni = S->ni, nj = S->nj, nk = S->nk;
+    ora_fft_plan_init(&S->fi, ni);
+    ora_fft_plan_init(&S->fj, nj);
+    S->spec = (double *)calloc(2 * (size_t)ni * nj * nk, sizeof(double));
+    S->specw = (double *)calloc(2 * (size_t)ni * nj, sizeof(double));
+    S->hcoef = (double *)calloc((size_t)ni * nj, sizeof(double));
+    double *kw = (double *)calloc(ni, sizeof(double)), *lw = (double *)calloc(nj, sizeof(double));
+    for (int i = 0; i < ni; i++) kw[i] = (double)i * 2 * trigpi / ((double)ni);
+    for (int j = 0; j < nj; j++) lw[j] = (double)j * 2 * trigpi / ((double)nj);
+    for (int i = 0; i < ni; i++)
+        for (int j = 0; j < nj; j++) S->hcoef[(long)i * nj + j] = cos(kw[i]) + cos(lw[j]) - 2.0;
+    free(kw);
+    free(lw);
+    S->acoef = (double *)calloc(nk, sizeof(double));
+    S->ccoef = (double *)calloc(nk, sizeof(double));
+    S->vcoef = (double *)calloc(nk, sizeof(double));
+    const double dz2 = S->dz * S->dz;
+    for (int k = 1; k < nk - 1; k++) {
+        S->acoef[k] = S->mu[k] * S->mw[k] * S->rhow[k] / dz2;
+        S->ccoef[k] = S->mu[k] * S->mw[k + 1] * S->rhow[k + 1] / dz2;
+    }
+    S->acoef[1] = 0;
+    S->ccoef[nk - 2] = 0;
+    S->vcoef[1] = S->mu[1] * S->mw[2] * S->rhow[2] / dz2;
+    for (int k = 2; k < nk - 2; k++)
+        S->vcoef[k] = S->mu[k] * (S->mw[k + 1] * S->rhow[k + 1] + S->mw[k] * S->rhow[k]) / dz2;
+    S->vcoef[nk - 2] = (S->mu[nk - 2] * S->mw[nk - 2] * S->rhow[nk - 2]) / dz2;
+    /* init_boundaries(iebuffer,iwbuffer,jnbuffer,jsbuffer,-1) (boundaries.cpp:44-114) */
+    int ie = cfg->boundary_width_east, iw = cfg->boundary_width_west;
+    int jn = cfg->boundary_width_north, js = cfg->boundary_width_south;
+    S->east_coeff = (double *)calloc(ie + 1, sizeof(double));
+    S->west_coeff = (double *)calloc(iw + 1, sizeof(double));
+    S->north_coeff = (double *)calloc(jn + 1, sizeof(double));
+    S->south_coeff = (double *)calloc(js + 1, sizeof(double));
+    S->eb = NX - ie; S->ee = NX; S->wb = 0; S->we = iw;
+    S->nb = NY - jn; S->ne = NY; S->sb = 0; S->se = js;
+    for (int i = 0; i < ie; i++) S->east_coeff[i] = 0.5 * cos_profile(-0.5, 0, (double)(i + 1) / (double)ie, 1);
+    for (int i = 0; i < iw; i++) S->west_coeff[i] = 0.5 * cos_profile(0, 0.5, (double)i / (double)iw, 1);
+    for (int i = 0; i < jn; i++) S->north_coeff[i] = 0.5 * cos_profile(-0.5, 0, (double)(i + 1) / (double)jn, 1);
+    for (int i = 0; i < js; i++) S->south_coeff[i] = 0.5 * cos_profile(0, 0.5, (double)i / (double)js, 1);
+    /* Rayleigh coefficients (damping.cpp:1150-1162) */
+    S->raylevel = cfg->rayleigh_damping_z;
+    S->ray_u = (double *)calloc(NZ, sizeof(double));
+    S->ray_w = (double *)calloc(NZ, sizeof(double));
+    if (S->raylevel >= 0 && S->raylevel < NZ) {
+        double raydmpcoef = 0.05, raydmpz = S->zu[S->raylevel];
+        for (int k = S->raylevel; k < NZ; k++) {
+            S->ray_u[k] = raydmpcoef * 0.5 * (1.0 - cos(trigpi * (S->zu[k] - raydmpz) / (S->zu[NZ - 1] - raydmpz)));
+            S->ray_w[k] = raydmpcoef * 0.5 * (1.0 - cos(trigpi * (S->zw[k] - raydmpz) / (S->zw[NZ - 1] - raydmpz)));
+        }
+    }
+    S->qp_edges = (double *)calloc(NZ, sizeof(double));
+    S->qn_edges = (double *)calloc(NZ, sizeof(double));
+    S->mono = (double *)calloc(NZ, sizeof(double));
+    S->za = (double *)calloc(NZ, sizeof(double));
+    S->qa = (double *)calloc(NZ, sizeof(double));
+    S->qd = (double *)calloc(NZ, sizeof(double));
+    S->ve = (double *)calloc(NZ, sizeof(double));
+    return S;
+}
+
+void ora_destroy(ora_state *S)
+{
+    if (!S) return;
+    double *cols[] = {S->zu, S->zw, S->zsu, S->zsw, S->mu, S->mw, S->rhou, S->rhow, S->one_d_rhou,
+                      S->one_d_rhow, S->tb, S->tbv, S->tbw, S->qb, S->pib, S->f};
+    for (unsigned n = 0; n < sizeof(cols) / sizeof(cols[0]); n++) free(cols[n]);
+    for (int f = 0; f < GA_NPROG; f++)
+        for (int s = 0; s < 3; s++) free(S->buf[f][s]);
+    free(S->pi);
+    for (int b = 0; b < 6; b++) free(S->bar[b]);
+    free(S->vt); free(S->accrain);
+    ora_fft_plan_free(&S->fi); ora_fft_plan_free(&S->fj);
+    free(S->spec); free(S->specw); free(S->hcoef);
+    free(S->acoef); free(S->ccoef); free(S->vcoef);
+    free(S->east_coeff); free(S->west_coeff); free(S->north_coeff); free(S->south_coeff);
+    free(S->ray_u); free(S->ray_w);
+    free(S->qp_edges); free(S->qn_edges); free(S->mono);
+    free(S->za); free(S->qa); free(S->qd); free(S->ve);
+    free(S);
+}
+
+static double *field_ptr(ora_state *S, int field, int slot, long *n)
+{
+    *n = S->N;
+    if (field >= 0 && field < GA_NPROG) {
+        if (slot == GA_SLOT_CUR) return S->cur[field];
+        if (slot == GA_SLOT_P) return S->P[field];
+        if (slot == GA_SLOT_M) return S->M[field];
+        return NULL;
+    }
+    switch (field) {
+    case GA_PI: return S->pi;
+    case GA_UBAR: case GA_VBAR: case GA_WBAR: case GA_THBAR: case GA_QBAR: case GA_PBAR:
+        return S->bar[field - GA_UBAR];
+    case GA_VT: return S->vt;
+    case GA_ACCRAIN: *n = (long)S->NX * S->NY; return S->accrain;
+    }
+    return NULL;
+}
+
+int ora_set_field(ora_state *S, int field, int slot, const double *src, long n)
+{
+    long nn;
+    double *d = field_ptr(S, field, slot, &nn);
+    if (!d || n != nn) return GA_ERR_ARG;
+    memcpy(d, src, sizeof(double) * n);
+    return GA_OK;
+}
+
+int ora_get_field(ora_state *S, int field, int slot, double *dst, long n)
+{
+    long nn;
+    double *d = field_ptr(S, field, slot, &nn);
+    if (!d || n != nn) return GA_ERR_ARG;
+    memcpy(dst, d, sizeof(double) * n);
+    return GA_OK;
+}
+
+int ora_op(ora_state *S, int op, double step)
+{
+    switch (op) {
+    case GA_OP_SIGN_CELLS: return GA_OK;
+    case GA_OP_ADVECT_UVW: op_advect_uvw(S, step); return GA_OK;
+    case GA_OP_SOLVE_PRESSURE: op_solve_pressure(S, step); return GA_OK;
+    case GA_OP_PROJECT: op_project(S, step); return GA_OK;
+    case GA_OP_INTEGRATE_NON_HYDRO: integrate_non_hydro(S, step); return GA_OK;
+    case GA_OP_ADVECT_THETA: op_advect_theta(S, step); return GA_OK;
+    case GA_OP_ADVECT_MICRO: op_advect_micro(S, step); return GA_OK;
+    case GA_OP_ZERO_MOISTURE: op_zero_moisture(S); return GA_OK;
+    case GA_OP_BC: op_bc(S); return GA_OK;
+    case GA_OP_BC_MICRO: op_bc_micro(S); return GA_OK;
+    case GA_OP_KESSLER: op_kessler(S); return S->err;
+    case GA_OP_RAYLEIGH: op_rayleigh(S); return GA_OK;
+    case GA_OP_ADVANCE_INNER: advance_inner(S); if (S->c.microphysics_option) micro_advance_inner(S); return GA_OK;
+    case GA_OP_ADVANCE_OUTER: advance_outer(S); if (S->c.microphysics_option) micro_advance(S); return GA_OK;
+    }
+    return GA_ERR_ARG;
+}
+
+int ora_step(ora_state *S, int nsteps)
+{
+    for (int n = 0; n < nsteps; n++) {
+        rk3_step(S);
+        if (S->err) return S->err;
+    }
+    return GA_OK;
+}
+
+long long ora_bigcounter(ora_state *S) { return S->bigcounter; }
+int ora_error(ora_state *S) { return S->err; }

@@ -1,0 +1,118 @@
+"""Generate the golden fixtures in this folder from the reference itself.
+
+Runs the reference's own serial step (oracle/_ref/ref_harness, built from the
+reference sources by oracle/build_ref.sh) on small seeded states and stores
+inputs and outputs as compressed .npz files:
+
+  run_<case>.npz   full steps (s_integrate_rk3, driver_serial.cpp:178-286)
+  ops_<case>.npz   single operators applied to one state whose three rotation
+                   buffers all hold different data
+
+Usage (where the reference sources exist):  python tests/golden/make_golden.py
+The fixtures are then read by tests/test_golden_oracle.py (CPU) and
+tests/test_gpu_parity.py (GPU) without needing the reference.
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+from model_gb300 import abi, configs  # noqa: E402
+from oracle import oracle as O  # noqa: E402
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+RUN_CASES = {
+    "dry": (lambda: configs.dry_bubble(nx=16, ny=14, nz=10, dx=500.0, dz=400.0, amp=3.0,
+                                       radius=2000.0, zc=1500.0, noise=0.2), 4),
+    "moist": (lambda: configs.moist_blob(nx=14, ny=13, nz=10), 4),
+    "moist_rf2": (lambda: configs.moist_blob(nx=14, ny=13, nz=10, rain_fallout=2), 4),
+    "moist_periodic": (lambda: configs.moist_blob(nx=18, ny=13, nz=10, periodic=1), 3),
+}
+
+OP_NAMES = ["advect_uvw", "solve_pressure", "integrate_non_hydro", "advect_theta",
+            "advect_micro", "zero_moisture", "bc", "bc_micro", "kessler", "rayleigh"]
+
+
+def _inputs(wl) -> dict:
+    d = {k: np.asarray(v, dtype=np.float64) for k, v in wl.settings().items()}
+    for k, v in wl.fields.items():
+        d["in_" + k] = np.asarray(v, dtype=np.float64).ravel()
+    d["nsteps"] = np.float64(wl.nsteps)
+    return d
+
+
+def make_runs():
+    for name, (mk, nsteps) in RUN_CASES.items():
+        wl = mk()
+        wl.nsteps = nsteps
+        out = O.run_reference(wl, "run", nsteps)
+        d = _inputs(wl)
+        for k, v in out.items():
+            d["out_" + k] = v
+        path = os.path.join(HERE, f"run_{name}.npz")
+        np.savez_compressed(path, **d)
+        print("wrote", path, os.path.getsize(path))
+
+
+def _ops_state(wl, seed: int) -> dict:
+    """Extra slot data so that current, P and M buffers all differ."""
+    n3 = (wl.nx, wl.ny, wl.nz)
+    extra = {}
+    s = seed
+    for f, name in enumerate(abi.PROG_NAMES):
+        base = wl.fields[name]
+        scale = {"u": 1.0, "v": 1.0, "w": 0.3, "th": 0.5, "qv": 2e-4, "qc": 4e-4, "qr": 4e-4}[name]
+        for suf in ("_p", "_m"):
+            r = 2.0 * configs.splitmix_uniform(s, wl.points).reshape(n3) - 1.0
+            s += 1
+            v = base + scale * r
+            if name in ("qc", "qr"):
+                v = np.abs(v) if suf == "_m" else v  # P may hold negatives for zero_moisture
+            extra[name + suf] = v
+    r = 2.0 * configs.splitmix_uniform(s, wl.points).reshape(n3) - 1.0
+    extra["pi"] = 20.0 * r
+    extra["vt"] = np.zeros(n3)
+    return extra
+
+
+def make_ops():
+    cases = {
+        "moist": configs.moist_blob(nx=14, ny=13, nz=10),
+        "moist_periodic_rf2": configs.moist_blob(nx=18, ny=13, nz=10, periodic=1, rain_fallout=2),
+    }
+    for cname, wl in cases.items():
+        extra = _ops_state(wl, 5000)
+        d = _inputs(wl)
+        for k, v in extra.items():
+            d["in_" + k] = v.ravel()
+        steps = {"advect_uvw": 1.0 / 3.0, "solve_pressure": 0.5, "integrate_non_hydro": 1.0,
+                 "advect_theta": 0.5, "advect_micro": 1.0 / 3.0}
+        for op in OP_NAMES:
+            st = steps.get(op, 1.0)
+            out = O.run_reference(wl, "op", op=op, step=st, extra=extra)
+            d[f"step_{op}"] = np.float64(st)
+            for k, v in out.items():
+                if k in abi.COLUMN_NAMES or k in ("f", "bigcounter", "mtime"):
+                    continue
+                ref_in = extra.get(k, wl.fields.get(k))
+                if ref_in is not None and np.array_equal(np.asarray(ref_in).ravel(), v):
+                    continue  # unchanged by this operator
+                d[f"{op}__{k}"] = v
+        path = os.path.join(HERE, f"ops_{cname}.npz")
+        np.savez_compressed(path, **d)
+        print("wrote", path, os.path.getsize(path))
+
+
+if __name__ == "__main__":
+    if not O.reference_available():
+        subprocess_rc = os.system(os.path.join(ROOT, "oracle", "build_ref.sh"))
+        if subprocess_rc != 0:
+            sys.exit("reference build failed")
+    make_runs()
+    make_ops()

@@ -1,0 +1,58 @@
+"""The CPU oracle against golden vectors produced by the reference itself.
+
+The fixtures in tests/golden/ hold the output of the reference's own serial
+step (built from its sources with oracle/build_ref.sh and
+tests/golden/make_golden.py).  The oracle restatement must reproduce them bit
+for bit: both use the same DFT, and neither contracts multiply-adds.
+"""
+import numpy as np
+import pytest
+
+from model_gb300 import abi
+from oracle import oracle as O
+from tests import fixtures as fx
+
+
+@pytest.mark.parametrize("name", fx.run_names())
+def test_columns_match_reference(name):
+    d = fx.load(name)
+    wl = fx.workload(d)
+    cols = O.build_columns(wl)
+    for n in abi.COLUMN_NAMES + ["f"]:
+        np.testing.assert_array_equal(cols[n], d["out_" + n], err_msg=n)
+
+
+@pytest.mark.parametrize("name", fx.run_names())
+def test_full_steps_bit_exact(name):
+    d = fx.load(name)
+    wl = fx.workload(d)
+    o = O.Oracle(wl, fx.columns(d))
+    assert o.step(wl.nsteps) == 0
+    st = o.state()
+    checked = 0
+    for k, v in st.items():
+        if "out_" + k not in d:
+            continue
+        np.testing.assert_array_equal(v, d["out_" + k], err_msg=f"{name}:{k}")
+        checked += 1
+    assert checked >= 13
+
+
+@pytest.mark.parametrize("name", fx.ops_names())
+@pytest.mark.parametrize("op", ["advect_uvw", "solve_pressure", "integrate_non_hydro",
+                                "advect_theta", "advect_micro", "zero_moisture", "bc",
+                                "bc_micro", "kessler", "rayleigh"])
+def test_single_operator_bit_exact(name, op):
+    d = fx.load(name)
+    wl = fx.workload(d)
+    o = O.Oracle(wl)
+    for k, v in fx.slot_extra(d).items():
+        f, slot = fx.FIELD_OF[k]
+        o.set(f, slot, v)
+    assert o.op(op, float(d[f"step_{op}"])) == 0
+    outs = [k for k in d if k.startswith(op + "__")]
+    assert outs, "fixture has no output for this operator"
+    for k in outs:
+        key = k.split("__", 1)[1]
+        f, slot = fx.FIELD_OF[key]
+        np.testing.assert_array_equal(o.get(f, slot), d[k], err_msg=f"{op}:{key}")
