@@ -29,6 +29,12 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#if defined(__GNUC__)
+#define GA_API __attribute__((visibility("default")))
+#else
+#define GA_API
+#endif
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -143,8 +149,8 @@ typedef struct ga_column_store {
 typedef struct ga_ctx ga_ctx;
 
 /* ---- library ----------------------------------------------------------- */
-int         ga_abi_version(void);
-const char *ga_last_error(void);
+GA_API int ga_abi_version(void);
+GA_API const char *ga_last_error(void);
 
 /*
  * Build the vertical column arrays from the base-state theta tb[NZ] and
@@ -154,7 +160,7 @@ const char *ga_last_error(void);
  * of tb/qb (tb[0]=tb[1] etc.).  height_lowest_level is the reference input of
  * the same name.  Host-only; needs no GPU.
  */
-int ga_columns_build(int nz, double dz, double height_lowest_level,
+GA_API int ga_columns_build(int nz, double dz, double height_lowest_level,
                      const double *tb_in, const double *qb_in,
                      ga_column_store *out);
 
@@ -164,51 +170,51 @@ int ga_columns_build(int nz, double dz, double height_lowest_level,
  * (initializer.cpp:1948-1967) then initialize_coriolis_parameter (:826-833).
  * Host-only.
  */
-int ga_coriolis_build(int ny, double dy, double corner_lat, double *f_out);
+GA_API int ga_coriolis_build(int ny, double dy, double corner_lat, double *f_out);
 
 /* ---- context ------------------------------------------------------------ */
 /* Replaces initialize_serial's solver set-up: initialize_pressure_solver
  * (pressure.cpp:99), init_boundaries (boundaries.cpp:44), init_microphysics
  * (microphysics.cpp:41).  Allocates every device buffer (zeroed, as the
  * reference's calloc) and precomputes the spectral and sponge tables. */
-int ga_create(const ga_config *cfg, const ga_columns *cols, ga_ctx **out);
-int ga_destroy(ga_ctx *ctx);
+GA_API int ga_create(const ga_config *cfg, const ga_columns *cols, ga_ctx **out);
+GA_API int ga_destroy(ga_ctx *ctx);
 
 /* Copy one field between host and device.  For prognostic fields `slot` picks
  * the rotation buffer; for the others it is ignored.  n must equal NX*NY*NZ
  * (NX*NY for GA_ACCRAIN).  Values are converted to/from FP32 for FP32
  * contexts. */
-int ga_set_field(ga_ctx *ctx, int field, int slot, const double *host, size_t n);
-int ga_get_field(ga_ctx *ctx, int field, int slot, double *host, size_t n);
+GA_API int ga_set_field(ga_ctx *ctx, int field, int slot, const double *host, size_t n);
+GA_API int ga_get_field(ga_ctx *ctx, int field, int slot, double *host, size_t n);
 
 /* Advance nsteps full RK3 steps: nsteps calls of s_integrate_rk3
  * (driver_serial.cpp:178-286), each followed by the counter updates of
  * s_run_model (bigcounter++, mtime += dt; driver_serial.cpp:366-369). */
-int ga_step(ga_ctx *ctx, int nsteps);
+GA_API int ga_step(ga_ctx *ctx, int nsteps);
 /* Same, queued on the context's stream without a final synchronize. */
-int ga_step_async(ga_ctx *ctx, int nsteps);
-int ga_synchronize(ga_ctx *ctx);
+GA_API int ga_step_async(ga_ctx *ctx, int nsteps);
+GA_API int ga_synchronize(ga_ctx *ctx);
 
 /* Run a single operator (GA_OP_*) with RK fraction `step`, for per-operator
  * parity tests.  Mirrors calling the reference global function directly. */
-int ga_op(ga_ctx *ctx, int op, double step);
+GA_API int ga_op(ga_ctx *ctx, int op, double step);
 
 /* Number of completed steps (reference: bigcounter) and model time (mtime). */
-int ga_get_counters(ga_ctx *ctx, long long *bigcounter, double *mtime);
+GA_API int ga_get_counters(ga_ctx *ctx, long long *bigcounter, double *mtime);
 
 /* Scan the prognostic forecast buffers for NaN/Inf on the device.
  * Returns GA_OK or GA_ERR_NONFINITE.  The reference has no such check. */
-int ga_check_finite(ga_ctx *ctx);
+GA_API int ga_check_finite(ga_ctx *ctx);
 
 /* Number of kernel launches issued by this context since creation. */
-long long ga_launch_count(ga_ctx *ctx);
+GA_API long long ga_launch_count(ga_ctx *ctx);
 
 /* CUDA stream the context runs on (a cudaStream_t, as void*). */
-void *ga_stream(ga_ctx *ctx);
+GA_API void *ga_stream(ga_ctx *ctx);
 
 /* Device pointer of a field buffer (FP64 or FP32 per the precision), for
  * callers that keep state resident on the GPU. */
-void *ga_field_device_ptr(ga_ctx *ctx, int field, int slot);
+GA_API void *ga_field_device_ptr(ga_ctx *ctx, int field, int slot);
 
 #ifdef __cplusplus
 }

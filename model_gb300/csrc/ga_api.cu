@@ -1,0 +1,226 @@
+// ga_api.cu - the extern "C" boundary declared in include/ga_anelastic.h.
+// Argument checks, error text, context bookkeeping and the host-only column
+// builders live here; everything else is forwarded to the per-precision
+// engine.
+#include <cmath>
+#include <cstring>
+#include <exception>
+#include <string>
+
+#include "ga_engine.h"
+
+namespace ga {
+static thread_local std::string g_last_error;
+void set_error(const std::string &msg) { g_last_error = msg; }
+}  // namespace ga
+
+struct ga_ctx {
+    ga::EngineBase *e;
+    ga_config cfg;
+};
+
+using ga::set_error;
+
+static int fail(int rc, const std::string &msg)
+{
+    set_error(msg);
+    return rc;
+}
+
+extern "C" {
+
+int ga_abi_version(void) { return GA_ABI_VERSION; }
+
+const char *ga_last_error(void) { return ga::g_last_error.c_str(); }
+
+/* setup_vertical_height_levels (initializer.cpp:840-849), stretched_grid
+ * (:1340-1385), initialize_vertical_basic_state2 (:858-928) */
+int ga_columns_build(int NZ, double dz, double z0, const double *tb_in, const double *qb_in,
+                     ga_column_store *o)
+{
+    if (!tb_in || !qb_in || !o) return fail(GA_ERR_ARG, "ga_columns_build: null pointer");
+    if (NZ < 6 || NZ > 512) return fail(GA_ERR_ARG, "ga_columns_build: NZ must be in [6,512]");
+    if (!(dz > 0)) return fail(GA_ERR_ARG, "ga_columns_build: dz must be positive");
+    const double Rd = 287.0, cp = 1004, cv = 717, p0 = 100000, grav = 9.8, pressfc = 100200;
+    std::memset(o, 0, sizeof(*o));
+    for (int k = 0; k < NZ; k++) {
+        o->zu[k] = ((double)k - 0.5) * dz;
+        o->zw[k] = ((double)k - 1) * dz;
+    }
+    const int lev = 1, nt = NZ - 1;
+    const double dzp = dz;
+    const double c2 = (1 - z0 / (dzp * lev)) / ((nt - 1) * dzp - dzp * lev);
+    const double c1 = z0 / (dzp * lev) - c2 * dzp * lev;
+    for (int i = 0; i <= nt; i++) {
+        const double fullLev = ((double)i - 1.0) * dzp, halfLev = ((double)i - 0.5) * dzp;
+        o->zsw[i] = (c1 + c2 * fullLev) * fullLev;
+        o->mw[i] = 1 / (c1 + 2 * c2 * fullLev);
+        o->zsu[i] = (c1 + c2 * halfLev) * halfLev;
+        o->mu[i] = 1 / (c1 + 2 * c2 * halfLev);
+    }
+    double *tb = o->tb, *qb = o->qb, *tbw = o->tbw, *tbv = o->tbv, *pib = o->pib;
+    double *rhou = o->rhou, *rhow = o->rhow, *zsu = o->zsu;
+    for (int k = 0; k < NZ; k++) { tb[k] = tb_in[k]; qb[k] = qb_in[k]; }
+    tb[0] = tb[1]; tb[NZ - 1] = tb[NZ - 2];
+    qb[0] = qb[1]; qb[NZ - 1] = qb[NZ - 2];
+    tbw[0] = 0.5 * (tb[0] + tb[1]);
+    for (int k = 1; k < NZ; k++) tbw[k] = 0.5 * (tb[k] + tb[k - 1]);
+    for (int k = 0; k < NZ; k++) tbv[k] = tb[k] * (1.0 + 0.61 * qb[k]);
+    const double pisfc = pow((pressfc / p0), (Rd / cp));
+    pib[1] = pisfc - grav * (zsu[1] - 0) / (cp * tbv[1]);
+    pib[0] = pisfc + grav * (0 - zsu[0]) / (cp * tbv[0]);
+    for (int k = 2; k < NZ; k++)
+        pib[k] = pib[k - 1] - grav * (zsu[k] - zsu[k - 1]) / (cp * (0.5 * (tbv[k] + tbv[k - 1])));
+    for (int k = 0; k < NZ; k++) rhou[k] = p0 * pow(pib[k], (cv / Rd)) / (Rd * tbv[k]);
+    for (int k = 1; k < NZ; k++) rhow[k] = 0.5 * (rhou[k] + rhou[k - 1]);
+    tbv[0] = tbv[1]; tbv[NZ - 1] = tbv[NZ - 2];
+    tbw[0] = tbw[1]; tbw[NZ - 1] = tbw[NZ - 2];
+    pib[0] = pib[1]; pib[NZ - 1] = pib[NZ - 2];
+    rhow[0] = rhow[1];
+    for (int k = 0; k < NZ; k++) {
+        o->one_d_rhow[k] = 1. / rhow[k];
+        o->one_d_rhou[k] = 1. / rhou[k];
+    }
+    return GA_OK;
+}
+
+/* setup_coordinates(0,-89.462997) (initializer.cpp:1948-1967) and
+ * initialize_coriolis_parameter (:826-833) */
+int ga_coriolis_build(int NY, double dy, double corner_lat, double *f)
+{
+    if (!f || NY < 1) return fail(GA_ERR_ARG, "ga_coriolis_build: bad arguments");
+    const double fc = 7.292e-5, mpd = 111000, trigpi = 3.14159265358979324;
+    double lat = -89.462997 + corner_lat + dy / mpd;
+    for (int j = 0; j < NY; j++) {
+        if (j > 0) lat = lat + dy / mpd;
+        f[j] = 2 * fc * sin(lat * trigpi / 180.);
+    }
+    return GA_OK;
+}
+
+int ga_create(const ga_config *cfg, const ga_columns *cols, ga_ctx **out)
+{
+    if (!cfg || !cols || !out) return fail(GA_ERR_ARG, "ga_create: null pointer");
+    *out = nullptr;
+    const ga_columns &c = *cols;
+    const double *req[] = {c.zu, c.zw, c.zsu, c.zsw, c.mu, c.mw, c.rhou, c.rhow, c.one_d_rhou,
+                           c.one_d_rhow, c.tb, c.tbv, c.tbw, c.qb, c.pib, c.f};
+    for (const double *p : req)
+        if (!p) return fail(GA_ERR_ARG, "ga_create: a column array is null");
+    if (cfg->nx < 12 || cfg->ny < 12) return fail(GA_ERR_CONFIG, "ga_create: NX and NY must be >= 12");
+    if (cfg->nz < 6 || cfg->nz > 128) return fail(GA_ERR_CONFIG, "ga_create: NZ must be in [6,128]");
+    if (!(cfg->dx > 0 && cfg->dy > 0 && cfg->dz > 0 && cfg->dt > 0))
+        return fail(GA_ERR_CONFIG, "ga_create: dx, dy, dz, dt must be positive");
+    if (cfg->microphysics_option == 2)
+        return fail(GA_ERR_UNSUPPORTED, "ga_create: microphysics_option 2 (ice) is not built");
+    if (cfg->microphysics_option < 0 || cfg->microphysics_option > 1)
+        return fail(GA_ERR_CONFIG, "ga_create: microphysics_option must be 0 or 1");
+    if (cfg->microphysics_option == 1 && cfg->rain_fallout != 1 && cfg->rain_fallout != 2)
+        return fail(GA_ERR_CONFIG, "ga_create: rain_fallout must be 1 or 2");
+    if (cfg->precision != GA_PREC_F64 && cfg->precision != GA_PREC_F32)
+        return fail(GA_ERR_CONFIG, "ga_create: unknown precision");
+    const int widths[] = {cfg->boundary_width_north, cfg->boundary_width_south, cfg->boundary_width_east,
+                          cfg->boundary_width_west};
+    for (int w : widths)
+        if (w < 0 || w > 64) return fail(GA_ERR_CONFIG, "ga_create: sponge widths must be in [0,64]");
+    if (cfg->periodic_ew_boundaries && cfg->nx < 13)
+        return fail(GA_ERR_CONFIG, "ga_create: periodic domains need NX >= 13");
+    int rc = GA_OK;
+    ga::EngineBase *e = nullptr;
+    try {
+        e = cfg->precision == GA_PREC_F64 ? ga::make_engine_f64(cfg, cols, &rc) : ga::make_engine_f32(cfg, cols, &rc);
+    } catch (const std::exception &ex) {
+        return fail(GA_ERR_NOMEM, std::string("ga_create: ") + ex.what());
+    }
+    if (!e) return fail(rc ? rc : GA_ERR_CUDA, "ga_create: device set-up failed");
+    ga_ctx *ctx = new ga_ctx;
+    ctx->e = e;
+    ctx->cfg = *cfg;
+    *out = ctx;
+    return GA_OK;
+}
+
+int ga_destroy(ga_ctx *ctx)
+{
+    if (!ctx) return fail(GA_ERR_ARG, "ga_destroy: null context");
+    delete ctx->e;
+    delete ctx;
+    return GA_OK;
+}
+
+int ga_set_field(ga_ctx *ctx, int field, int slot, const double *host, size_t n)
+{
+    if (!ctx || !host) return fail(GA_ERR_ARG, "ga_set_field: null pointer");
+    if (field < 0 || field > GA_ACCRAIN || slot < 0 || slot > 2) return fail(GA_ERR_ARG, "ga_set_field: bad field or slot");
+    int rc = ctx->e->set_field(field, slot, host, n);
+    if (rc == GA_ERR_ARG) set_error("ga_set_field: field not present in this context or wrong size");
+    return rc;
+}
+
+int ga_get_field(ga_ctx *ctx, int field, int slot, double *host, size_t n)
+{
+    if (!ctx || !host) return fail(GA_ERR_ARG, "ga_get_field: null pointer");
+    if (field < 0 || field > GA_ACCRAIN || slot < 0 || slot > 2) return fail(GA_ERR_ARG, "ga_get_field: bad field or slot");
+    int rc = ctx->e->get_field(field, slot, host, n);
+    if (rc == GA_ERR_ARG) set_error("ga_get_field: field not present in this context or wrong size");
+    return rc;
+}
+
+int ga_step_async(ga_ctx *ctx, int nsteps)
+{
+    if (!ctx || nsteps < 0) return fail(GA_ERR_ARG, "ga_step: bad arguments");
+    return ctx->e->step(nsteps);
+}
+
+int ga_synchronize(ga_ctx *ctx)
+{
+    if (!ctx) return fail(GA_ERR_ARG, "ga_synchronize: null context");
+    cudaSetDevice(ctx->e->device);
+    cudaError_t err = cudaStreamSynchronize(ctx->e->stream);
+    if (err != cudaSuccess) return fail(GA_ERR_CUDA, std::string("CUDA: ") + cudaGetErrorString(err));
+    return GA_OK;
+}
+
+int ga_step(ga_ctx *ctx, int nsteps)
+{
+    int rc = ga_step_async(ctx, nsteps);
+    if (rc) return rc;
+    rc = ga_synchronize(ctx);
+    if (rc) return rc;
+    return ctx->e->op(GA_OP_SIGN_CELLS, 0.0);  /* reports a Kessler E>100 flag */
+}
+
+int ga_op(ga_ctx *ctx, int op, double step)
+{
+    if (!ctx) return fail(GA_ERR_ARG, "ga_op: null context");
+    if (op < 0 || op >= GA_OP_COUNT) return fail(GA_ERR_ARG, "ga_op: unknown operator");
+    return ctx->e->op(op, step);
+}
+
+int ga_get_counters(ga_ctx *ctx, long long *bigcounter, double *mtime)
+{
+    if (!ctx) return fail(GA_ERR_ARG, "ga_get_counters: null context");
+    if (bigcounter) *bigcounter = ctx->e->bigcounter;
+    if (mtime) *mtime = ctx->e->mtime;
+    return GA_OK;
+}
+
+int ga_check_finite(ga_ctx *ctx)
+{
+    if (!ctx) return fail(GA_ERR_ARG, "ga_check_finite: null context");
+    int rc = ctx->e->check_finite();
+    if (rc == GA_ERR_NONFINITE) set_error("non-finite value in a prognostic buffer");
+    return rc;
+}
+
+long long ga_launch_count(ga_ctx *ctx) { return ctx ? ctx->e->launches : -1; }
+
+void *ga_stream(ga_ctx *ctx) { return ctx ? (void *)ctx->e->stream : nullptr; }
+
+void *ga_field_device_ptr(ga_ctx *ctx, int field, int slot)
+{
+    if (!ctx || field < 0 || field > GA_ACCRAIN || slot < 0 || slot > 2) return nullptr;
+    return ctx->e->field_ptr(field, slot);
+}
+
+}  /* extern "C" */

@@ -1,0 +1,581 @@
+// ga_engine.cuh - host side of one precision: device buffers, the buffer
+// rotation of the reference (solver.cpp:229-263, microphysics.cpp:642-669),
+// the per-operator launch sequences and the fused RK3 step.
+#pragma once
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "ga_engine.h"
+#include "ga_kernels.cuh"
+
+namespace ga {
+
+static inline int cdiv(long a, long b) { return (int)((a + b - 1) / b); }
+
+// prime factors of n for the shared-memory FFT, radix 4 first
+static inline FftPlan make_fft_plan(int n)
+{
+    FftPlan P;
+    std::memset(&P, 0, sizeof(P));
+    P.n = n;
+    int m = n;
+    while (m % 4 == 0 && P.nfac < 23) { P.fac[P.nfac++] = 4; m /= 4; }
+    for (int f = 2; m > 1 && P.nfac < 24;) {
+        if (m % f == 0) { P.fac[P.nfac++] = f; m /= f; }
+        else f = (f == 2) ? 3 : f + 2;
+    }
+    return P;
+}
+
+template <typename T>
+class Engine : public EngineBase {
+    typedef typename V2<T>::t T2;
+
+  public:
+    ga_config cfg;
+    int NX, NY, NZ;
+    long N;
+    int nprog;
+    T *buf[7][3] = {};
+    int ci[7], pi_[7], mi[7];  // rotation: which buffer is current / forecast / start-of-step
+    T *pi = nullptr, *bar[6] = {}, *vt = nullptr;
+    double *accrain = nullptr;
+    T2 *spec = nullptr;
+    T2 *tw_i = nullptr, *tw_j = nullptr;
+    FftPlan plan_i, plan_j;
+    std::vector<void *> allocs;
+    KParams<T> kp;
+    int *d_err = nullptr;
+    unsigned char *ppm_has = nullptr;
+    T *ppm_topq = nullptr, *ppm_topm = nullptr, *ppm_cin = nullptr, *ppm_carry = nullptr;
+    double *staging = nullptr;
+    int KTy = 1, KTx = 1, TC = 64;
+    size_t smem_y = 0, smem_x = 0, smem_th = 0;
+    int status = GA_OK;
+
+    template <typename X>
+    X *dalloc(size_t n)
+    {
+        void *p = nullptr;
+        if (cudaMalloc(&p, n * sizeof(X) ? n * sizeof(X) : 1) != cudaSuccess) {
+            status = GA_ERR_NOMEM;
+            return nullptr;
+        }
+        cudaMemset(p, 0, n * sizeof(X));
+        allocs.push_back(p);
+        return (X *)p;
+    }
+    template <typename X>
+    X *upload(const std::vector<X> &h)
+    {
+        X *d = dalloc<X>(h.size());
+        if (d) cudaMemcpy(d, h.data(), h.size() * sizeof(X), cudaMemcpyHostToDevice);
+        return d;
+    }
+    template <typename X>
+    const T *col_T(const X *src, int n)
+    {
+        std::vector<T> h(n);
+        for (int k = 0; k < n; k++) h[k] = (T)src[k];
+        return upload(h);
+    }
+
+    Engine(const ga_config *c, const ga_columns *cols) : cfg(*c)
+    {
+        NX = c->nx; NY = c->ny; NZ = c->nz;
+        N = (long)NX * NY * NZ;
+        device = c->device;
+        if (cudaSetDevice(device) != cudaSuccess) { status = GA_ERR_CUDA; return; }
+        if (cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking) != cudaSuccess) { status = GA_ERR_CUDA; return; }
+        const bool moist = c->microphysics_option == 1;
+        nprog = moist ? 7 : 4;
+        for (int f = 0; f < 7; f++) {
+            const int nb = f < nprog ? 3 : 0;
+            for (int s = 0; s < nb; s++) buf[f][s] = dalloc<T>(N);
+            ci[f] = 0; pi_[f] = 1; mi[f] = 2;
+        }
+        pi = dalloc<T>(N);
+        for (int b = 0; b < 6; b++) bar[b] = dalloc<T>(N);
+        vt = dalloc<T>(N);
+        accrain = dalloc<double>((size_t)NX * NY);
+        d_err = dalloc<int>(1);
+        const int periodic = c->periodic_ew_boundaries;
+        const int ni = periodic ? NX - 6 : NX, nj = NY;
+        spec = dalloc<T2>((size_t)ni * nj * NZ);
+
+        // ---- scalars (initialize_globals, initializer.cpp:168-179) ----
+        const double dx = c->dx, dy = c->dy, dz = c->dz, dt = c->dt;
+        std::memset(&kp, 0, sizeof(kp));
+        kp.nx = NX; kp.ny = NY; kp.nz = NZ; kp.n = N;
+        kp.ni = ni; kp.nj = nj; kp.ioff = periodic ? 3 : 0;
+        kp.periodic = periodic; kp.moist = moist; kp.rf = c->rain_fallout;
+        kp.dtx = (T)(dt / dx); kp.dty = (T)(dt / dy); kp.dtz = (T)(dt / dz); kp.dt = (T)dt;
+        kp.one_d_dx = (T)(1.0 / dx); kp.one_d_dy = (T)(1.0 / dy); kp.one_d_dz = (T)(1.0 / dz);
+        kp.mu = col_T(cols->mu, NZ); kp.mw = col_T(cols->mw, NZ);
+        kp.rhou = col_T(cols->rhou, NZ); kp.rhow = col_T(cols->rhow, NZ);
+        kp.one_d_rhou = col_T(cols->one_d_rhou, NZ);
+        kp.tb = col_T(cols->tb, NZ); kp.tbv = col_T(cols->tbv, NZ); kp.qb = col_T(cols->qb, NZ);
+        kp.f = col_T(cols->f, NY); kp.zsw = col_T(cols->zsw, NZ);
+        kp.rhou1 = (T)cols->rhou[1];
+
+        // ---- Rayleigh coefficients (damping.cpp:1150-1162) ----
+        const double trigpi = 3.14159265358979324;
+        std::vector<double> ru(NZ, 0.0), rw(NZ, 0.0);
+        kp.raylevel = c->rayleigh_damping_z;
+        if (kp.raylevel >= 0 && kp.raylevel < NZ) {
+            double raydmpcoef = 0.05, raydmpz = cols->zu[kp.raylevel];
+            for (int k = kp.raylevel; k < NZ; k++) {
+                ru[k] = raydmpcoef * 0.5 * (1.0 - cos(trigpi * (cols->zu[k] - raydmpz) / (cols->zu[NZ - 1] - raydmpz)));
+                rw[k] = raydmpcoef * 0.5 * (1.0 - cos(trigpi * (cols->zw[k] - raydmpz) / (cols->zw[NZ - 1] - raydmpz)));
+            }
+        } else {
+            kp.raylevel = NZ;
+        }
+        kp.ray_u = col_T(ru.data(), NZ); kp.ray_w = col_T(rw.data(), NZ);
+
+        // ---- sponge (init_boundaries, boundaries.cpp:44-114; cos_profile util.cpp:740) ----
+        auto cos_profile = [&](double pl, double ph, double frac, double shift) {
+            if (frac >= 0 && frac <= 1.0) return cos(pl * 2 * trigpi + (ph - pl) * 2 * trigpi * frac) + shift;
+            return 0.0;
+        };
+        const int ie = c->boundary_width_east, iw = c->boundary_width_west;
+        const int jn = c->boundary_width_north, js = c->boundary_width_south;
+        std::vector<double> ce(ie + 1), cw(iw + 1), cn(jn + 1), cs(js + 1);
+        for (int i = 0; i < ie; i++) ce[i] = 0.5 * cos_profile(-0.5, 0, (double)(i + 1) / (double)ie, 1);
+        for (int i = 0; i < iw; i++) cw[i] = 0.5 * cos_profile(0, 0.5, (double)i / (double)iw, 1);
+        for (int i = 0; i < jn; i++) cn[i] = 0.5 * cos_profile(-0.5, 0, (double)(i + 1) / (double)jn, 1);
+        for (int i = 0; i < js; i++) cs[i] = 0.5 * cos_profile(0, 0.5, (double)i / (double)js, 1);
+        kp.ce = col_T(ce.data(), ie + 1); kp.cw = col_T(cw.data(), iw + 1);
+        kp.cn = col_T(cn.data(), jn + 1); kp.cs = col_T(cs.data(), js + 1);
+        kp.eb = NX - ie; kp.ee = NX; kp.wb = 0; kp.we = iw;
+        kp.nb = NY - jn; kp.ne = NY; kp.sb = 0; kp.se = js;
+
+        // ---- pressure solver tables (init_fft3d, pressure.cpp:724-797) ----
+        std::vector<double> hcoef((size_t)ni * nj), kw(ni), lw(nj);
+        for (int i = 0; i < ni; i++) kw[i] = (double)i * 2 * trigpi / ((double)ni);
+        for (int j = 0; j < nj; j++) lw[j] = (double)j * 2 * trigpi / ((double)nj);
+        for (int i = 0; i < ni; i++)
+            for (int j = 0; j < nj; j++) hcoef[(size_t)i * nj + j] = cos(kw[i]) + cos(lw[j]) - 2.0;
+        kp.hcoef = upload(hcoef);
+        std::vector<double> ac(NZ, 0.0), cc(NZ, 0.0), vc(NZ, 0.0);
+        const double dz2 = dz * dz;
+        const double *mu = cols->mu, *mw = cols->mw, *rhow = cols->rhow;
+        for (int k = 1; k < NZ - 1; k++) {
+            ac[k] = mu[k] * mw[k] * rhow[k] / dz2;
+            cc[k] = mu[k] * mw[k + 1] * rhow[k + 1] / dz2;
+        }
+        ac[1] = 0;
+        cc[NZ - 2] = 0;
+        vc[1] = mu[1] * mw[2] * rhow[2] / dz2;
+        for (int k = 2; k < NZ - 2; k++) vc[k] = mu[k] * (mw[k + 1] * rhow[k + 1] + mw[k] * rhow[k]) / dz2;
+        vc[NZ - 2] = (mu[NZ - 2] * mw[NZ - 2] * rhow[NZ - 2]) / dz2;
+        kp.acoef = col_T(ac.data(), NZ); kp.ccoef = col_T(cc.data(), NZ); kp.vcoef = col_T(vc.data(), NZ);
+        kp.acoef_d = upload(ac); kp.ccoef_d = upload(cc); kp.vcoef_d = upload(vc);
+        kp.rhou_d = upload(std::vector<double>(cols->rhou, cols->rhou + NZ));
+        kp.dx2 = dx * dx;
+        kp.low_modes = sizeof(T) == 8 ? 0 : 3;
+
+        // ---- FFT plans and twiddles ----
+        plan_i = make_fft_plan(ni);
+        plan_j = make_fft_plan(nj);
+        auto twiddles = [&](int n) {
+            std::vector<T2> h(n);
+            for (int t = 0; t < n; t++) {
+                const double a = 6.283185307179586476925286766559 * (double)t / (double)n;
+                h[t].x = (T)cos(a);
+                h[t].y = (T)(-sin(a));
+            }
+            return upload(h);
+        };
+        tw_i = twiddles(ni);
+        tw_j = twiddles(nj);
+        const long budget = 32 * 1024;
+        KTy = (int)std::max(1L, std::min((long)NZ - 2, budget / (long)(2 * nj * sizeof(T2))));
+        KTx = (int)std::max(1L, std::min((long)NZ - 2, budget / (long)(2 * ni * sizeof(T2))));
+        smem_y = 2 * (size_t)nj * KTy * sizeof(T2);
+        smem_x = 2 * (size_t)ni * KTx * sizeof(T2);
+        smem_th = (size_t)TC * NZ * (sizeof(T2) + sizeof(T));
+        const int optin = 200 * 1024;
+        cudaFuncSetAttribute(k_div_fft_y<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+        cudaFuncSetAttribute(k_ifft_y_pi<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+        cudaFuncSetAttribute(k_fft_x<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+        cudaFuncSetAttribute(k_thomas<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+
+        if (moist && c->rain_fallout == 2) {
+            const long ncol = (long)(NX - 2) * (NY - 2);
+            ppm_has = dalloc<unsigned char>(ncol);
+            ppm_topq = dalloc<T>(ncol);
+            ppm_topm = dalloc<T>(ncol);
+            ppm_cin = dalloc<T>(ncol);
+            ppm_carry = dalloc<T>(1);
+        }
+        if (cudaDeviceSynchronize() != cudaSuccess && status == GA_OK) status = GA_ERR_CUDA;
+    }
+
+    ~Engine() override
+    {
+        cudaSetDevice(device);
+        if (stream) cudaStreamSynchronize(stream);
+        for (void *p : allocs) cudaFree(p);
+        if (staging) cudaFree(staging);
+        if (stream) cudaStreamDestroy(stream);
+    }
+
+    KFields<T> fields() const
+    {
+        KFields<T> F;
+        std::memset(&F, 0, sizeof(F));
+        for (int f = 0; f < 7; f++) {
+            F.cur[f] = buf[f][ci[f]];
+            F.P[f] = buf[f][pi_[f]];
+            F.M[f] = buf[f][mi[f]];
+        }
+        for (int b = 0; b < 6; b++) F.bar[b] = bar[b];
+        F.pi = pi;
+        F.vt = vt;
+        F.accrain = accrain;
+        return F;
+    }
+
+    T *host_field(int field, int slot, long *n)
+    {
+        *n = N;
+        if (field >= 0 && field < GA_NPROG) {
+            if (field >= nprog) return nullptr;
+            if (slot == GA_SLOT_CUR) return buf[field][ci[field]];
+            if (slot == GA_SLOT_P) return buf[field][pi_[field]];
+            if (slot == GA_SLOT_M) return buf[field][mi[field]];
+            return nullptr;
+        }
+        switch (field) {
+        case GA_PI: return pi;
+        case GA_UBAR: case GA_VBAR: case GA_WBAR: case GA_THBAR: case GA_QBAR: case GA_PBAR:
+            return bar[field - GA_UBAR];
+        case GA_VT: return vt;
+        }
+        return nullptr;
+    }
+
+    void *field_ptr(int field, int slot) override
+    {
+        if (field == GA_ACCRAIN) return accrain;
+        long n;
+        return host_field(field, slot, &n);
+    }
+
+    int ensure_staging()
+    {
+        if (!staging && cudaMalloc(&staging, N * sizeof(double)) != cudaSuccess) return GA_ERR_NOMEM;
+        return GA_OK;
+    }
+
+    int set_field(int field, int slot, const double *host, size_t n) override
+    {
+        if (!host) return GA_ERR_ARG;
+        cudaSetDevice(device);
+        if (field == GA_ACCRAIN) {
+            if (n != (size_t)NX * NY) return GA_ERR_ARG;
+            cudaMemcpyAsync(accrain, host, n * sizeof(double), cudaMemcpyHostToDevice, stream);
+            return sync_status();
+        }
+        long nn;
+        T *d = host_field(field, slot, &nn);
+        if (!d || (long)n != nn) return GA_ERR_ARG;
+        if (sizeof(T) == sizeof(double)) {
+            cudaMemcpyAsync(d, host, n * sizeof(double), cudaMemcpyHostToDevice, stream);
+        } else {
+            if (ensure_staging() != GA_OK) return GA_ERR_NOMEM;
+            cudaMemcpyAsync(staging, host, n * sizeof(double), cudaMemcpyHostToDevice, stream);
+            k_convert_in<T><<<cdiv(n, 256), 256, 0, stream>>>(d, staging, (long)n);
+            launches++;
+        }
+        return sync_status();
+    }
+
+    int get_field(int field, int slot, double *host, size_t n) override
+    {
+        if (!host) return GA_ERR_ARG;
+        cudaSetDevice(device);
+        if (field == GA_ACCRAIN) {
+            if (n != (size_t)NX * NY) return GA_ERR_ARG;
+            cudaMemcpyAsync(host, accrain, n * sizeof(double), cudaMemcpyDeviceToHost, stream);
+            return sync_status();
+        }
+        long nn;
+        T *d = host_field(field, slot, &nn);
+        if (!d || (long)n != nn) return GA_ERR_ARG;
+        if (sizeof(T) == sizeof(double)) {
+            cudaMemcpyAsync(host, d, n * sizeof(double), cudaMemcpyDeviceToHost, stream);
+        } else {
+            if (ensure_staging() != GA_OK) return GA_ERR_NOMEM;
+            k_convert_out<T><<<cdiv(n, 256), 256, 0, stream>>>(staging, d, (long)n);
+            launches++;
+            cudaMemcpyAsync(host, staging, n * sizeof(double), cudaMemcpyDeviceToHost, stream);
+        }
+        return sync_status();
+    }
+
+    int sync_status()
+    {
+        cudaError_t e = cudaStreamSynchronize(stream);
+        if (e != cudaSuccess) {
+            set_error(std::string("CUDA: ") + cudaGetErrorString(e));
+            return GA_ERR_CUDA;
+        }
+        return GA_OK;
+    }
+
+    int launch_status()
+    {
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) {
+            set_error(std::string("CUDA launch: ") + cudaGetErrorString(e));
+            return GA_ERR_CUDA;
+        }
+        return GA_OK;
+    }
+
+    // ------------------------------------------------------------------ ops
+    void advect(double step, int what)
+    {
+        const long tot = (long)(NX - 6) * (NY - 6) * (NZ - 2);
+        const double sdtg = step * cfg.dt * 9.8 * 0.5;  // step*dt*grav*0.5, advection.cpp:330
+        k_advect<T><<<cdiv(tot, 128), 128, 0, stream>>>(kp, fields(), (T)step, (T)sdtg, what);
+        launches++;
+    }
+
+    void edges_uvw()
+    {
+        KFields<T> F = fields();
+        if (!kp.periodic) {
+            const long tot = 2L * (NX + NY - 2) * (NZ - 2);
+            k_mirror_edges<T><<<cdiv(tot, 256), 256, 0, stream>>>(kp, F.P[FU], F.P[FV], F.P[FW]);
+        } else {
+            const long tot = 6L * NY * NZ;
+            k_periodic_copy<T><<<cdiv(tot, 256), 256, 0, stream>>>(kp, F.P[FU], F.P[FV], F.P[FW], (T *)nullptr);
+        }
+        launches++;
+    }
+
+    void poisson(double step)
+    {
+        KFields<T> F = fields();
+        const T sdt = (T)(step * cfg.dt);
+        const int nkt_y = cdiv(NZ - 2, KTy), nkt_x = cdiv(NZ - 2, KTx);
+        k_div_fft_y<T><<<dim3(kp.ni, nkt_y), 256, smem_y, stream>>>(kp, F, spec, plan_j, tw_j, sdt, KTy);
+        k_fft_x<T><<<dim3(kp.nj, nkt_x), 256, smem_x, stream>>>(kp, spec, plan_i, tw_i, 0, KTx);
+        const long ncol = (long)kp.ni * kp.nj;
+        k_thomas<T><<<cdiv(ncol, TC), TC, smem_th, stream>>>(kp, spec, TC);
+        k_fft_x<T><<<dim3(kp.nj, nkt_x), 256, smem_x, stream>>>(kp, spec, plan_i, tw_i, 1, KTx);
+        k_ifft_y_pi<T><<<dim3(kp.ni, nkt_y), 256, smem_y, stream>>>(kp, F, spec, plan_j, tw_j, KTy);
+        launches += 5;
+    }
+
+    void solve_pressure(double step)
+    {
+        edges_uvw();
+        poisson(step);
+    }
+
+    // per-field flags for k_post; pcopy selects the periodic two-pass form
+    void post(const int *flags, int nfields, double step, bool pcopy)
+    {
+        KFields<T> F = fields();
+        int fl[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        for (int f = 0; f < nfields && f < 7; f++) fl[f] = f < nprog ? flags[f] : 0;
+        int4 a = make_int4(fl[0], fl[1], fl[2], fl[3]), b = make_int4(fl[4], fl[5], fl[6], fl[7]);
+        const int wpb = 8;
+        if (pcopy && kp.periodic) {
+            k_post<T><<<cdiv(6L * NY, wpb), 32 * wpb, 0, stream>>>(kp, F, 7, a, b, (T)step, COLS_TARGETS);
+            k_post<T><<<cdiv((long)NX * NY, wpb), 32 * wpb, 0, stream>>>(kp, F, 7, a, b, (T)step, COLS_NONTARGETS);
+            launches += 2;
+        } else {
+            k_post<T><<<cdiv((long)NX * NY, wpb), 32 * wpb, 0, stream>>>(kp, F, 7, a, b, (T)step, COLS_ALL);
+            launches++;
+        }
+    }
+
+    void kessler()
+    {
+        if (!kp.moist) return;
+        KFields<T> F = fields();
+        const long tot = (long)(NX - 2) * (NY - 2) * (NZ - 2);
+        k_kessler<T><<<cdiv(tot, 128), 128, 0, stream>>>(kp, F, kp.rf != 2, d_err);
+        launches++;
+        if (kp.rf == 2) {
+            const long tv = (long)(NX - 2) * (NY - 2) * NZ;
+            k_fall_speed<T><<<cdiv(tv, 256), 256, 0, stream>>>(kp, F);
+            const long ncol = (long)(NX - 2) * (NY - 2);
+            k_ppm_prepare<T><<<cdiv(ncol, 64), 64, 0, stream>>>(kp, F, ppm_has, ppm_topq, ppm_topm);
+            k_ppm_carry<T><<<1, 1, 0, stream>>>(ncol, ppm_has, ppm_topq, ppm_topm, ppm_cin, ppm_carry);
+            k_ppm_remap<T><<<cdiv(ncol, 64), 64, 0, stream>>>(kp, F, ppm_has, ppm_cin);
+            k_fill<T><<<cdiv(N, 256), 256, 0, stream>>>(vt, N, T(0));
+            launches += 5;
+        }
+    }
+
+    void swap_inner(bool micro)
+    {
+        for (int f = 0; f < 4; f++) std::swap(ci[f], pi_[f]);
+        if (micro && nprog == 7)
+            for (int f = 4; f < 7; f++) std::swap(ci[f], pi_[f]);
+    }
+
+    void copy_m_from_p(int f0, int f1)
+    {
+        for (int f = f0; f < f1 && f < nprog; f++)
+            cudaMemcpyAsync(buf[f][mi[f]], buf[f][pi_[f]], N * sizeof(T), cudaMemcpyDeviceToDevice, stream);
+    }
+
+    int op(int o, double step) override
+    {
+        cudaSetDevice(device);
+        const bool moist = kp.moist;
+        int fl[7] = {0, 0, 0, 0, 0, 0, 0};
+        switch (o) {
+        case GA_OP_SIGN_CELLS: break;
+        case GA_OP_ADVECT_UVW: advect(step, ADV_UV | ADV_WB); break;
+        case GA_OP_SOLVE_PRESSURE: solve_pressure(step); break;
+        case GA_OP_PROJECT:
+            fl[FU] = fl[FV] = fl[FW] = PF_PROJECT;
+            post(fl, 7, step, false);
+            break;
+        case GA_OP_INTEGRATE_NON_HYDRO:
+            advect(step, ADV_UV | ADV_WB);
+            solve_pressure(step);
+            fl[FU] = fl[FV] = fl[FW] = PF_PROJECT;
+            post(fl, 7, step, false);
+            break;
+        case GA_OP_ADVECT_THETA: advect(step, ADV_TH); break;
+        case GA_OP_ADVECT_MICRO:
+            if (moist) advect(step, ADV_Q);
+            break;
+        case GA_OP_ZERO_MOISTURE:
+            if (moist) {
+                fl[FQV] = fl[FQC] = fl[FQR] = PF_ZERO;
+                post(fl, 7, step, false);
+            }
+            break;
+        case GA_OP_BC:
+            fl[FU] = fl[FV] = fl[FW] = fl[FTH] = PF_SPONGE | PF_VBC;
+            if (kp.periodic) periodic_pi();
+            post(fl, 7, step, true);
+            break;
+        case GA_OP_BC_MICRO:
+            if (moist) {
+                fl[FQV] = fl[FQC] = fl[FQR] = PF_SPONGE | PF_VBC;
+                post(fl, 7, step, true);
+            }
+            break;
+        case GA_OP_KESSLER: kessler(); break;
+        case GA_OP_RAYLEIGH:
+            fl[FU] = fl[FV] = fl[FW] = fl[FTH] = PF_RAYLEIGH;
+            post(fl, 7, step, false);
+            break;
+        case GA_OP_ADVANCE_INNER: swap_inner(true); break;
+        case GA_OP_ADVANCE_OUTER:
+            copy_m_from_p(0, 7);
+            swap_inner(true);
+            break;
+        default: return GA_ERR_ARG;
+        }
+        int rc = launch_status();
+        if (rc) return rc;
+        rc = sync_status();
+        if (rc) return rc;
+        return kessler_status();
+    }
+
+    void periodic_pi()
+    {
+        const long tot = 6L * NY * NZ;
+        k_periodic_copy<T><<<cdiv(tot, 256), 256, 0, stream>>>(kp, pi, (T *)nullptr, (T *)nullptr, (T *)nullptr);
+        launches++;
+    }
+
+    int kessler_status()
+    {
+        if (!kp.moist) return GA_OK;
+        int e = 0;
+        cudaMemcpy(&e, d_err, sizeof(int), cudaMemcpyDeviceToHost);
+        if (e) {
+            set_error("Kessler evaporation E>100 (the reference exits here, kessler.cpp:83-88)");
+            return GA_ERR_KESSLER;
+        }
+        return GA_OK;
+    }
+
+    // one RK3 step: s_integrate_rk3 (driver_serial.cpp:178-286), fused
+    void rk3_step()
+    {
+        static const double steps[3] = {1. / 3., 0.5, 1.0};
+        const bool moist = kp.moist;
+        for (int s = 0; s < 3; s++) {
+            const double st = steps[s];
+            advect(st, ADV_UV | ADV_WB | ADV_TH | (moist ? (ADV_Q | ADV_ZERO) : 0));
+            solve_pressure(st);
+            int fl[7] = {0, 0, 0, 0, 0, 0, 0};
+            fl[FU] = fl[FV] = fl[FW] = PF_PROJECT | PF_SPONGE | PF_VBC;
+            fl[FTH] = PF_SPONGE | PF_VBC;
+            fl[FQV] = fl[FQC] = fl[FQR] = PF_ZERO | PF_SPONGE | PF_VBC;
+            post(fl, 7, st, true);
+            if (s < 2) swap_inner(true);
+        }
+        if (moist) kessler();
+        int fl[7] = {0, 0, 0, 0, 0, 0, 0};
+        fl[FU] = fl[FV] = fl[FW] = fl[FTH] = PF_SPONGE | PF_VBC | PF_RAYLEIGH | PF_WRITE_M;
+        fl[FQV] = fl[FQC] = fl[FQR] = PF_SPONGE | PF_VBC | PF_WRITE_M;
+        post(fl, 7, 1.0, true);
+        swap_inner(true);
+        mtime += cfg.dt;
+        bigcounter++;
+    }
+
+    int step(int nsteps) override
+    {
+        cudaSetDevice(device);
+        for (int n = 0; n < nsteps; n++) {
+            rk3_step();
+            int rc = launch_status();
+            if (rc) return rc;
+        }
+        return GA_OK;
+    }
+
+    int check_finite() override
+    {
+        cudaSetDevice(device);
+        cudaMemsetAsync(d_err + 0, 0, 0, stream);
+        int *flag = nullptr;
+        if (cudaMalloc(&flag, sizeof(int)) != cudaSuccess) return GA_ERR_NOMEM;
+        cudaMemsetAsync(flag, 0, sizeof(int), stream);
+        for (int f = 0; f < nprog; f++)
+            for (int s = 0; s < 3; s++) {
+                k_check_finite<T><<<1024, 256, 0, stream>>>(buf[f][s], N, flag);
+                launches++;
+            }
+        int h = 0;
+        cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, stream);
+        int rc = sync_status();
+        cudaFree(flag);
+        if (rc) return rc;
+        return h ? GA_ERR_NONFINITE : GA_OK;
+    }
+};
+
+template <typename T>
+EngineBase *make_engine(const ga_config *cfg, const ga_columns *cols, int *rc)
+{
+    Engine<T> *e = new Engine<T>(cfg, cols);
+    if (e->status != GA_OK) {
+        *rc = e->status;
+        delete e;
+        return nullptr;
+    }
+    *rc = GA_OK;
+    return e;
+}
+
+}  // namespace ga

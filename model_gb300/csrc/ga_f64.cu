@@ -1,0 +1,10 @@
+// FP64 engine: the parity path.  Compiled with --fmad=false so that no
+// multiply-add is contracted and every expression rounds as the reference's.
+#include "ga_engine.cuh"
+
+namespace ga {
+EngineBase *make_engine_f64(const ga_config *cfg, const ga_columns *cols, int *rc)
+{
+    return make_engine<double>(cfg, cols, rc);
+}
+}  // namespace ga

@@ -1,0 +1,1164 @@
+// ga_kernels.cuh - device code of the anelastic step, templated on the real
+// type T (double: parity path, compiled without FMA contraction; float: fast
+// path).  Included once per precision by ga_f64.cu / ga_f32.cu.
+//
+// Layout: every 3-D field is [i][j][k], k fastest, as the reference's
+// INDEX(i,j,k) (include/model.h:50).  The spectral buffer of the pressure
+// solver is complex [i][q][k] (transform index q along y), so that the
+// vertical tridiagonal solve of one wavenumber reads one contiguous column.
+//
+// Arithmetic in every stencil, tendency, boundary and microphysics expression
+// keeps the evaluation order of the reference expression it implements (cited
+// file:line); with FP64 and no contraction the results match the reference's
+// serial build except where CUDA's pow/exp and the FFT round differently.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace ga {
+
+template <typename T> struct V2;
+template <> struct V2<double> { typedef double2 t; };
+template <> struct V2<float> { typedef float2 t; };
+
+// ---------------------------------------------------------------------------
+// parameters passed by value to every kernel
+// ---------------------------------------------------------------------------
+template <typename T>
+struct KParams {
+    int nx, ny, nz;
+    long n;
+    int ni, nj, ioff;        // spectral grid and its first physical column
+    int periodic, moist, rf;
+    T dtx, dty, dtz, dt, one_d_dx, one_d_dy, one_d_dz;
+    // vertical columns [nz] and Coriolis [ny]
+    const T *mu, *mw, *rhou, *rhow, *one_d_rhou, *tb, *tbv, *qb, *f, *zsw;
+    // Rayleigh coefficients [nz]
+    const T *ray_u, *ray_w;
+    int raylevel;
+    // sponge coefficients and strips (boundaries.cpp:44-114)
+    const T *ce, *cw, *cn, *cs;
+    int eb, ee, wb, we, nb, ne, sb, se;
+    // pressure solver tables (pressure.cpp:759-792)
+    const double *hcoef;                        // (cos kx + cos ly) - 2 per (p,q)
+    const T *acoef, *ccoef, *vcoef;             // [nz]
+    const double *acoef_d, *ccoef_d, *vcoef_d, *rhou_d;  // FP64 islands
+    double dx2;
+    T rhou1;
+    int low_modes;  // |p|,|q| below this solve in FP64 (FP32 contexts)
+};
+
+template <typename T>
+struct KFields {
+    T *cur[7], *P[7], *M[7];
+    const T *bar[6];
+    T *pi, *vt;
+    double *accrain;
+};
+
+enum { FU = 0, FV, FW, FTH, FQV, FQC, FQR };
+
+__host__ __device__ __forceinline__ long gix(int ny, int nz, int i, int j, int k)
+{
+    return ((long)i * ny + j) * nz + k;
+}
+
+template <typename T>
+__device__ __forceinline__ T sgn(T x) { return x > T(0) ? T(1) : T(-1); }
+
+// interpolation weights (fluxes.cpp:247-251)
+template <typename T> struct W {
+    static constexpr T c1_12 = T(1.0 / 12.0);
+    static constexpr T c7_12 = T(7.0 / 12.0);
+    static constexpr T c37_60 = T(37.0 / 60.0);
+    static constexpr T c2_15 = T(2.0 / 15.0);
+    static constexpr T c1_60 = T(1.0 / 60.0);
+};
+
+// INTERP_5TH_EAST (fluxes.cpp:110-122, 155-180): stencil a(-2)..a(+3)
+template <typename T>
+__device__ __forceinline__ T face5(T am2, T am1, T a0, T a1, T a2, T a3, T sign)
+{
+    T c6 = W<T>::c37_60 * (a1 + a0) - W<T>::c2_15 * (a2 + am1) + W<T>::c1_60 * (a3 + am2);
+    T u5 = -(a3 - am2) + T(5.0) * (a2 - am1) - T(10.0) * (a1 - a0);
+    return c6 + W<T>::c1_60 * sign * u5;
+}
+// INTERP_3RD_TOP (fluxes.cpp:131-136, 185-199): stencil a(-1)..a(+2)
+template <typename T>
+__device__ __forceinline__ T face3(T am1, T a0, T a1, T a2, T sign)
+{
+    T c4 = W<T>::c7_12 * (a1 + a0) - W<T>::c1_12 * (a2 + am1);
+    T u3 = (a2 - am1) - T(3.0) * (a1 - a0);
+    return c4 + W<T>::c1_12 * sign * u3;
+}
+
+template <typename T>
+struct Grid {
+    const KParams<T> &p;
+    __device__ Grid(const KParams<T> &pp) : p(pp) {}
+    __device__ __forceinline__ long ix(int i, int j, int k) const { return gix(p.ny, p.nz, i, j, k); }
+};
+
+#define LD(a, idx) __ldg((a) + (idx))
+
+// six points along i / j around the face between index 0 and +1
+template <typename T>
+__device__ __forceinline__ T f5i(const T *a, const KParams<T> &p, int i, int j, int k, T sign)
+{
+    const long s = (long)p.ny * p.nz, c = gix(p.ny, p.nz, i, j, k);
+    return face5<T>(LD(a, c - 2 * s), LD(a, c - s), LD(a, c), LD(a, c + s), LD(a, c + 2 * s),
+                    LD(a, c + 3 * s), sign);
+}
+template <typename T>
+__device__ __forceinline__ T f5j(const T *a, const KParams<T> &p, int i, int j, int k, T sign)
+{
+    const long s = p.nz, c = gix(p.ny, p.nz, i, j, k);
+    return face5<T>(LD(a, c - 2 * s), LD(a, c - s), LD(a, c), LD(a, c + s), LD(a, c + 2 * s),
+                    LD(a, c + 3 * s), sign);
+}
+template <typename T>
+__device__ __forceinline__ T f3k(const T *a, const KParams<T> &p, int i, int j, int k, T sign)
+{
+    const long c = gix(p.ny, p.nz, i, j, k);
+    return face3<T>(LD(a, c - 1), LD(a, c), LD(a, c + 1), LD(a, c + 2), sign);
+}
+template <typename T>
+__device__ __forceinline__ T f2k(const T *a, const KParams<T> &p, int i, int j, int k)
+{
+    const long c = gix(p.ny, p.nz, i, j, k);
+    return T(0.5) * (LD(a, c + 1) + LD(a, c));
+}
+
+// ---------------------------------------------------------------------------
+// momentum face fluxes: interpolate_velocity (fluxes.cpp:1384-1592),
+// advecting_velocity (:1109-1164), compute_fluxes (:582-627)
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ T u_east(const KParams<T> &p, const KFields<T> &F, int i, int j, int k)
+{
+    const T *U = F.cur[FU], *UB = F.bar[0];
+    const long c = gix(p.ny, p.nz, i, j, k), s = (long)p.ny * p.nz;
+    T ua = T(0.5) * (LD(U, c + s) + LD(U, c));
+    T uba = T(0.5) * (LD(UB, c + s) + LD(UB, c));
+    T ue = f5i(U, p, i, j, k, sgn(uba + ua));
+    T ube = f5i(UB, p, i, j, k, sgn(ua));
+    return ua * ube + (uba + ua) * ue;
+}
+template <typename T>
+__device__ T u_north(const KParams<T> &p, const KFields<T> &F, int i, int j, int k)
+{
+    const T *U = F.cur[FU], *UB = F.bar[0], *V = F.cur[FV], *VB = F.bar[1];
+    const long a = gix(p.ny, p.nz, i, j + 1, k), b = gix(p.ny, p.nz, i - 1, j + 1, k);
+    T va = T(0.5) * (LD(V, a) + LD(V, b));
+    T vba = T(0.5) * (LD(VB, a) + LD(VB, b));
+    T un = f5j(U, p, i, j, k, sgn(vba + va));
+    T ubn = f5j(UB, p, i, j, k, sgn(va));
+    return va * ubn + (vba + va) * un;
+}
+template <typename T>
+__device__ T u_top(const KParams<T> &p, const KFields<T> &F, int i, int j, int k)
+{
+    if (k == 0) return T(0);
+    const T *U = F.cur[FU], *UB = F.bar[0], *Wc = F.cur[FW], *WB = F.bar[2];
+    const long a = gix(p.ny, p.nz, i, j, k + 1), b = gix(p.ny, p.nz, i - 1, j, k + 1);
+    T wa = T(0.5) * (LD(Wc, a) + LD(Wc, b));
+    T wba = T(0.5) * (LD(WB, a) + LD(WB, b));
+    T ut, ubt;
+    if (k == 1 || k == p.nz - 2) {
+        ut = f2k(U, p, i, j, k);
+        ubt = f2k(UB, p, i, j, k);
+    } else {
+        ut = f3k(U, p, i, j, k, sgn(wba + wa));
+        ubt = f3k(UB, p, i, j, k, sgn(wa));
+    }
+    return wa * ubt + (wba + wa) * ut;
+}
+template <typename T>
+__device__ T v_east(const KParams<T> &p, const KFields<T> &F, int i, int j, int k)
+{
+    const T *U = F.cur[FU], *UB = F.bar[0], *V = F.cur[FV], *VB = F.bar[1];
+    const long a = gix(p.ny, p.nz, i + 1, j, k), b = gix(p.ny, p.nz, i + 1, j - 1, k);
+    T ua = T(0.5) * (LD(U, a) + LD(U, b));
+    T uba = T(0.5) * (LD(UB, a) + LD(UB, b));
+    T ve = f5i(V, p, i, j, k, sgn(uba + ua));
+    T vbe = f5i(VB, p, i, j, k, sgn(ua));
+    return ua * vbe + (uba + ua) * ve;
+}
+template <typename T>
+__device__ T v_north(const KParams<T> &p, const KFields<T> &F, int i, int j, int k)
+{
+    const T *V = F.cur[FV], *VB = F.bar[1];
+    const long c = gix(p.ny, p.nz, i, j, k);
+    T va = T(0.5) * (LD(V, c + p.nz) + LD(V, c));
+    T vba = T(0.5) * (LD(VB, c + p.nz) + LD(VB, c));
+    T vn = f5j(V, p, i, j, k, sgn(vba + va));
+    T vbn = f5j(VB, p, i, j, k, sgn(va));
+    return va * vbn + (vba + va) * vn;
+}
+template <typename T>
+__device__ T v_top(const KParams<T> &p, const KFields<T> &F, int i, int j, int k)
+{
+    if (k == 0) return T(0);
+    const T *V = F.cur[FV], *VB = F.bar[1], *Wc = F.cur[FW], *WB = F.bar[2];
+    const long a = gix(p.ny, p.nz, i, j, k + 1), b = gix(p.ny, p.nz, i, j - 1, k + 1);
+    T wa = T(0.5) * (LD(Wc, a) + LD(Wc, b));
+    T wba = T(0.5) * (LD(WB, a) + LD(WB, b));
+    T vt, vbt;
+    if (k == 1 || k == p.nz - 2) {
+        vt = f2k(V, p, i, j, k);
+        vbt = f2k(VB, p, i, j, k);
+    } else {
+        vt = f3k(V, p, i, j, k, sgn(wba + wa));
+        vbt = f3k(VB, p, i, j, k, sgn(wa));
+    }
+    return wa * vbt + (wba + wa) * vt;
+}
+
+// ---------------------------------------------------------------------------
+// scalar face fluxes: interpolate_scalar (fluxes.cpp:797-942) and
+// compute_fluxes_scalar / compute_fluxes_moisture (:632-654, :719-784).
+// Signs as compute_sign_cells (:316-341), taken from the current winds.
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ T s_east(const KParams<T> &p, const KFields<T> &F, const T *s, const T *sb, int i, int j, int k)
+{
+    const long a = gix(p.ny, p.nz, i + 1, j, k);
+    T u1 = LD(F.cur[FU], a);
+    T ut = LD(F.bar[0], a) + u1;
+    T se = f5i(s, p, i, j, k, sgn(ut));
+    if (!sb) return ut * se;
+    T be = f5i(sb, p, i, j, k, sgn(u1));
+    return u1 * be + ut * se;
+}
+template <typename T>
+__device__ T s_north(const KParams<T> &p, const KFields<T> &F, const T *s, const T *sb, int i, int j, int k)
+{
+    const long a = gix(p.ny, p.nz, i, j + 1, k);
+    T v1 = LD(F.cur[FV], a);
+    T vt = LD(F.bar[1], a) + v1;
+    T sn = f5j(s, p, i, j, k, sgn(vt));
+    if (!sb) return vt * sn;
+    T bn = f5j(sb, p, i, j, k, sgn(v1));
+    return v1 * bn + vt * sn;
+}
+template <typename T>
+__device__ T s_top(const KParams<T> &p, const KFields<T> &F, const T *s, const T *sb, int i, int j, int k)
+{
+    if (k == 0) return T(0);
+    const long a = gix(p.ny, p.nz, i, j, k + 1);
+    T w1 = LD(F.cur[FW], a);
+    T wt = LD(F.bar[2], a) + w1;
+    T st, bt = T(0);
+    if (k == 1 || k == p.nz - 2) {
+        st = f2k(s, p, i, j, k);
+        if (sb) bt = f2k(sb, p, i, j, k);
+    } else {
+        st = f3k(s, p, i, j, k, sgn(wt));
+        if (sb) bt = f3k(sb, p, i, j, k, sgn(w1));
+    }
+    if (!sb) return wt * st;
+    return w1 * bt + wt * st;
+}
+
+// rain fall speed of one point: calculate_rain_fall_speed_kessler
+// (kessler.cpp:222-252)
+template <typename T>
+__device__ __forceinline__ T fall_speed_point(const KParams<T> &p, T qr, int k)
+{
+    if (qr > T(1.0e-12)) {
+        T qrr = fmax(qr * T(0.001) * p.rhou[k], T(0.0));
+        T vtden = sqrt(p.rhou1 / p.rhou[k]);
+        return T(36.34) * (pow(qrr, T(0.1364))) * vtden;
+    }
+    return T(0);
+}
+
+// fall speed seen by the rain flux of an advected column: recomputed from the
+// current rain (Eulerian fallout, advection.cpp:456-457) or the stored field
+template <typename T>
+__device__ __forceinline__ T vt_at(const KParams<T> &p, const KFields<T> &F, int i, int j, int k)
+{
+    if (p.rf == 1 && k < p.nz - 1) {
+        int kk = k == 0 ? 1 : k;
+        return fall_speed_point(p, LD(F.cur[FQR], gix(p.ny, p.nz, i, j, kk)), kk);
+    }
+    return F.vt[gix(p.ny, p.nz, i, j, k)];
+}
+
+// interpolate_scalar_with_fallspeed + compute_fluxes_moisture, rain
+template <typename T>
+__device__ T r_top(const KParams<T> &p, const KFields<T> &F, int i, int j, int k)
+{
+    const T *s = F.cur[FQR];
+    if (k == 0) {
+        T s0 = T(0.5) * (LD(s, gix(p.ny, p.nz, i, j, 0)) + LD(s, gix(p.ny, p.nz, i, j, 1)));
+        return T(-0.5) * (vt_at(p, F, i, j, 1) + vt_at(p, F, i, j, 0)) * s0;
+    }
+    const long a = gix(p.ny, p.nz, i, j, k + 1);
+    T wb = LD(F.bar[2], a) + LD(F.cur[FW], a);
+    T wf = wb - T(0.5) * (vt_at(p, F, i, j, k) + vt_at(p, F, i, j, k + 1));
+    T st;
+    if (k == 1 || k == p.nz - 2) st = f2k(s, p, i, j, k);
+    else st = f3k(s, p, i, j, k, sgn(wf));
+    return wf * st;
+}
+
+// tendency of a flux-form scalar: theta_tend_cell / qv_tend_cell
+// (advection.cpp:152-168, :197-213), Z_ADVECT_BASE (:16-18)
+template <typename T>
+__device__ T s_tend(const KParams<T> &p, const KFields<T> &F, const T *s, const T *sb, const T *base,
+                    int i, int j, int k)
+{
+    const T DTZ = p.dtz * p.mu[k];
+    T t = -p.dtx * (s_east(p, F, s, sb, i, j, k) - s_east(p, F, s, sb, i - 1, j, k)) -
+          p.dty * (s_north(p, F, s, sb, i, j, k) - s_north(p, F, s, sb, i, j - 1, k)) -
+          DTZ * (p.rhow[k + 1] * s_top(p, F, s, sb, i, j, k) - p.rhow[k] * s_top(p, F, s, sb, i, j, k - 1)) *
+              p.one_d_rhou[k];
+    if (base) {
+        const T *Wc = F.cur[FW];
+        T zab = T(0.50) *
+                (p.rhow[k + 1] * LD(Wc, gix(p.ny, p.nz, i, j, k + 1)) * (base[k + 1] - base[k]) +
+                 p.rhow[k] * LD(Wc, gix(p.ny, p.nz, i, j, k)) * (base[k] - base[k - 1])) *
+                p.one_d_rhou[k];
+        t = t - DTZ * zab;
+    }
+    return t;
+}
+
+// ---------------------------------------------------------------------------
+// advection kernel: advect_uvw_velocity (+ buoyancy), advect_theta,
+// advect_microphysics_cell, optionally zero_moisture on the written points.
+// One thread per interior point [3,NX-3) x [3,NY-3) x [1,NZ-1).
+// ---------------------------------------------------------------------------
+enum { ADV_UV = 1, ADV_WB = 2, ADV_TH = 4, ADV_Q = 8, ADV_ZERO = 16 };
+
+template <typename T>
+__global__ void __launch_bounds__(128) k_advect(KParams<T> p, KFields<T> F, T step, T sdtg, int what)
+{
+    const int nzi = p.nz - 2, nyi = p.ny - 6, nxi = p.nx - 6;
+    const long tot = (long)nxi * nyi * nzi;
+    long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= tot) return;
+    const int k = 1 + (int)(t % nzi);
+    const int j = 3 + (int)((t / nzi) % nyi);
+    const int i = 3 + (int)(t / ((long)nzi * nyi));
+    const long c = gix(p.ny, p.nz, i, j, k);
+    const T DTZ = p.dtz * p.mu[k];
+    if (what & ADV_UV) {  // advection.cpp:318-322 with u_tend_cell / v_tend_cell (:73-122)
+        const T *U = F.cur[FU], *V = F.cur[FV];
+        const long sy = p.nz, sx = (long)p.ny * p.nz;
+        T ov_u = T(0.25) * (LD(V, c) + LD(V, c + sy) + LD(V, c - sx) + LD(V, c - sx + sy));
+        T ut = -p.dtx * (u_east(p, F, i, j, k) - u_east(p, F, i - 1, j, k)) -
+               p.dty * (u_north(p, F, i, j, k) - u_north(p, F, i, j - 1, k)) -
+               DTZ * (p.rhow[k + 1] * u_top(p, F, i, j, k) - p.rhow[k] * u_top(p, F, i, j, k - 1)) *
+                   p.one_d_rhou[k] +
+               p.dt * p.f[j] * ov_u;
+        F.P[FU][c] = LD(F.M[FU], c) + step * ut;
+        T ov_v = T(0.25) * (LD(U, c) + LD(U, c + sx) + LD(U, c - sy) + LD(U, c + sx - sy));
+        T vt = -p.dtx * (v_east(p, F, i, j, k) - v_east(p, F, i - 1, j, k)) -
+               p.dty * (v_north(p, F, i, j, k) - v_north(p, F, i, j - 1, k)) -
+               DTZ * (p.rhow[k + 1] * v_top(p, F, i, j, k) - p.rhow[k] * v_top(p, F, i, j, k - 1)) *
+                   p.one_d_rhou[k] -
+               p.dt * p.f[j] * ov_v;
+        F.P[FV][c] = LD(F.M[FV], c) + step * vt;
+    }
+    if ((what & ADV_WB) && k >= 2) {  // buoyancy overwrite, advection.cpp:329-337
+        const T *TH = F.cur[FTH];
+        T b0, b1;
+        if (!p.moist) {
+            b0 = LD(TH, c) / p.tbv[k];
+            b1 = LD(TH, c - 1) / p.tbv[k - 1];
+        } else {
+            const T *QV = F.cur[FQV], *QC = F.cur[FQC], *QR = F.cur[FQR];
+            b0 = LD(TH, c) / p.tbv[k] + T(0.61) * LD(QV, c) - LD(QC, c) - LD(QR, c);
+            b1 = LD(TH, c - 1) / p.tbv[k - 1] + T(0.61) * LD(QV, c - 1) - LD(QC, c - 1) - LD(QR, c - 1);
+        }
+        F.P[FW][c] = LD(F.M[FW], c) + sdtg * (b0 + b1);
+    }
+    if (what & ADV_TH)  // advection.cpp:366-370
+        F.P[FTH][c] = LD(F.M[FTH], c) + step * s_tend(p, F, F.cur[FTH], F.bar[3], p.tb, i, j, k);
+    if (what & ADV_Q) {  // advection.cpp:466-497
+        if (p.rf == 1) {
+            const T *QR = F.cur[FQR];
+            F.vt[c] = fall_speed_point(p, LD(QR, c), k);
+            if (k == 1) F.vt[c - 1] = fall_speed_point(p, LD(QR, c), 1);
+        }
+        T qv = LD(F.M[FQV], c) + step * s_tend(p, F, F.cur[FQV], F.bar[4], p.qb, i, j, k);
+        T qc = LD(F.M[FQC], c) + step * s_tend(p, F, F.cur[FQC], (const T *)nullptr, (const T *)nullptr, i, j, k);
+        T tr = -p.dtx * (s_east(p, F, F.cur[FQR], (const T *)nullptr, i, j, k) -
+                         s_east(p, F, F.cur[FQR], (const T *)nullptr, i - 1, j, k)) -
+               p.dty * (s_north(p, F, F.cur[FQR], (const T *)nullptr, i, j, k) -
+                        s_north(p, F, F.cur[FQR], (const T *)nullptr, i, j - 1, k)) -
+               DTZ * (p.rhow[k + 1] * r_top(p, F, i, j, k) - p.rhow[k] * r_top(p, F, i, j, k - 1)) *
+                   p.one_d_rhou[k];
+        T qr = LD(F.M[FQR], c) + step * tr;
+        if (what & ADV_ZERO) {  // zero_moisture on this point (microphysics.cpp:675-700)
+            if (qc < 0) qc = 0;
+            if (qr < 0) qr = 0;
+            T qbar = LD(F.bar[4], c);
+            if (qv + qbar + p.qb[k] < 0) qv = -(qbar + p.qb[k]);
+        }
+        F.P[FQV][c] = qv;
+        F.P[FQC][c] = qc;
+        F.P[FQR][c] = qr;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// lateral copies of UP/VP/WP before the pressure solve:
+// mirror_boundaries (boundaries.cpp:363-379) or periodic_uvw_boundaries
+// (:546-555).  Writes only edge points, reads only non-edge points.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void k_mirror_edges(KParams<T> p, T *a, T *b, T *c)
+{
+    const int ne = 2 * (p.nx + p.ny - 2);  // edge columns
+    long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int nzi = p.nz - 2;
+    if (t >= (long)ne * nzi) return;
+    const int k = 1 + (int)(t % nzi);
+    int e = (int)(t / nzi);
+    int i, j;
+    if (e < p.ny) { i = 0; j = e; }
+    else if ((e -= p.ny) < p.ny) { i = p.nx - 1; j = e; }
+    else if ((e -= p.ny) < p.nx - 2) { i = 1 + e; j = 0; }
+    else { e -= p.nx - 2; i = 1 + e; j = p.ny - 1; }
+    const int si = min(max(i, 1), p.nx - 2), sj = min(max(j, 1), p.ny - 2);
+    const long d = gix(p.ny, p.nz, i, j, k), s = gix(p.ny, p.nz, si, sj, k);
+    a[d] = a[s];
+    b[d] = b[s];
+    c[d] = c[s];
+}
+
+// periodic_boundaries_east_west (boundaries.cpp:562-574) for up to 4 fields:
+// columns 0,1,2 <- NX-6..NX-4 and NX-3..NX-1 <- 3..5, all j and k
+template <typename T>
+__global__ void k_periodic_copy(KParams<T> p, T *a, T *b, T *c, T *d)
+{
+    long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long per = (long)p.ny * p.nz;
+    if (t >= 6 * per) return;
+    const int col = (int)(t / per);
+    const long r = t % per;
+    const int dst = col < 3 ? col : p.nx - 6 + col;
+    const int src = col < 3 ? p.nx - 6 + col : col;  // col 3..5 -> dst NX-3..NX-1, src 3..5
+    const long od = (long)dst * per + r, os = (long)src * per + r;
+    if (a) a[od] = a[os];
+    if (b) b[od] = b[os];
+    if (c) c[od] = c[os];
+    if (d) d[od] = d[os];
+}
+
+// ---------------------------------------------------------------------------
+// shared-memory mixed-radix FFT (Stockham autosort).  Element (point n,
+// line l) of a batch of L lines lives at buf[n*L + l].  Twiddle table
+// tw[t] = exp(-2 pi i t / N); inverse transforms use its conjugate.
+// Unnormalised, like FFTW.
+// ---------------------------------------------------------------------------
+constexpr int PPM_MAXZ = 128;  // largest NZ the column kernels support
+
+struct FftPlan {
+    int n, nfac;
+    int fac[24];
+};
+
+template <typename T2>
+__device__ __forceinline__ T2 cmul(T2 a, T2 b)
+{
+    T2 r;
+    r.x = a.x * b.x - a.y * b.y;
+    r.y = a.x * b.y + a.y * b.x;
+    return r;
+}
+template <typename T2>
+__device__ __forceinline__ T2 twid(const T2 *tw, int t, bool inv)
+{
+    T2 w = tw[t];
+    if (inv) w.y = -w.y;
+    return w;
+}
+
+template <typename T, typename T2>
+__device__ T2 *fft_smem(T2 *a, T2 *b, int L, const FftPlan &P, const T2 *__restrict__ tw, bool inv)
+{
+    const int N = P.n;
+    int Ns = 1;
+    for (int f = 0; f < P.nfac; ++f) {
+        const int R = P.fac[f];
+        const int nb = N / R;
+        const int ts = N / (Ns * R);
+        for (int w = threadIdx.x; w < nb * L; w += blockDim.x) {
+            const int l = w % L, j = w / L, k = j % Ns;
+            const int ob = (j / Ns) * Ns * R + k;
+            if (R == 2) {
+                T2 v0 = a[j * L + l];
+                T2 v1 = a[(j + nb) * L + l];
+                if (k) v1 = cmul(v1, twid(tw, k * ts, inv));
+                T2 s, d;
+                s.x = v0.x + v1.x; s.y = v0.y + v1.y;
+                d.x = v0.x - v1.x; d.y = v0.y - v1.y;
+                b[ob * L + l] = s;
+                b[(ob + Ns) * L + l] = d;
+            } else if (R == 4) {
+                T2 v0 = a[j * L + l];
+                T2 v1 = a[(j + nb) * L + l];
+                T2 v2 = a[(j + 2 * nb) * L + l];
+                T2 v3 = a[(j + 3 * nb) * L + l];
+                if (k) {
+                    v1 = cmul(v1, twid(tw, k * ts, inv));
+                    v2 = cmul(v2, twid(tw, 2 * k * ts, inv));
+                    v3 = cmul(v3, twid(tw, 3 * k * ts, inv));
+                }
+                T2 s02, d02, s13, d13, x0, x1, x2, x3;
+                s02.x = v0.x + v2.x; s02.y = v0.y + v2.y;
+                d02.x = v0.x - v2.x; d02.y = v0.y - v2.y;
+                s13.x = v1.x + v3.x; s13.y = v1.y + v3.y;
+                d13.x = v1.x - v3.x; d13.y = v1.y - v3.y;
+                x0.x = s02.x + s13.x; x0.y = s02.y + s13.y;
+                x2.x = s02.x - s13.x; x2.y = s02.y - s13.y;
+                if (!inv) {  // X1 = d02 - i d13, X3 = d02 + i d13
+                    x1.x = d02.x + d13.y; x1.y = d02.y - d13.x;
+                    x3.x = d02.x - d13.y; x3.y = d02.y + d13.x;
+                } else {
+                    x1.x = d02.x - d13.y; x1.y = d02.y + d13.x;
+                    x3.x = d02.x + d13.y; x3.y = d02.y - d13.x;
+                }
+                b[ob * L + l] = x0;
+                b[(ob + Ns) * L + l] = x1;
+                b[(ob + 2 * Ns) * L + l] = x2;
+                b[(ob + 3 * Ns) * L + l] = x3;
+            } else {  // generic radix: direct R-point DFT with combined twiddles
+                for (int m = 0; m < R; ++m) {
+                    T2 acc;
+                    acc.x = T(0);
+                    acc.y = T(0);
+                    for (int r = 0; r < R; ++r) {
+                        const int t = (k * r * ts + ((r * m) % R) * nb) % N;
+                        T2 x = a[(j + r * nb) * L + l];
+                        T2 wv = twid(tw, t, inv);
+                        acc.x += x.x * wv.x - x.y * wv.y;
+                        acc.y += x.x * wv.y + x.y * wv.x;
+                    }
+                    b[(ob + m * Ns) * L + l] = acc;
+                }
+            }
+        }
+        __syncthreads();
+        T2 *tmp = a;
+        a = b;
+        b = tmp;
+        Ns *= R;
+    }
+    return a;
+}
+
+// divergence tendency of the pressure equation at a physical point
+// (divergence3d, pressure.cpp:1340-1381)
+template <typename T>
+__device__ __forceinline__ T divergence(const KParams<T> &p, const KFields<T> &F, int i, int j, int k, T sdt)
+{
+    const T *UP = F.P[FU], *VP = F.P[FV], *WP = F.P[FW];
+    const long c = gix(p.ny, p.nz, i, j, k);
+    T d = p.rhou[k] * (UP[c + (long)p.ny * p.nz] - UP[c]) * p.one_d_dx +
+          p.rhou[k] * (VP[c + p.nz] - VP[c]) * p.one_d_dy +
+          (p.rhow[k + 1] * WP[c + 1] - p.rhow[k] * WP[c]) * (p.one_d_dz * p.mu[k]);
+    d /= sdt;
+    return d;
+}
+
+// divergence (with the mirror / periodic placement of divergence3d and
+// divergence3d_periodic) + forward FFT along y.  Block = (spectral row i,
+// tile of KT levels starting at level 1).
+template <typename T>
+__global__ void k_div_fft_y(KParams<T> p, KFields<T> F, typename V2<T>::t *spec, FftPlan pj,
+                            const typename V2<T>::t *tw, T sdt, int KT)
+{
+    typedef typename V2<T>::t T2;
+    extern __shared__ unsigned char smem_raw[];
+    T2 *a = (T2 *)smem_raw;
+    T2 *b = a + (long)p.nj * KT;
+    const int is = blockIdx.x;
+    const int k0 = 1 + blockIdx.y * KT;
+    const int kt = min(KT, p.nz - 1 - k0);
+    int ii;
+    if (!p.periodic) ii = min(max(is, 1), p.nx - 2);
+    else ii = is + 3;
+    for (int w = threadIdx.x; w < p.nj * KT; w += blockDim.x) {
+        const int l = w % KT, q = w / KT;
+        T2 v;
+        v.y = T(0);
+        v.x = T(0);
+        if (l < kt) {
+            const int jj = min(max(q, 1), p.ny - 2);
+            v.x = divergence(p, F, ii, jj, k0 + l, sdt);
+        }
+        a[w] = v;
+    }
+    __syncthreads();
+    T2 *r = fft_smem<T, T2>(a, b, KT, pj, tw, false);
+    for (int w = threadIdx.x; w < p.nj * KT; w += blockDim.x) {
+        const int l = w % KT, q = w / KT;
+        if (l < kt) spec[((long)is * p.nj + q) * p.nz + k0 + l] = r[w];
+    }
+}
+
+// FFT along x of the spectral buffer for one y-wavenumber q and a tile of
+// levels.  sign: forward (false) or inverse (true).
+template <typename T>
+__global__ void k_fft_x(KParams<T> p, typename V2<T>::t *spec, FftPlan pi, const typename V2<T>::t *tw,
+                        int inv, int KT)
+{
+    typedef typename V2<T>::t T2;
+    extern __shared__ unsigned char smem_raw[];
+    T2 *a = (T2 *)smem_raw;
+    T2 *b = a + (long)p.ni * KT;
+    const int q = blockIdx.x;
+    const int k0 = 1 + blockIdx.y * KT;
+    const int kt = min(KT, p.nz - 1 - k0);
+    for (int w = threadIdx.x; w < p.ni * KT; w += blockDim.x) {
+        const int l = w % KT, i = w / KT;
+        T2 v;
+        v.x = T(0);
+        v.y = T(0);
+        if (l < kt) v = spec[((long)i * p.nj + q) * p.nz + k0 + l];
+        a[w] = v;
+    }
+    __syncthreads();
+    T2 *r = fft_smem<T, T2>(a, b, KT, pi, tw, inv != 0);
+    for (int w = threadIdx.x; w < p.ni * KT; w += blockDim.x) {
+        const int l = w % KT, i = w / KT;
+        if (l < kt) spec[((long)i * p.nj + q) * p.nz + k0 + l] = r[w];
+    }
+}
+
+// normalisation (pressure.cpp:827) + Thomas algorithm per horizontal
+// wavenumber (:834-871), with the diagonal of init_fft3d's stretched branch
+// (:778-792) formed from the (cos kx + cos ly - 2) table.  One thread per
+// column; columns staged through shared memory for coalesced access.
+template <typename T, typename A>
+__device__ void thomas_column(const KParams<T> &p, typename V2<T>::t *x, A *Fw, long col, double size2d,
+                              const A *rhou, const A *ac, const A *cc, const A *vc)
+{
+    typedef typename V2<T>::t T2;
+    const int nz = p.nz;
+    const A h = (A)p.hcoef[col];
+    const A dx2 = (A)p.dx2;
+    A xr[2], z;
+    // level 1
+    z = A(1.0) / (rhou[1] * A(2.0) * h / dx2 - vc[1]);
+    A Fk = cc[1] * z;
+    Fw[1] = Fk;
+    A pr = (A)x[1].x / (A)size2d, pim = (A)x[1].y / (A)size2d;
+    pr = pr * z;
+    pim = pim * z;
+    x[1].x = (T)pr;
+    x[1].y = (T)pim;
+    xr[0] = pr;
+    xr[1] = pim;
+    for (int k = 2; k < nz - 1; k++) {
+        A bk = rhou[k] * A(2.0) * h / dx2 - vc[k];
+        z = A(1.0) / (bk - ac[k] * Fk);
+        Fk = cc[k] * z;
+        Fw[k] = Fk;
+        A vr = (A)x[k].x / (A)size2d, vi = (A)x[k].y / (A)size2d;
+        vr = (vr - ac[k] * xr[0]) * z;
+        vi = (vi - ac[k] * xr[1]) * z;
+        x[k].x = (T)vr;
+        x[k].y = (T)vi;
+        xr[0] = vr;
+        xr[1] = vi;
+    }
+    if (col == 0) {  // mean-mode gauge (pressure.cpp:858-859)
+        x[nz - 2].x = T(0);
+        x[nz - 2].y = T(0);
+    }
+    A nr = (A)x[nz - 2].x, ni = (A)x[nz - 2].y;
+    for (int k = nz - 3; k >= 1; k--) {
+        A vr = (A)x[k].x, vi = (A)x[k].y;
+        vr -= Fw[k] * nr;
+        vi -= Fw[k] * ni;
+        x[k].x = (T)vr;
+        x[k].y = (T)vi;
+        nr = vr;
+        ni = vi;
+    }
+}
+
+template <typename T>
+__global__ void k_thomas(KParams<T> p, typename V2<T>::t *spec, int TC)
+{
+    typedef typename V2<T>::t T2;
+    extern __shared__ unsigned char smem_raw[];
+    T2 *xs = (T2 *)smem_raw;
+    T *fs = (T *)(xs + (long)TC * p.nz);
+    const long ncol = (long)p.ni * p.nj;
+    const long c0 = (long)blockIdx.x * TC;
+    const int nc = (int)min((long)TC, ncol - c0);
+    T2 *g = spec + c0 * p.nz;
+    for (int w = threadIdx.x; w < nc * p.nz; w += blockDim.x) xs[w] = g[w];
+    __syncthreads();
+    const double size2d = (double)(p.ni * p.nj);
+    for (int c = threadIdx.x; c < nc; c += blockDim.x) {
+        const long col = c0 + c;
+        const int pp = (int)(col / p.nj), qq = (int)(col % p.nj);
+        bool low = false;
+        if (p.low_modes > 0) {
+            int ap = min(pp, p.ni - pp), aq = min(qq, p.nj - qq);
+            low = ap < p.low_modes && aq < p.low_modes;
+        }
+        if (low) {
+            double Floc[PPM_MAXZ];
+            thomas_column<T, double>(p, xs + (long)c * p.nz, Floc, col, size2d, p.rhou_d, p.acoef_d,
+                                     p.ccoef_d, p.vcoef_d);
+        } else
+            thomas_column<T, T>(p, xs + (long)c * p.nz, fs + (long)c * p.nz, col, size2d, p.rhou, p.acoef,
+                                p.ccoef, p.vcoef);
+    }
+    __syncthreads();
+    for (int w = threadIdx.x; w < nc * p.nz; w += blockDim.x) g[w] = xs[w];
+}
+
+// inverse FFT along y + PI = real part, with the level copies of
+// poisson_fft3d (pressure.cpp:878-892) and the lateral placement of
+// mirror_boundaries(PI) or periodic_pressure_boundaries.
+template <typename T>
+__global__ void k_ifft_y_pi(KParams<T> p, KFields<T> F, typename V2<T>::t *spec, FftPlan pj,
+                            const typename V2<T>::t *tw, int KT)
+{
+    typedef typename V2<T>::t T2;
+    extern __shared__ unsigned char smem_raw[];
+    T2 *a = (T2 *)smem_raw;
+    T2 *b = a + (long)p.nj * KT;
+    const int is = blockIdx.x;
+    const int k0 = 1 + blockIdx.y * KT;
+    const int kt = min(KT, p.nz - 1 - k0);
+    for (int w = threadIdx.x; w < p.nj * KT; w += blockDim.x) {
+        const int l = w % KT, q = w / KT;
+        T2 v;
+        v.x = T(0);
+        v.y = T(0);
+        if (l < kt) v = spec[((long)is * p.nj + q) * p.nz + k0 + l];
+        a[w] = v;
+    }
+    __syncthreads();
+    T2 *r = fft_smem<T, T2>(a, b, KT, pj, tw, true);
+    T *PI = F.pi;
+    const int nz = p.nz, ny = p.ny;
+    for (int w = threadIdx.x; w < p.nj * KT; w += blockDim.x) {
+        const int l = w % KT, j = w / KT;
+        if (l >= kt) continue;
+        const int k = k0 + l;
+        if (!p.periodic) {
+            const int i = is;
+            // levels 1..NZ-2: mirrored in x and y
+            const T v = r[min(max(j, 1), ny - 2) * KT + l].x;
+            if (i >= 1 && i <= p.nx - 2) {
+                PI[gix(ny, nz, i, j, k)] = v;
+                if (i == 1) PI[gix(ny, nz, 0, j, k)] = v;
+                if (i == p.nx - 2) PI[gix(ny, nz, p.nx - 1, j, k)] = v;
+            }
+            // levels 0 and NZ-1: raw copies of levels 1 and NZ-2
+            const T raw = r[w].x;
+            if (k == 1) PI[gix(ny, nz, i, j, 0)] = raw;
+            if (k == nz - 2) PI[gix(ny, nz, i, j, nz - 1)] = raw;
+        } else {
+            const int i = is + 3;
+            const T raw = r[w].x;
+            int dst[2] = {i, -1};
+            if (i >= p.nx - 6 && i <= p.nx - 4) dst[1] = i - (p.nx - 6);
+            if (i >= 3 && i <= 5) dst[1] = p.nx - 3 + (i - 3);
+            for (int d = 0; d < 2; d++) {
+                if (dst[d] < 0) continue;
+                PI[gix(ny, nz, dst[d], j, k)] = raw;
+                if (k == 1) PI[gix(ny, nz, dst[d], j, 0)] = raw;
+                if (k == nz - 2) PI[gix(ny, nz, dst[d], j, nz - 1)] = raw;
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// column post-processing: a warp per (i,j) column applies, per field and in
+// the reference's order, zero_moisture (microphysics.cpp:675-700), the
+// pressure-gradient projection (solver.cpp:120-135), the sponge strips
+// (boundaries.cpp:436-498), the periodic copy (:562-574), the top/bottom
+// conditions (:304-326) and Rayleigh damping (damping.cpp:1148-1177); then
+// writes the forecast buffer and optionally the start-of-step buffer.  All
+// values of a column are read before any is written, and the k=1 / k=NZ-2
+// values the vertical condition needs travel by shuffle, so no thread reads a
+// point another thread writes.
+// ---------------------------------------------------------------------------
+enum { PF_ZERO = 1, PF_PROJECT = 2, PF_SPONGE = 4, PF_VBC = 8, PF_RAYLEIGH = 16, PF_WRITE_M = 32,
+       PF_PCOPY = 64 };
+enum { COLS_ALL = 0, COLS_TARGETS = 1, COLS_NONTARGETS = 2 };
+constexpr int KPL = 4;  // levels per lane: NZ <= 128
+
+template <typename T>
+__device__ __forceinline__ T chain_value(const KParams<T> &p, const KFields<T> &F, int f, int flags, int i,
+                                         int j, int k, T v, T step)
+{
+    const long c = gix(p.ny, p.nz, i, j, k);
+    if (flags & PF_ZERO) {
+        if (f == FQC || f == FQR) {
+            if (v < 0) v = 0;
+        } else if (f == FQV) {
+            if (i >= 1 && i < p.nx - 1 && j >= 1 && j < p.ny - 1 && k >= 1 && k < p.nz - 1) {
+                T qbar = F.bar[4][c];
+                if (v + qbar + p.qb[k] < 0) v = -(qbar + p.qb[k]);
+            }
+        }
+    }
+    if ((flags & PF_PROJECT) && f <= FW && i >= 1 && i < p.nx - 1 && j >= 1 && j < p.ny - 1 && k >= 1 &&
+        k < p.nz - 1) {
+        const T *PI = F.pi;
+        if (f == FU) v = v - step * (p.dtx * (PI[c] - PI[c - (long)p.ny * p.nz]));
+        else if (f == FV) v = v - step * (p.dty * (PI[c] - PI[c - p.nz]));
+        else if (k >= 2) v = v - step * ((p.dtz * p.mw[k]) * (PI[c] - PI[c - 1]));
+    }
+    if ((flags & PF_SPONGE) && k >= 1) {
+        if (!p.periodic && j >= 1) {
+            if (i >= p.eb && i < p.ee) v = v - p.ce[i - p.eb] * v;
+            if (i >= p.wb && i < p.we) v = v - p.cw[i - p.wb] * v;
+        }
+        if (i >= 1) {
+            if (j >= p.sb && j < p.se) v = v - p.cs[j - p.sb] * v;
+            if (j >= p.nb && j < p.ne) v = v - p.cn[j - p.nb] * v;
+        }
+    }
+    return v;
+}
+
+template <typename T>
+__global__ void k_post(KParams<T> p, KFields<T> F, int nfields, int4 fl0, int4 fl1, T step, int cols)
+{
+    const int lane = threadIdx.x & 31;
+    const long warp = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int i, j;
+    if (cols == COLS_TARGETS) {
+        if (warp >= 6L * p.ny) return;
+        const int col = (int)(warp / p.ny);
+        j = (int)(warp % p.ny);
+        i = col < 3 ? col : p.nx - 6 + col;
+    } else {
+        if (warp >= (long)p.nx * p.ny) return;
+        i = (int)(warp / p.ny);
+        j = (int)(warp % p.ny);
+        if (cols == COLS_NONTARGETS && (i < 3 || i >= p.nx - 3)) return;
+    }
+    // source column of a periodic target
+    int si = i;
+    if (cols == COLS_TARGETS) si = i < 3 ? p.nx - 6 + i : 3 + (i - (p.nx - 3));
+    const int nz = p.nz;
+    const int flv[8] = {fl0.x, fl0.y, fl0.z, fl0.w, fl1.x, fl1.y, fl1.z, fl1.w};
+    for (int f = 0; f < nfields; ++f) {
+        const int flags = flv[f];
+        if (!flags) continue;
+        T *P = F.P[f];
+        T vals[KPL];
+#pragma unroll
+        for (int r = 0; r < KPL; ++r) {
+            const int k = lane + 32 * r;
+            vals[r] = T(0);
+            if (k < nz) {
+                T v = P[gix(p.ny, nz, si, j, k)];
+                vals[r] = chain_value(p, F, f, flags, si, j, k, v, step);
+            }
+        }
+        // values at k=1 and k=NZ-2 after the chain, for the vertical condition
+        const T v1 = __shfl_sync(0xffffffffu, vals[0], 1);
+        const int kt = nz - 2;
+        T vtop = vals[0];
+#pragma unroll
+        for (int r = 0; r < KPL; ++r)
+            if (kt / 32 == r) vtop = __shfl_sync(0xffffffffu, vals[r], kt & 31);
+        __syncwarp();
+#pragma unroll
+        for (int r = 0; r < KPL; ++r) {
+            const int k = lane + 32 * r;
+            if (k >= nz) continue;
+            T v = vals[r];
+            if ((flags & PF_VBC) && i >= 1 && j >= 1) {
+                if (f == FW) {
+                    if (k == 0 || k == 1 || k == nz - 1) v = T(0);
+                } else {
+                    if (k == 0) v = v1;
+                    if (k == nz - 1) v = vtop;
+                }
+            }
+            if ((flags & PF_RAYLEIGH) && f <= FTH && i >= 1 && i < p.nx - 1 && j >= 1 && j < p.ny - 1 &&
+                k >= p.raylevel) {
+                const T cr = (f == FW) ? p.ray_w[k] : p.ray_u[k];
+                v = v - cr * v;
+            }
+            const long c = gix(p.ny, nz, i, j, k);
+            P[c] = v;
+            if (flags & PF_WRITE_M) F.M[f][c] = v;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Kessler warm rain, pointwise (kessler.cpp:25-183); the k=1 thread of each
+// column then adds the Eulerian precipitation (precip_rate,
+// microphysics.cpp:143-160) when rain_fallout == 1.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(128) k_kessler(KParams<T> p, KFields<T> F, int precip, int *err)
+{
+    const int nzi = p.nz - 2, nyi = p.ny - 2, nxi = p.nx - 2;
+    long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long)nxi * nyi * nzi) return;
+    const int k = 1 + (int)(t % nzi);
+    const int j = 1 + (int)((t / nzi) % nyi);
+    const int i = 1 + (int)(t / ((long)nzi * nyi));
+    const long ix = gix(p.ny, p.nz, i, j, k);
+    const T cp = T(1004), Rd = T(287.0), p0 = T(100000), Lv = T(2.5e6);
+    const T cpRd = T(1004.0 / 287.0);
+    const T dt = p.dt;
+    T *THP = F.P[FTH], *QVP = F.P[FQV], *QCP = F.P[FQC], *QRP = F.P[FQR];
+    const T rhou = p.rhou[k];
+    T thp = THP[ix], qvp = QVP[ix], qcp = QCP[ix], qrp = QRP[ix];
+    const T thbar = F.bar[3][ix], qbar = F.bar[4][ix], pbar = F.bar[5][ix];
+    T theta = thp + thbar + p.tb[k];
+    T pressure = F.pi[ix] / (cp * p.tbv[k]) + pbar;
+    T vapor = qvp + qbar + p.qb[k];
+    T temperature = theta * pressure;
+    T pd = p0 * pow(pressure, cpRd);
+    T A, B, E, esl, qvsat;
+    if (qcp > T(1.0e-3)) A = T(0.001) * (qcp - T(1.0e-3)) * dt;
+    else A = 0;
+    if (qrp > T(1.0e-12)) B = rhou * T(2.2) * qcp * pow(qrp, T(0.875)) * dt;
+    else B = 0;
+    if (qrp > T(1.0e-12)) {
+        esl = T(611.2) * exp(T(17.67) * (temperature - T(273.15)) / (temperature - T(29.65)));
+        qvsat = T(0.62197) * esl / (pd - esl);
+        T cvent = T(1.6) + T(30.3922) * pow(rhou * qrp, T(0.2046));
+        E = (T(1.0) / rhou) *
+            (((T(1.0) - vapor / qvsat) * cvent * pow(rhou * qrp, T(0.525))) / (T(2.03e4) + T(9.58e6) / (pd * qvsat))) *
+            dt;
+        E = fmin(qrp, E);
+        E = fmax(E, T(0.0));
+        if (E > T(100)) atomicExch(err, 1);
+    } else
+        E = 0;
+    qvp += E;
+    T total_convert = fmin(A + B, qcp);
+    qcp -= total_convert;
+    qrp += (total_convert - E);
+    T de = (Lv / (cp * pressure)) * E;
+    thp -= de;
+    theta = thp + thbar + p.tb[k];
+    vapor = qvp + qbar + p.qb[k];
+    temperature = theta * pressure;
+    esl = T(611.2) * exp(T(17.67) * (temperature - T(273.15)) / (temperature - T(29.65)));
+    qvsat = T(0.62197) * esl / (pd - esl);
+    const T fcoef = T(17.67 * (273.15 - 29.65) * 2.5e6 / 1004.0);
+    T tm = temperature - T(29.65);
+    T phi = pd / (pd - esl) * qvsat * fcoef / (tm * tm);
+    T C = T(0.0);
+    if (vapor > qvsat) C = (vapor - qvsat) / (T(1.0) + phi);
+    else if (vapor < qvsat && qcp > 0) C = -fmin(qcp, (qvsat - vapor) / (T(1.0) + phi));
+    qcp += C;
+    qvp -= C;
+    T dc = (Lv / (cp * pressure)) * C;
+    thp += dc;
+    THP[ix] = thp;
+    QVP[ix] = qvp;
+    QCP[ix] = qcp;
+    QRP[ix] = qrp;
+    (void)Rd;
+    if (precip && k == 1) {
+        const long i0 = ix - 1;
+        const double inc = (double)(p.rhow[1] * T(0.5) * (F.vt[i0] + F.vt[ix]) * T(0.5) * (QRP[i0] + qrp) * dt);
+        F.accrain[(long)i * p.ny + j] += inc;
+    }
+}
+
+// fall speed over [1,NX-1) x [1,NY-1) from the forecast rain (semi-Lagrangian
+// fallout path, kessler.cpp:190)
+template <typename T>
+__global__ void k_fall_speed(KParams<T> p, KFields<T> F)
+{
+    const int nyi = p.ny - 2, nxi = p.nx - 2;
+    long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long)nxi * nyi * p.nz) return;
+    const int k = (int)(t % p.nz);
+    const int j = 1 + (int)((t / p.nz) % nyi);
+    const int i = 1 + (int)(t / ((long)p.nz * nyi));
+    const long c = gix(p.ny, p.nz, i, j, k);
+    if (k >= 1 && k < p.nz - 1) F.vt[c] = fall_speed_point(p, F.P[FQR][c], k);
+    else if (k == 0) F.vt[c] = fall_speed_point(p, F.P[FQR][c + 1], 1);
+}
+
+// ---------------------------------------------------------------------------
+// semi-Lagrangian PPM fallout: hydrometeor_fallout (microphysics.cpp:210-292),
+// piecewise_parabolic_interp (:516-579), calculate_edge_values (:590-637),
+// integrate_parabolic (:339-350).  One thread per column.  The reference
+// keeps its edge buffer qp_edges between columns and steps and never
+// rewrites element NZ-2 of it, so that element carries from one rainy column
+// to the next in (i,j) order; pass 1 computes each column's inputs to that
+// recurrence, pass 2 (one thread) runs it, pass 3 remaps.
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ bool ppm_column_setup(const KParams<T> &p, const KFields<T> &F, int i, int j, T *ZA, T *QA)
+{
+    const int nz = p.nz;
+    const T *var = F.P[FQR], *vel = F.vt, *ZW = p.zsw;
+    bool has = false;
+    for (int k = 1; k < nz; k++)
+        if (var[gix(p.ny, nz, i, j, k)] > T(1e-12)) { has = true; break; }
+    if (!has) return false;
+    T Ve[PPM_MAXZ];
+    for (int k = 1; k < nz; k++) Ve[k] = T(0.5) * (vel[gix(p.ny, nz, i, j, k)] + vel[gix(p.ny, nz, i, j, k - 1)]);
+    Ve[0] = Ve[1];
+    const T DeCFL0 = T(0.05), dt = p.dt;
+    for (int k = nz - 2; k >= 0; k--) {
+        T dzu = ZW[k + 1] - ZW[k];
+        T decfl = (Ve[k + 1] - Ve[k]) * dt / dzu;
+        if (decfl >= DeCFL0) Ve[k] = Ve[k + 1] - DeCFL0 * dzu / dt;
+    }
+    for (int k = 0; k < nz - 1; k++) ZA[k] = ZW[k] - dt * Ve[k];
+    ZA[nz - 1] = ZW[nz - 1];
+    for (int k = 0; k < nz - 1; k++)
+        QA[k] = p.rhou[k] * var[gix(p.ny, nz, i, j, k)] * (ZW[k + 1] - ZW[k]) / (ZA[k + 1] - ZA[k]);
+    QA[nz - 1] = T(0);
+    return true;
+}
+
+template <typename T>
+__device__ __forceinline__ T ppm_mono(const T *qin, int k)
+{
+    T dq = T(0.25) * (qin[k + 1] - qin[k - 1]);
+    T dmax = fmax(qin[k + 1], fmax(qin[k], qin[k - 1])) - qin[k];
+    T dmin = qin[k] - fmin(qin[k + 1], fmin(qin[k], qin[k - 1]));
+    return sgn(dq) * fmin(fabs(dq), fmin(dmax, dmin));
+}
+
+template <typename T>
+__global__ void k_ppm_prepare(KParams<T> p, KFields<T> F, unsigned char *has, T *topq, T *topm)
+{
+    const int nyi = p.ny - 2, nxi = p.nx - 2;
+    long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long)nxi * nyi) return;
+    const int j = 1 + (int)(t % nyi), i = 1 + (int)(t / nyi);
+    T ZA[PPM_MAXZ], QA[PPM_MAXZ];
+    bool h = ppm_column_setup(p, F, i, j, ZA, QA);
+    has[t] = h;
+    if (h) {
+        const int n = p.nz;
+        topq[t] = QA[n - 2];
+        topm[t] = ppm_mono(QA, n - 2);  // mono[n-2] uses qin[n-1], qin[n-2], qin[n-3]
+    }
+}
+
+template <typename T>
+__global__ void k_ppm_carry(long ncol, const unsigned char *has, const T *topq, const T *topm, T *carry_in,
+                            T *carry)
+{
+    if (blockIdx.x || threadIdx.x) return;
+    T c = *carry;
+    for (long t = 0; t < ncol; t++) {
+        if (!has[t]) continue;
+        carry_in[t] = c;
+        T a = topq[t], m = topm[t];
+        c = a + sgn(m) * fmin(fabs(T(2.0) * m), fabs(c - a));
+    }
+    *carry = c;
+}
+
+template <typename T>
+__device__ T integ_parab(const T *zin, const T *qin, int p_, T zl, T zh, const T *qp, const T *qn)
+{
+    T t0 = (zl - zin[p_]) / (zin[p_ + 1] - zin[p_]);
+    T t1 = (zh - zin[p_]) / (zin[p_ + 1] - zin[p_]);
+    T high = (qp[p_] + qn[p_] - T(2.0) * qin[p_]) * t1 * t1 * t1 - (qp[p_] + T(2.0) * qn[p_] - T(3.0) * qin[p_]) * t1 * t1 +
+             qn[p_] * t1;
+    T low = (qp[p_] + qn[p_] - T(2.0) * qin[p_]) * t0 * t0 * t0 - (qp[p_] + T(2.0) * qn[p_] - T(3.0) * qin[p_]) * t0 * t0 +
+            qn[p_] * t0;
+    return high - low;
+}
+
+template <typename T>
+__global__ void k_ppm_remap(KParams<T> p, KFields<T> F, const unsigned char *has, const T *carry_in)
+{
+    const int nyi = p.ny - 2, nxi = p.nx - 2;
+    long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long)nxi * nyi || !has[t]) return;
+    const int j = 1 + (int)(t % nyi), i = 1 + (int)(t / nyi);
+    const int n = p.nz;
+    T ZA[PPM_MAXZ], QA[PPM_MAXZ], QD[PPM_MAXZ], qp[PPM_MAXZ], qn[PPM_MAXZ], mono[PPM_MAXZ];
+    ppm_column_setup(p, F, i, j, ZA, QA);
+    const T *zin = ZA, *qin = QA, *zout = p.zsw;
+    for (int k = 0; k < n; k++) QD[k] = T(0);
+    int hn = 1;
+    T rainfall = T(0);
+    for (int jj = 1; jj < n - 2; jj++)
+        if (zin[jj] < 0 && zin[jj + 1] < 0) {
+            rainfall += qin[jj] * (zin[jj + 1] - zin[jj]);
+            hn = jj + 1;
+        }
+    // calculate_edge_values
+    for (int k = 1; k < n - 1; k++) mono[k] = ppm_mono(qin, k);
+    mono[0] = mono[1];
+    mono[n - 1] = mono[n - 2];
+    for (int k = 1; k < n - 1; k++) {
+        qn[k] = (qin[k - 1] * (zin[k + 1] - zin[k]) + qin[k] * (zin[k] - zin[k - 1])) / (zin[k + 1] - zin[k - 1]) -
+                (mono[k] - mono[k - 1]) / T(3.0);
+        qp[k - 1] = qn[k];
+    }
+    qp[n - 2] = carry_in[t];
+    qp[n - 1] = qin[n - 1];
+    qp[0] = qin[0];
+    qn[n - 1] = qin[n - 1];
+    qn[0] = qin[0];
+    for (int k = 0; k < n; k++) {
+        qn[k] = qin[k] - sgn(mono[k]) * fmin(fabs(T(2.0) * mono[k]), fabs(qn[k] - qin[k]));
+        qp[k] = qin[k] + sgn(mono[k]) * fmin(fabs(T(2.0) * mono[k]), fabs(qp[k] - qin[k]));
+    }
+    if (zin[hn] < 0)
+        rainfall += integ_parab(zin, qin, hn, zin[hn], T(0), qp, qn) * -zin[hn] * ((zin[hn + 1] - zin[hn]) / -zin[hn]);
+    for (int a = 0; a < n - 1; a++)
+        for (int b = 0; b < n - 1; b++) {
+            T scale = (zin[b + 1] - zin[b]) / (zout[a + 1] - zout[a]);
+            if (zout[a] < zin[b] && zout[a + 1] < zin[b + 1] && zout[a + 1] > zin[b])
+                QD[a] = QD[a] + integ_parab(zin, qin, b, zin[b], zout[a + 1], qp, qn) * scale;
+            if (zout[a] < zin[b + 1] && zout[a + 1] > zin[b + 1] && zout[a] > zin[b])
+                QD[a] = QD[a] + integ_parab(zin, qin, b, zout[a], zin[b + 1], qp, qn) * scale;
+            if (zout[a] >= zin[b] && zout[a + 1] <= zin[b + 1])
+                QD[a] = QD[a] + integ_parab(zin, qin, b, zout[a], zout[a + 1], qp, qn) * scale;
+            if (zout[a] < zin[b] && zout[a + 1] > zin[b + 1])
+                QD[a] = QD[a] + integ_parab(zin, qin, b, zin[b], zin[b + 1], qp, qn) * scale;
+        }
+    F.accrain[(long)i * p.ny + j] += (double)rainfall;
+    for (int k = 0; k < n; k++) F.P[FQR][gix(p.ny, n, i, j, k)] = QD[k] * p.one_d_rhou[k];
+}
+
+template <typename T>
+__global__ void k_fill(T *a, long n, T v)
+{
+    long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) a[t] = v;
+}
+
+template <typename T>
+__global__ void k_check_finite(const T *a, long n, int *flag)
+{
+    long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    for (; t < n; t += (long)gridDim.x * blockDim.x)
+        if (!isfinite(a[t])) { atomicExch(flag, 1); return; }
+}
+
+template <typename T>
+__global__ void k_convert_in(T *dst, const double *src, long n)
+{
+    long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) dst[t] = (T)src[t];
+}
+template <typename T>
+__global__ void k_convert_out(double *dst, const T *src, long n)
+{
+    long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) dst[t] = (double)src[t];
+}
+
+}  // namespace ga
