@@ -1,0 +1,420 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 anelastic dynamical core.
+
+Metric: gridpoint-steps/s = NX*NY*NZ*steps / seconds of stepping, for the
+forward RK3 step (s_integrate_rk3, driver_serial.cpp:178-286) of the Kessler
+thunderstorm workload, 128x128x48, dx=dy=1 km, dz=400 m, dt=4 s (seeded
+synthetic state: analytic sounding + warm bubble + noise), FP32 storage and
+arithmetic with FP64 islands; FP64 beside it; each result's error against the
+FP64 path (itself checked against the CPU oracle in tests/) stated.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Timing: K model steps, each bracketed by CUDA events recorded on the
+library's stream, with a 256 MiB L2 flush (write) between steps outside the
+events; a barrier + synchronize on both sides of the loop; the max over ranks.
+Under torchrun (N>1) every rank integrates its own domain (replicas: the
+single-domain step does not shard) and `value` is the sum over ranks.
+
+--impl reference times the reference's CPU step: the oracle restatement,
+which matches the reference's own serial build bit for bit (tests/golden), on
+the host cores of this machine, over a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "gridpoint-steps/s (fwd, fwd+adjoint) FP32 vs FP64 at stated err; %HBM peak"
+UNIT = "gridpoint-steps/s"
+WORKLOAD_DESC = "Kessler thunderstorm 128x128x48, dx=dy=1 km, dz=400 m, dt=4 s, 600-step run"
+DATA = "synthetic: seeded thunderstorm sounding (theta 300->343 K, RH 0.95->0.25, u 0->15 m/s) + 3 K warm bubble + U(+-0.05 K) noise"
+L2_FLUSH_BYTES = 256 << 20
+
+# algorithmic field passes (one read or write of an N-point field) per launch
+# of each kernel group; spectral passes count complex values as two fields
+PASSES_DRY = {"advect": 16, "div_fft_y": 5, "fft_x": 4, "thomas": 4, "ifft_y_pi": 3, "post": 9,
+              "kessler": 0}
+PASSES_MOIST = {"advect": 27, "div_fft_y": 5, "fft_x": 4, "thomas": 4, "ifft_y_pi": 3, "post": 16,
+                "kessler": 12}
+# compulsory bytes per gridpoint-step of an ideally fused step (FP32 moist)
+STEP_BYTES_FP32_MOIST = 540.0
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as fp:
+            d = json.load(fp)
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during a region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.fp = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.fp, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.fp.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": float(max(smax)) if smax else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        import torch
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    return world, rank, local, dist
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def allreduce_max(dist, x: float, device) -> float:
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------------------
+def time_steps(model, torch, steps, flush, profile=False):
+    """Per-step CUDA-event times (ms) on the library's stream, with an L2
+    flush between steps outside the events."""
+    ext = torch.cuda.ExternalStream(model.stream_handle())
+    evs = []
+    for _ in range(steps):
+        with torch.cuda.stream(ext):
+            flush.zero_()
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(ext)
+        model.step_async(1)
+        b.record(ext)
+        evs.append((a, b))
+    model.synchronize()
+    return [a.elapsed_time(b) for a, b in evs]
+
+
+def profile_groups(model, torch, steps, flush):
+    from model_gb300 import anelastic
+    import ctypes as C
+    L = anelastic.load_library()
+    L.ga_profile_enable.argtypes = [C.c_void_p, C.c_int]
+    L.ga_profile_get.argtypes = [C.c_void_p, C.c_int, C.c_char_p, C.c_size_t, C.POINTER(C.c_double),
+                                 C.POINTER(C.c_longlong)]
+    L.ga_profile_enable(model.h, 1)
+    time_steps(model, torch, steps, flush)
+    out = {}
+    for i in range(L.ga_profile_count(model.h)):
+        name = C.create_string_buffer(32)
+        ms, n = C.c_double(), C.c_longlong()
+        L.ga_profile_get(model.h, i, name, 32, C.byref(ms), C.byref(n))
+        if n.value:
+            out[name.value.decode()] = {"ms": ms.value, "launches": n.value}
+    L.ga_profile_enable(model.h, 0)
+    return out
+
+
+def roofline(groups, wl, prec_bytes, peak_gbs, peak_kind):
+    passes = PASSES_MOIST if wl.microphysics_option else PASSES_DRY
+    dom = max((g for g in groups if g in passes and passes[g] > 0), key=lambda g: groups[g]["ms"])
+    g = groups[dom]
+    per_launch_ms = g["ms"] / g["launches"]
+    spec_pts = wl.nx * wl.ny * (wl.nz - 2)
+    pts = spec_pts if dom in ("div_fft_y", "fft_x", "thomas", "ifft_y_pi") else wl.points
+    nbytes = passes[dom] * pts * prec_bytes
+    achieved = nbytes / (per_launch_ms * 1e-3) / 1e9
+    table = {k: {"ms_per_launch": round(v["ms"] / v["launches"], 5), "share": round(v["ms"] / sum(
+        x["ms"] for x in groups.values()), 4)} for k, v in groups.items()}
+    return {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak_gbs, "unit": "GB/s",
+            "frac": round(achieved / peak_gbs, 4), "peak_source": peak_kind,
+            "algorithmic_bytes_per_launch": int(nbytes), "ms_per_launch": round(per_launch_ms, 5),
+            "traffic": None, "groups": table}
+
+
+def e2e_jobs(model_cls, wl, prec, torch, jobs, job_steps, device):
+    """Whole runs through the C ABI with pinned host buffers: upload the
+    initial state, integrate job_steps, download the prognostic fields."""
+    from model_gb300 import abi
+    m = model_cls(wl, prec, device=device, init_state=False)
+    n = wl.points
+    nprog = 7 if wl.microphysics_option else 4
+
+    def pinned(arr):
+        t = torch.empty(arr.size, dtype=torch.float64, pin_memory=True)
+        t.numpy()[:] = np.asarray(arr, dtype=np.float64).ravel()
+        return t
+
+    host_in = []
+    for b, name in enumerate(abi.BAR_NAMES):
+        host_in.append((abi.GA_UBAR + b, 0, pinned(wl.fields[name])))
+    zeros = pinned(np.zeros(n))
+    for f in range(nprog):
+        a = pinned(wl.fields[abi.PROG_NAMES[f]])
+        host_in += [(f, abi.GA_SLOT_CUR, a), (f, abi.GA_SLOT_M, a), (f, abi.GA_SLOT_P, zeros)]
+    host_out = [torch.empty(n, dtype=torch.float64, pin_memory=True) for _ in range(nprog + 1)]
+    import ctypes as C
+    L = m.L
+    dp = C.POINTER(C.c_double)
+
+    def one_job():
+        for f, slot, t in host_in:
+            rc = L.ga_set_field(m.h, f, slot, C.cast(t.data_ptr(), dp), n)
+            assert rc == 0
+        rc = L.ga_step(m.h, job_steps)
+        assert rc == 0, rc
+        for f in range(nprog):
+            assert L.ga_get_field(m.h, f, 0, C.cast(host_out[f].data_ptr(), dp), n) == 0
+        assert L.ga_get_field(m.h, abi.GA_PI, 0, C.cast(host_out[nprog].data_ptr(), dp), n) == 0
+
+    one_job()  # warm-up
+    t0 = time.perf_counter()
+    for _ in range(jobs):
+        one_job()
+    el = time.perf_counter() - t0
+    h2d = len(host_in) * n * 8
+    d2h = (nprog + 1) * n * 8
+    m.close()
+    return {"value": round(n * job_steps * jobs / el, 1), "unit": UNIT,
+            "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+            "step": f"one {job_steps}-step run: upload initial state, integrate, download fields",
+            "jobs": jobs, "seconds_per_run": round(el / jobs, 4)}
+
+
+def cpu_baseline(wl, steps):
+    """The reference's CPU step (oracle restatement, 1 core) on a bounded
+    sample of the same workload."""
+    from oracle import oracle as O
+    O.build()
+    o = O.Oracle(wl)
+    t0 = time.perf_counter()
+    rc = o.step(steps)
+    el = time.perf_counter() - t0
+    assert rc == 0
+    return {"value": round(wl.points * steps / el, 1), "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"{steps} steps of the {wl.nx}x{wl.ny}x{wl.nz} workload from its initial state "
+                      f"({el:.1f} s on 1 host core)",
+            "cpu": cpu_model()}
+
+
+def cpu_model() -> str:
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name"):
+                return line.split(":", 1)[1].strip() + f", nproc={os.cpu_count()}"
+    except Exception:
+        pass
+    return f"nproc={os.cpu_count()}"
+
+
+def accuracy(model_cls, wl, torch, device, steps):
+    """FP32 against FP64 after `steps` steps: relative L2 per field."""
+    from model_gb300 import abi
+    out = {}
+    m64 = model_cls(wl, abi.GA_PREC_F64, device=device)
+    m32 = model_cls(wl, abi.GA_PREC_F32, device=device)
+    t0 = time.perf_counter()
+    m64.step(steps)
+    t64 = time.perf_counter() - t0
+    m32.step(steps)
+    nprog = 7 if wl.microphysics_option else 4
+    for f in range(nprog):
+        a, b = m32.get(f), m64.get(f)
+        nb = np.linalg.norm(b)
+        out[abi.PROG_NAMES[f]] = float(np.linalg.norm(a - b) / nb) if nb > 0 else float(np.linalg.norm(a))
+    m64.close()
+    m32.close()
+    return {"steps": steps, "rel_l2_fp32_vs_fp64": {k: float(f"{v:.3e}") for k, v in out.items()},
+            "max": float(f"{max(out.values()):.3e}"), "fp64_wall_s": round(t64, 2)}
+
+
+# ---------------------------------------------------------------------------
+def run_ours(args):
+    import torch
+    from model_gb300 import abi, anelastic, configs
+
+    world, rank, local, dist = dist_setup()
+    device = local
+    torch.cuda.set_device(device)
+    wl = configs.thunderstorm()
+    prec = abi.GA_PREC_F32 if args.precision == "f32" else abi.GA_PREC_F64
+    model = anelastic.Model(wl, prec, device=device)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{device}")
+    # warm-up
+    for _ in range(args.warmup):
+        model.step(1)
+    torch.cuda.synchronize()
+    barrier(dist)
+    sampler = ClockSampler(device)
+    sampler.start()
+    l0 = model.launch_count()
+    torch.cuda.synchronize()
+    barrier(dist)
+    per = time_steps(model, torch, args.steps, flush)
+    torch.cuda.synchronize()
+    barrier(dist)
+    clocks = sampler.stop()
+    launches = model.launch_count() - l0
+    ms_total = allreduce_max(dist, float(sum(per)), f"cuda:{device}")
+    rc = model.check_finite()
+    if rc != 0:
+        raise RuntimeError("non-finite state after the timed steps")
+    value = world * wl.points * args.steps / (ms_total * 1e-3)
+
+    if rank != 0:
+        if dist is not None:
+            dist.barrier()
+            dist.destroy_process_group()
+        return
+    prec_bytes = 4 if prec == abi.GA_PREC_F32 else 8
+    peak, peak_kind = load_peaks()
+    groups = profile_groups(model, torch, min(args.steps, 10), flush)
+    roof = roofline(groups, wl, prec_bytes, peak, peak_kind)
+    line = {"metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms_total / args.steps, 5), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": args.precision, "data": DATA,
+            "config": {"workload": WORKLOAD_DESC, "grid": [wl.nx, wl.ny, wl.nz], "precision": args.precision,
+                       "physics": "Kessler, rain_fallout 1, 5-point sponges, Rayleigh from NZ-5",
+                       "l2": "256 MiB written between timed steps, outside the events",
+                       "parallelism": f"replicas x{world}" if world > 1 else "single domain"},
+            "roofline": roof, "gpu_launches": int(launches), "clocks": clocks}
+    line["hbm_fraction_step"] = round(value / world * STEP_BYTES_FP32_MOIST / 1e9 / peak, 4) \
+        if prec == abi.GA_PREC_F32 else None
+    if not args.no_fp64 and prec == abi.GA_PREC_F32:
+        m64 = anelastic.Model(wl, abi.GA_PREC_F64, device=device)
+        for _ in range(2):
+            m64.step(1)
+        per64 = time_steps(m64, torch, args.fp64_steps, flush)
+        v64 = wl.points * args.fp64_steps / (sum(per64) * 1e-3)
+        line["fp64"] = {"value": round(v64, 1), "unit": UNIT, "steps": args.fp64_steps,
+                        "ms_per_step": round(sum(per64) / args.fp64_steps, 4),
+                        "fp32_over_fp64": round(value / world / v64, 2)}
+        m64.close()
+    model.close()
+    if args.accuracy_steps > 0:
+        line["accuracy"] = accuracy(anelastic.Model, wl, torch, device, args.accuracy_steps)
+    if args.e2e_jobs > 0:
+        line["e2e"] = e2e_jobs(anelastic.Model, wl, prec, torch, args.e2e_jobs, args.e2e_steps, device)
+    if not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(wl, args.cpu_steps)
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from model_gb300 import configs
+    wl = configs.thunderstorm()
+    steps = max(1, min(args.steps, args.cpu_steps))
+    for _ in range(max(0, min(args.warmup, 1))):
+        cpu_baseline(configs.thunderstorm(nx=32, ny=32), 1)
+    base = cpu_baseline(wl, steps)
+    line = {"metric": METRIC, "value": base["value"], "unit": UNIT, "n_gpus": 0, "steps": steps,
+            "warmup": args.warmup, "ms_per_step": round(wl.points / base["value"] * 1e3, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": DATA,
+            "impl": "reference",
+            "config": {"workload": WORKLOAD_DESC, "grid": [wl.nx, wl.ny, wl.nz], "precision": "fp64",
+                       "implementation": "CPU restatement of the reference's serial step, bit-identical to "
+                                         "the reference build on the golden fixtures; single-threaded like "
+                                         "the reference"},
+            "cpu_baseline": base,
+            "e2e": {"value": base["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="f32", choices=["f32", "f64"])
+    ap.add_argument("--fp64-steps", type=int, default=10)
+    ap.add_argument("--accuracy-steps", type=int, default=600)
+    ap.add_argument("--e2e-jobs", type=int, default=2)
+    ap.add_argument("--e2e-steps", type=int, default=600)
+    ap.add_argument("--cpu-steps", type=int, default=5)
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        log("warning: fewer than 3 warm-up steps")
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        from model_gb300 import build
+        build.build()
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -216,6 +216,15 @@ GA_API void *ga_stream(ga_ctx *ctx);
  * callers that keep state resident on the GPU. */
 GA_API void *ga_field_device_ptr(ga_ctx *ctx, int field, int slot);
 
+/* Optional timing of the kernel groups with CUDA events recorded on the
+ * context's stream (advect, edges, div_fft_y, fft_x, thomas, ifft_y_pi,
+ * post, kessler, ppm, copy).  Enabling resets the totals.  The reference
+ * only prints the CPU time of whole steps (driver_serial.cpp:354-364). */
+GA_API int ga_profile_enable(ga_ctx *ctx, int on);
+GA_API int ga_profile_count(ga_ctx *ctx);
+GA_API int ga_profile_get(ga_ctx *ctx, int idx, char *name, size_t cap, double *total_ms,
+                          long long *launches);
+
 #ifdef __cplusplus
 }
 #endif

@@ -21,7 +21,10 @@ CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libga_anelastic.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# -ffp-contract=off for host code too: the host builds the sponge, Rayleigh and
+# spectral tables, and GCC on Arm would otherwise fuse their multiply-adds
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
+          "-Xcompiler", "-ffp-contract=off",
           "-I" + os.path.join(ROOT, "include")]
 UNITS = {
     "ga_f64": ["--fmad=false"],

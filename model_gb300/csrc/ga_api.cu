@@ -223,4 +223,31 @@ void *ga_field_device_ptr(ga_ctx *ctx, int field, int slot)
     return ctx->e->field_ptr(field, slot);
 }
 
+int ga_profile_enable(ga_ctx *ctx, int on)
+{
+    if (!ctx) return fail(GA_ERR_ARG, "ga_profile_enable: null context");
+    ctx->e->prof_reset();
+    ctx->e->prof = on != 0;
+    return GA_OK;
+}
+
+int ga_profile_count(ga_ctx *ctx)
+{
+    (void)ctx;
+    return ga::PC_COUNT;
+}
+
+int ga_profile_get(ga_ctx *ctx, int idx, char *name, size_t cap, double *total_ms, long long *launches)
+{
+    if (!ctx || idx < 0 || idx >= ga::PC_COUNT) return fail(GA_ERR_ARG, "ga_profile_get: bad arguments");
+    ctx->e->prof_collect();
+    if (name && cap) {
+        std::strncpy(name, ga::kProfNames[idx], cap - 1);
+        name[cap - 1] = 0;
+    }
+    if (total_ms) *total_ms = ctx->e->prof_ms[idx];
+    if (launches) *launches = ctx->e->prof_n[idx];
+    return GA_OK;
+}
+
 }  /* extern "C" */

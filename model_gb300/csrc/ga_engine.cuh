@@ -342,6 +342,7 @@ class Engine : public EngineBase {
     {
         const long tot = (long)(NX - 6) * (NY - 6) * (NZ - 2);
         const double sdtg = step * cfg.dt * 9.8 * 0.5;  // step*dt*grav*0.5, advection.cpp:330
+        ProfScope ps(this, PC_ADVECT, 1);
         k_advect<T><<<cdiv(tot, 128), 128, 0, stream>>>(kp, fields(), (T)step, (T)sdtg, what);
         launches++;
     }
@@ -349,6 +350,7 @@ class Engine : public EngineBase {
     void edges_uvw()
     {
         KFields<T> F = fields();
+        ProfScope ps(this, PC_EDGES, 1);
         if (!kp.periodic) {
             const long tot = 2L * (NX + NY - 2) * (NZ - 2);
             k_mirror_edges<T><<<cdiv(tot, 256), 256, 0, stream>>>(kp, F.P[FU], F.P[FV], F.P[FW]);
@@ -364,12 +366,27 @@ class Engine : public EngineBase {
         KFields<T> F = fields();
         const T sdt = (T)(step * cfg.dt);
         const int nkt_y = cdiv(NZ - 2, KTy), nkt_x = cdiv(NZ - 2, KTx);
-        k_div_fft_y<T><<<dim3(kp.ni, nkt_y), 256, smem_y, stream>>>(kp, F, spec, plan_j, tw_j, sdt, KTy);
-        k_fft_x<T><<<dim3(kp.nj, nkt_x), 256, smem_x, stream>>>(kp, spec, plan_i, tw_i, 0, KTx);
+        {
+            ProfScope ps(this, PC_DIV_FFT_Y, 1);
+            k_div_fft_y<T><<<dim3(kp.ni, nkt_y), 256, smem_y, stream>>>(kp, F, spec, plan_j, tw_j, sdt, KTy);
+        }
+        {
+            ProfScope ps(this, PC_FFT_X, 1);
+            k_fft_x<T><<<dim3(kp.nj, nkt_x), 256, smem_x, stream>>>(kp, spec, plan_i, tw_i, 0, KTx);
+        }
         const long ncol = (long)kp.ni * kp.nj;
-        k_thomas<T><<<cdiv(ncol, TC), TC, smem_th, stream>>>(kp, spec, TC);
-        k_fft_x<T><<<dim3(kp.nj, nkt_x), 256, smem_x, stream>>>(kp, spec, plan_i, tw_i, 1, KTx);
-        k_ifft_y_pi<T><<<dim3(kp.ni, nkt_y), 256, smem_y, stream>>>(kp, F, spec, plan_j, tw_j, KTy);
+        {
+            ProfScope ps(this, PC_THOMAS, 1);
+            k_thomas<T><<<cdiv(ncol, TC), TC, smem_th, stream>>>(kp, spec, TC);
+        }
+        {
+            ProfScope ps(this, PC_FFT_X, 1);
+            k_fft_x<T><<<dim3(kp.nj, nkt_x), 256, smem_x, stream>>>(kp, spec, plan_i, tw_i, 1, KTx);
+        }
+        {
+            ProfScope ps(this, PC_IFFT_Y_PI, 1);
+            k_ifft_y_pi<T><<<dim3(kp.ni, nkt_y), 256, smem_y, stream>>>(kp, F, spec, plan_j, tw_j, KTy);
+        }
         launches += 5;
     }
 
@@ -387,6 +404,7 @@ class Engine : public EngineBase {
         for (int f = 0; f < nfields && f < 7; f++) fl[f] = f < nprog ? flags[f] : 0;
         int4 a = make_int4(fl[0], fl[1], fl[2], fl[3]), b = make_int4(fl[4], fl[5], fl[6], fl[7]);
         const int wpb = 8;
+        ProfScope ps(this, PC_POST, (pcopy && kp.periodic) ? 2 : 1);
         if (pcopy && kp.periodic) {
             k_post<T><<<cdiv(6L * NY, wpb), 32 * wpb, 0, stream>>>(kp, F, 7, a, b, (T)step, COLS_TARGETS);
             k_post<T><<<cdiv((long)NX * NY, wpb), 32 * wpb, 0, stream>>>(kp, F, 7, a, b, (T)step, COLS_NONTARGETS);
@@ -402,9 +420,13 @@ class Engine : public EngineBase {
         if (!kp.moist) return;
         KFields<T> F = fields();
         const long tot = (long)(NX - 2) * (NY - 2) * (NZ - 2);
+        {
+        ProfScope ps(this, PC_KESSLER, 1);
         k_kessler<T><<<cdiv(tot, 128), 128, 0, stream>>>(kp, F, kp.rf != 2, d_err);
         launches++;
+        }
         if (kp.rf == 2) {
+            ProfScope ps(this, PC_PPM, 5);
             const long tv = (long)(NX - 2) * (NY - 2) * NZ;
             k_fall_speed<T><<<cdiv(tv, 256), 256, 0, stream>>>(kp, F);
             const long ncol = (long)(NX - 2) * (NY - 2);
@@ -425,6 +447,7 @@ class Engine : public EngineBase {
 
     void copy_m_from_p(int f0, int f1)
     {
+        ProfScope ps(this, PC_COPY, 0);
         for (int f = f0; f < f1 && f < nprog; f++)
             cudaMemcpyAsync(buf[f][mi[f]], buf[f][pi_[f]], N * sizeof(T), cudaMemcpyDeviceToDevice, stream);
     }

@@ -3,13 +3,26 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <string>
+#include <vector>
 
 #include "../../include/ga_anelastic.h"
 
 namespace ga {
 
+// kernel groups timed by the optional event profiler
+enum ProfCat { PC_ADVECT = 0, PC_EDGES, PC_DIV_FFT_Y, PC_FFT_X, PC_THOMAS, PC_IFFT_Y_PI, PC_POST, PC_KESSLER,
+               PC_PPM, PC_COPY, PC_COUNT };
+static const char *const kProfNames[PC_COUNT] = {"advect", "edges", "div_fft_y", "fft_x", "thomas",
+                                                 "ifft_y_pi", "post", "kessler", "ppm", "copy"};
+
 struct EngineBase {
-    virtual ~EngineBase() {}
+    virtual ~EngineBase()
+    {
+        for (auto &r : prof_pending) {
+            cudaEventDestroy(r.a);
+            cudaEventDestroy(r.b);
+        }
+    }
     virtual int set_field(int field, int slot, const double *host, size_t n) = 0;
     virtual int get_field(int field, int slot, double *host, size_t n) = 0;
     virtual int op(int op, double step) = 0;
@@ -21,6 +34,58 @@ struct EngineBase {
     long long bigcounter = 0;
     double mtime = 0.0;
     int device = 0;
+
+    // ---- optional per-group timing with CUDA events on the engine stream
+    struct ProfRec {
+        int cat;
+        int nlaunch;
+        cudaEvent_t a, b;
+    };
+    bool prof = false;
+    std::vector<ProfRec> prof_pending;
+    double prof_ms[PC_COUNT] = {};
+    long long prof_n[PC_COUNT] = {};
+    int prof_begin(int cat)
+    {
+        if (!prof) return -1;
+        ProfRec r{cat, 0, nullptr, nullptr};
+        cudaEventCreate(&r.a);
+        cudaEventCreate(&r.b);
+        cudaEventRecord(r.a, stream);
+        prof_pending.push_back(r);
+        return (int)prof_pending.size() - 1;
+    }
+    void prof_end(int h, int nlaunch)
+    {
+        if (h < 0) return;
+        prof_pending[h].nlaunch = nlaunch;
+        cudaEventRecord(prof_pending[h].b, stream);
+    }
+    void prof_collect()
+    {
+        cudaStreamSynchronize(stream);
+        for (auto &r : prof_pending) {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, r.a, r.b);
+            prof_ms[r.cat] += ms;
+            prof_n[r.cat] += r.nlaunch;
+            cudaEventDestroy(r.a);
+            cudaEventDestroy(r.b);
+        }
+        prof_pending.clear();
+    }
+    void prof_reset()
+    {
+        prof_collect();
+        for (int c = 0; c < PC_COUNT; c++) { prof_ms[c] = 0; prof_n[c] = 0; }
+    }
+};
+
+struct ProfScope {
+    EngineBase *e;
+    int h, n;
+    ProfScope(EngineBase *eng, int cat, int nl) : e(eng), h(eng->prof_begin(cat)), n(nl) {}
+    ~ProfScope() { e->prof_end(h, n); }
 };
 
 // set by the engines, read by ga_last_error (thread local)

@@ -67,3 +67,65 @@ def test_single_operator_matches_reference(name, op):
         else:
             e = fx.rel_l2(got, d[k])
             assert e <= 1e-12, f"{op}:{key} rel L2 {e:.3e}"
+
+
+def _oracle_compare(wl, nsteps, tol):
+    from oracle import oracle as O
+    cols = anelastic.build_columns(wl)
+    m = anelastic.Model(wl, abi.GA_PREC_F64, columns=cols)
+    m.step(nsteps)
+    o = O.Oracle(wl, cols)
+    assert o.step(nsteps) == 0
+    worst = {}
+    nprog = 7 if wl.microphysics_option else 4
+    for f in list(range(nprog)) + [abi.GA_PI]:
+        worst[f] = fx.rel_l2(m.get(f), o.get(f))
+    print(wl.name, nsteps, {k: f"{v:.2e}" for k, v in worst.items()})
+    for f, e in worst.items():
+        assert e <= tol, f"field {f}: rel L2 {e:.3e}"
+    return worst
+
+
+def test_dry_bubble_full_config_fp64_vs_oracle():
+    """Dry warm bubble, 64x64x40, 100 steps: every prognostic field within
+    1e-10 relative L2 of the oracle."""
+    from model_gb300 import configs
+    _oracle_compare(configs.dry_bubble(), 100, 1e-10)
+
+
+def test_thunderstorm_fp64_vs_oracle_short():
+    """Kessler thunderstorm at full size (128x128x48), 8 steps (the oracle
+    needs about 2 s per step)."""
+    from model_gb300 import configs
+    _oracle_compare(configs.thunderstorm(), 8, 1e-10)
+
+
+def test_periodic_rf2_fp64_vs_oracle():
+    from model_gb300 import configs
+    _oracle_compare(configs.moist_blob(nx=30, ny=24, nz=16, periodic=1, rain_fallout=2), 12, 1e-10)
+
+
+def test_fp32_error_against_fp64():
+    """FP32 path: relative L2 error against FP64 after 60 thunderstorm steps."""
+    from model_gb300 import configs
+    wl = configs.thunderstorm()
+    a = anelastic.Model(wl, abi.GA_PREC_F32)
+    b = anelastic.Model(wl, abi.GA_PREC_F64)
+    a.step(60)
+    b.step(60)
+    errs = {abi.PROG_NAMES[f]: fx.rel_l2(a.get(f), b.get(f)) for f in range(7)}
+    print("fp32 vs fp64 after 60 steps", {k: f"{v:.2e}" for k, v in errs.items()})
+    for k in ("u", "v", "w", "th", "qv"):
+        assert errs[k] <= 1e-4, (k, errs[k])
+
+
+def test_step_is_deterministic():
+    from model_gb300 import configs
+    wl = configs.moist_blob(nx=40, ny=36, nz=20, nsteps=5)
+    outs = []
+    for _ in range(2):
+        m = anelastic.Model(wl, abi.GA_PREC_F32)
+        m.step(5)
+        outs.append([m.get(f) for f in range(7)] + [m.get(abi.GA_ACCRAIN)])
+    for x, y in zip(*outs):
+        np.testing.assert_array_equal(x, y)
