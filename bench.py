@@ -301,7 +301,7 @@ def run_ours(args):
     world, rank, local, dist = dist_setup()
     device = local
     torch.cuda.set_device(device)
-    wl = configs.thunderstorm()
+    wl = configs.make(args.workload)
     prec = abi.GA_PREC_F32 if args.precision == "f32" else abi.GA_PREC_F64
     model = anelastic.Model(wl, prec, device=device)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{device}")
@@ -338,7 +338,8 @@ def run_ours(args):
     line = {"metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms_total / args.steps, 5), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": args.precision, "data": DATA,
-            "config": {"workload": WORKLOAD_DESC, "grid": [wl.nx, wl.ny, wl.nz], "precision": args.precision,
+            "config": {"workload": WORKLOAD_DESC if args.workload == "thunderstorm" else args.workload,
+                       "grid": [wl.nx, wl.ny, wl.nz], "precision": args.precision,
                        "physics": "Kessler, rain_fallout 1, 5-point sponges, Rayleigh from NZ-5",
                        "l2": "256 MiB written between timed steps, outside the events",
                        "parallelism": f"replicas x{world}" if world > 1 else "single domain"},
@@ -398,6 +399,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="f32", choices=["f32", "f64"])
+    ap.add_argument("--workload", default="thunderstorm",
+                    choices=["thunderstorm", "dry_bubble", "squall_line", "moist_blob"])
     ap.add_argument("--fp64-steps", type=int, default=10)
     ap.add_argument("--accuracy-steps", type=int, default=600)
     ap.add_argument("--e2e-jobs", type=int, default=2)

@@ -26,6 +26,11 @@ static inline FftPlan make_fft_plan(int n)
         if (m % f == 0) { P.fac[P.nfac++] = f; m /= f; }
         else f = (f == 2) ? 3 : f + 2;
     }
+    int ns = 1;
+    for (int f = 0; f < P.nfac; f++) {
+        P.nslog[f] = (ns & (ns - 1)) == 0 ? __builtin_ctz(ns) : -1;
+        ns *= P.fac[f];
+    }
     return P;
 }
 
@@ -51,8 +56,12 @@ class Engine : public EngineBase {
     unsigned char *ppm_has = nullptr;
     T *ppm_topq = nullptr, *ppm_topm = nullptr, *ppm_cin = nullptr, *ppm_carry = nullptr;
     double *staging = nullptr;
-    int KTy = 1, KTx = 1, TC = 64;
-    size_t smem_y = 0, smem_x = 0, smem_th = 0;
+    int KTy = 1, KTx = 1, lgKTy = 0, lgKTx = 0, TC = 64;
+    int Lsx = 0, lgLsx = -1;  // lines of the fused spectral-x kernel (0: not used)
+    size_t smem_y = 0, smem_x = 0, smem_th = 0, smem_sx = 0;
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    long long graph_launches[2] = {0, 0};
+    bool use_graphs = true;
     int status = GA_OK;
 
     template <typename X>
@@ -191,13 +200,31 @@ class Engine : public EngineBase {
         };
         tw_i = twiddles(ni);
         tw_j = twiddles(nj);
-        const long budget = 32 * 1024;
-        KTy = (int)std::max(1L, std::min((long)NZ - 2, budget / (long)(2 * nj * sizeof(T2))));
-        KTx = (int)std::max(1L, std::min((long)NZ - 2, budget / (long)(2 * ni * sizeof(T2))));
+        // power-of-two level tiles for the y and x transforms (~32 KiB per buffer)
+        auto pow2_tile = [&](int n, int *lg) {
+            const long budget = 32 * 1024;
+            long want = std::max(1L, budget / (long)(2 * n * sizeof(T2)));
+            int kt = 1, l = 0;
+            while ((kt << 1) <= want && (kt << 1) <= 2 * (NZ - 2)) { kt <<= 1; l++; }
+            while (kt > 1 && (kt >> 1) >= NZ - 2) { kt >>= 1; l--; }
+            *lg = l;
+            return kt;
+        };
+        KTy = pow2_tile(nj, &lgKTy);
+        KTx = pow2_tile(ni, &lgKTx);
         smem_y = 2 * (size_t)nj * KTy * sizeof(T2);
         smem_x = 2 * (size_t)ni * KTx * sizeof(T2);
         smem_th = (size_t)TC * NZ * (sizeof(T2) + sizeof(T));
         const int optin = 200 * 1024;
+        {   // fused x transform + Thomas when all levels of a wavenumber fit
+            const int nl = NZ - 2;
+            int l2 = 1, lg = 0;
+            while (l2 < nl) { l2 <<= 1; lg++; }
+            if (2 * (size_t)ni * l2 * sizeof(T2) <= (size_t)optin) { Lsx = l2; lgLsx = lg; }
+            else if (2 * (size_t)ni * nl * sizeof(T2) <= (size_t)optin) { Lsx = nl; lgLsx = -1; }
+            smem_sx = 2 * (size_t)ni * Lsx * sizeof(T2);
+        }
+        cudaFuncSetAttribute(k_spectral_x<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
         cudaFuncSetAttribute(k_div_fft_y<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
         cudaFuncSetAttribute(k_ifft_y_pi<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
         cudaFuncSetAttribute(k_fft_x<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
@@ -218,6 +245,8 @@ class Engine : public EngineBase {
     {
         cudaSetDevice(device);
         if (stream) cudaStreamSynchronize(stream);
+        for (auto &g : graph)
+            if (g) cudaGraphExecDestroy(g);
         for (void *p : allocs) cudaFree(p);
         if (staging) cudaFree(staging);
         if (stream) cudaStreamDestroy(stream);
@@ -368,26 +397,33 @@ class Engine : public EngineBase {
         const int nkt_y = cdiv(NZ - 2, KTy), nkt_x = cdiv(NZ - 2, KTx);
         {
             ProfScope ps(this, PC_DIV_FFT_Y, 1);
-            k_div_fft_y<T><<<dim3(kp.ni, nkt_y), 256, smem_y, stream>>>(kp, F, spec, plan_j, tw_j, sdt, KTy);
+            k_div_fft_y<T><<<dim3(kp.ni, nkt_y), 256, smem_y, stream>>>(kp, F, spec, plan_j, tw_j, sdt, lgKTy);
         }
-        {
-            ProfScope ps(this, PC_FFT_X, 1);
-            k_fft_x<T><<<dim3(kp.nj, nkt_x), 256, smem_x, stream>>>(kp, spec, plan_i, tw_i, 0, KTx);
-        }
-        const long ncol = (long)kp.ni * kp.nj;
-        {
+        if (Lsx > 0) {
             ProfScope ps(this, PC_THOMAS, 1);
-            k_thomas<T><<<cdiv(ncol, TC), TC, smem_th, stream>>>(kp, spec, TC);
-        }
-        {
-            ProfScope ps(this, PC_FFT_X, 1);
-            k_fft_x<T><<<dim3(kp.nj, nkt_x), 256, smem_x, stream>>>(kp, spec, plan_i, tw_i, 1, KTx);
+            k_spectral_x<T><<<kp.nj, 256, smem_sx, stream>>>(kp, spec, plan_i, tw_i, Lsx, lgLsx);
+            launches += 1;
+        } else {
+            {
+                ProfScope ps(this, PC_FFT_X, 1);
+                k_fft_x<T><<<dim3(kp.nj, nkt_x), 256, smem_x, stream>>>(kp, spec, plan_i, tw_i, 0, lgKTx);
+            }
+            const long ncol = (long)kp.ni * kp.nj;
+            {
+                ProfScope ps(this, PC_THOMAS, 1);
+                k_thomas<T><<<cdiv(ncol, TC), TC, smem_th, stream>>>(kp, spec, TC);
+            }
+            {
+                ProfScope ps(this, PC_FFT_X, 1);
+                k_fft_x<T><<<dim3(kp.nj, nkt_x), 256, smem_x, stream>>>(kp, spec, plan_i, tw_i, 1, lgKTx);
+            }
+            launches += 3;
         }
         {
             ProfScope ps(this, PC_IFFT_Y_PI, 1);
-            k_ifft_y_pi<T><<<dim3(kp.ni, nkt_y), 256, smem_y, stream>>>(kp, F, spec, plan_j, tw_j, KTy);
+            k_ifft_y_pi<T><<<dim3(kp.ni, nkt_y), 256, smem_y, stream>>>(kp, F, spec, plan_j, tw_j, lgKTy);
         }
-        launches += 5;
+        launches += 2;
     }
 
     void solve_pressure(double step)
@@ -556,15 +592,55 @@ class Engine : public EngineBase {
         bigcounter++;
     }
 
+    // CUDA graph of two steps: the rotation of the three buffers has period
+    // two steps, so one graph per starting parity replays any even count.
+    int capture_pair(int parity)
+    {
+        const long long bc = bigcounter, l0 = launches;
+        const double mt = mtime;
+        cudaGraph_t g = nullptr;
+        if (cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return GA_ERR_CUDA;
+        rk3_step();
+        rk3_step();
+        if (cudaStreamEndCapture(stream, &g) != cudaSuccess) return GA_ERR_CUDA;
+        cudaError_t e = cudaGraphInstantiate(&graph[parity], g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return GA_ERR_CUDA;
+        graph_launches[parity] = launches - l0;
+        launches = l0;
+        bigcounter = bc;
+        mtime = mt;
+        return GA_OK;
+    }
+
     int step(int nsteps) override
     {
         cudaSetDevice(device);
-        for (int n = 0; n < nsteps; n++) {
+        int n = 0;
+        if (use_graphs && !prof) {
+            while (nsteps - n >= 2) {
+                const int parity = ci[0] == 0 ? 0 : 1;
+                if (!graph[parity]) {
+                    int rc = capture_pair(parity);
+                    if (rc) {
+                        cudaGetLastError();
+                        use_graphs = false;
+                        break;
+                    }
+                }
+                if (cudaGraphLaunch(graph[parity], stream) != cudaSuccess) return launch_status();
+                launches += graph_launches[parity];
+                bigcounter += 2;
+                mtime += 2 * cfg.dt;
+                n += 2;
+            }
+        }
+        for (; n < nsteps; n++) {
             rk3_step();
             int rc = launch_status();
             if (rc) return rc;
         }
-        return GA_OK;
+        return launch_status();
     }
 
     int check_finite() override

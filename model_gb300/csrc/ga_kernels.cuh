@@ -460,6 +460,7 @@ constexpr int PPM_MAXZ = 128;  // largest NZ the column kernels support
 struct FftPlan {
     int n, nfac;
     int fac[24];
+    int nslog[24];  // log2 of the sub-transform size before each pass, -1 if not a power of two
 };
 
 template <typename T2>
@@ -478,8 +479,9 @@ __device__ __forceinline__ T2 twid(const T2 *tw, int t, bool inv)
     return w;
 }
 
+// L lines; lg2L = log2(L) when L is a power of two (shift indexing), else -1
 template <typename T, typename T2>
-__device__ T2 *fft_smem(T2 *a, T2 *b, int L, const FftPlan &P, const T2 *__restrict__ tw, bool inv)
+__device__ T2 *fft_smem(T2 *a, T2 *b, int L, int lg2L, const FftPlan &P, const T2 *__restrict__ tw, bool inv)
 {
     const int N = P.n;
     int Ns = 1;
@@ -487,9 +489,15 @@ __device__ T2 *fft_smem(T2 *a, T2 *b, int L, const FftPlan &P, const T2 *__restr
         const int R = P.fac[f];
         const int nb = N / R;
         const int ts = N / (Ns * R);
+        const int nsl = P.nslog[f];
         for (int w = threadIdx.x; w < nb * L; w += blockDim.x) {
-            const int l = w % L, j = w / L, k = j % Ns;
-            const int ob = (j / Ns) * Ns * R + k;
+            int l, j;
+            if (lg2L >= 0) { l = w & (L - 1); j = w >> lg2L; }
+            else { l = w % L; j = w / L; }
+            int k, jb;
+            if (nsl >= 0) { k = j & (Ns - 1); jb = j >> nsl; }
+            else { k = j % Ns; jb = j / Ns; }
+            const int ob = jb * Ns * R + k;
             if (R == 2) {
                 T2 v0 = a[j * L + l];
                 T2 v1 = a[(j + nb) * L + l];
@@ -571,10 +579,11 @@ __device__ __forceinline__ T divergence(const KParams<T> &p, const KFields<T> &F
 // tile of KT levels starting at level 1).
 template <typename T>
 __global__ void k_div_fft_y(KParams<T> p, KFields<T> F, typename V2<T>::t *spec, FftPlan pj,
-                            const typename V2<T>::t *tw, T sdt, int KT)
+                            const typename V2<T>::t *tw, T sdt, int lgKT)
 {
     typedef typename V2<T>::t T2;
     extern __shared__ unsigned char smem_raw[];
+    const int KT = 1 << lgKT;
     T2 *a = (T2 *)smem_raw;
     T2 *b = a + (long)p.nj * KT;
     const int is = blockIdx.x;
@@ -584,7 +593,7 @@ __global__ void k_div_fft_y(KParams<T> p, KFields<T> F, typename V2<T>::t *spec,
     if (!p.periodic) ii = min(max(is, 1), p.nx - 2);
     else ii = is + 3;
     for (int w = threadIdx.x; w < p.nj * KT; w += blockDim.x) {
-        const int l = w % KT, q = w / KT;
+        const int l = w & (KT - 1), q = w >> lgKT;
         T2 v;
         v.y = T(0);
         v.x = T(0);
@@ -595,9 +604,9 @@ __global__ void k_div_fft_y(KParams<T> p, KFields<T> F, typename V2<T>::t *spec,
         a[w] = v;
     }
     __syncthreads();
-    T2 *r = fft_smem<T, T2>(a, b, KT, pj, tw, false);
+    T2 *r = fft_smem<T, T2>(a, b, KT, lgKT, pj, tw, false);
     for (int w = threadIdx.x; w < p.nj * KT; w += blockDim.x) {
-        const int l = w % KT, q = w / KT;
+        const int l = w & (KT - 1), q = w >> lgKT;
         if (l < kt) spec[((long)is * p.nj + q) * p.nz + k0 + l] = r[w];
     }
 }
@@ -606,17 +615,18 @@ __global__ void k_div_fft_y(KParams<T> p, KFields<T> F, typename V2<T>::t *spec,
 // levels.  sign: forward (false) or inverse (true).
 template <typename T>
 __global__ void k_fft_x(KParams<T> p, typename V2<T>::t *spec, FftPlan pi, const typename V2<T>::t *tw,
-                        int inv, int KT)
+                        int inv, int lgKT)
 {
     typedef typename V2<T>::t T2;
     extern __shared__ unsigned char smem_raw[];
+    const int KT = 1 << lgKT;
     T2 *a = (T2 *)smem_raw;
     T2 *b = a + (long)p.ni * KT;
     const int q = blockIdx.x;
     const int k0 = 1 + blockIdx.y * KT;
     const int kt = min(KT, p.nz - 1 - k0);
     for (int w = threadIdx.x; w < p.ni * KT; w += blockDim.x) {
-        const int l = w % KT, i = w / KT;
+        const int l = w & (KT - 1), i = w >> lgKT;
         T2 v;
         v.x = T(0);
         v.y = T(0);
@@ -624,9 +634,9 @@ __global__ void k_fft_x(KParams<T> p, typename V2<T>::t *spec, FftPlan pi, const
         a[w] = v;
     }
     __syncthreads();
-    T2 *r = fft_smem<T, T2>(a, b, KT, pi, tw, inv != 0);
+    T2 *r = fft_smem<T, T2>(a, b, KT, lgKT, pi, tw, inv != 0);
     for (int w = threadIdx.x; w < p.ni * KT; w += blockDim.x) {
-        const int l = w % KT, i = w / KT;
+        const int l = w & (KT - 1), i = w >> lgKT;
         if (l < kt) spec[((long)i * p.nj + q) * p.nz + k0 + l] = r[w];
     }
 }
@@ -718,22 +728,74 @@ __global__ void k_thomas(KParams<T> p, typename V2<T>::t *spec, int TC)
     for (int w = threadIdx.x; w < nc * p.nz; w += blockDim.x) g[w] = xs[w];
 }
 
+// Forward FFT along x, normalisation + Thomas solve per wavenumber, inverse
+// FFT along x, for one y-wavenumber q with every level 1..NZ-2 resident in
+// shared memory (lines padded to a power of two).  After the forward pass
+// the other ping-pong buffer is free and holds the Thomas coefficients.
+template <typename T>
+__global__ void k_spectral_x(KParams<T> p, typename V2<T>::t *spec, FftPlan pi, const typename V2<T>::t *tw,
+                             int L, int lgL)
+{
+    typedef typename V2<T>::t T2;
+    extern __shared__ unsigned char smem_raw[];
+    T2 *a = (T2 *)smem_raw;
+    T2 *b = a + (long)p.ni * L;
+    const int q = blockIdx.x;
+    const int nl = p.nz - 2;  // levels 1..NZ-2
+    for (int w = threadIdx.x; w < p.ni * L; w += blockDim.x) {
+        const int l = lgL >= 0 ? (w & (L - 1)) : (w % L), i = lgL >= 0 ? (w >> lgL) : (w / L);
+        T2 v;
+        v.x = T(0);
+        v.y = T(0);
+        if (l < nl) v = spec[((long)i * p.nj + q) * p.nz + 1 + l];
+        a[w] = v;
+    }
+    __syncthreads();
+    T2 *r = fft_smem<T, T2>(a, b, L, lgL, pi, tw, false);
+    T2 *fr = (r == a) ? b : a;  // free buffer
+    const double size2d = (double)(p.ni * p.nj);
+    for (int pp = threadIdx.x; pp < p.ni; pp += blockDim.x) {
+        const long col = (long)pp * p.nj + q;
+        // x is indexed by level k at x[k]: column pp holds levels 1..NZ-2 at r[pp*L + k-1]
+        T2 *x = r + (long)pp * L - 1;
+        bool low = false;
+        if (p.low_modes > 0) {
+            const int ap = min(pp, p.ni - pp), aq = min(q, p.nj - q);
+            low = ap < p.low_modes && aq < p.low_modes;
+        }
+        if (low || sizeof(T) == 8) {
+            double *Fw = (double *)(fr + (long)pp * L) - 1;
+            thomas_column<T, double>(p, x, Fw, col, size2d, p.rhou_d, p.acoef_d, p.ccoef_d, p.vcoef_d);
+        } else {
+            T *Fw = (T *)(fr + (long)pp * L) - 1;
+            thomas_column<T, T>(p, x, Fw, col, size2d, p.rhou, p.acoef, p.ccoef, p.vcoef);
+        }
+    }
+    __syncthreads();
+    T2 *o = fft_smem<T, T2>(r, fr, L, lgL, pi, tw, true);
+    for (int w = threadIdx.x; w < p.ni * L; w += blockDim.x) {
+        const int l = lgL >= 0 ? (w & (L - 1)) : (w % L), i = lgL >= 0 ? (w >> lgL) : (w / L);
+        if (l < nl) spec[((long)i * p.nj + q) * p.nz + 1 + l] = o[w];
+    }
+}
+
 // inverse FFT along y + PI = real part, with the level copies of
 // poisson_fft3d (pressure.cpp:878-892) and the lateral placement of
 // mirror_boundaries(PI) or periodic_pressure_boundaries.
 template <typename T>
 __global__ void k_ifft_y_pi(KParams<T> p, KFields<T> F, typename V2<T>::t *spec, FftPlan pj,
-                            const typename V2<T>::t *tw, int KT)
+                            const typename V2<T>::t *tw, int lgKT)
 {
     typedef typename V2<T>::t T2;
     extern __shared__ unsigned char smem_raw[];
+    const int KT = 1 << lgKT;
     T2 *a = (T2 *)smem_raw;
     T2 *b = a + (long)p.nj * KT;
     const int is = blockIdx.x;
     const int k0 = 1 + blockIdx.y * KT;
     const int kt = min(KT, p.nz - 1 - k0);
     for (int w = threadIdx.x; w < p.nj * KT; w += blockDim.x) {
-        const int l = w % KT, q = w / KT;
+        const int l = w & (KT - 1), q = w >> lgKT;
         T2 v;
         v.x = T(0);
         v.y = T(0);
@@ -741,11 +803,11 @@ __global__ void k_ifft_y_pi(KParams<T> p, KFields<T> F, typename V2<T>::t *spec,
         a[w] = v;
     }
     __syncthreads();
-    T2 *r = fft_smem<T, T2>(a, b, KT, pj, tw, true);
+    T2 *r = fft_smem<T, T2>(a, b, KT, lgKT, pj, tw, true);
     T *PI = F.pi;
     const int nz = p.nz, ny = p.ny;
     for (int w = threadIdx.x; w < p.nj * KT; w += blockDim.x) {
-        const int l = w % KT, j = w / KT;
+        const int l = w & (KT - 1), j = w >> lgKT;
         if (l >= kt) continue;
         const int k = k0 + l;
         if (!p.periodic) {
@@ -829,7 +891,8 @@ __device__ __forceinline__ T chain_value(const KParams<T> &p, const KFields<T> &
 }
 
 template <typename T>
-__global__ void k_post(KParams<T> p, KFields<T> F, int nfields, int4 fl0, int4 fl1, T step, int cols)
+__global__ void __launch_bounds__(256) k_post(KParams<T> p, KFields<T> F, int nfields, int4 fl0, int4 fl1, T step,
+                                              int cols)
 {
     const int lane = threadIdx.x & 31;
     const long warp = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -849,34 +912,39 @@ __global__ void k_post(KParams<T> p, KFields<T> F, int nfields, int4 fl0, int4 f
     int si = i;
     if (cols == COLS_TARGETS) si = i < 3 ? p.nx - 6 + i : 3 + (i - (p.nx - 3));
     const int nz = p.nz;
-    const int flv[8] = {fl0.x, fl0.y, fl0.z, fl0.w, fl1.x, fl1.y, fl1.z, fl1.w};
-    for (int f = 0; f < nfields; ++f) {
-        const int flags = flv[f];
-        if (!flags) continue;
-        T *P = F.P[f];
-        T vals[KPL];
+    const int flv[7] = {fl0.x, fl0.y, fl0.z, fl0.w, fl1.x, fl1.y, fl1.z};
+    const long src0 = gix(p.ny, nz, si, j, 0), dst0 = gix(p.ny, nz, i, j, 0);
+    // all loads of the column first, so they are in flight together
+    T vals[7][KPL];
+#pragma unroll
+    for (int f = 0; f < 7; ++f) {
 #pragma unroll
         for (int r = 0; r < KPL; ++r) {
             const int k = lane + 32 * r;
-            vals[r] = T(0);
-            if (k < nz) {
-                T v = P[gix(p.ny, nz, si, j, k)];
-                vals[r] = chain_value(p, F, f, flags, si, j, k, v, step);
-            }
+            vals[f][r] = (f < nfields && flv[f] && k < nz) ? F.P[f][src0 + k] : T(0);
+        }
+    }
+#pragma unroll
+    for (int f = 0; f < 7; ++f) {
+        if (f >= nfields || !flv[f]) continue;
+        const int flags = flv[f];
+#pragma unroll
+        for (int r = 0; r < KPL; ++r) {
+            const int k = lane + 32 * r;
+            if (k < nz) vals[f][r] = chain_value(p, F, f, flags, si, j, k, vals[f][r], step);
         }
         // values at k=1 and k=NZ-2 after the chain, for the vertical condition
-        const T v1 = __shfl_sync(0xffffffffu, vals[0], 1);
+        const T v1 = __shfl_sync(0xffffffffu, vals[f][0], 1);
         const int kt = nz - 2;
-        T vtop = vals[0];
+        T vtop = vals[f][0];
 #pragma unroll
         for (int r = 0; r < KPL; ++r)
-            if (kt / 32 == r) vtop = __shfl_sync(0xffffffffu, vals[r], kt & 31);
-        __syncwarp();
+            if (kt / 32 == r) vtop = __shfl_sync(0xffffffffu, vals[f][r], kt & 31);
 #pragma unroll
         for (int r = 0; r < KPL; ++r) {
             const int k = lane + 32 * r;
             if (k >= nz) continue;
-            T v = vals[r];
+            T v = vals[f][r];
             if ((flags & PF_VBC) && i >= 1 && j >= 1) {
                 if (f == FW) {
                     if (k == 0 || k == 1 || k == nz - 1) v = T(0);
@@ -890,9 +958,20 @@ __global__ void k_post(KParams<T> p, KFields<T> F, int nfields, int4 fl0, int4 f
                 const T cr = (f == FW) ? p.ray_w[k] : p.ray_u[k];
                 v = v - cr * v;
             }
-            const long c = gix(p.ny, nz, i, j, k);
-            P[c] = v;
-            if (flags & PF_WRITE_M) F.M[f][c] = v;
+            vals[f][r] = v;
+        }
+    }
+    __syncwarp();
+#pragma unroll
+    for (int f = 0; f < 7; ++f) {
+        if (f >= nfields || !flv[f]) continue;
+        const bool wm = (flv[f] & PF_WRITE_M) != 0;
+#pragma unroll
+        for (int r = 0; r < KPL; ++r) {
+            const int k = lane + 32 * r;
+            if (k >= nz) continue;
+            F.P[f][dst0 + k] = vals[f][r];
+            if (wm) F.M[f][dst0 + k] = vals[f][r];
         }
     }
 }
