@@ -57,7 +57,7 @@ class Engine : public EngineBase {
     T *ppm_topq = nullptr, *ppm_topm = nullptr, *ppm_cin = nullptr, *ppm_carry = nullptr;
     double *staging = nullptr;
     int KTy = 1, KTx = 1, lgKTy = 0, lgKTx = 0, TC = 64;
-    int Lsx = 0, lgLsx = -1;  // lines of the fused spectral-x kernel (0: not used)
+    int Lsx = 0, lgLsx = -1, psx = 0;  // lines / point stride of the fused spectral-x kernel (0: not used)
     size_t smem_y = 0, smem_x = 0, smem_th = 0, smem_sx = 0;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     long long graph_launches[2] = {0, 0};
@@ -214,15 +214,20 @@ class Engine : public EngineBase {
         KTx = pow2_tile(ni, &lgKTx);
         smem_y = 2 * (size_t)nj * KTy * sizeof(T2);
         smem_x = 2 * (size_t)ni * KTx * sizeof(T2);
-        smem_th = (size_t)TC * NZ * (sizeof(T2) + sizeof(T));
+        smem_th = (size_t)TC * (NZ | 1) * (sizeof(T2) + sizeof(T));
         const int optin = 200 * 1024;
-        {   // fused x transform + Thomas when all levels of a wavenumber fit
+        {   // fused x transform + Thomas when all levels of a wavenumber fit.  The
+            // point stride is padded to 1 mod (banks per element) so the Thomas
+            // threads, one per x-wavenumber, hit distinct banks.
             const int nl = NZ - 2;
+            const int m = 32 / (int)(sizeof(T2) / 4);
+            auto pad = [&](int L) { return L + ((1 - L % m) % m + m) % m; };
             int l2 = 1, lg = 0;
             while (l2 < nl) { l2 <<= 1; lg++; }
-            if (2 * (size_t)ni * l2 * sizeof(T2) <= (size_t)optin) { Lsx = l2; lgLsx = lg; }
-            else if (2 * (size_t)ni * nl * sizeof(T2) <= (size_t)optin) { Lsx = nl; lgLsx = -1; }
-            smem_sx = 2 * (size_t)ni * Lsx * sizeof(T2);
+            if (2 * (size_t)ni * pad(l2) * sizeof(T2) <= (size_t)optin) { Lsx = l2; lgLsx = lg; psx = pad(l2); }
+            else if (2 * (size_t)ni * pad(nl) * sizeof(T2) <= (size_t)optin) { Lsx = nl; lgLsx = -1; psx = pad(nl); }
+            else if (2 * (size_t)ni * (nl | 1) * sizeof(T2) <= (size_t)optin) { Lsx = nl; lgLsx = -1; psx = nl | 1; }
+            smem_sx = 2 * (size_t)ni * psx * sizeof(T2);
         }
         cudaFuncSetAttribute(k_spectral_x<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
         cudaFuncSetAttribute(k_div_fft_y<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
@@ -401,7 +406,7 @@ class Engine : public EngineBase {
         }
         if (Lsx > 0) {
             ProfScope ps(this, PC_THOMAS, 1);
-            k_spectral_x<T><<<kp.nj, 256, smem_sx, stream>>>(kp, spec, plan_i, tw_i, Lsx, lgLsx);
+            k_spectral_x<T><<<kp.nj, 256, smem_sx, stream>>>(kp, spec, plan_i, tw_i, Lsx, lgLsx, psx);
             launches += 1;
         } else {
             {

@@ -479,9 +479,12 @@ __device__ __forceinline__ T2 twid(const T2 *tw, int t, bool inv)
     return w;
 }
 
-// L lines; lg2L = log2(L) when L is a power of two (shift indexing), else -1
+// L lines; lg2L = log2(L) when L is a power of two (shift indexing), else -1.
+// Element (point n, line l) lives at buf[n*ps + l]; ps >= L (padding keeps a
+// thread that walks one line across points off a single bank).
 template <typename T, typename T2>
-__device__ T2 *fft_smem(T2 *a, T2 *b, int L, int lg2L, const FftPlan &P, const T2 *__restrict__ tw, bool inv)
+__device__ T2 *fft_smem(T2 *a, T2 *b, int L, int lg2L, const FftPlan &P, const T2 *__restrict__ tw, bool inv,
+                        int ps)
 {
     const int N = P.n;
     int Ns = 1;
@@ -499,19 +502,19 @@ __device__ T2 *fft_smem(T2 *a, T2 *b, int L, int lg2L, const FftPlan &P, const T
             else { k = j % Ns; jb = j / Ns; }
             const int ob = jb * Ns * R + k;
             if (R == 2) {
-                T2 v0 = a[j * L + l];
-                T2 v1 = a[(j + nb) * L + l];
+                T2 v0 = a[j * ps + l];
+                T2 v1 = a[(j + nb) * ps + l];
                 if (k) v1 = cmul(v1, twid(tw, k * ts, inv));
                 T2 s, d;
                 s.x = v0.x + v1.x; s.y = v0.y + v1.y;
                 d.x = v0.x - v1.x; d.y = v0.y - v1.y;
-                b[ob * L + l] = s;
-                b[(ob + Ns) * L + l] = d;
+                b[ob * ps + l] = s;
+                b[(ob + Ns) * ps + l] = d;
             } else if (R == 4) {
-                T2 v0 = a[j * L + l];
-                T2 v1 = a[(j + nb) * L + l];
-                T2 v2 = a[(j + 2 * nb) * L + l];
-                T2 v3 = a[(j + 3 * nb) * L + l];
+                T2 v0 = a[j * ps + l];
+                T2 v1 = a[(j + nb) * ps + l];
+                T2 v2 = a[(j + 2 * nb) * ps + l];
+                T2 v3 = a[(j + 3 * nb) * ps + l];
                 if (k) {
                     v1 = cmul(v1, twid(tw, k * ts, inv));
                     v2 = cmul(v2, twid(tw, 2 * k * ts, inv));
@@ -531,10 +534,10 @@ __device__ T2 *fft_smem(T2 *a, T2 *b, int L, int lg2L, const FftPlan &P, const T
                     x1.x = d02.x - d13.y; x1.y = d02.y + d13.x;
                     x3.x = d02.x + d13.y; x3.y = d02.y - d13.x;
                 }
-                b[ob * L + l] = x0;
-                b[(ob + Ns) * L + l] = x1;
-                b[(ob + 2 * Ns) * L + l] = x2;
-                b[(ob + 3 * Ns) * L + l] = x3;
+                b[ob * ps + l] = x0;
+                b[(ob + Ns) * ps + l] = x1;
+                b[(ob + 2 * Ns) * ps + l] = x2;
+                b[(ob + 3 * Ns) * ps + l] = x3;
             } else {  // generic radix: direct R-point DFT with combined twiddles
                 for (int m = 0; m < R; ++m) {
                     T2 acc;
@@ -542,12 +545,12 @@ __device__ T2 *fft_smem(T2 *a, T2 *b, int L, int lg2L, const FftPlan &P, const T
                     acc.y = T(0);
                     for (int r = 0; r < R; ++r) {
                         const int t = (k * r * ts + ((r * m) % R) * nb) % N;
-                        T2 x = a[(j + r * nb) * L + l];
+                        T2 x = a[(j + r * nb) * ps + l];
                         T2 wv = twid(tw, t, inv);
                         acc.x += x.x * wv.x - x.y * wv.y;
                         acc.y += x.x * wv.y + x.y * wv.x;
                     }
-                    b[(ob + m * Ns) * L + l] = acc;
+                    b[(ob + m * Ns) * ps + l] = acc;
                 }
             }
         }
@@ -604,7 +607,7 @@ __global__ void k_div_fft_y(KParams<T> p, KFields<T> F, typename V2<T>::t *spec,
         a[w] = v;
     }
     __syncthreads();
-    T2 *r = fft_smem<T, T2>(a, b, KT, lgKT, pj, tw, false);
+    T2 *r = fft_smem<T, T2>(a, b, KT, lgKT, pj, tw, false, KT);
     for (int w = threadIdx.x; w < p.nj * KT; w += blockDim.x) {
         const int l = w & (KT - 1), q = w >> lgKT;
         if (l < kt) spec[((long)is * p.nj + q) * p.nz + k0 + l] = r[w];
@@ -634,7 +637,7 @@ __global__ void k_fft_x(KParams<T> p, typename V2<T>::t *spec, FftPlan pi, const
         a[w] = v;
     }
     __syncthreads();
-    T2 *r = fft_smem<T, T2>(a, b, KT, lgKT, pi, tw, inv != 0);
+    T2 *r = fft_smem<T, T2>(a, b, KT, lgKT, pi, tw, inv != 0, KT);
     for (int w = threadIdx.x; w < p.ni * KT; w += blockDim.x) {
         const int l = w & (KT - 1), i = w >> lgKT;
         if (l < kt) spec[((long)i * p.nj + q) * p.nz + k0 + l] = r[w];
@@ -699,13 +702,14 @@ __global__ void k_thomas(KParams<T> p, typename V2<T>::t *spec, int TC)
 {
     typedef typename V2<T>::t T2;
     extern __shared__ unsigned char smem_raw[];
+    const int cs = p.nz | 1;  // odd column stride: no bank conflicts between columns
     T2 *xs = (T2 *)smem_raw;
-    T *fs = (T *)(xs + (long)TC * p.nz);
+    T *fs = (T *)(xs + (long)TC * cs);
     const long ncol = (long)p.ni * p.nj;
     const long c0 = (long)blockIdx.x * TC;
     const int nc = (int)min((long)TC, ncol - c0);
     T2 *g = spec + c0 * p.nz;
-    for (int w = threadIdx.x; w < nc * p.nz; w += blockDim.x) xs[w] = g[w];
+    for (int w = threadIdx.x; w < nc * p.nz; w += blockDim.x) xs[(w / p.nz) * cs + w % p.nz] = g[w];
     __syncthreads();
     const double size2d = (double)(p.ni * p.nj);
     for (int c = threadIdx.x; c < nc; c += blockDim.x) {
@@ -718,14 +722,14 @@ __global__ void k_thomas(KParams<T> p, typename V2<T>::t *spec, int TC)
         }
         if (low) {
             double Floc[PPM_MAXZ];
-            thomas_column<T, double>(p, xs + (long)c * p.nz, Floc, col, size2d, p.rhou_d, p.acoef_d,
+            thomas_column<T, double>(p, xs + (long)c * cs, Floc, col, size2d, p.rhou_d, p.acoef_d,
                                      p.ccoef_d, p.vcoef_d);
         } else
-            thomas_column<T, T>(p, xs + (long)c * p.nz, fs + (long)c * p.nz, col, size2d, p.rhou, p.acoef,
+            thomas_column<T, T>(p, xs + (long)c * cs, fs + (long)c * cs, col, size2d, p.rhou, p.acoef,
                                 p.ccoef, p.vcoef);
     }
     __syncthreads();
-    for (int w = threadIdx.x; w < nc * p.nz; w += blockDim.x) g[w] = xs[w];
+    for (int w = threadIdx.x; w < nc * p.nz; w += blockDim.x) g[w] = xs[(w / p.nz) * cs + w % p.nz];
 }
 
 // Forward FFT along x, normalisation + Thomas solve per wavenumber, inverse
@@ -734,12 +738,12 @@ __global__ void k_thomas(KParams<T> p, typename V2<T>::t *spec, int TC)
 // the other ping-pong buffer is free and holds the Thomas coefficients.
 template <typename T>
 __global__ void k_spectral_x(KParams<T> p, typename V2<T>::t *spec, FftPlan pi, const typename V2<T>::t *tw,
-                             int L, int lgL)
+                             int L, int lgL, int ps)
 {
     typedef typename V2<T>::t T2;
     extern __shared__ unsigned char smem_raw[];
     T2 *a = (T2 *)smem_raw;
-    T2 *b = a + (long)p.ni * L;
+    T2 *b = a + (long)p.ni * ps;
     const int q = blockIdx.x;
     const int nl = p.nz - 2;  // levels 1..NZ-2
     for (int w = threadIdx.x; w < p.ni * L; w += blockDim.x) {
@@ -748,34 +752,34 @@ __global__ void k_spectral_x(KParams<T> p, typename V2<T>::t *spec, FftPlan pi, 
         v.x = T(0);
         v.y = T(0);
         if (l < nl) v = spec[((long)i * p.nj + q) * p.nz + 1 + l];
-        a[w] = v;
+        a[i * ps + l] = v;
     }
     __syncthreads();
-    T2 *r = fft_smem<T, T2>(a, b, L, lgL, pi, tw, false);
+    T2 *r = fft_smem<T, T2>(a, b, L, lgL, pi, tw, false, ps);
     T2 *fr = (r == a) ? b : a;  // free buffer
     const double size2d = (double)(p.ni * p.nj);
     for (int pp = threadIdx.x; pp < p.ni; pp += blockDim.x) {
         const long col = (long)pp * p.nj + q;
         // x is indexed by level k at x[k]: column pp holds levels 1..NZ-2 at r[pp*L + k-1]
-        T2 *x = r + (long)pp * L - 1;
+        T2 *x = r + (long)pp * ps - 1;
         bool low = false;
         if (p.low_modes > 0) {
             const int ap = min(pp, p.ni - pp), aq = min(q, p.nj - q);
             low = ap < p.low_modes && aq < p.low_modes;
         }
         if (low || sizeof(T) == 8) {
-            double *Fw = (double *)(fr + (long)pp * L) - 1;
+            double *Fw = (double *)(fr + (long)pp * ps) - 1;
             thomas_column<T, double>(p, x, Fw, col, size2d, p.rhou_d, p.acoef_d, p.ccoef_d, p.vcoef_d);
         } else {
-            T *Fw = (T *)(fr + (long)pp * L) - 1;
+            T *Fw = (T *)(fr + (long)pp * ps) - 1;
             thomas_column<T, T>(p, x, Fw, col, size2d, p.rhou, p.acoef, p.ccoef, p.vcoef);
         }
     }
     __syncthreads();
-    T2 *o = fft_smem<T, T2>(r, fr, L, lgL, pi, tw, true);
+    T2 *o = fft_smem<T, T2>(r, fr, L, lgL, pi, tw, true, ps);
     for (int w = threadIdx.x; w < p.ni * L; w += blockDim.x) {
         const int l = lgL >= 0 ? (w & (L - 1)) : (w % L), i = lgL >= 0 ? (w >> lgL) : (w / L);
-        if (l < nl) spec[((long)i * p.nj + q) * p.nz + 1 + l] = o[w];
+        if (l < nl) spec[((long)i * p.nj + q) * p.nz + 1 + l] = o[i * ps + l];
     }
 }
 
@@ -803,7 +807,7 @@ __global__ void k_ifft_y_pi(KParams<T> p, KFields<T> F, typename V2<T>::t *spec,
         a[w] = v;
     }
     __syncthreads();
-    T2 *r = fft_smem<T, T2>(a, b, KT, lgKT, pj, tw, true);
+    T2 *r = fft_smem<T, T2>(a, b, KT, lgKT, pj, tw, true, KT);
     T *PI = F.pi;
     const int nz = p.nz, ny = p.ny;
     for (int w = threadIdx.x; w < p.nj * KT; w += blockDim.x) {
