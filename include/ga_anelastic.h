@@ -216,6 +216,35 @@ GA_API void *ga_stream(ga_ctx *ctx);
  * callers that keep state resident on the GPU. */
 GA_API void *ga_field_device_ptr(ga_ctx *ctx, int field, int slot);
 
+/*
+ * Pressure solve without device allocation.  No counterpart in the reference:
+ * it is for callers that cannot allocate GPU memory themselves or through
+ * this library (a host model that owns every byte of device memory in its own
+ * pool, a plugin inside a process whose allocator forbids foreign cudaMalloc
+ * calls, code running inside a stream capture where an allocation would break
+ * the capture).
+ *
+ * Runs solve_pressure (pressure.cpp:142-224) in FP64 on caller-owned device
+ * arrays [NX][NY][NZ]: up, vp, wp (read, and their lateral boundary points
+ * overwritten by the mirror or periodic copy, as the reference does) and pi
+ * (written).  cols are host arrays as for ga_create.  The work is queued on
+ * `stream` (a cudaStream_t, or NULL for the legacy default stream) on the
+ * current CUDA device; the call returns without synchronizing.
+ *
+ * All scratch lives in one file-scope device array of GA_NOALLOC_SCRATCH_BYTES
+ * that every GPU loading this library holds until the process exits.  The
+ * first call on a device looks up that array's device address (once per
+ * device); make that first call before any stream capture.  Grids whose
+ * spectral buffer and tables exceed the array are rejected with GA_ERR_ARG
+ * (for a non-periodic grid: 16*NX*NY*NZ + 8*NX*NY + 16*(NX+NY) bytes plus
+ * small column tables, e.g. 128 x 128 x 96 fits).  Calls share the array:
+ * calls that overlap on the GPU race and must be ordered by the caller.
+ * The function calls no cudaMalloc, cudaFree or other allocating routine.
+ */
+#define GA_NOALLOC_SCRATCH_BYTES (32u << 20)
+GA_API int ga_solve_pressure_noalloc(const ga_config *cfg, const ga_columns *cols, double *up,
+                                     double *vp, double *wp, double *pi, double step, void *stream);
+
 /* Optional timing of the kernel groups with CUDA events recorded on the
  * context's stream (advect, edges, div_fft_y, fft_x, thomas, ifft_y_pi,
  * post, kessler, ppm, copy).  Enabling resets the totals.  The reference

@@ -4,6 +4,7 @@ Three translation units compiled in parallel with nvcc, then linked:
   ga_f64.cu  FP64 engine, --fmad=false (no contraction: the parity path)
   ga_f32.cu  FP32 engine
   ga_api.cu  the extern "C" boundary of include/ga_anelastic.h
+  ga_noalloc.cu  FP64 pressure solve with file-scope scratch (no allocation)
 Objects go to model_gb300/_build/ (git-ignored).  A rebuild happens only
 when a source is newer than the library.
 """
@@ -30,6 +31,7 @@ UNITS = {
     "ga_f64": ["--fmad=false"],
     "ga_f32": [],
     "ga_api": [],
+    "ga_noalloc": ["--fmad=false"],
 }
 
 

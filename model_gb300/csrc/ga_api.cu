@@ -223,6 +223,27 @@ void *ga_field_device_ptr(ga_ctx *ctx, int field, int slot)
     return ctx->e->field_ptr(field, slot);
 }
 
+int ga_solve_pressure_noalloc(const ga_config *cfg, const ga_columns *cols, double *up, double *vp, double *wp,
+                              double *pi, double step, void *stream)
+{
+    if (!cfg || !cols || !up || !vp || !wp || !pi)
+        return fail(GA_ERR_ARG, "ga_solve_pressure_noalloc: null pointer");
+    if (!cols->mu || !cols->mw || !cols->rhou || !cols->rhow)
+        return fail(GA_ERR_ARG, "ga_solve_pressure_noalloc: a column array is null");
+    if (cfg->nx < 12 || cfg->ny < 12 || cfg->nz < 6 || cfg->nz > 128)
+        return fail(GA_ERR_CONFIG, "ga_solve_pressure_noalloc: grid out of range (NX,NY >= 12, 6 <= NZ <= 128)");
+    if (cfg->periodic_ew_boundaries && cfg->nx < 13)
+        return fail(GA_ERR_CONFIG, "ga_solve_pressure_noalloc: periodic domains need NX >= 13");
+    if (!(cfg->dx > 0 && cfg->dy > 0 && cfg->dz > 0 && cfg->dt > 0) || !(step > 0))
+        return fail(GA_ERR_CONFIG, "ga_solve_pressure_noalloc: dx, dy, dz, dt and step must be positive");
+    const size_t need = ga::noalloc_bytes_needed(cfg);
+    if (need > GA_NOALLOC_SCRATCH_BYTES)
+        return fail(GA_ERR_ARG, "ga_solve_pressure_noalloc: grid needs " + std::to_string(need) +
+                                    " bytes of scratch, more than the fixed " +
+                                    std::to_string((size_t)GA_NOALLOC_SCRATCH_BYTES) + " bytes");
+    return ga::solve_pressure_noalloc(cfg, cols, up, vp, wp, pi, step, (cudaStream_t)stream);
+}
+
 int ga_profile_enable(ga_ctx *ctx, int on)
 {
     if (!ctx) return fail(GA_ERR_ARG, "ga_profile_enable: null context");

@@ -91,6 +91,10 @@ struct ProfScope {
 // set by the engines, read by ga_last_error (thread local)
 void set_error(const std::string &msg);
 
+size_t noalloc_bytes_needed(const ga_config *c);
+int solve_pressure_noalloc(const ga_config *c, const ga_columns *cols, double *up, double *vp, double *wp,
+                           double *pi, double step, cudaStream_t stream);
+
 EngineBase *make_engine_f64(const ga_config *cfg, const ga_columns *cols, int *rc);
 EngineBase *make_engine_f32(const ga_config *cfg, const ga_columns *cols, int *rc);
 
