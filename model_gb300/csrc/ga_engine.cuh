@@ -57,8 +57,8 @@ class Engine : public EngineBase {
     T *ppm_topq = nullptr, *ppm_topm = nullptr, *ppm_cin = nullptr, *ppm_carry = nullptr;
     double *staging = nullptr;
     int KTy = 1, KTx = 1, lgKTy = 0, lgKTx = 0, TC = 64;
-    int Lsx = 0, lgLsx = -1, psx = 0;  // lines / point stride of the fused spectral-x kernel (0: not used)
-    size_t smem_y = 0, smem_x = 0, smem_th = 0, smem_sx = 0;
+    int psx = 0;  // point stride of the fused spectral-x kernel (0: unfused path)
+    size_t smem_y = 0, smem_x = 0, smem_th = 0, smem_sx = 0, smem_adv = 0;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     long long graph_launches[2] = {0, 0};
     bool use_graphs = true;
@@ -95,6 +95,7 @@ class Engine : public EngineBase {
     {
         NX = c->nx; NY = c->ny; NZ = c->nz;
         N = (long)NX * NY * NZ;
+        if (N >= (1L << 31)) { status = GA_ERR_CONFIG; return; }
         device = c->device;
         if (cudaSetDevice(device) != cudaSuccess) { status = GA_ERR_CUDA; return; }
         if (cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking) != cudaSuccess) { status = GA_ERR_CUDA; return; }
@@ -184,7 +185,7 @@ class Engine : public EngineBase {
         kp.acoef_d = upload(ac); kp.ccoef_d = upload(cc); kp.vcoef_d = upload(vc);
         kp.rhou_d = upload(std::vector<double>(cols->rhou, cols->rhou + NZ));
         kp.dx2 = dx * dx;
-        kp.low_modes = sizeof(T) == 8 ? 0 : 3;
+        kp.low_modes = sizeof(T) == 8 ? 0 : 2;  // FP32: (p,q) in {0,1,N-1}^2 solve in FP64
 
         // ---- FFT plans and twiddles ----
         plan_i = make_fft_plan(ni);
@@ -221,15 +222,14 @@ class Engine : public EngineBase {
             // threads, one per x-wavenumber, hit distinct banks.
             const int nl = NZ - 2;
             const int m = 32 / (int)(sizeof(T2) / 4);
-            auto pad = [&](int L) { return L + ((1 - L % m) % m + m) % m; };
-            int l2 = 1, lg = 0;
-            while (l2 < nl) { l2 <<= 1; lg++; }
-            if (2 * (size_t)ni * pad(l2) * sizeof(T2) <= (size_t)optin) { Lsx = l2; lgLsx = lg; psx = pad(l2); }
-            else if (2 * (size_t)ni * pad(nl) * sizeof(T2) <= (size_t)optin) { Lsx = nl; lgLsx = -1; psx = pad(nl); }
-            else if (2 * (size_t)ni * (nl | 1) * sizeof(T2) <= (size_t)optin) { Lsx = nl; lgLsx = -1; psx = nl | 1; }
+            const int ps = nl + ((1 - nl % m) % m + m) % m;
+            if (2 * (size_t)ni * ps * sizeof(T2) <= (size_t)optin) psx = ps;
+            else if (2 * (size_t)ni * (nl | 1) * sizeof(T2) <= (size_t)optin) psx = nl | 1;
             smem_sx = 2 * (size_t)ni * psx * sizeof(T2);
         }
         cudaFuncSetAttribute(k_spectral_x<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+        smem_adv = (size_t)ADV_NF * ((ADV_TI + 1) * ADV_TJ + ADV_TI * (ADV_TJ + 1) + ADV_TI * ADV_TJ) * NZ * sizeof(T);
+        cudaFuncSetAttribute(k_advect_tile<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
         cudaFuncSetAttribute(k_div_fft_y<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
         cudaFuncSetAttribute(k_ifft_y_pi<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
         cudaFuncSetAttribute(k_fft_x<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
@@ -374,10 +374,15 @@ class Engine : public EngineBase {
     // ------------------------------------------------------------------ ops
     void advect(double step, int what)
     {
-        const long tot = (long)(NX - 6) * (NY - 6) * (NZ - 2);
         const double sdtg = step * cfg.dt * 9.8 * 0.5;  // step*dt*grav*0.5, advection.cpp:330
         ProfScope ps(this, PC_ADVECT, 1);
-        k_advect<T><<<cdiv(tot, 128), 128, 0, stream>>>(kp, fields(), (T)step, (T)sdtg, what);
+        if (smem_adv <= 200 * 1024) {
+            dim3 grid(cdiv(NX - 6, ADV_TI), cdiv(NY - 6, ADV_TJ));
+            k_advect_tile<T><<<grid, 256, smem_adv, stream>>>(kp, fields(), (T)step, (T)sdtg, what);
+        } else {  // face tiles of very tall columns do not fit: per-point form
+            const long tot = (long)(NX - 6) * (NY - 6) * (NZ - 2);
+            k_advect<T><<<cdiv(tot, 128), 128, 0, stream>>>(kp, fields(), (T)step, (T)sdtg, what);
+        }
         launches++;
     }
 
@@ -400,18 +405,20 @@ class Engine : public EngineBase {
         KFields<T> F = fields();
         const T sdt = (T)(step * cfg.dt);
         const int nkt_y = cdiv(NZ - 2, KTy), nkt_x = cdiv(NZ - 2, KTx);
+        const dim3 by_y(KTy, std::max(1, 256 / KTy)), by_x(KTx, std::max(1, 256 / KTx));
         {
             ProfScope ps(this, PC_DIV_FFT_Y, 1);
-            k_div_fft_y<T><<<dim3(kp.ni, nkt_y), 256, smem_y, stream>>>(kp, F, spec, plan_j, tw_j, sdt, lgKTy);
+            k_div_fft_y<T><<<dim3(kp.ni, nkt_y), by_y, smem_y, stream>>>(kp, F, spec, plan_j, tw_j, sdt, KTy);
         }
-        if (Lsx > 0) {
+        if (psx > 0) {
             ProfScope ps(this, PC_THOMAS, 1);
-            k_spectral_x<T><<<kp.nj, 256, smem_sx, stream>>>(kp, spec, plan_i, tw_i, Lsx, lgLsx, psx);
+            const int nl = NZ - 2, bx = std::min(nl, 64);
+            k_spectral_x<T><<<kp.nj, dim3(bx, std::max(1, 256 / bx)), smem_sx, stream>>>(kp, spec, plan_i, tw_i, psx);
             launches += 1;
         } else {
             {
                 ProfScope ps(this, PC_FFT_X, 1);
-                k_fft_x<T><<<dim3(kp.nj, nkt_x), 256, smem_x, stream>>>(kp, spec, plan_i, tw_i, 0, lgKTx);
+                k_fft_x<T><<<dim3(kp.nj, nkt_x), by_x, smem_x, stream>>>(kp, spec, plan_i, tw_i, 0, KTx);
             }
             const long ncol = (long)kp.ni * kp.nj;
             {
@@ -420,13 +427,13 @@ class Engine : public EngineBase {
             }
             {
                 ProfScope ps(this, PC_FFT_X, 1);
-                k_fft_x<T><<<dim3(kp.nj, nkt_x), 256, smem_x, stream>>>(kp, spec, plan_i, tw_i, 1, lgKTx);
+                k_fft_x<T><<<dim3(kp.nj, nkt_x), by_x, smem_x, stream>>>(kp, spec, plan_i, tw_i, 1, KTx);
             }
             launches += 3;
         }
         {
             ProfScope ps(this, PC_IFFT_Y_PI, 1);
-            k_ifft_y_pi<T><<<dim3(kp.ni, nkt_y), 256, smem_y, stream>>>(kp, F, spec, plan_j, tw_j, lgKTy);
+            k_ifft_y_pi<T><<<dim3(kp.ni, nkt_y), by_y, smem_y, stream>>>(kp, F, spec, plan_j, tw_j, KTy);
         }
         launches += 2;
     }
@@ -444,14 +451,14 @@ class Engine : public EngineBase {
         int fl[8] = {0, 0, 0, 0, 0, 0, 0, 0};
         for (int f = 0; f < nfields && f < 7; f++) fl[f] = f < nprog ? flags[f] : 0;
         int4 a = make_int4(fl[0], fl[1], fl[2], fl[3]), b = make_int4(fl[4], fl[5], fl[6], fl[7]);
-        const int wpb = 8;
         ProfScope ps(this, PC_POST, (pcopy && kp.periodic) ? 2 : 1);
         if (pcopy && kp.periodic) {
-            k_post<T><<<cdiv(6L * NY, wpb), 32 * wpb, 0, stream>>>(kp, F, 7, a, b, (T)step, COLS_TARGETS);
-            k_post<T><<<cdiv((long)NX * NY, wpb), 32 * wpb, 0, stream>>>(kp, F, 7, a, b, (T)step, COLS_NONTARGETS);
+            k_post<T><<<cdiv(6L * NY, POST_COLS), POST_THREADS, 0, stream>>>(kp, F, 7, a, b, (T)step, COLS_TARGETS);
+            k_post<T><<<cdiv((long)(NX - 6) * NY, POST_COLS), POST_THREADS, 0, stream>>>(kp, F, 7, a, b, (T)step,
+                                                                                      COLS_NONTARGETS);
             launches += 2;
         } else {
-            k_post<T><<<cdiv((long)NX * NY, wpb), 32 * wpb, 0, stream>>>(kp, F, 7, a, b, (T)step, COLS_ALL);
+            k_post<T><<<cdiv((long)NX * NY, POST_COLS), POST_THREADS, 0, stream>>>(kp, F, 7, a, b, (T)step, COLS_ALL);
             launches++;
         }
     }

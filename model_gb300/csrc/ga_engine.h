@@ -5,7 +5,7 @@
 #include <string>
 #include <vector>
 
-#include "../../include/ga_anelastic.h"
+#include "ga_anelastic.h"
 
 namespace ga {
 

@@ -58,9 +58,10 @@ struct KFields {
 
 enum { FU = 0, FV, FW, FTH, FQV, FQC, FQR };
 
-__host__ __device__ __forceinline__ long gix(int ny, int nz, int i, int j, int k)
+// grids are limited to fewer than 2^31 points (checked by the engine)
+__host__ __device__ __forceinline__ int gix(int ny, int nz, int i, int j, int k)
 {
-    return ((long)i * ny + j) * nz + k;
+    return (i * ny + j) * nz + k;
 }
 
 template <typename T>
@@ -105,14 +106,14 @@ struct Grid {
 template <typename T>
 __device__ __forceinline__ T f5i(const T *a, const KParams<T> &p, int i, int j, int k, T sign)
 {
-    const long s = (long)p.ny * p.nz, c = gix(p.ny, p.nz, i, j, k);
+    const int s = p.ny * p.nz, c = gix(p.ny, p.nz, i, j, k);
     return face5<T>(LD(a, c - 2 * s), LD(a, c - s), LD(a, c), LD(a, c + s), LD(a, c + 2 * s),
                     LD(a, c + 3 * s), sign);
 }
 template <typename T>
 __device__ __forceinline__ T f5j(const T *a, const KParams<T> &p, int i, int j, int k, T sign)
 {
-    const long s = p.nz, c = gix(p.ny, p.nz, i, j, k);
+    const int s = p.nz, c = gix(p.ny, p.nz, i, j, k);
     return face5<T>(LD(a, c - 2 * s), LD(a, c - s), LD(a, c), LD(a, c + s), LD(a, c + 2 * s),
                     LD(a, c + 3 * s), sign);
 }
@@ -405,6 +406,182 @@ __global__ void __launch_bounds__(128) k_advect(KParams<T> p, KFields<T> F, T st
 }
 
 // ---------------------------------------------------------------------------
+// Tiled advection: a block owns a TI x TJ tile of interior columns and every
+// interior level.  Phase 1 evaluates each east, north and top face flux of the
+// tile once (plus the west / south faces of its first row and column) into
+// shared memory; phase 2 forms every tendency from those faces.  Arithmetic is
+// that of k_advect, so results are identical.
+// ---------------------------------------------------------------------------
+constexpr int ADV_TI = 4, ADV_TJ = 4, ADV_NF = 6;  // flux fields: u, v, th, qv, qc, qr
+
+template <typename T>
+__device__ __forceinline__ void faces_east(const KParams<T> &p, const KFields<T> &F, int what, int i, int j, int k,
+                                           T *out)
+{
+    if (what & ADV_UV) {
+        out[0] = u_east(p, F, i, j, k);
+        out[1] = v_east(p, F, i, j, k);
+    }
+    if (what & ADV_TH) out[2] = s_east(p, F, F.cur[FTH], F.bar[3], i, j, k);
+    if (what & ADV_Q) {
+        out[3] = s_east(p, F, F.cur[FQV], F.bar[4], i, j, k);
+        out[4] = s_east(p, F, F.cur[FQC], (const T *)nullptr, i, j, k);
+        out[5] = s_east(p, F, F.cur[FQR], (const T *)nullptr, i, j, k);
+    }
+}
+template <typename T>
+__device__ __forceinline__ void faces_north(const KParams<T> &p, const KFields<T> &F, int what, int i, int j, int k,
+                                            T *out)
+{
+    if (what & ADV_UV) {
+        out[0] = u_north(p, F, i, j, k);
+        out[1] = v_north(p, F, i, j, k);
+    }
+    if (what & ADV_TH) out[2] = s_north(p, F, F.cur[FTH], F.bar[3], i, j, k);
+    if (what & ADV_Q) {
+        out[3] = s_north(p, F, F.cur[FQV], F.bar[4], i, j, k);
+        out[4] = s_north(p, F, F.cur[FQC], (const T *)nullptr, i, j, k);
+        out[5] = s_north(p, F, F.cur[FQR], (const T *)nullptr, i, j, k);
+    }
+}
+template <typename T>
+__device__ __forceinline__ void faces_top(const KParams<T> &p, const KFields<T> &F, int what, int i, int j, int k,
+                                          T *out)
+{
+    if (what & ADV_UV) {
+        out[0] = u_top(p, F, i, j, k);
+        out[1] = v_top(p, F, i, j, k);
+    }
+    if (what & ADV_TH) out[2] = s_top(p, F, F.cur[FTH], F.bar[3], i, j, k);
+    if (what & ADV_Q) {
+        out[3] = s_top(p, F, F.cur[FQV], F.bar[4], i, j, k);
+        out[4] = s_top(p, F, F.cur[FQC], (const T *)nullptr, i, j, k);
+        out[5] = r_top(p, F, i, j, k);
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_advect_tile(KParams<T> p, KFields<T> F, T step, T sdtg, int what)
+{
+    extern __shared__ unsigned char smem_raw[];
+    const int TI = ADV_TI, TJ = ADV_TJ, NF = ADV_NF;
+    const int nz = p.nz, nzi = nz - 2;
+    const int i0 = 3 + blockIdx.x * TI, j0 = 3 + blockIdx.y * TJ;
+    const int ti = min(TI, p.nx - 3 - i0), tj = min(TJ, p.ny - 3 - j0);
+    // face stores, each [field][...][level k = 0..nz-1]
+    T *E = (T *)smem_raw;                    // [(TI+1)][TJ] columns, east face of column i0-1+a
+    T *Nf = E + NF * (TI + 1) * TJ * nz;      // [TI][(TJ+1)] columns, north face of column j0-1+b
+    T *Tf = Nf + NF * TI * (TJ + 1) * nz;     // [TI][TJ] columns, top face at level k
+    const int sE = (TI + 1) * TJ * nz, sN = TI * (TJ + 1) * nz, sT = TI * TJ * nz;
+    T tmp[NF];
+    // phase 1a: east faces of columns i0-1 .. i0+ti-1
+    for (int w = threadIdx.x; w < (TI + 1) * TJ * nzi; w += blockDim.x) {
+        const int kk = w % nzi, c = w / nzi, b = c % TJ, a = c / TJ;
+        if (a > ti || b >= tj) continue;
+        faces_east(p, F, what, i0 - 1 + a, j0 + b, 1 + kk, tmp);
+        const int o = (a * TJ + b) * nz + 1 + kk;
+#pragma unroll
+        for (int f = 0; f < NF; f++) E[f * sE + o] = tmp[f];
+    }
+    // phase 1b: north faces of rows j0-1 .. j0+tj-1
+    for (int w = threadIdx.x; w < TI * (TJ + 1) * nzi; w += blockDim.x) {
+        const int kk = w % nzi, c = w / nzi, b = c % (TJ + 1), a = c / (TJ + 1);
+        if (a >= ti || b > tj) continue;
+        faces_north(p, F, what, i0 + a, j0 - 1 + b, 1 + kk, tmp);
+        const int o = (a * (TJ + 1) + b) * nz + 1 + kk;
+#pragma unroll
+        for (int f = 0; f < NF; f++) Nf[f * sN + o] = tmp[f];
+    }
+    // phase 1c: top faces at levels 0 .. nz-2
+    for (int w = threadIdx.x; w < TI * TJ * (nz - 1); w += blockDim.x) {
+        const int k = w % (nz - 1), c = w / (nz - 1), b = c % TJ, a = c / TJ;
+        if (a >= ti || b >= tj) continue;
+        faces_top(p, F, what, i0 + a, j0 + b, k, tmp);
+        const int o = (a * TJ + b) * nz + k;
+#pragma unroll
+        for (int f = 0; f < NF; f++) Tf[f * sT + o] = tmp[f];
+    }
+    __syncthreads();
+    // phase 2: tendencies
+    for (int w = threadIdx.x; w < TI * TJ * nzi; w += blockDim.x) {
+        const int kk = w % nzi, c = w / nzi, b = c % TJ, a = c / TJ;
+        if (a >= ti || b >= tj) continue;
+        const int i = i0 + a, j = j0 + b, k = 1 + kk;
+        const int cix = gix(p.ny, nz, i, j, k);
+        const T DTZ = p.dtz * p.mu[k];
+        const int oe = ((a + 1) * TJ + b) * nz + k, ow = (a * TJ + b) * nz + k;
+        const int on = (a * (TJ + 1) + b + 1) * nz + k, os = (a * (TJ + 1) + b) * nz + k;
+        const int ot = (a * TJ + b) * nz + k;
+        if (what & ADV_UV) {
+            const T *U = F.cur[FU], *V = F.cur[FV];
+            const int sy = nz, sx = p.ny * nz;
+            T ov_u = T(0.25) * (LD(V, cix) + LD(V, cix + sy) + LD(V, cix - sx) + LD(V, cix - sx + sy));
+            T ut = -p.dtx * (E[oe] - E[ow]) - p.dty * (Nf[on] - Nf[os]) -
+                   DTZ * (p.rhow[k + 1] * Tf[ot] - p.rhow[k] * Tf[ot - 1]) * p.one_d_rhou[k] +
+                   p.dt * p.f[j] * ov_u;
+            F.P[FU][cix] = LD(F.M[FU], cix) + step * ut;
+            T ov_v = T(0.25) * (LD(U, cix) + LD(U, cix + sx) + LD(U, cix - sy) + LD(U, cix + sx - sy));
+            T vt = -p.dtx * (E[sE + oe] - E[sE + ow]) - p.dty * (Nf[sN + on] - Nf[sN + os]) -
+                   DTZ * (p.rhow[k + 1] * Tf[sT + ot] - p.rhow[k] * Tf[sT + ot - 1]) * p.one_d_rhou[k] -
+                   p.dt * p.f[j] * ov_v;
+            F.P[FV][cix] = LD(F.M[FV], cix) + step * vt;
+        }
+        if ((what & ADV_WB) && k >= 2) {
+            const T *TH = F.cur[FTH];
+            T b0, b1;
+            if (!p.moist) {
+                b0 = LD(TH, cix) / p.tbv[k];
+                b1 = LD(TH, cix - 1) / p.tbv[k - 1];
+            } else {
+                const T *QV = F.cur[FQV], *QC = F.cur[FQC], *QR = F.cur[FQR];
+                b0 = LD(TH, cix) / p.tbv[k] + T(0.61) * LD(QV, cix) - LD(QC, cix) - LD(QR, cix);
+                b1 = LD(TH, cix - 1) / p.tbv[k - 1] + T(0.61) * LD(QV, cix - 1) - LD(QC, cix - 1) - LD(QR, cix - 1);
+            }
+            F.P[FW][cix] = LD(F.M[FW], cix) + sdtg * (b0 + b1);
+        }
+        auto tend = [&](int f) {
+            return -p.dtx * (E[f * sE + oe] - E[f * sE + ow]) - p.dty * (Nf[f * sN + on] - Nf[f * sN + os]) -
+                   DTZ * (p.rhow[k + 1] * Tf[f * sT + ot] - p.rhow[k] * Tf[f * sT + ot - 1]) * p.one_d_rhou[k];
+        };
+        const T *Wc = F.cur[FW];
+        if (what & ADV_TH) {
+            T t = tend(2);
+            T zab = T(0.50) *
+                    (p.rhow[k + 1] * LD(Wc, cix + 1) * (p.tb[k + 1] - p.tb[k]) +
+                     p.rhow[k] * LD(Wc, cix) * (p.tb[k] - p.tb[k - 1])) *
+                    p.one_d_rhou[k];
+            t = t - DTZ * zab;
+            F.P[FTH][cix] = LD(F.M[FTH], cix) + step * t;
+        }
+        if (what & ADV_Q) {
+            if (p.rf == 1) {
+                const T *QR = F.cur[FQR];
+                F.vt[cix] = fall_speed_point(p, LD(QR, cix), k);
+                if (k == 1) F.vt[cix - 1] = fall_speed_point(p, LD(QR, cix), 1);
+            }
+            T tv = tend(3);
+            T zab = T(0.50) *
+                    (p.rhow[k + 1] * LD(Wc, cix + 1) * (p.qb[k + 1] - p.qb[k]) +
+                     p.rhow[k] * LD(Wc, cix) * (p.qb[k] - p.qb[k - 1])) *
+                    p.one_d_rhou[k];
+            tv = tv - DTZ * zab;
+            T qv = LD(F.M[FQV], cix) + step * tv;
+            T qc = LD(F.M[FQC], cix) + step * tend(4);
+            T qr = LD(F.M[FQR], cix) + step * tend(5);
+            if (what & ADV_ZERO) {
+                if (qc < 0) qc = 0;
+                if (qr < 0) qr = 0;
+                T qbar = LD(F.bar[4], cix);
+                if (qv + qbar + p.qb[k] < 0) qv = -(qbar + p.qb[k]);
+            }
+            F.P[FQV][cix] = qv;
+            F.P[FQC][cix] = qc;
+            F.P[FQR][cix] = qr;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // lateral copies of UP/VP/WP before the pressure solve:
 // mirror_boundaries (boundaries.cpp:363-379) or periodic_uvw_boundaries
 // (:546-555).  Writes only edge points, reads only non-edge points.
@@ -479,12 +656,12 @@ __device__ __forceinline__ T2 twid(const T2 *tw, int t, bool inv)
     return w;
 }
 
-// L lines; lg2L = log2(L) when L is a power of two (shift indexing), else -1.
-// Element (point n, line l) lives at buf[n*ps + l]; ps >= L (padding keeps a
-// thread that walks one line across points off a single bank).
+// Batched shared-memory FFT.  L lines; element (point n, line l) lives at
+// buf[n*ps + l] with ps >= L (padding keeps a thread that walks one line
+// across points off a single bank).  Threads are 2-D: x runs over lines,
+// y over the butterflies of a pass, so no index needs a division by L.
 template <typename T, typename T2>
-__device__ T2 *fft_smem(T2 *a, T2 *b, int L, int lg2L, const FftPlan &P, const T2 *__restrict__ tw, bool inv,
-                        int ps)
+__device__ T2 *fft_smem(T2 *a, T2 *b, int L, const FftPlan &P, const T2 *__restrict__ tw, bool inv, int ps)
 {
     const int N = P.n;
     int Ns = 1;
@@ -493,64 +670,63 @@ __device__ T2 *fft_smem(T2 *a, T2 *b, int L, int lg2L, const FftPlan &P, const T
         const int nb = N / R;
         const int ts = N / (Ns * R);
         const int nsl = P.nslog[f];
-        for (int w = threadIdx.x; w < nb * L; w += blockDim.x) {
-            int l, j;
-            if (lg2L >= 0) { l = w & (L - 1); j = w >> lg2L; }
-            else { l = w % L; j = w / L; }
+        for (int j = threadIdx.y; j < nb; j += blockDim.y) {
             int k, jb;
             if (nsl >= 0) { k = j & (Ns - 1); jb = j >> nsl; }
             else { k = j % Ns; jb = j / Ns; }
             const int ob = jb * Ns * R + k;
-            if (R == 2) {
-                T2 v0 = a[j * ps + l];
-                T2 v1 = a[(j + nb) * ps + l];
-                if (k) v1 = cmul(v1, twid(tw, k * ts, inv));
-                T2 s, d;
-                s.x = v0.x + v1.x; s.y = v0.y + v1.y;
-                d.x = v0.x - v1.x; d.y = v0.y - v1.y;
-                b[ob * ps + l] = s;
-                b[(ob + Ns) * ps + l] = d;
-            } else if (R == 4) {
-                T2 v0 = a[j * ps + l];
-                T2 v1 = a[(j + nb) * ps + l];
-                T2 v2 = a[(j + 2 * nb) * ps + l];
-                T2 v3 = a[(j + 3 * nb) * ps + l];
-                if (k) {
-                    v1 = cmul(v1, twid(tw, k * ts, inv));
-                    v2 = cmul(v2, twid(tw, 2 * k * ts, inv));
-                    v3 = cmul(v3, twid(tw, 3 * k * ts, inv));
-                }
-                T2 s02, d02, s13, d13, x0, x1, x2, x3;
-                s02.x = v0.x + v2.x; s02.y = v0.y + v2.y;
-                d02.x = v0.x - v2.x; d02.y = v0.y - v2.y;
-                s13.x = v1.x + v3.x; s13.y = v1.y + v3.y;
-                d13.x = v1.x - v3.x; d13.y = v1.y - v3.y;
-                x0.x = s02.x + s13.x; x0.y = s02.y + s13.y;
-                x2.x = s02.x - s13.x; x2.y = s02.y - s13.y;
-                if (!inv) {  // X1 = d02 - i d13, X3 = d02 + i d13
-                    x1.x = d02.x + d13.y; x1.y = d02.y - d13.x;
-                    x3.x = d02.x - d13.y; x3.y = d02.y + d13.x;
-                } else {
-                    x1.x = d02.x - d13.y; x1.y = d02.y + d13.x;
-                    x3.x = d02.x + d13.y; x3.y = d02.y - d13.x;
-                }
-                b[ob * ps + l] = x0;
-                b[(ob + Ns) * ps + l] = x1;
-                b[(ob + 2 * Ns) * ps + l] = x2;
-                b[(ob + 3 * Ns) * ps + l] = x3;
-            } else {  // generic radix: direct R-point DFT with combined twiddles
-                for (int m = 0; m < R; ++m) {
-                    T2 acc;
-                    acc.x = T(0);
-                    acc.y = T(0);
-                    for (int r = 0; r < R; ++r) {
-                        const int t = (k * r * ts + ((r * m) % R) * nb) % N;
-                        T2 x = a[(j + r * nb) * ps + l];
-                        T2 wv = twid(tw, t, inv);
-                        acc.x += x.x * wv.x - x.y * wv.y;
-                        acc.y += x.x * wv.y + x.y * wv.x;
+            for (int l = threadIdx.x; l < L; l += blockDim.x) {
+                if (R == 2) {
+                    T2 v0 = a[j * ps + l];
+                    T2 v1 = a[(j + nb) * ps + l];
+                    if (k) v1 = cmul(v1, twid(tw, k * ts, inv));
+                    T2 s, d;
+                    s.x = v0.x + v1.x; s.y = v0.y + v1.y;
+                    d.x = v0.x - v1.x; d.y = v0.y - v1.y;
+                    b[ob * ps + l] = s;
+                    b[(ob + Ns) * ps + l] = d;
+                } else if (R == 4) {
+                    T2 v0 = a[j * ps + l];
+                    T2 v1 = a[(j + nb) * ps + l];
+                    T2 v2 = a[(j + 2 * nb) * ps + l];
+                    T2 v3 = a[(j + 3 * nb) * ps + l];
+                    if (k) {
+                        v1 = cmul(v1, twid(tw, k * ts, inv));
+                        v2 = cmul(v2, twid(tw, 2 * k * ts, inv));
+                        v3 = cmul(v3, twid(tw, 3 * k * ts, inv));
                     }
-                    b[(ob + m * Ns) * ps + l] = acc;
+                    T2 s02, d02, s13, d13, x0, x1, x2, x3;
+                    s02.x = v0.x + v2.x; s02.y = v0.y + v2.y;
+                    d02.x = v0.x - v2.x; d02.y = v0.y - v2.y;
+                    s13.x = v1.x + v3.x; s13.y = v1.y + v3.y;
+                    d13.x = v1.x - v3.x; d13.y = v1.y - v3.y;
+                    x0.x = s02.x + s13.x; x0.y = s02.y + s13.y;
+                    x2.x = s02.x - s13.x; x2.y = s02.y - s13.y;
+                    if (!inv) {  // X1 = d02 - i d13, X3 = d02 + i d13
+                        x1.x = d02.x + d13.y; x1.y = d02.y - d13.x;
+                        x3.x = d02.x - d13.y; x3.y = d02.y + d13.x;
+                    } else {
+                        x1.x = d02.x - d13.y; x1.y = d02.y + d13.x;
+                        x3.x = d02.x + d13.y; x3.y = d02.y - d13.x;
+                    }
+                    b[ob * ps + l] = x0;
+                    b[(ob + Ns) * ps + l] = x1;
+                    b[(ob + 2 * Ns) * ps + l] = x2;
+                    b[(ob + 3 * Ns) * ps + l] = x3;
+                } else {  // generic radix: direct R-point DFT with combined twiddles
+                    for (int m = 0; m < R; ++m) {
+                        T2 acc;
+                        acc.x = T(0);
+                        acc.y = T(0);
+                        for (int r = 0; r < R; ++r) {
+                            const int t = (k * r * ts + ((r * m) % R) * nb) % N;
+                            T2 x = a[(j + r * nb) * ps + l];
+                            T2 wv = twid(tw, t, inv);
+                            acc.x += x.x * wv.x - x.y * wv.y;
+                            acc.y += x.x * wv.y + x.y * wv.x;
+                        }
+                        b[(ob + m * Ns) * ps + l] = acc;
+                    }
                 }
             }
         }
@@ -582,11 +758,10 @@ __device__ __forceinline__ T divergence(const KParams<T> &p, const KFields<T> &F
 // tile of KT levels starting at level 1).
 template <typename T>
 __global__ void k_div_fft_y(KParams<T> p, KFields<T> F, typename V2<T>::t *spec, FftPlan pj,
-                            const typename V2<T>::t *tw, T sdt, int lgKT)
+                            const typename V2<T>::t *tw, T sdt, int KT)
 {
     typedef typename V2<T>::t T2;
     extern __shared__ unsigned char smem_raw[];
-    const int KT = 1 << lgKT;
     T2 *a = (T2 *)smem_raw;
     T2 *b = a + (long)p.nj * KT;
     const int is = blockIdx.x;
@@ -595,53 +770,50 @@ __global__ void k_div_fft_y(KParams<T> p, KFields<T> F, typename V2<T>::t *spec,
     int ii;
     if (!p.periodic) ii = min(max(is, 1), p.nx - 2);
     else ii = is + 3;
-    for (int w = threadIdx.x; w < p.nj * KT; w += blockDim.x) {
-        const int l = w & (KT - 1), q = w >> lgKT;
-        T2 v;
-        v.y = T(0);
-        v.x = T(0);
-        if (l < kt) {
-            const int jj = min(max(q, 1), p.ny - 2);
-            v.x = divergence(p, F, ii, jj, k0 + l, sdt);
+    for (int q = threadIdx.y; q < p.nj; q += blockDim.y)
+        for (int l = threadIdx.x; l < KT; l += blockDim.x) {
+            T2 v;
+            v.y = T(0);
+            v.x = T(0);
+            if (l < kt) {
+                const int jj = min(max(q, 1), p.ny - 2);
+                v.x = divergence(p, F, ii, jj, k0 + l, sdt);
+            }
+            a[q * KT + l] = v;
         }
-        a[w] = v;
-    }
     __syncthreads();
-    T2 *r = fft_smem<T, T2>(a, b, KT, lgKT, pj, tw, false, KT);
-    for (int w = threadIdx.x; w < p.nj * KT; w += blockDim.x) {
-        const int l = w & (KT - 1), q = w >> lgKT;
-        if (l < kt) spec[((long)is * p.nj + q) * p.nz + k0 + l] = r[w];
-    }
+    T2 *r = fft_smem<T, T2>(a, b, KT, pj, tw, false, KT);
+    for (int q = threadIdx.y; q < p.nj; q += blockDim.y)
+        for (int l = threadIdx.x; l < kt; l += blockDim.x)
+            spec[((long)is * p.nj + q) * p.nz + k0 + l] = r[q * KT + l];
 }
 
 // FFT along x of the spectral buffer for one y-wavenumber q and a tile of
 // levels.  sign: forward (false) or inverse (true).
 template <typename T>
 __global__ void k_fft_x(KParams<T> p, typename V2<T>::t *spec, FftPlan pi, const typename V2<T>::t *tw,
-                        int inv, int lgKT)
+                        int inv, int KT)
 {
     typedef typename V2<T>::t T2;
     extern __shared__ unsigned char smem_raw[];
-    const int KT = 1 << lgKT;
     T2 *a = (T2 *)smem_raw;
     T2 *b = a + (long)p.ni * KT;
     const int q = blockIdx.x;
     const int k0 = 1 + blockIdx.y * KT;
     const int kt = min(KT, p.nz - 1 - k0);
-    for (int w = threadIdx.x; w < p.ni * KT; w += blockDim.x) {
-        const int l = w & (KT - 1), i = w >> lgKT;
-        T2 v;
-        v.x = T(0);
-        v.y = T(0);
-        if (l < kt) v = spec[((long)i * p.nj + q) * p.nz + k0 + l];
-        a[w] = v;
-    }
+    for (int i = threadIdx.y; i < p.ni; i += blockDim.y)
+        for (int l = threadIdx.x; l < KT; l += blockDim.x) {
+            T2 v;
+            v.x = T(0);
+            v.y = T(0);
+            if (l < kt) v = spec[((long)i * p.nj + q) * p.nz + k0 + l];
+            a[i * KT + l] = v;
+        }
     __syncthreads();
-    T2 *r = fft_smem<T, T2>(a, b, KT, lgKT, pi, tw, inv != 0, KT);
-    for (int w = threadIdx.x; w < p.ni * KT; w += blockDim.x) {
-        const int l = w & (KT - 1), i = w >> lgKT;
-        if (l < kt) spec[((long)i * p.nj + q) * p.nz + k0 + l] = r[w];
-    }
+    T2 *r = fft_smem<T, T2>(a, b, KT, pi, tw, inv != 0, KT);
+    for (int i = threadIdx.y; i < p.ni; i += blockDim.y)
+        for (int l = threadIdx.x; l < kt; l += blockDim.x)
+            spec[((long)i * p.nj + q) * p.nz + k0 + l] = r[i * KT + l];
 }
 
 // normalisation (pressure.cpp:827) + Thomas algorithm per horizontal
@@ -697,11 +869,108 @@ __device__ void thomas_column(const KParams<T> &p, typename V2<T>::t *x, A *Fw, 
     }
 }
 
+// FP32 Thomas solve of one wavenumber: the reference recurrence
+// (pressure.cpp:834-871) with the horizontal term of the diagonal hoisted and
+// one reciprocal per level instead of three divisions.
+__device__ __forceinline__ void thomas_column_fast(float2 *x, float *Fw, int nz, float hb, float inv_size2d,
+                                                   const float *rhou, const float *ac, const float *cc,
+                                                   const float *vc, bool gauge)
+{
+    float z = __frcp_rn(rhou[1] * hb - vc[1]);
+    float Fk = cc[1] * z;
+    Fw[1] = Fk;
+    float xr = x[1].x * inv_size2d * z, xi = x[1].y * inv_size2d * z;
+    x[1] = make_float2(xr, xi);
+    for (int k = 2; k < nz - 1; k++) {
+        z = __frcp_rn(rhou[k] * hb - vc[k] - ac[k] * Fk);
+        Fk = cc[k] * z;
+        Fw[k] = Fk;
+        xr = (x[k].x * inv_size2d - ac[k] * xr) * z;
+        xi = (x[k].y * inv_size2d - ac[k] * xi) * z;
+        x[k] = make_float2(xr, xi);
+    }
+    if (gauge) { xr = 0.f; xi = 0.f; x[nz - 2] = make_float2(0.f, 0.f); }
+    for (int k = nz - 3; k >= 1; k--) {
+        xr = x[k].x - Fw[k] * xr;
+        xi = x[k].y - Fw[k] * xi;
+        x[k] = make_float2(xr, xi);
+    }
+}
+
+// FP64 solve of one wavenumber by parallel cyclic reduction across a warp
+// (rows 1..nl in shared memory, log2(nl) reduction steps, every row at once)
+// for the near-singular low wavenumbers of FP32 contexts.  For the mean mode
+// (gauge) the last row is replaced by x = 0, which is what the reference's
+// pinning after forward elimination (pressure.cpp:858-859) amounts to.
+template <typename T2>
+__device__ void pcr_column_f64(T2 *x, int nl, double hcol, double dx2, double size2d, const double *rhou,
+                               const double *ac, const double *cc, const double *vc, bool gauge, double *wk)
+{
+    // wk: 2 buffers x 5 arrays x 64 rows (a, b, c, dr, di).  Blocks may be
+    // 2-D, so the lane comes from the linear thread index.
+    const int lane = (threadIdx.y * blockDim.x + threadIdx.x) & 31;
+    double *A0 = wk, *B0 = wk + 64, *C0 = wk + 128, *R0 = wk + 192, *I0 = wk + 256;
+    double *A1 = wk + 320, *B1 = wk + 384, *C1 = wk + 448, *R1 = wk + 512, *I1 = wk + 576;
+    for (int r = lane; r < 64; r += 32) {
+        if (r < nl) {
+            const int k = r + 1;
+            double a = ac[k], c = cc[k];
+            double b = rhou[k] * 2.0 * hcol / dx2 - vc[k];
+            double dr = (double)x[k].x / size2d, di = (double)x[k].y / size2d;
+            if (gauge && r == nl - 1) { a = 0.0; b = 1.0; c = 0.0; dr = 0.0; di = 0.0; }
+            A0[r] = a; B0[r] = b; C0[r] = c; R0[r] = dr; I0[r] = di;
+        }
+    }
+    __syncwarp();
+    for (int s = 1; s < nl; s <<= 1) {
+        for (int r = lane; r < nl; r += 32) {
+            double a = A0[r], b = B0[r], c = C0[r], dr = R0[r], di = I0[r];
+            double na = 0.0, nc = 0.0;
+            if (r - s >= 0) {
+                const double al = -a / B0[r - s];
+                na = al * A0[r - s];
+                b += al * C0[r - s];
+                dr += al * R0[r - s];
+                di += al * I0[r - s];
+            }
+            if (r + s < nl) {
+                const double ga = -c / B0[r + s];
+                nc = ga * C0[r + s];
+                b += ga * A0[r + s];
+                dr += ga * R0[r + s];
+                di += ga * I0[r + s];
+            }
+            A1[r] = na; B1[r] = b; C1[r] = nc; R1[r] = dr; I1[r] = di;
+        }
+        __syncwarp();
+        double *t;
+        t = A0; A0 = A1; A1 = t; t = B0; B0 = B1; B1 = t; t = C0; C0 = C1; C1 = t;
+        t = R0; R0 = R1; R1 = t; t = I0; I0 = I1; I1 = t;
+    }
+    for (int r = lane; r < nl; r += 32) {
+        T2 v;
+        v.x = (decltype(v.x))(R0[r] / B0[r]);
+        v.y = (decltype(v.y))(I0[r] / B0[r]);
+        x[r + 1] = v;
+    }
+    __syncwarp();
+}
+
+// true for the low horizontal wavenumbers solved in FP64 in FP32 contexts
+template <typename T>
+__device__ __forceinline__ bool low_mode(const KParams<T> &p, long col)
+{
+    if (p.low_modes <= 0) return false;
+    const int pp = (int)(col / p.nj), qq = (int)(col % p.nj);
+    return min(pp, p.ni - pp) < p.low_modes && min(qq, p.nj - qq) < p.low_modes;
+}
+
 template <typename T>
 __global__ void k_thomas(KParams<T> p, typename V2<T>::t *spec, int TC)
 {
     typedef typename V2<T>::t T2;
     extern __shared__ unsigned char smem_raw[];
+    __shared__ double pcr_wk[2][640];
     const int cs = p.nz | 1;  // odd column stride: no bank conflicts between columns
     T2 *xs = (T2 *)smem_raw;
     T *fs = (T *)(xs + (long)TC * cs);
@@ -714,73 +983,98 @@ __global__ void k_thomas(KParams<T> p, typename V2<T>::t *spec, int TC)
     const double size2d = (double)(p.ni * p.nj);
     for (int c = threadIdx.x; c < nc; c += blockDim.x) {
         const long col = c0 + c;
-        const int pp = (int)(col / p.nj), qq = (int)(col % p.nj);
-        bool low = false;
-        if (p.low_modes > 0) {
-            int ap = min(pp, p.ni - pp), aq = min(qq, p.nj - qq);
-            low = ap < p.low_modes && aq < p.low_modes;
-        }
-        if (low) {
+        if (sizeof(T) == 8) {
             double Floc[PPM_MAXZ];
-            thomas_column<T, double>(p, xs + (long)c * cs, Floc, col, size2d, p.rhou_d, p.acoef_d,
-                                     p.ccoef_d, p.vcoef_d);
-        } else
-            thomas_column<T, T>(p, xs + (long)c * cs, fs + (long)c * cs, col, size2d, p.rhou, p.acoef,
-                                p.ccoef, p.vcoef);
+            thomas_column<T, double>(p, xs + (long)c * cs, Floc, col, size2d, p.rhou_d, p.acoef_d, p.ccoef_d,
+                                     p.vcoef_d);
+        } else if (!low_mode(p, col)) {
+            const float hb = 2.0f * (float)p.hcoef[col] / (float)p.dx2;
+            thomas_column_fast((float2 *)(xs + (long)c * cs), (float *)(fs + (long)c * cs), p.nz, hb,
+                               (float)(1.0 / size2d), (const float *)p.rhou, (const float *)p.acoef,
+                               (const float *)p.ccoef, (const float *)p.vcoef, col == 0);
+        }
+    }
+    if (sizeof(T) != 8 && p.low_modes > 0) {
+        const int warp = threadIdx.x >> 5;
+        if (warp < 2 && (int)blockDim.x >= 64) {
+            int n = 0;
+            for (int c = 0; c < nc; c++) {
+                const long col = c0 + c;
+                if (!low_mode(p, col)) continue;
+                if ((n++ & 1) != warp) continue;
+                pcr_column_f64(xs + (long)c * cs, p.nz - 2, p.hcoef[col], p.dx2, size2d, p.rhou_d, p.acoef_d,
+                               p.ccoef_d, p.vcoef_d, col == 0, pcr_wk[warp]);
+            }
+        }
     }
     __syncthreads();
     for (int w = threadIdx.x; w < nc * p.nz; w += blockDim.x) g[w] = xs[(w / p.nz) * cs + w % p.nz];
 }
 
-// Forward FFT along x, normalisation + Thomas solve per wavenumber, inverse
-// FFT along x, for one y-wavenumber q with every level 1..NZ-2 resident in
-// shared memory (lines padded to a power of two).  After the forward pass
-// the other ping-pong buffer is free and holds the Thomas coefficients.
 template <typename T>
 __global__ void k_spectral_x(KParams<T> p, typename V2<T>::t *spec, FftPlan pi, const typename V2<T>::t *tw,
-                             int L, int lgL, int ps)
+                             int ps)
 {
     typedef typename V2<T>::t T2;
     extern __shared__ unsigned char smem_raw[];
+    __shared__ T c_r[PPM_MAXZ], c_a[PPM_MAXZ], c_c[PPM_MAXZ], c_v[PPM_MAXZ];
+    __shared__ double d_r[PPM_MAXZ], d_a[PPM_MAXZ], d_c[PPM_MAXZ], d_v[PPM_MAXZ];
+    __shared__ double pcr_wk[2][640];
     T2 *a = (T2 *)smem_raw;
     T2 *b = a + (long)p.ni * ps;
     const int q = blockIdx.x;
-    const int nl = p.nz - 2;  // levels 1..NZ-2
-    for (int w = threadIdx.x; w < p.ni * L; w += blockDim.x) {
-        const int l = lgL >= 0 ? (w & (L - 1)) : (w % L), i = lgL >= 0 ? (w >> lgL) : (w / L);
-        T2 v;
-        v.x = T(0);
-        v.y = T(0);
-        if (l < nl) v = spec[((long)i * p.nj + q) * p.nz + 1 + l];
-        a[i * ps + l] = v;
+    const int nl = p.nz - 2;  // levels 1..NZ-2 are the lines
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x, nth = blockDim.x * blockDim.y;
+    for (int k = tid; k < p.nz; k += nth) {
+        c_r[k] = p.rhou[k]; c_a[k] = p.acoef[k]; c_c[k] = p.ccoef[k]; c_v[k] = p.vcoef[k];
+        d_r[k] = p.rhou_d[k]; d_a[k] = p.acoef_d[k]; d_c[k] = p.ccoef_d[k]; d_v[k] = p.vcoef_d[k];
     }
+    for (int i = threadIdx.y; i < p.ni; i += blockDim.y)
+        for (int l = threadIdx.x; l < nl; l += blockDim.x) a[i * ps + l] = spec[((long)i * p.nj + q) * p.nz + 1 + l];
     __syncthreads();
-    T2 *r = fft_smem<T, T2>(a, b, L, lgL, pi, tw, false, ps);
-    T2 *fr = (r == a) ? b : a;  // free buffer
+    T2 *r = fft_smem<T, T2>(a, b, nl, pi, tw, false, ps);
+    T2 *fr = (r == a) ? b : a;  // free buffer: holds the Thomas coefficients
     const double size2d = (double)(p.ni * p.nj);
-    for (int pp = threadIdx.x; pp < p.ni; pp += blockDim.x) {
-        const long col = (long)pp * p.nj + q;
-        // x is indexed by level k at x[k]: column pp holds levels 1..NZ-2 at r[pp*L + k-1]
-        T2 *x = r + (long)pp * ps - 1;
-        bool low = false;
-        if (p.low_modes > 0) {
-            const int ap = min(pp, p.ni - pp), aq = min(q, p.nj - q);
-            low = ap < p.low_modes && aq < p.low_modes;
-        }
-        if (low || sizeof(T) == 8) {
+    const int aq = min(q, p.nj - q);
+    const bool q_low = p.low_modes > 0 && aq < p.low_modes;
+    if (sizeof(T) == 8) {  // parity path: the reference's Thomas recurrence in FP64
+        for (int pp = tid; pp < p.ni; pp += nth) {
+            const long col = (long)pp * p.nj + q;
             double *Fw = (double *)(fr + (long)pp * ps) - 1;
-            thomas_column<T, double>(p, x, Fw, col, size2d, p.rhou_d, p.acoef_d, p.ccoef_d, p.vcoef_d);
-        } else {
-            T *Fw = (T *)(fr + (long)pp * ps) - 1;
-            thomas_column<T, T>(p, x, Fw, col, size2d, p.rhou, p.acoef, p.ccoef, p.vcoef);
+            thomas_column<T, double>(p, r + (long)pp * ps - 1, Fw, col, size2d, d_r, d_a, d_c, d_v);
+        }
+    } else {
+        const float dx2 = (float)p.dx2, inv_s = (float)(1.0 / size2d);
+        for (int pp = tid; pp < p.ni; pp += nth) {
+            const int ap = min(pp, p.ni - pp);
+            if (q_low && ap < p.low_modes) continue;  // FP64 islands below
+            const long col = (long)pp * p.nj + q;
+            const float hb = 2.0f * (float)p.hcoef[col] / dx2;
+            float *Fw = (float *)(fr + (long)pp * ps) - 1;
+            thomas_column_fast((float2 *)(r + (long)pp * ps - 1), Fw, p.nz, hb, inv_s, (const float *)c_r,
+                               (const float *)c_a, (const float *)c_c, (const float *)c_v, col == 0);
+        }
+        if (q_low) {  // low (p,q) wavenumbers: FP64 by warp PCR on warps 0 and 1
+            const int warp = tid >> 5;
+            if (warp < 2) {
+                int islands[16], nis = 0;
+                for (int pp = 0; pp < p.low_modes && nis < 15; pp++) {
+                    islands[nis++] = pp;
+                    if (pp > 0) islands[nis++] = p.ni - pp;
+                }
+                for (int w = warp; w < nis; w += 2) {
+                    const int pp = islands[w];
+                    const long col = (long)pp * p.nj + q;
+                    pcr_column_f64(r + (long)pp * ps - 1, nl, p.hcoef[col], p.dx2, size2d, d_r, d_a, d_c, d_v,
+                                   col == 0, pcr_wk[warp]);
+                }
+            }
         }
     }
     __syncthreads();
-    T2 *o = fft_smem<T, T2>(r, fr, L, lgL, pi, tw, true, ps);
-    for (int w = threadIdx.x; w < p.ni * L; w += blockDim.x) {
-        const int l = lgL >= 0 ? (w & (L - 1)) : (w % L), i = lgL >= 0 ? (w >> lgL) : (w / L);
-        if (l < nl) spec[((long)i * p.nj + q) * p.nz + 1 + l] = o[i * ps + l];
-    }
+    T2 *o = fft_smem<T, T2>(r, fr, nl, pi, tw, true, ps);
+    for (int i = threadIdx.y; i < p.ni; i += blockDim.y)
+        for (int l = threadIdx.x; l < nl; l += blockDim.x) spec[((long)i * p.nj + q) * p.nz + 1 + l] = o[i * ps + l];
 }
 
 // inverse FFT along y + PI = real part, with the level copies of
@@ -788,31 +1082,30 @@ __global__ void k_spectral_x(KParams<T> p, typename V2<T>::t *spec, FftPlan pi, 
 // mirror_boundaries(PI) or periodic_pressure_boundaries.
 template <typename T>
 __global__ void k_ifft_y_pi(KParams<T> p, KFields<T> F, typename V2<T>::t *spec, FftPlan pj,
-                            const typename V2<T>::t *tw, int lgKT)
+                            const typename V2<T>::t *tw, int KT)
 {
     typedef typename V2<T>::t T2;
     extern __shared__ unsigned char smem_raw[];
-    const int KT = 1 << lgKT;
     T2 *a = (T2 *)smem_raw;
     T2 *b = a + (long)p.nj * KT;
     const int is = blockIdx.x;
     const int k0 = 1 + blockIdx.y * KT;
     const int kt = min(KT, p.nz - 1 - k0);
-    for (int w = threadIdx.x; w < p.nj * KT; w += blockDim.x) {
-        const int l = w & (KT - 1), q = w >> lgKT;
-        T2 v;
-        v.x = T(0);
-        v.y = T(0);
-        if (l < kt) v = spec[((long)is * p.nj + q) * p.nz + k0 + l];
-        a[w] = v;
-    }
+    for (int q = threadIdx.y; q < p.nj; q += blockDim.y)
+        for (int l = threadIdx.x; l < KT; l += blockDim.x) {
+            T2 v;
+            v.x = T(0);
+            v.y = T(0);
+            if (l < kt) v = spec[((long)is * p.nj + q) * p.nz + k0 + l];
+            a[q * KT + l] = v;
+        }
     __syncthreads();
-    T2 *r = fft_smem<T, T2>(a, b, KT, lgKT, pj, tw, true, KT);
+    T2 *r = fft_smem<T, T2>(a, b, KT, pj, tw, true, KT);
     T *PI = F.pi;
     const int nz = p.nz, ny = p.ny;
-    for (int w = threadIdx.x; w < p.nj * KT; w += blockDim.x) {
-        const int l = w & (KT - 1), j = w >> lgKT;
-        if (l >= kt) continue;
+    for (int j = threadIdx.y; j < p.nj; j += blockDim.y)
+      for (int l = threadIdx.x; l < kt; l += blockDim.x) {
+        const int w = j * KT + l;
         const int k = k0 + l;
         if (!p.periodic) {
             const int i = is;
@@ -894,88 +1187,128 @@ __device__ __forceinline__ T chain_value(const KParams<T> &p, const KFields<T> &
     return v;
 }
 
-template <typename T>
-__global__ void __launch_bounds__(256) k_post(KParams<T> p, KFields<T> F, int nfields, int4 fl0, int4 fl1, T step,
-                                              int cols)
+// One block owns POST_COLS whole columns; one thread per (column, level)
+// element, up to POST_R elements per thread.  Chain values at k=1 and k=NZ-2
+// are exchanged through shared memory for the top/bottom condition.
+constexpr int POST_COLS = 8, POST_R = 4, POST_THREADS = 256;  // POST_COLS * NZ <= POST_R * POST_THREADS
+
+__device__ __forceinline__ void post_column(const int mode, const long c, const int nx, const int ny, int &i, int &j,
+                                            bool &ok)
 {
-    const int lane = threadIdx.x & 31;
-    const long warp = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    int i, j;
-    if (cols == COLS_TARGETS) {
-        if (warp >= 6L * p.ny) return;
-        const int col = (int)(warp / p.ny);
-        j = (int)(warp % p.ny);
-        i = col < 3 ? col : p.nx - 6 + col;
+    ok = true;
+    if (mode == COLS_TARGETS) {
+        if (c >= 6L * ny) { ok = false; return; }
+        const int col = (int)(c / ny);
+        j = (int)(c % ny);
+        i = col < 3 ? col : nx - 6 + col;
+    } else if (mode == COLS_NONTARGETS) {
+        if (c >= (long)(nx - 6) * ny) { ok = false; return; }
+        i = 3 + (int)(c / ny);
+        j = (int)(c % ny);
     } else {
-        if (warp >= (long)p.nx * p.ny) return;
-        i = (int)(warp / p.ny);
-        j = (int)(warp % p.ny);
-        if (cols == COLS_NONTARGETS && (i < 3 || i >= p.nx - 3)) return;
+        if (c >= (long)nx * ny) { ok = false; return; }
+        i = (int)(c / ny);
+        j = (int)(c % ny);
     }
-    // source column of a periodic target
-    int si = i;
-    if (cols == COLS_TARGETS) si = i < 3 ? p.nx - 6 + i : 3 + (i - (p.nx - 3));
-    const int nz = p.nz;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(POST_THREADS) k_post(KParams<T> p, KFields<T> F, int nfields, int4 fl0, int4 fl1,
+                                                       T step, int cols)
+{
+    __shared__ T edge[7][POST_COLS][2];
+    const int nz = p.nz, sx = p.ny * p.nz, sy = p.nz;
     const int flv[7] = {fl0.x, fl0.y, fl0.z, fl0.w, fl1.x, fl1.y, fl1.z};
-    const long src0 = gix(p.ny, nz, si, j, 0), dst0 = gix(p.ny, nz, i, j, 0);
-    // all loads of the column first, so they are in flight together
-    T vals[7][KPL];
+    const long c0 = (long)blockIdx.x * POST_COLS;
+    T vals[7][POST_R];
 #pragma unroll
-    for (int f = 0; f < 7; ++f) {
+    for (int r = 0; r < POST_R; ++r) {
+        const int e = threadIdx.x + r * POST_THREADS;
+        const int cl = e / nz, k = e - cl * nz;
+        int i = 0, j = 0;
+        bool ok = false;
+        if (cl < POST_COLS) post_column(cols, c0 + cl, p.nx, p.ny, i, j, ok);
+        if (!ok) continue;
+        // the chain runs at the source column (the column itself, or the
+        // column a periodic target copies)
+        const int si = cols == COLS_TARGETS ? (i < 3 ? p.nx - 6 + i : 3 + (i - (p.nx - 3))) : i;
+        const int c = gix(p.ny, nz, si, j, k);
+        const bool inner = si >= 1 && si < p.nx - 1 && j >= 1 && j < p.ny - 1 && k >= 1 && k < nz - 1;
+        // sponge strips of this point, in the reference's order (boundaries.cpp:481-498)
+        const bool kin = k >= 1;
+        const bool hE = kin && !p.periodic && j >= 1 && si >= p.eb && si < p.ee;
+        const bool hW = kin && !p.periodic && j >= 1 && si >= p.wb && si < p.we;
+        const bool hS = kin && si >= 1 && j >= p.sb && j < p.se;
+        const bool hN = kin && si >= 1 && j >= p.nb && j < p.ne;
+        const T cE = hE ? p.ce[si - p.eb] : T(0), cW = hW ? p.cw[si - p.wb] : T(0);
+        const T cS = hS ? p.cs[j - p.sb] : T(0), cN = hN ? p.cn[j - p.nb] : T(0);
+        T dpx = T(0), dpy = T(0), dpz = T(0);
+        if (inner && ((flv[FU] | flv[FV] | flv[FW]) & PF_PROJECT)) {
+            const T pc = F.pi[c];
+            dpx = pc - F.pi[c - sx];
+            dpy = pc - F.pi[c - sy];
+            dpz = pc - F.pi[c - 1];
+        }
 #pragma unroll
-        for (int r = 0; r < KPL; ++r) {
-            const int k = lane + 32 * r;
-            vals[f][r] = (f < nfields && flv[f] && k < nz) ? F.P[f][src0 + k] : T(0);
+        for (int f = 0; f < 7; ++f) {
+            const int flags = flv[f];
+            if (f >= nfields || !flags) continue;
+            T v = F.P[f][c];
+            if (flags & PF_ZERO) {  // zero_moisture, microphysics.cpp:675-700
+                if (f == FQC || f == FQR) {
+                    if (v < 0) v = 0;
+                } else if (f == FQV && inner) {
+                    const T qbar = F.bar[4][c];
+                    if (v + qbar + p.qb[k] < 0) v = -(qbar + p.qb[k]);
+                }
+            }
+            if ((flags & PF_PROJECT) && inner) {  // solver.cpp:123-135
+                if (f == FU) v = v - step * (p.dtx * dpx);
+                else if (f == FV) v = v - step * (p.dty * dpy);
+                else if (f == FW && k >= 2) v = v - step * ((p.dtz * p.mw[k]) * dpz);
+            }
+            if (flags & PF_SPONGE) {
+                if (hE) v = v - cE * v;
+                if (hW) v = v - cW * v;
+                if (hS) v = v - cS * v;
+                if (hN) v = v - cN * v;
+            }
+            vals[f][r] = v;
+            if (k == 1) edge[f][cl][0] = v;
+            if (k == nz - 2) edge[f][cl][1] = v;
         }
     }
+    __syncthreads();
 #pragma unroll
-    for (int f = 0; f < 7; ++f) {
-        if (f >= nfields || !flv[f]) continue;
-        const int flags = flv[f];
+    for (int r = 0; r < POST_R; ++r) {
+        const int e = threadIdx.x + r * POST_THREADS;
+        const int cl = e / nz, k = e - cl * nz;
+        int i = 0, j = 0;
+        bool ok = false;
+        if (cl < POST_COLS) post_column(cols, c0 + cl, p.nx, p.ny, i, j, ok);
+        if (!ok) continue;
+        const int c = gix(p.ny, nz, i, j, k);
+        const bool vbc = i >= 1 && j >= 1;
+        const bool ray = i >= 1 && i < p.nx - 1 && j >= 1 && j < p.ny - 1 && k >= p.raylevel;
 #pragma unroll
-        for (int r = 0; r < KPL; ++r) {
-            const int k = lane + 32 * r;
-            if (k < nz) vals[f][r] = chain_value(p, F, f, flags, si, j, k, vals[f][r], step);
-        }
-        // values at k=1 and k=NZ-2 after the chain, for the vertical condition
-        const T v1 = __shfl_sync(0xffffffffu, vals[f][0], 1);
-        const int kt = nz - 2;
-        T vtop = vals[f][0];
-#pragma unroll
-        for (int r = 0; r < KPL; ++r)
-            if (kt / 32 == r) vtop = __shfl_sync(0xffffffffu, vals[f][r], kt & 31);
-#pragma unroll
-        for (int r = 0; r < KPL; ++r) {
-            const int k = lane + 32 * r;
-            if (k >= nz) continue;
+        for (int f = 0; f < 7; ++f) {
+            const int flags = flv[f];
+            if (f >= nfields || !flags) continue;
             T v = vals[f][r];
-            if ((flags & PF_VBC) && i >= 1 && j >= 1) {
+            if ((flags & PF_VBC) && vbc) {  // boundaries.cpp:304-326
                 if (f == FW) {
                     if (k == 0 || k == 1 || k == nz - 1) v = T(0);
                 } else {
-                    if (k == 0) v = v1;
-                    if (k == nz - 1) v = vtop;
+                    if (k == 0) v = edge[f][cl][0];
+                    if (k == nz - 1) v = edge[f][cl][1];
                 }
             }
-            if ((flags & PF_RAYLEIGH) && f <= FTH && i >= 1 && i < p.nx - 1 && j >= 1 && j < p.ny - 1 &&
-                k >= p.raylevel) {
+            if ((flags & PF_RAYLEIGH) && f <= FTH && ray) {  // damping.cpp:1148-1177
                 const T cr = (f == FW) ? p.ray_w[k] : p.ray_u[k];
                 v = v - cr * v;
             }
-            vals[f][r] = v;
-        }
-    }
-    __syncwarp();
-#pragma unroll
-    for (int f = 0; f < 7; ++f) {
-        if (f >= nfields || !flv[f]) continue;
-        const bool wm = (flv[f] & PF_WRITE_M) != 0;
-#pragma unroll
-        for (int r = 0; r < KPL; ++r) {
-            const int k = lane + 32 * r;
-            if (k >= nz) continue;
-            F.P[f][dst0 + k] = vals[f][r];
-            if (wm) F.M[f][dst0 + k] = vals[f][r];
+            F.P[f][c] = v;
+            if (flags & PF_WRITE_M) F.M[f][c] = v;
         }
     }
 }

@@ -195,25 +195,27 @@ int solve_pressure_noalloc(const ga_config *c, const ga_columns *cols, double *u
     const size_t smem_y = 2 * (size_t)nj * KTy * sizeof(T2), smem_x = 2 * (size_t)ni * KTx * sizeof(T2);
     const FftPlan pj = plan_for(nj), pi_plan = plan_for(ni);
     const int nkt_y = (NZ - 2 + KTy - 1) / KTy, nkt_x = (NZ - 2 + KTx - 1) / KTx;
-    k_div_fft_y<double><<<dim3(ni, nkt_y), 256, smem_y, stream>>>(kp, F, spec, pj, tw_j, step * c->dt, lgy);
+    const dim3 by_y(KTy, std::max(1, 256 / KTy)), by_x(KTx, std::max(1, 256 / KTx));
+    k_div_fft_y<double><<<dim3(ni, nkt_y), by_y, smem_y, stream>>>(kp, F, spec, pj, tw_j, step * c->dt, KTy);
     // FFT along x + Thomas + inverse FFT along x
     const int nl = NZ - 2, m = 8;
     auto pad = [&](int L) { return L + ((1 - L % m) % m + m) % m; };
     const size_t optin = 200 * 1024;
     if (2 * (size_t)ni * pad(nl) * sizeof(T2) <= optin) {
         const int ps = pad(nl);
-        k_spectral_x<double><<<nj, 256, 2 * (size_t)ni * ps * sizeof(T2), stream>>>(kp, spec, pi_plan, tw_i, nl, -1,
-                                                                                    ps);
+        const int bx = std::min(nl, 64);
+        k_spectral_x<double><<<nj, dim3(bx, std::max(1, 256 / bx)), 2 * (size_t)ni * ps * sizeof(T2), stream>>>(
+            kp, spec, pi_plan, tw_i, ps);
     } else {
         const int TC = 64;
         const size_t smem_th = (size_t)TC * (NZ | 1) * (sizeof(T2) + sizeof(double));
-        k_fft_x<double><<<dim3(nj, nkt_x), 256, smem_x, stream>>>(kp, spec, pi_plan, tw_i, 0, lgx);
+        k_fft_x<double><<<dim3(nj, nkt_x), by_x, smem_x, stream>>>(kp, spec, pi_plan, tw_i, 0, KTx);
         const long ncol = (long)ni * nj;
         k_thomas<double><<<(int)((ncol + TC - 1) / TC), TC, smem_th, stream>>>(kp, spec, TC);
-        k_fft_x<double><<<dim3(nj, nkt_x), 256, smem_x, stream>>>(kp, spec, pi_plan, tw_i, 1, lgx);
+        k_fft_x<double><<<dim3(nj, nkt_x), by_x, smem_x, stream>>>(kp, spec, pi_plan, tw_i, 1, KTx);
     }
     // inverse FFT along y + PI with the level copies and lateral placement
-    k_ifft_y_pi<double><<<dim3(ni, nkt_y), 256, smem_y, stream>>>(kp, F, spec, pj, tw_j, lgy);
+    k_ifft_y_pi<double><<<dim3(ni, nkt_y), by_y, smem_y, stream>>>(kp, F, spec, pj, tw_j, KTy);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
         set_error(std::string("ga_solve_pressure_noalloc: launch failed: ") + cudaGetErrorString(e));
