@@ -278,11 +278,82 @@ def moist_blob(nx=24, ny=22, nz=16, dx=1000.0, dz=500.0, dt=4.0, nsteps=3, seed=
     return wl
 
 
+def monsoon_vortex(nx=192, ny=128, nz=32, dx=40000.0, dz=600.0, dt=120.0, nsteps=500, seed=1003,
+                   vort=1.0e-4, upper_shear=-2.0e-3, lower_shear=-1.0e-3, vmax=5.0, rmax=500000.0,
+                   zmax=4000.0, corner_lat=95.0, noise=0.0, moist=False, extra_basic=0.0) -> Workload:
+    """Sheared monsoon-depression state (dry): a zonal jet u(y, z) whose
+    relative vorticity peaks at `vort` (1/s) at the domain's centre latitude,
+    with vertical shear `lower_shear` below and `upper_shear` above the jet
+    level (1/s), theta in thermal-wind balance with it on the stable
+    sounding, and an axisymmetric vortex (max wind `vmax` at radius `rmax`,
+    peaking at height `zmax`).  Written from the description of the
+    reference's ITCZ-shear and vortex initialisers (data_initializer.cpp:
+    298-568, 760-1064); corner_lat places the domain over about 5-35 N.
+    extra_basic > 0 adds smooth horizontally varying VBAR, WBAR and QBAR of
+    that relative size (test cases for the general basic-state path)."""
+    wl = Workload("monsoon_vortex", nx, ny, nz, dx, dx, dz, dt, nsteps, microphysics_option=1 if moist else 0,
+                  corner_lat=corner_lat)
+    theta = stable_sounding(nz, dz)
+    qv = thunderstorm_sounding(nz, dz)[1] if moist else np.zeros(nz)
+    x, y, z = _grid_xyz(nx, ny, nz, dx, dx, dz)
+    yc = 0.5 * ny * dx
+    ly = 0.15 * ny * dx
+    eta = (y - yc) / ly
+    # u = -vort * ly * eta * exp(-eta^2 / 2) / e^-0 ... scaled so that
+    # -du/dy peaks at `vort` on the axis
+    shape_y = -vort * ly * eta * np.exp(-0.5 * eta * eta)
+    zj = 0.35 * nz * dz
+    zz = np.maximum(z, 0.0)
+    prof_z = 1.0 + np.where(zz < zj, lower_shear * (zz - zj) / (vort * ly), upper_shear * (zz - zj) / (vort * ly))
+    u = shape_y[:, None] * prof_z[None, :]  # [y][z]
+    # thermal wind: f du/dz = -(g/theta0) dtheta/dy  ->  dtheta/dy = -(f theta0 / g) du/dz
+    f0 = 2 * 7.292e-5 * math.sin(math.radians(20.0))
+    dudz = np.gradient(u, z, axis=1)
+    dthdy = -(f0 * 300.0 / GRAV) * dudz
+    th = np.cumsum(dthdy, axis=0) * dx
+    th -= th.mean(axis=0, keepdims=True)
+    n3 = (nx, ny, nz)
+    f = wl.fields
+    f["tb_in"] = theta.copy()
+    f["qb_in"] = qv.copy()
+    f["ubar"] = np.broadcast_to(u[None, :, :], n3).copy()
+    f["vbar"] = np.zeros(n3)
+    f["wbar"] = np.zeros(n3)
+    f["thbar"] = np.broadcast_to(th[None, :, :], n3).copy()
+    f["qbar"] = np.zeros(n3)
+    tb = theta.copy(); qb = qv.copy()
+    tb[0], tb[-1], qb[0], qb[-1] = tb[1], tb[-2], qb[1], qb[-2]
+    pib = _exner_profile(tb * (1.0 + 0.61 * qb), _levels(nz, dz))
+    pib[0], pib[-1] = pib[1], pib[-2]
+    f["pbar"] = np.broadcast_to(pib, n3).copy()
+    _zero_perturbation(wl)
+    # vortex: v_t(r, z) = vmax (r/rmax) exp(1 - r/rmax) exp(-((z - zmax)/(0.6 zmax))^2)
+    xc, ycv = 0.5 * nx * dx, 0.5 * ny * dx
+    X, Y = np.meshgrid(x - xc, y - ycv, indexing="ij")
+    r = np.sqrt(X * X + Y * Y) + 1e-9
+    vt = vmax * (r / rmax) * np.exp(1.0 - r / rmax)
+    vz = np.exp(-(((zz - zmax) / (0.6 * zmax)) ** 2))
+    f["u"] = (-vt * Y / r)[:, :, None] * vz[None, None, :]
+    f["v"] = (vt * X / r)[:, :, None] * vz[None, None, :]
+    if extra_basic > 0:
+        X3 = (x[:, None, None] / (nx * dx)) * 2 * math.pi
+        Y3 = (y[None, :, None] / (ny * dx)) * 2 * math.pi
+        Z3 = np.maximum(z, 0)[None, None, :] / (nz * dz)
+        f["vbar"] = extra_basic * 3.0 * np.sin(X3) * np.cos(Y3) * np.ones((1, 1, nz))
+        f["wbar"] = extra_basic * 0.05 * np.cos(X3 + Y3) * np.sin(math.pi * Z3)
+        if moist:
+            f["qbar"] = extra_basic * 1e-3 * np.sin(X3 - Y3) * np.exp(-3 * Z3)
+    if noise > 0:
+        _add_noise(wl, seed, noise)
+    return wl
+
+
 WORKLOADS = {
     "dry_bubble": dry_bubble,
     "thunderstorm": thunderstorm,
     "squall_line": squall_line,
     "moist_blob": moist_blob,
+    "monsoon_vortex": monsoon_vortex,
 }
 
 

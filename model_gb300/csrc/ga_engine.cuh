@@ -60,6 +60,9 @@ class Engine : public EngineBase {
     int psx = 0;  // point stride of the fused spectral-x kernel (0: unfused path)
     size_t smem_y = 0, smem_x = 0, smem_th = 0, smem_sx = 0, smem_adv = 0;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    bool bar_uniform[6] = {false, false, false, false, false, false};
+    bool btab_dirty = true;
+    T *btab = nullptr;
     long long graph_launches[2] = {0, 0};
     bool use_graphs = true;
     int status = GA_OK;
@@ -114,6 +117,7 @@ class Engine : public EngineBase {
         const int periodic = c->periodic_ew_boundaries;
         const int ni = periodic ? NX - 6 : NX, nj = NY;
         spec = dalloc<T2>((size_t)ni * nj * NZ);
+        btab = dalloc<T>((size_t)BT_COUNT * NZ);
 
         // ---- scalars (initialize_globals, initializer.cpp:168-179) ----
         const double dx = c->dx, dy = c->dy, dz = c->dz, dt = c->dt;
@@ -185,7 +189,7 @@ class Engine : public EngineBase {
         kp.acoef_d = upload(ac); kp.ccoef_d = upload(cc); kp.vcoef_d = upload(vc);
         kp.rhou_d = upload(std::vector<double>(cols->rhou, cols->rhou + NZ));
         kp.dx2 = dx * dx;
-        kp.low_modes = sizeof(T) == 8 ? 0 : 2;  // FP32: (p,q) in {0,1,N-1}^2 solve in FP64
+        kp.low_modes = sizeof(T) == 8 ? 0 : 1;  // FP32: the mean mode (0,0) solves in FP64
 
         // ---- FFT plans and twiddles ----
         plan_i = make_fft_plan(ni);
@@ -317,6 +321,15 @@ class Engine : public EngineBase {
         long nn;
         T *d = host_field(field, slot, &nn);
         if (!d || (long)n != nn) return GA_ERR_ARG;
+        if (field >= GA_UBAR && field <= GA_PBAR) {
+            // a basic state that depends on k only takes the tabulated path
+            bool uni = true;
+            for (long c = 1; c < (long)NX * NY && uni; c++)
+                uni = std::memcmp(host + c * NZ, host, NZ * sizeof(double)) == 0;
+            bar_uniform[field - GA_UBAR] = uni;
+            btab_dirty = true;
+            drop_graphs();
+        }
         if (sizeof(T) == sizeof(double)) {
             cudaMemcpyAsync(d, host, n * sizeof(double), cudaMemcpyHostToDevice, stream);
         } else {
@@ -369,6 +382,33 @@ class Engine : public EngineBase {
             return GA_ERR_CUDA;
         }
         return GA_OK;
+    }
+
+    void drop_graphs()
+    {
+        for (auto &g : graph)
+            if (g) {
+                cudaGraphExecDestroy(g);
+                g = nullptr;
+            }
+    }
+
+    // per-level basic-state tables (k_base_tables) when the basic state is
+    // horizontally uniform; rebuilt after any basic-state field changes
+    void refresh_base()
+    {
+        if (!btab_dirty) return;
+        btab_dirty = false;
+        const bool adv = bar_uniform[0] && bar_uniform[1] && bar_uniform[2] && bar_uniform[3] && bar_uniform[4];
+        const bool kes = bar_uniform[3] && bar_uniform[4] && bar_uniform[5];
+        if (adv || kes) {
+            k_base_tables<T><<<cdiv(NZ, 128), 128, 0, stream>>>(kp, bar[0], bar[1], bar[2], bar[3], bar[4], bar[5],
+                                                               btab);
+            launches++;
+        }
+        kp.btab = btab;
+        kp.ubase_adv = adv;
+        kp.ubase_kes = kes;
     }
 
     // ------------------------------------------------------------------ ops
@@ -503,6 +543,7 @@ class Engine : public EngineBase {
     int op(int o, double step) override
     {
         cudaSetDevice(device);
+        refresh_base();
         const bool moist = kp.moist;
         int fl[7] = {0, 0, 0, 0, 0, 0, 0};
         switch (o) {
@@ -628,6 +669,7 @@ class Engine : public EngineBase {
     int step(int nsteps) override
     {
         cudaSetDevice(device);
+        refresh_base();
         int n = 0;
         if (use_graphs && !prof) {
             while (nsteps - n >= 2) {

@@ -46,6 +46,21 @@ struct KParams {
     double dx2;
     T rhou1;
     int low_modes;  // |p|,|q| below this solve in FP64 (FP32 contexts)
+    // horizontally uniform basic state: per-level tables (BT_* rows of nz)
+    int ubase_adv;  // UBAR, VBAR, WBAR, THBAR, QBAR depend on k only
+    int ubase_kes;  // THBAR, QBAR, PBAR depend on k only
+    const T *btab;
+};
+
+// rows of the basic-state table (each nz long), filled by k_base_tables
+enum {
+    BT_UB = 0, BT_VB, BT_WB, BT_THB, BT_QB, BT_PB,  // column values
+    BT_C6_UB, BT_C6_VB, BT_C6_THB, BT_C6_QB,         // 5th-order face of six equal values
+    BT_C4_UB, BT_U3_UB, BT_C4_VB, BT_U3_VB,          // parts of the 3rd-order top face
+    BT_C4_THB, BT_U3_THB, BT_C4_QB, BT_U3_QB,
+    BT_H2_UB, BT_H2_VB, BT_H2_THB, BT_H2_QB,         // 2nd-order top face
+    BT_UA, BT_VA, BT_WA,                             // averaged advecting velocities
+    BT_COUNT
 };
 
 template <typename T>
@@ -406,6 +421,183 @@ __global__ void __launch_bounds__(128) k_advect(KParams<T> p, KFields<T> F, T st
 }
 
 // ---------------------------------------------------------------------------
+// Horizontally uniform basic state.  With UBAR..QBAR functions of k only, the
+// basic-state face values and averaged advecting velocities are per-level
+// constants.  For six equal values the upwind part of INTERP_5TH is exactly
+// zero and the face equals its centred part for either sign, so a table
+// evaluated once with the same device functions reproduces the general
+// expressions bit for bit.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void k_base_tables(KParams<T> p, const T *ub, const T *vb, const T *wb, const T *thb, const T *qb,
+                              const T *pb, T *tab)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nz = p.nz;
+    if (k >= nz) return;
+    // column 0 holds the profile (the host checked that every column equals it)
+    const T *src[6] = {ub, vb, wb, thb, qb, pb};
+    for (int r = 0; r < 6; r++) tab[r * nz + k] = src[r][k];
+    const T *hsrc[4] = {ub, vb, thb, qb};
+    for (int r = 0; r < 4; r++) {
+        const T a = hsrc[r][k];
+        tab[(BT_C6_UB + r) * nz + k] = face5<T>(a, a, a, a, a, a, T(1));
+        if (k >= 1 && k <= nz - 3) {
+            const T am1 = hsrc[r][k - 1], a0 = a, a1 = hsrc[r][k + 1], a2 = hsrc[r][k + 2];
+            tab[(BT_C4_UB + 2 * r) * nz + k] = W<T>::c7_12 * (a1 + a0) - W<T>::c1_12 * (a2 + am1);
+            tab[(BT_U3_UB + 2 * r) * nz + k] = (a2 - am1) - T(3.0) * (a1 - a0);
+        } else {
+            tab[(BT_C4_UB + 2 * r) * nz + k] = T(0);
+            tab[(BT_U3_UB + 2 * r) * nz + k] = T(0);
+        }
+        tab[(BT_H2_UB + r) * nz + k] = k + 1 < nz ? T(0.5) * (hsrc[r][k + 1] + a) : T(0);
+    }
+    tab[BT_UA * nz + k] = T(0.5) * (ub[k] + ub[k]);
+    tab[BT_VA * nz + k] = T(0.5) * (vb[k] + vb[k]);
+    tab[BT_WA * nz + k] = k + 1 < nz ? T(0.5) * (wb[k + 1] + wb[k + 1]) : T(0);
+}
+
+#define BTAB(row, k) p.btab[(row) * p.nz + (k)]
+
+template <typename T>
+__device__ __forceinline__ T face3_tab(const KParams<T> &p, int rc4, int k, T sign)
+{
+    return BTAB(rc4, k) + W<T>::c1_12 * sign * BTAB(rc4 + 1, k);
+}
+
+template <typename T>
+__device__ T u_east_ub(const KParams<T> &p, const KFields<T> &F, int i, int j, int k)
+{
+    const T *U = F.cur[FU];
+    const int c = gix(p.ny, p.nz, i, j, k), s = p.ny * p.nz;
+    T ua = T(0.5) * (LD(U, c + s) + LD(U, c));
+    T uba = BTAB(BT_UA, k);
+    T ue = f5i(U, p, i, j, k, sgn(uba + ua));
+    return ua * BTAB(BT_C6_UB, k) + (uba + ua) * ue;
+}
+template <typename T>
+__device__ T u_north_ub(const KParams<T> &p, const KFields<T> &F, int i, int j, int k)
+{
+    const T *U = F.cur[FU], *V = F.cur[FV];
+    const int a = gix(p.ny, p.nz, i, j + 1, k), b = gix(p.ny, p.nz, i - 1, j + 1, k);
+    T va = T(0.5) * (LD(V, a) + LD(V, b));
+    T vba = BTAB(BT_VA, k);
+    T un = f5j(U, p, i, j, k, sgn(vba + va));
+    return va * BTAB(BT_C6_UB, k) + (vba + va) * un;
+}
+template <typename T>
+__device__ T u_top_ub(const KParams<T> &p, const KFields<T> &F, int i, int j, int k)
+{
+    if (k == 0) return T(0);
+    const T *U = F.cur[FU], *Wc = F.cur[FW];
+    const int a = gix(p.ny, p.nz, i, j, k + 1), b = gix(p.ny, p.nz, i - 1, j, k + 1);
+    T wa = T(0.5) * (LD(Wc, a) + LD(Wc, b));
+    T wba = BTAB(BT_WA, k);
+    T ut, ubt;
+    if (k == 1 || k == p.nz - 2) {
+        ut = f2k(U, p, i, j, k);
+        ubt = BTAB(BT_H2_UB, k);
+    } else {
+        ut = f3k(U, p, i, j, k, sgn(wba + wa));
+        ubt = face3_tab(p, BT_C4_UB, k, sgn(wa));
+    }
+    return wa * ubt + (wba + wa) * ut;
+}
+template <typename T>
+__device__ T v_east_ub(const KParams<T> &p, const KFields<T> &F, int i, int j, int k)
+{
+    const T *U = F.cur[FU], *V = F.cur[FV];
+    const int a = gix(p.ny, p.nz, i + 1, j, k), b = gix(p.ny, p.nz, i + 1, j - 1, k);
+    T ua = T(0.5) * (LD(U, a) + LD(U, b));
+    T uba = BTAB(BT_UA, k);
+    T ve = f5i(V, p, i, j, k, sgn(uba + ua));
+    return ua * BTAB(BT_C6_VB, k) + (uba + ua) * ve;
+}
+template <typename T>
+__device__ T v_north_ub(const KParams<T> &p, const KFields<T> &F, int i, int j, int k)
+{
+    const T *V = F.cur[FV];
+    const int c = gix(p.ny, p.nz, i, j, k);
+    T va = T(0.5) * (LD(V, c + p.nz) + LD(V, c));
+    T vba = BTAB(BT_VA, k);
+    T vn = f5j(V, p, i, j, k, sgn(vba + va));
+    return va * BTAB(BT_C6_VB, k) + (vba + va) * vn;
+}
+template <typename T>
+__device__ T v_top_ub(const KParams<T> &p, const KFields<T> &F, int i, int j, int k)
+{
+    if (k == 0) return T(0);
+    const T *V = F.cur[FV], *Wc = F.cur[FW];
+    const int a = gix(p.ny, p.nz, i, j, k + 1), b = gix(p.ny, p.nz, i, j - 1, k + 1);
+    T wa = T(0.5) * (LD(Wc, a) + LD(Wc, b));
+    T wba = BTAB(BT_WA, k);
+    T vt, vbt;
+    if (k == 1 || k == p.nz - 2) {
+        vt = f2k(V, p, i, j, k);
+        vbt = BTAB(BT_H2_VB, k);
+    } else {
+        vt = f3k(V, p, i, j, k, sgn(wba + wa));
+        vbt = face3_tab(p, BT_C4_VB, k, sgn(wa));
+    }
+    return wa * vbt + (wba + wa) * vt;
+}
+// scalar faces; brow = basic-state row offset (0: theta, 1: qv) or -1 (none)
+template <typename T>
+__device__ T s_east_ub(const KParams<T> &p, const KFields<T> &F, const T *s, int brow, int i, int j, int k)
+{
+    const int a = gix(p.ny, p.nz, i + 1, j, k);
+    T u1 = LD(F.cur[FU], a);
+    T ut = BTAB(BT_UB, k) + u1;
+    T se = f5i(s, p, i, j, k, sgn(ut));
+    if (brow < 0) return ut * se;
+    return u1 * BTAB(BT_C6_THB + brow, k) + ut * se;
+}
+template <typename T>
+__device__ T s_north_ub(const KParams<T> &p, const KFields<T> &F, const T *s, int brow, int i, int j, int k)
+{
+    const int a = gix(p.ny, p.nz, i, j + 1, k);
+    T v1 = LD(F.cur[FV], a);
+    T vt = BTAB(BT_VB, k) + v1;
+    T sn = f5j(s, p, i, j, k, sgn(vt));
+    if (brow < 0) return vt * sn;
+    return v1 * BTAB(BT_C6_THB + brow, k) + vt * sn;
+}
+template <typename T>
+__device__ T s_top_ub(const KParams<T> &p, const KFields<T> &F, const T *s, int brow, int i, int j, int k)
+{
+    if (k == 0) return T(0);
+    const int a = gix(p.ny, p.nz, i, j, k + 1);
+    T w1 = LD(F.cur[FW], a);
+    T wt = BTAB(BT_WB, k + 1) + w1;
+    T st, bt = T(0);
+    if (k == 1 || k == p.nz - 2) {
+        st = f2k(s, p, i, j, k);
+        if (brow >= 0) bt = BTAB(BT_H2_THB + brow, k);
+    } else {
+        st = f3k(s, p, i, j, k, sgn(wt));
+        if (brow >= 0) bt = face3_tab(p, BT_C4_THB + 2 * brow, k, sgn(w1));
+    }
+    if (brow < 0) return wt * st;
+    return w1 * bt + wt * st;
+}
+template <typename T>
+__device__ T r_top_ub(const KParams<T> &p, const KFields<T> &F, int i, int j, int k)
+{
+    const T *s = F.cur[FQR];
+    if (k == 0) {
+        T s0 = T(0.5) * (LD(s, gix(p.ny, p.nz, i, j, 0)) + LD(s, gix(p.ny, p.nz, i, j, 1)));
+        return T(-0.5) * (vt_at(p, F, i, j, 1) + vt_at(p, F, i, j, 0)) * s0;
+    }
+    const int a = gix(p.ny, p.nz, i, j, k + 1);
+    T wb = BTAB(BT_WB, k + 1) + LD(F.cur[FW], a);
+    T wf = wb - T(0.5) * (vt_at(p, F, i, j, k) + vt_at(p, F, i, j, k + 1));
+    T st;
+    if (k == 1 || k == p.nz - 2) st = f2k(s, p, i, j, k);
+    else st = f3k(s, p, i, j, k, sgn(wf));
+    return wf * st;
+}
+
+// ---------------------------------------------------------------------------
 // Tiled advection: a block owns a TI x TJ tile of interior columns and every
 // interior level.  Phase 1 evaluates each east, north and top face flux of the
 // tile once (plus the west / south faces of its first row and column) into
@@ -418,6 +610,19 @@ template <typename T>
 __device__ __forceinline__ void faces_east(const KParams<T> &p, const KFields<T> &F, int what, int i, int j, int k,
                                            T *out)
 {
+    if (p.ubase_adv) {
+        if (what & ADV_UV) {
+            out[0] = u_east_ub(p, F, i, j, k);
+            out[1] = v_east_ub(p, F, i, j, k);
+        }
+        if (what & ADV_TH) out[2] = s_east_ub(p, F, F.cur[FTH], 0, i, j, k);
+        if (what & ADV_Q) {
+            out[3] = s_east_ub(p, F, F.cur[FQV], 1, i, j, k);
+            out[4] = s_east_ub(p, F, F.cur[FQC], -1, i, j, k);
+            out[5] = s_east_ub(p, F, F.cur[FQR], -1, i, j, k);
+        }
+        return;
+    }
     if (what & ADV_UV) {
         out[0] = u_east(p, F, i, j, k);
         out[1] = v_east(p, F, i, j, k);
@@ -433,6 +638,19 @@ template <typename T>
 __device__ __forceinline__ void faces_north(const KParams<T> &p, const KFields<T> &F, int what, int i, int j, int k,
                                             T *out)
 {
+    if (p.ubase_adv) {
+        if (what & ADV_UV) {
+            out[0] = u_north_ub(p, F, i, j, k);
+            out[1] = v_north_ub(p, F, i, j, k);
+        }
+        if (what & ADV_TH) out[2] = s_north_ub(p, F, F.cur[FTH], 0, i, j, k);
+        if (what & ADV_Q) {
+            out[3] = s_north_ub(p, F, F.cur[FQV], 1, i, j, k);
+            out[4] = s_north_ub(p, F, F.cur[FQC], -1, i, j, k);
+            out[5] = s_north_ub(p, F, F.cur[FQR], -1, i, j, k);
+        }
+        return;
+    }
     if (what & ADV_UV) {
         out[0] = u_north(p, F, i, j, k);
         out[1] = v_north(p, F, i, j, k);
@@ -448,6 +666,19 @@ template <typename T>
 __device__ __forceinline__ void faces_top(const KParams<T> &p, const KFields<T> &F, int what, int i, int j, int k,
                                           T *out)
 {
+    if (p.ubase_adv) {
+        if (what & ADV_UV) {
+            out[0] = u_top_ub(p, F, i, j, k);
+            out[1] = v_top_ub(p, F, i, j, k);
+        }
+        if (what & ADV_TH) out[2] = s_top_ub(p, F, F.cur[FTH], 0, i, j, k);
+        if (what & ADV_Q) {
+            out[3] = s_top_ub(p, F, F.cur[FQV], 1, i, j, k);
+            out[4] = s_top_ub(p, F, F.cur[FQC], -1, i, j, k);
+            out[5] = r_top_ub(p, F, i, j, k);
+        }
+        return;
+    }
     if (what & ADV_UV) {
         out[0] = u_top(p, F, i, j, k);
         out[1] = v_top(p, F, i, j, k);
@@ -571,7 +802,7 @@ __global__ void __launch_bounds__(256) k_advect_tile(KParams<T> p, KFields<T> F,
             if (what & ADV_ZERO) {
                 if (qc < 0) qc = 0;
                 if (qr < 0) qr = 0;
-                T qbar = LD(F.bar[4], cix);
+                T qbar = p.ubase_adv ? BTAB(BT_QB, k) : LD(F.bar[4], cix);
                 if (qv + qbar + p.qb[k] < 0) qv = -(qbar + p.qb[k]);
             }
             F.P[FQV][cix] = qv;
@@ -1334,7 +1565,9 @@ __global__ void __launch_bounds__(128) k_kessler(KParams<T> p, KFields<T> F, int
     T *THP = F.P[FTH], *QVP = F.P[FQV], *QCP = F.P[FQC], *QRP = F.P[FQR];
     const T rhou = p.rhou[k];
     T thp = THP[ix], qvp = QVP[ix], qcp = QCP[ix], qrp = QRP[ix];
-    const T thbar = F.bar[3][ix], qbar = F.bar[4][ix], pbar = F.bar[5][ix];
+    const T thbar = p.ubase_kes ? BTAB(BT_THB, k) : F.bar[3][ix];
+    const T qbar = p.ubase_kes ? BTAB(BT_QB, k) : F.bar[4][ix];
+    const T pbar = p.ubase_kes ? BTAB(BT_PB, k) : F.bar[5][ix];
     T theta = thp + thbar + p.tb[k];
     T pressure = F.pi[ix] / (cp * p.tbv[k]) + pbar;
     T vapor = qvp + qbar + p.qb[k];
