@@ -245,6 +245,45 @@ def e2e_jobs(model_cls, wl, prec, torch, jobs, job_steps, device):
             "jobs": jobs, "seconds_per_run": round(el / jobs, 4)}
 
 
+def ensemble_bench(torch, device, steps, warmup, n_small=64, n_large=32):
+    """Uneven ensemble (configs[3]): n_small members at 96x96x40 and n_large at
+    160x160x48, FP32, Kessler, batched kernels + CUDA graph.  The state
+    (about 8 GB) is far larger than L2, so no flush is needed."""
+    from model_gb300 import abi, anelastic, configs
+    layout = configs.ensemble_layout(n_small, n_large)
+    members = [configs.Workload(f"m{m}", nx, ny, nz, 1000.0, 1000.0, 400.0, 4.0, 300, microphysics_option=1)
+               for m, (nx, ny, nz) in enumerate(layout)]
+    cols_by_size, cols = {}, []
+    for m, (nx, ny, nz) in enumerate(layout):
+        if (nx, ny, nz) not in cols_by_size:
+            cols_by_size[(nx, ny, nz)] = anelastic.build_columns(configs.ensemble_member(m, nx, ny, nz))
+        cols.append(cols_by_size[(nx, ny, nz)])
+    t0 = time.perf_counter()
+    ens = anelastic.Ensemble(members, abi.GA_PREC_F32, device=device, columns=cols)
+    for m, (nx, ny, nz) in enumerate(layout):
+        ens.load_member(m, configs.ensemble_member(m, nx, ny, nz).fields)
+    setup = time.perf_counter() - t0
+    ens.step(max(2, warmup))
+    ext = torch.cuda.ExternalStream(ens.stream_handle())
+    l0 = ens.launch_count()
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    ens.synchronize()
+    a.record(ext)
+    ens.step_async(steps)
+    b.record(ext)
+    ens.synchronize()
+    ms = a.elapsed_time(b)
+    pts = sum(nx * ny * nz for nx, ny, nz in layout)
+    out = {"value": round(pts * steps / (ms * 1e-3), 1), "unit": UNIT, "members": len(layout),
+           "layout": f"{n_small} x 96x96x40 + {n_large} x 160x160x48", "points": pts, "steps": steps,
+           "ms_per_step": round(ms / steps, 4), "launches_per_step": (ens.launch_count() - l0) / steps,
+           "setup_s": round(setup, 1), "precision": "fp32",
+           "note": "one launch per kernel phase over all members; two-step CUDA graph"}
+    ens.close()
+    return out
+
+
 def cpu_baseline(wl, steps):
     """The reference's CPU step (oracle restatement, 1 core) on a bounded
     sample of the same workload."""
@@ -361,6 +400,8 @@ def run_ours(args):
         line["accuracy"] = accuracy(anelastic.Model, wl, torch, device, args.accuracy_steps)
     if args.e2e_jobs > 0:
         line["e2e"] = e2e_jobs(anelastic.Model, wl, prec, torch, args.e2e_jobs, args.e2e_steps, device)
+    if args.ensemble_steps > 0:
+        line["ensemble"] = ensemble_bench(torch, device, args.ensemble_steps, 2)
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(wl, args.cpu_steps)
     print(json.dumps(line), flush=True)
@@ -406,6 +447,7 @@ def main():
     ap.add_argument("--e2e-jobs", type=int, default=2)
     ap.add_argument("--e2e-steps", type=int, default=600)
     ap.add_argument("--cpu-steps", type=int, default=5)
+    ap.add_argument("--ensemble-steps", type=int, default=10)
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()

@@ -217,6 +217,31 @@ GA_API void *ga_stream(ga_ctx *ctx);
 GA_API void *ga_field_device_ptr(ga_ctx *ctx, int field, int slot);
 
 /*
+ * Ensembles.  The reference runs ensemble members as separate serial models
+ * farmed out over MPI tasks (run_ensemble, ensemble.cpp:45-144).  Here the
+ * members (independent domains; grids, spacings and time steps may differ)
+ * advance together: every kernel phase of the step is one launch over all
+ * members, from a packed member table, and the two-step cycle is captured in
+ * a CUDA graph.  Each member computes exactly what a standalone context with
+ * its configuration computes.  Members share precision, device and
+ * microphysics option; periodic members and semi-Lagrangian rain fallout are
+ * not batched (GA_ERR_UNSUPPORTED).  Fields are set and read per member with
+ * the same ids and slots as ga_set_field / ga_get_field.
+ */
+typedef struct ga_ens ga_ens;
+GA_API int ga_ensemble_create(const ga_config *cfgs, const ga_columns *cols, int nmembers, ga_ens **out);
+GA_API int ga_ensemble_destroy(ga_ens *ens);
+GA_API int ga_ensemble_size(ga_ens *ens);
+GA_API int ga_ensemble_set_field(ga_ens *ens, int member, int field, int slot, const double *host, size_t n);
+GA_API int ga_ensemble_get_field(ga_ens *ens, int member, int field, int slot, double *host, size_t n);
+GA_API int ga_ensemble_step(ga_ens *ens, int nsteps);
+GA_API int ga_ensemble_step_async(ga_ens *ens, int nsteps);
+GA_API int ga_ensemble_synchronize(ga_ens *ens);
+GA_API void *ga_ensemble_stream(ga_ens *ens);
+GA_API long long ga_ensemble_launch_count(ga_ens *ens);
+GA_API int ga_ensemble_get_counters(ga_ens *ens, int member, long long *bigcounter, double *mtime);
+
+/*
  * Pressure solve without device allocation.  No counterpart in the reference:
  * it is for callers that cannot allocate GPU memory themselves or through
  * this library (a host model that owns every byte of device memory in its own

@@ -59,6 +59,20 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     L.ga_stream.restype = C.c_void_p
     L.ga_field_device_ptr.argtypes = [C.c_void_p, C.c_int, C.c_int]
     L.ga_field_device_ptr.restype = C.c_void_p
+    L.ga_ensemble_create.argtypes = [C.POINTER(abi.GaConfig), C.POINTER(abi.GaColumns), C.c_int,
+                                     C.POINTER(C.c_void_p)]
+    L.ga_ensemble_destroy.argtypes = [C.c_void_p]
+    L.ga_ensemble_size.argtypes = [C.c_void_p]
+    L.ga_ensemble_set_field.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, _DP, C.c_size_t]
+    L.ga_ensemble_get_field.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, _DP, C.c_size_t]
+    L.ga_ensemble_step.argtypes = [C.c_void_p, C.c_int]
+    L.ga_ensemble_step_async.argtypes = [C.c_void_p, C.c_int]
+    L.ga_ensemble_synchronize.argtypes = [C.c_void_p]
+    L.ga_ensemble_stream.argtypes = [C.c_void_p]
+    L.ga_ensemble_stream.restype = C.c_void_p
+    L.ga_ensemble_launch_count.argtypes = [C.c_void_p]
+    L.ga_ensemble_launch_count.restype = C.c_longlong
+    L.ga_ensemble_get_counters.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_longlong), C.POINTER(C.c_double)]
     if L.ga_abi_version() != 1:
         raise RuntimeError("ABI version mismatch")
     _lib = L
@@ -230,3 +244,94 @@ class Model:
 
     def device_ptr(self, field: int, slot: int = 0) -> int:
         return self.L.ga_field_device_ptr(self.h, field, slot) or 0
+
+
+class Ensemble:
+    """Independent domains of uneven sizes advanced together by batched
+    kernels (one launch per kernel phase over all members).  The reference
+    farms such members out as separate serial runs (ensemble.cpp:45-144)."""
+
+    def __init__(self, members, precision: int = abi.GA_PREC_F32, device: int = 0, columns=None):
+        """members: list of Workload (their fields may be empty; load them
+        later with load_member).  columns: optional list of column dicts."""
+        self.L = load_library()
+        self.members = list(members)
+        n = len(self.members)
+        self.cols = columns if columns is not None else [build_columns(w) for w in self.members]
+        self._keep = []
+        cfgs = (abi.GaConfig * n)()
+        gcs = (abi.GaColumns * n)()
+        for m, (wl, cols) in enumerate(zip(self.members, self.cols)):
+            keep = {k: np.ascontiguousarray(v, dtype=np.float64) for k, v in cols.items()}
+            self._keep.append(keep)
+            cfgs[m] = abi.make_config(wl.settings(), precision, device)
+            for name in abi.COLUMN_NAMES + ["f"]:
+                setattr(gcs[m], name, _ptr(keep[name]))
+        h = C.c_void_p()
+        rc = self.L.ga_ensemble_create(cfgs, gcs, n, C.byref(h))
+        if rc:
+            raise GaError(rc, "ga_ensemble_create")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.ga_ensemble_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set(self, member: int, field: int, slot: int, arr) -> None:
+        a = np.ascontiguousarray(arr, dtype=np.float64).ravel()
+        rc = self.L.ga_ensemble_set_field(self.h, member, field, slot, _ptr(a), a.size)
+        if rc:
+            raise GaError(rc, "ga_ensemble_set_field")
+
+    def get(self, member: int, field: int, slot: int = 0) -> np.ndarray:
+        wl = self.members[member]
+        n = wl.nx * wl.ny if field == abi.GA_ACCRAIN else wl.points
+        a = np.zeros(n)
+        rc = self.L.ga_ensemble_get_field(self.h, member, field, slot, _ptr(a), n)
+        if rc:
+            raise GaError(rc, "ga_ensemble_get_field")
+        return a
+
+    def load_member(self, member: int, fields: dict) -> None:
+        for b, name in enumerate(abi.BAR_NAMES):
+            self.set(member, abi.GA_UBAR + b, 0, fields[name])
+        nprog = 7 if self.members[member].microphysics_option else 4
+        for f in range(nprog):
+            arr = fields[abi.PROG_NAMES[f]]
+            self.set(member, f, abi.GA_SLOT_CUR, arr)
+            self.set(member, f, abi.GA_SLOT_M, arr)
+
+    def step(self, n: int = 1) -> None:
+        rc = self.L.ga_ensemble_step(self.h, n)
+        if rc:
+            raise GaError(rc, "ga_ensemble_step")
+
+    def step_async(self, n: int = 1) -> None:
+        rc = self.L.ga_ensemble_step_async(self.h, n)
+        if rc:
+            raise GaError(rc, "ga_ensemble_step_async")
+
+    def synchronize(self) -> None:
+        rc = self.L.ga_ensemble_synchronize(self.h)
+        if rc:
+            raise GaError(rc, "ga_ensemble_synchronize")
+
+    def stream_handle(self) -> int:
+        return self.L.ga_ensemble_stream(self.h) or 0
+
+    def launch_count(self) -> int:
+        return self.L.ga_ensemble_launch_count(self.h)
+
+    def counters(self, member: int):
+        bc, mt = C.c_longlong(), C.c_double()
+        rc = self.L.ga_ensemble_get_counters(self.h, member, C.byref(bc), C.byref(mt))
+        if rc:
+            raise GaError(rc, "ga_ensemble_get_counters")
+        return bc.value, mt.value

@@ -348,6 +348,24 @@ def monsoon_vortex(nx=192, ny=128, nz=32, dx=40000.0, dz=600.0, dt=120.0, nsteps
     return wl
 
 
+def ensemble_member(m: int, nx: int, ny: int, nz: int = 48, dz: float = 400.0, nsteps: int = 300,
+                    base_seed: int = 1004) -> Workload:
+    """Member m of the uneven ensemble: the thunderstorm sounding and bubble
+    with a seeded amplitude drawn from U(1.5, 3.5) K and U(+-0.1 K) noise
+    (seed = base_seed + 7919 m)."""
+    seed = base_seed + 7919 * m
+    amp = 1.5 + 2.0 * float(splitmix_uniform(seed, 1)[0])
+    wl = thunderstorm(nx=nx, ny=ny, nz=nz, dz=dz, nsteps=nsteps, seed=seed + 1, amp=amp, noise=0.1,
+                      name=f"ensemble_member_{m}")
+    return wl
+
+
+def ensemble_layout(n_small: int = 64, n_large: int = 32):
+    """Grid sizes of the uneven ensemble: n_small members at 96x96x40 and
+    n_large at 160x160x48 (both with the thunderstorm spacing)."""
+    return [(96, 96, 40)] * n_small + [(160, 160, 48)] * n_large
+
+
 WORKLOADS = {
     "dry_bubble": dry_bubble,
     "thunderstorm": thunderstorm,

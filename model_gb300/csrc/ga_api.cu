@@ -19,6 +19,10 @@ struct ga_ctx {
     ga_config cfg;
 };
 
+struct ga_ens {
+    ga::EnsembleBase *e;
+};
+
 using ga::set_error;
 
 static int fail(int rc, const std::string &msg)
@@ -221,6 +225,102 @@ void *ga_field_device_ptr(ga_ctx *ctx, int field, int slot)
 {
     if (!ctx || field < 0 || field > GA_ACCRAIN || slot < 0 || slot > 2) return nullptr;
     return ctx->e->field_ptr(field, slot);
+}
+
+int ga_ensemble_create(const ga_config *cfgs, const ga_columns *cols, int nmembers, ga_ens **out)
+{
+    if (!cfgs || !cols || !out || nmembers < 1) return fail(GA_ERR_ARG, "ga_ensemble_create: bad arguments");
+    *out = nullptr;
+    for (int m = 0; m < nmembers; m++) {
+        const ga_config &c = cfgs[m];
+        if (c.precision != cfgs[0].precision || c.device != cfgs[0].device ||
+            c.microphysics_option != cfgs[0].microphysics_option)
+            return fail(GA_ERR_CONFIG, "ga_ensemble_create: members must share precision, device and microphysics");
+        if (c.periodic_ew_boundaries)
+            return fail(GA_ERR_UNSUPPORTED, "ga_ensemble_create: periodic members are not batched");
+        if (c.microphysics_option == 1 && c.rain_fallout != 1)
+            return fail(GA_ERR_UNSUPPORTED, "ga_ensemble_create: only Eulerian rain fallout is batched");
+        if (c.nx < 12 || c.ny < 12 || c.nz < 6 || c.nz > 128 || !(c.dx > 0 && c.dy > 0 && c.dz > 0 && c.dt > 0))
+            return fail(GA_ERR_CONFIG, "ga_ensemble_create: member grid out of range");
+        if (c.microphysics_option < 0 || c.microphysics_option > 1)
+            return fail(GA_ERR_CONFIG, "ga_ensemble_create: microphysics_option must be 0 or 1");
+    }
+    int rc = GA_OK;
+    ga::EnsembleBase *e = cfgs[0].precision == GA_PREC_F64 ? ga::make_ensemble_f64(cfgs, cols, nmembers, &rc)
+                                                           : ga::make_ensemble_f32(cfgs, cols, nmembers, &rc);
+    if (!e) return fail(rc ? rc : GA_ERR_CUDA, "ga_ensemble_create: set-up failed");
+    *out = new ga_ens{e};
+    return GA_OK;
+}
+
+int ga_ensemble_destroy(ga_ens *ens)
+{
+    if (!ens) return fail(GA_ERR_ARG, "ga_ensemble_destroy: null");
+    delete ens->e;
+    delete ens;
+    return GA_OK;
+}
+
+int ga_ensemble_size(ga_ens *ens) { return ens ? ens->e->size() : -1; }
+
+int ga_ensemble_set_field(ga_ens *ens, int member, int field, int slot, const double *host, size_t n)
+{
+    if (!ens || !host) return fail(GA_ERR_ARG, "ga_ensemble_set_field: null pointer");
+    ga::EngineBase *m = ens->e->member(member);
+    if (!m) return fail(GA_ERR_ARG, "ga_ensemble_set_field: no such member");
+    if (field < 0 || field > GA_ACCRAIN || slot < 0 || slot > 2) return fail(GA_ERR_ARG, "ga_ensemble_set_field: bad field or slot");
+    int rc = ens->e->synchronize();
+    if (rc) return rc;
+    rc = m->set_field(field, slot, host, n);
+    if (rc == GA_ERR_ARG) set_error("ga_ensemble_set_field: field not present or wrong size");
+    if (field >= GA_UBAR && field <= GA_PBAR) ens->e->mark_dirty();
+    return rc;
+}
+
+int ga_ensemble_get_field(ga_ens *ens, int member, int field, int slot, double *host, size_t n)
+{
+    if (!ens || !host) return fail(GA_ERR_ARG, "ga_ensemble_get_field: null pointer");
+    ga::EngineBase *m = ens->e->member(member);
+    if (!m) return fail(GA_ERR_ARG, "ga_ensemble_get_field: no such member");
+    if (field < 0 || field > GA_ACCRAIN || slot < 0 || slot > 2) return fail(GA_ERR_ARG, "ga_ensemble_get_field: bad field or slot");
+    int rc = ens->e->synchronize();
+    if (rc) return rc;
+    rc = m->get_field(field, slot, host, n);
+    if (rc == GA_ERR_ARG) set_error("ga_ensemble_get_field: field not present or wrong size");
+    return rc;
+}
+
+int ga_ensemble_step_async(ga_ens *ens, int nsteps)
+{
+    if (!ens || nsteps < 0) return fail(GA_ERR_ARG, "ga_ensemble_step: bad arguments");
+    return ens->e->step(nsteps);
+}
+
+int ga_ensemble_synchronize(ga_ens *ens)
+{
+    if (!ens) return fail(GA_ERR_ARG, "ga_ensemble_synchronize: null");
+    return ens->e->synchronize();
+}
+
+int ga_ensemble_step(ga_ens *ens, int nsteps)
+{
+    int rc = ga_ensemble_step_async(ens, nsteps);
+    if (rc) return rc;
+    return ga_ensemble_synchronize(ens);
+}
+
+void *ga_ensemble_stream(ga_ens *ens) { return ens ? ens->e->stream_handle() : nullptr; }
+
+long long ga_ensemble_launch_count(ga_ens *ens) { return ens ? ens->e->launches : -1; }
+
+int ga_ensemble_get_counters(ga_ens *ens, int member, long long *bigcounter, double *mtime)
+{
+    if (!ens) return fail(GA_ERR_ARG, "ga_ensemble_get_counters: null");
+    ga::EngineBase *m = ens->e->member(member);
+    if (!m) return fail(GA_ERR_ARG, "ga_ensemble_get_counters: no such member");
+    if (bigcounter) *bigcounter = m->bigcounter;
+    if (mtime) *mtime = m->mtime;
+    return GA_OK;
 }
 
 int ga_solve_pressure_noalloc(const ga_config *cfg, const ga_columns *cols, double *up, double *vp, double *wp,

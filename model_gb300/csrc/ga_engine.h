@@ -88,12 +88,27 @@ struct ProfScope {
     ~ProfScope() { e->prof_end(h, n); }
 };
 
+// ensemble of independent members advanced by batched kernels
+struct EnsembleBase {
+    virtual ~EnsembleBase() {}
+    virtual int step(int nsteps) = 0;  // queues work, no final synchronize
+    virtual int synchronize() = 0;
+    virtual EngineBase *member(int m) = 0;
+    virtual int size() const = 0;
+    virtual void *stream_handle() = 0;
+    virtual void mark_dirty() = 0;
+    long long launches = 0;
+};
+
 // set by the engines, read by ga_last_error (thread local)
 void set_error(const std::string &msg);
 
 size_t noalloc_bytes_needed(const ga_config *c);
 int solve_pressure_noalloc(const ga_config *c, const ga_columns *cols, double *up, double *vp, double *wp,
                            double *pi, double step, cudaStream_t stream);
+
+EnsembleBase *make_ensemble_f64(const ga_config *cfgs, const ga_columns *cols, int n, int *rc);
+EnsembleBase *make_ensemble_f32(const ga_config *cfgs, const ga_columns *cols, int n, int *rc);
 
 EngineBase *make_engine_f64(const ga_config *cfg, const ga_columns *cols, int *rc);
 EngineBase *make_engine_f32(const ga_config *cfg, const ga_columns *cols, int *rc);

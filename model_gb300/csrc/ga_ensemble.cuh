@@ -1,0 +1,417 @@
+// ga_ensemble.cuh - ensembles of independent domains of uneven sizes, advanced
+// together: one launch per kernel phase covers every member.
+//
+// The reference runs ensemble members as separate serial models, one MPI task
+// each (run_ensemble, ensemble.cpp:45-144).  Here the members' parameters and
+// field pointers live in a packed device table; each batched kernel walks a
+// flattened list of virtual blocks (grid-stride, so the grid is sized to the
+// machine, not to the work), maps a virtual block to (member, local block) by
+// binary search over per-member block prefixes, and calls the same device
+// body as the single-domain kernel.  Every member therefore computes exactly
+// what it computes alone.  The buffer rotation of all members moves in lock
+// step and takes only two states, so two field tables cover it, and the two-
+// step cycle is captured in a CUDA graph.
+#pragma once
+#include <algorithm>
+#include <vector>
+
+#include "ga_engine.cuh"
+
+namespace ga {
+
+// per-member data of the pressure solve that is not in KParams
+template <typename T>
+struct MemberAux {
+    typename V2<T>::t *spec, *tw_i, *tw_j;
+    FftPlan plan_i, plan_j;
+    int KTy, psx;
+};
+
+enum { EK_ADV = 0, EK_MIRROR, EK_DIVY, EK_SX, EK_IFFTY, EK_POST, EK_KES, EK_COUNT };
+
+__device__ __forceinline__ int find_member(const long *pre, int nmem, long vb)
+{
+    int lo = 0, hi = nmem;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(pre + mid) <= vb) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) kb_advect(const KParams<T> *P, const KFields<T> *F, const long *pre, int nmem,
+                                                 double step, int what)
+{
+    const long total = pre[nmem];
+    for (long vb = blockIdx.x; vb < total; vb += gridDim.x) {
+        const int m = find_member(pre, nmem, vb);
+        const KParams<T> &p = P[m];
+        const long lb = vb - pre[m];
+        const int gx = (p.nx - 6 + ADV_TI - 1) / ADV_TI;
+        const double sdtg = step * p.dt_d * 9.8 * 0.5;  // step*dt*grav*0.5, advection.cpp:330
+        advect_tile_body(p, F[m], (int)(lb % gx), (int)(lb / gx), (T)step, (T)sdtg, what);
+        __syncthreads();
+    }
+}
+
+template <typename T>
+__global__ void kb_mirror(const KParams<T> *P, const KFields<T> *F, const long *pre, int nmem)
+{
+    const long total = pre[nmem];
+    for (long vb = blockIdx.x; vb < total; vb += gridDim.x) {
+        const int m = find_member(pre, nmem, vb);
+        const long t = (vb - pre[m]) * blockDim.x + threadIdx.x;
+        mirror_edges_body(P[m], F[m].P[FU], F[m].P[FV], F[m].P[FW], t);
+    }
+}
+
+template <typename T>
+__global__ void kb_div_fft_y(const KParams<T> *P, const KFields<T> *F, const MemberAux<T> *A, const long *pre,
+                             int nmem, double step)
+{
+    const long total = pre[nmem];
+    for (long vb = blockIdx.x; vb < total; vb += gridDim.x) {
+        const int m = find_member(pre, nmem, vb);
+        const KParams<T> &p = P[m];
+        const MemberAux<T> &a = A[m];
+        const long lb = vb - pre[m];
+        div_fft_y_body(p, F[m], a.spec, a.plan_j, a.tw_j, (T)(step * p.dt_d), a.KTy, (int)(lb % p.ni),
+                       (int)(lb / p.ni));
+        __syncthreads();
+    }
+}
+
+template <typename T>
+__global__ void kb_spectral_x(const KParams<T> *P, const MemberAux<T> *A, const long *pre, int nmem)
+{
+    const long total = pre[nmem];
+    for (long vb = blockIdx.x; vb < total; vb += gridDim.x) {
+        const int m = find_member(pre, nmem, vb);
+        const MemberAux<T> &a = A[m];
+        spectral_x_body(P[m], a.spec, a.plan_i, a.tw_i, a.psx, (int)(vb - pre[m]));
+        __syncthreads();
+    }
+}
+
+template <typename T>
+__global__ void kb_ifft_y_pi(const KParams<T> *P, const KFields<T> *F, const MemberAux<T> *A, const long *pre,
+                             int nmem)
+{
+    const long total = pre[nmem];
+    for (long vb = blockIdx.x; vb < total; vb += gridDim.x) {
+        const int m = find_member(pre, nmem, vb);
+        const KParams<T> &p = P[m];
+        const MemberAux<T> &a = A[m];
+        const long lb = vb - pre[m];
+        ifft_y_pi_body(p, F[m], a.spec, a.plan_j, a.tw_j, a.KTy, (int)(lb % p.ni), (int)(lb / p.ni));
+        __syncthreads();
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(POST_THREADS) kb_post(const KParams<T> *P, const KFields<T> *F, const long *pre,
+                                                        int nmem, int4 fl0, int4 fl1, double step)
+{
+    const long total = pre[nmem];
+    for (long vb = blockIdx.x; vb < total; vb += gridDim.x) {
+        const int m = find_member(pre, nmem, vb);
+        post_body(P[m], F[m], 7, fl0, fl1, (T)step, COLS_ALL, vb - pre[m]);
+        __syncthreads();
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(128) kb_kessler(const KParams<T> *P, const KFields<T> *F, const long *pre, int nmem,
+                                                  int *err)
+{
+    const long total = pre[nmem];
+    for (long vb = blockIdx.x; vb < total; vb += gridDim.x) {
+        const int m = find_member(pre, nmem, vb);
+        kessler_body(P[m], F[m], 1, err, (vb - pre[m]) * blockDim.x + threadIdx.x);
+    }
+}
+
+template <typename T>
+class Ensemble : public EnsembleBase {
+    typedef typename V2<T>::t T2;
+
+  public:
+    std::vector<Engine<T> *> mem;
+    int nmem = 0;
+    cudaStream_t stream = nullptr;
+    KParams<T> *d_p = nullptr;
+    KFields<T> *d_f[2] = {nullptr, nullptr};
+    MemberAux<T> *d_aux = nullptr;
+    long *d_pre[EK_COUNT] = {};
+    long total[EK_COUNT] = {};
+    size_t smem[EK_COUNT] = {};
+    int grid[EK_COUNT] = {};
+    int rot = 0;  // which field table is current
+    int *d_err = nullptr;
+    bool tables_dirty = true;
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    long long graph_launches[2] = {0, 0};
+    bool moist = false;
+    int dev = 0;
+
+    Ensemble(const ga_config *cfgs, const ga_columns *cols, int n, int *rc)
+    {
+        *rc = GA_OK;
+        nmem = n;
+        dev = cfgs[0].device;
+        cudaSetDevice(dev);
+        cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking);
+        moist = cfgs[0].microphysics_option == 1;
+        for (int m = 0; m < n; m++) {
+            Engine<T> *e = new Engine<T>(&cfgs[m], &cols[m]);
+            if (e->status != GA_OK) {
+                *rc = e->status;
+                delete e;
+                return;
+            }
+            if (e->psx == 0 || e->smem_adv > 200 * 1024) {
+                *rc = GA_ERR_UNSUPPORTED;
+                set_error("ensemble: member too large for the batched kernels");
+                delete e;
+                return;
+            }
+            mem.push_back(e);
+        }
+        cudaMalloc(&d_p, sizeof(KParams<T>) * n);
+        cudaMalloc(&d_f[0], sizeof(KFields<T>) * n);
+        cudaMalloc(&d_f[1], sizeof(KFields<T>) * n);
+        cudaMalloc(&d_aux, sizeof(MemberAux<T>) * n);
+        cudaMalloc(&d_err, sizeof(int));
+        cudaMemset(d_err, 0, sizeof(int));
+        // virtual-block prefixes per kernel phase
+        std::vector<long> cnt(n);
+        for (int k = 0; k < EK_COUNT; k++) {
+            std::vector<long> pre(n + 1, 0);
+            size_t sm = 0;
+            for (int m = 0; m < n; m++) {
+                Engine<T> &e = *mem[m];
+                long c = 0;
+                switch (k) {
+                case EK_ADV:
+                    c = (long)cdiv(e.NX - 6, ADV_TI) * cdiv(e.NY - 6, ADV_TJ);
+                    sm = std::max(sm, e.smem_adv);
+                    break;
+                case EK_MIRROR: c = cdiv(2L * (e.NX + e.NY - 2) * (e.NZ - 2), 256); break;
+                case EK_DIVY:
+                case EK_IFFTY:
+                    c = (long)e.kp.ni * cdiv(e.NZ - 2, e.KTy);
+                    sm = std::max(sm, e.smem_y);
+                    break;
+                case EK_SX:
+                    c = e.kp.nj;
+                    sm = std::max(sm, e.smem_sx);
+                    break;
+                case EK_POST: c = cdiv((long)e.NX * e.NY, POST_COLS); break;
+                case EK_KES: c = cdiv((long)(e.NX - 2) * (e.NY - 2) * (e.NZ - 2), 128); break;
+                }
+                pre[m + 1] = pre[m] + c;
+            }
+            total[k] = pre[n];
+            smem[k] = sm;
+            cudaMalloc(&d_pre[k], sizeof(long) * (n + 1));
+            cudaMemcpy(d_pre[k], pre.data(), sizeof(long) * (n + 1), cudaMemcpyHostToDevice);
+        }
+        const int optin = 200 * 1024;
+        cudaFuncSetAttribute(kb_advect<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+        cudaFuncSetAttribute(kb_div_fft_y<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+        cudaFuncSetAttribute(kb_spectral_x<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+        cudaFuncSetAttribute(kb_ifft_y_pi<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+        // persistent grids: as many blocks as stay resident
+        int nsm = 0;
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        auto occ = [&](const void *fn, int threads, size_t sm) {
+            int b = 0;
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, fn, threads, sm);
+            return std::max(1, b) * nsm;
+        };
+        grid[EK_ADV] = occ((const void *)kb_advect<T>, 256, smem[EK_ADV]);
+        grid[EK_MIRROR] = occ((const void *)kb_mirror<T>, 256, 0);
+        grid[EK_DIVY] = occ((const void *)kb_div_fft_y<T>, 256, smem[EK_DIVY]);
+        grid[EK_SX] = occ((const void *)kb_spectral_x<T>, 256, smem[EK_SX]);
+        grid[EK_IFFTY] = occ((const void *)kb_ifft_y_pi<T>, 256, smem[EK_IFFTY]);
+        grid[EK_POST] = occ((const void *)kb_post<T>, POST_THREADS, 0);
+        grid[EK_KES] = occ((const void *)kb_kessler<T>, 128, 0);
+        for (int k = 0; k < EK_COUNT; k++) grid[k] = (int)std::min<long>(grid[k], std::max(1L, total[k]));
+        if (cudaDeviceSynchronize() != cudaSuccess) *rc = GA_ERR_CUDA;
+    }
+
+    ~Ensemble() override
+    {
+        cudaSetDevice(dev);
+        if (stream) cudaStreamSynchronize(stream);
+        for (auto &g : graph)
+            if (g) cudaGraphExecDestroy(g);
+        for (auto *e : mem) delete e;
+        cudaFree(d_p);
+        cudaFree(d_f[0]);
+        cudaFree(d_f[1]);
+        cudaFree(d_aux);
+        cudaFree(d_err);
+        for (auto *p : d_pre) cudaFree(p);
+        if (stream) cudaStreamDestroy(stream);
+    }
+
+    // member tables: parameters (after basic-state refresh) and both rotation states
+    void refresh_tables()
+    {
+        for (auto *e : mem) {
+            if (e->btab_dirty) {
+                e->refresh_base();
+                tables_dirty = true;
+                e->sync_status();
+            }
+        }
+        if (!tables_dirty) return;
+        tables_dirty = false;
+        std::vector<KParams<T>> hp(nmem);
+        std::vector<KFields<T>> f0(nmem), f1(nmem);
+        std::vector<MemberAux<T>> ha(nmem);
+        for (int m = 0; m < nmem; m++) {
+            Engine<T> &e = *mem[m];
+            hp[m] = e.kp;
+            hp[m].dt_d = e.cfg.dt;
+            f0[m] = e.fields();
+            f1[m] = f0[m];
+            for (int f = 0; f < 7; f++) std::swap(f1[m].cur[f], f1[m].P[f]);
+            ha[m].spec = e.spec; ha[m].tw_i = e.tw_i; ha[m].tw_j = e.tw_j;
+            ha[m].plan_i = e.plan_i; ha[m].plan_j = e.plan_j;
+            ha[m].KTy = e.KTy; ha[m].psx = e.psx;
+        }
+        cudaMemcpy(d_p, hp.data(), sizeof(KParams<T>) * nmem, cudaMemcpyHostToDevice);
+        cudaMemcpy(d_f[0], f0.data(), sizeof(KFields<T>) * nmem, cudaMemcpyHostToDevice);
+        cudaMemcpy(d_f[1], f1.data(), sizeof(KFields<T>) * nmem, cudaMemcpyHostToDevice);
+        cudaMemcpy(d_aux, ha.data(), sizeof(MemberAux<T>) * nmem, cudaMemcpyHostToDevice);
+        rot = 0;
+        for (auto &g : graph)
+            if (g) {
+                cudaGraphExecDestroy(g);
+                g = nullptr;
+            }
+    }
+
+    void swap_all()
+    {
+        rot ^= 1;
+        for (auto *e : mem) e->swap_inner(true);
+    }
+
+    void rk3_step()
+    {
+        static const double steps[3] = {1. / 3., 0.5, 1.0};
+        for (int s = 0; s < 3; s++) {
+            const double st = steps[s];
+            KFields<T> *F = d_f[rot];
+            const int what = ADV_UV | ADV_WB | ADV_TH | (moist ? (ADV_Q | ADV_ZERO) : 0);
+            kb_advect<T><<<grid[EK_ADV], 256, smem[EK_ADV], stream>>>(d_p, F, d_pre[EK_ADV], nmem, st, what);
+            kb_mirror<T><<<grid[EK_MIRROR], 256, 0, stream>>>(d_p, F, d_pre[EK_MIRROR], nmem);
+            kb_div_fft_y<T><<<grid[EK_DIVY], dim3(16, 16), smem[EK_DIVY], stream>>>(d_p, F, d_aux, d_pre[EK_DIVY],
+                                                                                   nmem, st);
+            kb_spectral_x<T><<<grid[EK_SX], dim3(64, 4), smem[EK_SX], stream>>>(d_p, d_aux, d_pre[EK_SX], nmem);
+            kb_ifft_y_pi<T><<<grid[EK_IFFTY], dim3(16, 16), smem[EK_IFFTY], stream>>>(d_p, F, d_aux, d_pre[EK_IFFTY],
+                                                                                     nmem);
+            const int fu = PF_PROJECT | PF_SPONGE | PF_VBC, ft = PF_SPONGE | PF_VBC, fq = PF_ZERO | PF_SPONGE | PF_VBC;
+            kb_post<T><<<grid[EK_POST], POST_THREADS, 0, stream>>>(d_p, F, d_pre[EK_POST], nmem,
+                                                                    make_int4(fu, fu, fu, ft), make_int4(fq, fq, fq, 0),
+                                                                    st);
+            launches += 6;
+            if (s < 2) swap_all();
+        }
+        KFields<T> *F = d_f[rot];
+        if (moist) {
+            kb_kessler<T><<<grid[EK_KES], 128, 0, stream>>>(d_p, F, d_pre[EK_KES], nmem, d_err);
+            launches++;
+        }
+        const int fu = PF_SPONGE | PF_VBC | PF_RAYLEIGH | PF_WRITE_M, fq = PF_SPONGE | PF_VBC | PF_WRITE_M;
+        kb_post<T><<<grid[EK_POST], POST_THREADS, 0, stream>>>(d_p, F, d_pre[EK_POST], nmem, make_int4(fu, fu, fu, fu),
+                                                                make_int4(fq, fq, fq, 0), 1.0);
+        launches++;
+        swap_all();
+        for (auto *e : mem) {
+            e->bigcounter++;
+            e->mtime += e->cfg.dt;
+        }
+    }
+
+    int step(int nsteps) override
+    {
+        cudaSetDevice(dev);
+        refresh_tables();
+        int n = 0;
+        while (nsteps - n >= 2) {
+            const int parity = rot;
+            if (!graph[parity]) {
+                std::vector<long long> bc(nmem);
+                std::vector<double> mt(nmem);
+                for (int m = 0; m < nmem; m++) { bc[m] = mem[m]->bigcounter; mt[m] = mem[m]->mtime; }
+                const long long l0 = launches;
+                cudaGraph_t g = nullptr;
+                if (cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) break;
+                rk3_step();
+                rk3_step();
+                if (cudaStreamEndCapture(stream, &g) != cudaSuccess) { cudaGetLastError(); break; }
+                cudaError_t e = cudaGraphInstantiate(&graph[parity], g, 0);
+                cudaGraphDestroy(g);
+                graph_launches[parity] = launches - l0;
+                launches = l0;
+                for (int m = 0; m < nmem; m++) { mem[m]->bigcounter = bc[m]; mem[m]->mtime = mt[m]; }
+                if (e != cudaSuccess) { cudaGetLastError(); graph[parity] = nullptr; break; }
+            }
+            if (cudaGraphLaunch(graph[parity], stream) != cudaSuccess) break;
+            launches += graph_launches[parity];
+            for (auto *e : mem) {
+                e->bigcounter += 2;
+                e->mtime += 2 * e->cfg.dt;
+            }
+            n += 2;
+        }
+        for (; n < nsteps; n++) rk3_step();
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) {
+            set_error(std::string("CUDA launch: ") + cudaGetErrorString(e));
+            return GA_ERR_CUDA;
+        }
+        return GA_OK;
+    }
+
+    int synchronize() override
+    {
+        cudaSetDevice(dev);
+        cudaError_t e = cudaStreamSynchronize(stream);
+        if (e != cudaSuccess) {
+            set_error(std::string("CUDA: ") + cudaGetErrorString(e));
+            return GA_ERR_CUDA;
+        }
+        int h = 0;
+        cudaMemcpy(&h, d_err, sizeof(int), cudaMemcpyDeviceToHost);
+        if (h) {
+            set_error("Kessler evaporation E>100 in an ensemble member (the reference exits here)");
+            return GA_ERR_KESSLER;
+        }
+        return GA_OK;
+    }
+
+    EngineBase *member(int m) override { return (m >= 0 && m < nmem) ? mem[m] : nullptr; }
+    int size() const override { return nmem; }
+    void *stream_handle() override { return stream; }
+    void mark_dirty() override { tables_dirty = true; }
+};
+
+template <typename T>
+EnsembleBase *make_ensemble(const ga_config *cfgs, const ga_columns *cols, int n, int *rc)
+{
+    Ensemble<T> *e = new Ensemble<T>(cfgs, cols, n, rc);
+    if (*rc != GA_OK) {
+        delete e;
+        return nullptr;
+    }
+    return e;
+}
+
+}  // namespace ga

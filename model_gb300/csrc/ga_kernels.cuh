@@ -28,6 +28,7 @@ template <typename T>
 struct KParams {
     int nx, ny, nz;
     long n;
+    double dt_d;             // time step in double (step constants are formed from it)
     int ni, nj, ioff;        // spectral grid and its first physical column
     int periodic, moist, rf;
     T dtx, dty, dtz, dt, one_d_dx, one_d_dy, one_d_dz;
@@ -692,12 +693,12 @@ __device__ __forceinline__ void faces_top(const KParams<T> &p, const KFields<T> 
 }
 
 template <typename T>
-__global__ void __launch_bounds__(256) k_advect_tile(KParams<T> p, KFields<T> F, T step, T sdtg, int what)
+__device__ void advect_tile_body(const KParams<T> &p, const KFields<T> &F, int bx, int by, T step, T sdtg, int what)
 {
     extern __shared__ unsigned char smem_raw[];
     const int TI = ADV_TI, TJ = ADV_TJ, NF = ADV_NF;
     const int nz = p.nz, nzi = nz - 2;
-    const int i0 = 3 + blockIdx.x * TI, j0 = 3 + blockIdx.y * TJ;
+    const int i0 = 3 + bx * TI, j0 = 3 + by * TJ;
     const int ti = min(TI, p.nx - 3 - i0), tj = min(TJ, p.ny - 3 - j0);
     // face stores, each [field][...][level k = 0..nz-1]
     T *E = (T *)smem_raw;                    // [(TI+1)][TJ] columns, east face of column i0-1+a
@@ -812,16 +813,21 @@ __global__ void __launch_bounds__(256) k_advect_tile(KParams<T> p, KFields<T> F,
     }
 }
 
+template <typename T>
+__global__ void __launch_bounds__(256) k_advect_tile(KParams<T> p, KFields<T> F, T step, T sdtg, int what)
+{
+    advect_tile_body(p, F, blockIdx.x, blockIdx.y, step, sdtg, what);
+}
+
 // ---------------------------------------------------------------------------
 // lateral copies of UP/VP/WP before the pressure solve:
 // mirror_boundaries (boundaries.cpp:363-379) or periodic_uvw_boundaries
 // (:546-555).  Writes only edge points, reads only non-edge points.
 // ---------------------------------------------------------------------------
 template <typename T>
-__global__ void k_mirror_edges(KParams<T> p, T *a, T *b, T *c)
+__device__ void mirror_edges_body(const KParams<T> &p, T *a, T *b, T *c, long t)
 {
     const int ne = 2 * (p.nx + p.ny - 2);  // edge columns
-    long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
     const int nzi = p.nz - 2;
     if (t >= (long)ne * nzi) return;
     const int k = 1 + (int)(t % nzi);
@@ -836,6 +842,11 @@ __global__ void k_mirror_edges(KParams<T> p, T *a, T *b, T *c)
     a[d] = a[s];
     b[d] = b[s];
     c[d] = c[s];
+}
+template <typename T>
+__global__ void k_mirror_edges(KParams<T> p, T *a, T *b, T *c)
+{
+    mirror_edges_body(p, a, b, c, (long)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // periodic_boundaries_east_west (boundaries.cpp:562-574) for up to 4 fields:
@@ -988,15 +999,15 @@ __device__ __forceinline__ T divergence(const KParams<T> &p, const KFields<T> &F
 // divergence3d_periodic) + forward FFT along y.  Block = (spectral row i,
 // tile of KT levels starting at level 1).
 template <typename T>
-__global__ void k_div_fft_y(KParams<T> p, KFields<T> F, typename V2<T>::t *spec, FftPlan pj,
-                            const typename V2<T>::t *tw, T sdt, int KT)
+__device__ void div_fft_y_body(const KParams<T> &p, const KFields<T> &F, typename V2<T>::t *spec, const FftPlan &pj,
+                               const typename V2<T>::t *tw, T sdt, int KT, int bx, int by)
 {
     typedef typename V2<T>::t T2;
     extern __shared__ unsigned char smem_raw[];
     T2 *a = (T2 *)smem_raw;
     T2 *b = a + (long)p.nj * KT;
-    const int is = blockIdx.x;
-    const int k0 = 1 + blockIdx.y * KT;
+    const int is = bx;
+    const int k0 = 1 + by * KT;
     const int kt = min(KT, p.nz - 1 - k0);
     int ii;
     if (!p.periodic) ii = min(max(is, 1), p.nx - 2);
@@ -1017,6 +1028,12 @@ __global__ void k_div_fft_y(KParams<T> p, KFields<T> F, typename V2<T>::t *spec,
     for (int q = threadIdx.y; q < p.nj; q += blockDim.y)
         for (int l = threadIdx.x; l < kt; l += blockDim.x)
             spec[((long)is * p.nj + q) * p.nz + k0 + l] = r[q * KT + l];
+}
+template <typename T>
+__global__ void k_div_fft_y(KParams<T> p, KFields<T> F, typename V2<T>::t *spec, FftPlan pj,
+                            const typename V2<T>::t *tw, T sdt, int KT)
+{
+    div_fft_y_body(p, F, spec, pj, tw, sdt, KT, blockIdx.x, blockIdx.y);
 }
 
 // FFT along x of the spectral buffer for one y-wavenumber q and a tile of
@@ -1243,8 +1260,8 @@ __global__ void k_thomas(KParams<T> p, typename V2<T>::t *spec, int TC)
 }
 
 template <typename T>
-__global__ void k_spectral_x(KParams<T> p, typename V2<T>::t *spec, FftPlan pi, const typename V2<T>::t *tw,
-                             int ps)
+__device__ void spectral_x_body(const KParams<T> &p, typename V2<T>::t *spec, const FftPlan &pi,
+                                const typename V2<T>::t *tw, int ps, int bx)
 {
     typedef typename V2<T>::t T2;
     extern __shared__ unsigned char smem_raw[];
@@ -1253,7 +1270,7 @@ __global__ void k_spectral_x(KParams<T> p, typename V2<T>::t *spec, FftPlan pi, 
     __shared__ double pcr_wk[2][640];
     T2 *a = (T2 *)smem_raw;
     T2 *b = a + (long)p.ni * ps;
-    const int q = blockIdx.x;
+    const int q = bx;
     const int nl = p.nz - 2;  // levels 1..NZ-2 are the lines
     const int tid = threadIdx.y * blockDim.x + threadIdx.x, nth = blockDim.x * blockDim.y;
     for (int k = tid; k < p.nz; k += nth) {
@@ -1307,20 +1324,26 @@ __global__ void k_spectral_x(KParams<T> p, typename V2<T>::t *spec, FftPlan pi, 
     for (int i = threadIdx.y; i < p.ni; i += blockDim.y)
         for (int l = threadIdx.x; l < nl; l += blockDim.x) spec[((long)i * p.nj + q) * p.nz + 1 + l] = o[i * ps + l];
 }
+template <typename T>
+__global__ void k_spectral_x(KParams<T> p, typename V2<T>::t *spec, FftPlan pi, const typename V2<T>::t *tw,
+                             int ps)
+{
+    spectral_x_body(p, spec, pi, tw, ps, blockIdx.x);
+}
 
 // inverse FFT along y + PI = real part, with the level copies of
 // poisson_fft3d (pressure.cpp:878-892) and the lateral placement of
 // mirror_boundaries(PI) or periodic_pressure_boundaries.
 template <typename T>
-__global__ void k_ifft_y_pi(KParams<T> p, KFields<T> F, typename V2<T>::t *spec, FftPlan pj,
-                            const typename V2<T>::t *tw, int KT)
+__device__ void ifft_y_pi_body(const KParams<T> &p, const KFields<T> &F, typename V2<T>::t *spec, const FftPlan &pj,
+                               const typename V2<T>::t *tw, int KT, int bx, int by)
 {
     typedef typename V2<T>::t T2;
     extern __shared__ unsigned char smem_raw[];
     T2 *a = (T2 *)smem_raw;
     T2 *b = a + (long)p.nj * KT;
-    const int is = blockIdx.x;
-    const int k0 = 1 + blockIdx.y * KT;
+    const int is = bx;
+    const int k0 = 1 + by * KT;
     const int kt = min(KT, p.nz - 1 - k0);
     for (int q = threadIdx.y; q < p.nj; q += blockDim.y)
         for (int l = threadIdx.x; l < KT; l += blockDim.x) {
@@ -1365,6 +1388,13 @@ __global__ void k_ifft_y_pi(KParams<T> p, KFields<T> F, typename V2<T>::t *spec,
             }
         }
     }
+}
+
+template <typename T>
+__global__ void k_ifft_y_pi(KParams<T> p, KFields<T> F, typename V2<T>::t *spec, FftPlan pj,
+                            const typename V2<T>::t *tw, int KT)
+{
+    ifft_y_pi_body(p, F, spec, pj, tw, KT, blockIdx.x, blockIdx.y);
 }
 
 // ---------------------------------------------------------------------------
@@ -1444,13 +1474,13 @@ __device__ __forceinline__ void post_column(const int mode, const long c, const 
 }
 
 template <typename T>
-__global__ void __launch_bounds__(POST_THREADS) k_post(KParams<T> p, KFields<T> F, int nfields, int4 fl0, int4 fl1,
-                                                       T step, int cols)
+__device__ void post_body(const KParams<T> &p, const KFields<T> &F, int nfields, int4 fl0, int4 fl1, T step, int cols,
+                          long bx)
 {
     __shared__ T edge[7][POST_COLS][2];
     const int nz = p.nz, sx = p.ny * p.nz, sy = p.nz;
     const int flv[7] = {fl0.x, fl0.y, fl0.z, fl0.w, fl1.x, fl1.y, fl1.z};
-    const long c0 = (long)blockIdx.x * POST_COLS;
+    const long c0 = bx * POST_COLS;
     T vals[7][POST_R];
 #pragma unroll
     for (int r = 0; r < POST_R; ++r) {
@@ -1544,16 +1574,22 @@ __global__ void __launch_bounds__(POST_THREADS) k_post(KParams<T> p, KFields<T> 
     }
 }
 
+template <typename T>
+__global__ void __launch_bounds__(POST_THREADS) k_post(KParams<T> p, KFields<T> F, int nfields, int4 fl0, int4 fl1,
+                                                       T step, int cols)
+{
+    post_body(p, F, nfields, fl0, fl1, step, cols, blockIdx.x);
+}
+
 // ---------------------------------------------------------------------------
 // Kessler warm rain, pointwise (kessler.cpp:25-183); the k=1 thread of each
 // column then adds the Eulerian precipitation (precip_rate,
 // microphysics.cpp:143-160) when rain_fallout == 1.
 // ---------------------------------------------------------------------------
 template <typename T>
-__global__ void __launch_bounds__(128) k_kessler(KParams<T> p, KFields<T> F, int precip, int *err)
+__device__ void kessler_body(const KParams<T> &p, const KFields<T> &F, int precip, int *err, long t)
 {
     const int nzi = p.nz - 2, nyi = p.ny - 2, nxi = p.nx - 2;
-    long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long)nxi * nyi * nzi) return;
     const int k = 1 + (int)(t % nzi);
     const int j = 1 + (int)((t / nzi) % nyi);
@@ -1621,6 +1657,11 @@ __global__ void __launch_bounds__(128) k_kessler(KParams<T> p, KFields<T> F, int
         const double inc = (double)(p.rhow[1] * T(0.5) * (F.vt[i0] + F.vt[ix]) * T(0.5) * (QRP[i0] + qrp) * dt);
         F.accrain[(long)i * p.ny + j] += inc;
     }
+}
+template <typename T>
+__global__ void __launch_bounds__(128) k_kessler(KParams<T> p, KFields<T> F, int precip, int *err)
+{
+    kessler_body(p, F, precip, err, (long)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // fall speed over [1,NX-1) x [1,NY-1) from the forecast rain (semi-Lagrangian
