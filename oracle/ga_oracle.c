@@ -1137,3 +1137,6 @@ int ora_step(ora_state *S, int nsteps)
 
 long long ora_bigcounter(ora_state *S) { return S->bigcounter; }
 int ora_error(ora_state *S) { return S->err; }
+
+/* Tangent-linear model and adjoint of the dry step (test infrastructure). */
+#include "ga_oracle_lin.c"

@@ -37,6 +37,21 @@ int ora_columns_build(int nz, double dz, double height_lowest_level,
                       const double *tb_in, const double *qb_in, ga_column_store *out);
 int ora_coriolis_build(int ny, double dy, double corner_lat, double *f_out);
 
+/* Tangent-linear model and adjoint of the dry, non-periodic step
+ * (ga_oracle_lin.c).  An ora_lin holds perturbation (or adjoint) copies of the
+ * current, P and M buffers of u, v, w, theta and of pi; its slots follow the
+ * state's rotation. */
+typedef struct ora_lin ora_lin;
+ora_lin *ora_lin_create(ora_state *s);
+void     ora_lin_destroy(ora_lin *l);
+int      ora_lin_set(ora_lin *l, int field, int slot, const double *src, long n);
+int      ora_lin_get(ora_lin *l, int field, int slot, double *dst, long n);
+/* advance the state and the tangent together */
+int      ora_tlm_step(ora_state *s, ora_lin *t, int nsteps);
+/* advance the state nsteps (recording), then map the adjoint of the final
+ * state held in a to the adjoint of the initial state */
+int      ora_adj_run(ora_state *s, ora_lin *a, int nsteps);
+
 #ifdef __cplusplus
 }
 #endif

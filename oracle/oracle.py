@@ -51,6 +51,13 @@ def lib() -> C.CDLL:
         L.ora_bigcounter.argtypes = [C.c_void_p]
         L.ora_bigcounter.restype = C.c_longlong
         L.ora_error.argtypes = [C.c_void_p]
+        L.ora_lin_create.argtypes = [C.c_void_p]
+        L.ora_lin_create.restype = C.c_void_p
+        L.ora_lin_destroy.argtypes = [C.c_void_p]
+        L.ora_lin_set.argtypes = [C.c_void_p, C.c_int, C.c_int, _DP, C.c_long]
+        L.ora_lin_get.argtypes = [C.c_void_p, C.c_int, C.c_int, _DP, C.c_long]
+        L.ora_tlm_step.argtypes = [C.c_void_p, C.c_void_p, C.c_int]
+        L.ora_adj_run.argtypes = [C.c_void_p, C.c_void_p, C.c_int]
         abi.declare(L, "ora_")
         _lib = L
     return _lib
@@ -144,6 +151,61 @@ class Oracle:
         out["vt"] = self.get(abi.GA_VT)
         out["accrain"] = self.get(abi.GA_ACCRAIN)
         return out
+
+
+LIN_FIELDS = (abi.GA_U, abi.GA_V, abi.GA_W, abi.GA_TH)
+LIN_SLOTS = (abi.GA_SLOT_CUR, abi.GA_SLOT_P, abi.GA_SLOT_M)
+
+
+class OracleLin:
+    """Perturbation or adjoint buffers of an Oracle's dry state (current, P,
+    M of u, v, w, theta, and pi), rotating with it (ga_oracle_lin.c)."""
+
+    def __init__(self, oracle: Oracle):
+        self.o = oracle
+        self.h = lib().ora_lin_create(oracle.h)
+        if not self.h:
+            raise RuntimeError("ora_lin_create failed (dry, non-periodic only)")
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h:
+            lib().ora_lin_destroy(h)
+            self.h = None
+
+    def set(self, field: int, slot: int, arr) -> None:
+        a = np.ascontiguousarray(arr, dtype=np.float64).ravel()
+        if lib().ora_lin_set(self.h, field, slot, _ptr(a), a.size) != 0:
+            raise RuntimeError("ora_lin_set")
+
+    def get(self, field: int, slot: int = 0) -> np.ndarray:
+        a = np.zeros(self.o.n3)
+        if lib().ora_lin_get(self.h, field, slot, _ptr(a), a.size) != 0:
+            raise RuntimeError("ora_lin_get")
+        return a
+
+    def set_all(self, d: dict) -> None:
+        """d maps (field, slot) -> array; (GA_PI, 0) for pi."""
+        for (f, s), v in d.items():
+            self.set(f, s, v)
+
+    def get_all(self) -> dict:
+        d = {(f, s): self.get(f, s) for f in LIN_FIELDS for s in LIN_SLOTS}
+        d[(abi.GA_PI, 0)] = self.get(abi.GA_PI)
+        return d
+
+    def tlm(self, nsteps: int) -> None:
+        """Advance the oracle's state and these perturbations together."""
+        rc = lib().ora_tlm_step(self.o.h, self.h, nsteps)
+        if rc != 0:
+            raise RuntimeError(f"ora_tlm_step -> {rc}")
+
+    def adjoint(self, nsteps: int) -> None:
+        """Advance the oracle's state nsteps; map the adjoint of the final state
+        held here to the adjoint of the initial state."""
+        rc = lib().ora_adj_run(self.o.h, self.h, nsteps)
+        if rc != 0:
+            raise RuntimeError(f"ora_adj_run -> {rc}")
 
 
 # ---------------------------------------------------------------------------
