@@ -217,6 +217,34 @@ GA_API void *ga_stream(ga_ctx *ctx);
 GA_API void *ga_field_device_ptr(ga_ctx *ctx, int field, int slot);
 
 /*
+ * Tangent-linear model and adjoint of the step.  No counterpart in the
+ * reference, which has no linearisation; this differentiates exactly the step
+ * ga_step runs, for dry (microphysics_option 0), non-periodic contexts
+ * (GA_ERR_UNSUPPORTED otherwise), in the context's precision.
+ *
+ * The context holds one set of perturbation buffers shaped like the state:
+ * current, P and M slots of GA_U, GA_V, GA_W, GA_TH, plus GA_PI (slot
+ * ignored), rotating with the state.  Upwind signs are frozen at the
+ * trajectory.
+ *
+ * ga_tlm_step advances the state and the perturbations together nsteps.
+ *
+ * ga_adjoint advances the state nsteps from its current value (it ends there,
+ * with the counters advanced) and maps the adjoint held in the perturbation
+ * buffers, taken as the gradient of a function of the final state, to the
+ * gradient with respect to the initial state.  The state is checkpointed every
+ * `checkpoint_every` steps (<= 0: one segment) and each segment is recomputed,
+ * recording the stage-start fields, before its adjoint runs: device memory
+ * holds nsteps/checkpoint_every + 1 states and checkpoint_every steps of
+ * trajectory (12 fields each).  The adjoint kernels are in gather form (no
+ * atomics).  The GA_PI entry is zero on return: the step never reads pi.
+ */
+GA_API int ga_lin_set_field(ga_ctx *ctx, int field, int slot, const double *host, size_t n);
+GA_API int ga_lin_get_field(ga_ctx *ctx, int field, int slot, double *host, size_t n);
+GA_API int ga_tlm_step(ga_ctx *ctx, int nsteps);
+GA_API int ga_adjoint(ga_ctx *ctx, int nsteps, int checkpoint_every);
+
+/*
  * Ensembles.  The reference runs ensemble members as separate serial models
  * farmed out over MPI tasks (run_ensemble, ensemble.cpp:45-144).  Here the
  * members (independent domains; grids, spacings and time steps may differ)

@@ -59,6 +59,10 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     L.ga_stream.restype = C.c_void_p
     L.ga_field_device_ptr.argtypes = [C.c_void_p, C.c_int, C.c_int]
     L.ga_field_device_ptr.restype = C.c_void_p
+    L.ga_lin_set_field.argtypes = [C.c_void_p, C.c_int, C.c_int, _DP, C.c_size_t]
+    L.ga_lin_get_field.argtypes = [C.c_void_p, C.c_int, C.c_int, _DP, C.c_size_t]
+    L.ga_tlm_step.argtypes = [C.c_void_p, C.c_int]
+    L.ga_adjoint.argtypes = [C.c_void_p, C.c_int, C.c_int]
     L.ga_ensemble_create.argtypes = [C.POINTER(abi.GaConfig), C.POINTER(abi.GaColumns), C.c_int,
                                      C.POINTER(C.c_void_p)]
     L.ga_ensemble_destroy.argtypes = [C.c_void_p]
@@ -244,6 +248,38 @@ class Model:
 
     def device_ptr(self, field: int, slot: int = 0) -> int:
         return self.L.ga_field_device_ptr(self.h, field, slot) or 0
+
+    # ---- tangent-linear model and adjoint (dry, non-periodic) -------------
+    LIN_FIELDS = (abi.GA_U, abi.GA_V, abi.GA_W, abi.GA_TH)
+    LIN_SLOTS = (abi.GA_SLOT_CUR, abi.GA_SLOT_P, abi.GA_SLOT_M)
+
+    def lin_set(self, field: int, slot: int, arr) -> None:
+        a = np.ascontiguousarray(arr, dtype=np.float64).ravel()
+        self._check(self.L.ga_lin_set_field(self.h, field, slot, _ptr(a), a.size), "ga_lin_set_field")
+
+    def lin_get(self, field: int, slot: int = 0) -> np.ndarray:
+        a = np.zeros(self.n3)
+        self._check(self.L.ga_lin_get_field(self.h, field, slot, _ptr(a), self.n3), "ga_lin_get_field")
+        return a
+
+    def lin_set_all(self, d: dict) -> None:
+        """d maps (field, slot) -> array; (GA_PI, 0) for pi."""
+        for (f, s), v in d.items():
+            self.lin_set(f, s, v)
+
+    def lin_get_all(self) -> dict:
+        d = {(f, s): self.lin_get(f, s) for f in self.LIN_FIELDS for s in self.LIN_SLOTS}
+        d[(abi.GA_PI, 0)] = self.lin_get(abi.GA_PI)
+        return d
+
+    def tlm_step(self, n: int = 1) -> None:
+        """Advance the state and the perturbation buffers together."""
+        self._check(self.L.ga_tlm_step(self.h, n), "ga_tlm_step")
+
+    def adjoint(self, n: int, checkpoint_every: int = 0) -> None:
+        """Advance the state n steps, then map the adjoint of the final state
+        held in the perturbation buffers to that of the initial state."""
+        self._check(self.L.ga_adjoint(self.h, n, checkpoint_every), "ga_adjoint")
 
 
 class Ensemble:

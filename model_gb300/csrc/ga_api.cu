@@ -219,6 +219,38 @@ int ga_check_finite(ga_ctx *ctx)
 
 long long ga_launch_count(ga_ctx *ctx) { return ctx ? ctx->e->launches : -1; }
 
+int ga_lin_set_field(ga_ctx *ctx, int field, int slot, const double *host, size_t n)
+{
+    if (!ctx || !host) return fail(GA_ERR_ARG, "ga_lin_set_field: null argument");
+    if (!((field >= GA_U && field <= GA_TH) || field == GA_PI))
+        return fail(GA_ERR_ARG, "ga_lin_set_field: field must be GA_U..GA_TH or GA_PI");
+    int rc = ctx->e->lin_set_field(field, slot, host, n);
+    if (rc == GA_ERR_ARG) set_error("ga_lin_set_field: bad slot or size");
+    return rc;
+}
+
+int ga_lin_get_field(ga_ctx *ctx, int field, int slot, double *host, size_t n)
+{
+    if (!ctx || !host) return fail(GA_ERR_ARG, "ga_lin_get_field: null argument");
+    if (!((field >= GA_U && field <= GA_TH) || field == GA_PI))
+        return fail(GA_ERR_ARG, "ga_lin_get_field: field must be GA_U..GA_TH or GA_PI");
+    int rc = ctx->e->lin_get_field(field, slot, host, n);
+    if (rc == GA_ERR_ARG) set_error("ga_lin_get_field: bad slot or size");
+    return rc;
+}
+
+int ga_tlm_step(ga_ctx *ctx, int nsteps)
+{
+    if (!ctx || nsteps < 0) return fail(GA_ERR_ARG, "ga_tlm_step: bad arguments");
+    return ctx->e->tlm_step(nsteps);
+}
+
+int ga_adjoint(ga_ctx *ctx, int nsteps, int checkpoint_every)
+{
+    if (!ctx || nsteps < 0) return fail(GA_ERR_ARG, "ga_adjoint: bad arguments");
+    return ctx->e->adjoint(nsteps, checkpoint_every);
+}
+
 void *ga_stream(ga_ctx *ctx) { return ctx ? (void *)ctx->e->stream : nullptr; }
 
 void *ga_field_device_ptr(ga_ctx *ctx, int field, int slot)

@@ -4,6 +4,7 @@
 #pragma once
 #include <cmath>
 #include <cstring>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -33,6 +34,9 @@ static inline FftPlan make_fft_plan(int n)
     }
     return P;
 }
+
+template <typename T>
+struct Lin;
 
 template <typename T>
 class Engine : public EngineBase {
@@ -66,6 +70,14 @@ class Engine : public EngineBase {
     long long graph_launches[2] = {0, 0};
     bool use_graphs = true;
     int status = GA_OK;
+    std::unique_ptr<LinBase> lin;  // tangent-linear / adjoint buffers, on first use
+
+    Lin<T> *linear();
+    int lin_supported() const;
+    int lin_set_field(int field, int slot, const double *host, size_t n) override;
+    int lin_get_field(int field, int slot, double *host, size_t n) override;
+    int tlm_step(int nsteps) override;
+    int adjoint(int nsteps, int checkpoint_every) override;
 
     template <typename X>
     X *dalloc(size_t n)
@@ -619,13 +631,19 @@ class Engine : public EngineBase {
         return GA_OK;
     }
 
-    // one RK3 step: s_integrate_rk3 (driver_serial.cpp:178-286), fused
-    void rk3_step()
+    // one RK3 step: s_integrate_rk3 (driver_serial.cpp:178-286), fused.
+    // rec (optional): the stage-start u, v, w, theta are copied to
+    // rec + (4*stage + field)*N, the trajectory of the adjoint.
+    void rk3_step(T *rec = nullptr)
     {
         static const double steps[3] = {1. / 3., 0.5, 1.0};
         const bool moist = kp.moist;
         for (int s = 0; s < 3; s++) {
             const double st = steps[s];
+            if (rec)
+                for (int f = 0; f < 4; f++)
+                    cudaMemcpyAsync(rec + (size_t)(4 * s + f) * N, buf[f][ci[f]], N * sizeof(T),
+                                    cudaMemcpyDeviceToDevice, stream);
             advect(st, ADV_UV | ADV_WB | ADV_TH | (moist ? (ADV_Q | ADV_ZERO) : 0));
             solve_pressure(st);
             int fl[7] = {0, 0, 0, 0, 0, 0, 0};
@@ -732,3 +750,6 @@ EngineBase *make_engine(const ga_config *cfg, const ga_columns *cols, int *rc)
 }
 
 }  // namespace ga
+
+// tangent-linear model and adjoint: members of Engine<T> declared above
+#include "ga_lin.cuh"

@@ -15,6 +15,11 @@ enum ProfCat { PC_ADVECT = 0, PC_EDGES, PC_DIV_FFT_Y, PC_FFT_X, PC_THOMAS, PC_IF
 static const char *const kProfNames[PC_COUNT] = {"advect", "edges", "div_fft_y", "fft_x", "thomas",
                                                  "ifft_y_pi", "post", "kessler", "ppm", "copy"};
 
+// tangent-linear / adjoint state of an engine (ga_lin.cuh)
+struct LinBase {
+    virtual ~LinBase() {}
+};
+
 struct EngineBase {
     virtual ~EngineBase()
     {
@@ -29,6 +34,11 @@ struct EngineBase {
     virtual int step(int nsteps) = 0;
     virtual int check_finite() = 0;
     virtual void *field_ptr(int field, int slot) = 0;
+    // tangent-linear model and adjoint (dry, non-periodic contexts)
+    virtual int lin_set_field(int field, int slot, const double *host, size_t n) = 0;
+    virtual int lin_get_field(int field, int slot, double *host, size_t n) = 0;
+    virtual int tlm_step(int nsteps) = 0;
+    virtual int adjoint(int nsteps, int checkpoint_every) = 0;
     cudaStream_t stream = nullptr;
     long long launches = 0;
     long long bigcounter = 0;

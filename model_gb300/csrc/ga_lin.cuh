@@ -1,0 +1,340 @@
+// ga_lin.cuh - host side of the tangent-linear model and the adjoint of one
+// precision (dry, non-periodic contexts): perturbation / adjoint buffers that
+// rotate like the state's, the TLM step, and the checkpointed adjoint sweep.
+// Included at the end of ga_engine.cuh; defines Engine<T>'s linearisation
+// members.
+#pragma once
+#include <memory>
+
+#include "ga_engine.cuh"
+#include "ga_lin_kernels.cuh"
+
+namespace ga {
+
+template <typename T>
+struct Lin : LinBase {
+    typedef typename V2<T>::t T2;
+    Engine<T> &e;
+    long N;
+    T *lb[4][3] = {};
+    int lci[4], lpi[4], lmi[4];
+    T *lpi_f = nullptr;  // pi (perturbation or adjoint)
+    T *dbar = nullptr;   // adjoint of the divergence, real [i][j][k]
+    T *tape = nullptr;   // stage-start u, v, w, theta of every step of a segment
+    size_t tape_steps = 0;
+    T *ckpt = nullptr;   // full states (current, P, M of u, v, w, theta)
+    size_t ckpt_slots = 0;
+
+    explicit Lin(Engine<T> &eng) : e(eng), N(eng.N)
+    {
+        for (int f = 0; f < 4; f++) {
+            for (int s = 0; s < 3; s++) lb[f][s] = e.template dalloc<T>(N);
+            lci[f] = 0; lpi[f] = 1; lmi[f] = 2;
+        }
+        lpi_f = e.template dalloc<T>(N);
+        dbar = e.template dalloc<T>(N);
+        const int optin = 200 * 1024;
+        cudaFuncSetAttribute(k_adj_fft_y_in<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+        cudaFuncSetAttribute(k_adj_ifft_y_out<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+        cudaFuncSetAttribute(k_thomas_adj<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+    }
+    ~Lin() override
+    {
+        if (tape) cudaFree(tape);
+        if (ckpt) cudaFree(ckpt);
+    }
+
+    KFields<T> fields() const
+    {
+        KFields<T> F;
+        std::memset(&F, 0, sizeof(F));
+        for (int f = 0; f < 4; f++) {
+            F.cur[f] = lb[f][lci[f]];
+            F.P[f] = lb[f][lpi[f]];
+            F.M[f] = lb[f][lmi[f]];
+        }
+        for (int b = 0; b < 6; b++) F.bar[b] = e.bar[b];
+        F.pi = lpi_f;
+        F.vt = e.vt;
+        return F;
+    }
+
+    T *slot_ptr(int field, int slot)
+    {
+        if (field == GA_PI) return lpi_f;
+        if (field < 0 || field >= 4) return nullptr;
+        if (slot == GA_SLOT_CUR) return lb[field][lci[field]];
+        if (slot == GA_SLOT_P) return lb[field][lpi[field]];
+        if (slot == GA_SLOT_M) return lb[field][lmi[field]];
+        return nullptr;
+    }
+
+    // run the engine's (linear) forward kernels on these buffers
+    void exchange()
+    {
+        for (int f = 0; f < 4; f++) {
+            for (int s = 0; s < 3; s++) std::swap(e.buf[f][s], lb[f][s]);
+            std::swap(e.ci[f], lci[f]);
+            std::swap(e.pi_[f], lpi[f]);
+            std::swap(e.mi[f], lmi[f]);
+        }
+        std::swap(e.pi, lpi_f);
+    }
+    void swap_inner()
+    {
+        for (int f = 0; f < 4; f++) std::swap(lci[f], lpi[f]);
+    }
+
+    static void stage_flags(int *fl)
+    {
+        for (int f = 0; f < 7; f++) fl[f] = 0;
+        fl[FU] = fl[FV] = fl[FW] = PF_PROJECT | PF_SPONGE | PF_VBC;
+        fl[FTH] = PF_SPONGE | PF_VBC;
+    }
+    static void final_flags(int *fl)
+    {
+        for (int f = 0; f < 7; f++) fl[f] = 0;
+        fl[FU] = fl[FV] = fl[FW] = fl[FTH] = PF_SPONGE | PF_VBC | PF_RAYLEIGH | PF_WRITE_M;
+    }
+
+    // one step of the state and of the perturbations together
+    void tlm_step()
+    {
+        static const double steps[3] = {1. / 3., 0.5, 1.0};
+        const long tot = (long)(e.NX - 6) * (e.NY - 6) * (e.NZ - 2);
+        int fl[7];
+        for (int s = 0; s < 3; s++) {
+            const double st = steps[s];
+            const T sdtg = (T)(st * e.cfg.dt * 9.8 * 0.5);
+            e.advect(st, ADV_UV | ADV_WB | ADV_TH);
+            k_tl_advect<T><<<cdiv(tot, 128), 128, 0, e.stream>>>(e.kp, e.fields(), fields(), (T)st, sdtg);
+            e.launches++;
+            stage_flags(fl);
+            e.solve_pressure(st);
+            e.post(fl, 7, st, true);
+            exchange();
+            e.solve_pressure(st);
+            e.post(fl, 7, st, true);
+            exchange();
+            if (s < 2) {
+                e.swap_inner(true);
+                swap_inner();
+            }
+        }
+        final_flags(fl);
+        e.post(fl, 7, 1.0, true);
+        exchange();
+        e.post(fl, 7, 1.0, true);
+        exchange();
+        e.swap_inner(true);
+        swap_inner();
+        e.mtime += e.cfg.dt;
+        e.bigcounter++;
+    }
+
+    // transposed pressure solve: pi-bar -> P-bar of u, v, w (pi-bar is left
+    // as read; the next transposed projection overwrites it)
+    void adj_pressure(double st)
+    {
+        KFields<T> A = fields();
+        const int nkt_y = cdiv(e.NZ - 2, e.KTy), nkt_x = cdiv(e.NZ - 2, e.KTx);
+        const dim3 by_y(e.KTy, std::max(1, 256 / e.KTy)), by_x(e.KTx, std::max(1, 256 / e.KTx));
+        cudaStream_t s = e.stream;
+        k_adj_fft_y_in<T><<<dim3(e.kp.ni, nkt_y), by_y, e.smem_y, s>>>(e.kp, lpi_f, e.spec, e.plan_j, e.tw_j, e.KTy);
+        k_fft_x<T><<<dim3(e.kp.nj, nkt_x), by_x, e.smem_x, s>>>(e.kp, e.spec, e.plan_i, e.tw_i, 0, e.KTx);
+        const long ncol = (long)e.kp.ni * e.kp.nj;
+        k_thomas_adj<T><<<cdiv(ncol, e.TC), e.TC, e.smem_th, s>>>(e.kp, e.spec, e.TC);
+        k_fft_x<T><<<dim3(e.kp.nj, nkt_x), by_x, e.smem_x, s>>>(e.kp, e.spec, e.plan_i, e.tw_i, 1, e.KTx);
+        k_adj_ifft_y_out<T><<<dim3(e.kp.ni, nkt_y), by_y, e.smem_y, s>>>(e.kp, e.spec, dbar, e.plan_j, e.tw_j, e.KTy);
+        k_adj_div<T><<<cdiv(N, 256), 256, 0, s>>>(e.kp, A, dbar, (T)(st * e.cfg.dt));
+        k_adj_mirror<T><<<e.NZ - 2, 256, 0, s>>>(e.kp, A.P[FU], A.P[FV], A.P[FW]);
+        e.launches += 7;
+    }
+
+    // adjoint of one step about the trajectory rec (stage-start u, v, w,
+    // theta: rec + (4*stage + field)*N).  first: the adjoint of the final pi
+    // held in pi-bar enters here.
+    void adj_step(const T *rec, bool first)
+    {
+        static const double steps[3] = {1. / 3., 0.5, 1.0};
+        cudaStream_t s = e.stream;
+        const long ncolblk = cdiv((long)e.NX * e.NY, POST_COLS);
+        const long tot = (long)(e.NX - 6) * (e.NY - 6) * (e.NZ - 2);
+        const dim3 gadv(cdiv(e.NX, AJ_TI), cdiv(e.NY, AJ_TJ), cdiv(e.NZ, AJ_TK));
+        swap_inner();  // advance_outer's swap
+        k_adj_post<T><<<ncolblk, POST_THREADS, 0, s>>>(e.kp, fields(), AP_OUTER | AP_RAYLEIGH | AP_VBC | AP_SPONGE);
+        e.launches++;
+        for (int st = 2; st >= 0; st--) {
+            const double step = steps[st];
+            if (st < 2) swap_inner();
+            k_adj_post<T><<<ncolblk, POST_THREADS, 0, s>>>(e.kp, fields(), AP_VBC | AP_SPONGE);
+            k_adj_project<T><<<cdiv(N, 256), 256, 0, s>>>(e.kp, fields(), (T)step, (first && st == 2) ? 1 : 0);
+            e.launches += 2;
+            adj_pressure(step);
+            KFields<T> R = e.fields();
+            for (int f = 0; f < 4; f++) R.cur[f] = const_cast<T *>(rec) + (size_t)(4 * st + f) * N;
+            const T sdtg = (T)(step * e.cfg.dt * 9.8 * 0.5);
+            k_adj_advect<T><<<gadv, AJ_THREADS, 0, s>>>(e.kp, R, fields(), (T)step, sdtg);
+            k_adj_fold<T><<<cdiv(tot, 256), 256, 0, s>>>(e.kp, fields());
+            e.launches += 2;
+        }
+    }
+
+    int reserve(size_t tape_need, size_t ckpt_need)
+    {
+        if (tape_need > tape_steps) {
+            if (tape) cudaFree(tape);
+            tape = nullptr;
+            tape_steps = 0;
+            if (cudaMalloc(&tape, tape_need * 12 * (size_t)N * sizeof(T)) != cudaSuccess) return GA_ERR_NOMEM;
+            tape_steps = tape_need;
+        }
+        if (ckpt_need > ckpt_slots) {
+            if (ckpt) cudaFree(ckpt);
+            ckpt = nullptr;
+            ckpt_slots = 0;
+            if (cudaMalloc(&ckpt, ckpt_need * 12 * (size_t)N * sizeof(T)) != cudaSuccess) return GA_ERR_NOMEM;
+            ckpt_slots = ckpt_need;
+        }
+        return GA_OK;
+    }
+
+    // copy the state (current, P, M of u, v, w, theta) to or from a checkpoint
+    void checkpoint(size_t slot, bool save)
+    {
+        T *base = ckpt + slot * 12 * (size_t)N;
+        for (int f = 0; f < 4; f++) {
+            const int idx[3] = {e.ci[f], e.pi_[f], e.mi[f]};
+            for (int s = 0; s < 3; s++) {
+                T *c = base + (size_t)(3 * f + s) * N;
+                if (save) cudaMemcpyAsync(c, e.buf[f][idx[s]], N * sizeof(T), cudaMemcpyDeviceToDevice, e.stream);
+                else cudaMemcpyAsync(e.buf[f][idx[s]], c, N * sizeof(T), cudaMemcpyDeviceToDevice, e.stream);
+            }
+        }
+    }
+
+    // nsteps forward from the current state, then the adjoint back to it.
+    // States are checkpointed every K steps and each segment is recomputed
+    // (recording its stage-start fields) before its adjoint runs; the last
+    // segment is recorded during the first sweep.
+    int adjoint(int nsteps, int K)
+    {
+        if (nsteps <= 0) return GA_OK;
+        if (K <= 0 || K > nsteps) K = nsteps;
+        const int nseg = (nsteps + K - 1) / K;
+        int rc = reserve((size_t)K, (size_t)nseg + 1);
+        if (rc) return rc;
+        const size_t per = 12 * (size_t)N;
+        for (int n = 0; n < nsteps; n++) {
+            const int seg = n / K;
+            if (n % K == 0) checkpoint(seg, true);
+            e.rk3_step(seg == nseg - 1 ? tape + (size_t)(n - seg * K) * per : nullptr);
+        }
+        checkpoint(nseg, true);
+        const long long bc = e.bigcounter;
+        const double mt = e.mtime;
+        for (int seg = nseg - 1; seg >= 0; seg--) {
+            const int n0 = seg * K, n1 = std::min(nsteps, n0 + K);
+            if (seg != nseg - 1) {
+                checkpoint(seg, false);
+                for (int n = n0; n < n1; n++) e.rk3_step(tape + (size_t)(n - n0) * per);
+            }
+            for (int n = n1 - 1; n >= n0; n--) adj_step(tape + (size_t)(n - n0) * per, n == nsteps - 1);
+        }
+        checkpoint(nseg, false);
+        e.bigcounter = bc;
+        e.mtime = mt;
+        cudaMemsetAsync(lpi_f, 0, N * sizeof(T), e.stream);  // the step does not read pi
+        return GA_OK;
+    }
+};
+
+template <typename T>
+Lin<T> *Engine<T>::linear()
+{
+    if (!lin) lin.reset(new Lin<T>(*this));
+    return static_cast<Lin<T> *>(lin.get());
+}
+
+template <typename T>
+int Engine<T>::lin_supported() const
+{
+    if (kp.moist || kp.periodic) {
+        set_error("tangent-linear / adjoint: dry, non-periodic contexts only");
+        return GA_ERR_UNSUPPORTED;
+    }
+    return GA_OK;
+}
+
+template <typename T>
+int Engine<T>::lin_set_field(int field, int slot, const double *host, size_t n)
+{
+    if (int rc = lin_supported()) return rc;
+    if (!host || n != (size_t)N) return GA_ERR_ARG;
+    cudaSetDevice(device);
+    T *d = linear()->slot_ptr(field, slot);
+    if (!d || status) return status ? status : GA_ERR_ARG;
+    if (sizeof(T) == sizeof(double)) {
+        cudaMemcpyAsync(d, host, n * sizeof(double), cudaMemcpyHostToDevice, stream);
+    } else {
+        if (ensure_staging() != GA_OK) return GA_ERR_NOMEM;
+        cudaMemcpyAsync(staging, host, n * sizeof(double), cudaMemcpyHostToDevice, stream);
+        k_convert_in<T><<<cdiv(n, 256), 256, 0, stream>>>(d, staging, (long)n);
+        launches++;
+    }
+    return sync_status();
+}
+
+template <typename T>
+int Engine<T>::lin_get_field(int field, int slot, double *host, size_t n)
+{
+    if (int rc = lin_supported()) return rc;
+    if (!host || n != (size_t)N) return GA_ERR_ARG;
+    cudaSetDevice(device);
+    T *d = linear()->slot_ptr(field, slot);
+    if (!d || status) return status ? status : GA_ERR_ARG;
+    if (sizeof(T) == sizeof(double)) {
+        cudaMemcpyAsync(host, d, n * sizeof(double), cudaMemcpyDeviceToHost, stream);
+    } else {
+        if (ensure_staging() != GA_OK) return GA_ERR_NOMEM;
+        k_convert_out<T><<<cdiv(n, 256), 256, 0, stream>>>(staging, d, (long)n);
+        launches++;
+        cudaMemcpyAsync(host, staging, n * sizeof(double), cudaMemcpyDeviceToHost, stream);
+    }
+    return sync_status();
+}
+
+template <typename T>
+int Engine<T>::tlm_step(int nsteps)
+{
+    if (int rc = lin_supported()) return rc;
+    cudaSetDevice(device);
+    refresh_base();
+    Lin<T> *L = linear();
+    if (status) return status;
+    for (int n = 0; n < nsteps; n++) {
+        L->tlm_step();
+        if (int rc = launch_status()) return rc;
+    }
+    return sync_status();
+}
+
+template <typename T>
+int Engine<T>::adjoint(int nsteps, int checkpoint_every)
+{
+    if (int rc = lin_supported()) return rc;
+    if (nsteps < 0) return GA_ERR_ARG;
+    cudaSetDevice(device);
+    refresh_base();
+    Lin<T> *L = linear();
+    if (status) return status;
+    int rc = L->adjoint(nsteps, checkpoint_every);
+    if (rc) {
+        set_error("adjoint: out of device memory for the checkpoints / trajectory");
+        return rc;
+    }
+    if ((rc = launch_status())) return rc;
+    return sync_status();
+}
+
+}  // namespace ga

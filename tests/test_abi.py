@@ -48,6 +48,10 @@ def test_null_arguments_are_rejected(lib):
     assert lib.ga_step(None, 1) == abi.GA_ERR_ARG
     assert lib.ga_op(None, 0, 1.0) == abi.GA_ERR_ARG
     assert lib.ga_launch_count(None) == -1
+    assert lib.ga_tlm_step(None, 1) == abi.GA_ERR_ARG
+    assert lib.ga_adjoint(None, 1, 1) == abi.GA_ERR_ARG
+    assert lib.ga_lin_set_field(None, 0, 0, None, 0) == abi.GA_ERR_ARG
+    assert lib.ga_lin_get_field(None, 0, 0, None, 0) == abi.GA_ERR_ARG
     store = abi.GaColumnStore()
     tb = np.zeros(4)
     rc = lib.ga_columns_build(4, 100.0, 100.0, tb.ctypes.data_as(C.POINTER(C.c_double)),
