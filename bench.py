@@ -284,6 +284,69 @@ def ensemble_bench(torch, device, steps, warmup, n_small=64, n_large=32):
     return out
 
 
+def adjoint_bench(torch, device, steps, every):
+    """Forward vs forward+adjoint of the dry monsoon-vortex workload
+    (192x128x32, dx=dy=40 km, dz=600 m, dt=120 s): `steps` steps from the
+    initial state, then the adjoint of the whole run back to it with the state
+    checkpointed every `every` steps and each segment recomputed.  One job per
+    timing, bracketed by CUDA events on the library stream, L2 flushed before
+    each job (the state of this grid fits in L2, so the steps of a job run
+    partly from L2, the same for both)."""
+    from model_gb300 import abi, anelastic, configs
+    wl = configs.monsoon_vortex(nsteps=steps)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{device}")
+    out = {"workload": f"dry monsoon vortex {wl.nx}x{wl.ny}x{wl.nz}, dx=dy=40 km, dz=600 m, dt=120 s",
+           "steps": steps, "checkpoint_every": every,
+           "memory": "checkpoints: steps/every+1 states of 12 fields; trajectory: every x 12 fields"}
+    for name, prec in (("fp32", abi.GA_PREC_F32), ("fp64", abi.GA_PREC_F64)):
+        m = anelastic.Model(wl, prec, device=device)
+        ext = torch.cuda.ExternalStream(m.stream_handle())
+        zero = np.zeros(wl.points)
+
+        def reset():
+            # initial state (current = M = perturbation, P = 0); the basic
+            # state is left alone so no graph is rebuilt inside a timing
+            for f in m.LIN_FIELDS:
+                init = wl.fields[abi.PROG_NAMES[f]]
+                m.set(f, abi.GA_SLOT_CUR, init)
+                m.set(f, abi.GA_SLOT_P, zero)
+                m.set(f, abi.GA_SLOT_M, init)
+            for f in m.LIN_FIELDS:
+                for s in m.LIN_SLOTS:
+                    m.lin_set(f, s, zero)
+            m.lin_set(abi.GA_PI, 0, zero)
+            m.lin_set(abi.GA_U, abi.GA_SLOT_CUR, np.full(wl.points, 1.0 / wl.points))
+
+        def timed(fn):
+            reset()
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(ext)
+            fn()
+            b.record(ext)
+            torch.cuda.synchronize()
+            return a.elapsed_time(b)
+
+        reset()
+        m.adjoint(steps, every)  # warm-up; sizes the checkpoint and trajectory buffers
+        m.step(2)  # captures the two-step graphs of both rotation parities
+        m.step(1)
+        m.step(2)
+        t_fwd = timed(lambda: m.step_async(steps))
+        l1 = m.launch_count()
+        t_adj = timed(lambda: m.adjoint(steps, every))
+        l2 = m.launch_count()
+        pts = wl.points * steps
+        out[name] = {"fwd_ms": round(t_fwd, 2), "fwd_adj_ms": round(t_adj, 2),
+                     "fwd_adj_over_fwd": round(t_adj / t_fwd, 3),
+                     "value_fwd": round(pts / (t_fwd * 1e-3), 1), "value_fwd_adj": round(pts / (t_adj * 1e-3), 1),
+                     "unit": UNIT, "launches_fwd_adj": int(l2 - l1)}
+        m.close()
+    return out
+
+
 def cpu_baseline(wl, steps):
     """The reference's CPU step (oracle restatement, 1 core) on a bounded
     sample of the same workload."""
@@ -402,6 +465,8 @@ def run_ours(args):
         line["e2e"] = e2e_jobs(anelastic.Model, wl, prec, torch, args.e2e_jobs, args.e2e_steps, device)
     if args.ensemble_steps > 0:
         line["ensemble"] = ensemble_bench(torch, device, args.ensemble_steps, 2)
+    if args.adjoint_steps > 0:
+        line["adjoint"] = adjoint_bench(torch, device, args.adjoint_steps, args.adjoint_every)
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(wl, args.cpu_steps)
     print(json.dumps(line), flush=True)
@@ -448,6 +513,8 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=600)
     ap.add_argument("--cpu-steps", type=int, default=5)
     ap.add_argument("--ensemble-steps", type=int, default=10)
+    ap.add_argument("--adjoint-steps", type=int, default=500)
+    ap.add_argument("--adjoint-every", type=int, default=50)
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()

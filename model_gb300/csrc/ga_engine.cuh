@@ -403,6 +403,7 @@ class Engine : public EngineBase {
                 cudaGraphExecDestroy(g);
                 g = nullptr;
             }
+        if (lin) lin->drop_graphs();
     }
 
     // per-level basic-state tables (k_base_tables) when the basic state is

@@ -18,6 +18,7 @@ static const char *const kProfNames[PC_COUNT] = {"advect", "edges", "div_fft_y",
 // tangent-linear / adjoint state of an engine (ga_lin.cuh)
 struct LinBase {
     virtual ~LinBase() {}
+    virtual void drop_graphs() {}
 };
 
 struct EngineBase {

@@ -1150,16 +1150,20 @@ __device__ __forceinline__ void thomas_column_fast(float2 *x, float *Fw, int nz,
 // for the near-singular low wavenumbers of FP32 contexts.  For the mean mode
 // (gauge) the last row is replaced by x = 0, which is what the reference's
 // pinning after forward elimination (pressure.cpp:858-859) amounts to.
+constexpr int PCR_ROWS = PPM_MAXZ;      // rows of one reduction (levels 1..NZ-2, NZ <= PPM_MAXZ)
+constexpr int PCR_WK = 10 * PCR_ROWS;    // workspace doubles: 2 buffers x (a, b, c, dr, di)
+
 template <typename T2>
 __device__ void pcr_column_f64(T2 *x, int nl, double hcol, double dx2, double size2d, const double *rhou,
                                const double *ac, const double *cc, const double *vc, bool gauge, double *wk)
 {
-    // wk: 2 buffers x 5 arrays x 64 rows (a, b, c, dr, di).  Blocks may be
-    // 2-D, so the lane comes from the linear thread index.
+    // wk: PCR_WK doubles, 2 buffers x 5 arrays x PCR_ROWS rows (a, b, c, dr,
+    // di).  Blocks may be 2-D, so the lane comes from the linear thread index.
     const int lane = (threadIdx.y * blockDim.x + threadIdx.x) & 31;
-    double *A0 = wk, *B0 = wk + 64, *C0 = wk + 128, *R0 = wk + 192, *I0 = wk + 256;
-    double *A1 = wk + 320, *B1 = wk + 384, *C1 = wk + 448, *R1 = wk + 512, *I1 = wk + 576;
-    for (int r = lane; r < 64; r += 32) {
+    constexpr int R = PCR_ROWS;
+    double *A0 = wk, *B0 = wk + R, *C0 = wk + 2 * R, *R0 = wk + 3 * R, *I0 = wk + 4 * R;
+    double *A1 = wk + 5 * R, *B1 = wk + 6 * R, *C1 = wk + 7 * R, *R1 = wk + 8 * R, *I1 = wk + 9 * R;
+    for (int r = lane; r < R; r += 32) {
         if (r < nl) {
             const int k = r + 1;
             double a = ac[k], c = cc[k];
@@ -1218,7 +1222,7 @@ __global__ void k_thomas(KParams<T> p, typename V2<T>::t *spec, int TC)
 {
     typedef typename V2<T>::t T2;
     extern __shared__ unsigned char smem_raw[];
-    __shared__ double pcr_wk[2][640];
+    __shared__ double pcr_wk[PCR_WK];
     const int cs = p.nz | 1;  // odd column stride: no bank conflicts between columns
     T2 *xs = (T2 *)smem_raw;
     T *fs = (T *)(xs + (long)TC * cs);
@@ -1244,14 +1248,12 @@ __global__ void k_thomas(KParams<T> p, typename V2<T>::t *spec, int TC)
     }
     if (sizeof(T) != 8 && p.low_modes > 0) {
         const int warp = threadIdx.x >> 5;
-        if (warp < 2 && (int)blockDim.x >= 64) {
-            int n = 0;
+        if (warp == 0) {  // the low modes of this block, one after the other
             for (int c = 0; c < nc; c++) {
                 const long col = c0 + c;
                 if (!low_mode(p, col)) continue;
-                if ((n++ & 1) != warp) continue;
                 pcr_column_f64(xs + (long)c * cs, p.nz - 2, p.hcoef[col], p.dx2, size2d, p.rhou_d, p.acoef_d,
-                               p.ccoef_d, p.vcoef_d, col == 0, pcr_wk[warp]);
+                               p.ccoef_d, p.vcoef_d, col == 0, pcr_wk);
             }
         }
     }
@@ -1267,7 +1269,7 @@ __device__ void spectral_x_body(const KParams<T> &p, typename V2<T>::t *spec, co
     extern __shared__ unsigned char smem_raw[];
     __shared__ T c_r[PPM_MAXZ], c_a[PPM_MAXZ], c_c[PPM_MAXZ], c_v[PPM_MAXZ];
     __shared__ double d_r[PPM_MAXZ], d_a[PPM_MAXZ], d_c[PPM_MAXZ], d_v[PPM_MAXZ];
-    __shared__ double pcr_wk[2][640];
+    __shared__ double pcr_wk[PCR_WK];
     T2 *a = (T2 *)smem_raw;
     T2 *b = a + (long)p.ni * ps;
     const int q = bx;
@@ -1302,19 +1304,19 @@ __device__ void spectral_x_body(const KParams<T> &p, typename V2<T>::t *spec, co
             thomas_column_fast((float2 *)(r + (long)pp * ps - 1), Fw, p.nz, hb, inv_s, (const float *)c_r,
                                (const float *)c_a, (const float *)c_c, (const float *)c_v, col == 0);
         }
-        if (q_low) {  // low (p,q) wavenumbers: FP64 by warp PCR on warps 0 and 1
+        if (q_low) {  // low (p,q) wavenumbers: FP64 by warp PCR on warp 0
             const int warp = tid >> 5;
-            if (warp < 2) {
+            if (warp == 0) {
                 int islands[16], nis = 0;
                 for (int pp = 0; pp < p.low_modes && nis < 15; pp++) {
                     islands[nis++] = pp;
                     if (pp > 0) islands[nis++] = p.ni - pp;
                 }
-                for (int w = warp; w < nis; w += 2) {
+                for (int w = 0; w < nis; w++) {
                     const int pp = islands[w];
                     const long col = (long)pp * p.nj + q;
                     pcr_column_f64(r + (long)pp * ps - 1, nl, p.hcoef[col], p.dx2, size2d, d_r, d_a, d_c, d_v,
-                                   col == 0, pcr_wk[warp]);
+                                   col == 0, pcr_wk);
                 }
             }
         }

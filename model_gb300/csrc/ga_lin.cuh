@@ -20,10 +20,14 @@ struct Lin : LinBase {
     int lci[4], lpi[4], lmi[4];
     T *lpi_f = nullptr;  // pi (perturbation or adjoint)
     T *dbar = nullptr;   // adjoint of the divergence, real [i][j][k]
+    T *coef = nullptr;   // linearised face coefficients of one stage (LIN_NCOEF fields)
     T *tape = nullptr;   // stage-start u, v, w, theta of every step of a segment
     size_t tape_steps = 0;
     T *ckpt = nullptr;   // full states (current, P, M of u, v, w, theta)
     size_t ckpt_slots = 0;
+    // two recorded steps into trajectory slots (2m, 2m+1), per rotation parity
+    std::vector<cudaGraphExec_t> rec_graph[2];
+    std::vector<long long> rec_graph_launches[2];
 
     explicit Lin(Engine<T> &eng) : e(eng), N(eng.N)
     {
@@ -33,15 +37,82 @@ struct Lin : LinBase {
         }
         lpi_f = e.template dalloc<T>(N);
         dbar = e.template dalloc<T>(N);
+        coef = e.template dalloc<T>((size_t)LIN_NCOEF * N);
         const int optin = 200 * 1024;
         cudaFuncSetAttribute(k_adj_fft_y_in<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
         cudaFuncSetAttribute(k_adj_ifft_y_out<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
         cudaFuncSetAttribute(k_thomas_adj<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+        cudaFuncSetAttribute(k_spectral_x_adj<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+        cudaFuncSetAttribute(k_adj_advect<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
     }
     ~Lin() override
     {
+        drop_graphs();
         if (tape) cudaFree(tape);
         if (ckpt) cudaFree(ckpt);
+    }
+
+    void drop_graphs() override
+    {
+        for (int par = 0; par < 2; par++) {
+            for (auto &g : rec_graph[par])
+                if (g) cudaGraphExecDestroy(g);
+            rec_graph[par].clear();
+            rec_graph_launches[par].clear();
+        }
+    }
+
+    // two steps recording into trajectory slots m2, m2+1: replayed from a
+    // CUDA graph captured on first use (slots and parity fix every pointer)
+    void record_pair(int m2)
+    {
+        const size_t per = 12 * (size_t)N;
+        const int par = e.ci[0] == 0 ? 0 : 1;
+        const size_t idx = (size_t)m2 / 2;
+        auto &gs = rec_graph[par];
+        auto &ls = rec_graph_launches[par];
+        if (gs.size() <= idx) {
+            gs.resize(idx + 1, nullptr);
+            ls.resize(idx + 1, 0);
+        }
+        if (!gs[idx] && e.use_graphs) {
+            const long long bc = e.bigcounter, l0 = e.launches;
+            const double mt = e.mtime;
+            cudaGraph_t g = nullptr;
+            bool ok = cudaStreamBeginCapture(e.stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+            if (ok) {
+                e.rk3_step(tape + (size_t)m2 * per);
+                e.rk3_step(tape + (size_t)(m2 + 1) * per);
+                ok = cudaStreamEndCapture(e.stream, &g) == cudaSuccess;
+            }
+            if (ok) ok = cudaGraphInstantiate(&gs[idx], g, 0) == cudaSuccess;
+            if (g) cudaGraphDestroy(g);
+            ls[idx] = e.launches - l0;
+            e.launches = l0;
+            e.bigcounter = bc;
+            e.mtime = mt;
+            if (!ok) {
+                cudaGetLastError();
+                gs[idx] = nullptr;
+            }
+        }
+        if (gs[idx] && cudaGraphLaunch(gs[idx], e.stream) == cudaSuccess) {
+            e.launches += ls[idx];
+            e.bigcounter += 2;
+            e.mtime += 2 * e.cfg.dt;
+        } else {
+            e.rk3_step(tape + (size_t)m2 * per);
+            e.rk3_step(tape + (size_t)(m2 + 1) * per);
+        }
+    }
+
+    // steps n0..n1-1 of a segment starting at n0, recording every step
+    void record_segment(int n0, int n1)
+    {
+        const size_t per = 12 * (size_t)N;
+        int n = n0;
+        for (; n + 1 < n1; n += 2) record_pair(n - n0);
+        if (n < n1) e.rk3_step(tape + (size_t)(n - n0) * per);
     }
 
     KFields<T> fields() const
@@ -141,41 +212,50 @@ struct Lin : LinBase {
         const dim3 by_y(e.KTy, std::max(1, 256 / e.KTy)), by_x(e.KTx, std::max(1, 256 / e.KTx));
         cudaStream_t s = e.stream;
         k_adj_fft_y_in<T><<<dim3(e.kp.ni, nkt_y), by_y, e.smem_y, s>>>(e.kp, lpi_f, e.spec, e.plan_j, e.tw_j, e.KTy);
-        k_fft_x<T><<<dim3(e.kp.nj, nkt_x), by_x, e.smem_x, s>>>(e.kp, e.spec, e.plan_i, e.tw_i, 0, e.KTx);
-        const long ncol = (long)e.kp.ni * e.kp.nj;
-        k_thomas_adj<T><<<cdiv(ncol, e.TC), e.TC, e.smem_th, s>>>(e.kp, e.spec, e.TC);
-        k_fft_x<T><<<dim3(e.kp.nj, nkt_x), by_x, e.smem_x, s>>>(e.kp, e.spec, e.plan_i, e.tw_i, 1, e.KTx);
+        if (e.psx > 0) {  // x transforms and the solves fused, as in the forward step
+            const int nl = e.NZ - 2, bx = std::min(nl, 64);
+            k_spectral_x_adj<T><<<e.kp.nj, dim3(bx, std::max(1, 256 / bx)), e.smem_sx, s>>>(e.kp, e.spec, e.plan_i,
+                                                                                          e.tw_i, e.psx);
+            e.launches += 1;
+        } else {
+            k_fft_x<T><<<dim3(e.kp.nj, nkt_x), by_x, e.smem_x, s>>>(e.kp, e.spec, e.plan_i, e.tw_i, 0, e.KTx);
+            const long ncol = (long)e.kp.ni * e.kp.nj;
+            k_thomas_adj<T><<<cdiv(ncol, e.TC), e.TC, e.smem_th, s>>>(e.kp, e.spec, e.TC);
+            k_fft_x<T><<<dim3(e.kp.nj, nkt_x), by_x, e.smem_x, s>>>(e.kp, e.spec, e.plan_i, e.tw_i, 1, e.KTx);
+            e.launches += 3;
+        }
         k_adj_ifft_y_out<T><<<dim3(e.kp.ni, nkt_y), by_y, e.smem_y, s>>>(e.kp, e.spec, dbar, e.plan_j, e.tw_j, e.KTy);
         k_adj_div<T><<<cdiv(N, 256), 256, 0, s>>>(e.kp, A, dbar, (T)(st * e.cfg.dt));
-        k_adj_mirror<T><<<e.NZ - 2, 256, 0, s>>>(e.kp, A.P[FU], A.P[FV], A.P[FW]);
-        e.launches += 7;
+        e.launches += 3;
     }
 
     // adjoint of one step about the trajectory rec (stage-start u, v, w,
-    // theta: rec + (4*stage + field)*N).  first: the adjoint of the final pi
-    // held in pi-bar enters here.
+    // theta: rec + (4*stage + field)*N).  first: the adjoint of the final
+    // state enters here (the final pi-bar, and a current slot that holds no
+    // stale P-bar).
     void adj_step(const T *rec, bool first)
     {
         static const double steps[3] = {1. / 3., 0.5, 1.0};
         cudaStream_t s = e.stream;
         const long ncolblk = cdiv((long)e.NX * e.NY, POST_COLS);
-        const long tot = (long)(e.NX - 6) * (e.NY - 6) * (e.NZ - 2);
         const dim3 gadv(cdiv(e.NX, AJ_TI), cdiv(e.NY, AJ_TJ), cdiv(e.NZ, AJ_TK));
+        const size_t smem_adv = (3 * (size_t)AJ_NFACE + AJ_NTB) * sizeof(T);
         swap_inner();  // advance_outer's swap
-        k_adj_post<T><<<ncolblk, POST_THREADS, 0, s>>>(e.kp, fields(), AP_OUTER | AP_RAYLEIGH | AP_VBC | AP_SPONGE);
-        e.launches++;
         for (int st = 2; st >= 0; st--) {
             const double step = steps[st];
             if (st < 2) swap_inner();
-            k_adj_post<T><<<ncolblk, POST_THREADS, 0, s>>>(e.kp, fields(), AP_VBC | AP_SPONGE);
+            // stage 2 shares its buffer with the step-final post: one pass
+            const int fl = st == 2 ? (AP_OUTER | AP_RAYLEIGH | AP_VBC | AP_SPONGE2) : (AP_VBC | AP_SPONGE);
+            k_adj_post<T><<<ncolblk, POST_THREADS, 0, s>>>(e.kp, fields(), fl);
             k_adj_project<T><<<cdiv(N, 256), 256, 0, s>>>(e.kp, fields(), (T)step, (first && st == 2) ? 1 : 0);
             e.launches += 2;
             adj_pressure(step);
             KFields<T> R = e.fields();
             for (int f = 0; f < 4; f++) R.cur[f] = const_cast<T *>(rec) + (size_t)(4 * st + f) * N;
             const T sdtg = (T)(step * e.cfg.dt * 9.8 * 0.5);
-            k_adj_advect<T><<<gadv, AJ_THREADS, 0, s>>>(e.kp, R, fields(), (T)step, sdtg);
-            k_adj_fold<T><<<cdiv(tot, 256), 256, 0, s>>>(e.kp, fields());
+            k_lin_coef<T><<<cdiv(N, 128), 128, 0, s>>>(e.kp, R, coef);
+            k_adj_advect<T><<<gadv, AJ_THREADS, smem_adv, s>>>(e.kp, coef, fields(), (T)step, sdtg,
+                                                               (first && st == 2) ? 0 : 1);
             e.launches += 2;
         }
     }
@@ -183,6 +263,7 @@ struct Lin : LinBase {
     int reserve(size_t tape_need, size_t ckpt_need)
     {
         if (tape_need > tape_steps) {
+            drop_graphs();
             if (tape) cudaFree(tape);
             tape = nullptr;
             tape_steps = 0;
@@ -225,10 +306,11 @@ struct Lin : LinBase {
         int rc = reserve((size_t)K, (size_t)nseg + 1);
         if (rc) return rc;
         const size_t per = 12 * (size_t)N;
-        for (int n = 0; n < nsteps; n++) {
-            const int seg = n / K;
-            if (n % K == 0) checkpoint(seg, true);
-            e.rk3_step(seg == nseg - 1 ? tape + (size_t)(n - seg * K) * per : nullptr);
+        for (int seg = 0; seg < nseg; seg++) {
+            const int n0 = seg * K, n1 = std::min(nsteps, n0 + K);
+            checkpoint(seg, true);
+            if (seg == nseg - 1) record_segment(n0, n1);
+            else if (int rc = e.step(n1 - n0)) return rc;
         }
         checkpoint(nseg, true);
         const long long bc = e.bigcounter;
@@ -237,10 +319,13 @@ struct Lin : LinBase {
             const int n0 = seg * K, n1 = std::min(nsteps, n0 + K);
             if (seg != nseg - 1) {
                 checkpoint(seg, false);
-                for (int n = n0; n < n1; n++) e.rk3_step(tape + (size_t)(n - n0) * per);
+                record_segment(n0, n1);
             }
             for (int n = n1 - 1; n >= n0; n--) adj_step(tape + (size_t)(n - n0) * per, n == nsteps - 1);
         }
+        const long tot = (long)(e.NX - 6) * (e.NY - 6) * (e.NZ - 2);
+        k_adj_zero_cells<T><<<cdiv(tot, 256), 256, 0, e.stream>>>(e.kp, fields());
+        e.launches++;
         checkpoint(nseg, false);
         e.bigcounter = bc;
         e.mtime = mt;

@@ -46,32 +46,35 @@ struct LinFace {
     T ga, gs;      // dF = ga*da + gs*dS
 };
 
-// Build the face of equation eq (0 u, 1 v, 2 theta) and direction dir at
+// Build the face of equation EQ (0 u, 1 v, 2 theta) and direction DIR at
 // (i,j,k) about the trajectory R (R.cur = fields at the start of the stage).
 // Returns false where the forward flux is identically zero (bottom faces).
-template <typename T>
-__device__ __forceinline__ bool lin_face(const KParams<T> &p, const KFields<T> &R, int eq, int dir, int i, int j,
-                                         int k, LinFace<T> &L)
+template <typename T, int EQ, int DIR>
+__device__ __forceinline__ bool lin_face_t(const KParams<T> &p, const KFields<T> &R, int i, int j, int k,
+                                           LinFace<T> &L)
 {
     const int ny = p.ny, nz = p.nz;
-    if (dir == 2 && k == 0) return false;
-    const int fx = eq == 0 ? FU : eq == 1 ? FV : FTH;
-    const T *X = R.cur[fx], *XB = R.bar[eq == 2 ? 3 : eq];
-    const T *A = R.cur[dir], *AB = R.bar[dir];
-    if (eq == 2) {
-        L.ia0 = dir == 0 ? gix(ny, nz, i + 1, j, k) : dir == 1 ? gix(ny, nz, i, j + 1, k) : gix(ny, nz, i, j, k + 1);
+    if (DIR == 2 && k == 0) return false;
+    constexpr int FX = EQ == 0 ? FU : EQ == 1 ? FV : FTH;
+    const T *X = R.cur[FX], *XB = R.bar[EQ == 2 ? 3 : EQ];
+    const T *A = R.cur[DIR], *AB = R.bar[DIR];
+    const int c = gix(ny, nz, i, j, k);
+    constexpr int one = 1;
+    const int sx = ny * nz, sy = nz;
+    if (EQ == 2) {
+        L.ia0 = DIR == 0 ? c + sx : DIR == 1 ? c + sy : c + one;
         L.ia1 = -1;
-    } else if (eq == 0) {
-        if (dir == 0) { L.ia0 = gix(ny, nz, i + 1, j, k); L.ia1 = gix(ny, nz, i, j, k); }
-        else if (dir == 1) { L.ia0 = gix(ny, nz, i, j + 1, k); L.ia1 = gix(ny, nz, i - 1, j + 1, k); }
-        else { L.ia0 = gix(ny, nz, i, j, k + 1); L.ia1 = gix(ny, nz, i - 1, j, k + 1); }
+    } else if (EQ == 0) {
+        if (DIR == 0) { L.ia0 = c + sx; L.ia1 = c; }
+        else if (DIR == 1) { L.ia0 = c + sy; L.ia1 = c - sx + sy; }
+        else { L.ia0 = c + 1; L.ia1 = c - sx + 1; }
     } else {
-        if (dir == 0) { L.ia0 = gix(ny, nz, i + 1, j, k); L.ia1 = gix(ny, nz, i + 1, j - 1, k); }
-        else if (dir == 1) { L.ia0 = gix(ny, nz, i, j + 1, k); L.ia1 = gix(ny, nz, i, j, k); }
-        else { L.ia0 = gix(ny, nz, i, j, k + 1); L.ia1 = gix(ny, nz, i, j - 1, k + 1); }
+        if (DIR == 0) { L.ia0 = c + sx; L.ia1 = c + sx - sy; }
+        else if (DIR == 1) { L.ia0 = c + sy; L.ia1 = c; }
+        else { L.ia0 = c + 1; L.ia1 = c - sy + 1; }
     }
     T a, ab;
-    if (L.ia1 < 0) {
+    if (EQ == 2) {
         a = A[L.ia0];
         ab = AB[L.ia0];
     } else {
@@ -80,27 +83,43 @@ __device__ __forceinline__ bool lin_face(const KParams<T> &p, const KFields<T> &
     }
     const T sgs = sgn(ab + a), sgb = sgn(a);
     T Sv, Bv;
-    if (dir < 2) {
-        const int st = dir == 0 ? ny * nz : nz;
-        const int c = gix(ny, nz, i, j, k) - 2 * st;
-        L.x0 = c; L.xs = st; L.nx = 6;
-        Sv = face5(X[c], X[c + st], X[c + 2 * st], X[c + 3 * st], X[c + 4 * st], X[c + 5 * st], sgs);
-        Bv = face5(XB[c], XB[c + st], XB[c + 2 * st], XB[c + 3 * st], XB[c + 4 * st], XB[c + 5 * st], sgb);
+    if (DIR < 2) {
+        const int st = DIR == 0 ? sx : sy;
+        const int c0 = c - 2 * st;
+        L.x0 = c0; L.xs = st; L.nx = 6;
+        Sv = face5(X[c0], X[c0 + st], X[c0 + 2 * st], X[c0 + 3 * st], X[c0 + 4 * st], X[c0 + 5 * st], sgs);
+        Bv = face5(XB[c0], XB[c0 + st], XB[c0 + 2 * st], XB[c0 + 3 * st], XB[c0 + 4 * st], XB[c0 + 5 * st], sgb);
     } else if (k == 1 || k == nz - 2) {
-        const int c = gix(ny, nz, i, j, k);
         L.x0 = c; L.xs = 1; L.nx = 2;
         Sv = T(0.5) * (X[c + 1] + X[c]);
         Bv = T(0.5) * (XB[c + 1] + XB[c]);
     } else {
-        const int c = gix(ny, nz, i, j, k) - 1;
-        L.x0 = c; L.xs = 1; L.nx = 4;
-        Sv = face3(X[c], X[c + 1], X[c + 2], X[c + 3], sgs);
-        Bv = face3(XB[c], XB[c + 1], XB[c + 2], XB[c + 3], sgb);
+        const int c0 = c - 1;
+        L.x0 = c0; L.xs = 1; L.nx = 4;
+        Sv = face3(X[c0], X[c0 + 1], X[c0 + 2], X[c0 + 3], sgs);
+        Bv = face3(XB[c0], XB[c0 + 1], XB[c0 + 2], XB[c0 + 3], sgb);
     }
     L.sg = sgs;
     L.ga = Bv + Sv;
     L.gs = ab + a;
     return true;
+}
+
+template <typename T>
+__device__ __forceinline__ bool lin_face(const KParams<T> &p, const KFields<T> &R, int eq, int dir, int i, int j,
+                                         int k, LinFace<T> &L)
+{
+    switch (eq * 3 + dir) {
+    case 0: return lin_face_t<T, 0, 0>(p, R, i, j, k, L);
+    case 1: return lin_face_t<T, 0, 1>(p, R, i, j, k, L);
+    case 2: return lin_face_t<T, 0, 2>(p, R, i, j, k, L);
+    case 3: return lin_face_t<T, 1, 0>(p, R, i, j, k, L);
+    case 4: return lin_face_t<T, 1, 1>(p, R, i, j, k, L);
+    case 5: return lin_face_t<T, 1, 2>(p, R, i, j, k, L);
+    case 6: return lin_face_t<T, 2, 0>(p, R, i, j, k, L);
+    case 7: return lin_face_t<T, 2, 1>(p, R, i, j, k, L);
+    default: return lin_face_t<T, 2, 2>(p, R, i, j, k, L);
+    }
 }
 
 // tangent of one face flux
@@ -175,165 +194,284 @@ __global__ void k_tl_advect(KParams<T> p, KFields<T> R, KFields<T> D, T step, T 
 
 // ---------------------------------------------------------------------------
 // adjoint of the advection step, gather form.  A block owns a tile of
-// AJ_TI x AJ_TJ x AJ_TK cells; for each of the nine face families (three
-// equations x three directions) it evaluates the adjoint of every face whose
-// stencil reaches the tile into shared memory (S' = Fbar*(ab+a), sign*S',
-// a' = Fbar*(B+S)), then every cell sums what reaches it.
+// AJ_TI x AJ_TJ x AJ_TK cells (AJ_CPT per thread); for each of the nine face
+// families (three equations x three directions, each specialised at compile
+// time) it evaluates the adjoint of every face whose stencil reaches the tile
+// into shared memory (S' = Fbar*(ab+a), sign*S', a' = Fbar*(B+S)), then every
+// cell sums what reaches it.  The same kernel finishes the stage's
+// bookkeeping on the cells it owns:
+//   - M-bar += P-bar where the forward advection overwrote P (the P-bar there
+//     is zeroed when the buffer next receives adjoint contributions: with
+//     zero_cur the current-slot values of the advected cells are replaced,
+//     not added to, since they are that stale P-bar);
+//   - the lateral ring of P-bar u, v, w is zeroed (mirror_boundaries wrote
+//     it; k_adj_div has already moved its values to the mirrored points).
 // ---------------------------------------------------------------------------
-constexpr int AJ_TI = 8, AJ_TJ = 8, AJ_TK = 4, AJ_THREADS = AJ_TI * AJ_TJ * AJ_TK;
+constexpr int AJ_TI = 16, AJ_TJ = 16, AJ_TK = 4, AJ_THREADS = 256;
+constexpr int AJ_CPT = AJ_TI * AJ_TJ * AJ_TK / AJ_THREADS;
 constexpr int AJ_NFACE = (AJ_TI + 1) * (AJ_TJ + 1) * (AJ_TK + 3);  // largest face box (z faces)
+// box of tendency adjoints one equation's faces read: the tile + 3 points in
+// x and y, 2 below and 2 above
+constexpr int AJ_BI = AJ_TI + 6, AJ_BJ = AJ_TJ + 6, AJ_BK = AJ_TK + 4, AJ_NTB = AJ_BI * AJ_BJ * AJ_BK;
 
-// adjoint of the tendency of equation eq at a cell (zero outside the cells
-// the forward step writes)
-template <typename T>
-__device__ __forceinline__ T adj_tbar(const KParams<T> &p, const KFields<T> &A, int eq, int i, int j, int k, T step)
+// The two coefficients of every linearised face, once per stage: for each
+// cell c and face family fam = 3*EQ + DIR, coef[(2*fam)*N + c] = B + S and
+// coef[(2*fam + 1)*N + c] = ab + a of the face at c (its sign is the frozen
+// upwind sign), zero where the face is not next to an advected cell.
+constexpr int LIN_NCOEF = 18;
+
+template <typename T, int EQ, int DIR>
+__device__ __forceinline__ void lin_coef_face(const KParams<T> &p, const KFields<T> &R, T *coef, int i, int j, int k,
+                                              int c)
 {
-    if (!adv_cell(p, i, j, k, 1)) return T(0);
-    return step * A.P[eq == 0 ? FU : eq == 1 ? FV : FTH][gix(p.ny, p.nz, i, j, k)];
+    bool need;
+    if (DIR == 0) need = adv_cell(p, i, j, k, 1) || adv_cell(p, i + 1, j, k, 1);
+    else if (DIR == 1) need = adv_cell(p, i, j, k, 1) || adv_cell(p, i, j + 1, k, 1);
+    else need = adv_cell(p, i, j, k, 1) || adv_cell(p, i, j, k + 1, 1);
+    T ga = T(0), gs = T(0);
+    LinFace<T> L;
+    if (need && lin_face_t<T, EQ, DIR>(p, R, i, j, k, L)) {
+        ga = L.ga;
+        gs = L.gs;
+    }
+    constexpr int fam = 3 * EQ + DIR;
+    coef[(size_t)(2 * fam) * p.n + c] = ga;
+    coef[(size_t)(2 * fam + 1) * p.n + c] = gs;
 }
 
-// adjoint of the face flux (eq, dir) at (i,j,k): the transposed difference
-// operator of the tendency
 template <typename T>
-__device__ __forceinline__ T adj_fbar(const KParams<T> &p, const KFields<T> &A, int eq, int dir, int i, int j, int k,
-                                      T step)
+__global__ void k_lin_coef(KParams<T> p, KFields<T> R, T *coef)
 {
-    if (dir == 0) return p.dtx * (adj_tbar(p, A, eq, i + 1, j, k, step) - adj_tbar(p, A, eq, i, j, k, step));
-    if (dir == 1) return p.dty * (adj_tbar(p, A, eq, i, j + 1, k, step) - adj_tbar(p, A, eq, i, j, k, step));
-    if (k < 1) return T(0);
-    T fb = T(0);
-    const T t0 = adj_tbar(p, A, eq, i, j, k, step);
-    if (t0 != T(0)) fb -= (p.dtz * p.mu[k]) * p.rhow[k + 1] * p.one_d_rhou[k] * t0;
-    const T t1 = adj_tbar(p, A, eq, i, j, k + 1, step);
-    if (t1 != T(0)) fb += (p.dtz * p.mu[k + 1]) * p.rhow[k + 1] * p.one_d_rhou[k + 1] * t1;
-    return fb;
+    const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= p.n) return;
+    const int nz = p.nz, ny = p.ny;
+    const int k = (int)(t % nz), j = (int)((t / nz) % ny), i = (int)(t / ((long)nz * ny));
+    const int c = (int)t;
+    lin_coef_face<T, 0, 0>(p, R, coef, i, j, k, c);
+    lin_coef_face<T, 0, 1>(p, R, coef, i, j, k, c);
+    lin_coef_face<T, 0, 2>(p, R, coef, i, j, k, c);
+    lin_coef_face<T, 1, 0>(p, R, coef, i, j, k, c);
+    lin_coef_face<T, 1, 1>(p, R, coef, i, j, k, c);
+    lin_coef_face<T, 1, 2>(p, R, coef, i, j, k, c);
+    lin_coef_face<T, 2, 0>(p, R, coef, i, j, k, c);
+    lin_coef_face<T, 2, 1>(p, R, coef, i, j, k, c);
+    lin_coef_face<T, 2, 2>(p, R, coef, i, j, k, c);
 }
 
-template <typename T>
-__global__ void __launch_bounds__(AJ_THREADS) k_adj_advect(KParams<T> p, KFields<T> R, KFields<T> A, T step, T sdtg)
+// tendency adjoints of equation EQ (zero off the advected cells) over the box
+template <typename T, int EQ>
+__device__ __forceinline__ void adj_stage_tbar(const KParams<T> &p, const KFields<T> &A, T step, int i0, int j0,
+                                               int k0, T *tb)
 {
-    __shared__ T fs1[AJ_NFACE], fs2[AJ_NFACE], fab[AJ_NFACE];
-    const int ny = p.ny, nz = p.nz;
-    const int i0 = blockIdx.x * AJ_TI, j0 = blockIdx.y * AJ_TJ, k0 = blockIdx.z * AJ_TK;
+    constexpr int XF = EQ == 0 ? FU : EQ == 1 ? FV : FTH;
+    const T *P = A.P[XF];
+    for (int e = threadIdx.x; e < AJ_NTB; e += AJ_THREADS) {
+        const int i = i0 - 3 + e / (AJ_BK * AJ_BJ), j = j0 - 3 + (e / AJ_BK) % AJ_BJ, k = k0 - 2 + e % AJ_BK;
+        tb[e] = adv_cell(p, i, j, k, 1) ? step * P[gix(p.ny, p.nz, i, j, k)] : T(0);
+    }
+}
+
+template <typename T, int EQ, int DIR>
+__device__ __forceinline__ void adj_family(const KParams<T> &p, const T *__restrict__ coef, const T *tb, int i0,
+                                           int j0, int k0, T *fs1, T *fs2, T *fab, T (&acc)[AJ_CPT][4])
+{
+    constexpr int XF = EQ == 0 ? FU : EQ == 1 ? FV : FTH;
+    constexpr int fam = 3 * EQ + DIR;
+    constexpr int bdi = DIR == 0 ? 3 : 0, bdj = DIR == 1 ? 3 : 0, bdk = DIR == 2 ? 2 : 0;
+    constexpr int bni = DIR == 0 ? AJ_TI + 5 : AJ_TI + 1;
+    constexpr int bnj = DIR == 1 ? AJ_TJ + 5 : AJ_TJ + 1;
+    constexpr int bnk = DIR == 2 ? AJ_TK + 3 : AJ_TK;
+    constexpr int nf = bni * bnj * bnk;
+    // offset of a face's own cell in the tendency box, and of its +1 neighbour
+    constexpr int tstep = DIR == 0 ? AJ_BJ * AJ_BK : DIR == 1 ? AJ_BK : 1;
+    const int bi0 = i0 - bdi, bj0 = j0 - bdj, bk0 = k0 - bdk;
     const int t = threadIdx.x;
-    const int lk = t % AJ_TK, lj = (t / AJ_TK) % AJ_TJ, li = t / (AJ_TK * AJ_TJ);
-    const int pi = i0 + li, pj = j0 + lj, pk = k0 + lk;
-    const bool own = pi < p.nx && pj < ny && pk < nz;
-    // face-stencil weights: w(sign) = C + sign * U
+    const T *ga_f = coef + (size_t)(2 * fam) * p.n, *gs_f = coef + (size_t)(2 * fam + 1) * p.n;
+#pragma unroll 2
+    for (int f = t; f < nf; f += AJ_THREADS) {
+        const int li = f / (bnk * bnj), lj = (f / bnk) % bnj, lk = f % bnk;
+        const int fi = bi0 + li, fj = bj0 + lj, fk = bk0 + lk;
+        const bool in = fi >= 0 && fi < p.nx && fj >= 0 && fj < p.ny && fk >= 0 && fk < p.nz;
+        T ga = T(0), gs = T(0);
+        if (in) {
+            const int c = gix(p.ny, p.nz, fi, fj, fk);
+            ga = ga_f[c];
+            gs = gs_f[c];
+        }
+        const int tb0 = ((li + 3 - bdi) * AJ_BJ + (lj + 3 - bdj)) * AJ_BK + (lk + 2 - bdk);
+        const T t0 = tb[tb0], t1 = tb[tb0 + tstep];
+        T fb;
+        if (DIR == 0) fb = p.dtx * (t1 - t0);
+        else if (DIR == 1) fb = p.dty * (t1 - t0);
+        else {
+            fb = T(0);
+            if (t0 != T(0)) fb -= (p.dtz * p.mu[fk]) * p.rhow[fk + 1] * p.one_d_rhou[fk] * t0;
+            if (t1 != T(0)) fb += (p.dtz * p.mu[fk + 1]) * p.rhow[fk + 1] * p.one_d_rhou[fk + 1] * t1;
+        }
+        const T s1 = fb * gs;
+        fs1[f] = s1;
+        fs2[f] = (DIR == 2 && (fk == 1 || fk == p.nz - 2)) ? T(0) : (gs > T(0) ? s1 : -s1);
+        fab[f] = fb * ga;
+    }
+    __syncthreads();
     const T C5[6] = {W<T>::c1_60, -W<T>::c2_15, W<T>::c37_60, W<T>::c37_60, -W<T>::c2_15, W<T>::c1_60};
     const T U5[6] = {W<T>::c1_60, T(-5) * W<T>::c1_60, T(10) * W<T>::c1_60, T(-10) * W<T>::c1_60,
                      T(5) * W<T>::c1_60, -W<T>::c1_60};
     const T C3[4] = {-W<T>::c1_12, W<T>::c7_12, W<T>::c7_12, -W<T>::c1_12};
     const T U3[4] = {-W<T>::c1_12, T(3) * W<T>::c1_12, T(-3) * W<T>::c1_12, W<T>::c1_12};
-    T acc[4] = {T(0), T(0), T(0), T(0)};  // u, v, w, theta
-    for (int eq = 0; eq < 3; eq++) {
-        const int xf = eq == 0 ? FU : eq == 1 ? FV : FTH;
-        for (int dir = 0; dir < 3; dir++) {
-            int bi0, bj0, bk0, bni, bnj, bnk;
-            if (dir == 0) { bi0 = i0 - 3; bni = AJ_TI + 5; bj0 = j0; bnj = AJ_TJ + 1; bk0 = k0; bnk = AJ_TK; }
-            else if (dir == 1) { bi0 = i0; bni = AJ_TI + 1; bj0 = j0 - 3; bnj = AJ_TJ + 5; bk0 = k0; bnk = AJ_TK; }
-            else { bi0 = i0; bni = AJ_TI + 1; bj0 = j0; bnj = AJ_TJ + 1; bk0 = k0 - 2; bnk = AJ_TK + 3; }
-            const int nf = bni * bnj * bnk;
-            for (int f = t; f < nf; f += AJ_THREADS) {
-                const int fk = bk0 + f % bnk, fj = bj0 + (f / bnk) % bnj, fi = bi0 + f / (bnk * bnj);
-                T s1 = T(0), s2 = T(0), sa = T(0);
-                const T fb = adj_fbar(p, A, eq, dir, fi, fj, fk, step);
-                LinFace<T> L;
-                if (fb != T(0) && lin_face(p, R, eq, dir, fi, fj, fk, L)) {
-                    s1 = fb * L.gs;
-                    s2 = L.nx == 2 ? T(0) : L.sg * s1;
-                    sa = fb * L.ga;
-                }
-                fs1[f] = s1;
-                fs2[f] = s2;
-                fab[f] = sa;
+    const int nz = p.nz;
+#pragma unroll
+    for (int r = 0; r < AJ_CPT; r++) {
+        const int e = t + r * AJ_THREADS;
+        const int li = e / (AJ_TK * AJ_TJ), lj = (e / AJ_TK) % AJ_TJ, lk = e % AJ_TK;
+        // face-box coordinates of the cell
+        const int bi = li + bdi, bj = lj + bdj, bk = lk + bdk;
+        auto at = [&](int di, int dj, int dk) { return ((bi + di) * bnj + (bj + dj)) * bnk + (bk + dk); };
+        T gx = T(0), ga;
+        if (DIR == 0) {
+#pragma unroll
+            for (int m = 0; m < 6; m++) {
+                const int w = at(2 - m, 0, 0);
+                gx += C5[m] * fs1[w] + U5[m] * fs2[w];
             }
-            __syncthreads();
-            if (own) {
-                auto at = [&](int fi, int fj, int fk) { return ((fi - bi0) * bnj + (fj - bj0)) * bnk + (fk - bk0); };
-                T gx = T(0), ga = T(0);
-                if (dir == 0) {
+            if (EQ == 0) ga = T(0.5) * (fab[at(-1, 0, 0)] + fab[at(0, 0, 0)]);
+            else if (EQ == 1) ga = T(0.5) * (fab[at(-1, 0, 0)] + fab[at(-1, 1, 0)]);
+            else ga = fab[at(-1, 0, 0)];
+        } else if (DIR == 1) {
 #pragma unroll
-                    for (int m = 0; m < 6; m++) {
-                        const int w = at(pi + 2 - m, pj, pk);
-                        gx += C5[m] * fs1[w] + U5[m] * fs2[w];
-                    }
-                    if (eq == 0) ga = T(0.5) * (fab[at(pi - 1, pj, pk)] + fab[at(pi, pj, pk)]);
-                    else if (eq == 1) ga = T(0.5) * (fab[at(pi - 1, pj, pk)] + fab[at(pi - 1, pj + 1, pk)]);
-                    else ga = fab[at(pi - 1, pj, pk)];
-                } else if (dir == 1) {
+            for (int m = 0; m < 6; m++) {
+                const int w = at(0, 2 - m, 0);
+                gx += C5[m] * fs1[w] + U5[m] * fs2[w];
+            }
+            if (EQ == 0) ga = T(0.5) * (fab[at(0, -1, 0)] + fab[at(1, -1, 0)]);
+            else if (EQ == 1) ga = T(0.5) * (fab[at(0, -1, 0)] + fab[at(0, 0, 0)]);
+            else ga = fab[at(0, -1, 0)];
+        } else {
+            const int pk = k0 + lk;
 #pragma unroll
-                    for (int m = 0; m < 6; m++) {
-                        const int w = at(pi, pj + 2 - m, pk);
-                        gx += C5[m] * fs1[w] + U5[m] * fs2[w];
-                    }
-                    if (eq == 0) ga = T(0.5) * (fab[at(pi, pj - 1, pk)] + fab[at(pi + 1, pj - 1, pk)]);
-                    else if (eq == 1) ga = T(0.5) * (fab[at(pi, pj - 1, pk)] + fab[at(pi, pj, pk)]);
-                    else ga = fab[at(pi, pj - 1, pk)];
+            for (int d = -2; d <= 1; d++) {
+                const int fk = pk + d;
+                if (fk < 1 || fk > nz - 2) continue;
+                const int w = at(0, 0, d);
+                if (fk == 1 || fk == nz - 2) {
+                    if (d == 0 || d == -1) gx += T(0.5) * fs1[w];
                 } else {
-                    for (int fk = pk - 2; fk <= pk + 1; fk++) {
-                        if (fk < 1 || fk > nz - 2) continue;
-                        const int w = at(pi, pj, fk);
-                        if (fk == 1 || fk == nz - 2) {
-                            if (pk == fk || pk == fk + 1) gx += T(0.5) * fs1[w];
-                        } else {
-                            const int m = pk - (fk - 1);
-                            gx += C3[m] * fs1[w] + U3[m] * fs2[w];
-                        }
-                    }
-                    if (eq == 0) ga = T(0.5) * (fab[at(pi, pj, pk - 1)] + fab[at(pi + 1, pj, pk - 1)]);
-                    else if (eq == 1) ga = T(0.5) * (fab[at(pi, pj, pk - 1)] + fab[at(pi, pj + 1, pk - 1)]);
-                    else ga = fab[at(pi, pj, pk - 1)];
+                    const int m = 1 - d;  // position of the cell in the face's stencil fk-1..fk+2
+                    gx += C3[m] * fs1[w] + U3[m] * fs2[w];
                 }
-                acc[xf] += gx;
-                acc[dir] += ga;
             }
-            __syncthreads();
+            if (EQ == 0) ga = T(0.5) * (fab[at(0, 0, -1)] + fab[at(1, 0, -1)]);
+            else if (EQ == 1) ga = T(0.5) * (fab[at(0, 0, -1)] + fab[at(0, 1, -1)]);
+            else ga = fab[at(0, 0, -1)];
         }
+        acc[r][XF] += gx;
+        acc[r][DIR] += ga;
     }
-    if (!own) return;
-    // Coriolis terms of u and v (advection.cpp:84-92, 112-120)
-    {
-        const T fdt = p.dt * T(0.25);
-        const int ci[4] = {pi, pi, pi + 1, pi + 1}, cj[4] = {pj, pj - 1, pj, pj - 1};
-#pragma unroll
-        for (int n = 0; n < 4; n++) {
-            const T tu = adj_tbar(p, A, 0, ci[n], cj[n], pk, step);
-            if (tu != T(0)) acc[FV] += (fdt * p.f[cj[n]]) * tu;
-        }
-        const int di[4] = {pi, pi - 1, pi, pi - 1}, dj[4] = {pj, pj, pj + 1, pj + 1};
-#pragma unroll
-        for (int n = 0; n < 4; n++) {
-            const T tv = adj_tbar(p, A, 1, di[n], dj[n], pk, step);
-            if (tv != T(0)) acc[FU] -= (fdt * p.f[dj[n]]) * tv;
-        }
-    }
-    // vertical advection of the basic-state theta (Z_ADVECT_BASE) into w
-    {
-        const T t0 = adj_tbar(p, A, 2, pi, pj, pk - 1, step);
-        const T t1 = adj_tbar(p, A, 2, pi, pj, pk, step);
-        if (t0 != T(0))
-            acc[FW] -= (p.dtz * p.mu[pk - 1]) * T(0.5) * p.rhow[pk] * (p.tb[pk] - p.tb[pk - 1]) * p.one_d_rhou[pk - 1] * t0;
-        if (t1 != T(0))
-            acc[FW] -= (p.dtz * p.mu[pk]) * T(0.5) * p.rhow[pk] * (p.tb[pk] - p.tb[pk - 1]) * p.one_d_rhou[pk] * t1;
-    }
-    // buoyancy of w into theta
-    {
-        const int c = gix(ny, nz, pi, pj, pk);
-        T bw = T(0);
-        if (adv_cell(p, pi, pj, pk, 2)) bw += A.P[FW][c];
-        if (adv_cell(p, pi, pj, pk + 1, 2)) bw += A.P[FW][c + 1];
-        if (bw != T(0)) acc[FTH] += sdtg / p.tbv[pk] * bw;
-    }
-    const int c = gix(ny, nz, pi, pj, pk);
-#pragma unroll
-    for (int f = 0; f < 4; f++)
-        if (acc[f] != T(0)) A.cur[f][c] += acc[f];
+    __syncthreads();
 }
 
-// the forward advection overwrote P on its cells: M-bar += P-bar, P-bar = 0 there
+// the terms of equation EQ outside the face fluxes, from its tendency box:
+// Coriolis of u into v and of v into u (advection.cpp:84-92, 112-120), the
+// vertical advection of the basic-state theta (Z_ADVECT_BASE) into w
+template <typename T, int EQ>
+__device__ __forceinline__ void adj_extra(const KParams<T> &p, const T *tb, int i0, int j0, int k0,
+                                          T (&acc)[AJ_CPT][4])
+{
+    const T fdt = p.dt * T(0.25);
+#pragma unroll
+    for (int r = 0; r < AJ_CPT; r++) {
+        const int e = threadIdx.x + r * AJ_THREADS;
+        const int li = e / (AJ_TK * AJ_TJ), lj = (e / AJ_TK) % AJ_TJ, lk = e % AJ_TK;
+        const int pj = j0 + lj, pk = k0 + lk;
+        auto TB = [&](int di, int dj, int dk) { return tb[((li + 3 + di) * AJ_BJ + (lj + 3 + dj)) * AJ_BK + lk + 2 + dk]; };
+        if (EQ == 0) {
+            const int di[4] = {0, 0, 1, 1}, dj[4] = {0, -1, 0, -1};
+#pragma unroll
+            for (int n = 0; n < 4; n++) {
+                const T tu = TB(di[n], dj[n], 0);
+                if (tu != T(0)) acc[r][FV] += (fdt * p.f[pj + dj[n]]) * tu;
+            }
+        } else if (EQ == 1) {
+            const int di[4] = {0, -1, 0, -1}, dj[4] = {0, 0, 1, 1};
+#pragma unroll
+            for (int n = 0; n < 4; n++) {
+                const T tv = TB(di[n], dj[n], 0);
+                if (tv != T(0)) acc[r][FU] -= (fdt * p.f[pj + dj[n]]) * tv;
+            }
+        } else {
+            const T t0 = TB(0, 0, -1), t1 = TB(0, 0, 0);
+            if (t0 != T(0))
+                acc[r][FW] -= (p.dtz * p.mu[pk - 1]) * T(0.5) * p.rhow[pk] * (p.tb[pk] - p.tb[pk - 1]) *
+                              p.one_d_rhou[pk - 1] * t0;
+            if (t1 != T(0))
+                acc[r][FW] -= (p.dtz * p.mu[pk]) * T(0.5) * p.rhow[pk] * (p.tb[pk] - p.tb[pk - 1]) * p.one_d_rhou[pk] *
+                              t1;
+        }
+    }
+}
+
+template <typename T, int EQ>
+__device__ __forceinline__ void adj_equation(const KParams<T> &p, const T *__restrict__ coef, const KFields<T> &A,
+                                             T step, int i0, int j0, int k0, T *tb, T *fs1, T *fs2, T *fab,
+                                             T (&acc)[AJ_CPT][4])
+{
+    adj_stage_tbar<T, EQ>(p, A, step, i0, j0, k0, tb);
+    __syncthreads();
+    adj_family<T, EQ, 0>(p, coef, tb, i0, j0, k0, fs1, fs2, fab, acc);
+    adj_family<T, EQ, 1>(p, coef, tb, i0, j0, k0, fs1, fs2, fab, acc);
+    adj_family<T, EQ, 2>(p, coef, tb, i0, j0, k0, fs1, fs2, fab, acc);
+    adj_extra<T, EQ>(p, tb, i0, j0, k0, acc);
+    __syncthreads();
+}
+
 template <typename T>
-__global__ void k_adj_fold(KParams<T> p, KFields<T> A)
+__global__ void __launch_bounds__(AJ_THREADS) k_adj_advect(KParams<T> p, const T *__restrict__ coef, KFields<T> A,
+                                                           T step, T sdtg, int zero_cur)
+{
+    extern __shared__ unsigned char smem_raw[];
+    T *fs1 = (T *)smem_raw, *fs2 = fs1 + AJ_NFACE, *fab = fs2 + AJ_NFACE, *tb = fab + AJ_NFACE;
+    const int ny = p.ny, nz = p.nz;
+    const int i0 = blockIdx.x * AJ_TI, j0 = blockIdx.y * AJ_TJ, k0 = blockIdx.z * AJ_TK;
+    T acc[AJ_CPT][4];
+#pragma unroll
+    for (int r = 0; r < AJ_CPT; r++)
+        for (int f = 0; f < 4; f++) acc[r][f] = T(0);
+    adj_equation<T, 0>(p, coef, A, step, i0, j0, k0, tb, fs1, fs2, fab, acc);
+    adj_equation<T, 1>(p, coef, A, step, i0, j0, k0, tb, fs1, fs2, fab, acc);
+    adj_equation<T, 2>(p, coef, A, step, i0, j0, k0, tb, fs1, fs2, fab, acc);
+#pragma unroll
+    for (int r = 0; r < AJ_CPT; r++) {
+        const int e = threadIdx.x + r * AJ_THREADS;
+        const int pi = i0 + e / (AJ_TK * AJ_TJ), pj = j0 + (e / AJ_TK) % AJ_TJ, pk = k0 + e % AJ_TK;
+        if (pi >= p.nx || pj >= ny || pk >= nz) continue;
+        T *a = acc[r];
+        const int c = gix(ny, nz, pi, pj, pk);
+        // buoyancy of w into theta
+        {
+            T bw = T(0);
+            if (adv_cell(p, pi, pj, pk, 2)) bw += A.P[FW][c];
+            if (adv_cell(p, pi, pj, pk + 1, 2)) bw += A.P[FW][c + 1];
+            if (bw != T(0)) a[FTH] += sdtg / p.tbv[pk] * bw;
+        }
+#pragma unroll
+        for (int f = 0; f < 4; f++) {
+            const bool cell = adv_cell(p, pi, pj, pk, f == FW ? 2 : 1);
+            if (cell) A.M[f][c] += A.P[f][c];
+            if (zero_cur && cell) A.cur[f][c] = a[f];
+            else if (a[f] != T(0)) A.cur[f][c] += a[f];
+        }
+        if (pk >= 1 && pk <= nz - 2 && (pi == 0 || pi == p.nx - 1 || pj == 0 || pj == ny - 1)) {
+            A.P[FU][c] = T(0);
+            A.P[FV][c] = T(0);
+            A.P[FW][c] = T(0);
+        }
+    }
+}
+
+// after the last stage of an adjoint run: the forward advection overwrote P
+// on its cells, so their P-bar is zero
+template <typename T>
+__global__ void k_adj_zero_cells(KParams<T> p, KFields<T> A)
 {
     const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
     const int nzi = p.nz - 2, nyi = p.ny - 6, nxi = p.nx - 6;
@@ -345,7 +483,6 @@ __global__ void k_adj_fold(KParams<T> p, KFields<T> A)
 #pragma unroll
     for (int f = 0; f < 4; f++) {
         if (f == FW && k < 2) continue;
-        A.M[f][c] += A.P[f][c];
         A.P[f][c] = T(0);
     }
 }
@@ -355,7 +492,10 @@ __global__ void k_adj_fold(KParams<T> p, KFields<T> A)
 // advance_outer, Rayleigh damping, the top/bottom conditions and the sponge
 // strips, in reverse order, for u, v, w, theta.  Blocks own whole columns.
 // ---------------------------------------------------------------------------
-enum { AP_OUTER = 1, AP_RAYLEIGH = 2, AP_VBC = 4, AP_SPONGE = 8 };
+// AP_SPONGE2: the sponge twice (the step-final post and the last stage's post
+// act on the same buffer back to back; the second top/bottom transpose is
+// then the identity, so only the sponge repeats)
+enum { AP_OUTER = 1, AP_RAYLEIGH = 2, AP_VBC = 4, AP_SPONGE = 8, AP_SPONGE2 = 16 };
 
 template <typename T>
 __device__ __forceinline__ T adj_post_pre(const KParams<T> &p, const KFields<T> &A, int f, int i, int j, int k,
@@ -402,7 +542,7 @@ __global__ void __launch_bounds__(POST_THREADS) k_adj_post(KParams<T> p, KFields
                     else if (k == nz - 2) v = v + adj_post_pre(p, A, f, i, j, nz - 1, flags);
                 }
             }
-            if (flags & AP_SPONGE) {
+            for (int rep = (flags & AP_SPONGE2) ? 2 : (flags & AP_SPONGE) ? 1 : 0; rep > 0; rep--) {
                 if (hN) v = v - p.cn[j - p.nb] * v;
                 if (hS) v = v - p.cs[j - p.sb] * v;
                 if (hW) v = v - p.cw[i - p.wb] * v;
@@ -565,6 +705,145 @@ __device__ void thomas_T_column(T2 *x, A *Fw, int nz, A hb, A inv_s, const A *rh
     }
 }
 
+// FP32 transposed solve of one wavenumber (not the mean mode): the recurrence
+// of thomas_T_column with one reciprocal per level
+__device__ __forceinline__ void thomas_T_column_fast(float2 *x, float *Fw, int nz, float hb, float inv_s,
+                                                     const float *rhou, const float *ac, const float *cc,
+                                                     const float *vc)
+{
+    const int K = nz - 2;
+    float rb = __frcp_rn(rhou[1] * hb - vc[1]);
+    float w = (1 < K) ? ac[2] * rb : 0.f;
+    Fw[1] = w;
+    float gr = x[1].x * inv_s * rb, gi = x[1].y * inv_s * rb;
+    x[1] = make_float2(gr, gi);
+    for (int k = 2; k <= K; k++) {
+        const float sb = cc[k - 1];
+        rb = __frcp_rn(rhou[k] * hb - vc[k] - sb * w);
+        w = (k < K) ? ac[k + 1] * rb : 0.f;
+        Fw[k] = w;
+        gr = (x[k].x * inv_s - sb * gr) * rb;
+        gi = (x[k].y * inv_s - sb * gi) * rb;
+        x[k] = make_float2(gr, gi);
+    }
+    for (int k = K - 1; k >= 1; k--) {
+        gr = x[k].x - Fw[k] * gr;
+        gi = x[k].y - Fw[k] * gi;
+        x[k] = make_float2(gr, gi);
+    }
+}
+
+// FP64 solve of the transposed mean-mode system M'^T z = y / (ni nj) by
+// parallel cyclic reduction across a warp (rows 1..nl), then z_K = 0 (see
+// thomas_T_column).  wk as for pcr_column_f64.
+template <typename T2>
+__device__ void pcr_column_T_f64(T2 *x, int nl, double hcol, double dx2, double size2d, const double *rhou,
+                                 const double *ac, const double *cc, const double *vc, double *wk)
+{
+    const int lane = (threadIdx.y * blockDim.x + threadIdx.x) & 31;
+    constexpr int R = PCR_ROWS;
+    double *A0 = wk, *B0 = wk + R, *C0 = wk + 2 * R, *R0 = wk + 3 * R, *I0 = wk + 4 * R;
+    double *A1 = wk + 5 * R, *B1 = wk + 6 * R, *C1 = wk + 7 * R, *R1 = wk + 8 * R, *I1 = wk + 9 * R;
+    const int K = nl;
+    for (int r = lane; r < R; r += 32) {
+        if (r < nl) {
+            const int k = r + 1;
+            const double a = k >= 2 ? cc[k - 1] : 0.0;
+            const double b = k == K ? 1.0 : rhou[k] * 2.0 * hcol / dx2 - vc[k];
+            const double c = k < K - 1 ? ac[k + 1] : 0.0;
+            A0[r] = a; B0[r] = b; C0[r] = c;
+            R0[r] = (double)x[k].x / size2d;
+            I0[r] = (double)x[k].y / size2d;
+        }
+    }
+    __syncwarp();
+    for (int s = 1; s < nl; s <<= 1) {
+        for (int r = lane; r < nl; r += 32) {
+            double a = A0[r], b = B0[r], c = C0[r], dr = R0[r], di = I0[r];
+            double na = 0.0, nc = 0.0;
+            if (r - s >= 0) {
+                const double al = -a / B0[r - s];
+                na = al * A0[r - s];
+                b += al * C0[r - s];
+                dr += al * R0[r - s];
+                di += al * I0[r - s];
+            }
+            if (r + s < nl) {
+                const double ga = -c / B0[r + s];
+                nc = ga * C0[r + s];
+                b += ga * A0[r + s];
+                dr += ga * R0[r + s];
+                di += ga * I0[r + s];
+            }
+            A1[r] = na; B1[r] = b; C1[r] = nc; R1[r] = dr; I1[r] = di;
+        }
+        __syncwarp();
+        double *t;
+        t = A0; A0 = A1; A1 = t; t = B0; B0 = B1; B1 = t; t = C0; C0 = C1; C1 = t;
+        t = R0; R0 = R1; R1 = t; t = I0; I0 = I1; I1 = t;
+    }
+    for (int r = lane; r < nl; r += 32) {
+        T2 v;
+        v.x = (decltype(v.x))(r == nl - 1 ? 0.0 : R0[r] / B0[r]);
+        v.y = (decltype(v.y))(r == nl - 1 ? 0.0 : I0[r] / B0[r]);
+        x[r + 1] = v;
+    }
+    __syncwarp();
+}
+
+// transposed spectral step of one y-wavenumber q: forward FFT along x,
+// transposed tridiagonal solves, inverse FFT along x (the adjoint of
+// k_spectral_x has the same transform directions)
+template <typename T>
+__global__ void k_spectral_x_adj(KParams<T> p, typename V2<T>::t *spec, FftPlan pi, const typename V2<T>::t *tw,
+                                 int ps)
+{
+    typedef typename V2<T>::t T2;
+    extern __shared__ unsigned char smem_raw[];
+    __shared__ T c_r[PPM_MAXZ], c_a[PPM_MAXZ], c_c[PPM_MAXZ], c_v[PPM_MAXZ];
+    __shared__ double d_r[PPM_MAXZ], d_a[PPM_MAXZ], d_c[PPM_MAXZ], d_v[PPM_MAXZ];
+    __shared__ double pcr_wk[PCR_WK];
+    T2 *a = (T2 *)smem_raw;
+    T2 *b = a + (long)p.ni * ps;
+    const int q = blockIdx.x;
+    const int nl = p.nz - 2;
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x, nth = blockDim.x * blockDim.y;
+    for (int k = tid; k < p.nz; k += nth) {
+        c_r[k] = p.rhou[k]; c_a[k] = p.acoef[k]; c_c[k] = p.ccoef[k]; c_v[k] = p.vcoef[k];
+        d_r[k] = p.rhou_d[k]; d_a[k] = p.acoef_d[k]; d_c[k] = p.ccoef_d[k]; d_v[k] = p.vcoef_d[k];
+    }
+    for (int i = threadIdx.y; i < p.ni; i += blockDim.y)
+        for (int l = threadIdx.x; l < nl; l += blockDim.x) a[i * ps + l] = spec[((long)i * p.nj + q) * p.nz + 1 + l];
+    __syncthreads();
+    T2 *r = fft_smem<T, T2>(a, b, nl, pi, tw, false, ps);
+    T2 *fr = (r == a) ? b : a;
+    const double size2d = (double)(p.ni * p.nj);
+    if (sizeof(T) == 8) {
+        for (int pp = tid; pp < p.ni; pp += nth) {
+            const long col = (long)pp * p.nj + q;
+            double *Fw = (double *)(fr + (long)pp * ps) - 1;
+            thomas_T_column<T2, double>(r + (long)pp * ps - 1, Fw, p.nz, 2.0 * p.hcoef[col] / p.dx2, 1.0 / size2d, d_r,
+                                        d_a, d_c, d_v, col == 0);
+        }
+    } else {
+        const float dx2 = (float)p.dx2, inv_s = (float)(1.0 / size2d);
+        for (int pp = tid; pp < p.ni; pp += nth) {
+            const long col = (long)pp * p.nj + q;
+            if (col == 0) continue;  // mean mode: FP64 below
+            const float hb = 2.0f * (float)p.hcoef[col] / dx2;
+            float *Fw = (float *)(fr + (long)pp * ps) - 1;
+            thomas_T_column_fast((float2 *)(r + (long)pp * ps - 1), Fw, p.nz, hb, inv_s, (const float *)c_r,
+                                 (const float *)c_a, (const float *)c_c, (const float *)c_v);
+        }
+        if (q == 0 && tid < 32)
+            pcr_column_T_f64(r - 1, nl, p.hcoef[0], p.dx2, size2d, d_r, d_a, d_c, d_v, pcr_wk);
+    }
+    __syncthreads();
+    T2 *o = fft_smem<T, T2>(r, fr, nl, pi, tw, true, ps);
+    for (int i = threadIdx.y; i < p.ni; i += blockDim.y)
+        for (int l = threadIdx.x; l < nl; l += blockDim.x) spec[((long)i * p.nj + q) * p.nz + 1 + l] = o[i * ps + l];
+}
+
 // transposed solves of every wavenumber, TC columns per block staged through
 // shared memory (one thread per column).  FP32 contexts solve the mean mode
 // in FP64.
@@ -599,7 +878,49 @@ __global__ void k_thomas_adj(KParams<T> p, typename V2<T>::t *spec, int TC)
 }
 
 // transposed divergence (divergence3d, pressure.cpp:1340-1381) with its
-// lateral copies: adds to P-bar of u, v, w at every point
+// lateral copies, then the transposed mirror_boundaries (boundaries.cpp:
+// 363-379) of P u, v, w that preceded it: a point of the lateral ring (levels
+// 1..NZ-2) passes its value to the interior point it copied, so every
+// interior point gathers the ring points that mirror it.  Ring points are
+// left as they are here and zeroed by k_adj_advect, which never reads them.
+template <typename T>
+__device__ __forceinline__ T adj_dint(const KParams<T> &p, const T *db, int a, int b, int c)
+{
+    const int nx = p.nx, ny = p.ny, nz = p.nz;
+    if (a < 1 || a > nx - 2 || b < 1 || b > ny - 2 || c < 1 || c > nz - 2) return T(0);
+    T v = db[gix(ny, nz, a, b, c)];
+    if (a == 1) v += db[gix(ny, nz, 0, b, c)];
+    if (a == nx - 2) v += db[gix(ny, nz, nx - 1, b, c)];
+    if (b == 1 || b == ny - 2) {
+        const int br = b == 1 ? 0 : ny - 1;
+        v += db[gix(ny, nz, a, br, c)];
+        if (a == 1) v += db[gix(ny, nz, 0, br, c)];
+        if (a == nx - 2) v += db[gix(ny, nz, nx - 1, br, c)];
+    }
+    return v;
+}
+
+// P-bar of u, v, w at (i,j,k) plus the transposed divergence there
+template <typename T>
+__device__ __forceinline__ void adj_div_point(const KParams<T> &p, const KFields<T> &A, const T *db, T sdt, int i,
+                                              int j, int k, T &u, T &v, T &w)
+{
+    const int c = gix(p.ny, p.nz, i, j, k);
+    const T d0 = adj_dint(p, db, i, j, k), dxm = adj_dint(p, db, i - 1, j, k);
+    const T dym = adj_dint(p, db, i, j - 1, k), dzm = adj_dint(p, db, i, j, k - 1);
+    u = A.P[FU][c];
+    v = A.P[FV][c];
+    w = A.P[FW][c];
+    if (dxm != T(0) || d0 != T(0)) u += p.rhou[k] * p.one_d_dx * (dxm - d0) / sdt;
+    if (dym != T(0) || d0 != T(0)) v += p.rhou[k] * p.one_d_dy * (dym - d0) / sdt;
+    if (dzm != T(0) || d0 != T(0)) {
+        T s = T(0);
+        if (dzm != T(0)) s += p.mu[k - 1] * dzm;
+        if (d0 != T(0)) s -= p.mu[k] * d0;
+        w += p.rhow[k] * p.one_d_dz * s / sdt;
+    }
+}
+
 template <typename T>
 __global__ void k_adj_div(KParams<T> p, KFields<T> A, const T *db, T sdt)
 {
@@ -607,58 +928,29 @@ __global__ void k_adj_div(KParams<T> p, KFields<T> A, const T *db, T sdt)
     if (t >= p.n) return;
     const int nz = p.nz, ny = p.ny, nx = p.nx;
     const int k = (int)(t % nz), j = (int)((t / nz) % ny), i = (int)(t / ((long)nz * ny));
-    auto dint = [&](int a, int b, int c) -> T {
-        if (a < 1 || a > nx - 2 || b < 1 || b > ny - 2 || c < 1 || c > nz - 2) return T(0);
-        T v = db[gix(ny, nz, a, b, c)];
-        if (a == 1) v += db[gix(ny, nz, 0, b, c)];
-        if (a == nx - 2) v += db[gix(ny, nz, nx - 1, b, c)];
-        if (b == 1 || b == ny - 2) {
-            const int br = b == 1 ? 0 : ny - 1;
-            v += db[gix(ny, nz, a, br, c)];
-            if (a == 1) v += db[gix(ny, nz, 0, br, c)];
-            if (a == nx - 2) v += db[gix(ny, nz, nx - 1, br, c)];
-        }
-        return v;
-    };
-    const T d0 = dint(i, j, k), dxm = dint(i - 1, j, k), dym = dint(i, j - 1, k), dzm = dint(i, j, k - 1);
+    const bool lev = k >= 1 && k <= nz - 2;
+    if (lev && (i == 0 || i == nx - 1 || j == 0 || j == ny - 1)) return;
+    T u, v, w;
+    adj_div_point(p, A, db, sdt, i, j, k, u, v, w);
+    if (lev) {
+        const int is[2] = {i, i == 1 ? 0 : i == nx - 2 ? nx - 1 : -1};
+        const int js[2] = {j, j == 1 ? 0 : j == ny - 2 ? ny - 1 : -1};
+#pragma unroll
+        for (int a = 0; a < 2; a++)
+#pragma unroll
+            for (int b = 0; b < 2; b++) {
+                if ((a == 0 && b == 0) || is[a] < 0 || js[b] < 0) continue;
+                T ru, rv, rw;
+                adj_div_point(p, A, db, sdt, is[a], js[b], k, ru, rv, rw);
+                u += ru;
+                v += rv;
+                w += rw;
+            }
+    }
     const int c = (int)t;
-    if (dxm != T(0) || d0 != T(0)) A.P[FU][c] += p.rhou[k] * p.one_d_dx * (dxm - d0) / sdt;
-    if (dym != T(0) || d0 != T(0)) A.P[FV][c] += p.rhou[k] * p.one_d_dy * (dym - d0) / sdt;
-    if (dzm != T(0) || d0 != T(0)) {
-        T v = T(0);
-        if (dzm != T(0)) v += p.mu[k - 1] * dzm;
-        if (d0 != T(0)) v -= p.mu[k] * d0;
-        A.P[FW][c] += p.rhow[k] * p.one_d_dz * v / sdt;
-    }
-}
-
-// transposed mirror_boundaries (boundaries.cpp:363-379) of up to three
-// fields, in place: block = one level; the j copies were applied last, so
-// their transpose runs first
-template <typename T>
-__global__ void k_adj_mirror(KParams<T> p, T *a0, T *a1, T *a2)
-{
-    const int nx = p.nx, ny = p.ny, nz = p.nz;
-    const int k = 1 + blockIdx.x;
-    T *fl[3] = {a0, a1, a2};
-    for (int n = 0; n < 3; n++) {
-        T *a = fl[n];
-        if (!a) continue;
-        for (int i = threadIdx.x; i < nx; i += blockDim.x) {
-            a[gix(ny, nz, i, 1, k)] += a[gix(ny, nz, i, 0, k)];
-            a[gix(ny, nz, i, 0, k)] = T(0);
-            a[gix(ny, nz, i, ny - 2, k)] += a[gix(ny, nz, i, ny - 1, k)];
-            a[gix(ny, nz, i, ny - 1, k)] = T(0);
-        }
-        __syncthreads();
-        for (int j = threadIdx.x; j < ny; j += blockDim.x) {
-            a[gix(ny, nz, 1, j, k)] += a[gix(ny, nz, 0, j, k)];
-            a[gix(ny, nz, 0, j, k)] = T(0);
-            a[gix(ny, nz, nx - 2, j, k)] += a[gix(ny, nz, nx - 1, j, k)];
-            a[gix(ny, nz, nx - 1, j, k)] = T(0);
-        }
-        __syncthreads();
-    }
+    A.P[FU][c] = u;
+    A.P[FV][c] = v;
+    A.P[FW][c] = w;
 }
 
 // a += b over n elements (tangent and adjoint bookkeeping)
