@@ -300,6 +300,7 @@ def adjoint_bench(torch, device, steps, every):
            "memory": "checkpoints: steps/every+1 states of 12 fields; trajectory: every x 12 fields"}
     for name, prec in (("fp32", abi.GA_PREC_F32), ("fp64", abi.GA_PREC_F64)):
         m = anelastic.Model(wl, prec, device=device)
+        m.tune()
         ext = torch.cuda.ExternalStream(m.stream_handle())
         zero = np.zeros(wl.points)
 
@@ -407,6 +408,9 @@ def run_ours(args):
     prec = abi.GA_PREC_F32 if args.precision == "f32" else abi.GA_PREC_F64
     model = anelastic.Model(wl, prec, device=device)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{device}")
+    t_tune = time.perf_counter()
+    tuning = model.tune()
+    t_tune = time.perf_counter() - t_tune
     # warm-up
     for _ in range(args.warmup):
         model.step(1)
@@ -445,11 +449,13 @@ def run_ours(args):
                        "physics": "Kessler, rain_fallout 1, 5-point sponges, Rayleigh from NZ-5",
                        "l2": "256 MiB written between timed steps, outside the events",
                        "parallelism": f"replicas x{world}" if world > 1 else "single domain"},
-            "roofline": roof, "gpu_launches": int(launches), "clocks": clocks}
+            "roofline": roof, "gpu_launches": int(launches), "clocks": clocks,
+            "tuning": {"choice": tuning, "seconds": round(t_tune, 2)}}
     line["hbm_fraction_step"] = round(value / world * STEP_BYTES_FP32_MOIST / 1e9 / peak, 4) \
         if prec == abi.GA_PREC_F32 else None
     if not args.no_fp64 and prec == abi.GA_PREC_F32:
         m64 = anelastic.Model(wl, abi.GA_PREC_F64, device=device)
+        m64.tune()
         for _ in range(2):
             m64.step(1)
         per64 = time_steps(m64, torch, args.fp64_steps, flush)

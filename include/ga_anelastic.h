@@ -217,6 +217,19 @@ GA_API void *ga_stream(ga_ctx *ctx);
 GA_API void *ga_field_device_ptr(ga_ctx *ctx, int field, int slot);
 
 /*
+ * Autotuner.  No counterpart in the reference.  ga_tune times the candidate
+ * tile shapes and FFT plans of this context on its current state (advection
+ * tile 4x4, 2x4, 4x2, 4x8, 8x4; the level tile of the y transforms; the
+ * factor order of the x and y FFTs; the x level tile when the x transform is
+ * not fused with the solve) and keeps the fastest.  The state is unchanged.
+ * Every tile gives bit-identical results; the FFT factor orders round
+ * differently (FP64: ~1e-15).  ga_tuning writes the current choice as text
+ * (NUL-terminated, truncated to n bytes).
+ */
+GA_API int ga_tune(ga_ctx *ctx);
+GA_API int ga_tuning(ga_ctx *ctx, char *buf, size_t n);
+
+/*
  * Tangent-linear model and adjoint of the step.  No counterpart in the
  * reference, which has no linearisation; this differentiates exactly the step
  * ga_step runs, for dry (microphysics_option 0), non-periodic contexts

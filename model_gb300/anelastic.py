@@ -59,6 +59,8 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     L.ga_stream.restype = C.c_void_p
     L.ga_field_device_ptr.argtypes = [C.c_void_p, C.c_int, C.c_int]
     L.ga_field_device_ptr.restype = C.c_void_p
+    L.ga_tune.argtypes = [C.c_void_p]
+    L.ga_tuning.argtypes = [C.c_void_p, C.c_char_p, C.c_size_t]
     L.ga_lin_set_field.argtypes = [C.c_void_p, C.c_int, C.c_int, _DP, C.c_size_t]
     L.ga_lin_get_field.argtypes = [C.c_void_p, C.c_int, C.c_int, _DP, C.c_size_t]
     L.ga_tlm_step.argtypes = [C.c_void_p, C.c_int]
@@ -248,6 +250,17 @@ class Model:
 
     def device_ptr(self, field: int, slot: int = 0) -> int:
         return self.L.ga_field_device_ptr(self.h, field, slot) or 0
+
+    # ---- autotuner -------------------------------------------------------
+    def tune(self) -> str:
+        """Time the candidate tile shapes and FFT plans, keep the fastest."""
+        self._check(self.L.ga_tune(self.h), "ga_tune")
+        return self.tuning()
+
+    def tuning(self) -> str:
+        buf = C.create_string_buffer(512)
+        self._check(self.L.ga_tuning(self.h, buf, 512), "ga_tuning")
+        return buf.value.decode()
 
     # ---- tangent-linear model and adjoint (dry, non-periodic) -------------
     LIN_FIELDS = (abi.GA_U, abi.GA_V, abi.GA_W, abi.GA_TH)

@@ -2,6 +2,7 @@
 // Argument checks, error text, context bookkeeping and the host-only column
 // builders live here; everything else is forwarded to the per-precision
 // engine.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <exception>
@@ -218,6 +219,22 @@ int ga_check_finite(ga_ctx *ctx)
 }
 
 long long ga_launch_count(ga_ctx *ctx) { return ctx ? ctx->e->launches : -1; }
+
+int ga_tune(ga_ctx *ctx)
+{
+    if (!ctx) return fail(GA_ERR_ARG, "ga_tune: null context");
+    return ctx->e->tune();
+}
+
+int ga_tuning(ga_ctx *ctx, char *buf, size_t n)
+{
+    if (!ctx || !buf || n == 0) return fail(GA_ERR_ARG, "ga_tuning: bad arguments");
+    const std::string &t = ctx->e->tuning.empty() ? std::string("defaults (not tuned)") : ctx->e->tuning;
+    const size_t m = std::min(n - 1, t.size());
+    std::memcpy(buf, t.data(), m);
+    buf[m] = 0;
+    return GA_OK;
+}
 
 int ga_lin_set_field(ga_ctx *ctx, int field, int slot, const double *host, size_t n)
 {

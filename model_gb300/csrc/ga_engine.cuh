@@ -3,6 +3,7 @@
 // the per-operator launch sequences and the fused RK3 step.
 #pragma once
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <memory>
 #include <string>
@@ -15,18 +16,39 @@ namespace ga {
 
 static inline int cdiv(long a, long b) { return (int)((a + b - 1) / b); }
 
-// prime factors of n for the shared-memory FFT, radix 4 first
-static inline FftPlan make_fft_plan(int n)
+// Factor plan of the shared-memory FFT of length n.  order (autotuned):
+// 0 radix 4 first, then 2, then odd primes; 1 the radix 2 first; 2 radix 2
+// only; 3 odd primes first.  Returns nfac = 0 for an order that gives no new
+// plan for this n.
+static inline FftPlan make_fft_plan(int n, int order = 0)
 {
     FftPlan P;
     std::memset(&P, 0, sizeof(P));
     P.n = n;
-    int m = n;
-    while (m % 4 == 0 && P.nfac < 23) { P.fac[P.nfac++] = 4; m /= 4; }
-    for (int f = 2; m > 1 && P.nfac < 24;) {
-        if (m % f == 0) { P.fac[P.nfac++] = f; m /= f; }
-        else f = (f == 2) ? 3 : f + 2;
+    int m = n, c4 = 0, c2 = 0, odd[24], no = 0;
+    while (m % 4 == 0) { c4++; m /= 4; }
+    if (m % 2 == 0) { c2 = 1; m /= 2; }
+    for (int f = 3; m > 1 && no < 24;) {
+        if (m % f == 0) { odd[no++] = f; m /= f; }
+        else f += 2;
     }
+    if (order == 1 && c2 == 0) return P;   // same as order 0
+    if (order == 2) {
+        if (c4 == 0) return P;
+        c2 += 2 * c4;
+        c4 = 0;
+    }
+    if (order == 3 && (no == 0 || (c4 == 0 && c2 == 0))) return P;
+    auto push = [&](int f) { if (P.nfac < 24) P.fac[P.nfac++] = f; };
+    if (order == 3)
+        for (int t = 0; t < no; t++) push(odd[t]);
+    if (order == 1)
+        for (int t = 0; t < c2; t++) push(2);
+    for (int t = 0; t < c4; t++) push(4);
+    if (order != 1)
+        for (int t = 0; t < c2; t++) push(2);
+    if (order != 3)
+        for (int t = 0; t < no; t++) push(odd[t]);
     int ns = 1;
     for (int f = 0; f < P.nfac; f++) {
         P.nslog[f] = (ns & (ns - 1)) == 0 ? __builtin_ctz(ns) : -1;
@@ -71,6 +93,8 @@ class Engine : public EngineBase {
     bool use_graphs = true;
     int status = GA_OK;
     std::unique_ptr<LinBase> lin;  // tangent-linear / adjoint buffers, on first use
+    int adv_ti = ADV_TI, adv_tj = ADV_TJ;  // advection tile (autotuned)
+    int plan_order_i = 0, plan_order_j = 0;
 
     Lin<T> *linear();
     int lin_supported() const;
@@ -244,8 +268,12 @@ class Engine : public EngineBase {
             smem_sx = 2 * (size_t)ni * psx * sizeof(T2);
         }
         cudaFuncSetAttribute(k_spectral_x<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
-        smem_adv = (size_t)ADV_NF * ((ADV_TI + 1) * ADV_TJ + ADV_TI * (ADV_TJ + 1) + ADV_TI * ADV_TJ) * NZ * sizeof(T);
-        cudaFuncSetAttribute(k_advect_tile<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+        smem_adv = advect_tile_smem(adv_ti, adv_tj, NZ, sizeof(T));
+        cudaFuncSetAttribute(k_advect_tile<T, 4, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+        cudaFuncSetAttribute(k_advect_tile<T, 2, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+        cudaFuncSetAttribute(k_advect_tile<T, 4, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+        cudaFuncSetAttribute(k_advect_tile<T, 4, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+        cudaFuncSetAttribute(k_advect_tile<T, 8, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
         cudaFuncSetAttribute(k_div_fft_y<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
         cudaFuncSetAttribute(k_ifft_y_pi<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
         cudaFuncSetAttribute(k_fft_x<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
@@ -425,13 +453,26 @@ class Engine : public EngineBase {
     }
 
     // ------------------------------------------------------------------ ops
+    // the advection tiles the autotuner chooses from
+    static constexpr int kAdvTiles[5][2] = {{4, 4}, {2, 4}, {4, 2}, {4, 8}, {8, 4}};
+    template <int TI, int TJ>
+    void launch_advect_tile(T step, T sdtg, int what)
+    {
+        dim3 grid(cdiv(NX - 6, TI), cdiv(NY - 6, TJ));
+        k_advect_tile<T, TI, TJ><<<grid, 256, smem_adv, stream>>>(kp, fields(), step, sdtg, what);
+    }
+
     void advect(double step, int what)
     {
         const double sdtg = step * cfg.dt * 9.8 * 0.5;  // step*dt*grav*0.5, advection.cpp:330
         ProfScope ps(this, PC_ADVECT, 1);
         if (smem_adv <= 200 * 1024) {
-            dim3 grid(cdiv(NX - 6, ADV_TI), cdiv(NY - 6, ADV_TJ));
-            k_advect_tile<T><<<grid, 256, smem_adv, stream>>>(kp, fields(), (T)step, (T)sdtg, what);
+            const T st = (T)step, sg = (T)sdtg;
+            if (adv_ti == 2) launch_advect_tile<2, 4>(st, sg, what);
+            else if (adv_tj == 2) launch_advect_tile<4, 2>(st, sg, what);
+            else if (adv_tj == 8) launch_advect_tile<4, 8>(st, sg, what);
+            else if (adv_ti == 8) launch_advect_tile<8, 4>(st, sg, what);
+            else launch_advect_tile<4, 4>(st, sg, what);
         } else {  // face tiles of very tall columns do not fit: per-point form
             const long tot = (long)(NX - 6) * (NY - 6) * (NZ - 2);
             k_advect<T><<<cdiv(tot, 128), 128, 0, stream>>>(kp, fields(), (T)step, (T)sdtg, what);
@@ -662,6 +703,137 @@ class Engine : public EngineBase {
         swap_inner(true);
         mtime += cfg.dt;
         bigcounter++;
+    }
+
+    // ---------------------------------------------------------------- tuning
+    // Times the candidates of each tunable kernel group on this context's own
+    // data and keeps the fastest: the advection tile, the level tile of the y
+    // transforms, the factor order of both FFTs and (unfused x path) the level
+    // tile of the x transforms.  The groups write P, the fall speed, the
+    // spectral buffer and pi; P, the fall speed and pi are restored afterwards.
+    int tune() override
+    {
+        cudaSetDevice(device);
+        refresh_base();
+        const int nsnap = nprog + 2;
+        T *snap = nullptr;
+        if (cudaMalloc(&snap, (size_t)nsnap * N * sizeof(T)) != cudaSuccess) return GA_ERR_NOMEM;
+        for (int f = 0; f < nprog; f++)
+            cudaMemcpyAsync(snap + (size_t)f * N, buf[f][pi_[f]], N * sizeof(T), cudaMemcpyDeviceToDevice, stream);
+        cudaMemcpyAsync(snap + (size_t)nprog * N, pi, N * sizeof(T), cudaMemcpyDeviceToDevice, stream);
+        cudaMemcpyAsync(snap + (size_t)(nprog + 1) * N, vt, N * sizeof(T), cudaMemcpyDeviceToDevice, stream);
+        cudaEvent_t ea, eb;
+        cudaEventCreate(&ea);
+        cudaEventCreate(&eb);
+        const long long l0 = launches;
+        auto timeit = [&](auto fn) {
+            fn();  // warm-up
+            cudaEventRecord(ea, stream);
+            for (int r = 0; r < 3; r++) fn();
+            cudaEventRecord(eb, stream);
+            cudaEventSynchronize(eb);
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, ea, eb);
+            return cudaGetLastError() == cudaSuccess ? ms / 3.f : 1e30f;
+        };
+        const int what = ADV_UV | ADV_WB | ADV_TH | (kp.moist ? (ADV_Q | ADV_ZERO) : 0);
+        std::string info;
+        char line[160];
+        // advection tile
+        {
+            float best = 1e30f;
+            int bi = adv_ti, bj = adv_tj;
+            for (auto &tl : kAdvTiles) {
+                const size_t sm = advect_tile_smem(tl[0], tl[1], NZ, sizeof(T));
+                if (sm > 200 * 1024) continue;
+                adv_ti = tl[0]; adv_tj = tl[1]; smem_adv = sm;
+                const float t = timeit([&] { advect(1. / 3., what); });
+                if (t < best) { best = t; bi = tl[0]; bj = tl[1]; }
+            }
+            adv_ti = bi; adv_tj = bj;
+            smem_adv = advect_tile_smem(bi, bj, NZ, sizeof(T));
+            std::snprintf(line, sizeof line, "advect tile %dx%d (%.4f ms); ", bi, bj, best);
+            info += line;
+        }
+        // y transforms: level tile, then factor order
+        auto set_kty = [&](int kt) {
+            KTy = kt;
+            lgKTy = 0;
+            while ((1 << lgKTy) < kt) lgKTy++;
+            smem_y = 2 * (size_t)kp.nj * KTy * sizeof(T2);
+        };
+        {
+            float best = 1e30f;
+            int bk = KTy;
+            for (int kt = 1; kt <= 64 && kt <= 2 * (NZ - 2); kt <<= 1) {
+                if (2 * (size_t)kp.nj * kt * sizeof(T2) > 200 * 1024) break;
+                set_kty(kt);
+                const float t = timeit([&] { solve_pressure(1. / 3.); });
+                if (t < best) { best = t; bk = kt; }
+            }
+            set_kty(bk);
+            float bestp = best;
+            int bo = 0;
+            for (int order = 1; order < 4; order++) {
+                FftPlan cand = make_fft_plan(kp.nj, order);
+                if (!cand.nfac) continue;
+                const FftPlan keep = plan_j;
+                plan_j = cand;
+                const float t = timeit([&] { solve_pressure(1. / 3.); });
+                if (t < bestp) { bestp = t; bo = order; }
+                plan_j = keep;
+            }
+            plan_order_j = bo;
+            plan_j = make_fft_plan(kp.nj, bo);
+            std::snprintf(line, sizeof line, "y level tile %d, y FFT order %d; ", bk, bo);
+            info += line;
+            // x transforms: factor order (and the level tile of the unfused path)
+            float bx = bestp;
+            int bxo = 0;
+            for (int order = 1; order < 4; order++) {
+                FftPlan cand = make_fft_plan(kp.ni, order);
+                if (!cand.nfac) continue;
+                const FftPlan keep = plan_i;
+                plan_i = cand;
+                const float t = timeit([&] { solve_pressure(1. / 3.); });
+                if (t < bx) { bx = t; bxo = order; }
+                plan_i = keep;
+            }
+            plan_order_i = bxo;
+            plan_i = make_fft_plan(kp.ni, bxo);
+            if (psx == 0) {
+                int bkx = KTx;
+                for (int kt = 1; kt <= 64 && kt <= 2 * (NZ - 2); kt <<= 1) {
+                    if (2 * (size_t)kp.ni * kt * sizeof(T2) > 200 * 1024) break;
+                    const int keep = KTx;
+                    KTx = kt;
+                    smem_x = 2 * (size_t)kp.ni * KTx * sizeof(T2);
+                    const float t = timeit([&] { solve_pressure(1. / 3.); });
+                    if (t < bx) { bx = t; bkx = kt; }
+                    KTx = keep;
+                }
+                KTx = bkx;
+                lgKTx = 0;
+                while ((1 << lgKTx) < KTx) lgKTx++;
+                smem_x = 2 * (size_t)kp.ni * KTx * sizeof(T2);
+                std::snprintf(line, sizeof line, "x level tile %d, ", KTx);
+                info += line;
+            }
+            std::snprintf(line, sizeof line, "x FFT order %d (pressure solve %.4f ms)", bxo, bx);
+            info += line;
+        }
+        for (int f = 0; f < nprog; f++)
+            cudaMemcpyAsync(buf[f][pi_[f]], snap + (size_t)f * N, N * sizeof(T), cudaMemcpyDeviceToDevice, stream);
+        cudaMemcpyAsync(pi, snap + (size_t)nprog * N, N * sizeof(T), cudaMemcpyDeviceToDevice, stream);
+        cudaMemcpyAsync(vt, snap + (size_t)(nprog + 1) * N, N * sizeof(T), cudaMemcpyDeviceToDevice, stream);
+        const int rc = sync_status();
+        cudaEventDestroy(ea);
+        cudaEventDestroy(eb);
+        cudaFree(snap);
+        launches = l0;
+        drop_graphs();
+        tuning = info;
+        return rc;
     }
 
     // CUDA graph of two steps: the rotation of the three buffers has period

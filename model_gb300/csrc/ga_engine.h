@@ -40,6 +40,9 @@ struct EngineBase {
     virtual int lin_get_field(int field, int slot, double *host, size_t n) = 0;
     virtual int tlm_step(int nsteps) = 0;
     virtual int adjoint(int nsteps, int checkpoint_every) = 0;
+    // autotuner: times the candidate tile shapes and FFT plans, keeps the fastest
+    virtual int tune() = 0;
+    std::string tuning;  // the choice, as text
     cudaStream_t stream = nullptr;
     long long launches = 0;
     long long bigcounter = 0;

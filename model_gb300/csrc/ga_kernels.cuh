@@ -692,11 +692,11 @@ __device__ __forceinline__ void faces_top(const KParams<T> &p, const KFields<T> 
     }
 }
 
-template <typename T>
+template <typename T, int TI = ADV_TI, int TJ = ADV_TJ>
 __device__ void advect_tile_body(const KParams<T> &p, const KFields<T> &F, int bx, int by, T step, T sdtg, int what)
 {
     extern __shared__ unsigned char smem_raw[];
-    const int TI = ADV_TI, TJ = ADV_TJ, NF = ADV_NF;
+    const int NF = ADV_NF;
     const int nz = p.nz, nzi = nz - 2;
     const int i0 = 3 + bx * TI, j0 = 3 + by * TJ;
     const int ti = min(TI, p.nx - 3 - i0), tj = min(TJ, p.ny - 3 - j0);
@@ -813,10 +813,16 @@ __device__ void advect_tile_body(const KParams<T> &p, const KFields<T> &F, int b
     }
 }
 
-template <typename T>
+template <typename T, int TI = ADV_TI, int TJ = ADV_TJ>
 __global__ void __launch_bounds__(256) k_advect_tile(KParams<T> p, KFields<T> F, T step, T sdtg, int what)
 {
-    advect_tile_body(p, F, blockIdx.x, blockIdx.y, step, sdtg, what);
+    advect_tile_body<T, TI, TJ>(p, F, blockIdx.x, blockIdx.y, step, sdtg, what);
+}
+
+// shared memory of an advection tile: the face stores of every flux field
+__host__ __device__ constexpr size_t advect_tile_smem(int ti, int tj, int nz, size_t tsize)
+{
+    return (size_t)ADV_NF * ((ti + 1) * tj + ti * (tj + 1) + ti * tj) * nz * tsize;
 }
 
 // ---------------------------------------------------------------------------

@@ -129,3 +129,26 @@ def test_step_is_deterministic():
         outs.append([m.get(f) for f in range(7)] + [m.get(abi.GA_ACCRAIN)])
     for x, y in zip(*outs):
         np.testing.assert_array_equal(x, y)
+
+
+@pytest.mark.gpu
+def test_autotuner_keeps_state_and_results(_built):
+    """ga_tune leaves the state untouched; a tuned context steps to the same
+    result (bit-identical tiles; FFT factor orders agree to rounding)."""
+    from model_gb300 import configs
+    wl = configs.moist_blob(nx=30, ny=26, nz=20)
+    a = anelastic.Model(wl, abi.GA_PREC_F64)
+    b = anelastic.Model(wl, abi.GA_PREC_F64)
+    a.step(3)
+    b.step(3)
+    before = b.state()
+    info = b.tune()
+    assert "advect tile" in info and "FFT order" in info
+    after = b.state()
+    for k in before:
+        assert np.array_equal(before[k], after[k]), k
+    a.step(4)
+    b.step(4)
+    sa, sb = a.state(), b.state()
+    for k in sa:
+        assert fx.rel_l2(sb[k], sa[k]) <= 1e-12, k
