@@ -263,6 +263,9 @@ def ensemble_bench(torch, device, steps, warmup, n_small=64, n_large=32):
     for m, (nx, ny, nz) in enumerate(layout):
         ens.load_member(m, configs.ensemble_member(m, nx, ny, nz).fields)
     setup = time.perf_counter() - t0
+    t1 = time.perf_counter()
+    tuning = ens.tune()
+    t_tune = time.perf_counter() - t1
     ens.step(max(2, warmup))
     ext = torch.cuda.ExternalStream(ens.stream_handle())
     l0 = ens.launch_count()
@@ -279,6 +282,7 @@ def ensemble_bench(torch, device, steps, warmup, n_small=64, n_large=32):
            "layout": f"{n_small} x 96x96x40 + {n_large} x 160x160x48", "points": pts, "steps": steps,
            "ms_per_step": round(ms / steps, 4), "launches_per_step": (ens.launch_count() - l0) / steps,
            "setup_s": round(setup, 1), "precision": "fp32",
+           "tuning": {"choice": tuning, "seconds": round(t_tune, 2)},
            "note": "one launch per kernel phase over all members; two-step CUDA graph"}
     ens.close()
     return out

@@ -281,6 +281,9 @@ GA_API int ga_ensemble_synchronize(ga_ens *ens);
 GA_API void *ga_ensemble_stream(ga_ens *ens);
 GA_API long long ga_ensemble_launch_count(ga_ens *ens);
 GA_API int ga_ensemble_get_counters(ga_ens *ens, int member, long long *bigcounter, double *mtime);
+/* Autotuner of the batched step (advection tile, y level tile), as ga_tune. */
+GA_API int ga_ensemble_tune(ga_ens *ens);
+GA_API int ga_ensemble_tuning(ga_ens *ens, char *buf, size_t n);
 
 /*
  * Pressure solve without device allocation.  No counterpart in the reference:

@@ -59,6 +59,8 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     L.ga_stream.restype = C.c_void_p
     L.ga_field_device_ptr.argtypes = [C.c_void_p, C.c_int, C.c_int]
     L.ga_field_device_ptr.restype = C.c_void_p
+    L.ga_ensemble_tune.argtypes = [C.c_void_p]
+    L.ga_ensemble_tuning.argtypes = [C.c_void_p, C.c_char_p, C.c_size_t]
     L.ga_tune.argtypes = [C.c_void_p]
     L.ga_tuning.argtypes = [C.c_void_p, C.c_char_p, C.c_size_t]
     L.ga_lin_set_field.argtypes = [C.c_void_p, C.c_int, C.c_int, _DP, C.c_size_t]
@@ -377,6 +379,17 @@ class Ensemble:
 
     def launch_count(self) -> int:
         return self.L.ga_ensemble_launch_count(self.h)
+
+    def tune(self) -> str:
+        """Time the batched kernels' tile candidates over all members, keep the fastest."""
+        rc = self.L.ga_ensemble_tune(self.h)
+        if rc:
+            raise GaError(rc, "ga_ensemble_tune")
+        buf = C.create_string_buffer(512)
+        rc = self.L.ga_ensemble_tuning(self.h, buf, 512)
+        if rc:
+            raise GaError(rc, "ga_ensemble_tuning")
+        return buf.value.decode()
 
     def counters(self, member: int):
         bc, mt = C.c_longlong(), C.c_double()

@@ -220,6 +220,22 @@ int ga_check_finite(ga_ctx *ctx)
 
 long long ga_launch_count(ga_ctx *ctx) { return ctx ? ctx->e->launches : -1; }
 
+int ga_ensemble_tune(ga_ens *ens)
+{
+    if (!ens) return fail(GA_ERR_ARG, "ga_ensemble_tune: null ensemble");
+    return ens->e->tune();
+}
+
+int ga_ensemble_tuning(ga_ens *ens, char *buf, size_t n)
+{
+    if (!ens || !buf || n == 0) return fail(GA_ERR_ARG, "ga_ensemble_tuning: bad arguments");
+    const std::string t = ens->e->tuning.empty() ? std::string("defaults (not tuned)") : ens->e->tuning;
+    const size_t m = std::min(n - 1, t.size());
+    std::memcpy(buf, t.data(), m);
+    buf[m] = 0;
+    return GA_OK;
+}
+
 int ga_tune(ga_ctx *ctx)
 {
     if (!ctx) return fail(GA_ERR_ARG, "ga_tune: null context");

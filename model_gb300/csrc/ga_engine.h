@@ -111,6 +111,8 @@ struct EnsembleBase {
     virtual int size() const = 0;
     virtual void *stream_handle() = 0;
     virtual void mark_dirty() = 0;
+    virtual int tune() = 0;
+    std::string tuning;
     long long launches = 0;
 };
 

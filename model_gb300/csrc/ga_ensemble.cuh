@@ -40,7 +40,7 @@ __device__ __forceinline__ int find_member(const long *pre, int nmem, long vb)
     return lo;
 }
 
-template <typename T>
+template <typename T, int TI, int TJ>
 __global__ void __launch_bounds__(256) kb_advect(const KParams<T> *P, const KFields<T> *F, const long *pre, int nmem,
                                                  double step, int what)
 {
@@ -49,9 +49,9 @@ __global__ void __launch_bounds__(256) kb_advect(const KParams<T> *P, const KFie
         const int m = find_member(pre, nmem, vb);
         const KParams<T> &p = P[m];
         const long lb = vb - pre[m];
-        const int gx = (p.nx - 6 + ADV_TI - 1) / ADV_TI;
+        const int gx = (p.nx - 6 + TI - 1) / TI;
         const double sdtg = step * p.dt_d * 9.8 * 0.5;  // step*dt*grav*0.5, advection.cpp:330
-        advect_tile_body(p, F[m], (int)(lb % gx), (int)(lb / gx), (T)step, (T)sdtg, what);
+        advect_tile_body<T, TI, TJ>(p, F[m], (int)(lb % gx), (int)(lb / gx), (T)step, (T)sdtg, what);
         __syncthreads();
     }
 }
@@ -155,6 +155,8 @@ class Ensemble : public EnsembleBase {
     long long graph_launches[2] = {0, 0};
     bool moist = false;
     int dev = 0;
+    int adv_ti = ADV_TI, adv_tj = ADV_TJ;  // advection tile of every member (autotuned)
+    int nsm = 0;
 
     Ensemble(const ga_config *cfgs, const ga_columns *cols, int n, int *rc)
     {
@@ -185,8 +187,62 @@ class Ensemble : public EnsembleBase {
         cudaMalloc(&d_aux, sizeof(MemberAux<T>) * n);
         cudaMalloc(&d_err, sizeof(int));
         cudaMemset(d_err, 0, sizeof(int));
-        // virtual-block prefixes per kernel phase
-        std::vector<long> cnt(n);
+        const int optin = 200 * 1024;
+        cudaFuncSetAttribute(kb_advect<T, 4, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+        cudaFuncSetAttribute(kb_advect<T, 2, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+        cudaFuncSetAttribute(kb_advect<T, 4, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+        cudaFuncSetAttribute(kb_advect<T, 4, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+        cudaFuncSetAttribute(kb_advect<T, 8, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+        cudaFuncSetAttribute(kb_div_fft_y<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+        cudaFuncSetAttribute(kb_spectral_x<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+        cudaFuncSetAttribute(kb_ifft_y_pi<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        build_prefixes();
+        if (cudaDeviceSynchronize() != cudaSuccess) *rc = GA_ERR_CUDA;
+    }
+
+    ~Ensemble() override
+    {
+        cudaSetDevice(dev);
+        if (stream) cudaStreamSynchronize(stream);
+        for (auto &g : graph)
+            if (g) cudaGraphExecDestroy(g);
+        for (auto *e : mem) delete e;
+        cudaFree(d_p);
+        cudaFree(d_f[0]);
+        cudaFree(d_f[1]);
+        cudaFree(d_aux);
+        cudaFree(d_err);
+        for (auto *p : d_pre) cudaFree(p);
+        if (stream) cudaStreamDestroy(stream);
+    }
+
+    const void *advect_fn() const
+    {
+        if (adv_ti == 2) return (const void *)kb_advect<T, 2, 4>;
+        if (adv_tj == 2) return (const void *)kb_advect<T, 4, 2>;
+        if (adv_tj == 8) return (const void *)kb_advect<T, 4, 8>;
+        if (adv_ti == 8) return (const void *)kb_advect<T, 8, 4>;
+        return (const void *)kb_advect<T, 4, 4>;
+    }
+    void launch_advect(const KFields<T> *F, double st, int what)
+    {
+        const dim3 g(grid[EK_ADV]);
+        const size_t sm = smem[EK_ADV];
+        const long *pr = d_pre[EK_ADV];
+        if (adv_ti == 2) kb_advect<T, 2, 4><<<g, 256, sm, stream>>>(d_p, F, pr, nmem, st, what);
+        else if (adv_tj == 2) kb_advect<T, 4, 2><<<g, 256, sm, stream>>>(d_p, F, pr, nmem, st, what);
+        else if (adv_tj == 8) kb_advect<T, 4, 8><<<g, 256, sm, stream>>>(d_p, F, pr, nmem, st, what);
+        else if (adv_ti == 8) kb_advect<T, 8, 4><<<g, 256, sm, stream>>>(d_p, F, pr, nmem, st, what);
+        else kb_advect<T, 4, 4><<<g, 256, sm, stream>>>(d_p, F, pr, nmem, st, what);
+    }
+
+    // virtual-block prefixes per kernel phase (for the current advection tile
+    // and level tiles) and the persistent grid of each phase: as many blocks
+    // as stay resident
+    void build_prefixes()
+    {
+        const int n = nmem;
         for (int k = 0; k < EK_COUNT; k++) {
             std::vector<long> pre(n + 1, 0);
             size_t sm = 0;
@@ -195,8 +251,8 @@ class Ensemble : public EnsembleBase {
                 long c = 0;
                 switch (k) {
                 case EK_ADV:
-                    c = (long)cdiv(e.NX - 6, ADV_TI) * cdiv(e.NY - 6, ADV_TJ);
-                    sm = std::max(sm, e.smem_adv);
+                    c = (long)cdiv(e.NX - 6, adv_ti) * cdiv(e.NY - 6, adv_tj);
+                    sm = std::max(sm, advect_tile_smem(adv_ti, adv_tj, e.NZ, sizeof(T)));
                     break;
                 case EK_MIRROR: c = cdiv(2L * (e.NX + e.NY - 2) * (e.NZ - 2), 256); break;
                 case EK_DIVY:
@@ -215,23 +271,15 @@ class Ensemble : public EnsembleBase {
             }
             total[k] = pre[n];
             smem[k] = sm;
-            cudaMalloc(&d_pre[k], sizeof(long) * (n + 1));
+            if (!d_pre[k]) cudaMalloc(&d_pre[k], sizeof(long) * (n + 1));
             cudaMemcpy(d_pre[k], pre.data(), sizeof(long) * (n + 1), cudaMemcpyHostToDevice);
         }
-        const int optin = 200 * 1024;
-        cudaFuncSetAttribute(kb_advect<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
-        cudaFuncSetAttribute(kb_div_fft_y<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
-        cudaFuncSetAttribute(kb_spectral_x<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
-        cudaFuncSetAttribute(kb_ifft_y_pi<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
-        // persistent grids: as many blocks as stay resident
-        int nsm = 0;
-        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
         auto occ = [&](const void *fn, int threads, size_t sm) {
             int b = 0;
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, fn, threads, sm);
             return std::max(1, b) * nsm;
         };
-        grid[EK_ADV] = occ((const void *)kb_advect<T>, 256, smem[EK_ADV]);
+        grid[EK_ADV] = occ(advect_fn(), 256, smem[EK_ADV]);
         grid[EK_MIRROR] = occ((const void *)kb_mirror<T>, 256, 0);
         grid[EK_DIVY] = occ((const void *)kb_div_fft_y<T>, 256, smem[EK_DIVY]);
         grid[EK_SX] = occ((const void *)kb_spectral_x<T>, 256, smem[EK_SX]);
@@ -239,23 +287,135 @@ class Ensemble : public EnsembleBase {
         grid[EK_POST] = occ((const void *)kb_post<T>, POST_THREADS, 0);
         grid[EK_KES] = occ((const void *)kb_kessler<T>, 128, 0);
         for (int k = 0; k < EK_COUNT; k++) grid[k] = (int)std::min<long>(grid[k], std::max(1L, total[k]));
-        if (cudaDeviceSynchronize() != cudaSuccess) *rc = GA_ERR_CUDA;
     }
 
-    ~Ensemble() override
+    // Autotuner of the batched step: the advection tile and the level tile of
+    // the y transforms (one for every member), timed over all members on
+    // their current state; P, the fall speed and pi of every member are
+    // restored afterwards.  Results are bit-identical for every choice.
+    int tune() override
     {
         cudaSetDevice(dev);
-        if (stream) cudaStreamSynchronize(stream);
+        refresh_tables();
+        const int nf = (moist ? 7 : 4) + 2;
+        size_t tot = 0;
+        for (auto *e : mem) tot += (size_t)nf * e->N;
+        T *snap = nullptr;
+        if (cudaMalloc(&snap, tot * sizeof(T)) != cudaSuccess) return GA_ERR_NOMEM;
+        auto copy_all = [&](bool save) {
+            size_t o = 0;
+            for (auto *e : mem) {
+                T *ptr[9];
+                int np = 0;
+                for (int f = 0; f < nf - 2; f++) ptr[np++] = e->buf[f][e->pi_[f]];
+                ptr[np++] = e->pi;
+                ptr[np++] = e->vt;
+                for (int q = 0; q < np; q++, o += e->N) {
+                    if (save) cudaMemcpyAsync(snap + o, ptr[q], e->N * sizeof(T), cudaMemcpyDeviceToDevice, stream);
+                    else cudaMemcpyAsync(ptr[q], snap + o, e->N * sizeof(T), cudaMemcpyDeviceToDevice, stream);
+                }
+            }
+        };
+        copy_all(true);
+        cudaEvent_t ea, eb;
+        cudaEventCreate(&ea);
+        cudaEventCreate(&eb);
+        const long long l0 = launches;
+        auto timeit = [&](auto fn) {
+            fn();
+            cudaEventRecord(ea, stream);
+            for (int r = 0; r < 3; r++) fn();
+            cudaEventRecord(eb, stream);
+            cudaEventSynchronize(eb);
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, ea, eb);
+            return cudaGetLastError() == cudaSuccess ? ms / 3.f : 1e30f;
+        };
+        const int what = ADV_UV | ADV_WB | ADV_TH | (moist ? (ADV_Q | ADV_ZERO) : 0);
+        const KFields<T> *F = d_f[rot];
+        std::string info;
+        char line[160];
+        {
+            float best = 1e30f;
+            int bi = adv_ti, bj = adv_tj;
+            for (auto &tl : Engine<T>::kAdvTiles) {
+                bool fits = true;
+                for (auto *e : mem) fits = fits && advect_tile_smem(tl[0], tl[1], e->NZ, sizeof(T)) <= 200 * 1024;
+                if (!fits) continue;
+                adv_ti = tl[0];
+                adv_tj = tl[1];
+                build_prefixes();
+                const float t = timeit([&] { launch_advect(F, 1. / 3., what); });
+                if (t < best) { best = t; bi = tl[0]; bj = tl[1]; }
+            }
+            adv_ti = bi;
+            adv_tj = bj;
+            std::snprintf(line, sizeof line, "advect tile %dx%d (%.3f ms); ", bi, bj, best);
+            info += line;
+        }
+        {
+            std::vector<int> keep(nmem);
+            for (int m = 0; m < nmem; m++) keep[m] = mem[m]->KTy;
+            auto set_kty = [&](int kt) {
+                for (auto *e : mem) {
+                    e->KTy = kt;
+                    e->smem_y = 2 * (size_t)e->kp.nj * kt * sizeof(T2);
+                }
+                tables_dirty = true;
+                refresh_tables();
+                build_prefixes();
+            };
+            auto chain = [&] {
+                const KFields<T> *G = d_f[rot];
+                kb_mirror<T><<<grid[EK_MIRROR], 256, 0, stream>>>(d_p, G, d_pre[EK_MIRROR], nmem);
+                kb_div_fft_y<T><<<grid[EK_DIVY], dim3(16, 16), smem[EK_DIVY], stream>>>(d_p, G, d_aux,
+                                                                                       d_pre[EK_DIVY], nmem, 1. / 3.);
+                kb_spectral_x<T><<<grid[EK_SX], dim3(64, 4), smem[EK_SX], stream>>>(d_p, d_aux, d_pre[EK_SX], nmem);
+                kb_ifft_y_pi<T><<<grid[EK_IFFTY], dim3(16, 16), smem[EK_IFFTY], stream>>>(d_p, G, d_aux,
+                                                                                         d_pre[EK_IFFTY], nmem);
+            };
+            float best = 1e30f;
+            int bk = -1;
+            for (int kt = 1; kt <= 64; kt <<= 1) {
+                bool fits = true;
+                for (auto *e : mem)
+                    fits = fits && kt <= 2 * (e->NZ - 2) && 2 * (size_t)e->kp.nj * kt * sizeof(T2) <= 200 * 1024;
+                if (!fits) break;
+                set_kty(kt);
+                const float t = timeit(chain);
+                if (t < best) { best = t; bk = kt; }
+            }
+            if (bk > 0) {
+                set_kty(bk);
+            } else {
+                for (int m = 0; m < nmem; m++) {
+                    mem[m]->KTy = keep[m];
+                    mem[m]->smem_y = 2 * (size_t)mem[m]->kp.nj * keep[m] * sizeof(T2);
+                }
+                tables_dirty = true;
+                refresh_tables();
+                build_prefixes();
+            }
+            std::snprintf(line, sizeof line, "y level tile %d (pressure solve %.3f ms)", bk, best);
+            info += line;
+        }
+        copy_all(false);
+        cudaError_t e = cudaStreamSynchronize(stream);
+        cudaEventDestroy(ea);
+        cudaEventDestroy(eb);
+        cudaFree(snap);
+        launches = l0;
         for (auto &g : graph)
-            if (g) cudaGraphExecDestroy(g);
-        for (auto *e : mem) delete e;
-        cudaFree(d_p);
-        cudaFree(d_f[0]);
-        cudaFree(d_f[1]);
-        cudaFree(d_aux);
-        cudaFree(d_err);
-        for (auto *p : d_pre) cudaFree(p);
-        if (stream) cudaStreamDestroy(stream);
+            if (g) {
+                cudaGraphExecDestroy(g);
+                g = nullptr;
+            }
+        tuning = info;
+        if (e != cudaSuccess) {
+            set_error(std::string("CUDA: ") + cudaGetErrorString(e));
+            return GA_ERR_CUDA;
+        }
+        return GA_OK;
     }
 
     // member tables: parameters (after basic-state refresh) and both rotation states
@@ -309,7 +469,7 @@ class Ensemble : public EnsembleBase {
             const double st = steps[s];
             KFields<T> *F = d_f[rot];
             const int what = ADV_UV | ADV_WB | ADV_TH | (moist ? (ADV_Q | ADV_ZERO) : 0);
-            kb_advect<T><<<grid[EK_ADV], 256, smem[EK_ADV], stream>>>(d_p, F, d_pre[EK_ADV], nmem, st, what);
+            launch_advect(F, st, what);
             kb_mirror<T><<<grid[EK_MIRROR], 256, 0, stream>>>(d_p, F, d_pre[EK_MIRROR], nmem);
             kb_div_fft_y<T><<<grid[EK_DIVY], dim3(16, 16), smem[EK_DIVY], stream>>>(d_p, F, d_aux, d_pre[EK_DIVY],
                                                                                    nmem, st);

@@ -9,8 +9,10 @@ from model_gb300 import abi, anelastic, configs
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("precision", [abi.GA_PREC_F64, abi.GA_PREC_F32])
-def test_ensemble_members_equal_standalone_runs(precision):
+@pytest.mark.parametrize("precision,tune", [(abi.GA_PREC_F64, False), (abi.GA_PREC_F32, False),
+                                            (abi.GA_PREC_F32, True)])
+def test_ensemble_members_equal_standalone_runs(precision, tune):
+    """tune: the autotuner runs mid-run; tiles change nothing bit for bit."""
     members = [configs.moist_blob(nx=24, ny=22, nz=16, seed=3000),
                configs.moist_blob(nx=36, ny=30, nz=20, seed=3100, qc=2e-3),
                configs.moist_blob(nx=40, ny=24, nz=12, seed=3200, dt=3.0)]
@@ -18,7 +20,12 @@ def test_ensemble_members_equal_standalone_runs(precision):
     for m, wl in enumerate(members):
         ens.load_member(m, wl.fields)
     nsteps = 5
-    ens.step(nsteps)
+    if tune:
+        ens.step(2)
+        assert "advect tile" in ens.tune()
+        ens.step(nsteps - 2)
+    else:
+        ens.step(nsteps)
     for m, wl in enumerate(members):
         solo = anelastic.Model(wl, precision)
         solo.step(nsteps)
