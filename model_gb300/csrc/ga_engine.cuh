@@ -517,7 +517,7 @@ class Engine : public EngineBase {
             const long ncol = (long)kp.ni * kp.nj;
             {
                 ProfScope ps(this, PC_THOMAS, 1);
-                k_thomas<T><<<cdiv(ncol, TC), TC, smem_th, stream>>>(kp, spec, TC);
+                k_thomas<T><<<cdiv(ncol, TC), 256, smem_th, stream>>>(kp, spec, TC);  // 256 threads stage, TC solve
             }
             {
                 ProfScope ps(this, PC_FFT_X, 1);

@@ -220,7 +220,7 @@ struct Lin : LinBase {
         } else {
             k_fft_x<T><<<dim3(e.kp.nj, nkt_x), by_x, e.smem_x, s>>>(e.kp, e.spec, e.plan_i, e.tw_i, 0, e.KTx);
             const long ncol = (long)e.kp.ni * e.kp.nj;
-            k_thomas_adj<T><<<cdiv(ncol, e.TC), e.TC, e.smem_th, s>>>(e.kp, e.spec, e.TC);
+            k_thomas_adj<T><<<cdiv(ncol, e.TC), 256, e.smem_th, s>>>(e.kp, e.spec, e.TC);
             k_fft_x<T><<<dim3(e.kp.nj, nkt_x), by_x, e.smem_x, s>>>(e.kp, e.spec, e.plan_i, e.tw_i, 1, e.KTx);
             e.launches += 3;
         }
