@@ -1590,10 +1590,204 @@ __global__ void __launch_bounds__(POST_THREADS) k_post(KParams<T> p, KFields<T> 
 }
 
 // ---------------------------------------------------------------------------
-// Kessler warm rain, pointwise (kessler.cpp:25-183); the k=1 thread of each
-// column then adds the Eulerian precipitation (precip_rate,
-// microphysics.cpp:143-160) when rain_fallout == 1.
+// Kessler warm rain, pointwise (kessler.cpp:25-183).  kessler_point is written
+// once for a scalar type S: the real type T (the step) or Dual<T,N> (the
+// linearisation, which differentiates exactly this arithmetic with the branch
+// decisions of the trajectory).  The k=1 thread of each column then adds the
+// Eulerian precipitation (precip_rate, microphysics.cpp:143-160) when
+// rain_fallout == 1.
 // ---------------------------------------------------------------------------
+template <typename T, int N>
+struct Dual {
+    T v, d[N];
+};
+template <typename T> __device__ __forceinline__ T val(T x) { return x; }
+template <typename T, int N> __device__ __forceinline__ T val(const Dual<T, N> &x) { return x.v; }
+
+#define DUAL_T template <typename T, int N> __device__ __forceinline__ Dual<T, N>
+DUAL_T operator+(const Dual<T, N> &a, const Dual<T, N> &b)
+{
+    Dual<T, N> r;
+    r.v = a.v + b.v;
+    for (int q = 0; q < N; q++) r.d[q] = a.d[q] + b.d[q];
+    return r;
+}
+DUAL_T operator-(const Dual<T, N> &a, const Dual<T, N> &b)
+{
+    Dual<T, N> r;
+    r.v = a.v - b.v;
+    for (int q = 0; q < N; q++) r.d[q] = a.d[q] - b.d[q];
+    return r;
+}
+DUAL_T operator*(const Dual<T, N> &a, const Dual<T, N> &b)
+{
+    Dual<T, N> r;
+    r.v = a.v * b.v;
+    for (int q = 0; q < N; q++) r.d[q] = a.d[q] * b.v + a.v * b.d[q];
+    return r;
+}
+DUAL_T operator/(const Dual<T, N> &a, const Dual<T, N> &b)
+{
+    Dual<T, N> r;
+    r.v = a.v / b.v;
+    for (int q = 0; q < N; q++) r.d[q] = (a.d[q] - r.v * b.d[q]) / b.v;
+    return r;
+}
+DUAL_T operator+(const Dual<T, N> &a, T b)
+{
+    Dual<T, N> r = a;
+    r.v = a.v + b;
+    return r;
+}
+DUAL_T operator+(T a, const Dual<T, N> &b) { return b + a; }
+DUAL_T operator-(const Dual<T, N> &a, T b)
+{
+    Dual<T, N> r = a;
+    r.v = a.v - b;
+    return r;
+}
+DUAL_T operator-(T a, const Dual<T, N> &b)
+{
+    Dual<T, N> r;
+    r.v = a - b.v;
+    for (int q = 0; q < N; q++) r.d[q] = -b.d[q];
+    return r;
+}
+DUAL_T operator*(const Dual<T, N> &a, T b)
+{
+    Dual<T, N> r;
+    r.v = a.v * b;
+    for (int q = 0; q < N; q++) r.d[q] = a.d[q] * b;
+    return r;
+}
+DUAL_T operator*(T a, const Dual<T, N> &b) { return b * a; }
+DUAL_T operator/(const Dual<T, N> &a, T b)
+{
+    Dual<T, N> r;
+    r.v = a.v / b;
+    for (int q = 0; q < N; q++) r.d[q] = a.d[q] / b;
+    return r;
+}
+DUAL_T operator/(T a, const Dual<T, N> &b)
+{
+    Dual<T, N> r;
+    r.v = a / b.v;
+    for (int q = 0; q < N; q++) r.d[q] = -r.v * b.d[q] / b.v;
+    return r;
+}
+DUAL_T kpow(const Dual<T, N> &x, T e)  // x > 0 wherever it is used
+{
+    Dual<T, N> r;
+    r.v = pow(x.v, e);
+    const T g = e * r.v / x.v;
+    for (int q = 0; q < N; q++) r.d[q] = g * x.d[q];
+    return r;
+}
+DUAL_T kexp(const Dual<T, N> &x)
+{
+    Dual<T, N> r;
+    r.v = exp(x.v);
+    for (int q = 0; q < N; q++) r.d[q] = r.v * x.d[q];
+    return r;
+}
+DUAL_T kmin(const Dual<T, N> &a, const Dual<T, N> &b) { return b.v < a.v ? b : a; }
+DUAL_T kmax(const Dual<T, N> &a, const Dual<T, N> &b) { return b.v > a.v ? b : a; }
+DUAL_T kneg(const Dual<T, N> &a)
+{
+    Dual<T, N> r;
+    r.v = -a.v;
+    for (int q = 0; q < N; q++) r.d[q] = -a.d[q];
+    return r;
+}
+DUAL_T kconst(T c)
+{
+    Dual<T, N> r;
+    r.v = c;
+    for (int q = 0; q < N; q++) r.d[q] = T(0);
+    return r;
+}
+#undef DUAL_T
+template <typename T> __device__ __forceinline__ T kpow(T x, T e) { return pow(x, e); }
+template <typename T> __device__ __forceinline__ T kexp(T x) { return exp(x); }
+template <typename T> __device__ __forceinline__ T kmin(T a, T b) { return fmin(a, b); }
+template <typename T> __device__ __forceinline__ T kmax(T a, T b) { return fmax(a, b); }
+template <typename T> __device__ __forceinline__ T kneg(T a) { return -a; }
+
+// the column values Kessler reads at a point
+template <typename T>
+struct KesPoint {
+    T thbar, qbar, pbar, tb, qb, tbv, rhou, dt;
+};
+
+// run_kessler_microphysics at one point: (thp, qvp, qcp, qrp) updated in
+// place from themselves and pi.  Returns true where the reference exits
+// (evaporation E > 100, kessler.cpp:83-88).
+template <typename S, typename T>
+__device__ __forceinline__ bool kessler_point(S &thp, S &qvp, S &qcp, S &qrp, const S &pi, const KesPoint<T> &c)
+{
+    const T cp = T(1004), p0 = T(100000), Lv = T(2.5e6);
+    const T cpRd = T(1004.0 / 287.0);
+    const T dt = c.dt, rhou = c.rhou;
+    const S zero = thp - thp;  // 0 of the scalar type, derivative 0
+    S theta = thp + c.thbar + c.tb;
+    S pressure = pi / (cp * c.tbv) + c.pbar;
+    S vapor = qvp + c.qbar + c.qb;
+    S temperature = theta * pressure;
+    S pd = p0 * kpow(pressure, cpRd);
+    S A = zero, B = zero, E = zero, esl, qvsat;
+    bool bad = false;
+    if (val(qcp) > T(1.0e-3)) A = T(0.001) * (qcp - T(1.0e-3)) * dt;
+    if (val(qrp) > T(1.0e-12)) B = rhou * T(2.2) * qcp * kpow(qrp, T(0.875)) * dt;
+    if (val(qrp) > T(1.0e-12)) {
+        esl = T(611.2) * kexp(T(17.67) * (temperature - T(273.15)) / (temperature - T(29.65)));
+        qvsat = T(0.62197) * esl / (pd - esl);
+        S cvent = T(1.6) + T(30.3922) * kpow(rhou * qrp, T(0.2046));
+        E = (T(1.0) / rhou) *
+            (((T(1.0) - vapor / qvsat) * cvent * kpow(rhou * qrp, T(0.525))) / (T(2.03e4) + T(9.58e6) / (pd * qvsat))) *
+            dt;
+        E = kmin(qrp, E);
+        E = kmax(E, zero);
+        bad = val(E) > T(100);
+    }
+    qvp = qvp + E;
+    S total_convert = kmin(A + B, qcp);
+    qcp = qcp - total_convert;
+    qrp = qrp + (total_convert - E);
+    S de = (Lv / (cp * pressure)) * E;
+    thp = thp - de;
+    theta = thp + c.thbar + c.tb;
+    vapor = qvp + c.qbar + c.qb;
+    temperature = theta * pressure;
+    esl = T(611.2) * kexp(T(17.67) * (temperature - T(273.15)) / (temperature - T(29.65)));
+    qvsat = T(0.62197) * esl / (pd - esl);
+    const T fcoef = T(17.67 * (273.15 - 29.65) * 2.5e6 / 1004.0);
+    S tm = temperature - T(29.65);
+    S phi = pd / (pd - esl) * qvsat * fcoef / (tm * tm);
+    S C = zero;
+    if (val(vapor) > val(qvsat)) C = (vapor - qvsat) / (T(1.0) + phi);
+    else if (val(vapor) < val(qvsat) && val(qcp) > 0) C = kneg(kmin(qcp, (qvsat - vapor) / (T(1.0) + phi)));
+    qcp = qcp + C;
+    qvp = qvp - C;
+    S dc = (Lv / (cp * pressure)) * C;
+    thp = thp + dc;
+    return bad;
+}
+
+template <typename T>
+__device__ __forceinline__ KesPoint<T> kes_point(const KParams<T> &p, const KFields<T> &F, int k, long ix)
+{
+    KesPoint<T> c;
+    c.thbar = p.ubase_kes ? BTAB(BT_THB, k) : F.bar[3][ix];
+    c.qbar = p.ubase_kes ? BTAB(BT_QB, k) : F.bar[4][ix];
+    c.pbar = p.ubase_kes ? BTAB(BT_PB, k) : F.bar[5][ix];
+    c.tb = p.tb[k];
+    c.qb = p.qb[k];
+    c.tbv = p.tbv[k];
+    c.rhou = p.rhou[k];
+    c.dt = p.dt;
+    return c;
+}
+
 template <typename T>
 __device__ void kessler_body(const KParams<T> &p, const KFields<T> &F, int precip, int *err, long t)
 {
@@ -1603,64 +1797,16 @@ __device__ void kessler_body(const KParams<T> &p, const KFields<T> &F, int preci
     const int j = 1 + (int)((t / nzi) % nyi);
     const int i = 1 + (int)(t / ((long)nzi * nyi));
     const long ix = gix(p.ny, p.nz, i, j, k);
-    const T cp = T(1004), Rd = T(287.0), p0 = T(100000), Lv = T(2.5e6);
-    const T cpRd = T(1004.0 / 287.0);
-    const T dt = p.dt;
     T *THP = F.P[FTH], *QVP = F.P[FQV], *QCP = F.P[FQC], *QRP = F.P[FQR];
-    const T rhou = p.rhou[k];
     T thp = THP[ix], qvp = QVP[ix], qcp = QCP[ix], qrp = QRP[ix];
-    const T thbar = p.ubase_kes ? BTAB(BT_THB, k) : F.bar[3][ix];
-    const T qbar = p.ubase_kes ? BTAB(BT_QB, k) : F.bar[4][ix];
-    const T pbar = p.ubase_kes ? BTAB(BT_PB, k) : F.bar[5][ix];
-    T theta = thp + thbar + p.tb[k];
-    T pressure = F.pi[ix] / (cp * p.tbv[k]) + pbar;
-    T vapor = qvp + qbar + p.qb[k];
-    T temperature = theta * pressure;
-    T pd = p0 * pow(pressure, cpRd);
-    T A, B, E, esl, qvsat;
-    if (qcp > T(1.0e-3)) A = T(0.001) * (qcp - T(1.0e-3)) * dt;
-    else A = 0;
-    if (qrp > T(1.0e-12)) B = rhou * T(2.2) * qcp * pow(qrp, T(0.875)) * dt;
-    else B = 0;
-    if (qrp > T(1.0e-12)) {
-        esl = T(611.2) * exp(T(17.67) * (temperature - T(273.15)) / (temperature - T(29.65)));
-        qvsat = T(0.62197) * esl / (pd - esl);
-        T cvent = T(1.6) + T(30.3922) * pow(rhou * qrp, T(0.2046));
-        E = (T(1.0) / rhou) *
-            (((T(1.0) - vapor / qvsat) * cvent * pow(rhou * qrp, T(0.525))) / (T(2.03e4) + T(9.58e6) / (pd * qvsat))) *
-            dt;
-        E = fmin(qrp, E);
-        E = fmax(E, T(0.0));
-        if (E > T(100)) atomicExch(err, 1);
-    } else
-        E = 0;
-    qvp += E;
-    T total_convert = fmin(A + B, qcp);
-    qcp -= total_convert;
-    qrp += (total_convert - E);
-    T de = (Lv / (cp * pressure)) * E;
-    thp -= de;
-    theta = thp + thbar + p.tb[k];
-    vapor = qvp + qbar + p.qb[k];
-    temperature = theta * pressure;
-    esl = T(611.2) * exp(T(17.67) * (temperature - T(273.15)) / (temperature - T(29.65)));
-    qvsat = T(0.62197) * esl / (pd - esl);
-    const T fcoef = T(17.67 * (273.15 - 29.65) * 2.5e6 / 1004.0);
-    T tm = temperature - T(29.65);
-    T phi = pd / (pd - esl) * qvsat * fcoef / (tm * tm);
-    T C = T(0.0);
-    if (vapor > qvsat) C = (vapor - qvsat) / (T(1.0) + phi);
-    else if (vapor < qvsat && qcp > 0) C = -fmin(qcp, (qvsat - vapor) / (T(1.0) + phi));
-    qcp += C;
-    qvp -= C;
-    T dc = (Lv / (cp * pressure)) * C;
-    thp += dc;
+    const T piv = F.pi[ix];
+    if (kessler_point(thp, qvp, qcp, qrp, piv, kes_point(p, F, k, ix))) atomicExch(err, 1);
     THP[ix] = thp;
     QVP[ix] = qvp;
     QCP[ix] = qcp;
     QRP[ix] = qrp;
-    (void)Rd;
     if (precip && k == 1) {
+        const T dt = p.dt;
         const long i0 = ix - 1;
         const double inc = (double)(p.rhow[1] * T(0.5) * (F.vt[i0] + F.vt[ix]) * T(0.5) * (QRP[i0] + qrp) * dt);
         F.accrain[(long)i * p.ny + j] += inc;
