@@ -232,13 +232,16 @@ GA_API int ga_tuning(ga_ctx *ctx, char *buf, size_t n);
 /*
  * Tangent-linear model and adjoint of the step.  No counterpart in the
  * reference, which has no linearisation; this differentiates exactly the step
- * ga_step runs, for dry (microphysics_option 0), non-periodic contexts
- * (GA_ERR_UNSUPPORTED otherwise), in the context's precision.
+ * ga_step runs, for non-periodic contexts, dry or with Kessler microphysics
+ * and Eulerian rain fallout (rain_fallout 1); GA_ERR_UNSUPPORTED otherwise.
+ * Arithmetic is in the context's precision.
  *
  * The context holds one set of perturbation buffers shaped like the state:
- * current, P and M slots of GA_U, GA_V, GA_W, GA_TH, plus GA_PI (slot
- * ignored), rotating with the state.  Upwind signs are frozen at the
- * trajectory.
+ * current, P and M slots of the prognostic fields (GA_U .. GA_TH, and GA_QV ..
+ * GA_QR when moist), plus GA_PI (slot ignored), rotating with the state.
+ * Upwind signs, zero_moisture clipping and the branches of Kessler are
+ * frozen at the trajectory (recorded on the forward pass: clipping bits per
+ * point and stage, Kessler's inputs per step).
  *
  * ga_tlm_step advances the state and the perturbations together nsteps.
  *
@@ -249,8 +252,9 @@ GA_API int ga_tuning(ga_ctx *ctx, char *buf, size_t n);
  * `checkpoint_every` steps (<= 0: one segment) and each segment is recomputed,
  * recording the stage-start fields, before its adjoint runs: device memory
  * holds nsteps/checkpoint_every + 1 states and checkpoint_every steps of
- * trajectory (12 fields each).  The adjoint kernels are in gather form (no
- * atomics).  The GA_PI entry is zero on return: the step never reads pi.
+ * trajectory (12 fields a step dry, 26 fields + 3 clipping records moist).
+ * The adjoint kernels are in gather form (no atomics).  The GA_PI entry is
+ * zero on return: the step never reads pi.
  */
 GA_API int ga_lin_set_field(ga_ctx *ctx, int field, int slot, const double *host, size_t n);
 GA_API int ga_lin_get_field(ga_ctx *ctx, int field, int slot, double *host, size_t n);

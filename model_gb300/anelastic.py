@@ -282,8 +282,12 @@ class Model:
         for (f, s), v in d.items():
             self.lin_set(f, s, v)
 
+    def lin_fields(self):
+        """The linearised prognostic fields of this context."""
+        return tuple(range(7)) if self.wl.microphysics_option else self.LIN_FIELDS
+
     def lin_get_all(self) -> dict:
-        d = {(f, s): self.lin_get(f, s) for f in self.LIN_FIELDS for s in self.LIN_SLOTS}
+        d = {(f, s): self.lin_get(f, s) for f in self.lin_fields() for s in self.LIN_SLOTS}
         d[(abi.GA_PI, 0)] = self.lin_get(abi.GA_PI)
         return d
 

@@ -255,8 +255,8 @@ int ga_tuning(ga_ctx *ctx, char *buf, size_t n)
 int ga_lin_set_field(ga_ctx *ctx, int field, int slot, const double *host, size_t n)
 {
     if (!ctx || !host) return fail(GA_ERR_ARG, "ga_lin_set_field: null argument");
-    if (!((field >= GA_U && field <= GA_TH) || field == GA_PI))
-        return fail(GA_ERR_ARG, "ga_lin_set_field: field must be GA_U..GA_TH or GA_PI");
+    if (!((field >= GA_U && field <= GA_QR) || field == GA_PI))
+        return fail(GA_ERR_ARG, "ga_lin_set_field: field must be a prognostic field or GA_PI");
     int rc = ctx->e->lin_set_field(field, slot, host, n);
     if (rc == GA_ERR_ARG) set_error("ga_lin_set_field: bad slot or size");
     return rc;
@@ -265,8 +265,8 @@ int ga_lin_set_field(ga_ctx *ctx, int field, int slot, const double *host, size_
 int ga_lin_get_field(ga_ctx *ctx, int field, int slot, double *host, size_t n)
 {
     if (!ctx || !host) return fail(GA_ERR_ARG, "ga_lin_get_field: null argument");
-    if (!((field >= GA_U && field <= GA_TH) || field == GA_PI))
-        return fail(GA_ERR_ARG, "ga_lin_get_field: field must be GA_U..GA_TH or GA_PI");
+    if (!((field >= GA_U && field <= GA_QR) || field == GA_PI))
+        return fail(GA_ERR_ARG, "ga_lin_get_field: field must be a prognostic field or GA_PI");
     int rc = ctx->e->lin_get_field(field, slot, host, n);
     if (rc == GA_ERR_ARG) set_error("ga_lin_get_field: bad slot or size");
     return rc;

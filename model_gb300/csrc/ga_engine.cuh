@@ -94,6 +94,7 @@ class Engine : public EngineBase {
     int status = GA_OK;
     std::unique_ptr<LinBase> lin;  // tangent-linear / adjoint buffers, on first use
     int adv_ti = ADV_TI, adv_tj = ADV_TJ;  // advection tile (autotuned)
+    unsigned char *qmask = nullptr;         // clipping record of the next advection (linearisation)
     int plan_order_i = 0, plan_order_j = 0;
 
     Lin<T> *linear();
@@ -314,6 +315,7 @@ class Engine : public EngineBase {
         F.pi = pi;
         F.vt = vt;
         F.accrain = accrain;
+        F.qmask = qmask;
         return F;
     }
 
@@ -674,19 +676,24 @@ class Engine : public EngineBase {
     }
 
     // one RK3 step: s_integrate_rk3 (driver_serial.cpp:178-286), fused.
-    // rec (optional): the stage-start u, v, w, theta are copied to
-    // rec + (4*stage + field)*N, the trajectory of the adjoint.
-    void rk3_step(T *rec = nullptr)
+    // rec (optional), the trajectory of the adjoint: the stage-start
+    // prognostic fields go to rec + (nprog*stage + field)*N and, when moist,
+    // the inputs of Kessler (P of theta, qv, qc, qr, then pi) to
+    // rec + (3*nprog + q)*N, with each stage's clipping record in
+    // mrec + stage*N.
+    void rk3_step(T *rec = nullptr, unsigned char *mrec = nullptr)
     {
         static const double steps[3] = {1. / 3., 0.5, 1.0};
         const bool moist = kp.moist;
         for (int s = 0; s < 3; s++) {
             const double st = steps[s];
             if (rec)
-                for (int f = 0; f < 4; f++)
-                    cudaMemcpyAsync(rec + (size_t)(4 * s + f) * N, buf[f][ci[f]], N * sizeof(T),
+                for (int f = 0; f < nprog; f++)
+                    cudaMemcpyAsync(rec + (size_t)(nprog * s + f) * N, buf[f][ci[f]], N * sizeof(T),
                                     cudaMemcpyDeviceToDevice, stream);
+            qmask = mrec ? mrec + (size_t)s * N : nullptr;
             advect(st, ADV_UV | ADV_WB | ADV_TH | (moist ? (ADV_Q | ADV_ZERO) : 0));
+            qmask = nullptr;
             solve_pressure(st);
             int fl[7] = {0, 0, 0, 0, 0, 0, 0};
             fl[FU] = fl[FV] = fl[FW] = PF_PROJECT | PF_SPONGE | PF_VBC;
@@ -694,6 +701,13 @@ class Engine : public EngineBase {
             fl[FQV] = fl[FQC] = fl[FQR] = PF_ZERO | PF_SPONGE | PF_VBC;
             post(fl, 7, st, true);
             if (s < 2) swap_inner(true);
+        }
+        if (moist && rec) {
+            const int kin[4] = {FTH, FQV, FQC, FQR};
+            for (int q = 0; q < 4; q++)
+                cudaMemcpyAsync(rec + (size_t)(3 * nprog + q) * N, buf[kin[q]][pi_[kin[q]]], N * sizeof(T),
+                                cudaMemcpyDeviceToDevice, stream);
+            cudaMemcpyAsync(rec + (size_t)(3 * nprog + 4) * N, pi, N * sizeof(T), cudaMemcpyDeviceToDevice, stream);
         }
         if (moist) kessler();
         int fl[7] = {0, 0, 0, 0, 0, 0, 0};

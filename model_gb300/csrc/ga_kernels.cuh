@@ -70,6 +70,10 @@ struct KFields {
     const T *bar[6];
     T *pi, *vt;
     double *accrain;
+    // optional: per point of the advected cells, which moisture fields
+    // zero_moisture clipped (bit 0 qv, 1 qc, 2 qr) -- the branch record of
+    // the linearisation
+    unsigned char *qmask;
 };
 
 enum { FU = 0, FV, FW, FTH, FQV, FQC, FQR };
@@ -410,10 +414,12 @@ __global__ void __launch_bounds__(128) k_advect(KParams<T> p, KFields<T> F, T st
                    p.one_d_rhou[k];
         T qr = LD(F.M[FQR], c) + step * tr;
         if (what & ADV_ZERO) {  // zero_moisture on this point (microphysics.cpp:675-700)
-            if (qc < 0) qc = 0;
-            if (qr < 0) qr = 0;
+            unsigned char bits = 0;
+            if (qc < 0) { qc = 0; bits |= 2; }
+            if (qr < 0) { qr = 0; bits |= 4; }
             T qbar = LD(F.bar[4], c);
-            if (qv + qbar + p.qb[k] < 0) qv = -(qbar + p.qb[k]);
+            if (qv + qbar + p.qb[k] < 0) { qv = -(qbar + p.qb[k]); bits |= 1; }
+            if (F.qmask) F.qmask[c] = bits;
         }
         F.P[FQV][c] = qv;
         F.P[FQC][c] = qc;
@@ -801,10 +807,12 @@ __device__ void advect_tile_body(const KParams<T> &p, const KFields<T> &F, int b
             T qc = LD(F.M[FQC], cix) + step * tend(4);
             T qr = LD(F.M[FQR], cix) + step * tend(5);
             if (what & ADV_ZERO) {
-                if (qc < 0) qc = 0;
-                if (qr < 0) qr = 0;
+                unsigned char bits = 0;
+                if (qc < 0) { qc = 0; bits |= 2; }
+                if (qr < 0) { qr = 0; bits |= 4; }
                 T qbar = p.ubase_adv ? BTAB(BT_QB, k) : LD(F.bar[4], cix);
-                if (qv + qbar + p.qb[k] < 0) qv = -(qbar + p.qb[k]);
+                if (qv + qbar + p.qb[k] < 0) { qv = -(qbar + p.qb[k]); bits |= 1; }
+                if (F.qmask) F.qmask[cix] = bits;
             }
             F.P[FQV][cix] = qv;
             F.P[FQC][cix] = qc;

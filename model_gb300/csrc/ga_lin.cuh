@@ -16,11 +16,15 @@ struct Lin : LinBase {
     typedef typename V2<T>::t T2;
     Engine<T> &e;
     long N;
-    T *lb[4][3] = {};
-    int lci[4], lpi[4], lmi[4];
+    int nf;              // linearised prognostic fields: 4 dry, 7 moist
+    T *lb[7][3] = {};
+    int lci[7], lpi[7], lmi[7];
     T *lpi_f = nullptr;  // pi (perturbation or adjoint)
     T *dbar = nullptr;   // adjoint of the divergence, real [i][j][k]
-    T *coef = nullptr;   // linearised face coefficients of one stage (LIN_NCOEF fields)
+    T *coef = nullptr;   // linearised face coefficients of one stage (LIN_NCOEF[_MOIST] fields)
+    unsigned char *mask = nullptr;   // clipping record of the trajectory's current stage (TLM)
+    unsigned char *mtape = nullptr;  // clipping records of a segment: 3 stages x N per step (adjoint)
+    double *rain_keep = nullptr;     // accumulated rain of the final state, kept over the recomputation
     T *tape = nullptr;   // stage-start u, v, w, theta of every step of a segment
     size_t tape_steps = 0;
     T *ckpt = nullptr;   // full states (current, P, M of u, v, w, theta)
@@ -29,15 +33,19 @@ struct Lin : LinBase {
     std::vector<cudaGraphExec_t> rec_graph[2];
     std::vector<long long> rec_graph_launches[2];
 
-    explicit Lin(Engine<T> &eng) : e(eng), N(eng.N)
+    explicit Lin(Engine<T> &eng) : e(eng), N(eng.N), nf(eng.nprog)
     {
-        for (int f = 0; f < 4; f++) {
+        for (int f = 0; f < nf; f++) {
             for (int s = 0; s < 3; s++) lb[f][s] = e.template dalloc<T>(N);
             lci[f] = 0; lpi[f] = 1; lmi[f] = 2;
         }
         lpi_f = e.template dalloc<T>(N);
         dbar = e.template dalloc<T>(N);
-        coef = e.template dalloc<T>((size_t)LIN_NCOEF * N);
+        coef = e.template dalloc<T>((size_t)(nf == 7 ? LIN_NCOEF_MOIST : LIN_NCOEF) * N);
+        if (nf == 7) {
+            mask = e.template dalloc<unsigned char>(N);
+            rain_keep = e.template dalloc<double>((size_t)e.NX * e.NY);
+        }
         const int optin = 200 * 1024;
         cudaFuncSetAttribute(k_adj_fft_y_in<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
         cudaFuncSetAttribute(k_adj_ifft_y_out<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
@@ -49,8 +57,15 @@ struct Lin : LinBase {
     {
         drop_graphs();
         if (tape) cudaFree(tape);
+        if (mtape) cudaFree(mtape);
         if (ckpt) cudaFree(ckpt);
     }
+
+    // trajectory fields per step: stage-start prognostic fields, and (moist)
+    // the inputs of Kessler
+    size_t per_step() const { return (size_t)(3 * nf + (nf == 7 ? 5 : 0)) * N; }
+    T *rec_at(int slot) { return tape + (size_t)slot * per_step(); }
+    unsigned char *mrec_at(int slot) { return mtape ? mtape + (size_t)slot * 3 * N : nullptr; }
 
     void drop_graphs() override
     {
@@ -66,7 +81,6 @@ struct Lin : LinBase {
     // CUDA graph captured on first use (slots and parity fix every pointer)
     void record_pair(int m2)
     {
-        const size_t per = 12 * (size_t)N;
         const int par = e.ci[0] == 0 ? 0 : 1;
         const size_t idx = (size_t)m2 / 2;
         auto &gs = rec_graph[par];
@@ -81,8 +95,8 @@ struct Lin : LinBase {
             cudaGraph_t g = nullptr;
             bool ok = cudaStreamBeginCapture(e.stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
             if (ok) {
-                e.rk3_step(tape + (size_t)m2 * per);
-                e.rk3_step(tape + (size_t)(m2 + 1) * per);
+                e.rk3_step(rec_at(m2), mrec_at(m2));
+                e.rk3_step(rec_at(m2 + 1), mrec_at(m2 + 1));
                 ok = cudaStreamEndCapture(e.stream, &g) == cudaSuccess;
             }
             if (ok) ok = cudaGraphInstantiate(&gs[idx], g, 0) == cudaSuccess;
@@ -101,25 +115,24 @@ struct Lin : LinBase {
             e.bigcounter += 2;
             e.mtime += 2 * e.cfg.dt;
         } else {
-            e.rk3_step(tape + (size_t)m2 * per);
-            e.rk3_step(tape + (size_t)(m2 + 1) * per);
+            e.rk3_step(rec_at(m2), mrec_at(m2));
+            e.rk3_step(rec_at(m2 + 1), mrec_at(m2 + 1));
         }
     }
 
     // steps n0..n1-1 of a segment starting at n0, recording every step
     void record_segment(int n0, int n1)
     {
-        const size_t per = 12 * (size_t)N;
         int n = n0;
         for (; n + 1 < n1; n += 2) record_pair(n - n0);
-        if (n < n1) e.rk3_step(tape + (size_t)(n - n0) * per);
+        if (n < n1) e.rk3_step(rec_at(n - n0), mrec_at(n - n0));
     }
 
     KFields<T> fields() const
     {
         KFields<T> F;
         std::memset(&F, 0, sizeof(F));
-        for (int f = 0; f < 4; f++) {
+        for (int f = 0; f < nf; f++) {
             F.cur[f] = lb[f][lci[f]];
             F.P[f] = lb[f][lpi[f]];
             F.M[f] = lb[f][lmi[f]];
@@ -133,7 +146,7 @@ struct Lin : LinBase {
     T *slot_ptr(int field, int slot)
     {
         if (field == GA_PI) return lpi_f;
-        if (field < 0 || field >= 4) return nullptr;
+        if (field < 0 || field >= nf) return nullptr;
         if (slot == GA_SLOT_CUR) return lb[field][lci[field]];
         if (slot == GA_SLOT_P) return lb[field][lpi[field]];
         if (slot == GA_SLOT_M) return lb[field][lmi[field]];
@@ -143,7 +156,7 @@ struct Lin : LinBase {
     // run the engine's (linear) forward kernels on these buffers
     void exchange()
     {
-        for (int f = 0; f < 4; f++) {
+        for (int f = 0; f < nf; f++) {
             for (int s = 0; s < 3; s++) std::swap(e.buf[f][s], lb[f][s]);
             std::swap(e.ci[f], lci[f]);
             std::swap(e.pi_[f], lpi[f]);
@@ -153,19 +166,23 @@ struct Lin : LinBase {
     }
     void swap_inner()
     {
-        for (int f = 0; f < 4; f++) std::swap(lci[f], lpi[f]);
+        for (int f = 0; f < nf; f++) std::swap(lci[f], lpi[f]);
     }
 
+    // the posts of the step as they act on perturbations: zero_moisture is
+    // left out (values reaching the post are already clipped, so it is
+    // inactive there; the advection's clipping carries the mask)
     static void stage_flags(int *fl)
     {
         for (int f = 0; f < 7; f++) fl[f] = 0;
         fl[FU] = fl[FV] = fl[FW] = PF_PROJECT | PF_SPONGE | PF_VBC;
-        fl[FTH] = PF_SPONGE | PF_VBC;
+        fl[FTH] = fl[FQV] = fl[FQC] = fl[FQR] = PF_SPONGE | PF_VBC;
     }
     static void final_flags(int *fl)
     {
         for (int f = 0; f < 7; f++) fl[f] = 0;
         fl[FU] = fl[FV] = fl[FW] = fl[FTH] = PF_SPONGE | PF_VBC | PF_RAYLEIGH | PF_WRITE_M;
+        fl[FQV] = fl[FQC] = fl[FQR] = PF_SPONGE | PF_VBC | PF_WRITE_M;
     }
 
     // one step of the state and of the perturbations together
@@ -174,11 +191,16 @@ struct Lin : LinBase {
         static const double steps[3] = {1. / 3., 0.5, 1.0};
         const long tot = (long)(e.NX - 6) * (e.NY - 6) * (e.NZ - 2);
         int fl[7];
+        const bool moist = nf == 7;
         for (int s = 0; s < 3; s++) {
             const double st = steps[s];
             const T sdtg = (T)(st * e.cfg.dt * 9.8 * 0.5);
-            e.advect(st, ADV_UV | ADV_WB | ADV_TH);
-            k_tl_advect<T><<<cdiv(tot, 128), 128, 0, e.stream>>>(e.kp, e.fields(), fields(), (T)st, sdtg);
+            e.qmask = mask;
+            e.advect(st, ADV_UV | ADV_WB | ADV_TH | (moist ? (ADV_Q | ADV_ZERO) : 0));
+            e.qmask = nullptr;
+            KFields<T> R = e.fields();
+            R.qmask = mask;
+            k_tl_advect<T><<<cdiv(tot, 128), 128, 0, e.stream>>>(e.kp, R, fields(), (T)st, sdtg);
             e.launches++;
             stage_flags(fl);
             e.solve_pressure(st);
@@ -191,6 +213,12 @@ struct Lin : LinBase {
                 e.swap_inner(true);
                 swap_inner();
             }
+        }
+        if (moist) {  // Kessler: the tangent about the trajectory before its own update
+            const long tk = (long)(e.NX - 2) * (e.NY - 2) * (e.NZ - 2);
+            k_tl_kessler<T><<<cdiv(tk, 128), 128, 0, e.stream>>>(e.kp, e.fields(), fields());
+            e.launches++;
+            e.kessler();
         }
         final_flags(fl);
         e.post(fl, 7, 1.0, true);
@@ -233,28 +261,45 @@ struct Lin : LinBase {
     // theta: rec + (4*stage + field)*N).  first: the adjoint of the final
     // state enters here (the final pi-bar, and a current slot that holds no
     // stale P-bar).
-    void adj_step(const T *rec, bool first)
+    void adj_step(const T *rec, const unsigned char *mrec, bool first)
     {
         static const double steps[3] = {1. / 3., 0.5, 1.0};
         cudaStream_t s = e.stream;
+        const bool moist = nf == 7;
         const long ncolblk = cdiv((long)e.NX * e.NY, POST_COLS);
         const dim3 gadv(cdiv(e.NX, AJ_TI), cdiv(e.NY, AJ_TJ), cdiv(e.NZ, AJ_TK));
         const size_t smem_adv = (3 * (size_t)AJ_NFACE + AJ_NTB) * sizeof(T);
         swap_inner();  // advance_outer's swap
+        if (moist) {
+            // the step-final post, then Kessler (its inputs: rec + 3*nf*N);
+            // pi-bar takes Kessler's pi row (first: on top of the final pi-bar)
+            k_adj_post<T><<<ncolblk, POST_THREADS, 0, s>>>(e.kp, fields(), AP_OUTER | AP_RAYLEIGH | AP_VBC | AP_SPONGE);
+            k_adj_kessler<T><<<cdiv(N, 128), 128, 0, s>>>(e.kp, e.fields(), rec + (size_t)3 * nf * N, fields(),
+                                                         first ? 1 : 0);
+            e.launches += 2;
+        }
         for (int st = 2; st >= 0; st--) {
             const double step = steps[st];
             if (st < 2) swap_inner();
-            // stage 2 shares its buffer with the step-final post: one pass
-            const int fl = st == 2 ? (AP_OUTER | AP_RAYLEIGH | AP_VBC | AP_SPONGE2) : (AP_VBC | AP_SPONGE);
+            // dry: stage 2 shares its buffer with the step-final post, one pass
+            int fl = AP_VBC | AP_SPONGE, acc = 0;
+            if (st == 2) {
+                if (moist) acc = 1;
+                else {
+                    fl = AP_OUTER | AP_RAYLEIGH | AP_VBC | AP_SPONGE2;
+                    acc = first ? 1 : 0;
+                }
+            }
             k_adj_post<T><<<ncolblk, POST_THREADS, 0, s>>>(e.kp, fields(), fl);
-            k_adj_project<T><<<cdiv(N, 256), 256, 0, s>>>(e.kp, fields(), (T)step, (first && st == 2) ? 1 : 0);
+            k_adj_project<T><<<cdiv(N, 256), 256, 0, s>>>(e.kp, fields(), (T)step, acc);
             e.launches += 2;
             adj_pressure(step);
             KFields<T> R = e.fields();
-            for (int f = 0; f < 4; f++) R.cur[f] = const_cast<T *>(rec) + (size_t)(4 * st + f) * N;
+            for (int f = 0; f < nf; f++) R.cur[f] = const_cast<T *>(rec) + (size_t)(nf * st + f) * N;
+            const unsigned char *qm = moist ? mrec + (size_t)st * N : nullptr;
             const T sdtg = (T)(step * e.cfg.dt * 9.8 * 0.5);
             k_lin_coef<T><<<cdiv(N, 128), 128, 0, s>>>(e.kp, R, coef);
-            k_adj_advect<T><<<gadv, AJ_THREADS, smem_adv, s>>>(e.kp, coef, fields(), (T)step, sdtg,
+            k_adj_advect<T><<<gadv, AJ_THREADS, smem_adv, s>>>(e.kp, coef, fields(), qm, (T)step, sdtg,
                                                                (first && st == 2) ? 0 : 1);
             e.launches += 2;
         }
@@ -265,16 +310,19 @@ struct Lin : LinBase {
         if (tape_need > tape_steps) {
             drop_graphs();
             if (tape) cudaFree(tape);
+            if (mtape) cudaFree(mtape);
             tape = nullptr;
+            mtape = nullptr;
             tape_steps = 0;
-            if (cudaMalloc(&tape, tape_need * 12 * (size_t)N * sizeof(T)) != cudaSuccess) return GA_ERR_NOMEM;
+            if (cudaMalloc(&tape, tape_need * per_step() * sizeof(T)) != cudaSuccess) return GA_ERR_NOMEM;
+            if (nf == 7 && cudaMalloc(&mtape, tape_need * 3 * (size_t)N) != cudaSuccess) return GA_ERR_NOMEM;
             tape_steps = tape_need;
         }
         if (ckpt_need > ckpt_slots) {
             if (ckpt) cudaFree(ckpt);
             ckpt = nullptr;
             ckpt_slots = 0;
-            if (cudaMalloc(&ckpt, ckpt_need * 12 * (size_t)N * sizeof(T)) != cudaSuccess) return GA_ERR_NOMEM;
+            if (cudaMalloc(&ckpt, ckpt_need * 3 * nf * (size_t)N * sizeof(T)) != cudaSuccess) return GA_ERR_NOMEM;
             ckpt_slots = ckpt_need;
         }
         return GA_OK;
@@ -283,8 +331,8 @@ struct Lin : LinBase {
     // copy the state (current, P, M of u, v, w, theta) to or from a checkpoint
     void checkpoint(size_t slot, bool save)
     {
-        T *base = ckpt + slot * 12 * (size_t)N;
-        for (int f = 0; f < 4; f++) {
+        T *base = ckpt + slot * 3 * nf * (size_t)N;
+        for (int f = 0; f < nf; f++) {
             const int idx[3] = {e.ci[f], e.pi_[f], e.mi[f]};
             for (int s = 0; s < 3; s++) {
                 T *c = base + (size_t)(3 * f + s) * N;
@@ -305,28 +353,32 @@ struct Lin : LinBase {
         const int nseg = (nsteps + K - 1) / K;
         int rc = reserve((size_t)K, (size_t)nseg + 1);
         if (rc) return rc;
-        const size_t per = 12 * (size_t)N;
         for (int seg = 0; seg < nseg; seg++) {
             const int n0 = seg * K, n1 = std::min(nsteps, n0 + K);
             checkpoint(seg, true);
             if (seg == nseg - 1) record_segment(n0, n1);
-            else if (int rc = e.step(n1 - n0)) return rc;
+            else if (int rc2 = e.step(n1 - n0)) return rc2;
         }
         checkpoint(nseg, true);
         const long long bc = e.bigcounter;
         const double mt = e.mtime;
+        const size_t nrain = (size_t)e.NX * e.NY;
+        if (rain_keep)  // the recomputation would accumulate the rain again
+            cudaMemcpyAsync(rain_keep, e.accrain, nrain * sizeof(double), cudaMemcpyDeviceToDevice, e.stream);
         for (int seg = nseg - 1; seg >= 0; seg--) {
             const int n0 = seg * K, n1 = std::min(nsteps, n0 + K);
             if (seg != nseg - 1) {
                 checkpoint(seg, false);
                 record_segment(n0, n1);
             }
-            for (int n = n1 - 1; n >= n0; n--) adj_step(tape + (size_t)(n - n0) * per, n == nsteps - 1);
+            for (int n = n1 - 1; n >= n0; n--) adj_step(rec_at(n - n0), mrec_at(n - n0), n == nsteps - 1);
         }
         const long tot = (long)(e.NX - 6) * (e.NY - 6) * (e.NZ - 2);
         k_adj_zero_cells<T><<<cdiv(tot, 256), 256, 0, e.stream>>>(e.kp, fields());
         e.launches++;
         checkpoint(nseg, false);
+        if (rain_keep)
+            cudaMemcpyAsync(e.accrain, rain_keep, nrain * sizeof(double), cudaMemcpyDeviceToDevice, e.stream);
         e.bigcounter = bc;
         e.mtime = mt;
         cudaMemsetAsync(lpi_f, 0, N * sizeof(T), e.stream);  // the step does not read pi
@@ -344,8 +396,8 @@ Lin<T> *Engine<T>::linear()
 template <typename T>
 int Engine<T>::lin_supported() const
 {
-    if (kp.moist || kp.periodic) {
-        set_error("tangent-linear / adjoint: dry, non-periodic contexts only");
+    if (kp.periodic || (kp.moist && kp.rf != 1)) {
+        set_error("tangent-linear / adjoint: non-periodic contexts, Eulerian rain fallout (rain_fallout 1) only");
         return GA_ERR_UNSUPPORTED;
     }
     return GA_OK;

@@ -46,22 +46,95 @@ struct LinFace {
     T ga, gs;      // dF = ga*da + gs*dS
 };
 
-// Build the face of equation EQ (0 u, 1 v, 2 theta) and direction DIR at
-// (i,j,k) about the trajectory R (R.cur = fields at the start of the stage).
-// Returns false where the forward flux is identically zero (bottom faces).
+// The equations of the linearised advection: 0 u, 1 v, 2 theta, 3 qv, 4 qc,
+// 5 qr.  FX: advected field; BX: its basic state (-1: none); ZBIT: its
+// zero_moisture clipping bit.
+template <int EQ>
+struct LinEq {
+    static constexpr int FX = EQ == 0 ? FU : EQ == 1 ? FV : EQ == 2 ? FTH : EQ == 3 ? FQV : EQ == 4 ? FQC : FQR;
+    static constexpr int BX = EQ == 0 ? 0 : EQ == 1 ? 1 : EQ == 2 ? 3 : EQ == 3 ? 4 : -1;
+    static constexpr int ZBIT = EQ == 3 ? 1 : EQ == 4 ? 2 : EQ == 5 ? 4 : 0;
+};
+
+// fall speed of the rain flux at level m of a column (vt_at): recomputed from
+// the rain on levels 1..NZ-2 (level 0 uses level 1), stored above
+template <typename T>
+__device__ __forceinline__ T lin_vt(const KParams<T> &p, const KFields<T> &R, int c0, int m)
+{
+    if (m < p.nz - 1) {
+        const int mm = m == 0 ? 1 : m;
+        return fall_speed_point(p, R.cur[FQR][c0 + mm], mm);
+    }
+    return R.vt[c0 + m];
+}
+// d(fall speed)/d(rain) at level m (0 where the fall speed is stored or
+// the rain is below the threshold): vt = c * qr^0.1364
+template <typename T>
+__device__ __forceinline__ T lin_dvt(const KParams<T> &p, const KFields<T> &R, int c0, int m)
+{
+    if (m < 1 || m > p.nz - 2) return T(0);
+    const T qr = R.cur[FQR][c0 + m];
+    if (!(qr > T(1.0e-12))) return T(0);
+    return T(0.1364) * fall_speed_point(p, qr, m) / qr;
+}
+
+// The rain's vertical face (interpolate_scalar_with_fallspeed and the qr
+// fluxes of compute_fluxes_moisture): F = wf * st with wf = WBAR + W -
+// (VT_k + VT_k+1)/2; at the bottom F = -(VT_1 + VT_1)/2 * (qr_0 + qr_1)/2,
+// the outflow.  ga = st, gs = wf; the fall-speed part of d(wf) is carried by
+// lin_dvt.
+template <typename T>
+__device__ __forceinline__ bool lin_face_rain(const KParams<T> &p, const KFields<T> &R, int i, int j, int k,
+                                              LinFace<T> &L)
+{
+    const int nz = p.nz;
+    const int c = gix(p.ny, nz, i, j, k), c0 = c - k;
+    const T *Q = R.cur[FQR];
+    T Sv, wf;
+    if (k == 0) {
+        const T v1 = lin_vt(p, R, c0, 1);
+        Sv = T(0.5) * (Q[c] + Q[c + 1]);
+        wf = T(-0.5) * (v1 + v1);
+        L.ia0 = -1;
+        L.x0 = c; L.nx = 2;
+    } else {
+        const int a = c + 1;
+        const T wb = R.bar[2][a] + R.cur[FW][a];
+        wf = wb - T(0.5) * (lin_vt(p, R, c0, k) + lin_vt(p, R, c0, k + 1));
+        L.ia0 = a;
+        if (k == 1 || k == nz - 2) {
+            Sv = T(0.5) * (Q[c + 1] + Q[c]);
+            L.x0 = c; L.nx = 2;
+        } else {
+            Sv = face3(Q[c - 1], Q[c], Q[c + 1], Q[c + 2], sgn(wf));
+            L.x0 = c - 1; L.nx = 4;
+        }
+    }
+    L.ia1 = -1;
+    L.xs = 1;
+    L.sg = sgn(wf);
+    L.ga = Sv;
+    L.gs = wf;
+    return true;
+}
+
+// Build the face of equation EQ and direction DIR at (i,j,k) about the
+// trajectory R (R.cur = fields at the start of the stage).  Returns false
+// where the forward flux is identically zero (bottom faces but the rain's).
 template <typename T, int EQ, int DIR>
 __device__ __forceinline__ bool lin_face_t(const KParams<T> &p, const KFields<T> &R, int i, int j, int k,
                                            LinFace<T> &L)
 {
+    if (EQ == 5 && DIR == 2) return lin_face_rain(p, R, i, j, k, L);
     const int ny = p.ny, nz = p.nz;
     if (DIR == 2 && k == 0) return false;
-    constexpr int FX = EQ == 0 ? FU : EQ == 1 ? FV : FTH;
-    const T *X = R.cur[FX], *XB = R.bar[EQ == 2 ? 3 : EQ];
+    constexpr int FX = LinEq<EQ>::FX, BX = LinEq<EQ>::BX;
+    const T *X = R.cur[FX], *XB = BX >= 0 ? R.bar[BX] : nullptr;
     const T *A = R.cur[DIR], *AB = R.bar[DIR];
     const int c = gix(ny, nz, i, j, k);
     constexpr int one = 1;
     const int sx = ny * nz, sy = nz;
-    if (EQ == 2) {
+    if (EQ >= 2) {
         L.ia0 = DIR == 0 ? c + sx : DIR == 1 ? c + sy : c + one;
         L.ia1 = -1;
     } else if (EQ == 0) {
@@ -74,7 +147,7 @@ __device__ __forceinline__ bool lin_face_t(const KParams<T> &p, const KFields<T>
         else { L.ia0 = c + 1; L.ia1 = c - sy + 1; }
     }
     T a, ab;
-    if (EQ == 2) {
+    if (EQ >= 2) {
         a = A[L.ia0];
         ab = AB[L.ia0];
     } else {
@@ -82,22 +155,23 @@ __device__ __forceinline__ bool lin_face_t(const KParams<T> &p, const KFields<T>
         ab = T(0.5) * (AB[L.ia0] + AB[L.ia1]);
     }
     const T sgs = sgn(ab + a), sgb = sgn(a);
-    T Sv, Bv;
+    T Sv, Bv = T(0);
     if (DIR < 2) {
         const int st = DIR == 0 ? sx : sy;
         const int c0 = c - 2 * st;
         L.x0 = c0; L.xs = st; L.nx = 6;
         Sv = face5(X[c0], X[c0 + st], X[c0 + 2 * st], X[c0 + 3 * st], X[c0 + 4 * st], X[c0 + 5 * st], sgs);
-        Bv = face5(XB[c0], XB[c0 + st], XB[c0 + 2 * st], XB[c0 + 3 * st], XB[c0 + 4 * st], XB[c0 + 5 * st], sgb);
+        if (BX >= 0)
+            Bv = face5(XB[c0], XB[c0 + st], XB[c0 + 2 * st], XB[c0 + 3 * st], XB[c0 + 4 * st], XB[c0 + 5 * st], sgb);
     } else if (k == 1 || k == nz - 2) {
         L.x0 = c; L.xs = 1; L.nx = 2;
         Sv = T(0.5) * (X[c + 1] + X[c]);
-        Bv = T(0.5) * (XB[c + 1] + XB[c]);
+        if (BX >= 0) Bv = T(0.5) * (XB[c + 1] + XB[c]);
     } else {
         const int c0 = c - 1;
         L.x0 = c0; L.xs = 1; L.nx = 4;
         Sv = face3(X[c0], X[c0 + 1], X[c0 + 2], X[c0 + 3], sgs);
-        Bv = face3(XB[c0], XB[c0 + 1], XB[c0 + 2], XB[c0 + 3], sgb);
+        if (BX >= 0) Bv = face3(XB[c0], XB[c0 + 1], XB[c0 + 2], XB[c0 + 3], sgb);
     }
     L.sg = sgs;
     L.ga = Bv + Sv;
@@ -118,7 +192,16 @@ __device__ __forceinline__ bool lin_face(const KParams<T> &p, const KFields<T> &
     case 5: return lin_face_t<T, 1, 2>(p, R, i, j, k, L);
     case 6: return lin_face_t<T, 2, 0>(p, R, i, j, k, L);
     case 7: return lin_face_t<T, 2, 1>(p, R, i, j, k, L);
-    default: return lin_face_t<T, 2, 2>(p, R, i, j, k, L);
+    case 8: return lin_face_t<T, 2, 2>(p, R, i, j, k, L);
+    case 9: return lin_face_t<T, 3, 0>(p, R, i, j, k, L);
+    case 10: return lin_face_t<T, 3, 1>(p, R, i, j, k, L);
+    case 11: return lin_face_t<T, 3, 2>(p, R, i, j, k, L);
+    case 12: return lin_face_t<T, 4, 0>(p, R, i, j, k, L);
+    case 13: return lin_face_t<T, 4, 1>(p, R, i, j, k, L);
+    case 14: return lin_face_t<T, 4, 2>(p, R, i, j, k, L);
+    case 15: return lin_face_t<T, 5, 0>(p, R, i, j, k, L);
+    case 16: return lin_face_t<T, 5, 1>(p, R, i, j, k, L);
+    default: return lin_face_t<T, 5, 2>(p, R, i, j, k, L);
     }
 }
 
@@ -130,8 +213,21 @@ __device__ __forceinline__ T tl_face(const KParams<T> &p, const KFields<T> &R, c
     LinFace<T> L;
     if (!lin_face(p, R, eq, dir, i, j, k, L)) return T(0);
     const T *dA = D.cur[dir];
-    const T *dX = D.cur[eq == 0 ? FU : eq == 1 ? FV : FTH];
-    const T da = L.ia1 < 0 ? dA[L.ia0] : T(0.5) * (dA[L.ia0] + dA[L.ia1]);
+    const int fx = eq == 0 ? FU : eq == 1 ? FV : eq == 2 ? FTH : eq == 3 ? FQV : eq == 4 ? FQC : FQR;
+    const T *dX = D.cur[fx];
+    T da = L.ia0 < 0 ? T(0) : L.ia1 < 0 ? dA[L.ia0] : T(0.5) * (dA[L.ia0] + dA[L.ia1]);
+    if (eq == 5 && dir == 2) {  // the fall speed follows the rain
+        const int c0 = gix(p.ny, p.nz, i, j, 0);
+        const T *dQ = D.cur[FQR];
+        if (k == 0) {
+            const T d1 = lin_dvt(p, R, c0, 1) * dQ[c0 + 1];
+            da = da - T(0.5) * (d1 + d1);
+        } else {
+            const T d0 = lin_dvt(p, R, c0, k) * dQ[c0 + k];
+            const T d1 = k + 1 < p.nz ? lin_dvt(p, R, c0, k + 1) * dQ[c0 + k + 1] : T(0);
+            da = da - T(0.5) * (d0 + d1);
+        }
+    }
     T ds;
     const int c = L.x0, st = L.xs;
     if (L.nx == 6) ds = face5(dX[c], dX[c + st], dX[c + 2 * st], dX[c + 3 * st], dX[c + 4 * st], dX[c + 5 * st], L.sg);
@@ -141,7 +237,8 @@ __device__ __forceinline__ T tl_face(const KParams<T> &p, const KFields<T> &R, c
 }
 
 // tangent of the tendency of equation eq at a cell (u_tend_cell, v_tend_cell,
-// theta_tend_cell with Z_ADVECT_BASE: advection.cpp:16-18, 73-122, 152-168)
+// theta/qv/qc/qr_tend_cell with Z_ADVECT_BASE: advection.cpp:16-18, 73-122,
+// 152-253)
 template <typename T>
 __device__ T tl_tend(const KParams<T> &p, const KFields<T> &R, const KFields<T> &D, int eq, int i, int j, int k)
 {
@@ -161,18 +258,20 @@ __device__ T tl_tend(const KParams<T> &p, const KFields<T> &R, const KFields<T> 
         t -= p.dt * p.f[j] * T(0.25) *
              (dU[gix(ny, nz, i, j, k)] + dU[gix(ny, nz, i + 1, j, k)] + dU[gix(ny, nz, i, j - 1, k)] +
               dU[gix(ny, nz, i + 1, j - 1, k)]);
-    } else {
-        const T *dW = D.cur[FW];
+    } else if (eq == 2 || eq == 3) {
+        const T *dW = D.cur[FW], *base = eq == 2 ? p.tb : p.qb;
         const int c = gix(ny, nz, i, j, k);
         t -= DTZ * T(0.5) *
-             (p.rhow[k + 1] * dW[c + 1] * (p.tb[k + 1] - p.tb[k]) + p.rhow[k] * dW[c] * (p.tb[k] - p.tb[k - 1])) *
+             (p.rhow[k + 1] * dW[c + 1] * (base[k + 1] - base[k]) + p.rhow[k] * dW[c] * (base[k] - base[k - 1])) *
              p.one_d_rhou[k];
     }
     return t;
 }
 
-// TLM of advect_uvw_velocity + advect_theta (advection.cpp:304-373): D.P =
-// D.M + step * d(tendency) on the cells the forward step writes.
+// TLM of advect_uvw_velocity, advect_theta and (moist) advect_microphysics_
+// cell with zero_moisture (advection.cpp:304-498, microphysics.cpp:675-700):
+// D.P = D.M + step * d(tendency) on the cells the forward step writes; a
+// moisture point the trajectory clipped (R.qmask) has no tangent.
 template <typename T>
 __global__ void k_tl_advect(KParams<T> p, KFields<T> R, KFields<T> D, T step, T sdtg)
 {
@@ -186,10 +285,96 @@ __global__ void k_tl_advect(KParams<T> p, KFields<T> R, KFields<T> D, T step, T 
     D.P[FU][c] = D.M[FU][c] + step * tl_tend(p, R, D, 0, i, j, k);
     D.P[FV][c] = D.M[FV][c] + step * tl_tend(p, R, D, 1, i, j, k);
     D.P[FTH][c] = D.M[FTH][c] + step * tl_tend(p, R, D, 2, i, j, k);
-    if (k >= 2) {  // buoyancy_dry (advection.cpp:42-52, 329-337): linear in theta
-        const T b0 = D.cur[FTH][c] / p.tbv[k], b1 = D.cur[FTH][c - 1] / p.tbv[k - 1];
+    if (k >= 2) {  // buoyancy_dry / buoyancy_warm_micro (advection.cpp:42-58, 329-337): linear
+        T b0 = D.cur[FTH][c] / p.tbv[k], b1 = D.cur[FTH][c - 1] / p.tbv[k - 1];
+        if (p.moist) {
+            b0 = b0 + T(0.61) * D.cur[FQV][c] - D.cur[FQC][c] - D.cur[FQR][c];
+            b1 = b1 + T(0.61) * D.cur[FQV][c - 1] - D.cur[FQC][c - 1] - D.cur[FQR][c - 1];
+        }
         D.P[FW][c] = D.M[FW][c] + sdtg * (b0 + b1);
     }
+    if (p.moist) {
+        const unsigned char bits = R.qmask ? R.qmask[c] : 0;
+        D.P[FQV][c] = (bits & 1) ? T(0) : D.M[FQV][c] + step * tl_tend(p, R, D, 3, i, j, k);
+        D.P[FQC][c] = (bits & 2) ? T(0) : D.M[FQC][c] + step * tl_tend(p, R, D, 4, i, j, k);
+        D.P[FQR][c] = (bits & 4) ? T(0) : D.M[FQR][c] + step * tl_tend(p, R, D, 5, i, j, k);
+    }
+}
+
+// Jacobian of run_kessler_microphysics at one point: d(theta, qv, qc, qr)/
+// d(theta, qv, qc, qr, pi), by kessler_point on dual numbers (the branch
+// decisions are the trajectory's)
+template <typename T>
+__device__ __forceinline__ void kessler_jacobian(const KParams<T> &p, const KFields<T> &R, int k, int ix,
+                                                 const T in[5], T J[4][5])
+{
+    Dual<T, 5> x[5];
+    for (int a = 0; a < 5; a++) {
+        x[a].v = in[a];
+        for (int q = 0; q < 5; q++) x[a].d[q] = a == q ? T(1) : T(0);
+    }
+    kessler_point(x[0], x[1], x[2], x[3], x[4], kes_point(p, R, k, ix));
+    for (int a = 0; a < 4; a++)
+        for (int q = 0; q < 5; q++) J[a][q] = x[a].d[q];
+}
+
+// TLM of the Kessler step: D.P (theta, qv, qc, qr) <- J * (D.P, D.pi) with J
+// at the trajectory R.P, R.pi (before the trajectory's own Kessler step)
+template <typename T>
+__global__ void __launch_bounds__(128) k_tl_kessler(KParams<T> p, KFields<T> R, KFields<T> D)
+{
+    const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int nzi = p.nz - 2, nyi = p.ny - 2, nxi = p.nx - 2;
+    if (t >= (long)nxi * nyi * nzi) return;
+    const int k = 1 + (int)(t % nzi);
+    const int j = 1 + (int)((t / nzi) % nyi);
+    const int i = 1 + (int)(t / ((long)nzi * nyi));
+    const int ix = gix(p.ny, p.nz, i, j, k);
+    const int fl[4] = {FTH, FQV, FQC, FQR};
+    T in[5], d[5], J[4][5];
+    for (int a = 0; a < 4; a++) {
+        in[a] = R.P[fl[a]][ix];
+        d[a] = D.P[fl[a]][ix];
+    }
+    in[4] = R.pi[ix];
+    d[4] = D.pi[ix];
+    kessler_jacobian(p, R, k, ix, in, J);
+    for (int a = 0; a < 4; a++) {
+        T v = T(0);
+        for (int q = 0; q < 5; q++) v += J[a][q] * d[q];
+        D.P[fl[a]][ix] = v;
+    }
+}
+
+// adjoint of the Kessler step about the recorded inputs kin (theta, qv, qc,
+// qr, pi: kin + q*N): A.P <- J^T A.P, pi-bar gets the pi row.  Covers every
+// point: off the Kessler points pi-bar is only reset (acc = 0) or kept.
+template <typename T>
+__global__ void __launch_bounds__(128) k_adj_kessler(KParams<T> p, KFields<T> R, const T *kin, KFields<T> A, int acc)
+{
+    const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= p.n) return;
+    const int nz = p.nz, ny = p.ny;
+    const int k = (int)(t % nz), j = (int)((t / nz) % ny), i = (int)(t / ((long)nz * ny));
+    const int ix = (int)t;
+    const T pib = acc ? A.pi[ix] : T(0);
+    if (i < 1 || i > p.nx - 2 || j < 1 || j > ny - 2 || k < 1 || k > nz - 2) {
+        A.pi[ix] = pib;
+        return;
+    }
+    const int fl[4] = {FTH, FQV, FQC, FQR};
+    T in[5], ob[4], J[4][5];
+    for (int q = 0; q < 5; q++) in[q] = kin[(size_t)q * p.n + ix];
+    for (int a = 0; a < 4; a++) ob[a] = A.P[fl[a]][ix];
+    kessler_jacobian(p, R, k, ix, in, J);
+    for (int q = 0; q < 4; q++) {
+        T v = T(0);
+        for (int a = 0; a < 4; a++) v += J[a][q] * ob[a];
+        A.P[fl[q]][ix] = v;
+    }
+    T v = T(0);
+    for (int a = 0; a < 4; a++) v += J[a][4] * ob[a];
+    A.pi[ix] = pib + v;
 }
 
 // ---------------------------------------------------------------------------
@@ -218,7 +403,8 @@ constexpr int AJ_BI = AJ_TI + 6, AJ_BJ = AJ_TJ + 6, AJ_BK = AJ_TK + 4, AJ_NTB = 
 // cell c and face family fam = 3*EQ + DIR, coef[(2*fam)*N + c] = B + S and
 // coef[(2*fam + 1)*N + c] = ab + a of the face at c (its sign is the frozen
 // upwind sign), zero where the face is not next to an advected cell.
-constexpr int LIN_NCOEF = 18;
+constexpr int LIN_NCOEF = 18;        // dry: 9 families x 2
+constexpr int LIN_NCOEF_MOIST = 37;  // moist: 18 families x 2 + d(fall speed)/d(rain) per cell
 
 template <typename T, int EQ, int DIR>
 __device__ __forceinline__ void lin_coef_face(const KParams<T> &p, const KFields<T> &R, T *coef, int i, int j, int k,
@@ -227,7 +413,7 @@ __device__ __forceinline__ void lin_coef_face(const KParams<T> &p, const KFields
     bool need;
     if (DIR == 0) need = adv_cell(p, i, j, k, 1) || adv_cell(p, i + 1, j, k, 1);
     else if (DIR == 1) need = adv_cell(p, i, j, k, 1) || adv_cell(p, i, j + 1, k, 1);
-    else need = adv_cell(p, i, j, k, 1) || adv_cell(p, i, j, k + 1, 1);
+    else need = adv_cell(p, i, j, k, 1) || (k + 1 < p.nz && adv_cell(p, i, j, k + 1, 1));
     T ga = T(0), gs = T(0);
     LinFace<T> L;
     if (need && lin_face_t<T, EQ, DIR>(p, R, i, j, k, L)) {
@@ -256,27 +442,46 @@ __global__ void k_lin_coef(KParams<T> p, KFields<T> R, T *coef)
     lin_coef_face<T, 2, 0>(p, R, coef, i, j, k, c);
     lin_coef_face<T, 2, 1>(p, R, coef, i, j, k, c);
     lin_coef_face<T, 2, 2>(p, R, coef, i, j, k, c);
+    if (p.moist) {
+        lin_coef_face<T, 3, 0>(p, R, coef, i, j, k, c);
+        lin_coef_face<T, 3, 1>(p, R, coef, i, j, k, c);
+        lin_coef_face<T, 3, 2>(p, R, coef, i, j, k, c);
+        lin_coef_face<T, 4, 0>(p, R, coef, i, j, k, c);
+        lin_coef_face<T, 4, 1>(p, R, coef, i, j, k, c);
+        lin_coef_face<T, 4, 2>(p, R, coef, i, j, k, c);
+        lin_coef_face<T, 5, 0>(p, R, coef, i, j, k, c);
+        lin_coef_face<T, 5, 1>(p, R, coef, i, j, k, c);
+        lin_coef_face<T, 5, 2>(p, R, coef, i, j, k, c);
+        const bool inner = i >= 3 && i < p.nx - 3 && j >= 3 && j < p.ny - 3;
+        coef[(size_t)36 * p.n + c] = inner ? lin_dvt(p, R, c - k, k) : T(0);
+    }
 }
 
 // tendency adjoints of equation EQ (zero off the advected cells) over the box
 template <typename T, int EQ>
-__device__ __forceinline__ void adj_stage_tbar(const KParams<T> &p, const KFields<T> &A, T step, int i0, int j0,
-                                               int k0, T *tb)
+__device__ __forceinline__ void adj_stage_tbar(const KParams<T> &p, const KFields<T> &A, const unsigned char *qm,
+                                               T step, int i0, int j0, int k0, T *tb)
 {
-    constexpr int XF = EQ == 0 ? FU : EQ == 1 ? FV : FTH;
+    constexpr int XF = LinEq<EQ>::FX, ZB = LinEq<EQ>::ZBIT;
     const T *P = A.P[XF];
     for (int e = threadIdx.x; e < AJ_NTB; e += AJ_THREADS) {
         const int i = i0 - 3 + e / (AJ_BK * AJ_BJ), j = j0 - 3 + (e / AJ_BK) % AJ_BJ, k = k0 - 2 + e % AJ_BK;
-        tb[e] = adv_cell(p, i, j, k, 1) ? step * P[gix(p.ny, p.nz, i, j, k)] : T(0);
+        T v = T(0);
+        if (adv_cell(p, i, j, k, 1)) {
+            const int c = gix(p.ny, p.nz, i, j, k);
+            if (!ZB || !(qm[c] & ZB)) v = step * P[c];  // a clipped point has no tendency adjoint
+        }
+        tb[e] = v;
     }
 }
 
 template <typename T, int EQ, int DIR>
 __device__ __forceinline__ void adj_family(const KParams<T> &p, const T *__restrict__ coef, const T *tb, int i0,
-                                           int j0, int k0, T *fs1, T *fs2, T *fab, T (&acc)[AJ_CPT][4])
+                                           int j0, int k0, T *fs1, T *fs2, T *fab, T (&acc)[AJ_CPT][7])
 {
-    constexpr int XF = EQ == 0 ? FU : EQ == 1 ? FV : FTH;
+    constexpr int XF = LinEq<EQ>::FX;
     constexpr int fam = 3 * EQ + DIR;
+    constexpr bool RAIN_Z = EQ == 5 && DIR == 2;
     constexpr int bdi = DIR == 0 ? 3 : 0, bdj = DIR == 1 ? 3 : 0, bdk = DIR == 2 ? 2 : 0;
     constexpr int bni = DIR == 0 ? AJ_TI + 5 : AJ_TI + 1;
     constexpr int bnj = DIR == 1 ? AJ_TJ + 5 : AJ_TJ + 1;
@@ -310,7 +515,7 @@ __device__ __forceinline__ void adj_family(const KParams<T> &p, const T *__restr
         }
         const T s1 = fb * gs;
         fs1[f] = s1;
-        fs2[f] = (DIR == 2 && (fk == 1 || fk == p.nz - 2)) ? T(0) : (gs > T(0) ? s1 : -s1);
+        fs2[f] = (DIR == 2 && (fk <= 1 || fk == p.nz - 2)) ? T(0) : (gs > T(0) ? s1 : -s1);
         fab[f] = fb * ga;
     }
     __syncthreads();
@@ -351,9 +556,9 @@ __device__ __forceinline__ void adj_family(const KParams<T> &p, const T *__restr
 #pragma unroll
             for (int d = -2; d <= 1; d++) {
                 const int fk = pk + d;
-                if (fk < 1 || fk > nz - 2) continue;
+                if (fk < (RAIN_Z ? 0 : 1) || fk > nz - 2) continue;
                 const int w = at(0, 0, d);
-                if (fk == 1 || fk == nz - 2) {
+                if (fk <= 1 || fk == nz - 2) {  // 2nd order (and the rain's bottom outflow)
                     if (d == 0 || d == -1) gx += T(0.5) * fs1[w];
                 } else {
                     const int m = 1 - d;  // position of the cell in the face's stencil fk-1..fk+2
@@ -362,7 +567,16 @@ __device__ __forceinline__ void adj_family(const KParams<T> &p, const T *__restr
             }
             if (EQ == 0) ga = T(0.5) * (fab[at(0, 0, -1)] + fab[at(1, 0, -1)]);
             else if (EQ == 1) ga = T(0.5) * (fab[at(0, 0, -1)] + fab[at(0, 1, -1)]);
-            else ga = fab[at(0, 0, -1)];
+            else if (RAIN_Z) {
+                // the bottom outflow does not depend on w; the fall speed of
+                // levels 1..NZ-2 follows their rain (face 0 holds level 1 twice)
+                ga = pk >= 2 ? fab[at(0, 0, -1)] : T(0);
+                if (pk >= 1 && pk <= nz - 2) {
+                    const T dv = coef[(size_t)36 * p.n + gix(p.ny, p.nz, i0 + li, j0 + lj, pk)];
+                    const T below = fab[at(0, 0, -1)] * (pk == 1 ? T(2) : T(1));
+                    gx -= T(0.5) * dv * (fab[at(0, 0, 0)] + below);
+                }
+            } else ga = fab[at(0, 0, -1)];
         }
         acc[r][XF] += gx;
         acc[r][DIR] += ga;
@@ -375,7 +589,7 @@ __device__ __forceinline__ void adj_family(const KParams<T> &p, const T *__restr
 // vertical advection of the basic-state theta (Z_ADVECT_BASE) into w
 template <typename T, int EQ>
 __device__ __forceinline__ void adj_extra(const KParams<T> &p, const T *tb, int i0, int j0, int k0,
-                                          T (&acc)[AJ_CPT][4])
+                                          T (&acc)[AJ_CPT][7])
 {
     const T fdt = p.dt * T(0.25);
 #pragma unroll
@@ -398,24 +612,25 @@ __device__ __forceinline__ void adj_extra(const KParams<T> &p, const T *tb, int 
                 const T tv = TB(di[n], dj[n], 0);
                 if (tv != T(0)) acc[r][FU] -= (fdt * p.f[pj + dj[n]]) * tv;
             }
-        } else {
+        } else if (EQ == 2 || EQ == 3) {
+            const T *base = EQ == 2 ? p.tb : p.qb;
             const T t0 = TB(0, 0, -1), t1 = TB(0, 0, 0);
             if (t0 != T(0))
-                acc[r][FW] -= (p.dtz * p.mu[pk - 1]) * T(0.5) * p.rhow[pk] * (p.tb[pk] - p.tb[pk - 1]) *
+                acc[r][FW] -= (p.dtz * p.mu[pk - 1]) * T(0.5) * p.rhow[pk] * (base[pk] - base[pk - 1]) *
                               p.one_d_rhou[pk - 1] * t0;
             if (t1 != T(0))
-                acc[r][FW] -= (p.dtz * p.mu[pk]) * T(0.5) * p.rhow[pk] * (p.tb[pk] - p.tb[pk - 1]) * p.one_d_rhou[pk] *
-                              t1;
+                acc[r][FW] -= (p.dtz * p.mu[pk]) * T(0.5) * p.rhow[pk] * (base[pk] - base[pk - 1]) *
+                              p.one_d_rhou[pk] * t1;
         }
     }
 }
 
 template <typename T, int EQ>
 __device__ __forceinline__ void adj_equation(const KParams<T> &p, const T *__restrict__ coef, const KFields<T> &A,
-                                             T step, int i0, int j0, int k0, T *tb, T *fs1, T *fs2, T *fab,
-                                             T (&acc)[AJ_CPT][4])
+                                             const unsigned char *qm, T step, int i0, int j0, int k0, T *tb, T *fs1,
+                                             T *fs2, T *fab, T (&acc)[AJ_CPT][7])
 {
-    adj_stage_tbar<T, EQ>(p, A, step, i0, j0, k0, tb);
+    adj_stage_tbar<T, EQ>(p, A, qm, step, i0, j0, k0, tb);
     __syncthreads();
     adj_family<T, EQ, 0>(p, coef, tb, i0, j0, k0, fs1, fs2, fab, acc);
     adj_family<T, EQ, 1>(p, coef, tb, i0, j0, k0, fs1, fs2, fab, acc);
@@ -426,19 +641,25 @@ __device__ __forceinline__ void adj_equation(const KParams<T> &p, const T *__res
 
 template <typename T>
 __global__ void __launch_bounds__(AJ_THREADS) k_adj_advect(KParams<T> p, const T *__restrict__ coef, KFields<T> A,
-                                                           T step, T sdtg, int zero_cur)
+                                                           const unsigned char *qm, T step, T sdtg, int zero_cur)
 {
     extern __shared__ unsigned char smem_raw[];
     T *fs1 = (T *)smem_raw, *fs2 = fs1 + AJ_NFACE, *fab = fs2 + AJ_NFACE, *tb = fab + AJ_NFACE;
     const int ny = p.ny, nz = p.nz;
     const int i0 = blockIdx.x * AJ_TI, j0 = blockIdx.y * AJ_TJ, k0 = blockIdx.z * AJ_TK;
-    T acc[AJ_CPT][4];
+    const int nf = p.moist ? 7 : 4;
+    T acc[AJ_CPT][7];
 #pragma unroll
     for (int r = 0; r < AJ_CPT; r++)
-        for (int f = 0; f < 4; f++) acc[r][f] = T(0);
-    adj_equation<T, 0>(p, coef, A, step, i0, j0, k0, tb, fs1, fs2, fab, acc);
-    adj_equation<T, 1>(p, coef, A, step, i0, j0, k0, tb, fs1, fs2, fab, acc);
-    adj_equation<T, 2>(p, coef, A, step, i0, j0, k0, tb, fs1, fs2, fab, acc);
+        for (int f = 0; f < 7; f++) acc[r][f] = T(0);
+    adj_equation<T, 0>(p, coef, A, qm, step, i0, j0, k0, tb, fs1, fs2, fab, acc);
+    adj_equation<T, 1>(p, coef, A, qm, step, i0, j0, k0, tb, fs1, fs2, fab, acc);
+    adj_equation<T, 2>(p, coef, A, qm, step, i0, j0, k0, tb, fs1, fs2, fab, acc);
+    if (p.moist) {
+        adj_equation<T, 3>(p, coef, A, qm, step, i0, j0, k0, tb, fs1, fs2, fab, acc);
+        adj_equation<T, 4>(p, coef, A, qm, step, i0, j0, k0, tb, fs1, fs2, fab, acc);
+        adj_equation<T, 5>(p, coef, A, qm, step, i0, j0, k0, tb, fs1, fs2, fab, acc);
+    }
 #pragma unroll
     for (int r = 0; r < AJ_CPT; r++) {
         const int e = threadIdx.x + r * AJ_THREADS;
@@ -446,17 +667,27 @@ __global__ void __launch_bounds__(AJ_THREADS) k_adj_advect(KParams<T> p, const T
         if (pi >= p.nx || pj >= ny || pk >= nz) continue;
         T *a = acc[r];
         const int c = gix(ny, nz, pi, pj, pk);
-        // buoyancy of w into theta
+        // buoyancy of w into theta (and the moisture loading)
         {
             T bw = T(0);
             if (adv_cell(p, pi, pj, pk, 2)) bw += A.P[FW][c];
             if (adv_cell(p, pi, pj, pk + 1, 2)) bw += A.P[FW][c + 1];
-            if (bw != T(0)) a[FTH] += sdtg / p.tbv[pk] * bw;
+            if (bw != T(0)) {
+                a[FTH] += sdtg / p.tbv[pk] * bw;
+                if (p.moist) {
+                    a[FQV] += sdtg * T(0.61) * bw;
+                    a[FQC] -= sdtg * bw;
+                    a[FQR] -= sdtg * bw;
+                }
+            }
         }
+        const unsigned char bits = p.moist ? qm[c] : 0;
 #pragma unroll
-        for (int f = 0; f < 4; f++) {
+        for (int f = 0; f < 7; f++) {
+            if (f >= nf) break;
             const bool cell = adv_cell(p, pi, pj, pk, f == FW ? 2 : 1);
-            if (cell) A.M[f][c] += A.P[f][c];
+            const int zb = f == FQV ? 1 : f == FQC ? 2 : f == FQR ? 4 : 0;
+            if (cell && !(bits & zb)) A.M[f][c] += A.P[f][c];
             if (zero_cur && cell) A.cur[f][c] = a[f];
             else if (a[f] != T(0)) A.cur[f][c] += a[f];
         }
@@ -480,8 +711,8 @@ __global__ void k_adj_zero_cells(KParams<T> p, KFields<T> A)
     const int j = 3 + (int)((t / nzi) % nyi);
     const int i = 3 + (int)(t / ((long)nzi * nyi));
     const int c = gix(p.ny, p.nz, i, j, k);
-#pragma unroll
-    for (int f = 0; f < 4; f++) {
+    const int nf = p.moist ? 7 : 4;
+    for (int f = 0; f < nf; f++) {
         if (f == FW && k < 2) continue;
         A.P[f][c] = T(0);
     }
@@ -504,7 +735,7 @@ __device__ __forceinline__ T adj_post_pre(const KParams<T> &p, const KFields<T> 
     const int c = gix(p.ny, p.nz, i, j, k);
     T v = A.P[f][c];
     if (flags & AP_OUTER) v = v + A.M[f][c];
-    if ((flags & AP_RAYLEIGH) && i >= 1 && i < p.nx - 1 && j >= 1 && j < p.ny - 1 && k >= p.raylevel) {
+    if ((flags & AP_RAYLEIGH) && f <= FTH && i >= 1 && i < p.nx - 1 && j >= 1 && j < p.ny - 1 && k >= p.raylevel) {
         const T cr = (f == FW) ? p.ray_w[k] : p.ray_u[k];
         v = v - cr * v;
     }
@@ -514,9 +745,9 @@ __device__ __forceinline__ T adj_post_pre(const KParams<T> &p, const KFields<T> 
 template <typename T>
 __global__ void __launch_bounds__(POST_THREADS) k_adj_post(KParams<T> p, KFields<T> A, int flags)
 {
-    const int nz = p.nz;
+    const int nz = p.nz, nf = p.moist ? 7 : 4;
     const long c0 = (long)blockIdx.x * POST_COLS;
-    T vals[4][POST_R];
+    T vals[7][POST_R];
 #pragma unroll
     for (int r = 0; r < POST_R; ++r) {
         const int e = threadIdx.x + r * POST_THREADS;
@@ -531,7 +762,8 @@ __global__ void __launch_bounds__(POST_THREADS) k_adj_post(KParams<T> p, KFields
         const bool hS = kin && i >= 1 && j >= p.sb && j < p.se;
         const bool hN = kin && i >= 1 && j >= p.nb && j < p.ne;
 #pragma unroll
-        for (int f = 0; f < 4; ++f) {
+        for (int f = 0; f < 7; ++f) {
+            if (f >= nf) break;
             T v = adj_post_pre(p, A, f, i, j, k, flags);
             if (vbc) {  // transposed boundaries.cpp:304-326
                 if (f == FW) {
@@ -560,7 +792,8 @@ __global__ void __launch_bounds__(POST_THREADS) k_adj_post(KParams<T> p, KFields
         if (cl >= POST_COLS || col >= (long)p.nx * p.ny) continue;
         const int c = (int)col * nz + k;
 #pragma unroll
-        for (int f = 0; f < 4; ++f) {
+        for (int f = 0; f < 7; ++f) {
+            if (f >= nf) break;
             A.P[f][c] = vals[f][r];
             if (flags & AP_OUTER) A.M[f][c] = T(0);
         }

@@ -11,7 +11,9 @@ The reference has no linearisation, so its checks are mathematical:
     function) against finite differences along random directions.
 The trajectory carries small noise in every slot so that no upwind sign is
 decided at an exact zero (there the flux is a kink and central differences
-average the two one-sided derivatives).
+average the two one-sided derivatives).  The moist cases (Kessler, Eulerian
+rain fallout) freeze zero_moisture's clipping and Kessler's branches at the
+trajectory; their finite-difference check keeps cloud and rain above zero.
 """
 from __future__ import annotations
 
@@ -324,8 +326,102 @@ def test_gpu_vorticity_gradient_matches_finite_differences(built):
 
 
 @pytest.mark.gpu
-def test_gpu_adjoint_rejects_moist(built):
+@pytest.mark.parametrize("kw", [dict(rain_fallout=2), dict(periodic=1)])
+def test_gpu_adjoint_rejects_unsupported(built, kw):
+    """Semi-Lagrangian rain fallout and periodic boundaries are not linearised."""
     from model_gb300 import anelastic
-    m = anelastic.Model(configs.moist_blob(nx=14, ny=13, nz=10), abi.GA_PREC_F64)
+    m = anelastic.Model(configs.moist_blob(nx=18, ny=13, nz=10, **kw), abi.GA_PREC_F64)
     with pytest.raises(anelastic.GaError):
         m.tlm_step(1)
+    with pytest.raises(anelastic.GaError):
+        m.adjoint(1, 1)
+
+
+# ---------------------------------------------------------------------------
+# moist (Kessler, Eulerian rain fallout): the clipping of zero_moisture and
+# the branches of Kessler are frozen at the trajectory
+# ---------------------------------------------------------------------------
+MOIST = [(f, s) for f in range(7) for s in (abi.GA_SLOT_CUR, abi.GA_SLOT_P, abi.GA_SLOT_M)]
+MSCALE = {0: 1.0, 1: 1.0, 2: 0.1, 3: 0.5, 4: 1e-5, 5: 1e-5, 6: 1e-5}
+
+
+def moist_state(wl, positive, seed=77):
+    """Every slot: the workload's state plus noise; positive: cloud and rain
+    above zero everywhere, so that no clipping decision sits at a kink."""
+    rng = np.random.default_rng(seed)
+    st = {}
+    for f, s in MOIST:
+        v = np.asarray(wl.fields[abi.PROG_NAMES[f]], dtype=np.float64).ravel() * (0.9 if s == abi.GA_SLOT_P else 1.0)
+        if f < 4:
+            v = v + 0.05 * rng.standard_normal(wl.points)
+        elif positive:
+            v = np.abs(v) + 4e-4 * (1.0 + 0.2 * rng.standard_normal(wl.points))
+        st[(f, s)] = v
+    return st
+
+
+def moist_dirs(wl, seed, with_pi=True):
+    rng = np.random.default_rng(seed)
+    d = {(f, s): MSCALE[f] * rng.standard_normal(wl.points) for f, s in MOIST}
+    if with_pi:
+        d[(abi.GA_PI, 0)] = rng.standard_normal(wl.points)
+    return d
+
+
+def _moist_model_state(m):
+    d = {(f, s): m.get(f, s) for f, s in MOIST}
+    d[(abi.GA_PI, 0)] = m.get(abi.GA_PI)
+    return d
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec,tol", [(abi.GA_PREC_F64, 1e-8), (abi.GA_PREC_F32, 1e-4)])
+@pytest.mark.parametrize("positive", [False, True])
+def test_gpu_moist_dot_product(built, prec, tol, positive):
+    wl = configs.moist_blob(nx=24, ny=22, nz=16)
+    st = moist_state(wl, positive)
+    x, y = moist_dirs(wl, 21), moist_dirs(wl, 22)
+    m = _model(wl, st, prec)
+    m.lin_set_all(x)
+    m.tlm_step(4)
+    Lx = m.lin_get_all()
+    m = _model(wl, st, prec)
+    m.lin_set_all(y)
+    m.adjoint(4, 2)
+    LTy = m.lin_get_all()
+    lhs, rhs = dot(Lx, y), dot(x, LTy)
+    assert abs(lhs - rhs) <= tol * abs(lhs), (lhs, rhs)
+
+
+@pytest.mark.gpu
+def test_gpu_moist_tlm_matches_finite_differences(built):
+    wl = configs.moist_blob(nx=24, ny=22, nz=16)
+    st = moist_state(wl, True)
+    dx = moist_dirs(wl, 41, with_pi=False)
+    m = _model(wl, st)
+    m.lin_set_all(dx)
+    m.tlm_step(3)
+    dy = m.lin_get_all()
+    eps = 1e-5
+    mp = _model(wl, st, pert=dx, eps=eps); mp.step(3)
+    mm = _model(wl, st, pert=dx, eps=-eps); mm.step(3)
+    yp, ym = _moist_model_state(mp), _moist_model_state(mm)
+    fd = {k: (yp[k] - ym[k]) / (2 * eps) for k in dy}
+    assert rel(fd, dy) < 1e-6
+
+
+@pytest.mark.gpu
+def test_gpu_moist_checkpointing_is_exact(built):
+    wl = configs.moist_blob(nx=24, ny=22, nz=16)
+    st = moist_state(wl, False)
+    y = moist_dirs(wl, 31)
+    outs = []
+    for K in (1, 2, 0):
+        m = _model(wl, st)
+        m.lin_set_all(y)
+        m.adjoint(4, K)
+        outs.append(m.lin_get_all())
+        assert m.counters()[0] == 4
+    for o in outs[1:]:
+        for k in MOIST:
+            assert np.array_equal(o[k], outs[0][k]), k
