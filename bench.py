@@ -288,21 +288,29 @@ def ensemble_bench(torch, device, steps, warmup, n_small=64, n_large=32):
     return out
 
 
-def adjoint_bench(torch, device, steps, every):
-    """Forward vs forward+adjoint of the dry monsoon-vortex workload
-    (192x128x32, dx=dy=40 km, dz=600 m, dt=120 s): `steps` steps from the
-    initial state, then the adjoint of the whole run back to it with the state
-    checkpointed every `every` steps and each segment recomputed.  One job per
-    timing, bracketed by CUDA events on the library stream, L2 flushed before
-    each job (the state of this grid fits in L2, so the steps of a job run
-    partly from L2, the same for both)."""
+def adjoint_bench(torch, device, steps, every, moist=False, size=512):
+    """Forward vs forward+adjoint: `steps` steps from the initial state, then
+    the adjoint of the whole run back to it with the state checkpointed every
+    `every` steps and each segment recomputed.  Dry: the monsoon vortex
+    (192x128x32, dx=dy=40 km, dz=600 m, dt=120 s), FP32 and FP64.  Moist: the
+    Kessler squall line (size x size x 64, dx=dy=1 km, dz=300 m, dt=3 s), FP32.
+    One job per timing, bracketed by CUDA events on the library stream, L2
+    flushed before each job."""
     from model_gb300 import abi, anelastic, configs
-    wl = configs.monsoon_vortex(nsteps=steps)
+    if moist:
+        wl = configs.squall_line(nx=size, ny=size, nsteps=steps)
+        desc = f"Kessler squall line {wl.nx}x{wl.ny}x{wl.nz}, dx=dy=1 km, dz=300 m, dt=3 s"
+        precs = (("fp32", abi.GA_PREC_F32),)
+        mem = "checkpoints: steps/every+1 states of 21 fields; trajectory: every x (26 fields + 3 clipping records)"
+    else:
+        wl = configs.monsoon_vortex(nsteps=steps)
+        desc = f"dry monsoon vortex {wl.nx}x{wl.ny}x{wl.nz}, dx=dy=40 km, dz=600 m, dt=120 s"
+        precs = (("fp32", abi.GA_PREC_F32), ("fp64", abi.GA_PREC_F64))
+        mem = "checkpoints: steps/every+1 states of 12 fields; trajectory: every x 12 fields"
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{device}")
-    out = {"workload": f"dry monsoon vortex {wl.nx}x{wl.ny}x{wl.nz}, dx=dy=40 km, dz=600 m, dt=120 s",
-           "steps": steps, "checkpoint_every": every,
-           "memory": "checkpoints: steps/every+1 states of 12 fields; trajectory: every x 12 fields"}
-    for name, prec in (("fp32", abi.GA_PREC_F32), ("fp64", abi.GA_PREC_F64)):
+    out = {"workload": desc, "steps": steps, "checkpoint_every": every, "memory": mem}
+    nprog = 7 if moist else 4
+    for name, prec in precs:
         m = anelastic.Model(wl, prec, device=device)
         m.tune()
         ext = torch.cuda.ExternalStream(m.stream_handle())
@@ -311,12 +319,12 @@ def adjoint_bench(torch, device, steps, every):
         def reset():
             # initial state (current = M = perturbation, P = 0); the basic
             # state is left alone so no graph is rebuilt inside a timing
-            for f in m.LIN_FIELDS:
+            for f in range(nprog):
                 init = wl.fields[abi.PROG_NAMES[f]]
                 m.set(f, abi.GA_SLOT_CUR, init)
                 m.set(f, abi.GA_SLOT_P, zero)
                 m.set(f, abi.GA_SLOT_M, init)
-            for f in m.LIN_FIELDS:
+            for f in range(nprog):
                 for s in m.LIN_SLOTS:
                     m.lin_set(f, s, zero)
             m.lin_set(abi.GA_PI, 0, zero)
@@ -477,6 +485,9 @@ def run_ours(args):
         line["ensemble"] = ensemble_bench(torch, device, args.ensemble_steps, 2)
     if args.adjoint_steps > 0:
         line["adjoint"] = adjoint_bench(torch, device, args.adjoint_steps, args.adjoint_every)
+    if args.adjoint_moist_steps > 0:
+        line["adjoint_moist"] = adjoint_bench(torch, device, args.adjoint_moist_steps, args.adjoint_moist_every,
+                                              moist=True, size=args.adjoint_moist_size)
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(wl, args.cpu_steps)
     print(json.dumps(line), flush=True)
@@ -525,6 +536,9 @@ def main():
     ap.add_argument("--ensemble-steps", type=int, default=10)
     ap.add_argument("--adjoint-steps", type=int, default=500)
     ap.add_argument("--adjoint-every", type=int, default=50)
+    ap.add_argument("--adjoint-moist-steps", type=int, default=400)
+    ap.add_argument("--adjoint-moist-every", type=int, default=40)
+    ap.add_argument("--adjoint-moist-size", type=int, default=512, help="NX = NY of the moist adjoint case")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()

@@ -51,7 +51,8 @@ struct Lin : LinBase {
         cudaFuncSetAttribute(k_adj_ifft_y_out<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
         cudaFuncSetAttribute(k_thomas_adj<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
         cudaFuncSetAttribute(k_spectral_x_adj<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
-        cudaFuncSetAttribute(k_adj_advect<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+        cudaFuncSetAttribute(k_adj_advect<T, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+        cudaFuncSetAttribute(k_adj_advect<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
     }
     ~Lin() override
     {
@@ -299,9 +300,13 @@ struct Lin : LinBase {
             const unsigned char *qm = moist ? mrec + (size_t)st * N : nullptr;
             const T sdtg = (T)(step * e.cfg.dt * 9.8 * 0.5);
             k_lin_coef<T><<<cdiv(N, 128), 128, 0, s>>>(e.kp, R, coef);
-            k_adj_advect<T><<<gadv, AJ_THREADS, smem_adv, s>>>(e.kp, coef, fields(), qm, (T)step, sdtg,
-                                                               (first && st == 2) ? 0 : 1);
+            const int zc = (first && st == 2) ? 0 : 1;
+            k_adj_advect<T, 0><<<gadv, AJ_THREADS, smem_adv, s>>>(e.kp, coef, fields(), qm, (T)step, sdtg, zc);
             e.launches += 2;
+            if (moist) {
+                k_adj_advect<T, 1><<<gadv, AJ_THREADS, smem_adv, s>>>(e.kp, coef, fields(), qm, (T)step, sdtg, zc);
+                e.launches++;
+            }
         }
     }
 

@@ -392,9 +392,14 @@ __global__ void __launch_bounds__(128) k_adj_kessler(KParams<T> p, KFields<T> R,
 //   - the lateral ring of P-bar u, v, w is zeroed (mirror_boundaries wrote
 //     it; k_adj_div has already moved its values to the mirrored points).
 // ---------------------------------------------------------------------------
-constexpr int AJ_TI = 16, AJ_TJ = 16, AJ_TK = 4, AJ_THREADS = 256;
+// 8 levels per tile: a row of a tile is a whole 32-byte sector in FP32
+constexpr int AJ_TI = 16, AJ_TJ = 8, AJ_TK = 8, AJ_THREADS = 256;
 constexpr int AJ_CPT = AJ_TI * AJ_TJ * AJ_TK / AJ_THREADS;
-constexpr int AJ_NFACE = (AJ_TI + 1) * (AJ_TJ + 1) * (AJ_TK + 3);  // largest face box (z faces)
+constexpr int AJ_BOX_X = (AJ_TI + 5) * (AJ_TJ + 1) * AJ_TK;
+constexpr int AJ_BOX_Y = (AJ_TI + 1) * (AJ_TJ + 5) * AJ_TK;
+constexpr int AJ_BOX_Z = (AJ_TI + 1) * (AJ_TJ + 1) * (AJ_TK + 3);
+constexpr int AJ_NFACE = AJ_BOX_X > AJ_BOX_Y ? (AJ_BOX_X > AJ_BOX_Z ? AJ_BOX_X : AJ_BOX_Z)
+                                             : (AJ_BOX_Y > AJ_BOX_Z ? AJ_BOX_Y : AJ_BOX_Z);  // largest face box
 // box of tendency adjoints one equation's faces read: the tile + 3 points in
 // x and y, 2 below and 2 above
 constexpr int AJ_BI = AJ_TI + 6, AJ_BJ = AJ_TJ + 6, AJ_BK = AJ_TK + 4, AJ_NTB = AJ_BI * AJ_BJ * AJ_BK;
@@ -487,6 +492,7 @@ __device__ __forceinline__ void adj_family(const KParams<T> &p, const T *__restr
     constexpr int bnj = DIR == 1 ? AJ_TJ + 5 : AJ_TJ + 1;
     constexpr int bnk = DIR == 2 ? AJ_TK + 3 : AJ_TK;
     constexpr int nf = bni * bnj * bnk;
+    static_assert(nf <= AJ_NFACE, "face box larger than its shared-memory store");
     // offset of a face's own cell in the tendency box, and of its +1 neighbour
     constexpr int tstep = DIR == 0 ? AJ_BJ * AJ_BK : DIR == 1 ? AJ_BK : 1;
     const int bi0 = i0 - bdi, bj0 = j0 - bdj, bk0 = k0 - bdk;
@@ -639,27 +645,38 @@ __device__ __forceinline__ void adj_equation(const KParams<T> &p, const T *__res
     __syncthreads();
 }
 
-template <typename T>
-__global__ void __launch_bounds__(AJ_THREADS) k_adj_advect(KParams<T> p, const T *__restrict__ coef, KFields<T> A,
-                                                           const unsigned char *qm, T step, T sdtg, int zero_cur)
+// The adjoint advection runs as two launches over the same tiles: group 0
+// the momentum and theta equations (gathering into u, v, w, theta), group 1
+// the moisture equations (into u, v, w, qv, qc, qr), so that each keeps only
+// its own accumulators live.  Group 0 runs first: it replaces the stale
+// current-slot values (zero_cur) of u, v, w, theta and zeroes the mirror ring;
+// group 1 adds into u, v, w and replaces qv, qc, qr.
+template <typename T, int G>
+__global__ void __launch_bounds__(AJ_THREADS, sizeof(T) == 4 ? 3 : 2)
+    k_adj_advect(KParams<T> p, const T *__restrict__ coef, KFields<T> A, const unsigned char *qm, T step, T sdtg,
+                 int zero_cur)
 {
     extern __shared__ unsigned char smem_raw[];
     T *fs1 = (T *)smem_raw, *fs2 = fs1 + AJ_NFACE, *fab = fs2 + AJ_NFACE, *tb = fab + AJ_NFACE;
     const int ny = p.ny, nz = p.nz;
     const int i0 = blockIdx.x * AJ_TI, j0 = blockIdx.y * AJ_TJ, k0 = blockIdx.z * AJ_TK;
-    const int nf = p.moist ? 7 : 4;
     T acc[AJ_CPT][7];
 #pragma unroll
     for (int r = 0; r < AJ_CPT; r++)
+#pragma unroll
         for (int f = 0; f < 7; f++) acc[r][f] = T(0);
-    adj_equation<T, 0>(p, coef, A, qm, step, i0, j0, k0, tb, fs1, fs2, fab, acc);
-    adj_equation<T, 1>(p, coef, A, qm, step, i0, j0, k0, tb, fs1, fs2, fab, acc);
-    adj_equation<T, 2>(p, coef, A, qm, step, i0, j0, k0, tb, fs1, fs2, fab, acc);
-    if (p.moist) {
+    if (G == 0) {
+        adj_equation<T, 0>(p, coef, A, qm, step, i0, j0, k0, tb, fs1, fs2, fab, acc);
+        adj_equation<T, 1>(p, coef, A, qm, step, i0, j0, k0, tb, fs1, fs2, fab, acc);
+        adj_equation<T, 2>(p, coef, A, qm, step, i0, j0, k0, tb, fs1, fs2, fab, acc);
+    } else {
         adj_equation<T, 3>(p, coef, A, qm, step, i0, j0, k0, tb, fs1, fs2, fab, acc);
         adj_equation<T, 4>(p, coef, A, qm, step, i0, j0, k0, tb, fs1, fs2, fab, acc);
         adj_equation<T, 5>(p, coef, A, qm, step, i0, j0, k0, tb, fs1, fs2, fab, acc);
     }
+    // the fields this group gathers into
+    constexpr int NG = G == 0 ? 4 : 6;
+    constexpr int GF[2][6] = {{FU, FV, FW, FTH, -1, -1}, {FU, FV, FW, FQV, FQC, FQR}};
 #pragma unroll
     for (int r = 0; r < AJ_CPT; r++) {
         const int e = threadIdx.x + r * AJ_THREADS;
@@ -667,31 +684,35 @@ __global__ void __launch_bounds__(AJ_THREADS) k_adj_advect(KParams<T> p, const T
         if (pi >= p.nx || pj >= ny || pk >= nz) continue;
         T *a = acc[r];
         const int c = gix(ny, nz, pi, pj, pk);
-        // buoyancy of w into theta (and the moisture loading)
+        // buoyancy of w into theta (group 0) and the moisture loading (group 1)
         {
             T bw = T(0);
             if (adv_cell(p, pi, pj, pk, 2)) bw += A.P[FW][c];
             if (adv_cell(p, pi, pj, pk + 1, 2)) bw += A.P[FW][c + 1];
             if (bw != T(0)) {
-                a[FTH] += sdtg / p.tbv[pk] * bw;
-                if (p.moist) {
+                if (G == 0) {
+                    a[FTH] += sdtg / p.tbv[pk] * bw;
+                } else {
                     a[FQV] += sdtg * T(0.61) * bw;
                     a[FQC] -= sdtg * bw;
                     a[FQR] -= sdtg * bw;
                 }
             }
         }
-        const unsigned char bits = p.moist ? qm[c] : 0;
+        const unsigned char bits = G == 1 ? qm[c] : 0;
 #pragma unroll
-        for (int f = 0; f < 7; f++) {
-            if (f >= nf) break;
+        for (int g = 0; g < NG; g++) {
+            const int f = GF[G][g];
             const bool cell = adv_cell(p, pi, pj, pk, f == FW ? 2 : 1);
-            const int zb = f == FQV ? 1 : f == FQC ? 2 : f == FQR ? 4 : 0;
-            if (cell && !(bits & zb)) A.M[f][c] += A.P[f][c];
-            if (zero_cur && cell) A.cur[f][c] = a[f];
+            const bool mine = G == 0 || f >= FQV;  // fields this group folds and replaces
+            if (mine) {
+                const int zb = f == FQV ? 1 : f == FQC ? 2 : f == FQR ? 4 : 0;
+                if (cell && !(bits & zb)) A.M[f][c] += A.P[f][c];
+            }
+            if (mine && zero_cur && cell) A.cur[f][c] = a[f];
             else if (a[f] != T(0)) A.cur[f][c] += a[f];
         }
-        if (pk >= 1 && pk <= nz - 2 && (pi == 0 || pi == p.nx - 1 || pj == 0 || pj == ny - 1)) {
+        if (G == 0 && pk >= 1 && pk <= nz - 2 && (pi == 0 || pi == p.nx - 1 || pj == 0 || pj == ny - 1)) {
             A.P[FU][c] = T(0);
             A.P[FV][c] = T(0);
             A.P[FW][c] = T(0);
