@@ -267,14 +267,16 @@ struct Lin : LinBase {
         static const double steps[3] = {1. / 3., 0.5, 1.0};
         cudaStream_t s = e.stream;
         const bool moist = nf == 7;
-        const long ncolblk = cdiv((long)e.NX * e.NY, POST_COLS);
         const dim3 gadv(cdiv(e.NX, AJ_TI), cdiv(e.NY, AJ_TJ), cdiv(e.NZ, AJ_TK));
         const size_t smem_adv = (3 * (size_t)AJ_NFACE + AJ_NTB) * sizeof(T);
         swap_inner();  // advance_outer's swap
+        const int ncol = cdiv((long)e.NX * e.NY, 128);
+        k_adj_fold_m<T><<<cdiv(N, 256), 256, 0, s>>>(e.kp, fields());  // advance_outer's M <- P
+        e.launches++;
         if (moist) {
             // the step-final post, then Kessler (its inputs: rec + 3*nf*N);
             // pi-bar takes Kessler's pi row (first: on top of the final pi-bar)
-            k_adj_post<T><<<ncolblk, POST_THREADS, 0, s>>>(e.kp, fields(), AP_OUTER | AP_RAYLEIGH | AP_VBC | AP_SPONGE);
+            k_adj_cols<T><<<ncol, 128, 0, s>>>(e.kp, fields(), AP_RAYLEIGH | AP_VBC | AP_SPONGE);
             k_adj_kessler<T><<<cdiv(N, 128), 128, 0, s>>>(e.kp, e.fields(), rec + (size_t)3 * nf * N, fields(),
                                                          first ? 1 : 0);
             e.launches += 2;
@@ -287,11 +289,11 @@ struct Lin : LinBase {
             if (st == 2) {
                 if (moist) acc = 1;
                 else {
-                    fl = AP_OUTER | AP_RAYLEIGH | AP_VBC | AP_SPONGE2;
+                    fl = AP_RAYLEIGH | AP_VBC | AP_SPONGE2;
                     acc = first ? 1 : 0;
                 }
             }
-            k_adj_post<T><<<ncolblk, POST_THREADS, 0, s>>>(e.kp, fields(), fl);
+            k_adj_cols<T><<<ncol, 128, 0, s>>>(e.kp, fields(), fl);
             k_adj_project<T><<<cdiv(N, 256), 256, 0, s>>>(e.kp, fields(), (T)step, acc);
             e.launches += 2;
             adj_pressure(step);

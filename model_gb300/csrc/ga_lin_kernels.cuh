@@ -498,17 +498,30 @@ __device__ __forceinline__ void adj_family(const KParams<T> &p, const T *__restr
     const int bi0 = i0 - bdi, bj0 = j0 - bdj, bk0 = k0 - bdk;
     const int t = threadIdx.x;
     const T *ga_f = coef + (size_t)(2 * fam) * p.n, *gs_f = coef + (size_t)(2 * fam + 1) * p.n;
-#pragma unroll 2
-    for (int f = t; f < nf; f += AJ_THREADS) {
-        const int li = f / (bnk * bnj), lj = (f / bnk) % bnj, lk = f % bnk;
-        const int fi = bi0 + li, fj = bj0 + lj, fk = bk0 + lk;
-        const bool in = fi >= 0 && fi < p.nx && fj >= 0 && fj < p.ny && fk >= 0 && fk < p.nz;
-        T ga = T(0), gs = T(0);
-        if (in) {
-            const int c = gix(p.ny, p.nz, fi, fj, fk);
-            ga = ga_f[c];
-            gs = gs_f[c];
+    // this thread's coefficient pairs, all loads issued before any is used
+    constexpr int NPF = (nf + AJ_THREADS - 1) / AJ_THREADS;
+    T pga[NPF], pgs[NPF];
+#pragma unroll
+    for (int q = 0; q < NPF; q++) {
+        const int f = t + q * AJ_THREADS;
+        pga[q] = T(0);
+        pgs[q] = T(0);
+        if (f < nf) {
+            const int fi = bi0 + f / (bnk * bnj), fj = bj0 + (f / bnk) % bnj, fk = bk0 + f % bnk;
+            if (fi >= 0 && fi < p.nx && fj >= 0 && fj < p.ny && fk >= 0 && fk < p.nz) {
+                const int c = gix(p.ny, p.nz, fi, fj, fk);
+                pga[q] = ga_f[c];
+                pgs[q] = gs_f[c];
+            }
         }
+    }
+#pragma unroll
+    for (int q = 0; q < NPF; q++) {
+        const int f = t + q * AJ_THREADS;
+        if (f >= nf) break;
+        const int li = f / (bnk * bnj), lj = (f / bnk) % bnj, lk = f % bnk;
+        const int fk = bk0 + lk;
+        const T ga = pga[q], gs = pgs[q];
         const int tb0 = ((li + 3 - bdi) * AJ_BJ + (lj + 3 - bdj)) * AJ_BK + (lk + 2 - bdk);
         const T t0 = tb[tb0], t1 = tb[tb0 + tstep];
         T fb;
@@ -817,6 +830,78 @@ __global__ void __launch_bounds__(POST_THREADS) k_adj_post(KParams<T> p, KFields
             if (f >= nf) break;
             A.P[f][c] = vals[f][r];
             if (flags & AP_OUTER) A.M[f][c] = T(0);
+        }
+    }
+}
+
+// transpose of advance_outer's M <- P copy, every point: P-bar += M-bar,
+// M-bar = 0
+template <typename T>
+__global__ void k_adj_fold_m(KParams<T> p, KFields<T> A)
+{
+    const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= p.n) return;
+    const int nf = p.moist ? 7 : 4;
+    for (int f = 0; f < nf; f++) {
+        A.P[f][t] += A.M[f][t];
+        A.M[f][t] = T(0);
+    }
+}
+
+// The transposed column chain without the M fold: Rayleigh damping, the
+// top/bottom copies, the sponge strips (once, or twice with AP_SPONGE2), in
+// that order, for every linearised field.  One thread per column visits only
+// the levels these operators change: every level of a sponge-strip column,
+// otherwise levels 0, 1, NZ-2, NZ-1 and (Rayleigh) the damped levels.
+template <typename T>
+__global__ void k_adj_cols(KParams<T> p, KFields<T> A, int flags)
+{
+    const long col = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (col >= (long)p.nx * p.ny) return;
+    const int nz = p.nz, nf = p.moist ? 7 : 4;
+    const int i = (int)(col / p.ny), j = (int)(col % p.ny);
+    const bool hE = j >= 1 && i >= p.eb && i < p.ee, hW = j >= 1 && i >= p.wb && i < p.we;
+    const bool hS = i >= 1 && j >= p.sb && j < p.se, hN = i >= 1 && j >= p.nb && j < p.ne;
+    const int reps = (flags & AP_SPONGE2) ? 2 : (flags & AP_SPONGE) ? 1 : 0;
+    const bool strip = reps > 0 && (hE || hW || hS || hN);
+    const bool vbc = (flags & AP_VBC) && i >= 1 && j >= 1;
+    const bool rcol = (flags & AP_RAYLEIGH) && i >= 1 && i < p.nx - 1 && j >= 1 && j < p.ny - 1;
+    const long c0 = col * nz;
+    for (int f = 0; f < nf; f++) {
+        T *P = A.P[f];
+        const bool ray = rcol && f <= FTH;
+        auto pre = [&](int k) {
+            T v = P[c0 + k];
+            if (ray && k >= p.raylevel) {
+                const T cr = (f == FW) ? p.ray_w[k] : p.ray_u[k];
+                v = v - cr * v;
+            }
+            return v;
+        };
+        const T vb = vbc ? pre(0) : T(0), vt = vbc ? pre(nz - 1) : T(0);
+        // levels to visit: all (strip), else 0, 1 and from the first damped or
+        // top-copy level up
+        const int kup = strip ? 2 : min(nz - 2, ray ? max(p.raylevel, 2) : nz - 2);
+        for (int k = 0; k < nz; k++) {
+            if (!strip && k >= 2 && k < kup) k = kup;
+            T v = pre(k);
+            if (vbc) {
+                if (f == FW) {
+                    if (k == 0 || k == 1 || k == nz - 1) v = T(0);
+                } else {
+                    if (k == 0 || k == nz - 1) v = T(0);
+                    else if (k == 1) v = v + vb;
+                    else if (k == nz - 2) v = v + vt;
+                }
+            }
+            if (strip && k >= 1)
+                for (int rp = 0; rp < reps; rp++) {
+                    if (hN) v = v - p.cn[j - p.nb] * v;
+                    if (hS) v = v - p.cs[j - p.sb] * v;
+                    if (hW) v = v - p.cw[i - p.wb] * v;
+                    if (hE) v = v - p.ce[i - p.eb] * v;
+                }
+            P[c0 + k] = v;
         }
     }
 }
