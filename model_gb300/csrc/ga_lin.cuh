@@ -270,7 +270,7 @@ struct Lin : LinBase {
         const dim3 gadv(cdiv(e.NX, AJ_TI), cdiv(e.NY, AJ_TJ), cdiv(e.NZ, AJ_TK));
         const size_t smem_adv = (3 * (size_t)AJ_NFACE + AJ_NTB) * sizeof(T);
         swap_inner();  // advance_outer's swap
-        const int ncol = cdiv((long)e.NX * e.NY, 128);
+        const int ncol = cdiv((long)e.NX * e.NY * nf, 128);  // threads of k_adj_cols: (field, column)
         k_adj_fold_m<T><<<cdiv(N, 256), 256, 0, s>>>(e.kp, fields());  // advance_outer's M <- P
         e.launches++;
         if (moist) {

@@ -405,11 +405,19 @@ constexpr int AJ_NFACE = AJ_BOX_X > AJ_BOX_Y ? (AJ_BOX_X > AJ_BOX_Z ? AJ_BOX_X :
 constexpr int AJ_BI = AJ_TI + 6, AJ_BJ = AJ_TJ + 6, AJ_BK = AJ_TK + 4, AJ_NTB = AJ_BI * AJ_BJ * AJ_BK;
 
 // The two coefficients of every linearised face, once per stage: for each
-// cell c and face family fam = 3*EQ + DIR, coef[(2*fam)*N + c] = B + S and
-// coef[(2*fam + 1)*N + c] = ab + a of the face at c (its sign is the frozen
-// upwind sign), zero where the face is not next to an advected cell.
-constexpr int LIN_NCOEF = 18;        // dry: 9 families x 2
-constexpr int LIN_NCOEF_MOIST = 37;  // moist: 18 families x 2 + d(fall speed)/d(rain) per cell
+// cell c and face family (EQ, DIR), coef[GA*N + c] = B + S and
+// coef[GS*N + c] = ab + a of the face at c (its sign is the frozen upwind
+// sign), zero where the face is not next to an advected cell.  The scalar
+// equations (theta, qv, qc, qr) share ab + a on every face but the rain's
+// vertical one, so those are stored once per direction (LinSlot).
+constexpr int LIN_NCOEF = 18;        // dry: u, v (6 families x 2), scalar ab+a (3), theta B+S (3)
+constexpr int LIN_NCOEF_MOIST = 29;  // moist: + qv, qc, qr B+S (9), rain vertical ab+a, d(fall speed)/d(rain)
+constexpr int LIN_DVT_SLOT = 28;
+template <int EQ, int DIR> struct LinSlot {
+    static constexpr int GA = EQ < 2 ? 2 * (3 * EQ + DIR) : 15 + 3 * (EQ - 2) + DIR;
+    static constexpr int GS = EQ < 2 ? 2 * (3 * EQ + DIR) + 1 : (EQ == 5 && DIR == 2) ? 27 : 12 + DIR;
+    static constexpr bool OWNS_GS = EQ < 3 || (EQ == 5 && DIR == 2);  // the family that writes GS
+};
 
 template <typename T, int EQ, int DIR>
 __device__ __forceinline__ void lin_coef_face(const KParams<T> &p, const KFields<T> &R, T *coef, int i, int j, int k,
@@ -425,9 +433,8 @@ __device__ __forceinline__ void lin_coef_face(const KParams<T> &p, const KFields
         ga = L.ga;
         gs = L.gs;
     }
-    constexpr int fam = 3 * EQ + DIR;
-    coef[(size_t)(2 * fam) * p.n + c] = ga;
-    coef[(size_t)(2 * fam + 1) * p.n + c] = gs;
+    coef[(size_t)LinSlot<EQ, DIR>::GA * p.n + c] = ga;
+    if (LinSlot<EQ, DIR>::OWNS_GS) coef[(size_t)LinSlot<EQ, DIR>::GS * p.n + c] = gs;
 }
 
 template <typename T>
@@ -458,7 +465,7 @@ __global__ void k_lin_coef(KParams<T> p, KFields<T> R, T *coef)
         lin_coef_face<T, 5, 1>(p, R, coef, i, j, k, c);
         lin_coef_face<T, 5, 2>(p, R, coef, i, j, k, c);
         const bool inner = i >= 3 && i < p.nx - 3 && j >= 3 && j < p.ny - 3;
-        coef[(size_t)36 * p.n + c] = inner ? lin_dvt(p, R, c - k, k) : T(0);
+        coef[(size_t)LIN_DVT_SLOT * p.n + c] = inner ? lin_dvt(p, R, c - k, k) : T(0);
     }
 }
 
@@ -485,7 +492,6 @@ __device__ __forceinline__ void adj_family(const KParams<T> &p, const T *__restr
                                            int j0, int k0, T *fs1, T *fs2, T *fab, T (&acc)[AJ_CPT][7])
 {
     constexpr int XF = LinEq<EQ>::FX;
-    constexpr int fam = 3 * EQ + DIR;
     constexpr bool RAIN_Z = EQ == 5 && DIR == 2;
     constexpr int bdi = DIR == 0 ? 3 : 0, bdj = DIR == 1 ? 3 : 0, bdk = DIR == 2 ? 2 : 0;
     constexpr int bni = DIR == 0 ? AJ_TI + 5 : AJ_TI + 1;
@@ -497,7 +503,7 @@ __device__ __forceinline__ void adj_family(const KParams<T> &p, const T *__restr
     constexpr int tstep = DIR == 0 ? AJ_BJ * AJ_BK : DIR == 1 ? AJ_BK : 1;
     const int bi0 = i0 - bdi, bj0 = j0 - bdj, bk0 = k0 - bdk;
     const int t = threadIdx.x;
-    const T *ga_f = coef + (size_t)(2 * fam) * p.n, *gs_f = coef + (size_t)(2 * fam + 1) * p.n;
+    const T *ga_f = coef + (size_t)LinSlot<EQ, DIR>::GA * p.n, *gs_f = coef + (size_t)LinSlot<EQ, DIR>::GS * p.n;
     // this thread's coefficient pairs, all loads issued before any is used
     constexpr int NPF = (nf + AJ_THREADS - 1) / AJ_THREADS;
     T pga[NPF], pgs[NPF];
@@ -591,7 +597,7 @@ __device__ __forceinline__ void adj_family(const KParams<T> &p, const T *__restr
                 // levels 1..NZ-2 follows their rain (face 0 holds level 1 twice)
                 ga = pk >= 2 ? fab[at(0, 0, -1)] : T(0);
                 if (pk >= 1 && pk <= nz - 2) {
-                    const T dv = coef[(size_t)36 * p.n + gix(p.ny, p.nz, i0 + li, j0 + lj, pk)];
+                    const T dv = coef[(size_t)LIN_DVT_SLOT * p.n + gix(p.ny, p.nz, i0 + li, j0 + lj, pk)];
                     const T below = fab[at(0, 0, -1)] * (pk == 1 ? T(2) : T(1));
                     gx -= T(0.5) * dv * (fab[at(0, 0, 0)] + below);
                 }
@@ -850,15 +856,21 @@ __global__ void k_adj_fold_m(KParams<T> p, KFields<T> A)
 
 // The transposed column chain without the M fold: Rayleigh damping, the
 // top/bottom copies, the sponge strips (once, or twice with AP_SPONGE2), in
-// that order, for every linearised field.  One thread per column visits only
-// the levels these operators change: every level of a sponge-strip column,
-// otherwise levels 0, 1, NZ-2, NZ-1 and (Rayleigh) the damped levels.
+// that order, for every linearised field.  One thread per (field, column)
+// visits only the levels these operators change: every level of a
+// sponge-strip column, otherwise levels 0, 1, NZ-2, NZ-1 and (Rayleigh) the
+// damped levels.
 template <typename T>
 __global__ void k_adj_cols(KParams<T> p, KFields<T> A, int flags)
 {
-    const long col = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (col >= (long)p.nx * p.ny) return;
-    const int nz = p.nz, nf = p.moist ? 7 : 4;
+    // one thread per (field, column)
+    const int nf = p.moist ? 7 : 4;
+    const long ncols = (long)p.nx * p.ny;
+    const long tid = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid >= ncols * nf) return;
+    const long col = tid % ncols;
+    const int fsel = (int)(tid / ncols);
+    const int nz = p.nz;
     const int i = (int)(col / p.ny), j = (int)(col % p.ny);
     const bool hE = j >= 1 && i >= p.eb && i < p.ee, hW = j >= 1 && i >= p.wb && i < p.we;
     const bool hS = i >= 1 && j >= p.sb && j < p.se, hN = i >= 1 && j >= p.nb && j < p.ne;
@@ -867,7 +879,7 @@ __global__ void k_adj_cols(KParams<T> p, KFields<T> A, int flags)
     const bool vbc = (flags & AP_VBC) && i >= 1 && j >= 1;
     const bool rcol = (flags & AP_RAYLEIGH) && i >= 1 && i < p.nx - 1 && j >= 1 && j < p.ny - 1;
     const long c0 = col * nz;
-    for (int f = 0; f < nf; f++) {
+    for (int f = fsel; f <= fsel; f++) {
         T *P = A.P[f];
         const bool ray = rcol && f <= FTH;
         auto pre = [&](int k) {
