@@ -268,7 +268,7 @@ struct Lin : LinBase {
         cudaStream_t s = e.stream;
         const bool moist = nf == 7;
         const dim3 gadv(cdiv(e.NX, AJ_TI), cdiv(e.NY, AJ_TJ), cdiv(e.NZ, AJ_TK));
-        const size_t smem_adv = (3 * (size_t)AJ_NFACE + AJ_NTB) * sizeof(T);
+        const size_t smem_adv = AjCfg<T>::smem;
         swap_inner();  // advance_outer's swap
         const int ncol = cdiv((long)e.NX * e.NY * nf, 128);  // threads of k_adj_cols: (field, column)
         k_adj_fold_m<T><<<cdiv(N, 256), 256, 0, s>>>(e.kp, fields());  // advance_outer's M <- P
@@ -301,12 +301,12 @@ struct Lin : LinBase {
             for (int f = 0; f < nf; f++) R.cur[f] = const_cast<T *>(rec) + (size_t)(nf * st + f) * N;
             const unsigned char *qm = moist ? mrec + (size_t)st * N : nullptr;
             const T sdtg = (T)(step * e.cfg.dt * 9.8 * 0.5);
-            k_lin_coef<T><<<cdiv(N, 128), 128, 0, s>>>(e.kp, R, coef);
+            k_lin_coef<T><<<cdiv(N, 128), 128, 0, s>>>(e.kp, R, coef, fields(), qm);
             const int zc = (first && st == 2) ? 0 : 1;
-            k_adj_advect<T, 0><<<gadv, AJ_THREADS, smem_adv, s>>>(e.kp, coef, fields(), qm, (T)step, sdtg, zc);
+            k_adj_advect<T, 0><<<gadv, AJ_THREADS, smem_adv, s>>>(e.kp, coef, fields(), (T)step, sdtg, zc);
             e.launches += 2;
             if (moist) {
-                k_adj_advect<T, 1><<<gadv, AJ_THREADS, smem_adv, s>>>(e.kp, coef, fields(), qm, (T)step, sdtg, zc);
+                k_adj_advect<T, 1><<<gadv, AJ_THREADS, smem_adv, s>>>(e.kp, coef, fields(), (T)step, sdtg, zc);
                 e.launches++;
             }
         }

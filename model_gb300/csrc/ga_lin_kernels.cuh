@@ -437,8 +437,12 @@ __device__ __forceinline__ void lin_coef_face(const KParams<T> &p, const KFields
     if (LinSlot<EQ, DIR>::OWNS_GS) coef[(size_t)LinSlot<EQ, DIR>::GS * p.n + c] = gs;
 }
 
+// The moist pass also zeroes P-bar of qv, qc, qr at the advected points
+// the stage's zero_moisture clipped (qm bits 1, 2, 4): the clipped value does
+// not depend on the advection, so its adjoint reaches neither the tendency
+// nor the M fold.
 template <typename T>
-__global__ void k_lin_coef(KParams<T> p, KFields<T> R, T *coef)
+__global__ void k_lin_coef(KParams<T> p, KFields<T> R, T *coef, KFields<T> A, const unsigned char *qm)
 {
     const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= p.n) return;
@@ -466,154 +470,109 @@ __global__ void k_lin_coef(KParams<T> p, KFields<T> R, T *coef)
         lin_coef_face<T, 5, 2>(p, R, coef, i, j, k, c);
         const bool inner = i >= 3 && i < p.nx - 3 && j >= 3 && j < p.ny - 3;
         coef[(size_t)LIN_DVT_SLOT * p.n + c] = inner ? lin_dvt(p, R, c - k, k) : T(0);
-    }
-}
-
-// tendency adjoints of equation EQ (zero off the advected cells) over the box
-template <typename T, int EQ>
-__device__ __forceinline__ void adj_stage_tbar(const KParams<T> &p, const KFields<T> &A, const unsigned char *qm,
-                                               T step, int i0, int j0, int k0, T *tb)
-{
-    constexpr int XF = LinEq<EQ>::FX, ZB = LinEq<EQ>::ZBIT;
-    const T *P = A.P[XF];
-    for (int e = threadIdx.x; e < AJ_NTB; e += AJ_THREADS) {
-        const int i = i0 - 3 + e / (AJ_BK * AJ_BJ), j = j0 - 3 + (e / AJ_BK) % AJ_BJ, k = k0 - 2 + e % AJ_BK;
-        T v = T(0);
-        if (adv_cell(p, i, j, k, 1)) {
-            const int c = gix(p.ny, p.nz, i, j, k);
-            if (!ZB || !(qm[c] & ZB)) v = step * P[c];  // a clipped point has no tendency adjoint
+        const unsigned char b = qm[c];
+        if (b && adv_cell(p, i, j, k, 1)) {
+            if (b & 1) A.P[FQV][c] = T(0);
+            if (b & 2) A.P[FQC][c] = T(0);
+            if (b & 4) A.P[FQR][c] = T(0);
         }
-        tb[e] = v;
     }
 }
 
-template <typename T, int EQ, int DIR>
-__device__ __forceinline__ void adj_family(const KParams<T> &p, const T *__restrict__ coef, const T *tb, int i0,
-                                           int j0, int k0, T *fs1, T *fs2, T *fab, T (&acc)[AJ_CPT][7])
+// asynchronous element copy global -> shared (cp.async), zero-filled where
+// `ok` is false (src is then a placeholder address and is not read)
+template <typename T>
+__device__ __forceinline__ void cp_elem(T *dst, const T *src, bool ok)
 {
-    constexpr int XF = LinEq<EQ>::FX;
-    constexpr bool RAIN_Z = EQ == 5 && DIR == 2;
-    constexpr int bdi = DIR == 0 ? 3 : 0, bdj = DIR == 1 ? 3 : 0, bdk = DIR == 2 ? 2 : 0;
-    constexpr int bni = DIR == 0 ? AJ_TI + 5 : AJ_TI + 1;
-    constexpr int bnj = DIR == 1 ? AJ_TJ + 5 : AJ_TJ + 1;
-    constexpr int bnk = DIR == 2 ? AJ_TK + 3 : AJ_TK;
-    constexpr int nf = bni * bnj * bnk;
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    const int n = ok ? (int)sizeof(T) : 0;
+    if (sizeof(T) == 4)
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(d), "l"(src), "r"(n) : "memory");
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(d), "l"(src), "r"(n) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_wait()
+{
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+// Shared memory of k_adj_advect.  FP32 double-buffers the coefficient and
+// tendency boxes (the next family's copies run under the current one's
+// work, 3 blocks per SM); FP64 has one of each (2 blocks per SM) and copies
+// the next family's coefficients during the current gather, so it keeps the
+// face signs in an array of their own (fs2).
+template <typename T>
+struct AjCfg {
+    static constexpr int CB = sizeof(T) == 4 ? 2 : 1;   // coefficient box buffers (B+S and ab+a each)
+    static constexpr int TBB = sizeof(T) == 4 ? 2 : 1;  // tendency box buffers
+    static constexpr int NFS = CB == 1 ? 3 : 2;          // face arrays: fs1, fab (+ fs2)
+    static constexpr int NZF = AJ_TK + 3;                // z faces of a tile column (level factors)
+    static constexpr int FS = 2 * CB * AJ_NFACE, TB = FS + NFS * AJ_NFACE, ZF = TB + TBB * AJ_NTB;
+    static constexpr size_t smem = (size_t)(ZF + 2 * NZF) * sizeof(T);
+};
+
+// face-box geometry of the family (EQ, DIR): the tile plus the faces whose
+// stencil reaches it (3 before and 2 after in x and y, 2 below and 1 above in z)
+template <int DIR>
+struct AjBox {
+    static constexpr int bdi = DIR == 0 ? 3 : 0, bdj = DIR == 1 ? 3 : 0, bdk = DIR == 2 ? 2 : 0;
+    static constexpr int bni = DIR == 0 ? AJ_TI + 5 : AJ_TI + 1;
+    static constexpr int bnj = DIR == 1 ? AJ_TJ + 5 : AJ_TJ + 1;
+    static constexpr int bnk = DIR == 2 ? AJ_TK + 3 : AJ_TK;
+    static constexpr int nf = bni * bnj * bnk;
+    static constexpr int NPF = (nf + AJ_THREADS - 1) / AJ_THREADS;
     static_assert(nf <= AJ_NFACE, "face box larger than its shared-memory store");
-    // offset of a face's own cell in the tendency box, and of its +1 neighbour
-    constexpr int tstep = DIR == 0 ? AJ_BJ * AJ_BK : DIR == 1 ? AJ_BK : 1;
-    const int bi0 = i0 - bdi, bj0 = j0 - bdj, bk0 = k0 - bdk;
-    const int t = threadIdx.x;
+};
+
+// copies of the family's two coefficient boxes (zero off the domain)
+template <typename T, int EQ, int DIR>
+__device__ __forceinline__ void issue_coef(const KParams<T> &p, const T *__restrict__ coef, int i0, int j0, int k0,
+                                           T *cb)
+{
+    using B = AjBox<DIR>;
     const T *ga_f = coef + (size_t)LinSlot<EQ, DIR>::GA * p.n, *gs_f = coef + (size_t)LinSlot<EQ, DIR>::GS * p.n;
-    // this thread's coefficient pairs, all loads issued before any is used
-    constexpr int NPF = (nf + AJ_THREADS - 1) / AJ_THREADS;
-    T pga[NPF], pgs[NPF];
-#pragma unroll
-    for (int q = 0; q < NPF; q++) {
-        const int f = t + q * AJ_THREADS;
-        pga[q] = T(0);
-        pgs[q] = T(0);
-        if (f < nf) {
-            const int fi = bi0 + f / (bnk * bnj), fj = bj0 + (f / bnk) % bnj, fk = bk0 + f % bnk;
-            if (fi >= 0 && fi < p.nx && fj >= 0 && fj < p.ny && fk >= 0 && fk < p.nz) {
-                const int c = gix(p.ny, p.nz, fi, fj, fk);
-                pga[q] = ga_f[c];
-                pgs[q] = gs_f[c];
-            }
+    const int bi0 = i0 - B::bdi, bj0 = j0 - B::bdj, bk0 = k0 - B::bdk;
+    // not unrolled: the copies are asynchronous, and an unrolled issue holds
+    // every address in registers at once
+#pragma unroll 1
+    for (int q = 0; q < B::NPF; q++) {
+        const int f = threadIdx.x + q * AJ_THREADS;
+        if (f < B::nf) {
+            const int fi = bi0 + f / (B::bnk * B::bnj), fj = bj0 + (f / B::bnk) % B::bnj, fk = bk0 + f % B::bnk;
+            const bool ok = fi >= 0 && fi < p.nx && fj >= 0 && fj < p.ny && fk >= 0 && fk < p.nz;
+            const int c = ok ? gix(p.ny, p.nz, fi, fj, fk) : 0;
+            cp_elem(cb + f, ga_f + c, ok);
+            cp_elem(cb + AJ_NFACE + f, gs_f + c, ok);
         }
     }
-#pragma unroll
-    for (int q = 0; q < NPF; q++) {
-        const int f = t + q * AJ_THREADS;
-        if (f >= nf) break;
-        const int li = f / (bnk * bnj), lj = (f / bnk) % bnj, lk = f % bnk;
-        const int fk = bk0 + lk;
-        const T ga = pga[q], gs = pgs[q];
-        const int tb0 = ((li + 3 - bdi) * AJ_BJ + (lj + 3 - bdj)) * AJ_BK + (lk + 2 - bdk);
-        const T t0 = tb[tb0], t1 = tb[tb0 + tstep];
-        T fb;
-        if (DIR == 0) fb = p.dtx * (t1 - t0);
-        else if (DIR == 1) fb = p.dty * (t1 - t0);
-        else {
-            fb = T(0);
-            if (t0 != T(0)) fb -= (p.dtz * p.mu[fk]) * p.rhow[fk + 1] * p.one_d_rhou[fk] * t0;
-            if (t1 != T(0)) fb += (p.dtz * p.mu[fk + 1]) * p.rhow[fk + 1] * p.one_d_rhou[fk + 1] * t1;
+}
+
+// copy of equation EQ's P-bar over the tendency box, zero off the advected
+// cells: times the stage's step it is the tendency adjoint.  The moisture
+// fields hold no P-bar at their clipped points (k_lin_coef zeroes it).
+template <typename T, int EQ>
+__device__ __forceinline__ void issue_tb(const KParams<T> &p, const KFields<T> &A, int i0, int j0, int k0, T *tb)
+{
+    const T *P = A.P[LinEq<EQ>::FX];
+    constexpr int NQ = (AJ_NTB + AJ_THREADS - 1) / AJ_THREADS;
+#pragma unroll 1
+    for (int q = 0; q < NQ; q++) {
+        const int e = threadIdx.x + q * AJ_THREADS;
+        if (e < AJ_NTB) {
+            const int i = i0 - 3 + e / (AJ_BK * AJ_BJ), j = j0 - 3 + (e / AJ_BK) % AJ_BJ, k = k0 - 2 + e % AJ_BK;
+            const bool ok = adv_cell(p, i, j, k, 1);
+            cp_elem(tb + e, P + (ok ? gix(p.ny, p.nz, i, j, k) : 0), ok);
         }
-        const T s1 = fb * gs;
-        fs1[f] = s1;
-        fs2[f] = (DIR == 2 && (fk <= 1 || fk == p.nz - 2)) ? T(0) : (gs > T(0) ? s1 : -s1);
-        fab[f] = fb * ga;
     }
-    __syncthreads();
-    const T C5[6] = {W<T>::c1_60, -W<T>::c2_15, W<T>::c37_60, W<T>::c37_60, -W<T>::c2_15, W<T>::c1_60};
-    const T U5[6] = {W<T>::c1_60, T(-5) * W<T>::c1_60, T(10) * W<T>::c1_60, T(-10) * W<T>::c1_60,
-                     T(5) * W<T>::c1_60, -W<T>::c1_60};
-    const T C3[4] = {-W<T>::c1_12, W<T>::c7_12, W<T>::c7_12, -W<T>::c1_12};
-    const T U3[4] = {-W<T>::c1_12, T(3) * W<T>::c1_12, T(-3) * W<T>::c1_12, W<T>::c1_12};
-    const int nz = p.nz;
-#pragma unroll
-    for (int r = 0; r < AJ_CPT; r++) {
-        const int e = t + r * AJ_THREADS;
-        const int li = e / (AJ_TK * AJ_TJ), lj = (e / AJ_TK) % AJ_TJ, lk = e % AJ_TK;
-        // face-box coordinates of the cell
-        const int bi = li + bdi, bj = lj + bdj, bk = lk + bdk;
-        auto at = [&](int di, int dj, int dk) { return ((bi + di) * bnj + (bj + dj)) * bnk + (bk + dk); };
-        T gx = T(0), ga;
-        if (DIR == 0) {
-#pragma unroll
-            for (int m = 0; m < 6; m++) {
-                const int w = at(2 - m, 0, 0);
-                gx += C5[m] * fs1[w] + U5[m] * fs2[w];
-            }
-            if (EQ == 0) ga = T(0.5) * (fab[at(-1, 0, 0)] + fab[at(0, 0, 0)]);
-            else if (EQ == 1) ga = T(0.5) * (fab[at(-1, 0, 0)] + fab[at(-1, 1, 0)]);
-            else ga = fab[at(-1, 0, 0)];
-        } else if (DIR == 1) {
-#pragma unroll
-            for (int m = 0; m < 6; m++) {
-                const int w = at(0, 2 - m, 0);
-                gx += C5[m] * fs1[w] + U5[m] * fs2[w];
-            }
-            if (EQ == 0) ga = T(0.5) * (fab[at(0, -1, 0)] + fab[at(1, -1, 0)]);
-            else if (EQ == 1) ga = T(0.5) * (fab[at(0, -1, 0)] + fab[at(0, 0, 0)]);
-            else ga = fab[at(0, -1, 0)];
-        } else {
-            const int pk = k0 + lk;
-#pragma unroll
-            for (int d = -2; d <= 1; d++) {
-                const int fk = pk + d;
-                if (fk < (RAIN_Z ? 0 : 1) || fk > nz - 2) continue;
-                const int w = at(0, 0, d);
-                if (fk <= 1 || fk == nz - 2) {  // 2nd order (and the rain's bottom outflow)
-                    if (d == 0 || d == -1) gx += T(0.5) * fs1[w];
-                } else {
-                    const int m = 1 - d;  // position of the cell in the face's stencil fk-1..fk+2
-                    gx += C3[m] * fs1[w] + U3[m] * fs2[w];
-                }
-            }
-            if (EQ == 0) ga = T(0.5) * (fab[at(0, 0, -1)] + fab[at(1, 0, -1)]);
-            else if (EQ == 1) ga = T(0.5) * (fab[at(0, 0, -1)] + fab[at(0, 1, -1)]);
-            else if (RAIN_Z) {
-                // the bottom outflow does not depend on w; the fall speed of
-                // levels 1..NZ-2 follows their rain (face 0 holds level 1 twice)
-                ga = pk >= 2 ? fab[at(0, 0, -1)] : T(0);
-                if (pk >= 1 && pk <= nz - 2) {
-                    const T dv = coef[(size_t)LIN_DVT_SLOT * p.n + gix(p.ny, p.nz, i0 + li, j0 + lj, pk)];
-                    const T below = fab[at(0, 0, -1)] * (pk == 1 ? T(2) : T(1));
-                    gx -= T(0.5) * dv * (fab[at(0, 0, 0)] + below);
-                }
-            } else ga = fab[at(0, 0, -1)];
-        }
-        acc[r][XF] += gx;
-        acc[r][DIR] += ga;
-    }
-    __syncthreads();
 }
 
 // the terms of equation EQ outside the face fluxes, from its tendency box:
 // Coriolis of u into v and of v into u (advection.cpp:84-92, 112-120), the
 // vertical advection of the basic-state theta (Z_ADVECT_BASE) into w
 template <typename T, int EQ>
-__device__ __forceinline__ void adj_extra(const KParams<T> &p, const T *tb, int i0, int j0, int k0,
+__device__ __forceinline__ void adj_extra(const KParams<T> &p, const T *tb, T step, int i0, int j0, int k0,
                                           T (&acc)[AJ_CPT][7])
 {
     const T fdt = p.dt * T(0.25);
@@ -622,7 +581,9 @@ __device__ __forceinline__ void adj_extra(const KParams<T> &p, const T *tb, int 
         const int e = threadIdx.x + r * AJ_THREADS;
         const int li = e / (AJ_TK * AJ_TJ), lj = (e / AJ_TK) % AJ_TJ, lk = e % AJ_TK;
         const int pj = j0 + lj, pk = k0 + lk;
-        auto TB = [&](int di, int dj, int dk) { return tb[((li + 3 + di) * AJ_BJ + (lj + 3 + dj)) * AJ_BK + lk + 2 + dk]; };
+        auto TB = [&](int di, int dj, int dk) {
+            return step * tb[((li + 3 + di) * AJ_BJ + (lj + 3 + dj)) * AJ_BK + lk + 2 + dk];
+        };
         if (EQ == 0) {
             const int di[4] = {0, 0, 1, 1}, dj[4] = {0, -1, 0, -1};
 #pragma unroll
@@ -650,18 +611,151 @@ __device__ __forceinline__ void adj_extra(const KParams<T> &p, const T *tb, int 
     }
 }
 
-template <typename T, int EQ>
-__device__ __forceinline__ void adj_equation(const KParams<T> &p, const T *__restrict__ coef, const KFields<T> &A,
-                                             const unsigned char *qm, T step, int i0, int j0, int k0, T *tb, T *fs1,
-                                             T *fs2, T *fab, T (&acc)[AJ_CPT][7])
+// One face family (EQ, DIR) of group G: wait for its coefficient box (and,
+// for DIR 0, the equation's tendency box), start the copies of the next
+// family's, evaluate the adjoint of every face of the box into shared memory
+// (S' = Fbar*(ab+a), a' = Fbar*(B+S)), then every cell of the tile gathers
+// what reaches it.
+template <typename T, int G, int EQ, int DIR>
+__device__ __forceinline__ void adj_family(const KParams<T> &p, const T *__restrict__ coef, const KFields<T> &A,
+                                           T step, int i0, int j0, int k0, T *sm, T (&acc)[AJ_CPT][7])
 {
-    adj_stage_tbar<T, EQ>(p, A, qm, step, i0, j0, k0, tb);
+    using C = AjCfg<T>;
+    using B = AjBox<DIR>;
+    constexpr int EQ0 = 3 * G, n = 3 * (EQ - EQ0) + DIR;
+    constexpr bool HAS_NEXT = n < 8, NEXT_EQ = DIR == 2 && EQ < EQ0 + 2;
+    constexpr int NEQ = DIR == 2 ? EQ + 1 : EQ, NDIR = (DIR + 1) % 3;
+    constexpr int XF = LinEq<EQ>::FX;
+    constexpr bool RAIN_Z = EQ == 5 && DIR == 2;
+    const T *cga = sm + (n % C::CB) * 2 * AJ_NFACE, *cgs = cga + AJ_NFACE;
+    T *fs1 = sm + C::FS, *fab = fs1 + AJ_NFACE, *fs2 = fab + AJ_NFACE;
+    const T *tb = sm + C::TB + ((EQ - EQ0) % C::TBB) * AJ_NTB;
+    const T *zf0 = sm + C::ZF, *zf1 = zf0 + C::NZF;
+    const int nz = p.nz, t = threadIdx.x;
+    if (C::CB == 2) {
+        if (HAS_NEXT) issue_coef<T, NEQ, NDIR>(p, coef, i0, j0, k0, sm + ((n + 1) % 2) * 2 * AJ_NFACE);
+        if (C::TBB == 2 && DIR == 0 && EQ < EQ0 + 2)
+            issue_tb<T, (EQ < EQ0 + 2 ? EQ + 1 : EQ)>(p, A, i0, j0, k0, sm + C::TB + ((EQ + 1 - EQ0) % 2) * AJ_NTB);
+        cp_commit();
+        cp_wait<1>();
+    } else {
+        cp_wait<0>();
+    }
+    // the rain's fall-speed derivative at the tile's cells
+    T dvr[AJ_CPT];
+    if (RAIN_Z) {
+#pragma unroll
+        for (int r = 0; r < AJ_CPT; r++) {
+            const int e = t + r * AJ_THREADS;
+            const int pi = i0 + e / (AJ_TK * AJ_TJ), pj = j0 + (e / AJ_TK) % AJ_TJ, pk = k0 + e % AJ_TK;
+            dvr[r] = (pi < p.nx && pj < p.ny && pk >= 1 && pk <= nz - 2)
+                         ? coef[(size_t)LIN_DVT_SLOT * p.n + gix(p.ny, nz, pi, pj, pk)]
+                         : T(0);
+        }
+    }
     __syncthreads();
-    adj_family<T, EQ, 0>(p, coef, tb, i0, j0, k0, fs1, fs2, fab, acc);
-    adj_family<T, EQ, 1>(p, coef, tb, i0, j0, k0, fs1, fs2, fab, acc);
-    adj_family<T, EQ, 2>(p, coef, tb, i0, j0, k0, fs1, fs2, fab, acc);
-    adj_extra<T, EQ>(p, tb, i0, j0, k0, acc);
+    if (DIR == 0) adj_extra<T, EQ>(p, tb, step, i0, j0, k0, acc);
+    // offset of a face's own cell in the tendency box, and of its +1 neighbour
+    constexpr int tstep = DIR == 0 ? AJ_BJ * AJ_BK : DIR == 1 ? AJ_BK : 1;
+#pragma unroll
+    for (int q = 0; q < B::NPF; q++) {
+        const int f = t + q * AJ_THREADS;
+        if (f >= B::nf) break;
+        const int li = f / (B::bnk * B::bnj), lj = (f / B::bnk) % B::bnj, lk = f % B::bnk;
+        const T ga = cga[f], gs = cgs[f];
+        const int tb0 = ((li + 3 - B::bdi) * AJ_BJ + (lj + 3 - B::bdj)) * AJ_BK + (lk + 2 - B::bdk);
+        const T t0 = step * tb[tb0], t1 = step * tb[tb0 + tstep];
+        T fb;
+        if (DIR == 0) fb = p.dtx * (t1 - t0);
+        else if (DIR == 1) fb = p.dty * (t1 - t0);
+        else fb = zf1[lk] * t1 - zf0[lk] * t0;
+        const T s1 = fb * gs;
+        fs1[f] = s1;
+        if (C::CB == 1) fs2[f] = gs > T(0) ? s1 : -s1;
+        fab[f] = fb * ga;
+    }
     __syncthreads();
+    if (C::CB == 1) {
+        // the face phase has read the coefficient and tendency boxes
+        if (HAS_NEXT) issue_coef<T, NEQ, NDIR>(p, coef, i0, j0, k0, sm);
+        if (NEXT_EQ) issue_tb<T, (NEXT_EQ ? EQ + 1 : EQ)>(p, A, i0, j0, k0, sm + C::TB);
+        cp_commit();
+    }
+    const T C5[6] = {W<T>::c1_60, -W<T>::c2_15, W<T>::c37_60, W<T>::c37_60, -W<T>::c2_15, W<T>::c1_60};
+    const T U5[6] = {W<T>::c1_60, T(-5) * W<T>::c1_60, T(10) * W<T>::c1_60, T(-10) * W<T>::c1_60,
+                     T(5) * W<T>::c1_60, -W<T>::c1_60};
+    const T C3[4] = {-W<T>::c1_12, W<T>::c7_12, W<T>::c7_12, -W<T>::c1_12};
+    const T U3[4] = {-W<T>::c1_12, T(3) * W<T>::c1_12, T(-3) * W<T>::c1_12, W<T>::c1_12};
+    // the upwind part of a face: sign(ab+a) * S'
+    auto sgn = [&](int w, T s) { return C::CB == 1 ? fs2[w] : (cgs[w] > T(0) ? s : -s); };
+#pragma unroll
+    for (int r = 0; r < AJ_CPT; r++) {
+        const int e = t + r * AJ_THREADS;
+        const int li = e / (AJ_TK * AJ_TJ), lj = (e / AJ_TK) % AJ_TJ, lk = e % AJ_TK;
+        // face-box coordinates of the cell
+        const int bi = li + B::bdi, bj = lj + B::bdj, bk = lk + B::bdk;
+        auto at = [&](int di, int dj, int dk) { return ((bi + di) * B::bnj + (bj + dj)) * B::bnk + (bk + dk); };
+        T gx = T(0), ga;
+        if (DIR == 0) {
+#pragma unroll
+            for (int m = 0; m < 6; m++) {
+                const int w = at(2 - m, 0, 0);
+                const T s = fs1[w];
+                gx += C5[m] * s + U5[m] * sgn(w, s);
+            }
+            if (EQ == 0) ga = T(0.5) * (fab[at(-1, 0, 0)] + fab[at(0, 0, 0)]);
+            else if (EQ == 1) ga = T(0.5) * (fab[at(-1, 0, 0)] + fab[at(-1, 1, 0)]);
+            else ga = fab[at(-1, 0, 0)];
+        } else if (DIR == 1) {
+#pragma unroll
+            for (int m = 0; m < 6; m++) {
+                const int w = at(0, 2 - m, 0);
+                const T s = fs1[w];
+                gx += C5[m] * s + U5[m] * sgn(w, s);
+            }
+            if (EQ == 0) ga = T(0.5) * (fab[at(0, -1, 0)] + fab[at(1, -1, 0)]);
+            else if (EQ == 1) ga = T(0.5) * (fab[at(0, -1, 0)] + fab[at(0, 0, 0)]);
+            else ga = fab[at(0, -1, 0)];
+        } else {
+            const int pk = k0 + lk;
+#pragma unroll
+            for (int d = -2; d <= 1; d++) {
+                const int fk = pk + d;
+                if (fk < (RAIN_Z ? 0 : 1) || fk > nz - 2) continue;
+                const int w = at(0, 0, d);
+                const T s = fs1[w];
+                if (fk <= 1 || fk == nz - 2) {  // 2nd order (and the rain's bottom outflow)
+                    if (d == 0 || d == -1) gx += T(0.5) * s;
+                } else {
+                    const int m = 1 - d;  // position of the cell in the face's stencil fk-1..fk+2
+                    gx += C3[m] * s + U3[m] * sgn(w, s);
+                }
+            }
+            if (EQ == 0) ga = T(0.5) * (fab[at(0, 0, -1)] + fab[at(1, 0, -1)]);
+            else if (EQ == 1) ga = T(0.5) * (fab[at(0, 0, -1)] + fab[at(0, 1, -1)]);
+            else if (RAIN_Z) {
+                // the bottom outflow does not depend on w; the fall speed of
+                // levels 1..NZ-2 follows their rain (face 0 holds level 1 twice)
+                ga = pk >= 2 ? fab[at(0, 0, -1)] : T(0);
+                if (pk >= 1 && pk <= nz - 2) {
+                    const T below = fab[at(0, 0, -1)] * (pk == 1 ? T(2) : T(1));
+                    gx -= T(0.5) * dvr[r] * (fab[at(0, 0, 0)] + below);
+                }
+            } else ga = fab[at(0, 0, -1)];
+        }
+        acc[r][XF] += gx;
+        acc[r][DIR] += ga;
+    }
+    __syncthreads();
+}
+
+template <typename T, int G, int EQ>
+__device__ __forceinline__ void adj_equation(const KParams<T> &p, const T *__restrict__ coef, const KFields<T> &A,
+                                             T step, int i0, int j0, int k0, T *sm, T (&acc)[AJ_CPT][7])
+{
+    adj_family<T, G, EQ, 0>(p, coef, A, step, i0, j0, k0, sm, acc);
+    adj_family<T, G, EQ, 1>(p, coef, A, step, i0, j0, k0, sm, acc);
+    adj_family<T, G, EQ, 2>(p, coef, A, step, i0, j0, k0, sm, acc);
 }
 
 // The adjoint advection runs as two launches over the same tiles: group 0
@@ -672,27 +766,37 @@ __device__ __forceinline__ void adj_equation(const KParams<T> &p, const T *__res
 // group 1 adds into u, v, w and replaces qv, qc, qr.
 template <typename T, int G>
 __global__ void __launch_bounds__(AJ_THREADS, sizeof(T) == 4 ? 3 : 2)
-    k_adj_advect(KParams<T> p, const T *__restrict__ coef, KFields<T> A, const unsigned char *qm, T step, T sdtg,
-                 int zero_cur)
+    k_adj_advect(KParams<T> p, const T *__restrict__ coef, KFields<T> A, T step, T sdtg, int zero_cur)
 {
-    extern __shared__ unsigned char smem_raw[];
-    T *fs1 = (T *)smem_raw, *fs2 = fs1 + AJ_NFACE, *fab = fs2 + AJ_NFACE, *tb = fab + AJ_NFACE;
+    using C = AjCfg<T>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *sm = (T *)smem_raw;
     const int ny = p.ny, nz = p.nz;
     const int i0 = blockIdx.x * AJ_TI, j0 = blockIdx.y * AJ_TJ, k0 = blockIdx.z * AJ_TK;
+    constexpr int EQ0 = 3 * G;
+    issue_tb<T, EQ0>(p, A, i0, j0, k0, sm + C::TB);
+    issue_coef<T, EQ0, 0>(p, coef, i0, j0, k0, sm);
+    cp_commit();
+    // level factors of the z faces fk = k0-2 .. k0+TK: d(flux)/d(tendency)
+    // below and above the face
+    if (threadIdx.x < C::NZF) {
+        const int fk = k0 - 2 + threadIdx.x;
+        T z0 = T(0), z1 = T(0);
+        if (fk >= 0 && fk <= nz - 2) {
+            z0 = (p.dtz * p.mu[fk]) * p.rhow[fk + 1] * p.one_d_rhou[fk];
+            z1 = (p.dtz * p.mu[fk + 1]) * p.rhow[fk + 1] * p.one_d_rhou[fk + 1];
+        }
+        sm[C::ZF + threadIdx.x] = z0;
+        sm[C::ZF + C::NZF + threadIdx.x] = z1;
+    }
     T acc[AJ_CPT][7];
 #pragma unroll
     for (int r = 0; r < AJ_CPT; r++)
 #pragma unroll
         for (int f = 0; f < 7; f++) acc[r][f] = T(0);
-    if (G == 0) {
-        adj_equation<T, 0>(p, coef, A, qm, step, i0, j0, k0, tb, fs1, fs2, fab, acc);
-        adj_equation<T, 1>(p, coef, A, qm, step, i0, j0, k0, tb, fs1, fs2, fab, acc);
-        adj_equation<T, 2>(p, coef, A, qm, step, i0, j0, k0, tb, fs1, fs2, fab, acc);
-    } else {
-        adj_equation<T, 3>(p, coef, A, qm, step, i0, j0, k0, tb, fs1, fs2, fab, acc);
-        adj_equation<T, 4>(p, coef, A, qm, step, i0, j0, k0, tb, fs1, fs2, fab, acc);
-        adj_equation<T, 5>(p, coef, A, qm, step, i0, j0, k0, tb, fs1, fs2, fab, acc);
-    }
+    adj_equation<T, G, EQ0>(p, coef, A, step, i0, j0, k0, sm, acc);
+    adj_equation<T, G, EQ0 + 1>(p, coef, A, step, i0, j0, k0, sm, acc);
+    adj_equation<T, G, EQ0 + 2>(p, coef, A, step, i0, j0, k0, sm, acc);
     // the fields this group gathers into
     constexpr int NG = G == 0 ? 4 : 6;
     constexpr int GF[2][6] = {{FU, FV, FW, FTH, -1, -1}, {FU, FV, FW, FQV, FQC, FQR}};
@@ -718,16 +822,13 @@ __global__ void __launch_bounds__(AJ_THREADS, sizeof(T) == 4 ? 3 : 2)
                 }
             }
         }
-        const unsigned char bits = G == 1 ? qm[c] : 0;
 #pragma unroll
         for (int g = 0; g < NG; g++) {
             const int f = GF[G][g];
             const bool cell = adv_cell(p, pi, pj, pk, f == FW ? 2 : 1);
             const bool mine = G == 0 || f >= FQV;  // fields this group folds and replaces
-            if (mine) {
-                const int zb = f == FQV ? 1 : f == FQC ? 2 : f == FQR ? 4 : 0;
-                if (cell && !(bits & zb)) A.M[f][c] += A.P[f][c];
-            }
+            // (a clipped moisture point holds no P-bar: the fold adds zero)
+            if (mine && cell) A.M[f][c] += A.P[f][c];
             if (mine && zero_cur && cell) A.cur[f][c] = a[f];
             else if (a[f] != T(0)) A.cur[f][c] += a[f];
         }
