@@ -267,7 +267,7 @@ struct Lin : LinBase {
         static const double steps[3] = {1. / 3., 0.5, 1.0};
         cudaStream_t s = e.stream;
         const bool moist = nf == 7;
-        const dim3 gadv(cdiv(e.NX, AJ_TI), cdiv(e.NY, AJ_TJ), cdiv(e.NZ, AJ_TK));
+        const dim3 gadv(cdiv(e.NZ, AJ_TK), cdiv(e.NX, AJ_TI), cdiv(e.NY, AJ_TJ));
         const size_t smem_adv = AjCfg<T>::smem;
         swap_inner();  // advance_outer's swap
         const int ncol = cdiv((long)e.NX * e.NY * nf, 128);  // threads of k_adj_cols: (field, column)

@@ -772,7 +772,9 @@ __global__ void __launch_bounds__(AJ_THREADS, sizeof(T) == 4 ? 3 : 2)
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T *sm = (T *)smem_raw;
     const int ny = p.ny, nz = p.nz;
-    const int i0 = blockIdx.x * AJ_TI, j0 = blockIdx.y * AJ_TJ, k0 = blockIdx.z * AJ_TK;
+    // the level tiles of a column run next to each other: their rows share
+    // DRAM lines, read once while all of them are resident
+    const int i0 = blockIdx.y * AJ_TI, j0 = blockIdx.z * AJ_TJ, k0 = blockIdx.x * AJ_TK;
     constexpr int EQ0 = 3 * G;
     issue_tb<T, EQ0>(p, A, i0, j0, k0, sm + C::TB);
     issue_coef<T, EQ0, 0>(p, coef, i0, j0, k0, sm);
