@@ -504,7 +504,7 @@ class Engine : public EngineBase {
         const dim3 by_y(KTy, std::max(1, 256 / KTy)), by_x(KTx, std::max(1, 256 / KTx));
         {
             ProfScope ps(this, PC_DIV_FFT_Y, 1);
-            k_div_fft_y<T><<<dim3(kp.ni, nkt_y), by_y, smem_y, stream>>>(kp, F, spec, plan_j, tw_j, sdt, KTy);
+            k_div_fft_y<T><<<dim3(nkt_y, kp.ni), by_y, smem_y, stream>>>(kp, F, spec, plan_j, tw_j, sdt, KTy);
         }
         if (psx > 0) {
             ProfScope ps(this, PC_THOMAS, 1);
@@ -529,7 +529,7 @@ class Engine : public EngineBase {
         }
         {
             ProfScope ps(this, PC_IFFT_Y_PI, 1);
-            k_ifft_y_pi<T><<<dim3(kp.ni, nkt_y), by_y, smem_y, stream>>>(kp, F, spec, plan_j, tw_j, KTy);
+            k_ifft_y_pi<T><<<dim3(nkt_y, kp.ni), by_y, smem_y, stream>>>(kp, F, spec, plan_j, tw_j, KTy);
         }
         launches += 2;
     }

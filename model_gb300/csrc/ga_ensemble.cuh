@@ -77,8 +77,9 @@ __global__ void kb_div_fft_y(const KParams<T> *P, const KFields<T> *F, const Mem
         const KParams<T> &p = P[m];
         const MemberAux<T> &a = A[m];
         const long lb = vb - pre[m];
-        div_fft_y_body(p, F[m], a.spec, a.plan_j, a.tw_j, (T)(step * p.dt_d), a.KTy, (int)(lb % p.ni),
-                       (int)(lb / p.ni));
+        const long nkt = (p.nz - 2 + a.KTy - 1) / a.KTy;  // level tiles of a plane run next to each other
+        div_fft_y_body(p, F[m], a.spec, a.plan_j, a.tw_j, (T)(step * p.dt_d), a.KTy, (int)(lb / nkt),
+                       (int)(lb % nkt));
         __syncthreads();
     }
 }
@@ -105,7 +106,8 @@ __global__ void kb_ifft_y_pi(const KParams<T> *P, const KFields<T> *F, const Mem
         const KParams<T> &p = P[m];
         const MemberAux<T> &a = A[m];
         const long lb = vb - pre[m];
-        ifft_y_pi_body(p, F[m], a.spec, a.plan_j, a.tw_j, a.KTy, (int)(lb % p.ni), (int)(lb / p.ni));
+        const long nkt = (p.nz - 2 + a.KTy - 1) / a.KTy;
+        ifft_y_pi_body(p, F[m], a.spec, a.plan_j, a.tw_j, a.KTy, (int)(lb / nkt), (int)(lb % nkt));
         __syncthreads();
     }
 }

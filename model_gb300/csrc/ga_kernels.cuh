@@ -1047,7 +1047,7 @@ template <typename T>
 __global__ void k_div_fft_y(KParams<T> p, KFields<T> F, typename V2<T>::t *spec, FftPlan pj,
                             const typename V2<T>::t *tw, T sdt, int KT)
 {
-    div_fft_y_body(p, F, spec, pj, tw, sdt, KT, blockIdx.x, blockIdx.y);
+    div_fft_y_body(p, F, spec, pj, tw, sdt, KT, blockIdx.y, blockIdx.x);
 }
 
 // FFT along x of the spectral buffer for one y-wavenumber q and a tile of
@@ -1410,7 +1410,7 @@ template <typename T>
 __global__ void k_ifft_y_pi(KParams<T> p, KFields<T> F, typename V2<T>::t *spec, FftPlan pj,
                             const typename V2<T>::t *tw, int KT)
 {
-    ifft_y_pi_body(p, F, spec, pj, tw, KT, blockIdx.x, blockIdx.y);
+    ifft_y_pi_body(p, F, spec, pj, tw, KT, blockIdx.y, blockIdx.x);
 }
 
 // ---------------------------------------------------------------------------

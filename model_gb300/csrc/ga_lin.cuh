@@ -240,7 +240,7 @@ struct Lin : LinBase {
         const int nkt_y = cdiv(e.NZ - 2, e.KTy), nkt_x = cdiv(e.NZ - 2, e.KTx);
         const dim3 by_y(e.KTy, std::max(1, 256 / e.KTy)), by_x(e.KTx, std::max(1, 256 / e.KTx));
         cudaStream_t s = e.stream;
-        k_adj_fft_y_in<T><<<dim3(e.kp.ni, nkt_y), by_y, e.smem_y, s>>>(e.kp, lpi_f, e.spec, e.plan_j, e.tw_j, e.KTy);
+        k_adj_fft_y_in<T><<<dim3(nkt_y, e.kp.ni), by_y, e.smem_y, s>>>(e.kp, lpi_f, e.spec, e.plan_j, e.tw_j, e.KTy);
         if (e.psx > 0) {  // x transforms and the solves fused, as in the forward step
             const int nl = e.NZ - 2, bx = std::min(nl, 64);
             k_spectral_x_adj<T><<<e.kp.nj, dim3(bx, std::max(1, 256 / bx)), e.smem_sx, s>>>(e.kp, e.spec, e.plan_i,
@@ -253,7 +253,7 @@ struct Lin : LinBase {
             k_fft_x<T><<<dim3(e.kp.nj, nkt_x), by_x, e.smem_x, s>>>(e.kp, e.spec, e.plan_i, e.tw_i, 1, e.KTx);
             e.launches += 3;
         }
-        k_adj_ifft_y_out<T><<<dim3(e.kp.ni, nkt_y), by_y, e.smem_y, s>>>(e.kp, e.spec, dbar, e.plan_j, e.tw_j, e.KTy);
+        k_adj_ifft_y_out<T><<<dim3(nkt_y, e.kp.ni), by_y, e.smem_y, s>>>(e.kp, e.spec, dbar, e.plan_j, e.tw_j, e.KTy);
         k_adj_div<T><<<cdiv(N, 256), 256, 0, s>>>(e.kp, A, dbar, (T)(st * e.cfg.dt));
         e.launches += 3;
     }

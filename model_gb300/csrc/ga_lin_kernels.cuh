@@ -1056,8 +1056,8 @@ __global__ void k_adj_fft_y_in(KParams<T> p, const T *pib, typename V2<T>::t *sp
     T2 *a = (T2 *)smem_raw;
     T2 *b = a + (long)p.nj * KT;
     const int nx = p.nx, ny = p.ny, nz = p.nz;
-    const int i = blockIdx.x;
-    const int k0 = 1 + blockIdx.y * KT;
+    const int i = blockIdx.y;
+    const int k0 = 1 + blockIdx.x * KT;
     const int kt = min(KT, nz - 1 - k0);
     const bool ii = i >= 1 && i <= nx - 2;
     for (int q = threadIdx.y; q < p.nj; q += blockDim.y)
@@ -1102,8 +1102,8 @@ __global__ void k_adj_ifft_y_out(KParams<T> p, const typename V2<T>::t *spec, T 
     T2 *a = (T2 *)smem_raw;
     T2 *b = a + (long)p.nj * KT;
     const int nz = p.nz;
-    const int i = blockIdx.x;
-    const int k0 = 1 + blockIdx.y * KT;
+    const int i = blockIdx.y;
+    const int k0 = 1 + blockIdx.x * KT;
     const int kt = min(KT, nz - 1 - k0);
     for (int q = threadIdx.y; q < p.nj; q += blockDim.y)
         for (int l = threadIdx.x; l < KT; l += blockDim.x) {

@@ -196,7 +196,7 @@ int solve_pressure_noalloc(const ga_config *c, const ga_columns *cols, double *u
     const FftPlan pj = plan_for(nj), pi_plan = plan_for(ni);
     const int nkt_y = (NZ - 2 + KTy - 1) / KTy, nkt_x = (NZ - 2 + KTx - 1) / KTx;
     const dim3 by_y(KTy, std::max(1, 256 / KTy)), by_x(KTx, std::max(1, 256 / KTx));
-    k_div_fft_y<double><<<dim3(ni, nkt_y), by_y, smem_y, stream>>>(kp, F, spec, pj, tw_j, step * c->dt, KTy);
+    k_div_fft_y<double><<<dim3(nkt_y, ni), by_y, smem_y, stream>>>(kp, F, spec, pj, tw_j, step * c->dt, KTy);
     // FFT along x + Thomas + inverse FFT along x
     const int nl = NZ - 2, m = 8;
     auto pad = [&](int L) { return L + ((1 - L % m) % m + m) % m; };
@@ -215,7 +215,7 @@ int solve_pressure_noalloc(const ga_config *c, const ga_columns *cols, double *u
         k_fft_x<double><<<dim3(nj, nkt_x), by_x, smem_x, stream>>>(kp, spec, pi_plan, tw_i, 1, KTx);
     }
     // inverse FFT along y + PI with the level copies and lateral placement
-    k_ifft_y_pi<double><<<dim3(ni, nkt_y), by_y, smem_y, stream>>>(kp, F, spec, pj, tw_j, KTy);
+    k_ifft_y_pi<double><<<dim3(nkt_y, ni), by_y, smem_y, stream>>>(kp, F, spec, pj, tw_j, KTy);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
         set_error(std::string("ga_solve_pressure_noalloc: launch failed: ") + cudaGetErrorString(e));
