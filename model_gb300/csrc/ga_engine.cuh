@@ -514,7 +514,7 @@ class Engine : public EngineBase {
         } else {
             {
                 ProfScope ps(this, PC_FFT_X, 1);
-                k_fft_x<T><<<dim3(kp.nj, nkt_x), by_x, smem_x, stream>>>(kp, spec, plan_i, tw_i, 0, KTx);
+                k_fft_x<T><<<dim3(nkt_x, kp.nj), by_x, smem_x, stream>>>(kp, spec, plan_i, tw_i, 0, KTx);
             }
             const long ncol = (long)kp.ni * kp.nj;
             {
@@ -523,7 +523,7 @@ class Engine : public EngineBase {
             }
             {
                 ProfScope ps(this, PC_FFT_X, 1);
-                k_fft_x<T><<<dim3(kp.nj, nkt_x), by_x, smem_x, stream>>>(kp, spec, plan_i, tw_i, 1, KTx);
+                k_fft_x<T><<<dim3(nkt_x, kp.nj), by_x, smem_x, stream>>>(kp, spec, plan_i, tw_i, 1, KTx);
             }
             launches += 3;
         }

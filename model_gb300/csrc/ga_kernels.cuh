@@ -890,6 +890,36 @@ __global__ void k_periodic_copy(KParams<T> p, T *a, T *b, T *c, T *d)
 // ---------------------------------------------------------------------------
 constexpr int PPM_MAXZ = 128;  // largest NZ the column kernels support
 
+// asynchronous element copy global -> shared (cp.async), zero-filled where
+// `ok` is false (src is then a placeholder address and is not read).
+// 4- and 8-byte elements go through L1; 16-byte ones (complex FP64) bypass it.
+template <typename E>
+__device__ __forceinline__ void cp_elem(E *dst, const E *src, bool ok)
+{
+    static_assert(sizeof(E) == 4 || sizeof(E) == 8 || sizeof(E) == 16, "cp.async copies 4, 8 or 16 bytes");
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    const int n = ok ? (int)sizeof(E) : 0;
+    if (sizeof(E) == 16)
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(src), "r"(n) : "memory");
+    else if (sizeof(E) == 8)
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(d), "l"(src), "r"(n) : "memory");
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(d), "l"(src), "r"(n) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_wait()
+{
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+// every copy of this thread complete, then visible to the block
+__device__ __forceinline__ void cp_wait_all_sync()
+{
+    cp_commit();
+    cp_wait<0>();
+    __syncthreads();
+}
+
 struct FftPlan {
     int n, nfac;
     int fac[24];
@@ -1026,6 +1056,9 @@ __device__ void div_fft_y_body(const KParams<T> &p, const KFields<T> &F, typenam
     int ii;
     if (!p.periodic) ii = min(max(is, 1), p.nx - 2);
     else ii = is + 3;
+    // several rows in flight per thread: the loads of a row do not wait for
+    // the previous row's store
+#pragma unroll 4
     for (int q = threadIdx.y; q < p.nj; q += blockDim.y)
         for (int l = threadIdx.x; l < KT; l += blockDim.x) {
             T2 v;
@@ -1060,18 +1093,14 @@ __global__ void k_fft_x(KParams<T> p, typename V2<T>::t *spec, FftPlan pi, const
     extern __shared__ unsigned char smem_raw[];
     T2 *a = (T2 *)smem_raw;
     T2 *b = a + (long)p.ni * KT;
-    const int q = blockIdx.x;
-    const int k0 = 1 + blockIdx.y * KT;
+    // the level tiles of a wavenumber run next to each other (shared rows)
+    const int q = blockIdx.y;
+    const int k0 = 1 + blockIdx.x * KT;
     const int kt = min(KT, p.nz - 1 - k0);
     for (int i = threadIdx.y; i < p.ni; i += blockDim.y)
-        for (int l = threadIdx.x; l < KT; l += blockDim.x) {
-            T2 v;
-            v.x = T(0);
-            v.y = T(0);
-            if (l < kt) v = spec[((long)i * p.nj + q) * p.nz + k0 + l];
-            a[i * KT + l] = v;
-        }
-    __syncthreads();
+        for (int l = threadIdx.x; l < KT; l += blockDim.x)
+            cp_elem(a + i * KT + l, spec + ((long)i * p.nj + q) * p.nz + k0 + min(l, kt - 1), l < kt);
+    cp_wait_all_sync();
     T2 *r = fft_smem<T, T2>(a, b, KT, pi, tw, inv != 0, KT);
     for (int i = threadIdx.y; i < p.ni; i += blockDim.y)
         for (int l = threadIdx.x; l < kt; l += blockDim.x)
@@ -1244,8 +1273,8 @@ __global__ void k_thomas(KParams<T> p, typename V2<T>::t *spec, int TC)
     const long c0 = (long)blockIdx.x * TC;
     const int nc = (int)min((long)TC, ncol - c0);
     T2 *g = spec + c0 * p.nz;
-    for (int w = threadIdx.x; w < nc * p.nz; w += blockDim.x) xs[(w / p.nz) * cs + w % p.nz] = g[w];
-    __syncthreads();
+    for (int w = threadIdx.x; w < nc * p.nz; w += blockDim.x) cp_elem(xs + (w / p.nz) * cs + w % p.nz, g + w, true);
+    cp_wait_all_sync();
     const double size2d = (double)(p.ni * p.nj);
     for (int c = threadIdx.x; c < nc; c += blockDim.x) {
         const long col = c0 + c;
@@ -1294,8 +1323,9 @@ __device__ void spectral_x_body(const KParams<T> &p, typename V2<T>::t *spec, co
         d_r[k] = p.rhou_d[k]; d_a[k] = p.acoef_d[k]; d_c[k] = p.ccoef_d[k]; d_v[k] = p.vcoef_d[k];
     }
     for (int i = threadIdx.y; i < p.ni; i += blockDim.y)
-        for (int l = threadIdx.x; l < nl; l += blockDim.x) a[i * ps + l] = spec[((long)i * p.nj + q) * p.nz + 1 + l];
-    __syncthreads();
+        for (int l = threadIdx.x; l < nl; l += blockDim.x)
+            cp_elem(a + i * ps + l, spec + ((long)i * p.nj + q) * p.nz + 1 + l, true);
+    cp_wait_all_sync();
     T2 *r = fft_smem<T, T2>(a, b, nl, pi, tw, false, ps);
     T2 *fr = (r == a) ? b : a;  // free buffer: holds the Thomas coefficients
     const double size2d = (double)(p.ni * p.nj);
@@ -1362,14 +1392,9 @@ __device__ void ifft_y_pi_body(const KParams<T> &p, const KFields<T> &F, typenam
     const int k0 = 1 + by * KT;
     const int kt = min(KT, p.nz - 1 - k0);
     for (int q = threadIdx.y; q < p.nj; q += blockDim.y)
-        for (int l = threadIdx.x; l < KT; l += blockDim.x) {
-            T2 v;
-            v.x = T(0);
-            v.y = T(0);
-            if (l < kt) v = spec[((long)is * p.nj + q) * p.nz + k0 + l];
-            a[q * KT + l] = v;
-        }
-    __syncthreads();
+        for (int l = threadIdx.x; l < KT; l += blockDim.x)
+            cp_elem(a + q * KT + l, spec + ((long)is * p.nj + q) * p.nz + k0 + min(l, kt - 1), l < kt);
+    cp_wait_all_sync();
     T2 *r = fft_smem<T, T2>(a, b, KT, pj, tw, true, KT);
     T *PI = F.pi;
     const int nz = p.nz, ny = p.ny;

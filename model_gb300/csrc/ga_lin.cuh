@@ -247,10 +247,10 @@ struct Lin : LinBase {
                                                                                           e.tw_i, e.psx);
             e.launches += 1;
         } else {
-            k_fft_x<T><<<dim3(e.kp.nj, nkt_x), by_x, e.smem_x, s>>>(e.kp, e.spec, e.plan_i, e.tw_i, 0, e.KTx);
+            k_fft_x<T><<<dim3(nkt_x, e.kp.nj), by_x, e.smem_x, s>>>(e.kp, e.spec, e.plan_i, e.tw_i, 0, e.KTx);
             const long ncol = (long)e.kp.ni * e.kp.nj;
             k_thomas_adj<T><<<cdiv(ncol, e.TC), 256, e.smem_th, s>>>(e.kp, e.spec, e.TC);
-            k_fft_x<T><<<dim3(e.kp.nj, nkt_x), by_x, e.smem_x, s>>>(e.kp, e.spec, e.plan_i, e.tw_i, 1, e.KTx);
+            k_fft_x<T><<<dim3(nkt_x, e.kp.nj), by_x, e.smem_x, s>>>(e.kp, e.spec, e.plan_i, e.tw_i, 1, e.KTx);
             e.launches += 3;
         }
         k_adj_ifft_y_out<T><<<dim3(nkt_y, e.kp.ni), by_y, e.smem_y, s>>>(e.kp, e.spec, dbar, e.plan_j, e.tw_j, e.KTy);

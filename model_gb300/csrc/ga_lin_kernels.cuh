@@ -479,25 +479,6 @@ __global__ void k_lin_coef(KParams<T> p, KFields<T> R, T *coef, KFields<T> A, co
     }
 }
 
-// asynchronous element copy global -> shared (cp.async), zero-filled where
-// `ok` is false (src is then a placeholder address and is not read)
-template <typename T>
-__device__ __forceinline__ void cp_elem(T *dst, const T *src, bool ok)
-{
-    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
-    const int n = ok ? (int)sizeof(T) : 0;
-    if (sizeof(T) == 4)
-        asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(d), "l"(src), "r"(n) : "memory");
-    else
-        asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(d), "l"(src), "r"(n) : "memory");
-}
-__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_wait()
-{
-    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
-}
-
 // Shared memory of k_adj_advect.  FP32 double-buffers the coefficient and
 // tendency boxes (the next family's copies run under the current one's
 // work, 3 blocks per SM); FP64 has one of each (2 blocks per SM) and copies
@@ -1106,14 +1087,9 @@ __global__ void k_adj_ifft_y_out(KParams<T> p, const typename V2<T>::t *spec, T 
     const int k0 = 1 + blockIdx.x * KT;
     const int kt = min(KT, nz - 1 - k0);
     for (int q = threadIdx.y; q < p.nj; q += blockDim.y)
-        for (int l = threadIdx.x; l < KT; l += blockDim.x) {
-            T2 v;
-            v.x = T(0);
-            v.y = T(0);
-            if (l < kt) v = spec[((long)i * p.nj + q) * nz + k0 + l];
-            a[q * KT + l] = v;
-        }
-    __syncthreads();
+        for (int l = threadIdx.x; l < KT; l += blockDim.x)
+            cp_elem(a + q * KT + l, spec + ((long)i * p.nj + q) * nz + k0 + min(l, kt - 1), l < kt);
+    cp_wait_all_sync();
     T2 *r = fft_smem<T, T2>(a, b, KT, pj, tw, true, KT);
     for (int j = threadIdx.y; j < p.nj; j += blockDim.y)
         for (int l = threadIdx.x; l < kt; l += blockDim.x) dbar[gix(p.ny, nz, i, j, k0 + l)] = r[j * KT + l].x;
@@ -1267,8 +1243,9 @@ __global__ void k_spectral_x_adj(KParams<T> p, typename V2<T>::t *spec, FftPlan 
         d_r[k] = p.rhou_d[k]; d_a[k] = p.acoef_d[k]; d_c[k] = p.ccoef_d[k]; d_v[k] = p.vcoef_d[k];
     }
     for (int i = threadIdx.y; i < p.ni; i += blockDim.y)
-        for (int l = threadIdx.x; l < nl; l += blockDim.x) a[i * ps + l] = spec[((long)i * p.nj + q) * p.nz + 1 + l];
-    __syncthreads();
+        for (int l = threadIdx.x; l < nl; l += blockDim.x)
+            cp_elem(a + i * ps + l, spec + ((long)i * p.nj + q) * p.nz + 1 + l, true);
+    cp_wait_all_sync();
     T2 *r = fft_smem<T, T2>(a, b, nl, pi, tw, false, ps);
     T2 *fr = (r == a) ? b : a;
     const double size2d = (double)(p.ni * p.nj);
@@ -1313,8 +1290,8 @@ __global__ void k_thomas_adj(KParams<T> p, typename V2<T>::t *spec, int TC)
     const long c0 = (long)blockIdx.x * TC;
     const int nc = (int)min((long)TC, ncol - c0);
     T2 *g = spec + c0 * p.nz;
-    for (int w = threadIdx.x; w < nc * p.nz; w += blockDim.x) xs[(w / p.nz) * cs + w % p.nz] = g[w];
-    __syncthreads();
+    for (int w = threadIdx.x; w < nc * p.nz; w += blockDim.x) cp_elem(xs + (w / p.nz) * cs + w % p.nz, g + w, true);
+    cp_wait_all_sync();
     const double inv_s = 1.0 / (double)(p.ni * p.nj);
     for (int c = threadIdx.x; c < nc; c += blockDim.x) {
         const long col = c0 + c;

@@ -209,10 +209,10 @@ int solve_pressure_noalloc(const ga_config *c, const ga_columns *cols, double *u
     } else {
         const int TC = 64;
         const size_t smem_th = (size_t)TC * (NZ | 1) * (sizeof(T2) + sizeof(double));
-        k_fft_x<double><<<dim3(nj, nkt_x), by_x, smem_x, stream>>>(kp, spec, pi_plan, tw_i, 0, KTx);
+        k_fft_x<double><<<dim3(nkt_x, nj), by_x, smem_x, stream>>>(kp, spec, pi_plan, tw_i, 0, KTx);
         const long ncol = (long)ni * nj;
         k_thomas<double><<<(int)((ncol + TC - 1) / TC), TC, smem_th, stream>>>(kp, spec, TC);
-        k_fft_x<double><<<dim3(nj, nkt_x), by_x, smem_x, stream>>>(kp, spec, pi_plan, tw_i, 1, KTx);
+        k_fft_x<double><<<dim3(nkt_x, nj), by_x, smem_x, stream>>>(kp, spec, pi_plan, tw_i, 1, KTx);
     }
     // inverse FFT along y + PI with the level copies and lateral placement
     k_ifft_y_pi<double><<<dim3(nkt_y, ni), by_y, smem_y, stream>>>(kp, F, spec, pj, tw_j, KTy);
