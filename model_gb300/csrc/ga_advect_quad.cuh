@@ -1,0 +1,544 @@
+// ---------------------------------------------------------------------------
+// FP32 advection with four levels per thread (advection.cpp:304-497 with the
+// face fluxes of fluxes.cpp), for a horizontally uniform basic state and NZ a
+// multiple of 4.
+//
+// A block owns TI x TJ interior columns at every level, as k_advect_tile
+// does, but a work item is one column and one aligned quad of levels
+// k0..k0+3: each stencil row is one 16-byte load, and the index arithmetic is
+// paid once per four levels.  The six flux fields go in three passes of two
+// (u and v; theta and qv; qc and qr), so only two fields' face columns are in
+// shared memory at a time.  Per level the arithmetic is that of the
+// k_advect_tile face and tendency functions, expression for expression.
+// Levels outside a face's or a cell's range are computed on padding values
+// and never stored.
+// ---------------------------------------------------------------------------
+#pragma once
+#include "ga_kernels.cuh"
+
+namespace ga {
+
+constexpr int AQ_THREADS = 256;
+constexpr int AQ_LV = 7;  // staged level arrays: mu, rhow, one_d_rhou, tb, qb, tbv, rhou
+
+template <int TI, int TJ>
+struct AQGeom {
+    static constexpr int CE = (TI + 1) * TJ;  // east-face columns: i0-1 .. i0+TI-1
+    static constexpr int CN = TI * (TJ + 1);  // north-face columns: j0-1 .. j0+TJ-1
+    static constexpr int CT = TI * TJ;        // top faces, and the cells
+    static constexpr int CF = CE + CN + CT;   // face columns of one field
+};
+
+// two field slots of face columns, the basic-state table, the level arrays
+__host__ __device__ constexpr size_t advect_quad_smem(int ti, int tj, int nz)
+{
+    return (2 * (size_t)((ti + 1) * tj + ti * (tj + 1) + ti * tj) * nz + (size_t)BT_COUNT * nz +
+            (size_t)AQ_LV * nz) *
+           sizeof(float);
+}
+
+struct Q4 {
+    float v[4];
+};
+__device__ __forceinline__ Q4 ldg4(const float *a, int idx)
+{
+    const float4 t = __ldg(reinterpret_cast<const float4 *>(a + idx));
+    return Q4{{t.x, t.y, t.z, t.w}};
+}
+__device__ __forceinline__ Q4 lds4(const float *a)
+{
+    const float4 t = *reinterpret_cast<const float4 *>(a);
+    return Q4{{t.x, t.y, t.z, t.w}};
+}
+__device__ __forceinline__ void sts4(float *a, const Q4 &q)
+{
+    *reinterpret_cast<float4 *>(a) = make_float4(q.v[0], q.v[1], q.v[2], q.v[3]);
+}
+__device__ __forceinline__ void stg4(float *a, const Q4 &q)
+{
+    *reinterpret_cast<float4 *>(a) = make_float4(q.v[0], q.v[1], q.v[2], q.v[3]);
+}
+// a column window of 12 levels k0-4 .. k0+7 (zero outside the column)
+struct Win {
+    float v[12];
+    __device__ __forceinline__ float at(int d) const { return v[4 + d]; }  // level k0 + d
+};
+__device__ __forceinline__ Win ldwin(const float *a, int c, int k0, int nz)
+{
+    Win w;
+    const Q4 lo = k0 >= 4 ? ldg4(a, c - 4) : Q4{{0.f, 0.f, 0.f, 0.f}};
+    const Q4 mi = ldg4(a, c);
+    const Q4 hi = k0 + 4 < nz ? ldg4(a, c + 4) : Q4{{0.f, 0.f, 0.f, 0.f}};
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+        w.v[e] = lo.v[e];
+        w.v[4 + e] = mi.v[e];
+        w.v[8 + e] = hi.v[e];
+    }
+    return w;
+}
+
+// field kinds of the passes: 0 u, 1 v, 2 theta, 3 qv, 4 qc, 5 qr
+__host__ __device__ constexpr int aq_field(int fk)
+{
+    return fk == 0 ? FU : fk == 1 ? FV : fk == 2 ? FTH : fk == 3 ? FQV : fk == 4 ? FQC : FQR;
+}
+// basic-state row of a scalar (brow of s_*_ub): 0 theta, 1 qv, -1 none
+__host__ __device__ constexpr int aq_brow(int fk) { return fk == 2 ? 0 : fk == 3 ? 1 : -1; }
+
+// east face (between i and i+1) at levels k0..k0+3: u_east_ub, v_east_ub, s_east_ub
+template <int FK>
+__device__ __forceinline__ Q4 aq_east(const KParams<float> &p, const KFields<float> &F, const float *tab, int i,
+                                      int j, int k0)
+{
+    const int nz = p.nz, sx = p.ny * nz, sy = nz;
+    const int c = gix(p.ny, nz, i, j, k0);
+    const float *X = F.cur[aq_field(FK)], *U = F.cur[FU];
+    Q4 x[6];
+#pragma unroll
+    for (int m = 0; m < 6; m++) x[m] = ldg4(X, c + (m - 2) * sx);
+    Q4 r;
+    if (FK == 0) {
+        const Q4 up = ldg4(U, c + sx), u0 = ldg4(U, c), uba = lds4(tab + BT_UA * nz + k0),
+                 c6 = lds4(tab + BT_C6_UB * nz + k0);
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+            const float ua = 0.5f * (up.v[e] + u0.v[e]);
+            const float ue = face5<float>(x[0].v[e], x[1].v[e], x[2].v[e], x[3].v[e], x[4].v[e], x[5].v[e],
+                                          sgn(uba.v[e] + ua));
+            r.v[e] = ua * c6.v[e] + (uba.v[e] + ua) * ue;
+        }
+    } else if (FK == 1) {
+        const Q4 ua_ = ldg4(U, c + sx), ub_ = ldg4(U, c + sx - sy), uba = lds4(tab + BT_UA * nz + k0),
+                 c6 = lds4(tab + BT_C6_VB * nz + k0);
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+            const float ua = 0.5f * (ua_.v[e] + ub_.v[e]);
+            const float ve = face5<float>(x[0].v[e], x[1].v[e], x[2].v[e], x[3].v[e], x[4].v[e], x[5].v[e],
+                                          sgn(uba.v[e] + ua));
+            r.v[e] = ua * c6.v[e] + (uba.v[e] + ua) * ve;
+        }
+    } else {
+        constexpr int BR = aq_brow(FK);
+        const Q4 u1 = ldg4(U, c + sx), ub = lds4(tab + BT_UB * nz + k0);
+        const Q4 c6 = BR >= 0 ? lds4(tab + (BT_C6_THB + BR) * nz + k0) : Q4{{0.f, 0.f, 0.f, 0.f}};
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+            const float ut = ub.v[e] + u1.v[e];
+            const float se = face5<float>(x[0].v[e], x[1].v[e], x[2].v[e], x[3].v[e], x[4].v[e], x[5].v[e],
+                                          sgn(ut));
+            if (BR < 0) r.v[e] = ut * se;
+            else r.v[e] = u1.v[e] * c6.v[e] + ut * se;
+        }
+    }
+    return r;
+}
+
+// north face (between j and j+1): u_north_ub, v_north_ub, s_north_ub
+template <int FK>
+__device__ __forceinline__ Q4 aq_north(const KParams<float> &p, const KFields<float> &F, const float *tab, int i,
+                                       int j, int k0)
+{
+    const int nz = p.nz, sx = p.ny * nz, sy = nz;
+    const int c = gix(p.ny, nz, i, j, k0);
+    const float *X = F.cur[aq_field(FK)], *V = F.cur[FV];
+    Q4 x[6];
+#pragma unroll
+    for (int m = 0; m < 6; m++) x[m] = ldg4(X, c + (m - 2) * sy);
+    Q4 r;
+    if (FK == 0) {
+        const Q4 va_ = ldg4(V, c + sy), vb_ = ldg4(V, c - sx + sy), vba = lds4(tab + BT_VA * nz + k0),
+                 c6 = lds4(tab + BT_C6_UB * nz + k0);
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+            const float va = 0.5f * (va_.v[e] + vb_.v[e]);
+            const float un = face5<float>(x[0].v[e], x[1].v[e], x[2].v[e], x[3].v[e], x[4].v[e], x[5].v[e],
+                                          sgn(vba.v[e] + va));
+            r.v[e] = va * c6.v[e] + (vba.v[e] + va) * un;
+        }
+    } else if (FK == 1) {
+        const Q4 vp = ldg4(V, c + sy), v0 = ldg4(V, c), vba = lds4(tab + BT_VA * nz + k0),
+                 c6 = lds4(tab + BT_C6_VB * nz + k0);
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+            const float va = 0.5f * (vp.v[e] + v0.v[e]);
+            const float vn = face5<float>(x[0].v[e], x[1].v[e], x[2].v[e], x[3].v[e], x[4].v[e], x[5].v[e],
+                                          sgn(vba.v[e] + va));
+            r.v[e] = va * c6.v[e] + (vba.v[e] + va) * vn;
+        }
+    } else {
+        constexpr int BR = aq_brow(FK);
+        const Q4 v1 = ldg4(V, c + sy), vb = lds4(tab + BT_VB * nz + k0);
+        const Q4 c6 = BR >= 0 ? lds4(tab + (BT_C6_THB + BR) * nz + k0) : Q4{{0.f, 0.f, 0.f, 0.f}};
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+            const float vt = vb.v[e] + v1.v[e];
+            const float sn = face5<float>(x[0].v[e], x[1].v[e], x[2].v[e], x[3].v[e], x[4].v[e], x[5].v[e],
+                                          sgn(vt));
+            if (BR < 0) r.v[e] = vt * sn;
+            else r.v[e] = v1.v[e] * c6.v[e] + vt * sn;
+        }
+    }
+    return r;
+}
+
+// top face (between k and k+1) at k = k0..k0+3: u_top_ub, v_top_ub,
+// s_top_ub, r_top_ub; level NZ-1 is not a face of an advected cell (0)
+template <int FK>
+__device__ __forceinline__ Q4 aq_top(const KParams<float> &p, const KFields<float> &F, const float *tab, int i,
+                                     int j, int k0)
+{
+    const int nz = p.nz, sx = p.ny * nz, sy = nz;
+    const int c = gix(p.ny, nz, i, j, k0);
+    const Win x = ldwin(F.cur[aq_field(FK)], c, k0, nz);
+    const Win w = ldwin(F.cur[FW], c, k0, nz);
+    Q4 r;
+    if (FK == 0 || FK == 1) {
+        // the second w of the averaged advecting velocity: column i-1 (u) or j-1 (v)
+        const Win w2 = ldwin(F.cur[FW], c - (FK == 0 ? sx : sy), k0, nz);
+        constexpr int C4 = FK == 0 ? BT_C4_UB : BT_C4_VB, H2 = FK == 0 ? BT_H2_UB : BT_H2_VB;
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+            const int k = k0 + e;
+            float f = 0.f;
+            if (k >= 1 && k <= nz - 2) {
+                const float wa = 0.5f * (w.at(e + 1) + w2.at(e + 1));
+                const float wba = tab[BT_WA * nz + k];
+                float xt, xbt;
+                if (k == 1 || k == nz - 2) {
+                    xt = 0.5f * (x.at(e + 1) + x.at(e));
+                    xbt = tab[H2 * nz + k];
+                } else {
+                    xt = face3<float>(x.at(e - 1), x.at(e), x.at(e + 1), x.at(e + 2), sgn(wba + wa));
+                    xbt = tab[C4 * nz + k] + W<float>::c1_12 * sgn(wa) * tab[(C4 + 1) * nz + k];
+                }
+                f = wa * xbt + (wba + wa) * xt;
+            }
+            r.v[e] = f;
+        }
+    } else if (FK != 5) {
+        constexpr int BR = aq_brow(FK);
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+            const int k = k0 + e;
+            float f = 0.f;
+            if (k >= 1 && k <= nz - 2) {
+                const float w1 = w.at(e + 1);
+                const float wt = tab[BT_WB * nz + k + 1] + w1;
+                float st, bt = 0.f;
+                if (k == 1 || k == nz - 2) {
+                    st = 0.5f * (x.at(e + 1) + x.at(e));
+                    if (BR >= 0) bt = tab[(BT_H2_THB + BR) * nz + k];
+                } else {
+                    st = face3<float>(x.at(e - 1), x.at(e), x.at(e + 1), x.at(e + 2), sgn(wt));
+                    if (BR >= 0)
+                        bt = tab[(BT_C4_THB + 2 * BR) * nz + k] +
+                             W<float>::c1_12 * sgn(w1) * tab[(BT_C4_THB + 2 * BR + 1) * nz + k];
+                }
+                if (BR < 0) f = wt * st;
+                else f = w1 * bt + wt * st;
+            }
+            r.v[e] = f;
+        }
+    } else {
+        // rain: the fall speed at levels k0..k0+4 (vt_at)
+        float vt[5];
+#pragma unroll
+        for (int e = 0; e < 5; e++) {
+            const int k = k0 + e;
+            float v = 0.f;
+            if (k < nz) {
+                if (p.rf == 1 && k < nz - 1) {
+                    const int kk = k == 0 ? 1 : k;
+                    v = fall_speed_point(p, x.at(kk - k0), kk);
+                } else {
+                    v = F.vt[c + e];
+                }
+            }
+            vt[e] = v;
+        }
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+            const int k = k0 + e;
+            float f = 0.f;
+            if (k == 0) {
+                const float s0 = 0.5f * (x.at(0) + x.at(1));
+                f = -0.5f * (vt[1] + vt[0]) * s0;
+            } else if (k <= nz - 2) {
+                const float wb = tab[BT_WB * nz + k + 1] + w.at(e + 1);
+                const float wf = wb - 0.5f * (vt[e] + vt[e + 1]);
+                float st;
+                if (k == 1 || k == nz - 2) st = 0.5f * (x.at(e + 1) + x.at(e));
+                else st = face3<float>(x.at(e - 1), x.at(e), x.at(e + 1), x.at(e + 2), sgn(wf));
+                f = wf * st;
+            }
+            r.v[e] = f;
+        }
+    }
+    return r;
+}
+
+// the face columns of field FK into slot `sl` (E, N and T of the tile)
+template <int TI, int TJ, int FK>
+__device__ __forceinline__ void aq_faces(const KParams<float> &p, const KFields<float> &F, const float *tab,
+                                         float *sl, int i0, int j0, int ti, int tj)
+{
+    using G = AQGeom<TI, TJ>;
+    const int nz = p.nz, NQ = nz >> 2;
+    float *E = sl, *N = sl + G::CE * nz, *T = N + G::CN * nz;
+    for (int w = threadIdx.x; w < G::CE * NQ; w += AQ_THREADS) {
+        const int q = w % NQ, col = w / NQ, b = col % TJ, a = col / TJ;
+        if (a > ti || b >= tj) continue;
+        sts4(E + col * nz + 4 * q, aq_east<FK>(p, F, tab, i0 - 1 + a, j0 + b, 4 * q));
+    }
+    for (int w = threadIdx.x; w < G::CN * NQ; w += AQ_THREADS) {
+        const int q = w % NQ, col = w / NQ, b = col % (TJ + 1), a = col / (TJ + 1);
+        if (a >= ti || b > tj) continue;
+        sts4(N + col * nz + 4 * q, aq_north<FK>(p, F, tab, i0 + a, j0 - 1 + b, 4 * q));
+    }
+    for (int w = threadIdx.x; w < G::CT * NQ; w += AQ_THREADS) {
+        const int q = w % NQ, col = w / NQ, b = col % TJ, a = col / TJ;
+        if (a >= ti || b >= tj) continue;
+        sts4(T + col * nz + 4 * q, aq_top<FK>(p, F, tab, i0 + a, j0 + b, 4 * q));
+    }
+}
+
+// flux divergence of the slot at the cell quad (tend of k_advect_tile)
+template <int TI, int TJ>
+__device__ __forceinline__ Q4 aq_div(const KParams<float> &p, const float *sl, const float *lv, int a, int b, int k0)
+{
+    using G = AQGeom<TI, TJ>;
+    const int nz = p.nz;
+    const float *E = sl, *N = sl + G::CE * nz, *T = N + G::CN * nz;
+    const float *s_mu = lv, *s_rhow = lv + nz, *s_odr = lv + 2 * nz;
+    const int oe = ((a + 1) * TJ + b) * nz + k0, ow = (a * TJ + b) * nz + k0;
+    const int on = (a * (TJ + 1) + b + 1) * nz + k0, os = (a * (TJ + 1) + b) * nz + k0;
+    const int ot = (a * TJ + b) * nz + k0;
+    const Q4 ee = lds4(E + oe), ew = lds4(E + ow), nn = lds4(N + on), ns = lds4(N + os), tt = lds4(T + ot);
+    const float tb0 = k0 > 0 ? T[ot - 1] : 0.f;
+    Q4 r;
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+        const int k = k0 + e;
+        const float tlo = e == 0 ? tb0 : tt.v[e - 1];
+        const float DTZ = p.dtz * s_mu[k];
+        const int kp1 = min(k + 1, nz - 1);  // level NZ-1 is padding
+        r.v[e] = -p.dtx * (ee.v[e] - ew.v[e]) - p.dty * (nn.v[e] - ns.v[e]) -
+                 DTZ * (s_rhow[kp1] * tt.v[e] - s_rhow[k] * tlo) * s_odr[k];
+    }
+    return r;
+}
+
+// store the levels of a quad that are cells of the field (kmin .. NZ-2)
+__device__ __forceinline__ void aq_store(float *dst, int c, int k0, int nz, int kmin, const Q4 &q)
+{
+    if (k0 >= kmin && k0 + 3 <= nz - 2) {
+        stg4(dst + c, q);
+    } else {
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+            const int k = k0 + e;
+            if (k >= kmin && k <= nz - 2) dst[c + e] = q.v[e];
+        }
+    }
+}
+
+template <int TI, int TJ>
+__global__ void __launch_bounds__(AQ_THREADS, 3)
+    k_advect_quad(KParams<float> p, KFields<float> F, float step, float sdtg, int what)
+{
+    using G = AQGeom<TI, TJ>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int nz = p.nz, NQ = nz >> 2, sx = p.ny * nz, sy = nz;
+    float *s0 = (float *)smem_raw, *s1 = s0 + G::CF * nz;
+    float *tab = s1 + G::CF * nz;
+    float *lv = tab + BT_COUNT * nz;
+    float *s_mu = lv, *s_rhow = lv + nz, *s_odr = lv + 2 * nz, *s_tb = lv + 3 * nz, *s_qb = lv + 4 * nz,
+          *s_tbv = lv + 5 * nz;
+    for (int e = threadIdx.x; e < BT_COUNT * nz; e += AQ_THREADS) tab[e] = p.btab[e];
+    for (int k = threadIdx.x; k < nz; k += AQ_THREADS) {
+        s_mu[k] = p.mu[k];
+        s_rhow[k] = p.rhow[k];
+        s_odr[k] = p.one_d_rhou[k];
+        s_tb[k] = p.tb[k];
+        s_qb[k] = p.moist ? p.qb[k] : 0.f;
+        s_tbv[k] = p.tbv[k];
+        lv[6 * nz + k] = p.rhou[k];
+    }
+    const int i0 = 3 + blockIdx.x * TI, j0 = 3 + blockIdx.y * TJ;
+    const int ti = min(TI, p.nx - 3 - i0), tj = min(TJ, p.ny - 3 - j0);
+    __syncthreads();
+
+    // ---- pass 1: u, v (and the buoyancy of w)
+    if (what & (ADV_UV | ADV_WB)) {
+        if (what & ADV_UV) {
+            aq_faces<TI, TJ, 0>(p, F, tab, s0, i0, j0, ti, tj);
+            aq_faces<TI, TJ, 1>(p, F, tab, s1, i0, j0, ti, tj);
+        }
+        __syncthreads();
+        for (int w = threadIdx.x; w < G::CT * NQ; w += AQ_THREADS) {
+            const int q = w % NQ, col = w / NQ, b = col % TJ, a = col / TJ;
+            if (a >= ti || b >= tj) continue;
+            const int i = i0 + a, j = j0 + b, k0 = 4 * q;
+            const int c = gix(p.ny, nz, i, j, k0);
+            if (what & ADV_UV) {
+                const float *U = F.cur[FU], *V = F.cur[FV];
+                const float fj = p.f[j];
+                {
+                    const Q4 d = aq_div<TI, TJ>(p, s0, lv, a, b, k0);
+                    const Q4 v0 = ldg4(V, c), v1 = ldg4(V, c + sy), v2 = ldg4(V, c - sx), v3 = ldg4(V, c - sx + sy);
+                    const Q4 m = ldg4(F.M[FU], c);
+                    Q4 r;
+#pragma unroll
+                    for (int e = 0; e < 4; e++) {
+                        const float ov_u = 0.25f * (v0.v[e] + v1.v[e] + v2.v[e] + v3.v[e]);
+                        const float ut = d.v[e] + p.dt * fj * ov_u;
+                        r.v[e] = m.v[e] + step * ut;
+                    }
+                    aq_store(F.P[FU], c, k0, nz, 1, r);
+                }
+                {
+                    const Q4 d = aq_div<TI, TJ>(p, s1, lv, a, b, k0);
+                    const Q4 u0 = ldg4(U, c), u1 = ldg4(U, c + sx), u2 = ldg4(U, c - sy), u3 = ldg4(U, c + sx - sy);
+                    const Q4 m = ldg4(F.M[FV], c);
+                    Q4 r;
+#pragma unroll
+                    for (int e = 0; e < 4; e++) {
+                        const float ov_v = 0.25f * (u0.v[e] + u1.v[e] + u2.v[e] + u3.v[e]);
+                        const float vt = d.v[e] - p.dt * fj * ov_v;
+                        r.v[e] = m.v[e] + step * vt;
+                    }
+                    aq_store(F.P[FV], c, k0, nz, 1, r);
+                }
+            }
+            if (what & ADV_WB) {
+                // buoyancy at levels k0-1 .. k0+3 (b1 of level k is b0 of level k-1)
+                const Win th = ldwin(F.cur[FTH], c, k0, nz);
+                Win qv, qc, qr;
+                if (p.moist) {
+                    qv = ldwin(F.cur[FQV], c, k0, nz);
+                    qc = ldwin(F.cur[FQC], c, k0, nz);
+                    qr = ldwin(F.cur[FQR], c, k0, nz);
+                }
+                float bb[5];
+#pragma unroll
+                for (int e = 0; e < 5; e++) {
+                    const int k = k0 + e - 1;
+                    const int kc = max(k, 0);
+                    if (!p.moist) bb[e] = th.at(e - 1) / s_tbv[kc];
+                    else bb[e] = th.at(e - 1) / s_tbv[kc] + 0.61f * qv.at(e - 1) - qc.at(e - 1) - qr.at(e - 1);
+                }
+                const Q4 m = ldg4(F.M[FW], c);
+                Q4 r;
+#pragma unroll
+                for (int e = 0; e < 4; e++) r.v[e] = m.v[e] + sdtg * (bb[e + 1] + bb[e]);
+                aq_store(F.P[FW], c, k0, nz, 2, r);
+            }
+        }
+        __syncthreads();
+    }
+
+    // ---- pass 2: theta, qv (qv's clipping bit)
+    const bool th_on = (what & ADV_TH) != 0, q_on = (what & ADV_Q) != 0;
+    if (th_on || q_on) {
+        if (th_on) aq_faces<TI, TJ, 2>(p, F, tab, s0, i0, j0, ti, tj);
+        if (q_on) aq_faces<TI, TJ, 3>(p, F, tab, s1, i0, j0, ti, tj);
+        __syncthreads();
+        for (int w = threadIdx.x; w < G::CT * NQ; w += AQ_THREADS) {
+            const int q = w % NQ, col = w / NQ, b = col % TJ, a = col / TJ;
+            if (a >= ti || b >= tj) continue;
+            const int i = i0 + a, j = j0 + b, k0 = 4 * q;
+            const int c = gix(p.ny, nz, i, j, k0);
+            const Win wc = ldwin(F.cur[FW], c, k0, nz);
+            for (int fi = 0; fi < 2; fi++) {
+                if (fi == 0 ? !th_on : !q_on) continue;
+                const float *base = fi == 0 ? s_tb : s_qb;
+                const Q4 d = aq_div<TI, TJ>(p, fi == 0 ? s0 : s1, lv, a, b, k0);
+                const Q4 m = ldg4(F.M[fi == 0 ? FTH : FQV], c);
+                Q4 r;
+                unsigned bits = 0;
+#pragma unroll
+                for (int e = 0; e < 4; e++) {
+                    const int k = k0 + e;
+                    const int kl = max(k - 1, 0), kh = min(k + 1, nz - 1);
+                    const float DTZ = p.dtz * s_mu[k];
+                    const float zab = 0.50f *
+                                      (s_rhow[kh] * wc.at(e + 1) * (base[kh] - base[k]) +
+                                       s_rhow[k] * wc.at(e) * (base[k] - base[kl])) *
+                                      s_odr[k];
+                    const float t = d.v[e] - DTZ * zab;
+                    float v = m.v[e] + step * t;
+                    if (fi == 1 && (what & ADV_ZERO)) {
+                        const float qbar = tab[BT_QB * nz + k];
+                        if (v + qbar + s_qb[k] < 0) {
+                            v = -(qbar + s_qb[k]);
+                            bits |= 1u << (8 * e);
+                        }
+                    }
+                    r.v[e] = v;
+                }
+                aq_store(F.P[fi == 0 ? FTH : FQV], c, k0, nz, 1, r);
+                if (fi == 1 && (what & ADV_ZERO) && F.qmask) {
+                    unsigned char *qm = F.qmask + c;
+#pragma unroll
+                    for (int e = 0; e < 4; e++) {
+                        const int k = k0 + e;
+                        if (k >= 1 && k <= nz - 2) qm[e] = (unsigned char)((bits >> (8 * e)) & 1u);
+                    }
+                }
+            }
+        }
+        __syncthreads();
+    }
+
+    // ---- pass 3: qc, qr (clipping bits 2 and 4, the rain's fall speed)
+    if (q_on) {
+        aq_faces<TI, TJ, 4>(p, F, tab, s0, i0, j0, ti, tj);
+        aq_faces<TI, TJ, 5>(p, F, tab, s1, i0, j0, ti, tj);
+        __syncthreads();
+        for (int w = threadIdx.x; w < G::CT * NQ; w += AQ_THREADS) {
+            const int q = w % NQ, col = w / NQ, b = col % TJ, a = col / TJ;
+            if (a >= ti || b >= tj) continue;
+            const int i = i0 + a, j = j0 + b, k0 = 4 * q;
+            const int c = gix(p.ny, nz, i, j, k0);
+            const Q4 dc = aq_div<TI, TJ>(p, s0, lv, a, b, k0);
+            const Q4 dr = aq_div<TI, TJ>(p, s1, lv, a, b, k0);
+            const Q4 mc = ldg4(F.M[FQC], c), mr = ldg4(F.M[FQR], c);
+            Q4 rc, rr;
+            unsigned char bits[4] = {0, 0, 0, 0};
+#pragma unroll
+            for (int e = 0; e < 4; e++) {
+                float qc = mc.v[e] + step * dc.v[e];
+                float qr = mr.v[e] + step * dr.v[e];
+                if (what & ADV_ZERO) {
+                    if (qc < 0) { qc = 0; bits[e] |= 2; }
+                    if (qr < 0) { qr = 0; bits[e] |= 4; }
+                }
+                rc.v[e] = qc;
+                rr.v[e] = qr;
+            }
+            aq_store(F.P[FQC], c, k0, nz, 1, rc);
+            aq_store(F.P[FQR], c, k0, nz, 1, rr);
+            if ((what & ADV_ZERO) && F.qmask) {
+                unsigned char *qm = F.qmask + c;
+#pragma unroll
+                for (int e = 0; e < 4; e++) {
+                    const int k = k0 + e;
+                    if (k >= 1 && k <= nz - 2) qm[e] |= bits[e];
+                }
+            }
+            if (p.rf == 1) {
+                // fall speed of the advected cells; level 0 repeats level 1
+                const Q4 qrc = ldg4(F.cur[FQR], c);
+#pragma unroll
+                for (int e = 0; e < 4; e++) {
+                    const int k = k0 + e;
+                    if (k >= 1 && k <= nz - 2) F.vt[c + e] = fall_speed_point(p, qrc.v[e], k);
+                    if (k == 1) F.vt[c + e - 1] = fall_speed_point(p, qrc.v[e], 1);
+                }
+            }
+        }
+    }
+}
+
+}  // namespace ga

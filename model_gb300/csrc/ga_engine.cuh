@@ -4,6 +4,7 @@
 #pragma once
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <string>
@@ -11,6 +12,7 @@
 
 #include "ga_engine.h"
 #include "ga_kernels.cuh"
+#include "ga_advect_quad.cuh"
 
 namespace ga {
 
@@ -94,6 +96,10 @@ class Engine : public EngineBase {
     int status = GA_OK;
     std::unique_ptr<LinBase> lin;  // tangent-linear / adjoint buffers, on first use
     int adv_ti = ADV_TI, adv_tj = ADV_TJ;  // advection tile (autotuned)
+    // the four-level advection kernel (FP32, uniform basic state, NZ % 4 == 0)
+    // and its tile; GA_ADVECT=tile or =quad restricts both the default and the
+    // autotuner to one kernel
+    int adv_quad = 1, adv_qi = 4, adv_qj = 8, adv_force = 0;
     unsigned char *qmask = nullptr;         // clipping record of the next advection (linearisation)
     int plan_order_i = 0, plan_order_j = 0;
 
@@ -275,6 +281,14 @@ class Engine : public EngineBase {
         cudaFuncSetAttribute(k_advect_tile<T, 4, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
         cudaFuncSetAttribute(k_advect_tile<T, 4, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
         cudaFuncSetAttribute(k_advect_tile<T, 8, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+        if (const char *ev = std::getenv("GA_ADVECT")) {
+            if (!std::strcmp(ev, "tile")) adv_force = 1;
+            else if (!std::strcmp(ev, "quad")) adv_force = 2;
+        }
+        adv_quad = adv_force != 1;
+        if constexpr (sizeof(T) == 4) {
+            for (auto &tl : kQuadTiles) quad_attr(tl[0], tl[1], optin);
+        }
         cudaFuncSetAttribute(k_div_fft_y<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
         cudaFuncSetAttribute(k_ifft_y_pi<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
         cudaFuncSetAttribute(k_fft_x<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
@@ -464,11 +478,49 @@ class Engine : public EngineBase {
         k_advect_tile<T, TI, TJ><<<grid, 256, smem_adv, stream>>>(kp, fields(), step, sdtg, what);
     }
 
+    // the four-level kernel's tiles the autotuner chooses from
+    static constexpr int kQuadTiles[5][2] = {{4, 4}, {4, 8}, {8, 4}, {2, 8}, {8, 8}};
+    template <int TI, int TJ>
+    void launch_advect_quad(T step, T sdtg, int what)
+    {
+        if constexpr (sizeof(T) == 4) {
+            dim3 grid(cdiv(NX - 6, TI), cdiv(NY - 6, TJ));
+            k_advect_quad<TI, TJ><<<grid, AQ_THREADS, advect_quad_smem(TI, TJ, NZ), stream>>>(kp, fields(), step,
+                                                                                            sdtg, what);
+        }
+    }
+    template <int TI, int TJ>
+    static void quad_attr_t(int optin)
+    {
+        cudaFuncSetAttribute(k_advect_quad<TI, TJ>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+    }
+    static void quad_attr(int ti, int tj, int optin)
+    {
+        if (ti == 4 && tj == 4) quad_attr_t<4, 4>(optin);
+        else if (ti == 4 && tj == 8) quad_attr_t<4, 8>(optin);
+        else if (ti == 8 && tj == 4) quad_attr_t<8, 4>(optin);
+        else if (ti == 2 && tj == 8) quad_attr_t<2, 8>(optin);
+        else if (ti == 8 && tj == 8) quad_attr_t<8, 8>(optin);
+    }
+    // the four-level kernel applies: FP32, basic state a function of height,
+    // whole quads of levels, face columns within the shared-memory limit
+    bool quad_ok(int ti, int tj) const
+    {
+        return sizeof(T) == 4 && kp.ubase_adv && NZ % 4 == 0 && advect_quad_smem(ti, tj, NZ) <= 200 * 1024;
+    }
+
     void advect(double step, int what)
     {
         const double sdtg = step * cfg.dt * 9.8 * 0.5;  // step*dt*grav*0.5, advection.cpp:330
         ProfScope ps(this, PC_ADVECT, 1);
-        if (smem_adv <= 200 * 1024) {
+        if (adv_quad && quad_ok(adv_qi, adv_qj)) {
+            const T st = (T)step, sg = (T)sdtg;
+            if (adv_qi == 4 && adv_qj == 4) launch_advect_quad<4, 4>(st, sg, what);
+            else if (adv_qi == 8 && adv_qj == 4) launch_advect_quad<8, 4>(st, sg, what);
+            else if (adv_qi == 2) launch_advect_quad<2, 8>(st, sg, what);
+            else if (adv_qi == 8) launch_advect_quad<8, 8>(st, sg, what);
+            else launch_advect_quad<4, 8>(st, sg, what);
+        } else if (smem_adv <= 200 * 1024) {
             const T st = (T)step, sg = (T)sdtg;
             if (adv_ti == 2) launch_advect_tile<2, 4>(st, sg, what);
             else if (adv_tj == 2) launch_advect_tile<4, 2>(st, sg, what);
@@ -756,17 +808,30 @@ class Engine : public EngineBase {
         // advection tile
         {
             float best = 1e30f;
-            int bi = adv_ti, bj = adv_tj;
-            for (auto &tl : kAdvTiles) {
-                const size_t sm = advect_tile_smem(tl[0], tl[1], NZ, sizeof(T));
-                if (sm > 200 * 1024) continue;
-                adv_ti = tl[0]; adv_tj = tl[1]; smem_adv = sm;
-                const float t = timeit([&] { advect(1. / 3., what); });
-                if (t < best) { best = t; bi = tl[0]; bj = tl[1]; }
+            int bi = adv_ti, bj = adv_tj, bq = 0, qi = adv_qi, qj = adv_qj;
+            if (adv_force != 2 || !quad_ok(adv_qi, adv_qj)) {
+                adv_quad = 0;
+                for (auto &tl : kAdvTiles) {
+                    const size_t sm = advect_tile_smem(tl[0], tl[1], NZ, sizeof(T));
+                    if (sm > 200 * 1024) continue;
+                    adv_ti = tl[0]; adv_tj = tl[1]; smem_adv = sm;
+                    const float t = timeit([&] { advect(1. / 3., what); });
+                    if (t < best) { best = t; bi = tl[0]; bj = tl[1]; }
+                }
             }
-            adv_ti = bi; adv_tj = bj;
+            if (adv_force != 1) {
+                adv_quad = 1;
+                for (auto &tl : kQuadTiles) {
+                    if (!quad_ok(tl[0], tl[1])) continue;
+                    adv_qi = tl[0]; adv_qj = tl[1];
+                    const float t = timeit([&] { advect(1. / 3., what); });
+                    if (t < best) { best = t; bq = 1; qi = tl[0]; qj = tl[1]; }
+                }
+            }
+            adv_ti = bi; adv_tj = bj; adv_quad = bq; adv_qi = qi; adv_qj = qj;
             smem_adv = advect_tile_smem(bi, bj, NZ, sizeof(T));
-            std::snprintf(line, sizeof line, "advect tile %dx%d (%.4f ms); ", bi, bj, best);
+            if (bq) std::snprintf(line, sizeof line, "advect tile %dx%d, four levels per thread (%.4f ms); ", qi, qj, best);
+            else std::snprintf(line, sizeof line, "advect tile %dx%d (%.4f ms); ", bi, bj, best);
             info += line;
         }
         // y transforms: level tile, then factor order

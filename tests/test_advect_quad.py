@@ -1,0 +1,106 @@
+"""The FP32 four-level advection kernel (k_advect_quad) against the per-level
+tile kernel (k_advect_tile) on the same inputs.
+
+Both evaluate the same face and tendency expressions level by level, so a
+single advection operator must agree bit for bit; whole steps are compared
+to a relative L2 of 1e-6 (the pressure solve's FFT runs the same code on
+both sides, so any difference would come from the advection alone).
+GA_ADVECT selects the kernel when a context is created.
+"""
+import numpy as np
+import pytest
+
+from model_gb300 import abi, anelastic, configs
+from tests import fixtures as fx
+
+pytestmark = pytest.mark.gpu
+
+ADVECT_OPS = {
+    "advect_uvw": (abi.PROG_NAMES.index("u"), abi.PROG_NAMES.index("v"), abi.PROG_NAMES.index("w")),
+    "advect_theta": (abi.PROG_NAMES.index("th"),),
+    "advect_micro": (abi.PROG_NAMES.index("qv"), abi.PROG_NAMES.index("qc"), abi.PROG_NAMES.index("qr")),
+}
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    from model_gb300 import build
+    build.build()
+
+
+def _pair(monkeypatch, wl):
+    ms = []
+    for mode in ("tile", "quad"):
+        monkeypatch.setenv("GA_ADVECT", mode)
+        ms.append(anelastic.Model(wl, abi.GA_PREC_F32))
+    monkeypatch.delenv("GA_ADVECT")
+    return ms
+
+
+def _perturb(ms, wl, seed):
+    """random current and start-of-step states, the same in every model;
+    moisture straddles zero so that clipping takes both branches"""
+    rng = np.random.default_rng(seed)
+    n = wl.nx * wl.ny * wl.nz
+    nprog = 7 if wl.microphysics_option else 4
+    scale = [2.0, 2.0, 0.5, 0.3, 1e-3, 4e-4, 4e-4]
+    for f in range(nprog):
+        for slot in (abi.GA_SLOT_CUR, abi.GA_SLOT_M):
+            x = rng.standard_normal(n) * scale[f]
+            if f >= 5:
+                x = x + 2e-4
+            for m in ms:
+                m.set(f, slot, x)
+
+
+@pytest.mark.parametrize("case", ["moist_rf1", "moist_rf2", "dry"])
+def test_single_advection_operator_bit_identical(monkeypatch, case):
+    if case == "dry":
+        wl = configs.dry_bubble(nx=30, ny=26, nz=20, nsteps=2)
+    else:
+        wl = configs.moist_blob(nx=30, ny=26, nz=16, rain_fallout=1 if case == "moist_rf1" else 2)
+    ms = _pair(monkeypatch, wl)
+    _perturb(ms, wl, 11)
+    for op, fields in ADVECT_OPS.items():
+        if op == "advect_micro" and not wl.microphysics_option:
+            continue
+        for m in ms:
+            m.op(op, 0.5)
+        for f in fields:
+            a, b = (m.get(f, abi.GA_SLOT_P) for m in ms)
+            np.testing.assert_array_equal(b, a, err_msg=f"{case} {op} field {abi.PROG_NAMES[f]}")
+
+
+@pytest.mark.parametrize("case", ["moist_blob", "thunderstorm_small", "dry_bubble", "nz_not_multiple_of_4"])
+def test_steps_match_tile_kernel(monkeypatch, case):
+    if case == "moist_blob":
+        wl = configs.moist_blob(nx=30, ny=26, nz=16, nsteps=6)
+    elif case == "thunderstorm_small":
+        wl = configs.thunderstorm(nx=44, ny=38, nsteps=6)
+    elif case == "dry_bubble":
+        wl = configs.dry_bubble(nx=34, ny=30, nz=20, nsteps=6)
+    else:  # falls back to the tile kernel: both contexts run the same code
+        wl = configs.moist_blob(nx=30, ny=26, nz=18, nsteps=6)
+    ms = _pair(monkeypatch, wl)
+    for m in ms:
+        m.step(wl.nsteps)
+    nprog = 7 if wl.microphysics_option else 4
+    worst = 0.0
+    for f in list(range(nprog)) + [abi.GA_PI]:
+        a, b = (m.get(f) for m in ms)
+        e = fx.rel_l2(b, a)
+        worst = max(worst, e)
+        assert e <= 1e-6, f"{case} field {f}: rel L2 {e:.3e}"
+    print(case, f"worst rel L2 {worst:.2e}")
+
+
+def test_autotuner_reports_the_kernel(monkeypatch):
+    wl = configs.thunderstorm(nx=44, ny=38, nsteps=2)
+    monkeypatch.setenv("GA_ADVECT", "quad")
+    m = anelastic.Model(wl, abi.GA_PREC_F32)
+    info = m.tune()
+    assert "four levels per thread" in info, info
+    monkeypatch.setenv("GA_ADVECT", "tile")
+    m2 = anelastic.Model(wl, abi.GA_PREC_F32)
+    info2 = m2.tune()
+    assert "four levels per thread" not in info2, info2
