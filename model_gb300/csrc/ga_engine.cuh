@@ -12,7 +12,7 @@
 
 #include "ga_engine.h"
 #include "ga_kernels.cuh"
-#include "ga_advect_quad.cuh"
+#include "ga_quad.cuh"
 
 namespace ga {
 
@@ -86,6 +86,7 @@ class Engine : public EngineBase {
     double *staging = nullptr;
     int KTy = 1, KTx = 1, lgKTy = 0, lgKTx = 0, TC = 64;
     int psx = 0;  // point stride of the fused spectral-x kernel (0: unfused path)
+    int sx_threads = 256;  // threads of a fused spectral-x block (autotuned)
     size_t smem_y = 0, smem_x = 0, smem_th = 0, smem_sx = 0, smem_adv = 0;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     bool bar_uniform[6] = {false, false, false, false, false, false};
@@ -100,6 +101,9 @@ class Engine : public EngineBase {
     // and its tile; GA_ADVECT=tile or =quad restricts both the default and the
     // autotuner to one kernel
     int adv_quad = 1, adv_qi = 4, adv_qj = 8, adv_force = 0;
+    // the four-level post-processing kernel (FP32, NZ % 4 == 0); GA_POST=column
+    // keeps the per-level one
+    bool post_quad = true;
     unsigned char *qmask = nullptr;         // clipping record of the next advection (linearisation)
     int plan_order_i = 0, plan_order_j = 0;
 
@@ -286,6 +290,8 @@ class Engine : public EngineBase {
             else if (!std::strcmp(ev, "quad")) adv_force = 2;
         }
         adv_quad = adv_force != 1;
+        if (const char *ev = std::getenv("GA_POST")) post_quad = std::strcmp(ev, "column") != 0;
+        post_quad = post_quad && sizeof(T) == 4 && NZ % 4 == 0;
         if constexpr (sizeof(T) == 4) {
             for (auto &tl : kQuadTiles) quad_attr(tl[0], tl[1], optin);
         }
@@ -561,7 +567,8 @@ class Engine : public EngineBase {
         if (psx > 0) {
             ProfScope ps(this, PC_THOMAS, 1);
             const int nl = NZ - 2, bx = std::min(nl, 64);
-            k_spectral_x<T><<<kp.nj, dim3(bx, std::max(1, 256 / bx)), smem_sx, stream>>>(kp, spec, plan_i, tw_i, psx);
+            k_spectral_x<T><<<kp.nj, dim3(bx, std::max(1, sx_threads / bx)), smem_sx, stream>>>(kp, spec, plan_i,
+                                                                                               tw_i, psx);
             launches += 1;
         } else {
             {
@@ -600,6 +607,22 @@ class Engine : public EngineBase {
         for (int f = 0; f < nfields && f < 7; f++) fl[f] = f < nprog ? flags[f] : 0;
         int4 a = make_int4(fl[0], fl[1], fl[2], fl[3]), b = make_int4(fl[4], fl[5], fl[6], fl[7]);
         ProfScope ps(this, PC_POST, (pcopy && kp.periodic) ? 2 : 1);
+        if constexpr (sizeof(T) == 4) {
+            if (post_quad) {
+                const long nq = NZ / 4;
+                auto go = [&](long ncols, int mode) {
+                    k_post_quad<T><<<cdiv(ncols * nq, PQ_THREADS), PQ_THREADS, 0, stream>>>(kp, F, a, b, (T)step, mode);
+                    launches++;
+                };
+                if (pcopy && kp.periodic) {
+                    go(6L * NY, COLS_TARGETS);
+                    go((long)(NX - 6) * NY, COLS_NONTARGETS);
+                } else {
+                    go((long)NX * NY, COLS_ALL);
+                }
+                return;
+            }
+        }
         if (pcopy && kp.periodic) {
             k_post<T><<<cdiv(6L * NY, POST_COLS), POST_THREADS, 0, stream>>>(kp, F, 7, a, b, (T)step, COLS_TARGETS);
             k_post<T><<<cdiv((long)(NX - 6) * NY, POST_COLS), POST_THREADS, 0, stream>>>(kp, F, 7, a, b, (T)step,
@@ -880,22 +903,38 @@ class Engine : public EngineBase {
             }
             plan_order_i = bxo;
             plan_i = make_fft_plan(kp.ni, bxo);
-            if (psx == 0) {
-                int bkx = KTx;
+            // the fused x kernel's block size
+            if (psx > 0) {
+                const int keep = sx_threads;
+                sx_threads = 512;
+                const float t = timeit([&] { solve_pressure(1. / 3.); });
+                if (t < bx) bx = t;
+                else sx_threads = keep;
+            }
+            // the unfused path (x FFT, Thomas, inverse x FFT) and its level
+            // tile, against the fused kernel where that fits
+            {
+                const int keep_psx = psx, keep_kt = KTx;
+                psx = 0;
+                int bkx = -1;
                 for (int kt = 1; kt <= 64 && kt <= 2 * (NZ - 2); kt <<= 1) {
                     if (2 * (size_t)kp.ni * kt * sizeof(T2) > 200 * 1024) break;
-                    const int keep = KTx;
                     KTx = kt;
                     smem_x = 2 * (size_t)kp.ni * KTx * sizeof(T2);
                     const float t = timeit([&] { solve_pressure(1. / 3.); });
-                    if (t < bx) { bx = t; bkx = kt; }
-                    KTx = keep;
+                    if (t < bx || (keep_psx == 0 && bkx < 0)) { bx = std::min(bx, t); bkx = kt; }
                 }
-                KTx = bkx;
+                if (bkx > 0) {
+                    KTx = bkx;
+                } else {
+                    psx = keep_psx;
+                    KTx = keep_kt;
+                }
                 lgKTx = 0;
                 while ((1 << lgKTx) < KTx) lgKTx++;
                 smem_x = 2 * (size_t)kp.ni * KTx * sizeof(T2);
-                std::snprintf(line, sizeof line, "x level tile %d, ", KTx);
+                if (psx == 0) std::snprintf(line, sizeof line, "x level tile %d, ", KTx);
+                else std::snprintf(line, sizeof line, "x fused, %d threads, ", sx_threads);
                 info += line;
             }
             std::snprintf(line, sizeof line, "x FFT order %d (pressure solve %.4f ms)", bxo, bx);

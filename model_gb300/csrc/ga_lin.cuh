@@ -243,7 +243,7 @@ struct Lin : LinBase {
         k_adj_fft_y_in<T><<<dim3(nkt_y, e.kp.ni), by_y, e.smem_y, s>>>(e.kp, lpi_f, e.spec, e.plan_j, e.tw_j, e.KTy);
         if (e.psx > 0) {  // x transforms and the solves fused, as in the forward step
             const int nl = e.NZ - 2, bx = std::min(nl, 64);
-            k_spectral_x_adj<T><<<e.kp.nj, dim3(bx, std::max(1, 256 / bx)), e.smem_sx, s>>>(e.kp, e.spec, e.plan_i,
+            k_spectral_x_adj<T><<<e.kp.nj, dim3(bx, std::max(1, e.sx_threads / bx)), e.smem_sx, s>>>(e.kp, e.spec, e.plan_i,
                                                                                           e.tw_i, e.psx);
             e.launches += 1;
         } else {

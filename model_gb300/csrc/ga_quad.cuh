@@ -1,7 +1,10 @@
 // ---------------------------------------------------------------------------
-// FP32 advection with four levels per thread (advection.cpp:304-497 with the
-// face fluxes of fluxes.cpp), for a horizontally uniform basic state and NZ a
+// FP32 kernels with four levels per thread: a work item is one column and one
+// aligned quad of levels k0..k0+3, read and written as 16-byte rows.  NZ is a
 // multiple of 4.
+//
+// k_advect_quad: advection (advection.cpp:304-497 with the face fluxes of
+// fluxes.cpp) for a horizontally uniform basic state.
 //
 // A block owns TI x TJ interior columns at every level, as k_advect_tile
 // does, but a work item is one column and one aligned quad of levels
@@ -538,6 +541,110 @@ __global__ void __launch_bounds__(AQ_THREADS, 3)
                 }
             }
         }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// k_post_quad: the column post-processing of k_post, expression for
+// expression.  A column's bottom and top conditions copy level 1 to 0 and
+// NZ-2 to NZ-1, both inside one quad, so every thread reads and writes only
+// its own points and the fields go one after another without a barrier.
+// ---------------------------------------------------------------------------
+constexpr int PQ_THREADS = 256;
+
+template <typename T>
+__global__ void __launch_bounds__(PQ_THREADS)
+    k_post_quad(KParams<T> p, KFields<T> F, int4 fl0, int4 fl1, T step, int cols)
+{
+    static_assert(sizeof(T) == 4, "four-level kernels are FP32");
+    const int nz = p.nz, NQ = nz >> 2, sx = p.ny * nz, sy = nz;
+    const long w = (long)blockIdx.x * PQ_THREADS + threadIdx.x;
+    const int q = (int)(w % NQ), k0 = 4 * q;
+    int i = 0, j = 0;
+    bool ok = false;
+    post_column(cols, w / NQ, p.nx, p.ny, i, j, ok);
+    if (!ok) return;
+    const int flv[7] = {fl0.x, fl0.y, fl0.z, fl0.w, fl1.x, fl1.y, fl1.z};
+    // the chain runs at the source column (the column itself, or the column a
+    // periodic target copies)
+    const int si = cols == COLS_TARGETS ? (i < 3 ? p.nx - 6 + i : 3 + (i - (p.nx - 3))) : i;
+    const int cs = gix(p.ny, nz, si, j, k0), c = gix(p.ny, nz, i, j, k0);
+    const bool col_in = si >= 1 && si < p.nx - 1 && j >= 1 && j < p.ny - 1;
+    const bool vbc = i >= 1 && j >= 1;
+    const bool ray_col = i >= 1 && i < p.nx - 1 && j >= 1 && j < p.ny - 1;
+    // sponge strips of the column (boundaries.cpp:481-498); every level k >= 1
+    const bool hE = !p.periodic && j >= 1 && si >= p.eb && si < p.ee;
+    const bool hW = !p.periodic && j >= 1 && si >= p.wb && si < p.we;
+    const bool hS = si >= 1 && j >= p.sb && j < p.se;
+    const bool hN = si >= 1 && j >= p.nb && j < p.ne;
+    const float cE = hE ? p.ce[si - p.eb] : 0.f, cW = hW ? p.cw[si - p.wb] : 0.f;
+    const float cS = hS ? p.cs[j - p.sb] : 0.f, cN = hN ? p.cn[j - p.nb] : 0.f;
+    float dpx[4] = {0.f, 0.f, 0.f, 0.f}, dpy[4] = {0.f, 0.f, 0.f, 0.f}, dpz[4] = {0.f, 0.f, 0.f, 0.f};
+    if (col_in && ((flv[FU] | flv[FV] | flv[FW]) & PF_PROJECT)) {
+        const Win pc = ldwin(F.pi, cs, k0, nz);
+        const Q4 px = ldg4(F.pi, cs - sx), py = ldg4(F.pi, cs - sy);
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+            dpx[e] = pc.at(e) - px.v[e];
+            dpy[e] = pc.at(e) - py.v[e];
+            dpz[e] = pc.at(e) - pc.at(e - 1);
+        }
+    }
+#pragma unroll 1
+    for (int f = 0; f < 7; ++f) {
+        const int flags = flv[f];
+        if (!flags) continue;
+        const Q4 in = ldg4(F.P[f], cs);
+        Q4 qb4{{0.f, 0.f, 0.f, 0.f}};
+        if ((flags & PF_ZERO) && f == FQV && col_in) qb4 = ldg4(F.bar[4], cs);
+        float ch[4];
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+            const int k = k0 + e;
+            const bool inner = col_in && k >= 1 && k < nz - 1;
+            float v = in.v[e];
+            if (flags & PF_ZERO) {  // zero_moisture, microphysics.cpp:675-700
+                if (f == FQC || f == FQR) {
+                    if (v < 0) v = 0;
+                } else if (f == FQV && inner) {
+                    const float qbar = qb4.v[e];
+                    if (v + qbar + p.qb[k] < 0) v = -(qbar + p.qb[k]);
+                }
+            }
+            if ((flags & PF_PROJECT) && inner) {  // solver.cpp:123-135
+                if (f == FU) v = v - step * (p.dtx * dpx[e]);
+                else if (f == FV) v = v - step * (p.dty * dpy[e]);
+                else if (f == FW && k >= 2) v = v - step * ((p.dtz * p.mw[k]) * dpz[e]);
+            }
+            if ((flags & PF_SPONGE) && k >= 1) {
+                if (hE) v = v - cE * v;
+                if (hW) v = v - cW * v;
+                if (hS) v = v - cS * v;
+                if (hN) v = v - cN * v;
+            }
+            ch[e] = v;
+        }
+        Q4 out;
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+            const int k = k0 + e;
+            float v = ch[e];
+            if ((flags & PF_VBC) && vbc) {  // boundaries.cpp:304-326
+                if (f == FW) {
+                    if (k == 0 || k == 1 || k == nz - 1) v = 0.f;
+                } else {
+                    if (k == 0) v = ch[1];
+                    if (k == nz - 1) v = ch[2];
+                }
+            }
+            if ((flags & PF_RAYLEIGH) && f <= FTH && ray_col && k >= p.raylevel) {  // damping.cpp:1148-1177
+                const float cr = (f == FW) ? p.ray_w[k] : p.ray_u[k];
+                v = v - cr * v;
+            }
+            out.v[e] = v;
+        }
+        stg4(F.P[f] + c, out);
+        if (flags & PF_WRITE_M) stg4(F.M[f] + c, out);
     }
 }
 

@@ -104,3 +104,30 @@ def test_autotuner_reports_the_kernel(monkeypatch):
     m2 = anelastic.Model(wl, abi.GA_PREC_F32)
     info2 = m2.tune()
     assert "four levels per thread" not in info2, info2
+
+
+@pytest.mark.parametrize("case", ["moist_blob", "periodic_rf2", "dry_bubble", "thunderstorm_small"])
+def test_post_quad_matches_column_kernel(monkeypatch, case):
+    """k_post_quad against k_post (GA_POST=column): whole steps, every
+    prognostic field, pi and the accumulated rain bit for bit"""
+    if case == "moist_blob":
+        wl = configs.moist_blob(nx=30, ny=26, nz=16, nsteps=4)
+    elif case == "periodic_rf2":
+        wl = configs.moist_blob(nx=30, ny=24, nz=16, nsteps=4, periodic=1, rain_fallout=2)
+    elif case == "dry_bubble":
+        wl = configs.dry_bubble(nx=34, ny=30, nz=20, nsteps=4)
+    else:
+        wl = configs.thunderstorm(nx=44, ny=38, nsteps=4)
+    ms = []
+    for mode in ("column", "quad"):
+        monkeypatch.setenv("GA_POST", mode)
+        ms.append(anelastic.Model(wl, abi.GA_PREC_F32))
+    monkeypatch.delenv("GA_POST")
+    for m in ms:
+        m.step(wl.nsteps)
+    nprog = 7 if wl.microphysics_option else 4
+    fields = list(range(nprog)) + [abi.GA_PI] + ([abi.GA_ACCRAIN] if wl.microphysics_option else [])
+    for f in fields:
+        for slot in ((abi.GA_SLOT_CUR, abi.GA_SLOT_M) if f < nprog else (abi.GA_SLOT_CUR,)):
+            a, b = (m.get(f, slot) for m in ms)
+            np.testing.assert_array_equal(b, a, err_msg=f"{case} field {f} slot {slot}")
