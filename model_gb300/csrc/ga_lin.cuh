@@ -8,6 +8,7 @@
 
 #include "ga_engine.cuh"
 #include "ga_lin_kernels.cuh"
+#include "ga_adj_quad.cuh"
 
 namespace ga {
 
@@ -32,6 +33,9 @@ struct Lin : LinBase {
     // two recorded steps into trajectory slots (2m, 2m+1), per rotation parity
     std::vector<cudaGraphExec_t> rec_graph[2];
     std::vector<long long> rec_graph_launches[2];
+    // the four-level adjoint advection (FP32, NZ % 4 == 0); GA_ADJ=level keeps
+    // the per-level kernel
+    bool adj_quad = false;
 
     explicit Lin(Engine<T> &eng) : e(eng), N(eng.N), nf(eng.nprog)
     {
@@ -53,6 +57,12 @@ struct Lin : LinBase {
         cudaFuncSetAttribute(k_spectral_x_adj<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
         cudaFuncSetAttribute(k_adj_advect<T, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
         cudaFuncSetAttribute(k_adj_advect<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+        if constexpr (sizeof(T) == 4) {
+            const char *ev = std::getenv("GA_ADJ");
+            adj_quad = e.NZ % 4 == 0 && !(ev && !std::strcmp(ev, "level"));
+            cudaFuncSetAttribute(k_adj_advect_quad<T, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+            cudaFuncSetAttribute(k_adj_advect_quad<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+        }
     }
     ~Lin() override
     {
@@ -303,12 +313,18 @@ struct Lin : LinBase {
             const T sdtg = (T)(step * e.cfg.dt * 9.8 * 0.5);
             k_lin_coef<T><<<cdiv(N, 128), 128, 0, s>>>(e.kp, R, coef, fields(), qm);
             const int zc = (first && st == 2) ? 0 : 1;
-            k_adj_advect<T, 0><<<gadv, AJ_THREADS, smem_adv, s>>>(e.kp, coef, fields(), (T)step, sdtg, zc);
-            e.launches += 2;
-            if (moist) {
-                k_adj_advect<T, 1><<<gadv, AJ_THREADS, smem_adv, s>>>(e.kp, coef, fields(), (T)step, sdtg, zc);
-                e.launches++;
+            e.launches += 2 + (moist ? 1 : 0);
+            if constexpr (sizeof(T) == 4) {
+                if (adj_quad) {
+                    k_adj_advect_quad<T, 0><<<gadv, AJ_THREADS, QJ_SMEM, s>>>(e.kp, coef, fields(), (T)step, sdtg, zc);
+                    if (moist)
+                        k_adj_advect_quad<T, 1><<<gadv, AJ_THREADS, QJ_SMEM, s>>>(e.kp, coef, fields(), (T)step, sdtg,
+                                                                                 zc);
+                    continue;
+                }
             }
+            k_adj_advect<T, 0><<<gadv, AJ_THREADS, smem_adv, s>>>(e.kp, coef, fields(), (T)step, sdtg, zc);
+            if (moist) k_adj_advect<T, 1><<<gadv, AJ_THREADS, smem_adv, s>>>(e.kp, coef, fields(), (T)step, sdtg, zc);
         }
     }
 

@@ -425,3 +425,27 @@ def test_gpu_moist_checkpointing_is_exact(built):
     for o in outs[1:]:
         for k in MOIST:
             assert np.array_equal(o[k], outs[0][k]), k
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("moist", [False, True])
+def test_gpu_adjoint_quad_kernel_matches_level_kernel(built, monkeypatch, moist):
+    """FP32: the four-level adjoint advection (the default when NZ % 4 == 0)
+    against the per-level kernel (GA_ADJ=level), bit for bit.  Both grids are
+    ragged against the 16 x 8 x 8 tiles; NZ = 12 leaves a half level tile."""
+    if moist:
+        wl = configs.moist_blob(nx=24, ny=22, nz=16)
+        st, y = moist_state(wl, False), moist_dirs(wl, 31)
+    else:
+        wl = small_vortex(nx=24, ny=20, nz=12)
+        st, y = trajectory_state(wl), random_dirs(wl, 22)
+    outs = []
+    for mode in ("level", "quad"):
+        monkeypatch.setenv("GA_ADJ", mode)
+        m = _model(wl, st, abi.GA_PREC_F32)
+        m.lin_set_all(y)
+        m.adjoint(4, 2)
+        outs.append(m.lin_get_all())
+    monkeypatch.delenv("GA_ADJ")
+    for k in outs[0]:
+        np.testing.assert_array_equal(outs[1][k], outs[0][k], err_msg=str(k))
