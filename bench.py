@@ -291,7 +291,10 @@ def ensemble_bench(torch, device, steps, warmup, n_small=64, n_large=32):
 def adjoint_bench(torch, device, steps, every, moist=False, size=512):
     """Forward vs forward+adjoint: `steps` steps from the initial state, then
     the adjoint of the whole run back to it with the state checkpointed every
-    `every` steps and each segment recomputed.  Dry: the monsoon vortex
+    `every` steps.  The library keeps the trajectories of as many of the last
+    segments as device memory holds and recomputes the others; the
+    `*_one_resident` figures force one (every segment but the last
+    recomputed).  Dry: the monsoon vortex
     (192x128x32, dx=dy=40 km, dz=600 m, dt=120 s), FP32 and FP64.  Moist: the
     Kessler squall line (size x size x 64, dx=dy=1 km, dz=300 m, dt=3 s), FP32.
     One job per timing, bracketed by CUDA events on the library stream, L2
@@ -351,11 +354,20 @@ def adjoint_bench(torch, device, steps, every, moist=False, size=512):
         l1 = m.launch_count()
         t_adj = timed(lambda: m.adjoint(steps, every))
         l2 = m.launch_count()
+        free, total = torch.cuda.mem_get_info(device)
+        os.environ["GA_ADJ_RESIDENT"] = "1"
+        try:
+            t_adj1 = timed(lambda: m.adjoint(steps, every))
+        finally:
+            del os.environ["GA_ADJ_RESIDENT"]
         pts = wl.points * steps
         out[name] = {"fwd_ms": round(t_fwd, 2), "fwd_adj_ms": round(t_adj, 2),
                      "fwd_adj_over_fwd": round(t_adj / t_fwd, 3),
                      "value_fwd": round(pts / (t_fwd * 1e-3), 1), "value_fwd_adj": round(pts / (t_adj * 1e-3), 1),
-                     "unit": UNIT, "launches_fwd_adj": int(l2 - l1)}
+                     "unit": UNIT, "launches_fwd_adj": int(l2 - l1),
+                     "device_gb_in_use": round((total - free) / 1e9, 1),
+                     "fwd_adj_ms_one_resident": round(t_adj1, 2),
+                     "fwd_adj_over_fwd_one_resident": round(t_adj1 / t_fwd, 3)}
         m.close()
     return out
 

@@ -32,7 +32,10 @@ static_assert(AJ_BK == QJ_ZR, "tendency rows hold levels k0-2 .. k0+TK+1");
 // x2, level factors of the z faces
 constexpr int QJ_CB = 0, QJ_FS = 4 * QJ_NFACE, QJ_FAB = 5 * QJ_NFACE, QJ_TB = 6 * QJ_NFACE,
               QJ_ZF = 6 * QJ_NFACE + 2 * QJ_NTB;
-constexpr size_t QJ_SMEM = (size_t)(QJ_ZF + 2 * QJ_ZR) * sizeof(float);
+// then the basic-state term factors of the tile's levels (theta, qv; below
+// and above the cell) and the Coriolis parameter of rows j0-1 .. j0+TJ
+constexpr int QJ_BF = QJ_ZF + 2 * QJ_ZR, QJ_FC = QJ_BF + 4 * AJ_TK;
+constexpr size_t QJ_SMEM = (size_t)(QJ_FC + AJ_TJ + 2) * sizeof(float);
 
 template <int DIR>
 struct QBox {
@@ -113,11 +116,9 @@ __device__ __forceinline__ void qj_issue_tb(const KParams<float> &p, const KFiel
 // Coriolis of u into v and of v into u, the basic-state theta / qv term into
 // w, for the thread's cell quad (adj_extra)
 template <int EQ>
-__device__ __forceinline__ void qj_extra(const KParams<float> &p, const float *tb, float step, int j0, int k0,
-                                         int li, int lj, int lq, float (&acc)[4][7])
+__device__ __forceinline__ void qj_extra(const KParams<float> &p, const float *tb, const float *sm, float step,
+                                         int j0, int k0, int li, int lj, int lq, float (&acc)[4][7])
 {
-    const float fdt = p.dt * 0.25f;
-    const int pj = j0 + lj;
     auto row = [&](int di, int dj) { return tb + ((li + 3 + di) * AJ_BJ + (lj + 3 + dj)) * QJ_ZR; };
     if (EQ == 0 || EQ == 1) {
         const int di[4] = {0, 0, 1, 1}, dj[4] = {0, -1, 0, -1};
@@ -126,7 +127,7 @@ __device__ __forceinline__ void qj_extra(const KParams<float> &p, const float *t
         for (int n = 0; n < 4; n++) {
             const int a = EQ == 0 ? di[n] : ei[n], b = EQ == 0 ? dj[n] : ej[n];
             const Q4 t = lds2x2(row(a, b) + 4 * lq + 2);
-            const float fc = fdt * p.f[pj + b];
+            const float fc = sm[QJ_FC + lj + 1 + b];  // fdt * f of row j0+lj+b
 #pragma unroll
             for (int e = 0; e < 4; e++) {
                 const float tv = step * t.v[e];
@@ -137,20 +138,16 @@ __device__ __forceinline__ void qj_extra(const KParams<float> &p, const float *t
             }
         }
     } else if (EQ == 2 || EQ == 3) {
-        const float *base = EQ == 2 ? p.tb : p.qb;
+        const float *bf = sm + QJ_BF + (EQ - 2) * 2 * AJ_TK;  // [below | above] x tile levels
         const float *rw = row(0, 0) + 4 * lq;
         const Q4 lo = lds4(rw), hi = lds4(rw + 4);
         const float w8[8] = {lo.v[0], lo.v[1], lo.v[2], lo.v[3], hi.v[0], hi.v[1], hi.v[2], hi.v[3]};
 #pragma unroll
         for (int e = 0; e < 4; e++) {
-            const int pk = k0 + 4 * lq + e;
+            const int lk = 4 * lq + e;
             const float t0 = step * w8[e + 1], t1 = step * w8[e + 2];
-            if (t0 != 0.f)
-                acc[e][FW] -= (p.dtz * p.mu[pk - 1]) * 0.5f * p.rhow[pk] * (base[pk] - base[pk - 1]) *
-                              p.one_d_rhou[pk - 1] * t0;
-            if (t1 != 0.f)
-                acc[e][FW] -= (p.dtz * p.mu[pk]) * 0.5f * p.rhow[pk] * (base[pk] - base[pk - 1]) *
-                              p.one_d_rhou[pk] * t1;
+            if (t0 != 0.f) acc[e][FW] -= bf[lk] * t0;
+            if (t1 != 0.f) acc[e][FW] -= bf[AJ_TK + lk] * t1;
         }
     }
 }
@@ -184,7 +181,7 @@ __device__ __forceinline__ void qj_family(const KParams<float> &p, const float *
         if (pi < p.nx && pj < p.ny && pk0 < nz) dvr = ldg4(coef + (size_t)LIN_DVT_SLOT * p.n, gix(p.ny, nz, pi, pj, pk0));
     }
     __syncthreads();
-    if (DIR == 0) qj_extra<EQ>(p, tb, step, j0, k0, li, lj, lq, acc);
+    if (DIR == 0) qj_extra<EQ>(p, tb, sm, step, j0, k0, li, lj, lq, acc);
     // faces of the box, one face quad per item
 #pragma unroll
     for (int q = 0; q < (B::rows * B::NCH + AJ_THREADS - 1) / AJ_THREADS; q++) {
@@ -336,6 +333,24 @@ __global__ void __launch_bounds__(AJ_THREADS, 3)
         sm[QJ_ZF + threadIdx.x] = z0;
         sm[QJ_ZF + QJ_ZR + threadIdx.x] = z1;
     }
+    // the basic-state term of theta (G 0) or qv (G 1) into w: for the cell
+    // at level pk, the factor of the tendency adjoint below and above it
+    // (adj_extra's products, in its order, without the tendency)
+    if (threadIdx.x >= 32 && threadIdx.x < 32 + 2 * AJ_TK) {
+        const int h = (threadIdx.x - 32) / AJ_TK, lk = (threadIdx.x - 32) % AJ_TK, pk = k0 + lk;
+        const float *base = G == 0 ? p.tb : p.qb;
+        float v = 0.f;
+        if (pk >= 1 && pk < nz && (G == 0 || p.moist)) {
+            const int kk = h == 0 ? pk - 1 : pk;
+            v = (p.dtz * p.mu[kk]) * 0.5f * p.rhow[pk] * (base[pk] - base[pk - 1]) * p.one_d_rhou[kk];
+        }
+        sm[QJ_BF + (G == 0 ? 0 : 2 * AJ_TK) + h * AJ_TK + lk] = v;
+    }
+    // fdt * f of rows j0-1 .. j0+TJ (Coriolis)
+    if (threadIdx.x >= 64 && threadIdx.x < 64 + AJ_TJ + 2) {
+        const int jj = j0 - 1 + (threadIdx.x - 64);
+        sm[QJ_FC + threadIdx.x - 64] = jj >= 0 && jj < ny ? p.dt * 0.25f * p.f[jj] : 0.f;
+    }
     float acc[4][7];
 #pragma unroll
     for (int e = 0; e < 4; e++)
@@ -409,6 +424,268 @@ __global__ void __launch_bounds__(AJ_THREADS, 3)
                 A.P[FW][c + e] = 0.f;
             }
         }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// k_lin_coef_quad: k_lin_coef for a cell quad per thread (FP32, NZ % 4 == 0,
+// basic state a function of height).  The basic state's column values come
+// from the basic-state table in shared memory; every face is lin_face_t's
+// expression on the same values, so the coefficients are k_lin_coef's.
+// ---------------------------------------------------------------------------
+constexpr int LQ_THREADS = 256;
+
+template <int EQ, int DIR>
+__device__ __forceinline__ void lq_family(const KParams<float> &p, const KFields<float> &R, const float *tab,
+                                          float *coef, int i, int j, int k0, int c)
+{
+    const int nz = p.nz, sx = p.ny * nz, sy = nz;
+    constexpr int FX = LinEq<EQ>::FX, BX = LinEq<EQ>::BX;
+    bool need[4], any = false;
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+        const int k = k0 + e;
+        if (DIR == 0) need[e] = adv_cell(p, i, j, k, 1) || adv_cell(p, i + 1, j, k, 1);
+        else if (DIR == 1) need[e] = adv_cell(p, i, j, k, 1) || adv_cell(p, i, j + 1, k, 1);
+        else need[e] = adv_cell(p, i, j, k, 1) || (k + 1 < nz && adv_cell(p, i, j, k + 1, 1));
+        any = any || need[e];
+    }
+    Q4 ga{{0.f, 0.f, 0.f, 0.f}}, gs{{0.f, 0.f, 0.f, 0.f}};
+    if (any) {
+        const float *X = R.cur[FX];
+        if (EQ == 5 && DIR == 2) {
+            // the rain's vertical face (lin_face_rain)
+            const Win q = ldwin(X, c, k0, nz), w = ldwin(R.cur[FW], c, k0, nz);
+            const int c0 = c - k0;
+            float vt[5];
+#pragma unroll
+            for (int e = 0; e < 5; e++) {
+                const int m = k0 + e;
+                float v = 0.f;
+                if (m < nz - 1) {
+                    const int mm = m == 0 ? 1 : m;
+                    v = fall_speed_point(p, q.at(mm - k0), mm);
+                } else if (m < nz) {
+                    v = R.vt[c0 + m];
+                }
+                vt[e] = v;
+            }
+#pragma unroll
+            for (int e = 0; e < 4; e++) {
+                const int k = k0 + e;
+                if (!need[e]) continue;
+                float Sv, wf;
+                if (k == 0) {
+                    const float v1 = vt[1 - k0];
+                    Sv = 0.5f * (q.at(0) + q.at(1));
+                    wf = -0.5f * (v1 + v1);
+                } else {
+                    const float wb = tab[2 * nz + k + 1] + w.at(e + 1);
+                    wf = wb - 0.5f * (vt[e] + vt[e + 1]);
+                    if (k == 1 || k == nz - 2) Sv = 0.5f * (q.at(e + 1) + q.at(e));
+                    else Sv = face3<float>(q.at(e - 1), q.at(e), q.at(e + 1), q.at(e + 2), sgn(wf));
+                }
+                ga.v[e] = Sv;
+                gs.v[e] = wf;
+            }
+        } else if (DIR < 2) {
+            const int st = DIR == 0 ? sx : sy;
+            Q4 x[6];
+#pragma unroll
+            for (int m = 0; m < 6; m++) x[m] = ldg4(X, c + (m - 2) * st);
+            const float *A = R.cur[DIR];
+            Q4 a0, a1;
+            if (EQ >= 2) a0 = ldg4(A, c + st);
+            else if (EQ == 0) {
+                a0 = ldg4(A, DIR == 0 ? c + sx : c + sy);
+                a1 = ldg4(A, DIR == 0 ? c : c - sx + sy);
+            } else {
+                a0 = ldg4(A, DIR == 0 ? c + sx : c + sy);
+                a1 = ldg4(A, DIR == 0 ? c + sx - sy : c);
+            }
+#pragma unroll
+            for (int e = 0; e < 4; e++) {
+                const int k = k0 + e;
+                if (!need[e]) continue;
+                const float abv = tab[DIR * nz + k];
+                float a, ab;
+                if (EQ >= 2) {
+                    a = a0.v[e];
+                    ab = abv;
+                } else {
+                    a = 0.5f * (a0.v[e] + a1.v[e]);
+                    ab = 0.5f * (abv + abv);
+                }
+                const float sgs = sgn(ab + a), sgb = sgn(a);
+                const float Sv = face5<float>(x[0].v[e], x[1].v[e], x[2].v[e], x[3].v[e], x[4].v[e], x[5].v[e], sgs);
+                float Bv = 0.f;
+                if (BX >= 0) {
+                    const float b = tab[BX * nz + k];
+                    Bv = face5<float>(b, b, b, b, b, b, sgb);
+                }
+                ga.v[e] = Bv + Sv;
+                gs.v[e] = ab + a;
+            }
+        } else {
+            const Win x = ldwin(X, c, k0, nz);
+            const float *A = R.cur[FW];
+            const Win w0 = ldwin(A, c, k0, nz);
+            Win w1 = w0;
+            if (EQ == 0) w1 = ldwin(A, c - sx, k0, nz);
+            else if (EQ == 1) w1 = ldwin(A, c - sy, k0, nz);
+#pragma unroll
+            for (int e = 0; e < 4; e++) {
+                const int k = k0 + e;
+                if (!need[e] || k == 0) continue;
+                const float abv = tab[2 * nz + k + 1];
+                float a, ab;
+                if (EQ >= 2) {
+                    a = w0.at(e + 1);
+                    ab = abv;
+                } else {
+                    a = 0.5f * (w0.at(e + 1) + w1.at(e + 1));
+                    ab = 0.5f * (abv + abv);
+                }
+                const float sgs = sgn(ab + a), sgb = sgn(a);
+                float Sv, Bv = 0.f;
+                if (k == 1 || k == nz - 2) {
+                    Sv = 0.5f * (x.at(e + 1) + x.at(e));
+                    if (BX >= 0) Bv = 0.5f * (tab[BX * nz + k + 1] + tab[BX * nz + k]);
+                } else {
+                    Sv = face3<float>(x.at(e - 1), x.at(e), x.at(e + 1), x.at(e + 2), sgs);
+                    if (BX >= 0)
+                        Bv = face3<float>(tab[BX * nz + k - 1], tab[BX * nz + k], tab[BX * nz + k + 1],
+                                          tab[BX * nz + k + 2], sgb);
+                }
+                ga.v[e] = Bv + Sv;
+                gs.v[e] = ab + a;
+            }
+        }
+    }
+    stg4(coef + (size_t)LinSlot<EQ, DIR>::GA * p.n + c, ga);
+    if (LinSlot<EQ, DIR>::OWNS_GS) stg4(coef + (size_t)LinSlot<EQ, DIR>::GS * p.n + c, gs);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(LQ_THREADS)
+    k_lin_coef_quad(KParams<T> p, KFields<T> R, T *coef, KFields<T> A, const unsigned char *qm)
+{
+    static_assert(sizeof(T) == 4, "four-level kernels are FP32");
+    __shared__ float tab[5 * PPM_MAXZ];  // column values of UBAR, VBAR, WBAR, THBAR, QBAR
+    const int nz = p.nz, NQ = nz >> 2;
+    for (int e = threadIdx.x; e < 5 * nz; e += LQ_THREADS) tab[e] = p.btab[e];
+    __syncthreads();
+    const long w = (long)blockIdx.x * LQ_THREADS + threadIdx.x;
+    if (w >= (long)p.nx * p.ny * NQ) return;
+    const int q = (int)(w % NQ), col = (int)(w / NQ);
+    const int j = col % p.ny, i = col / p.ny, k0 = 4 * q;
+    const int c = gix(p.ny, nz, i, j, k0);
+    lq_family<0, 0>(p, R, tab, coef, i, j, k0, c);
+    lq_family<0, 1>(p, R, tab, coef, i, j, k0, c);
+    lq_family<0, 2>(p, R, tab, coef, i, j, k0, c);
+    lq_family<1, 0>(p, R, tab, coef, i, j, k0, c);
+    lq_family<1, 1>(p, R, tab, coef, i, j, k0, c);
+    lq_family<1, 2>(p, R, tab, coef, i, j, k0, c);
+    lq_family<2, 0>(p, R, tab, coef, i, j, k0, c);
+    lq_family<2, 1>(p, R, tab, coef, i, j, k0, c);
+    lq_family<2, 2>(p, R, tab, coef, i, j, k0, c);
+    if (p.moist) {
+        lq_family<3, 0>(p, R, tab, coef, i, j, k0, c);
+        lq_family<3, 1>(p, R, tab, coef, i, j, k0, c);
+        lq_family<3, 2>(p, R, tab, coef, i, j, k0, c);
+        lq_family<4, 0>(p, R, tab, coef, i, j, k0, c);
+        lq_family<4, 1>(p, R, tab, coef, i, j, k0, c);
+        lq_family<4, 2>(p, R, tab, coef, i, j, k0, c);
+        lq_family<5, 0>(p, R, tab, coef, i, j, k0, c);
+        lq_family<5, 1>(p, R, tab, coef, i, j, k0, c);
+        lq_family<5, 2>(p, R, tab, coef, i, j, k0, c);
+        // d(fall speed)/d(rain) (lin_dvt) and the clipped points' P-bar
+        const bool inner = i >= 3 && i < p.nx - 3 && j >= 3 && j < p.ny - 3;
+        const Q4 qr = ldg4(R.cur[FQR], c);
+        Q4 dv{{0.f, 0.f, 0.f, 0.f}};
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+            const int m = k0 + e;
+            if (inner && m >= 1 && m <= nz - 2 && qr.v[e] > 1.0e-12f)
+                dv.v[e] = 0.1364f * fall_speed_point(p, qr.v[e], m) / qr.v[e];
+        }
+        stg4(coef + (size_t)LIN_DVT_SLOT * p.n + c, dv);
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+            const unsigned char b = qm[c + e];
+            if (b && adv_cell(p, i, j, k0 + e, 1)) {
+                if (b & 1) A.P[FQV][c + e] = 0.f;
+                if (b & 2) A.P[FQC][c + e] = 0.f;
+                if (b & 4) A.P[FQR][c + e] = 0.f;
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// k_adj_div_quad: k_adj_div for a cell quad per thread (FP32, NZ % 4 == 0).
+// Columns at least three points inside the lateral boundary involve no mirror
+// copy: their four adj_dint terms are plain reads of db, done as 16-byte
+// rows.  Other columns run adj_div_point level by level.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(256, 4) k_adj_div_quad(KParams<T> p, KFields<T> A, const T *db, T sdt)
+{
+    static_assert(sizeof(T) == 4, "four-level kernels are FP32");
+    const int nz = p.nz, ny = p.ny, nx = p.nx, NQ = nz >> 2;
+    const long w = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= (long)nx * ny * NQ) return;
+    const int q = (int)(w % NQ), col = (int)(w / NQ);
+    const int j = col % ny, i = col / ny, k0 = 4 * q;
+    const int c = gix(ny, nz, i, j, k0), sx = ny * nz, sy = nz;
+    if (i >= 3 && i <= nx - 3 && j >= 3 && j <= ny - 3) {
+        const Win d = ldwin(db, c, k0, nz);
+        const Q4 dx = ldg4(db, c - sx), dy = ldg4(db, c - sy);
+        Q4 u = ldg4(A.P[FU], c), v = ldg4(A.P[FV], c), wv = ldg4(A.P[FW], c);
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+            const int k = k0 + e;
+            const bool lv = k >= 1 && k <= nz - 2, lvm = k - 1 >= 1 && k - 1 <= nz - 2;
+            const float d0 = lv ? d.at(e) : 0.f, dxm = lv ? dx.v[e] : 0.f, dym = lv ? dy.v[e] : 0.f;
+            const float dzm = lvm ? d.at(e - 1) : 0.f;
+            if (dxm != 0.f || d0 != 0.f) u.v[e] += p.rhou[k] * p.one_d_dx * (dxm - d0) / sdt;
+            if (dym != 0.f || d0 != 0.f) v.v[e] += p.rhou[k] * p.one_d_dy * (dym - d0) / sdt;
+            if (dzm != 0.f || d0 != 0.f) {
+                float s = 0.f;
+                if (dzm != 0.f) s += p.mu[k - 1] * dzm;
+                if (d0 != 0.f) s -= p.mu[k] * d0;
+                wv.v[e] += p.rhow[k] * p.one_d_dz * s / sdt;
+            }
+        }
+        stg4(A.P[FU] + c, u);
+        stg4(A.P[FV] + c, v);
+        stg4(A.P[FW] + c, wv);
+        return;
+    }
+    for (int e = 0; e < 4; e++) {
+        const int k = k0 + e;
+        const bool lev = k >= 1 && k <= nz - 2;
+        if (lev && (i == 0 || i == nx - 1 || j == 0 || j == ny - 1)) continue;
+        float u, v, wz;
+        adj_div_point(p, A, db, sdt, i, j, k, u, v, wz);
+        if (lev) {
+            const int is[2] = {i, i == 1 ? 0 : i == nx - 2 ? nx - 1 : -1};
+            const int js[2] = {j, j == 1 ? 0 : j == ny - 2 ? ny - 1 : -1};
+#pragma unroll
+            for (int a = 0; a < 2; a++)
+#pragma unroll
+                for (int b = 0; b < 2; b++) {
+                    if ((a == 0 && b == 0) || is[a] < 0 || js[b] < 0) continue;
+                    float ru, rv, rw;
+                    adj_div_point(p, A, db, sdt, is[a], js[b], k, ru, rv, rw);
+                    u += ru;
+                    v += rv;
+                    wz += rw;
+                }
+        }
+        A.P[FU][c + e] = u;
+        A.P[FV][c + e] = v;
+        A.P[FW][c + e] = wz;
     }
 }
 

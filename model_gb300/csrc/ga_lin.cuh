@@ -36,6 +36,10 @@ struct Lin : LinBase {
     // the four-level adjoint advection (FP32, NZ % 4 == 0); GA_ADJ=level keeps
     // the per-level kernel
     bool adj_quad = false;
+    // the coefficient pass of a stage needs only the trajectory: it runs on a
+    // side stream beside the pressure adjoint
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_cols = nullptr, ev_coef = nullptr;
 
     explicit Lin(Engine<T> &eng) : e(eng), N(eng.N), nf(eng.nprog)
     {
@@ -50,6 +54,9 @@ struct Lin : LinBase {
             mask = e.template dalloc<unsigned char>(N);
             rain_keep = e.template dalloc<double>((size_t)e.NX * e.NY);
         }
+        cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking);
+        cudaEventCreateWithFlags(&ev_cols, cudaEventDisableTiming);
+        cudaEventCreateWithFlags(&ev_coef, cudaEventDisableTiming);
         const int optin = 200 * 1024;
         cudaFuncSetAttribute(k_adj_fft_y_in<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
         cudaFuncSetAttribute(k_adj_ifft_y_out<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
@@ -70,6 +77,12 @@ struct Lin : LinBase {
         if (tape) cudaFree(tape);
         if (mtape) cudaFree(mtape);
         if (ckpt) cudaFree(ckpt);
+        if (side) {
+            cudaStreamSynchronize(side);
+            cudaStreamDestroy(side);
+        }
+        if (ev_cols) cudaEventDestroy(ev_cols);
+        if (ev_coef) cudaEventDestroy(ev_coef);
     }
 
     // trajectory fields per step: stage-start prognostic fields, and (moist)
@@ -93,7 +106,7 @@ struct Lin : LinBase {
     void record_pair(int m2)
     {
         const int par = e.ci[0] == 0 ? 0 : 1;
-        const size_t idx = (size_t)m2 / 2;
+        const size_t idx = (size_t)m2;
         auto &gs = rec_graph[par];
         auto &ls = rec_graph_launches[par];
         if (gs.size() <= idx) {
@@ -131,13 +144,16 @@ struct Lin : LinBase {
         }
     }
 
-    // steps n0..n1-1 of a segment starting at n0, recording every step
-    void record_segment(int n0, int n1)
+    // steps n0..n1-1 of a segment, recording step n into trajectory slot
+    // base + n - n0
+    void record_segment(int n0, int n1, int base)
     {
         int n = n0;
-        for (; n + 1 < n1; n += 2) record_pair(n - n0);
-        if (n < n1) e.rk3_step(rec_at(n - n0), mrec_at(n - n0));
+        for (; n + 1 < n1; n += 2) record_pair(base + n - n0);
+        if (n < n1) e.rk3_step(rec_at(base + n - n0), mrec_at(base + n - n0));
     }
+    // bytes of the trajectory of one step (fields and clipping records)
+    size_t step_bytes() const { return per_step() * sizeof(T) + (nf == 7 ? 3 * (size_t)N : 0); }
 
     KFields<T> fields() const
     {
@@ -264,7 +280,14 @@ struct Lin : LinBase {
             e.launches += 3;
         }
         k_adj_ifft_y_out<T><<<dim3(nkt_y, e.kp.ni), by_y, e.smem_y, s>>>(e.kp, e.spec, dbar, e.plan_j, e.tw_j, e.KTy);
-        k_adj_div<T><<<cdiv(N, 256), 256, 0, s>>>(e.kp, A, dbar, (T)(st * e.cfg.dt));
+        bool div_quad = false;
+        if constexpr (sizeof(T) == 4) div_quad = adj_quad;
+        if (div_quad) {
+            if constexpr (sizeof(T) == 4)
+                k_adj_div_quad<T><<<cdiv(N / 4, 256), 256, 0, s>>>(e.kp, A, dbar, (T)(st * e.cfg.dt));
+        } else {
+            k_adj_div<T><<<cdiv(N, 256), 256, 0, s>>>(e.kp, A, dbar, (T)(st * e.cfg.dt));
+        }
         e.launches += 3;
     }
 
@@ -304,14 +327,33 @@ struct Lin : LinBase {
                 }
             }
             k_adj_cols<T><<<ncol, 128, 0, s>>>(e.kp, fields(), fl);
+            // the coefficient pass (trajectory in, coefficients and the clipped
+            // points' moisture P-bar out) runs on the side stream beside the
+            // pressure adjoint: after the column transposes, which write that
+            // P-bar, and after the previous stage's advection adjoint, which
+            // read the coefficients
+            {
+                KFields<T> R = e.fields();
+                for (int f = 0; f < nf; f++) R.cur[f] = const_cast<T *>(rec) + (size_t)(nf * st + f) * N;
+                const unsigned char *qm = moist ? mrec + (size_t)st * N : nullptr;
+                cudaEventRecord(ev_cols, s);
+                cudaStreamWaitEvent(side, ev_cols, 0);
+                bool coef_quad = false;
+                if constexpr (sizeof(T) == 4) coef_quad = adj_quad && e.kp.ubase_adv;
+                if (coef_quad) {
+                    if constexpr (sizeof(T) == 4)
+                        k_lin_coef_quad<T><<<cdiv(N / 4, LQ_THREADS), LQ_THREADS, 0, side>>>(e.kp, R, coef, fields(),
+                                                                                            qm);
+                } else {
+                    k_lin_coef<T><<<cdiv(N, 128), 128, 0, side>>>(e.kp, R, coef, fields(), qm);
+                }
+                cudaEventRecord(ev_coef, side);
+            }
             k_adj_project<T><<<cdiv(N, 256), 256, 0, s>>>(e.kp, fields(), (T)step, acc);
             e.launches += 2;
             adj_pressure(step);
-            KFields<T> R = e.fields();
-            for (int f = 0; f < nf; f++) R.cur[f] = const_cast<T *>(rec) + (size_t)(nf * st + f) * N;
-            const unsigned char *qm = moist ? mrec + (size_t)st * N : nullptr;
+            cudaStreamWaitEvent(s, ev_coef, 0);
             const T sdtg = (T)(step * e.cfg.dt * 9.8 * 0.5);
-            k_lin_coef<T><<<cdiv(N, 128), 128, 0, s>>>(e.kp, R, coef, fields(), qm);
             const int zc = (first && st == 2) ? 0 : 1;
             e.launches += 2 + (moist ? 1 : 0);
             if constexpr (sizeof(T) == 4) {
@@ -365,21 +407,59 @@ struct Lin : LinBase {
         }
     }
 
+    // Segments whose trajectory the first sweep keeps on the tape: the last
+    // ones, as many as device memory holds beside the checkpoints with a
+    // tenth of the GPU's memory to spare (at least one, at most all).
+    // GA_ADJ_RESIDENT=n fixes the count.
+    int resident_segments(int nseg, int K)
+    {
+        int R = 1;
+        size_t fr = 0, tot = 0;
+        if (cudaMemGetInfo(&fr, &tot) == cudaSuccess) {
+            const size_t sb = step_bytes(), cb = 3 * (size_t)nf * N * sizeof(T);
+            const size_t have = fr + tape_steps * sb + ckpt_slots * cb;  // the current tape and checkpoints are given back
+            const size_t need = (size_t)(nseg + 1) * cb + tot / 10;
+            if (have > need) R = (int)std::min<size_t>((size_t)nseg, (have - need) / ((size_t)K * sb));
+        } else {
+            cudaGetLastError();
+        }
+        if (const char *ev = std::getenv("GA_ADJ_RESIDENT")) R = std::atoi(ev);
+        return std::max(1, std::min(R, nseg));
+    }
+
     // nsteps forward from the current state, then the adjoint back to it.
-    // States are checkpointed every K steps and each segment is recomputed
-    // (recording its stage-start fields) before its adjoint runs; the last
-    // segment is recorded during the first sweep.
+    // States are checkpointed every K steps.  The first sweep records the
+    // stage-start fields of the last `resident` segments; every earlier
+    // segment is recomputed from its checkpoint (recording) before its
+    // adjoint runs.
+    int resident = 1;
     int adjoint(int nsteps, int K)
     {
         if (nsteps <= 0) return GA_OK;
         if (K <= 0 || K > nsteps) K = nsteps;
         const int nseg = (nsteps + K - 1) / K;
-        int rc = reserve((size_t)K, (size_t)nseg + 1);
+        int R = resident_segments(nseg, K);
+        if (R > 1 && (size_t)R * K > tape_steps) {  // give the old tape back before the larger one
+            drop_graphs();
+            if (tape) cudaFree(tape);
+            if (mtape) cudaFree(mtape);
+            tape = nullptr;
+            mtape = nullptr;
+            tape_steps = 0;
+        }
+        int rc = reserve((size_t)R * K, (size_t)nseg + 1);
+        if (rc == GA_ERR_NOMEM && R > 1) {
+            cudaGetLastError();
+            R = 1;
+            rc = reserve((size_t)K, (size_t)nseg + 1);
+        }
         if (rc) return rc;
+        resident = R;
+        const int first_res = nseg - R;  // first resident segment
         for (int seg = 0; seg < nseg; seg++) {
             const int n0 = seg * K, n1 = std::min(nsteps, n0 + K);
             checkpoint(seg, true);
-            if (seg == nseg - 1) record_segment(n0, n1);
+            if (seg >= first_res) record_segment(n0, n1, (seg - first_res) * K);
             else if (int rc2 = e.step(n1 - n0)) return rc2;
         }
         checkpoint(nseg, true);
@@ -390,11 +470,15 @@ struct Lin : LinBase {
             cudaMemcpyAsync(rain_keep, e.accrain, nrain * sizeof(double), cudaMemcpyDeviceToDevice, e.stream);
         for (int seg = nseg - 1; seg >= 0; seg--) {
             const int n0 = seg * K, n1 = std::min(nsteps, n0 + K);
-            if (seg != nseg - 1) {
+            int base = 0;
+            if (seg >= first_res) {
+                base = (seg - first_res) * K;
+            } else {  // the resident segments' slots are consumed by now
                 checkpoint(seg, false);
-                record_segment(n0, n1);
+                record_segment(n0, n1, 0);
             }
-            for (int n = n1 - 1; n >= n0; n--) adj_step(rec_at(n - n0), mrec_at(n - n0), n == nsteps - 1);
+            for (int n = n1 - 1; n >= n0; n--)
+                adj_step(rec_at(base + n - n0), mrec_at(base + n - n0), n == nsteps - 1);
         }
         const long tot = (long)(e.NX - 6) * (e.NY - 6) * (e.NZ - 2);
         k_adj_zero_cells<T><<<cdiv(tot, 256), 256, 0, e.stream>>>(e.kp, fields());

@@ -250,17 +250,25 @@ def test_gpu_dot_product(built, prec, tol):
 
 
 @pytest.mark.gpu
-def test_gpu_checkpointing_is_exact(built):
+def test_gpu_checkpointing_is_exact(built, monkeypatch):
+    """any checkpoint interval, with every segment recomputed but the last
+    (GA_ADJ_RESIDENT=1) or as many kept on the tape as memory allows (all of
+    them on this grid), gives the same adjoint bit for bit"""
     wl = small_vortex()
     st = trajectory_state(wl)
     y = random_dirs(wl, 31)
     outs = []
-    for K in (1, 2, 5, 0):
+    for K, res in ((1, "1"), (2, "1"), (5, "1"), (0, "1"), (2, None), (2, "2")):
+        if res is None:
+            monkeypatch.delenv("GA_ADJ_RESIDENT", raising=False)
+        else:
+            monkeypatch.setenv("GA_ADJ_RESIDENT", res)
         m = _model(wl, st)
         m.lin_set_all(y)
         m.adjoint(5, K)
         outs.append(m.lin_get_all())
         assert m.counters()[0] == 5
+    monkeypatch.delenv("GA_ADJ_RESIDENT", raising=False)
     for o in outs[1:]:
         for k in LIN:
             assert np.array_equal(o[k], outs[0][k]), k
@@ -411,33 +419,39 @@ def test_gpu_moist_tlm_matches_finite_differences(built):
 
 
 @pytest.mark.gpu
-def test_gpu_moist_checkpointing_is_exact(built):
+def test_gpu_moist_checkpointing_is_exact(built, monkeypatch):
     wl = configs.moist_blob(nx=24, ny=22, nz=16)
     st = moist_state(wl, False)
     y = moist_dirs(wl, 31)
     outs = []
-    for K in (1, 2, 0):
+    for K, res in ((1, "1"), (2, "1"), (0, "1"), (1, None), (1, "3")):
+        if res is None:
+            monkeypatch.delenv("GA_ADJ_RESIDENT", raising=False)
+        else:
+            monkeypatch.setenv("GA_ADJ_RESIDENT", res)
         m = _model(wl, st)
         m.lin_set_all(y)
         m.adjoint(4, K)
         outs.append(m.lin_get_all())
         assert m.counters()[0] == 4
+    monkeypatch.delenv("GA_ADJ_RESIDENT", raising=False)
     for o in outs[1:]:
         for k in MOIST:
             assert np.array_equal(o[k], outs[0][k]), k
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("moist", [False, True])
-def test_gpu_adjoint_quad_kernel_matches_level_kernel(built, monkeypatch, moist):
-    """FP32: the four-level adjoint advection (the default when NZ % 4 == 0)
-    against the per-level kernel (GA_ADJ=level), bit for bit.  Both grids are
+@pytest.mark.parametrize("case", ["dry_varying_base", "dry_uniform_base", "moist"])
+def test_gpu_adjoint_quad_kernel_matches_level_kernel(built, monkeypatch, case):
+    """FP32: the four-level adjoint advection and, for a basic state of height
+    only, the four-level coefficient pass (the defaults when NZ % 4 == 0)
+    against the per-level kernels (GA_ADJ=level), bit for bit.  The grids are
     ragged against the 16 x 8 x 8 tiles; NZ = 12 leaves a half level tile."""
-    if moist:
+    if case == "moist":
         wl = configs.moist_blob(nx=24, ny=22, nz=16)
         st, y = moist_state(wl, False), moist_dirs(wl, 31)
     else:
-        wl = small_vortex(nx=24, ny=20, nz=12)
+        wl = small_vortex(nx=24, ny=20, nz=12, extra_basic=1.0 if case == "dry_varying_base" else 0.0)
         st, y = trajectory_state(wl), random_dirs(wl, 22)
     outs = []
     for mode in ("level", "quad"):
