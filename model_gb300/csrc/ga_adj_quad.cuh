@@ -689,4 +689,116 @@ __global__ void __launch_bounds__(256, 4) k_adj_div_quad(KParams<T> p, KFields<T
     }
 }
 
+// ---------------------------------------------------------------------------
+// k_adj_project_quad: k_adj_project for a cell quad per thread (FP32,
+// NZ % 4 == 0): pi-bar from the projection's transposed gradient.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(256) k_adj_project_quad(KParams<T> p, KFields<T> A, T step, int acc)
+{
+    static_assert(sizeof(T) == 4, "four-level kernels are FP32");
+    const int nz = p.nz, ny = p.ny, nx = p.nx, NQ = nz >> 2;
+    const long w = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= (long)nx * ny * NQ) return;
+    const int q = (int)(w % NQ), col = (int)(w / NQ);
+    const int j = col % ny, i = col / ny, k0 = 4 * q;
+    const int c = gix(ny, nz, i, j, k0), sx = ny * nz, sy = nz;
+    const bool cin = i >= 1 && i <= nx - 2 && j >= 1 && j <= ny - 2;        // column (i, j) inner
+    const bool cxp = i + 1 >= 1 && i + 1 <= nx - 2 && j >= 1 && j <= ny - 2;  // column (i+1, j)
+    const bool cyp = i >= 1 && i <= nx - 2 && j + 1 >= 1 && j + 1 <= ny - 2;  // column (i, j+1)
+    const Q4 z{{0.f, 0.f, 0.f, 0.f}};
+    Q4 v = acc ? ldg4(A.pi, c) : z;
+    const Q4 pu = cin ? ldg4(A.P[FU], c) : z, pv = cin ? ldg4(A.P[FV], c) : z;
+    const Win pw = cin ? ldwin(A.P[FW], c, k0, nz) : Win{};
+    const Q4 pux = cxp ? ldg4(A.P[FU], c + sx) : z, pvy = cyp ? ldg4(A.P[FV], c + sy) : z;
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+        const int k = k0 + e;
+        const bool lv = k >= 1 && k <= nz - 2, lvp = k + 1 >= 1 && k + 1 <= nz - 2;
+        float x = v.v[e];
+        if (cin && lv) {
+            x -= step * p.dtx * pu.v[e];
+            x -= step * p.dty * pv.v[e];
+            if (k >= 2) x -= step * (p.dtz * p.mw[k]) * pw.at(e);
+        }
+        if (cxp && lv) x += step * p.dtx * pux.v[e];
+        if (cyp && lv) x += step * p.dty * pvy.v[e];
+        if (cin && lvp && k + 1 >= 2) x += step * (p.dtz * p.mw[k + 1]) * pw.at(e + 1);
+        v.v[e] = x;
+    }
+    stg4(A.pi + c, v);
+}
+
+// ---------------------------------------------------------------------------
+// k_adj_cols_quad: k_adj_cols (one (field, column) per thread, FP32,
+// NZ % 4 == 0) on 16-byte level quads: a sponge-strip column goes through
+// every quad, any other through quad 0 and the quads from its first damped
+// or top-copy level up.  The transposed top and bottom copies couple levels
+// 0 and 1, and NZ-2 and NZ-1, each pair inside one quad; on the levels of a
+// visited quad that k_adj_cols would not visit the chain leaves the value
+// as it is.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(128) k_adj_cols_quad(KParams<T> p, KFields<T> A, int flags)
+{
+    static_assert(sizeof(T) == 4, "four-level kernels are FP32");
+    const int nf = p.moist ? 7 : 4, nz = p.nz, NQ = nz >> 2;
+    const long ncols = (long)p.nx * p.ny;
+    const long tid = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid >= ncols * nf) return;
+    const long col = tid % ncols;
+    const int f = (int)(tid / ncols);
+    const int i = (int)(col / p.ny), j = (int)(col % p.ny);
+    const bool hE = j >= 1 && i >= p.eb && i < p.ee, hW = j >= 1 && i >= p.wb && i < p.we;
+    const bool hS = i >= 1 && j >= p.sb && j < p.se, hN = i >= 1 && j >= p.nb && j < p.ne;
+    const int reps = (flags & AP_SPONGE2) ? 2 : (flags & AP_SPONGE) ? 1 : 0;
+    const bool strip = reps > 0 && (hE || hW || hS || hN);
+    const bool vbc = (flags & AP_VBC) && i >= 1 && j >= 1;
+    const bool rcol = (flags & AP_RAYLEIGH) && i >= 1 && i < p.nx - 1 && j >= 1 && j < p.ny - 1;
+    const bool ray = rcol && f <= FTH;
+    if (!strip && !vbc && !ray) return;  // nothing changes in this column
+    const int kup = strip ? 2 : min(nz - 2, ray ? max(p.raylevel, 2) : nz - 2);
+    float *P = A.P[f] + col * nz;
+    auto quad = [&](int k0) {
+        const Q4 in = ldg4(P, k0);
+        float pre[4];
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+            const int k = k0 + e;
+            float v = in.v[e];
+            if (ray && k >= p.raylevel) {
+                const float cr = (f == FW) ? p.ray_w[k] : p.ray_u[k];
+                v = v - cr * v;
+            }
+            pre[e] = v;
+        }
+        Q4 out;
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+            const int k = k0 + e;
+            float v = pre[e];
+            if (vbc) {
+                if (f == FW) {
+                    if (k == 0 || k == 1 || k == nz - 1) v = 0.f;
+                } else {
+                    if (k == 0 || k == nz - 1) v = 0.f;
+                    else if (k == 1) v = v + pre[0];       // + pre(0): level 0 is in this quad
+                    else if (k == nz - 2) v = v + pre[3];  // + pre(NZ-1): level NZ-1 is in this quad
+                }
+            }
+            if (strip && k >= 1)
+                for (int rp = 0; rp < reps; rp++) {
+                    if (hN) v = v - p.cn[j - p.nb] * v;
+                    if (hS) v = v - p.cs[j - p.sb] * v;
+                    if (hW) v = v - p.cw[i - p.wb] * v;
+                    if (hE) v = v - p.ce[i - p.eb] * v;
+                }
+            out.v[e] = v;
+        }
+        stg4(P + k0, out);
+    };
+    quad(0);
+    for (int q = strip ? 1 : max(1, kup >> 2); q < NQ; q++) quad(4 * q);
+}
+
 }  // namespace ga

@@ -304,12 +304,22 @@ struct Lin : LinBase {
         const size_t smem_adv = AjCfg<T>::smem;
         swap_inner();  // advance_outer's swap
         const int ncol = cdiv((long)e.NX * e.NY * nf, 128);  // threads of k_adj_cols: (field, column)
+        // the column transposes: one (field, column, level quad) per thread in FP32
+        auto cols = [&](int fl) {
+            if constexpr (sizeof(T) == 4) {
+                if (adj_quad) {
+                    k_adj_cols_quad<T><<<ncol, 128, 0, s>>>(e.kp, fields(), fl);
+                    return;
+                }
+            }
+            k_adj_cols<T><<<ncol, 128, 0, s>>>(e.kp, fields(), fl);
+        };
         k_adj_fold_m<T><<<cdiv(N, 256), 256, 0, s>>>(e.kp, fields());  // advance_outer's M <- P
         e.launches++;
         if (moist) {
             // the step-final post, then Kessler (its inputs: rec + 3*nf*N);
             // pi-bar takes Kessler's pi row (first: on top of the final pi-bar)
-            k_adj_cols<T><<<ncol, 128, 0, s>>>(e.kp, fields(), AP_RAYLEIGH | AP_VBC | AP_SPONGE);
+            cols(AP_RAYLEIGH | AP_VBC | AP_SPONGE);
             k_adj_kessler<T><<<cdiv(N, 128), 128, 0, s>>>(e.kp, e.fields(), rec + (size_t)3 * nf * N, fields(),
                                                          first ? 1 : 0);
             e.launches += 2;
@@ -326,7 +336,7 @@ struct Lin : LinBase {
                     acc = first ? 1 : 0;
                 }
             }
-            k_adj_cols<T><<<ncol, 128, 0, s>>>(e.kp, fields(), fl);
+            cols(fl);
             // the coefficient pass (trajectory in, coefficients and the clipped
             // points' moisture P-bar out) runs on the side stream beside the
             // pressure adjoint: after the column transposes, which write that
@@ -349,7 +359,14 @@ struct Lin : LinBase {
                 }
                 cudaEventRecord(ev_coef, side);
             }
-            k_adj_project<T><<<cdiv(N, 256), 256, 0, s>>>(e.kp, fields(), (T)step, acc);
+            bool proj_quad = false;
+            if constexpr (sizeof(T) == 4) proj_quad = adj_quad;
+            if (proj_quad) {
+                if constexpr (sizeof(T) == 4)
+                    k_adj_project_quad<T><<<cdiv(N / 4, 256), 256, 0, s>>>(e.kp, fields(), (T)step, acc);
+            } else {
+                k_adj_project<T><<<cdiv(N, 256), 256, 0, s>>>(e.kp, fields(), (T)step, acc);
+            }
             e.launches += 2;
             adj_pressure(step);
             cudaStreamWaitEvent(s, ev_coef, 0);
