@@ -56,6 +56,34 @@ __global__ void __launch_bounds__(256) kb_advect(const KParams<T> *P, const KFie
     }
 }
 
+// FP32 members with whole level quads: the four-level advection and post
+template <typename T, int TI, int TJ>
+__global__ void __launch_bounds__(AQ_THREADS, 3) kb_advect_quad(const KParams<T> *P, const KFields<T> *F,
+                                                               const long *pre, int nmem, double step, int what)
+{
+    static_assert(sizeof(T) == 4, "four-level kernels are FP32");
+    const long total = pre[nmem];
+    for (long vb = blockIdx.x; vb < total; vb += gridDim.x) {
+        const int m = find_member(pre, nmem, vb);
+        const KParams<T> &p = P[m];
+        const long lb = vb - pre[m];
+        const int gx = (p.nx - 6 + TI - 1) / TI;
+        const double sdtg = step * p.dt_d * 9.8 * 0.5;  // step*dt*grav*0.5, advection.cpp:330
+        advect_quad_body<TI, TJ>(p, F[m], (int)(lb % gx), (int)(lb / gx), (T)step, (T)sdtg, what);
+        __syncthreads();
+    }
+}
+template <typename T>
+__global__ void __launch_bounds__(PQ_THREADS) kb_post_quad(const KParams<T> *P, const KFields<T> *F, const long *pre,
+                                                           int nmem, int4 fl0, int4 fl1, double step)
+{
+    const long total = pre[nmem];
+    for (long vb = blockIdx.x; vb < total; vb += gridDim.x) {
+        const int m = find_member(pre, nmem, vb);
+        post_quad_body(P[m], F[m], fl0, fl1, (T)step, COLS_ALL, (vb - pre[m]) * PQ_THREADS + threadIdx.x);
+    }
+}
+
 template <typename T>
 __global__ void kb_mirror(const KParams<T> *P, const KFields<T> *F, const long *pre, int nmem)
 {
@@ -158,7 +186,22 @@ class Ensemble : public EnsembleBase {
     bool moist = false;
     int dev = 0;
     int adv_ti = ADV_TI, adv_tj = ADV_TJ;  // advection tile of every member (autotuned)
+    // FP32 members with whole level quads run the four-level post, and the
+    // four-level advection (tile adv_qi x adv_qj) while every basic state is
+    // a function of height and adv_quad is set (autotuned)
+    bool quad = false, adv_quad = true;
+    int adv_qi = 4, adv_qj = 8;
+    int sx_threads = 256;  // threads of a fused spectral-x block (autotuned)
     int nsm = 0;
+    bool adv_quad_now = false;  // the choice build_prefixes made (prefixes and launches agree)
+    bool quad_applies() const
+    {
+        if (!quad || !adv_quad) return false;
+        for (auto *e : mem)
+            if (!e->quad_ok(adv_qi, adv_qj)) return false;
+        return true;
+    }
+    bool use_adv_quad() const { return adv_quad_now; }
 
     Ensemble(const ga_config *cfgs, const ga_columns *cols, int n, int *rc)
     {
@@ -198,6 +241,15 @@ class Ensemble : public EnsembleBase {
         cudaFuncSetAttribute(kb_div_fft_y<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
         cudaFuncSetAttribute(kb_spectral_x<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
         cudaFuncSetAttribute(kb_ifft_y_pi<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+        if constexpr (sizeof(T) == 4) {
+            quad = true;
+            for (auto *e : mem) quad = quad && e->NZ % 4 == 0;
+            cudaFuncSetAttribute(kb_advect_quad<T, 4, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+            cudaFuncSetAttribute(kb_advect_quad<T, 4, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+            cudaFuncSetAttribute(kb_advect_quad<T, 8, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+            cudaFuncSetAttribute(kb_advect_quad<T, 2, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+            cudaFuncSetAttribute(kb_advect_quad<T, 8, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+        }
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
         build_prefixes();
         if (cudaDeviceSynchronize() != cudaSuccess) *rc = GA_ERR_CUDA;
@@ -221,6 +273,15 @@ class Ensemble : public EnsembleBase {
 
     const void *advect_fn() const
     {
+        if constexpr (sizeof(T) == 4) {
+            if (use_adv_quad()) {
+                if (adv_qi == 4 && adv_qj == 4) return (const void *)kb_advect_quad<T, 4, 4>;
+                if (adv_qi == 8 && adv_qj == 4) return (const void *)kb_advect_quad<T, 8, 4>;
+                if (adv_qi == 2) return (const void *)kb_advect_quad<T, 2, 8>;
+                if (adv_qi == 8) return (const void *)kb_advect_quad<T, 8, 8>;
+                return (const void *)kb_advect_quad<T, 4, 8>;
+            }
+        }
         if (adv_ti == 2) return (const void *)kb_advect<T, 2, 4>;
         if (adv_tj == 2) return (const void *)kb_advect<T, 4, 2>;
         if (adv_tj == 8) return (const void *)kb_advect<T, 4, 8>;
@@ -232,11 +293,37 @@ class Ensemble : public EnsembleBase {
         const dim3 g(grid[EK_ADV]);
         const size_t sm = smem[EK_ADV];
         const long *pr = d_pre[EK_ADV];
+        if constexpr (sizeof(T) == 4) {
+            if (use_adv_quad()) {
+                if (adv_qi == 4 && adv_qj == 4) kb_advect_quad<T, 4, 4><<<g, AQ_THREADS, sm, stream>>>(d_p, F, pr, nmem, st, what);
+                else if (adv_qi == 8 && adv_qj == 4) kb_advect_quad<T, 8, 4><<<g, AQ_THREADS, sm, stream>>>(d_p, F, pr, nmem, st, what);
+                else if (adv_qi == 2) kb_advect_quad<T, 2, 8><<<g, AQ_THREADS, sm, stream>>>(d_p, F, pr, nmem, st, what);
+                else if (adv_qi == 8) kb_advect_quad<T, 8, 8><<<g, AQ_THREADS, sm, stream>>>(d_p, F, pr, nmem, st, what);
+                else kb_advect_quad<T, 4, 8><<<g, AQ_THREADS, sm, stream>>>(d_p, F, pr, nmem, st, what);
+                return;
+            }
+        }
         if (adv_ti == 2) kb_advect<T, 2, 4><<<g, 256, sm, stream>>>(d_p, F, pr, nmem, st, what);
         else if (adv_tj == 2) kb_advect<T, 4, 2><<<g, 256, sm, stream>>>(d_p, F, pr, nmem, st, what);
         else if (adv_tj == 8) kb_advect<T, 4, 8><<<g, 256, sm, stream>>>(d_p, F, pr, nmem, st, what);
         else if (adv_ti == 8) kb_advect<T, 8, 4><<<g, 256, sm, stream>>>(d_p, F, pr, nmem, st, what);
         else kb_advect<T, 4, 4><<<g, 256, sm, stream>>>(d_p, F, pr, nmem, st, what);
+    }
+
+    void launch_post(const KFields<T> *F, int4 a, int4 b, double st)
+    {
+        if constexpr (sizeof(T) == 4) {
+            if (quad) {
+                kb_post_quad<T><<<grid[EK_POST], PQ_THREADS, 0, stream>>>(d_p, F, d_pre[EK_POST], nmem, a, b, st);
+                return;
+            }
+        }
+        kb_post<T><<<grid[EK_POST], POST_THREADS, 0, stream>>>(d_p, F, d_pre[EK_POST], nmem, a, b, st);
+    }
+    void launch_sx()
+    {
+        kb_spectral_x<T><<<grid[EK_SX], dim3(64, sx_threads / 64), smem[EK_SX], stream>>>(d_p, d_aux, d_pre[EK_SX],
+                                                                                          nmem);
     }
 
     // virtual-block prefixes per kernel phase (for the current advection tile
@@ -245,6 +332,7 @@ class Ensemble : public EnsembleBase {
     void build_prefixes()
     {
         const int n = nmem;
+        adv_quad_now = quad_applies();
         for (int k = 0; k < EK_COUNT; k++) {
             std::vector<long> pre(n + 1, 0);
             size_t sm = 0;
@@ -253,8 +341,13 @@ class Ensemble : public EnsembleBase {
                 long c = 0;
                 switch (k) {
                 case EK_ADV:
-                    c = (long)cdiv(e.NX - 6, adv_ti) * cdiv(e.NY - 6, adv_tj);
-                    sm = std::max(sm, advect_tile_smem(adv_ti, adv_tj, e.NZ, sizeof(T)));
+                    if (use_adv_quad()) {
+                        c = (long)cdiv(e.NX - 6, adv_qi) * cdiv(e.NY - 6, adv_qj);
+                        sm = std::max(sm, advect_quad_smem(adv_qi, adv_qj, e.NZ));
+                    } else {
+                        c = (long)cdiv(e.NX - 6, adv_ti) * cdiv(e.NY - 6, adv_tj);
+                        sm = std::max(sm, advect_tile_smem(adv_ti, adv_tj, e.NZ, sizeof(T)));
+                    }
                     break;
                 case EK_MIRROR: c = cdiv(2L * (e.NX + e.NY - 2) * (e.NZ - 2), 256); break;
                 case EK_DIVY:
@@ -266,7 +359,9 @@ class Ensemble : public EnsembleBase {
                     c = e.kp.nj;
                     sm = std::max(sm, e.smem_sx);
                     break;
-                case EK_POST: c = cdiv((long)e.NX * e.NY, POST_COLS); break;
+                case EK_POST:
+                    c = quad ? cdiv((long)e.NX * e.NY * (e.NZ / 4), PQ_THREADS) : cdiv((long)e.NX * e.NY, POST_COLS);
+                    break;
                 case EK_KES: c = cdiv((long)(e.NX - 2) * (e.NY - 2) * (e.NZ - 2), 128); break;
                 }
                 pre[m + 1] = pre[m] + c;
@@ -287,6 +382,9 @@ class Ensemble : public EnsembleBase {
         grid[EK_SX] = occ((const void *)kb_spectral_x<T>, 256, smem[EK_SX]);
         grid[EK_IFFTY] = occ((const void *)kb_ifft_y_pi<T>, 256, smem[EK_IFFTY]);
         grid[EK_POST] = occ((const void *)kb_post<T>, POST_THREADS, 0);
+        if constexpr (sizeof(T) == 4) {
+            if (quad) grid[EK_POST] = occ((const void *)kb_post_quad<T>, PQ_THREADS, 0);
+        }
         grid[EK_KES] = occ((const void *)kb_kessler<T>, 128, 0);
         for (int k = 0; k < EK_COUNT; k++) grid[k] = (int)std::min<long>(grid[k], std::max(1L, total[k]));
     }
@@ -339,7 +437,9 @@ class Ensemble : public EnsembleBase {
         char line[160];
         {
             float best = 1e30f;
-            int bi = adv_ti, bj = adv_tj;
+            int bi = adv_ti, bj = adv_tj, qi = adv_qi, qj = adv_qj;
+            bool bq = false;
+            adv_quad = false;
             for (auto &tl : Engine<T>::kAdvTiles) {
                 bool fits = true;
                 for (auto *e : mem) fits = fits && advect_tile_smem(tl[0], tl[1], e->NZ, sizeof(T)) <= 200 * 1024;
@@ -350,9 +450,25 @@ class Ensemble : public EnsembleBase {
                 const float t = timeit([&] { launch_advect(F, 1. / 3., what); });
                 if (t < best) { best = t; bi = tl[0]; bj = tl[1]; }
             }
+            if (quad) {
+                adv_quad = true;
+                for (auto &tl : Engine<T>::kQuadTiles) {
+                    adv_qi = tl[0];
+                    adv_qj = tl[1];
+                    if (!quad_applies()) continue;
+                    build_prefixes();
+                    const float t = timeit([&] { launch_advect(F, 1. / 3., what); });
+                    if (t < best) { best = t; bq = true; qi = tl[0]; qj = tl[1]; }
+                }
+            }
             adv_ti = bi;
             adv_tj = bj;
-            std::snprintf(line, sizeof line, "advect tile %dx%d (%.3f ms); ", bi, bj, best);
+            adv_quad = bq;
+            adv_qi = qi;
+            adv_qj = qj;
+            build_prefixes();
+            if (bq) std::snprintf(line, sizeof line, "advect tile %dx%d, four levels per thread (%.3f ms); ", qi, qj, best);
+            else std::snprintf(line, sizeof line, "advect tile %dx%d (%.3f ms); ", bi, bj, best);
             info += line;
         }
         {
@@ -372,7 +488,7 @@ class Ensemble : public EnsembleBase {
                 kb_mirror<T><<<grid[EK_MIRROR], 256, 0, stream>>>(d_p, G, d_pre[EK_MIRROR], nmem);
                 kb_div_fft_y<T><<<grid[EK_DIVY], dim3(16, 16), smem[EK_DIVY], stream>>>(d_p, G, d_aux,
                                                                                        d_pre[EK_DIVY], nmem, 1. / 3.);
-                kb_spectral_x<T><<<grid[EK_SX], dim3(64, 4), smem[EK_SX], stream>>>(d_p, d_aux, d_pre[EK_SX], nmem);
+                launch_sx();
                 kb_ifft_y_pi<T><<<grid[EK_IFFTY], dim3(16, 16), smem[EK_IFFTY], stream>>>(d_p, G, d_aux,
                                                                                          d_pre[EK_IFFTY], nmem);
             };
@@ -398,7 +514,16 @@ class Ensemble : public EnsembleBase {
                 refresh_tables();
                 build_prefixes();
             }
-            std::snprintf(line, sizeof line, "y level tile %d (pressure solve %.3f ms)", bk, best);
+            // the fused x kernel's block size
+            {
+                const int keep = sx_threads;
+                sx_threads = 512;
+                const float t = timeit(chain);
+                if (t < best) best = t;
+                else sx_threads = keep;
+            }
+            std::snprintf(line, sizeof line, "y level tile %d, x block %d threads (pressure solve %.3f ms)", bk,
+                          sx_threads, best);
             info += line;
         }
         copy_all(false);
@@ -450,6 +575,7 @@ class Ensemble : public EnsembleBase {
         cudaMemcpy(d_f[0], f0.data(), sizeof(KFields<T>) * nmem, cudaMemcpyHostToDevice);
         cudaMemcpy(d_f[1], f1.data(), sizeof(KFields<T>) * nmem, cudaMemcpyHostToDevice);
         cudaMemcpy(d_aux, ha.data(), sizeof(MemberAux<T>) * nmem, cudaMemcpyHostToDevice);
+        build_prefixes();  // a basic state that changed may change the advection kernel
         rot = 0;
         for (auto &g : graph)
             if (g) {
@@ -475,13 +601,11 @@ class Ensemble : public EnsembleBase {
             kb_mirror<T><<<grid[EK_MIRROR], 256, 0, stream>>>(d_p, F, d_pre[EK_MIRROR], nmem);
             kb_div_fft_y<T><<<grid[EK_DIVY], dim3(16, 16), smem[EK_DIVY], stream>>>(d_p, F, d_aux, d_pre[EK_DIVY],
                                                                                    nmem, st);
-            kb_spectral_x<T><<<grid[EK_SX], dim3(64, 4), smem[EK_SX], stream>>>(d_p, d_aux, d_pre[EK_SX], nmem);
+            launch_sx();
             kb_ifft_y_pi<T><<<grid[EK_IFFTY], dim3(16, 16), smem[EK_IFFTY], stream>>>(d_p, F, d_aux, d_pre[EK_IFFTY],
                                                                                      nmem);
             const int fu = PF_PROJECT | PF_SPONGE | PF_VBC, ft = PF_SPONGE | PF_VBC, fq = PF_ZERO | PF_SPONGE | PF_VBC;
-            kb_post<T><<<grid[EK_POST], POST_THREADS, 0, stream>>>(d_p, F, d_pre[EK_POST], nmem,
-                                                                    make_int4(fu, fu, fu, ft), make_int4(fq, fq, fq, 0),
-                                                                    st);
+            launch_post(F, make_int4(fu, fu, fu, ft), make_int4(fq, fq, fq, 0), st);
             launches += 6;
             if (s < 2) swap_all();
         }
@@ -491,8 +615,7 @@ class Ensemble : public EnsembleBase {
             launches++;
         }
         const int fu = PF_SPONGE | PF_VBC | PF_RAYLEIGH | PF_WRITE_M, fq = PF_SPONGE | PF_VBC | PF_WRITE_M;
-        kb_post<T><<<grid[EK_POST], POST_THREADS, 0, stream>>>(d_p, F, d_pre[EK_POST], nmem, make_int4(fu, fu, fu, fu),
-                                                                make_int4(fq, fq, fq, 0), 1.0);
+        launch_post(F, make_int4(fu, fu, fu, fu), make_int4(fq, fq, fq, 0), 1.0);
         launches++;
         swap_all();
         for (auto *e : mem) {

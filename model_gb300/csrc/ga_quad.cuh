@@ -346,9 +346,10 @@ __device__ __forceinline__ void aq_store(float *dst, int c, int k0, int nz, int 
     }
 }
 
+// one TI x TJ tile (bx, by); the batched ensemble kernel calls it per member
 template <int TI, int TJ>
-__global__ void __launch_bounds__(AQ_THREADS, 3)
-    k_advect_quad(KParams<float> p, KFields<float> F, float step, float sdtg, int what)
+__device__ __forceinline__ void advect_quad_body(const KParams<float> &p, const KFields<float> &F, int bx, int by,
+                                                 float step, float sdtg, int what)
 {
     using G = AQGeom<TI, TJ>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -368,7 +369,7 @@ __global__ void __launch_bounds__(AQ_THREADS, 3)
         s_tbv[k] = p.tbv[k];
         lv[6 * nz + k] = p.rhou[k];
     }
-    const int i0 = 3 + blockIdx.x * TI, j0 = 3 + blockIdx.y * TJ;
+    const int i0 = 3 + bx * TI, j0 = 3 + by * TJ;
     const int ti = min(TI, p.nx - 3 - i0), tj = min(TJ, p.ny - 3 - j0);
     __syncthreads();
 
@@ -544,6 +545,13 @@ __global__ void __launch_bounds__(AQ_THREADS, 3)
     }
 }
 
+template <int TI, int TJ>
+__global__ void __launch_bounds__(AQ_THREADS, 3)
+    k_advect_quad(KParams<float> p, KFields<float> F, float step, float sdtg, int what)
+{
+    advect_quad_body<TI, TJ>(p, F, blockIdx.x, blockIdx.y, step, sdtg, what);
+}
+
 // ---------------------------------------------------------------------------
 // k_post_quad: the column post-processing of k_post, expression for
 // expression.  A column's bottom and top conditions copy level 1 to 0 and
@@ -552,13 +560,13 @@ __global__ void __launch_bounds__(AQ_THREADS, 3)
 // ---------------------------------------------------------------------------
 constexpr int PQ_THREADS = 256;
 
+// item w: column w / (NZ/4) of the enumeration `cols`, level quad w % (NZ/4)
 template <typename T>
-__global__ void __launch_bounds__(PQ_THREADS)
-    k_post_quad(KParams<T> p, KFields<T> F, int4 fl0, int4 fl1, T step, int cols)
+__device__ __forceinline__ void post_quad_body(const KParams<T> &p, const KFields<T> &F, int4 fl0, int4 fl1, T step,
+                                               int cols, long w)
 {
     static_assert(sizeof(T) == 4, "four-level kernels are FP32");
     const int nz = p.nz, NQ = nz >> 2, sx = p.ny * nz, sy = nz;
-    const long w = (long)blockIdx.x * PQ_THREADS + threadIdx.x;
     const int q = (int)(w % NQ), k0 = 4 * q;
     int i = 0, j = 0;
     bool ok = false;
@@ -646,6 +654,13 @@ __global__ void __launch_bounds__(PQ_THREADS)
         stg4(F.P[f] + c, out);
         if (flags & PF_WRITE_M) stg4(F.M[f] + c, out);
     }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(PQ_THREADS)
+    k_post_quad(KParams<T> p, KFields<T> F, int4 fl0, int4 fl1, T step, int cols)
+{
+    post_quad_body(p, F, fl0, fl1, step, cols, (long)blockIdx.x * PQ_THREADS + threadIdx.x);
 }
 
 }  // namespace ga
