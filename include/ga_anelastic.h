@@ -249,10 +249,15 @@ GA_API int ga_tuning(ga_ctx *ctx, char *buf, size_t n);
  * with the counters advanced) and maps the adjoint held in the perturbation
  * buffers, taken as the gradient of a function of the final state, to the
  * gradient with respect to the initial state.  The state is checkpointed every
- * `checkpoint_every` steps (<= 0: one segment) and each segment is recomputed,
- * recording the stage-start fields, before its adjoint runs: device memory
- * holds nsteps/checkpoint_every + 1 states and checkpoint_every steps of
- * trajectory (12 fields a step dry, 26 fields + 3 clipping records moist).
+ * `checkpoint_every` steps (<= 0: one segment).  A segment's adjoint runs on
+ * its trajectory (the stage-start fields: 12 fields a step dry, 26 fields + 3
+ * clipping records moist): the first sweep records the trajectories of the
+ * last segments, as many as device memory holds beside the checkpoints with a
+ * tenth of the GPU's memory to spare (at least one), and every earlier segment
+ * is recomputed from its checkpoint, recording, before its adjoint runs.  The
+ * environment variable GA_ADJ_RESIDENT=n fixes that count.  Results do not
+ * depend on it or on checkpoint_every.  The trajectory buffer is kept for
+ * later calls and released by ga_destroy.
  * The adjoint kernels are in gather form (no atomics).  The GA_PI entry is
  * zero on return: the step never reads pi.
  */
