@@ -2,7 +2,6 @@
 // rotation of the reference (solver.cpp:229-263, microphysics.cpp:642-669),
 // the per-operator launch sequences and the fused RK3 step.
 #pragma once
-#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -102,7 +101,6 @@ class Engine : public EngineBase {
     // and its tile; GA_ADVECT=tile or =quad restricts both the default and the
     // autotuner to one kernel
     int adv_quad = 1, adv_qi = 4, adv_qj = 8, adv_force = 0;
-    int adv_qs = 1;  // level slabs per column of the four-level kernel (GA_ADVECT_SLABS sets the default)
     // the four-level post-processing kernel (FP32, NZ % 4 == 0); GA_POST=column
     // keeps the per-level one
     bool post_quad = true;
@@ -292,7 +290,6 @@ class Engine : public EngineBase {
             else if (!std::strcmp(ev, "quad")) adv_force = 2;
         }
         adv_quad = adv_force != 1;
-        if (const char *ev = std::getenv("GA_ADVECT_SLABS")) adv_qs = std::max(1, std::min(4, std::atoi(ev)));
         if (const char *ev = std::getenv("GA_POST")) post_quad = std::strcmp(ev, "column") != 0;
         post_quad = post_quad && sizeof(T) == 4 && NZ % 4 == 0;
         if constexpr (sizeof(T) == 4) {
@@ -493,10 +490,9 @@ class Engine : public EngineBase {
     void launch_advect_quad(T step, T sdtg, int what)
     {
         if constexpr (sizeof(T) == 4) {
-            const int ns = std::min(adv_qs, NZ / 4);
-            dim3 grid(cdiv(NX - 6, TI), cdiv(NY - 6, TJ), ns);
-            k_advect_quad<TI, TJ><<<grid, AQ_THREADS, advect_quad_smem(TI, TJ, NZ, ns), stream>>>(kp, fields(),
-                                                                                                step, sdtg, what);
+            dim3 grid(cdiv(NX - 6, TI), cdiv(NY - 6, TJ));
+            k_advect_quad<TI, TJ><<<grid, AQ_THREADS, advect_quad_smem(TI, TJ, NZ), stream>>>(kp, fields(), step,
+                                                                                            sdtg, what);
         }
     }
     template <int TI, int TJ>
@@ -835,7 +831,7 @@ class Engine : public EngineBase {
         // advection tile
         {
             float best = 1e30f;
-            int bi = adv_ti, bj = adv_tj, bq = 0, qi = adv_qi, qj = adv_qj, qs = adv_qs;
+            int bi = adv_ti, bj = adv_tj, bq = 0, qi = adv_qi, qj = adv_qj;
             if (adv_force != 2 || !quad_ok(adv_qi, adv_qj)) {
                 adv_quad = 0;
                 for (auto &tl : kAdvTiles) {
@@ -850,18 +846,14 @@ class Engine : public EngineBase {
                 adv_quad = 1;
                 for (auto &tl : kQuadTiles) {
                     if (!quad_ok(tl[0], tl[1])) continue;
-                    for (int ns = 1; ns <= 2 && ns <= NZ / 4; ns++) {
-                        adv_qi = tl[0]; adv_qj = tl[1]; adv_qs = ns;
-                        const float t = timeit([&] { advect(1. / 3., what); });
-                        if (t < best) { best = t; bq = 1; qi = tl[0]; qj = tl[1]; qs = ns; }
-                    }
+                    adv_qi = tl[0]; adv_qj = tl[1];
+                    const float t = timeit([&] { advect(1. / 3., what); });
+                    if (t < best) { best = t; bq = 1; qi = tl[0]; qj = tl[1]; }
                 }
             }
-            adv_ti = bi; adv_tj = bj; adv_quad = bq; adv_qi = qi; adv_qj = qj; adv_qs = qs;
+            adv_ti = bi; adv_tj = bj; adv_quad = bq; adv_qi = qi; adv_qj = qj;
             smem_adv = advect_tile_smem(bi, bj, NZ, sizeof(T));
-            if (bq)
-                std::snprintf(line, sizeof line, "advect tile %dx%d, four levels per thread, %d level slab%s (%.4f ms); ",
-                              qi, qj, qs, qs > 1 ? "s" : "", best);
+            if (bq) std::snprintf(line, sizeof line, "advect tile %dx%d, four levels per thread (%.4f ms); ", qi, qj, best);
             else std::snprintf(line, sizeof line, "advect tile %dx%d (%.4f ms); ", bi, bj, best);
             info += line;
         }

@@ -69,7 +69,7 @@ __global__ void __launch_bounds__(AQ_THREADS, 3) kb_advect_quad(const KParams<T>
         const long lb = vb - pre[m];
         const int gx = (p.nx - 6 + TI - 1) / TI;
         const double sdtg = step * p.dt_d * 9.8 * 0.5;  // step*dt*grav*0.5, advection.cpp:330
-        advect_quad_body<TI, TJ>(p, F[m], (int)(lb % gx), (int)(lb / gx), 0, 1, (T)step, (T)sdtg, what);
+        advect_quad_body<TI, TJ>(p, F[m], (int)(lb % gx), (int)(lb / gx), (T)step, (T)sdtg, what);
         __syncthreads();
     }
 }

@@ -32,26 +32,11 @@ struct AQGeom {
     static constexpr int CF = CE + CN + CT;   // face columns of one field
 };
 
-// A block covers the level quads q0 .. q0+nq-1 of its columns: the column's
-// quads split into nslab slabs (a second slab doubles the blocks of a small
-// grid).  Face columns in shared memory are L = 4 (nq + 1) floats long: east
-// and north faces of the slab's quads from 0, top faces from 4, with the quad
-// below the slab (its top face at level 4 q0 - 1 is the lower face of the
-// slab's first cell) at 0.
-struct AQSlab {
-    int q0, nq, L;
-};
-__host__ __device__ inline AQSlab aq_slab(int nz, int kslab, int nslab)
-{
-    const int NQ = nz >> 2, q0 = kslab * NQ / nslab, q1 = (kslab + 1) * NQ / nslab;
-    return AQSlab{q0, q1 - q0, 4 * ((NQ + nslab - 1) / nslab + 1)};
-}
-
 // two field slots of face columns, the basic-state table, the level arrays
-__host__ __device__ constexpr size_t advect_quad_smem(int ti, int tj, int nz, int nslab = 1)
+__host__ __device__ constexpr size_t advect_quad_smem(int ti, int tj, int nz)
 {
-    return (2 * (size_t)((ti + 1) * tj + ti * (tj + 1) + ti * tj) * (4 * ((nz / 4 + nslab - 1) / nslab + 1)) +
-            (size_t)BT_COUNT * nz + (size_t)AQ_LV * nz) *
+    return (2 * (size_t)((ti + 1) * tj + ti * (tj + 1) + ti * tj) * nz + (size_t)BT_COUNT * nz +
+            (size_t)AQ_LV * nz) *
            sizeof(float);
 }
 
@@ -299,42 +284,39 @@ __device__ __forceinline__ Q4 aq_top(const KParams<float> &p, const KFields<floa
 // the face columns of field FK into slot `sl` (E, N and T of the tile)
 template <int TI, int TJ, int FK>
 __device__ __forceinline__ void aq_faces(const KParams<float> &p, const KFields<float> &F, const float *tab,
-                                         float *sl, int i0, int j0, int ti, int tj, const AQSlab &S)
+                                         float *sl, int i0, int j0, int ti, int tj)
 {
     using G = AQGeom<TI, TJ>;
-    const int nq = S.nq, L = S.L;
-    float *E = sl, *N = sl + G::CE * L, *T = N + G::CN * L;
-    for (int w = threadIdx.x; w < G::CE * nq; w += AQ_THREADS) {
-        const int lq = w % nq, col = w / nq, b = col % TJ, a = col / TJ;
+    const int nz = p.nz, NQ = nz >> 2;
+    float *E = sl, *N = sl + G::CE * nz, *T = N + G::CN * nz;
+    for (int w = threadIdx.x; w < G::CE * NQ; w += AQ_THREADS) {
+        const int q = w % NQ, col = w / NQ, b = col % TJ, a = col / TJ;
         if (a > ti || b >= tj) continue;
-        sts4(E + col * L + 4 * lq, aq_east<FK>(p, F, tab, i0 - 1 + a, j0 + b, 4 * (S.q0 + lq)));
+        sts4(E + col * nz + 4 * q, aq_east<FK>(p, F, tab, i0 - 1 + a, j0 + b, 4 * q));
     }
-    for (int w = threadIdx.x; w < G::CN * nq; w += AQ_THREADS) {
-        const int lq = w % nq, col = w / nq, b = col % (TJ + 1), a = col / (TJ + 1);
+    for (int w = threadIdx.x; w < G::CN * NQ; w += AQ_THREADS) {
+        const int q = w % NQ, col = w / NQ, b = col % (TJ + 1), a = col / (TJ + 1);
         if (a >= ti || b > tj) continue;
-        sts4(N + col * L + 4 * lq, aq_north<FK>(p, F, tab, i0 + a, j0 - 1 + b, 4 * (S.q0 + lq)));
+        sts4(N + col * nz + 4 * q, aq_north<FK>(p, F, tab, i0 + a, j0 - 1 + b, 4 * q));
     }
-    // top faces of the slab's quads and, above the bottom slab, the quad below
-    const int lt0 = S.q0 > 0 ? -1 : 0, nt = nq - lt0;
-    for (int w = threadIdx.x; w < G::CT * nt; w += AQ_THREADS) {
-        const int lt = lt0 + w % nt, col = w / nt, b = col % TJ, a = col / TJ;
+    for (int w = threadIdx.x; w < G::CT * NQ; w += AQ_THREADS) {
+        const int q = w % NQ, col = w / NQ, b = col % TJ, a = col / TJ;
         if (a >= ti || b >= tj) continue;
-        sts4(T + col * L + 4 * (lt + 1), aq_top<FK>(p, F, tab, i0 + a, j0 + b, 4 * (S.q0 + lt)));
+        sts4(T + col * nz + 4 * q, aq_top<FK>(p, F, tab, i0 + a, j0 + b, 4 * q));
     }
 }
 
 // flux divergence of the slot at the cell quad (tend of k_advect_tile)
 template <int TI, int TJ>
-__device__ __forceinline__ Q4 aq_div(const KParams<float> &p, const float *sl, const float *lv, int a, int b, int k0,
-                                     int lq, int L)
+__device__ __forceinline__ Q4 aq_div(const KParams<float> &p, const float *sl, const float *lv, int a, int b, int k0)
 {
     using G = AQGeom<TI, TJ>;
     const int nz = p.nz;
-    const float *E = sl, *N = sl + G::CE * L, *T = N + G::CN * L;
+    const float *E = sl, *N = sl + G::CE * nz, *T = N + G::CN * nz;
     const float *s_mu = lv, *s_rhow = lv + nz, *s_odr = lv + 2 * nz;
-    const int oe = ((a + 1) * TJ + b) * L + 4 * lq, ow = (a * TJ + b) * L + 4 * lq;
-    const int on = (a * (TJ + 1) + b + 1) * L + 4 * lq, os = (a * (TJ + 1) + b) * L + 4 * lq;
-    const int ot = (a * TJ + b) * L + 4 * (lq + 1);
+    const int oe = ((a + 1) * TJ + b) * nz + k0, ow = (a * TJ + b) * nz + k0;
+    const int on = (a * (TJ + 1) + b + 1) * nz + k0, os = (a * (TJ + 1) + b) * nz + k0;
+    const int ot = (a * TJ + b) * nz + k0;
     const Q4 ee = lds4(E + oe), ew = lds4(E + ow), nn = lds4(N + on), ns = lds4(N + os), tt = lds4(T + ot);
     const float tb0 = k0 > 0 ? T[ot - 1] : 0.f;
     Q4 r;
@@ -367,15 +349,13 @@ __device__ __forceinline__ void aq_store(float *dst, int c, int k0, int nz, int 
 // one TI x TJ tile (bx, by); the batched ensemble kernel calls it per member
 template <int TI, int TJ>
 __device__ __forceinline__ void advect_quad_body(const KParams<float> &p, const KFields<float> &F, int bx, int by,
-                                                 int kslab, int nslab, float step, float sdtg, int what)
+                                                 float step, float sdtg, int what)
 {
     using G = AQGeom<TI, TJ>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int nz = p.nz, sx = p.ny * nz, sy = nz;
-    const AQSlab S = aq_slab(nz, kslab, nslab);
-    const int nq = S.nq, L = S.L;
-    float *s0 = (float *)smem_raw, *s1 = s0 + G::CF * L;
-    float *tab = s1 + G::CF * L;
+    const int nz = p.nz, NQ = nz >> 2, sx = p.ny * nz, sy = nz;
+    float *s0 = (float *)smem_raw, *s1 = s0 + G::CF * nz;
+    float *tab = s1 + G::CF * nz;
     float *lv = tab + BT_COUNT * nz;
     float *s_mu = lv, *s_rhow = lv + nz, *s_odr = lv + 2 * nz, *s_tb = lv + 3 * nz, *s_qb = lv + 4 * nz,
           *s_tbv = lv + 5 * nz;
@@ -396,20 +376,20 @@ __device__ __forceinline__ void advect_quad_body(const KParams<float> &p, const 
     // ---- pass 1: u, v (and the buoyancy of w)
     if (what & (ADV_UV | ADV_WB)) {
         if (what & ADV_UV) {
-            aq_faces<TI, TJ, 0>(p, F, tab, s0, i0, j0, ti, tj, S);
-            aq_faces<TI, TJ, 1>(p, F, tab, s1, i0, j0, ti, tj, S);
+            aq_faces<TI, TJ, 0>(p, F, tab, s0, i0, j0, ti, tj);
+            aq_faces<TI, TJ, 1>(p, F, tab, s1, i0, j0, ti, tj);
         }
         __syncthreads();
-        for (int w = threadIdx.x; w < G::CT * nq; w += AQ_THREADS) {
-            const int lq = w % nq, col = w / nq, b = col % TJ, a = col / TJ;
+        for (int w = threadIdx.x; w < G::CT * NQ; w += AQ_THREADS) {
+            const int q = w % NQ, col = w / NQ, b = col % TJ, a = col / TJ;
             if (a >= ti || b >= tj) continue;
-            const int i = i0 + a, j = j0 + b, k0 = 4 * (S.q0 + lq);
+            const int i = i0 + a, j = j0 + b, k0 = 4 * q;
             const int c = gix(p.ny, nz, i, j, k0);
             if (what & ADV_UV) {
                 const float *U = F.cur[FU], *V = F.cur[FV];
                 const float fj = p.f[j];
                 {
-                    const Q4 d = aq_div<TI, TJ>(p, s0, lv, a, b, k0, lq, L);
+                    const Q4 d = aq_div<TI, TJ>(p, s0, lv, a, b, k0);
                     const Q4 v0 = ldg4(V, c), v1 = ldg4(V, c + sy), v2 = ldg4(V, c - sx), v3 = ldg4(V, c - sx + sy);
                     const Q4 m = ldg4(F.M[FU], c);
                     Q4 r;
@@ -422,7 +402,7 @@ __device__ __forceinline__ void advect_quad_body(const KParams<float> &p, const 
                     aq_store(F.P[FU], c, k0, nz, 1, r);
                 }
                 {
-                    const Q4 d = aq_div<TI, TJ>(p, s1, lv, a, b, k0, lq, L);
+                    const Q4 d = aq_div<TI, TJ>(p, s1, lv, a, b, k0);
                     const Q4 u0 = ldg4(U, c), u1 = ldg4(U, c + sx), u2 = ldg4(U, c - sy), u3 = ldg4(U, c + sx - sy);
                     const Q4 m = ldg4(F.M[FV], c);
                     Q4 r;
@@ -465,19 +445,19 @@ __device__ __forceinline__ void advect_quad_body(const KParams<float> &p, const 
     // ---- pass 2: theta, qv (qv's clipping bit)
     const bool th_on = (what & ADV_TH) != 0, q_on = (what & ADV_Q) != 0;
     if (th_on || q_on) {
-        if (th_on) aq_faces<TI, TJ, 2>(p, F, tab, s0, i0, j0, ti, tj, S);
-        if (q_on) aq_faces<TI, TJ, 3>(p, F, tab, s1, i0, j0, ti, tj, S);
+        if (th_on) aq_faces<TI, TJ, 2>(p, F, tab, s0, i0, j0, ti, tj);
+        if (q_on) aq_faces<TI, TJ, 3>(p, F, tab, s1, i0, j0, ti, tj);
         __syncthreads();
-        for (int w = threadIdx.x; w < G::CT * nq; w += AQ_THREADS) {
-            const int lq = w % nq, col = w / nq, b = col % TJ, a = col / TJ;
+        for (int w = threadIdx.x; w < G::CT * NQ; w += AQ_THREADS) {
+            const int q = w % NQ, col = w / NQ, b = col % TJ, a = col / TJ;
             if (a >= ti || b >= tj) continue;
-            const int i = i0 + a, j = j0 + b, k0 = 4 * (S.q0 + lq);
+            const int i = i0 + a, j = j0 + b, k0 = 4 * q;
             const int c = gix(p.ny, nz, i, j, k0);
             const Win wc = ldwin(F.cur[FW], c, k0, nz);
             for (int fi = 0; fi < 2; fi++) {
                 if (fi == 0 ? !th_on : !q_on) continue;
                 const float *base = fi == 0 ? s_tb : s_qb;
-                const Q4 d = aq_div<TI, TJ>(p, fi == 0 ? s0 : s1, lv, a, b, k0, lq, L);
+                const Q4 d = aq_div<TI, TJ>(p, fi == 0 ? s0 : s1, lv, a, b, k0);
                 const Q4 m = ldg4(F.M[fi == 0 ? FTH : FQV], c);
                 Q4 r;
                 unsigned bits = 0;
@@ -517,16 +497,16 @@ __device__ __forceinline__ void advect_quad_body(const KParams<float> &p, const 
 
     // ---- pass 3: qc, qr (clipping bits 2 and 4, the rain's fall speed)
     if (q_on) {
-        aq_faces<TI, TJ, 4>(p, F, tab, s0, i0, j0, ti, tj, S);
-        aq_faces<TI, TJ, 5>(p, F, tab, s1, i0, j0, ti, tj, S);
+        aq_faces<TI, TJ, 4>(p, F, tab, s0, i0, j0, ti, tj);
+        aq_faces<TI, TJ, 5>(p, F, tab, s1, i0, j0, ti, tj);
         __syncthreads();
-        for (int w = threadIdx.x; w < G::CT * nq; w += AQ_THREADS) {
-            const int lq = w % nq, col = w / nq, b = col % TJ, a = col / TJ;
+        for (int w = threadIdx.x; w < G::CT * NQ; w += AQ_THREADS) {
+            const int q = w % NQ, col = w / NQ, b = col % TJ, a = col / TJ;
             if (a >= ti || b >= tj) continue;
-            const int i = i0 + a, j = j0 + b, k0 = 4 * (S.q0 + lq);
+            const int i = i0 + a, j = j0 + b, k0 = 4 * q;
             const int c = gix(p.ny, nz, i, j, k0);
-            const Q4 dc = aq_div<TI, TJ>(p, s0, lv, a, b, k0, lq, L);
-            const Q4 dr = aq_div<TI, TJ>(p, s1, lv, a, b, k0, lq, L);
+            const Q4 dc = aq_div<TI, TJ>(p, s0, lv, a, b, k0);
+            const Q4 dr = aq_div<TI, TJ>(p, s1, lv, a, b, k0);
             const Q4 mc = ldg4(F.M[FQC], c), mr = ldg4(F.M[FQR], c);
             Q4 rc, rr;
             unsigned char bits[4] = {0, 0, 0, 0};
@@ -569,7 +549,7 @@ template <int TI, int TJ>
 __global__ void __launch_bounds__(AQ_THREADS, 3)
     k_advect_quad(KParams<float> p, KFields<float> F, float step, float sdtg, int what)
 {
-    advect_quad_body<TI, TJ>(p, F, blockIdx.x, blockIdx.y, blockIdx.z, gridDim.z, step, sdtg, what);
+    advect_quad_body<TI, TJ>(p, F, blockIdx.x, blockIdx.y, step, sdtg, what);
 }
 
 // ---------------------------------------------------------------------------
@@ -618,13 +598,18 @@ __device__ __forceinline__ void post_quad_body(const KParams<T> &p, const KField
             dpz[e] = pc.at(e) - pc.at(e - 1);
         }
     }
-#pragma unroll 1
+    // every field's quad is loaded before any is written (a store to one
+    // field's buffer would otherwise order the next field's load after it)
+    Q4 inq[7];
+#pragma unroll
+    for (int f = 0; f < 7; ++f) inq[f] = flv[f] ? ldg4(F.P[f], cs) : Q4{{0.f, 0.f, 0.f, 0.f}};
+    Q4 qb4{{0.f, 0.f, 0.f, 0.f}};
+    if ((flv[FQV] & PF_ZERO) && col_in) qb4 = ldg4(F.bar[4], cs);
+#pragma unroll
     for (int f = 0; f < 7; ++f) {
         const int flags = flv[f];
         if (!flags) continue;
-        const Q4 in = ldg4(F.P[f], cs);
-        Q4 qb4{{0.f, 0.f, 0.f, 0.f}};
-        if ((flags & PF_ZERO) && f == FQV && col_in) qb4 = ldg4(F.bar[4], cs);
+        const Q4 in = inq[f];
         float ch[4];
 #pragma unroll
         for (int e = 0; e < 4; e++) {

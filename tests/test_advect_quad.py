@@ -28,16 +28,12 @@ def _built():
     build.build()
 
 
-def _pair(monkeypatch, wl, slabs=1):
-    """a per-level tile context and a four-level one whose columns split
-    into `slabs` level slabs"""
+def _pair(monkeypatch, wl):
     ms = []
     for mode in ("tile", "quad"):
         monkeypatch.setenv("GA_ADVECT", mode)
-        monkeypatch.setenv("GA_ADVECT_SLABS", str(slabs))
         ms.append(anelastic.Model(wl, abi.GA_PREC_F32))
     monkeypatch.delenv("GA_ADVECT")
-    monkeypatch.delenv("GA_ADVECT_SLABS")
     return ms
 
 
@@ -57,14 +53,13 @@ def _perturb(ms, wl, seed):
                 m.set(f, slot, x)
 
 
-@pytest.mark.parametrize("slabs", [1, 2, 3])
 @pytest.mark.parametrize("case", ["moist_rf1", "moist_rf2", "dry"])
-def test_single_advection_operator_bit_identical(monkeypatch, case, slabs):
+def test_single_advection_operator_bit_identical(monkeypatch, case):
     if case == "dry":
         wl = configs.dry_bubble(nx=30, ny=26, nz=20, nsteps=2)
     else:
         wl = configs.moist_blob(nx=30, ny=26, nz=16, rain_fallout=1 if case == "moist_rf1" else 2)
-    ms = _pair(monkeypatch, wl, slabs)
+    ms = _pair(monkeypatch, wl)
     _perturb(ms, wl, 11)
     for op, fields in ADVECT_OPS.items():
         if op == "advect_micro" and not wl.microphysics_option:
@@ -76,9 +71,8 @@ def test_single_advection_operator_bit_identical(monkeypatch, case, slabs):
             np.testing.assert_array_equal(b, a, err_msg=f"{case} {op} field {abi.PROG_NAMES[f]}")
 
 
-@pytest.mark.parametrize("slabs", [1, 2])
 @pytest.mark.parametrize("case", ["moist_blob", "thunderstorm_small", "dry_bubble", "nz_not_multiple_of_4"])
-def test_steps_match_tile_kernel(monkeypatch, case, slabs):
+def test_steps_match_tile_kernel(monkeypatch, case):
     if case == "moist_blob":
         wl = configs.moist_blob(nx=30, ny=26, nz=16, nsteps=6)
     elif case == "thunderstorm_small":
@@ -87,7 +81,7 @@ def test_steps_match_tile_kernel(monkeypatch, case, slabs):
         wl = configs.dry_bubble(nx=34, ny=30, nz=20, nsteps=6)
     else:  # falls back to the tile kernel: both contexts run the same code
         wl = configs.moist_blob(nx=30, ny=26, nz=18, nsteps=6)
-    ms = _pair(monkeypatch, wl, slabs)
+    ms = _pair(monkeypatch, wl)
     for m in ms:
         m.step(wl.nsteps)
     nprog = 7 if wl.microphysics_option else 4
