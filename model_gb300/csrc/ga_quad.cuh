@@ -385,36 +385,27 @@ __device__ __forceinline__ void advect_quad_body(const KParams<float> &p, const 
             if (a >= ti || b >= tj) continue;
             const int i = i0 + a, j = j0 + b, k0 = 4 * q;
             const int c = gix(p.ny, nz, i, j, k0);
+            // every load of the quad's u, v and w results before any store
+            // (a store to P would otherwise order the later loads after it)
+            Q4 ru, rv;
             if (what & ADV_UV) {
                 const float *U = F.cur[FU], *V = F.cur[FV];
                 const float fj = p.f[j];
-                {
-                    const Q4 d = aq_div<TI, TJ>(p, s0, lv, a, b, k0);
-                    const Q4 v0 = ldg4(V, c), v1 = ldg4(V, c + sy), v2 = ldg4(V, c - sx), v3 = ldg4(V, c - sx + sy);
-                    const Q4 m = ldg4(F.M[FU], c);
-                    Q4 r;
+                const Q4 v0 = ldg4(V, c), v1 = ldg4(V, c + sy), v2 = ldg4(V, c - sx), v3 = ldg4(V, c - sx + sy);
+                const Q4 u0 = ldg4(U, c), u1 = ldg4(U, c + sx), u2 = ldg4(U, c - sy), u3 = ldg4(U, c + sx - sy);
+                const Q4 mu = ldg4(F.M[FU], c), mv = ldg4(F.M[FV], c);
+                const Q4 du = aq_div<TI, TJ>(p, s0, lv, a, b, k0), dv = aq_div<TI, TJ>(p, s1, lv, a, b, k0);
 #pragma unroll
-                    for (int e = 0; e < 4; e++) {
-                        const float ov_u = 0.25f * (v0.v[e] + v1.v[e] + v2.v[e] + v3.v[e]);
-                        const float ut = d.v[e] + p.dt * fj * ov_u;
-                        r.v[e] = m.v[e] + step * ut;
-                    }
-                    aq_store(F.P[FU], c, k0, nz, 1, r);
-                }
-                {
-                    const Q4 d = aq_div<TI, TJ>(p, s1, lv, a, b, k0);
-                    const Q4 u0 = ldg4(U, c), u1 = ldg4(U, c + sx), u2 = ldg4(U, c - sy), u3 = ldg4(U, c + sx - sy);
-                    const Q4 m = ldg4(F.M[FV], c);
-                    Q4 r;
-#pragma unroll
-                    for (int e = 0; e < 4; e++) {
-                        const float ov_v = 0.25f * (u0.v[e] + u1.v[e] + u2.v[e] + u3.v[e]);
-                        const float vt = d.v[e] - p.dt * fj * ov_v;
-                        r.v[e] = m.v[e] + step * vt;
-                    }
-                    aq_store(F.P[FV], c, k0, nz, 1, r);
+                for (int e = 0; e < 4; e++) {
+                    const float ov_u = 0.25f * (v0.v[e] + v1.v[e] + v2.v[e] + v3.v[e]);
+                    const float ut = du.v[e] + p.dt * fj * ov_u;
+                    ru.v[e] = mu.v[e] + step * ut;
+                    const float ov_v = 0.25f * (u0.v[e] + u1.v[e] + u2.v[e] + u3.v[e]);
+                    const float vt = dv.v[e] - p.dt * fj * ov_v;
+                    rv.v[e] = mv.v[e] + step * vt;
                 }
             }
+            Q4 rw;
             if (what & ADV_WB) {
                 // buoyancy at levels k0-1 .. k0+3 (b1 of level k is b0 of level k-1)
                 const Win th = ldwin(F.cur[FTH], c, k0, nz);
@@ -433,11 +424,14 @@ __device__ __forceinline__ void advect_quad_body(const KParams<float> &p, const 
                     else bb[e] = th.at(e - 1) / s_tbv[kc] + 0.61f * qv.at(e - 1) - qc.at(e - 1) - qr.at(e - 1);
                 }
                 const Q4 m = ldg4(F.M[FW], c);
-                Q4 r;
 #pragma unroll
-                for (int e = 0; e < 4; e++) r.v[e] = m.v[e] + sdtg * (bb[e + 1] + bb[e]);
-                aq_store(F.P[FW], c, k0, nz, 2, r);
+                for (int e = 0; e < 4; e++) rw.v[e] = m.v[e] + sdtg * (bb[e + 1] + bb[e]);
             }
+            if (what & ADV_UV) {
+                aq_store(F.P[FU], c, k0, nz, 1, ru);
+                aq_store(F.P[FV], c, k0, nz, 1, rv);
+            }
+            if (what & ADV_WB) aq_store(F.P[FW], c, k0, nz, 2, rw);
         }
         __syncthreads();
     }
@@ -454,13 +448,18 @@ __device__ __forceinline__ void advect_quad_body(const KParams<float> &p, const 
             const int i = i0 + a, j = j0 + b, k0 = 4 * q;
             const int c = gix(p.ny, nz, i, j, k0);
             const Win wc = ldwin(F.cur[FW], c, k0, nz);
+            // both fields' start-of-step values before either store
+            const Q4 z4{{0.f, 0.f, 0.f, 0.f}};
+            const Q4 mq[2] = {th_on ? ldg4(F.M[FTH], c) : z4, q_on ? ldg4(F.M[FQV], c) : z4};
+            Q4 rq[2];
+            unsigned bits = 0;
+#pragma unroll
             for (int fi = 0; fi < 2; fi++) {
                 if (fi == 0 ? !th_on : !q_on) continue;
                 const float *base = fi == 0 ? s_tb : s_qb;
                 const Q4 d = aq_div<TI, TJ>(p, fi == 0 ? s0 : s1, lv, a, b, k0);
-                const Q4 m = ldg4(F.M[fi == 0 ? FTH : FQV], c);
+                const Q4 m = mq[fi];
                 Q4 r;
-                unsigned bits = 0;
 #pragma unroll
                 for (int e = 0; e < 4; e++) {
                     const int k = k0 + e;
@@ -481,14 +480,16 @@ __device__ __forceinline__ void advect_quad_body(const KParams<float> &p, const 
                     }
                     r.v[e] = v;
                 }
-                aq_store(F.P[fi == 0 ? FTH : FQV], c, k0, nz, 1, r);
-                if (fi == 1 && (what & ADV_ZERO) && F.qmask) {
-                    unsigned char *qm = F.qmask + c;
+                rq[fi] = r;
+            }
+            if (th_on) aq_store(F.P[FTH], c, k0, nz, 1, rq[0]);
+            if (q_on) aq_store(F.P[FQV], c, k0, nz, 1, rq[1]);
+            if (q_on && (what & ADV_ZERO) && F.qmask) {
+                unsigned char *qm = F.qmask + c;
 #pragma unroll
-                    for (int e = 0; e < 4; e++) {
-                        const int k = k0 + e;
-                        if (k >= 1 && k <= nz - 2) qm[e] = (unsigned char)((bits >> (8 * e)) & 1u);
-                    }
+                for (int e = 0; e < 4; e++) {
+                    const int k = k0 + e;
+                    if (k >= 1 && k <= nz - 2) qm[e] = (unsigned char)((bits >> (8 * e)) & 1u);
                 }
             }
         }
