@@ -87,6 +87,10 @@ class Engine : public EngineBase {
     int KTy = 1, KTx = 1, lgKTy = 0, lgKTx = 0, TC = 64;
     int psx = 0;  // point stride of the fused spectral-x kernel (0: unfused path)
     int sx_threads = 256;  // threads of a fused spectral-x block (autotuned)
+    // FP32: the fused x kernel as clusters of two CTAs per y-wavenumber
+    // (autotuned; GA_SPECTRAL_X=pair makes it the default)
+    bool sx_pair = false;
+    size_t smem_sxp = 0;
     size_t smem_y = 0, smem_x = 0, smem_th = 0, smem_sx = 0, smem_adv = 0;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     bool bar_uniform[6] = {false, false, false, false, false, false};
@@ -237,6 +241,37 @@ class Engine : public EngineBase {
         kp.rhou_d = upload(std::vector<double>(cols->rhou, cols->rhou + NZ));
         kp.dx2 = dx * dx;
         kp.low_modes = sizeof(T) == 8 ? 0 : 1;  // FP32: the mean mode (0,0) solves in FP64
+        if (const char *ev = std::getenv("GA_LOW_MODES"))  // FP32: |p|, |q| below this solve in FP64
+            if (sizeof(T) == 4) kp.low_modes = std::max(0, std::atoi(ev));
+        kp.mean_inv = nullptr;
+        if (sizeof(T) == 4 && kp.low_modes > 0) {
+            // the mean mode's system, rows = levels 1..NZ-2 as the FP64 reduction
+            // builds them (top row replaced by x = 0), inverted column by
+            // column with the Thomas algorithm in extended precision
+            const int nl = NZ - 2;
+            std::vector<long double> a(nl), b(nl), c(nl), f(nl), y(nl);
+            for (int r = 0; r < nl; r++) {
+                const int k = r + 1;
+                a[r] = ac[k];
+                b[r] = cols->rhou[k] * 2.0 * hcoef[0] / kp.dx2 - vc[k];
+                c[r] = cc[k];
+            }
+            a[nl - 1] = 0; b[nl - 1] = 1; c[nl - 1] = 0;
+            std::vector<double> inv((size_t)nl * nl);
+            for (int jc = 0; jc < nl; jc++) {
+                long double den = b[0];
+                f[0] = c[0] / den;
+                y[0] = (jc == 0 ? 1.0L : 0.0L) / den;
+                for (int r = 1; r < nl; r++) {
+                    den = b[r] - a[r] * f[r - 1];
+                    f[r] = c[r] / den;
+                    y[r] = ((r == jc ? 1.0L : 0.0L) - a[r] * y[r - 1]) / den;
+                }
+                for (int r = nl - 2; r >= 0; r--) y[r] -= f[r] * y[r + 1];
+                for (int r = 0; r < nl; r++) inv[(size_t)r * nl + jc] = (double)y[r];
+            }
+            kp.mean_inv = upload(inv);
+        }
 
         // ---- FFT plans and twiddles ----
         plan_i = make_fft_plan(ni);
@@ -292,6 +327,12 @@ class Engine : public EngineBase {
         adv_quad = adv_force != 1;
         if (const char *ev = std::getenv("GA_POST")) post_quad = std::strcmp(ev, "column") != 0;
         post_quad = post_quad && sizeof(T) == 4 && NZ % 4 == 0;
+        if constexpr (sizeof(T) == 4) {
+            smem_sxp = sx_pair_smem(kp.ni, NZ);
+            cudaFuncSetAttribute(k_spectral_x_pair<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+            const char *ev = std::getenv("GA_SPECTRAL_X");
+            sx_pair = ev && !std::strcmp(ev, "pair") && pair_ok();
+        }
         if constexpr (sizeof(T) == 4) {
             for (auto &tl : kQuadTiles) quad_attr(tl[0], tl[1], optin);
         }
@@ -508,6 +549,8 @@ class Engine : public EngineBase {
         else if (ti == 2 && tj == 8) quad_attr_t<2, 8>(optin);
         else if (ti == 8 && tj == 8) quad_attr_t<8, 8>(optin);
     }
+    // the paired x kernel applies: FP32, the fused path, its shared memory
+    bool pair_ok() const { return sizeof(T) == 4 && psx > 0 && smem_sxp <= 200 * 1024; }
     // the four-level kernel applies: FP32, basic state a function of height,
     // whole quads of levels, face columns within the shared-memory limit
     bool quad_ok(int ti, int tj) const
@@ -567,8 +610,18 @@ class Engine : public EngineBase {
         if (psx > 0) {
             ProfScope ps(this, PC_THOMAS, 1);
             const int nl = NZ - 2, bx = std::min(nl, 64);
-            k_spectral_x<T><<<kp.nj, dim3(bx, std::max(1, sx_threads / bx)), smem_sx, stream>>>(kp, spec, plan_i,
-                                                                                               tw_i, psx);
+            bool pair = false;
+            if constexpr (sizeof(T) == 4) pair = sx_pair && pair_ok();
+            if (pair) {
+                if constexpr (sizeof(T) == 4) {
+                    const int bh = std::min((nl + 1) / 2, 32);
+                    k_spectral_x_pair<T><<<2 * kp.nj, dim3(bh, std::max(1, sx_threads / bh)), smem_sxp, stream>>>(
+                        kp, spec, plan_i, tw_i, sx_pair_layout(NZ));
+                }
+            } else {
+                k_spectral_x<T><<<kp.nj, dim3(bx, std::max(1, sx_threads / bx)), smem_sx, stream>>>(kp, spec, plan_i,
+                                                                                                   tw_i, psx);
+            }
             launches += 1;
         } else {
             {
@@ -903,13 +956,25 @@ class Engine : public EngineBase {
             }
             plan_order_i = bxo;
             plan_i = make_fft_plan(kp.ni, bxo);
-            // the fused x kernel's block size
+            // the fused x kernel's block size, and (FP32) its paired-CTA form
             if (psx > 0) {
                 const int keep = sx_threads;
+                int bt = keep;
+                bool bp = false;
+                sx_pair = false;
                 sx_threads = 512;
-                const float t = timeit([&] { solve_pressure(1. / 3.); });
-                if (t < bx) bx = t;
-                else sx_threads = keep;
+                float t = timeit([&] { solve_pressure(1. / 3.); });
+                if (t < bx) { bx = t; bt = 512; }
+                if (pair_ok()) {
+                    sx_pair = true;
+                    for (int nt : {256, 512}) {
+                        sx_threads = nt;
+                        t = timeit([&] { solve_pressure(1. / 3.); });
+                        if (t < bx) { bx = t; bt = nt; bp = true; }
+                    }
+                }
+                sx_threads = bt;
+                sx_pair = bp;
             }
             // the unfused path (x FFT, Thomas, inverse x FFT) and its level
             // tile, against the fused kernel where that fits
@@ -934,7 +999,8 @@ class Engine : public EngineBase {
                 while ((1 << lgKTx) < KTx) lgKTx++;
                 smem_x = 2 * (size_t)kp.ni * KTx * sizeof(T2);
                 if (psx == 0) std::snprintf(line, sizeof line, "x level tile %d, ", KTx);
-                else std::snprintf(line, sizeof line, "x fused, %d threads, ", sx_threads);
+                else std::snprintf(line, sizeof line, "x fused%s, %d threads, ", sx_pair ? " (CTA pairs)" : "",
+                                   sx_threads);
                 info += line;
             }
             std::snprintf(line, sizeof line, "x FFT order %d (pressure solve %.4f ms)", bxo, bx);

@@ -47,6 +47,9 @@ struct KParams {
     double dx2;
     T rhou1;
     int low_modes;  // |p|,|q| below this solve in FP64 (FP32 contexts)
+    // FP32: inverse of the mean mode's gauge-pinned system, nl x nl row-major
+    // (rows and columns: levels 1 .. NZ-2), or null
+    const double *mean_inv;
     // horizontally uniform basic state: per-level tables (BT_* rows of nz)
     int ubase_adv;  // UBAR, VBAR, WBAR, THBAR, QBAR depend on k only
     int ubase_kes;  // THBAR, QBAR, PBAR depend on k only
@@ -1251,6 +1254,32 @@ __device__ void pcr_column_f64(T2 *x, int nl, double hcol, double dx2, double si
     __syncwarp();
 }
 
+// The mean mode (p, q) = (0, 0) of an FP32 context in FP64: x = M'^-1 d with
+// the inverse of its gauge-pinned tridiagonal system (top row x = 0, as the
+// reduction above sets it) built once on the host; d = the column / size2d,
+// zero in the gauge row.  Every thread of the block calls it (it holds two
+// block barriers); x[1 .. nl] is the column, wk 2 nl doubles of shared memory.
+template <typename T2>
+__device__ void mean_mode_solve(T2 *x, int nl, const double *__restrict__ Minv, double size2d, double *wk)
+{
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x, nth = blockDim.x * blockDim.y;
+    for (int r = tid; r < nl; r += nth) {
+        const bool g = r == nl - 1;
+        wk[r] = g ? 0.0 : (double)x[r + 1].x / size2d;
+        wk[nl + r] = g ? 0.0 : (double)x[r + 1].y / size2d;
+    }
+    __syncthreads();
+    for (int w = tid; w < 2 * nl; w += nth) {
+        const int r = w % nl, part = w / nl;
+        const double *row = Minv + (size_t)r * nl, *d = wk + part * nl;
+        double s = 0.0;
+        for (int j = 0; j < nl; j++) s += row[j] * d[j];
+        if (part == 0) x[r + 1].x = (decltype(x[0].x))s;
+        else x[r + 1].y = (decltype(x[0].y))s;
+    }
+    __syncthreads();
+}
+
 // true for the low horizontal wavenumbers solved in FP64 in FP32 contexts
 template <typename T>
 __device__ __forceinline__ bool low_mode(const KParams<T> &p, long col)
@@ -1294,10 +1323,14 @@ __global__ void k_thomas(KParams<T> p, typename V2<T>::t *spec, int TC)
         if (warp == 0) {  // the low modes of this block, one after the other
             for (int c = 0; c < nc; c++) {
                 const long col = c0 + c;
-                if (!low_mode(p, col)) continue;
+                if (!low_mode(p, col) || (col == 0 && p.mean_inv)) continue;
                 pcr_column_f64(xs + (long)c * cs, p.nz - 2, p.hcoef[col], p.dx2, size2d, p.rhou_d, p.acoef_d,
                                p.ccoef_d, p.vcoef_d, col == 0, pcr_wk);
             }
+        }
+        if (c0 == 0 && p.mean_inv) {  // the mean mode: block-wide, after warp 0's reductions
+            __syncthreads();
+            mean_mode_solve(xs, p.nz - 2, p.mean_inv, size2d, pcr_wk);
         }
     }
     __syncthreads();
@@ -1359,9 +1392,14 @@ __device__ void spectral_x_body(const KParams<T> &p, typename V2<T>::t *spec, co
                 for (int w = 0; w < nis; w++) {
                     const int pp = islands[w];
                     const long col = (long)pp * p.nj + q;
+                    if (col == 0 && p.mean_inv) continue;
                     pcr_column_f64(r + (long)pp * ps - 1, nl, p.hcoef[col], p.dx2, size2d, d_r, d_a, d_c, d_v,
                                    col == 0, pcr_wk);
                 }
+            }
+            if (q == 0 && p.mean_inv) {  // the mean mode: block-wide, after warp 0's reductions
+                __syncthreads();
+                mean_mode_solve(r - 1, nl, p.mean_inv, size2d, pcr_wk);
             }
         }
     }

@@ -19,6 +19,8 @@
 #pragma once
 #include "ga_kernels.cuh"
 
+#include <cooperative_groups.h>
+
 namespace ga {
 
 constexpr int AQ_THREADS = 256;
@@ -667,6 +669,111 @@ __global__ void __launch_bounds__(PQ_THREADS)
     k_post_quad(KParams<T> p, KFields<T> F, int4 fl0, int4 fl1, T step, int cols)
 {
     post_quad_body(p, F, fl0, fl1, step, cols, (long)blockIdx.x * PQ_THREADS + threadIdx.x);
+}
+
+// ---------------------------------------------------------------------------
+// k_spectral_x_pair: the fused x transform + Thomas + inverse x transform of
+// k_spectral_x for one y-wavenumber, split over a cluster of two CTAs (FP32).
+// CTA r transforms levels l0 .. l1-1 of every x line (half the lines), then
+// solves the tridiagonal columns of x-wavenumbers p0 .. p1-1 (half the
+// columns): it gathers the other half of those columns' levels from its
+// peer's shared memory, solves them in a local buffer and writes the peer's
+// half back; after a second cluster barrier each CTA runs the inverse
+// transform of its own lines.  Per column the arithmetic is k_spectral_x's.
+// ---------------------------------------------------------------------------
+struct SxPair {
+    int ps;  // point stride of a CTA's half lines (1 mod 16 complex values)
+    int xs;  // column stride of the gathered columns (odd)
+};
+__host__ inline SxPair sx_pair_layout(int nz)
+{
+    const int nl = nz - 2, nlr = (nl + 1) / 2;
+    const int ps = nlr + ((1 - nlr % 16) % 16 + 16) % 16;
+    return SxPair{ps, nl | 1};
+}
+__host__ inline size_t sx_pair_smem(int ni, int nz)
+{
+    const SxPair L = sx_pair_layout(nz);
+    return (2 * (size_t)ni * L.ps + (size_t)((ni + 1) / 2) * L.xs) * sizeof(float2);
+}
+
+template <typename T>
+__global__ void __cluster_dims__(2, 1, 1) k_spectral_x_pair(KParams<T> p, typename V2<T>::t *spec, FftPlan pi,
+                                                           const typename V2<T>::t *tw, SxPair lay)
+{
+    static_assert(sizeof(T) == 4, "the paired x kernel is FP32");
+    namespace cg = cooperative_groups;
+    cg::cluster_group cluster = cg::this_cluster();
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ float c_r[PPM_MAXZ], c_a[PPM_MAXZ], c_c[PPM_MAXZ], c_v[PPM_MAXZ];
+    __shared__ double d_r[PPM_MAXZ], d_a[PPM_MAXZ], d_c[PPM_MAXZ], d_v[PPM_MAXZ];
+    __shared__ double pcr_wk[PCR_WK];
+    const int rank = (int)cluster.block_rank(), q = blockIdx.x / 2;
+    const int nl = p.nz - 2, ni = p.ni, ps = lay.ps, xs = lay.xs;
+    const int l0 = rank * ((nl + 1) / 2), l1 = rank ? nl : (nl + 1) / 2, nlr = l1 - l0;
+    const int ol0 = rank ? 0 : (nl + 1) / 2;  // the peer's first level
+    const int p0 = rank * ((ni + 1) / 2), p1 = rank ? ni : (ni + 1) / 2, np = p1 - p0;
+    float2 *a = (float2 *)smem_raw, *b = a + (long)ni * ps, *X = b + (long)ni * ps;
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x, nth = blockDim.x * blockDim.y;
+    for (int k = tid; k < p.nz; k += nth) {
+        c_r[k] = p.rhou[k]; c_a[k] = p.acoef[k]; c_c[k] = p.ccoef[k]; c_v[k] = p.vcoef[k];
+        d_r[k] = p.rhou_d[k]; d_a[k] = p.acoef_d[k]; d_c[k] = p.ccoef_d[k]; d_v[k] = p.vcoef_d[k];
+    }
+    // this CTA's levels of every x line
+    for (int i = threadIdx.y; i < ni; i += blockDim.y)
+        for (int l = threadIdx.x; l < nlr; l += blockDim.x)
+            cp_elem(a + i * ps + l, spec + ((long)i * p.nj + q) * p.nz + 1 + l0 + l, true);
+    cp_wait_all_sync();
+    float2 *r = fft_smem<float, float2>(a, b, nlr, pi, tw, false, ps);
+    float2 *fr = (r == a) ? b : a;  // free: the Thomas coefficients
+    cluster.sync();  // both halves transformed (both CTAs end in the same buffer)
+    float2 *pr = cluster.map_shared_rank(r, rank ^ 1);
+    // gather the columns p0 .. p1-1: own levels locally, the peer's from its shared memory
+    for (int w = tid; w < np * nl; w += nth) {
+        const int pc = w / nl, l = w % nl, pp = p0 + pc;
+        const bool own = l >= l0 && l < l1;
+        X[pc * xs + l] = own ? r[pp * ps + (l - l0)] : pr[pp * ps + (l - ol0)];
+    }
+    __syncthreads();
+    const double size2d = (double)(ni * p.nj);
+    const int aq = min(q, p.nj - q);
+    const bool q_low = p.low_modes > 0 && aq < p.low_modes;
+    {
+        const float dx2 = (float)p.dx2, inv_s = (float)(1.0 / size2d);
+        for (int pc = tid; pc < np; pc += nth) {
+            const int pp = p0 + pc, ap = min(pp, ni - pp);
+            if (q_low && ap < p.low_modes) continue;  // FP64 islands below
+            const long col = (long)pp * p.nj + q;
+            const float hb = 2.0f * (float)p.hcoef[col] / dx2;
+            float *Fw = (float *)fr + (long)pc * xs - 1;  // nl floats per column
+            thomas_column_fast(X + (long)pc * xs - 1, Fw, p.nz, hb, inv_s, c_r, c_a, c_c, c_v, col == 0);
+        }
+        if (q_low && (tid >> 5) == 0) {  // low (p, q) wavenumbers of this CTA: FP64 by warp PCR
+            for (int pc = 0; pc < np; pc++) {
+                const int pp = p0 + pc, ap = min(pp, ni - pp);
+                if (ap >= p.low_modes) continue;
+                const long col = (long)pp * p.nj + q;
+                if (col == 0 && p.mean_inv) continue;
+                pcr_column_f64(X + (long)pc * xs - 1, nl, p.hcoef[col], p.dx2, size2d, d_r, d_a, d_c, d_v,
+                               col == 0, pcr_wk);
+            }
+        }
+        if (q_low && q == 0 && p0 == 0 && p.mean_inv) {  // the mean mode: block-wide
+            __syncthreads();
+            mean_mode_solve(X - 1, nl, p.mean_inv, size2d, pcr_wk);
+        }
+    }
+    __syncthreads();
+    // the solved columns back to both CTAs' lines
+    for (int w = tid; w < np * nl; w += nth) {
+        const int pc = w / nl, l = w % nl, pp = p0 + pc;
+        if (l >= l0 && l < l1) r[pp * ps + (l - l0)] = X[pc * xs + l];
+        else pr[pp * ps + (l - ol0)] = X[pc * xs + l];
+    }
+    cluster.sync();  // every column written back
+    float2 *o = fft_smem<float, float2>(r, fr, nlr, pi, tw, true, ps);
+    for (int i = threadIdx.y; i < ni; i += blockDim.y)
+        for (int l = threadIdx.x; l < nlr; l += blockDim.x) spec[((long)i * p.nj + q) * p.nz + 1 + l0 + l] = o[i * ps + l];
 }
 
 }  // namespace ga

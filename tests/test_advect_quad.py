@@ -131,3 +131,25 @@ def test_post_quad_matches_column_kernel(monkeypatch, case):
         for slot in ((abi.GA_SLOT_CUR, abi.GA_SLOT_M) if f < nprog else (abi.GA_SLOT_CUR,)):
             a, b = (m.get(f, slot) for m in ms)
             np.testing.assert_array_equal(b, a, err_msg=f"{case} field {f} slot {slot}")
+
+
+@pytest.mark.parametrize("case", ["thunderstorm_small", "moist_blob_odd"])
+def test_spectral_x_pair_matches_single_cta(monkeypatch, case):
+    """the fused x kernel as CTA pairs (GA_SPECTRAL_X=pair) against one CTA
+    per y-wavenumber: whole steps bit for bit (an odd interior size splits
+    the lines and the columns unevenly)"""
+    if case == "thunderstorm_small":
+        wl = configs.thunderstorm(nx=44, ny=38, nsteps=4)
+    else:
+        wl = configs.moist_blob(nx=31, ny=27, nz=17, nsteps=4)
+    ms = []
+    for mode in ("single", "pair"):
+        monkeypatch.setenv("GA_SPECTRAL_X", mode)
+        ms.append(anelastic.Model(wl, abi.GA_PREC_F32))
+    monkeypatch.delenv("GA_SPECTRAL_X")
+    for m in ms:
+        m.step(wl.nsteps)
+    nprog = 7 if wl.microphysics_option else 4
+    for f in list(range(nprog)) + [abi.GA_PI]:
+        a, b = (m.get(f) for m in ms)
+        np.testing.assert_array_equal(b, a, err_msg=f"{case} field {f}")
