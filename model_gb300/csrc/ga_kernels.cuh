@@ -1280,6 +1280,30 @@ __device__ void mean_mode_solve(T2 *x, int nl, const double *__restrict__ Minv, 
     __syncthreads();
 }
 
+// The adjoint of mean_mode_solve: z = (M'^T)^-1 d = (M'^-1)^T d with d = the
+// column / size2d in every row, then z_top = 0 (the transposed gauge).  Block-
+// wide as mean_mode_solve.
+template <typename T2>
+__device__ void mean_mode_solve_T(T2 *x, int nl, const double *__restrict__ Minv, double size2d, double *wk)
+{
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x, nth = blockDim.x * blockDim.y;
+    for (int r = tid; r < nl; r += nth) {
+        wk[r] = (double)x[r + 1].x / size2d;
+        wk[nl + r] = (double)x[r + 1].y / size2d;
+    }
+    __syncthreads();
+    for (int w = tid; w < 2 * nl; w += nth) {
+        const int r = w % nl, part = w / nl;
+        const double *d = wk + part * nl;
+        double s = 0.0;
+        for (int j = 0; j < nl; j++) s += Minv[(size_t)j * nl + r] * d[j];
+        if (r == nl - 1) s = 0.0;
+        if (part == 0) x[r + 1].x = (decltype(x[0].x))s;
+        else x[r + 1].y = (decltype(x[0].y))s;
+    }
+    __syncthreads();
+}
+
 // true for the low horizontal wavenumbers solved in FP64 in FP32 contexts
 template <typename T>
 __device__ __forceinline__ bool low_mode(const KParams<T> &p, long col)

@@ -1041,6 +1041,9 @@ __global__ void k_adj_fft_y_in(KParams<T> p, const T *pib, typename V2<T>::t *sp
     const int k0 = 1 + blockIdx.x * KT;
     const int kt = min(KT, nz - 1 - k0);
     const bool ii = i >= 1 && i <= nx - 2;
+    // several rows in flight per thread: the loads of a row do not wait for
+    // the previous row's store
+#pragma unroll 4
     for (int q = threadIdx.y; q < p.nj; q += blockDim.y)
         for (int l = threadIdx.x; l < KT; l += blockDim.x) {
             T2 v;
@@ -1266,7 +1269,8 @@ __global__ void k_spectral_x_adj(KParams<T> p, typename V2<T>::t *spec, FftPlan 
             thomas_T_column_fast((float2 *)(r + (long)pp * ps - 1), Fw, p.nz, hb, inv_s, (const float *)c_r,
                                  (const float *)c_a, (const float *)c_c, (const float *)c_v);
         }
-        if (q == 0 && tid < 32)
+        if (q == 0 && p.mean_inv) mean_mode_solve_T(r - 1, nl, p.mean_inv, size2d, pcr_wk);  // block-wide
+        else if (q == 0 && tid < 32)
             pcr_column_T_f64(r - 1, nl, p.hcoef[0], p.dx2, size2d, d_r, d_a, d_c, d_v, pcr_wk);
     }
     __syncthreads();
@@ -1293,8 +1297,10 @@ __global__ void k_thomas_adj(KParams<T> p, typename V2<T>::t *spec, int TC)
     for (int w = threadIdx.x; w < nc * p.nz; w += blockDim.x) cp_elem(xs + (w / p.nz) * cs + w % p.nz, g + w, true);
     cp_wait_all_sync();
     const double inv_s = 1.0 / (double)(p.ni * p.nj);
+    const bool mean_block = sizeof(T) != 8 && c0 == 0 && p.mean_inv;  // the mean mode, block-wide below
     for (int c = threadIdx.x; c < nc; c += blockDim.x) {
         const long col = c0 + c;
+        if (col == 0 && mean_block) continue;
         if (sizeof(T) == 8 || col == 0) {
             double Floc[PPM_MAXZ];
             thomas_T_column<T2, double>(xs + (long)c * cs, Floc, p.nz, 2.0 * p.hcoef[col] / p.dx2, inv_s, p.rhou_d,
@@ -1303,6 +1309,10 @@ __global__ void k_thomas_adj(KParams<T> p, typename V2<T>::t *spec, int TC)
             thomas_T_column<T2, T>(xs + (long)c * cs, fs + (long)c * cs, p.nz, (T)(2.0 * p.hcoef[col] / p.dx2),
                                    (T)inv_s, p.rhou, p.acoef, p.ccoef, p.vcoef, false);
         }
+    }
+    if (mean_block) {
+        __shared__ double mwk[2 * PPM_MAXZ];
+        mean_mode_solve_T(xs, p.nz - 2, p.mean_inv, (double)(p.ni * p.nj), mwk);
     }
     __syncthreads();
     for (int w = threadIdx.x; w < nc * p.nz; w += blockDim.x) g[w] = xs[(w / p.nz) * cs + w % p.nz];
