@@ -105,6 +105,7 @@ class Engine : public EngineBase {
     // and its tile; GA_ADVECT=tile or =quad restricts both the default and the
     // autotuner to one kernel
     int adv_quad = 1, adv_qi = 4, adv_qj = 8, adv_force = 0;
+    int adv_qb = 3;  // blocks per SM the four-level kernel's registers are sized for (3 or 4)
     // the four-level post-processing kernel (FP32, NZ % 4 == 0); GA_POST=column
     // keeps the per-level one
     bool post_quad = true;
@@ -325,6 +326,7 @@ class Engine : public EngineBase {
             else if (!std::strcmp(ev, "quad")) adv_force = 2;
         }
         adv_quad = adv_force != 1;
+        if (const char *ev = std::getenv("GA_ADVECT_BLOCKS")) adv_qb = std::atoi(ev) == 4 ? 4 : 3;
         if (const char *ev = std::getenv("GA_POST")) post_quad = std::strcmp(ev, "column") != 0;
         post_quad = post_quad && sizeof(T) == 4 && NZ % 4 == 0;
         if constexpr (sizeof(T) == 4) {
@@ -532,14 +534,16 @@ class Engine : public EngineBase {
     {
         if constexpr (sizeof(T) == 4) {
             dim3 grid(cdiv(NX - 6, TI), cdiv(NY - 6, TJ));
-            k_advect_quad<TI, TJ><<<grid, AQ_THREADS, advect_quad_smem(TI, TJ, NZ), stream>>>(kp, fields(), step,
-                                                                                            sdtg, what);
+            const size_t sm = advect_quad_smem(TI, TJ, NZ);
+            if (adv_qb == 4) k_advect_quad<TI, TJ, 4><<<grid, AQ_THREADS, sm, stream>>>(kp, fields(), step, sdtg, what);
+            else k_advect_quad<TI, TJ, 3><<<grid, AQ_THREADS, sm, stream>>>(kp, fields(), step, sdtg, what);
         }
     }
     template <int TI, int TJ>
     static void quad_attr_t(int optin)
     {
-        cudaFuncSetAttribute(k_advect_quad<TI, TJ>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+        cudaFuncSetAttribute(k_advect_quad<TI, TJ, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+        cudaFuncSetAttribute(k_advect_quad<TI, TJ, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
     }
     static void quad_attr(int ti, int tj, int optin)
     {
@@ -884,7 +888,7 @@ class Engine : public EngineBase {
         // advection tile
         {
             float best = 1e30f;
-            int bi = adv_ti, bj = adv_tj, bq = 0, qi = adv_qi, qj = adv_qj;
+            int bi = adv_ti, bj = adv_tj, bq = 0, qi = adv_qi, qj = adv_qj, qb = adv_qb;
             if (adv_force != 2 || !quad_ok(adv_qi, adv_qj)) {
                 adv_quad = 0;
                 for (auto &tl : kAdvTiles) {
@@ -899,14 +903,18 @@ class Engine : public EngineBase {
                 adv_quad = 1;
                 for (auto &tl : kQuadTiles) {
                     if (!quad_ok(tl[0], tl[1])) continue;
-                    adv_qi = tl[0]; adv_qj = tl[1];
-                    const float t = timeit([&] { advect(1. / 3., what); });
-                    if (t < best) { best = t; bq = 1; qi = tl[0]; qj = tl[1]; }
+                    for (int mb = 3; mb <= 4; mb++) {
+                        adv_qi = tl[0]; adv_qj = tl[1]; adv_qb = mb;
+                        const float t = timeit([&] { advect(1. / 3., what); });
+                        if (t < best) { best = t; bq = 1; qi = tl[0]; qj = tl[1]; qb = mb; }
+                    }
                 }
             }
-            adv_ti = bi; adv_tj = bj; adv_quad = bq; adv_qi = qi; adv_qj = qj;
+            adv_ti = bi; adv_tj = bj; adv_quad = bq; adv_qi = qi; adv_qj = qj; adv_qb = qb;
             smem_adv = advect_tile_smem(bi, bj, NZ, sizeof(T));
-            if (bq) std::snprintf(line, sizeof line, "advect tile %dx%d, four levels per thread (%.4f ms); ", qi, qj, best);
+            if (bq)
+                std::snprintf(line, sizeof line, "advect tile %dx%d, four levels per thread, %d blocks/SM (%.4f ms); ",
+                              qi, qj, qb, best);
             else std::snprintf(line, sizeof line, "advect tile %dx%d (%.4f ms); ", bi, bj, best);
             info += line;
         }

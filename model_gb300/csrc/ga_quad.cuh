@@ -548,8 +548,9 @@ __device__ __forceinline__ void advect_quad_body(const KParams<float> &p, const 
     }
 }
 
-template <int TI, int TJ>
-__global__ void __launch_bounds__(AQ_THREADS, 3)
+// MB: blocks per SM the registers are sized for (3: 80 registers, 4: 64)
+template <int TI, int TJ, int MB>
+__global__ void __launch_bounds__(AQ_THREADS, MB)
     k_advect_quad(KParams<float> p, KFields<float> F, float step, float sdtg, int what)
 {
     advect_quad_body<TI, TJ>(p, F, blockIdx.x, blockIdx.y, step, sdtg, what);

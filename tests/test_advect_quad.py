@@ -28,12 +28,16 @@ def _built():
     build.build()
 
 
-def _pair(monkeypatch, wl):
+def _pair(monkeypatch, wl, blocks=3):
+    """a per-level tile context and a four-level one whose registers are
+    sized for `blocks` blocks per SM"""
     ms = []
     for mode in ("tile", "quad"):
         monkeypatch.setenv("GA_ADVECT", mode)
+        monkeypatch.setenv("GA_ADVECT_BLOCKS", str(blocks))
         ms.append(anelastic.Model(wl, abi.GA_PREC_F32))
     monkeypatch.delenv("GA_ADVECT")
+    monkeypatch.delenv("GA_ADVECT_BLOCKS")
     return ms
 
 
@@ -53,13 +57,14 @@ def _perturb(ms, wl, seed):
                 m.set(f, slot, x)
 
 
+@pytest.mark.parametrize("blocks", [3, 4])
 @pytest.mark.parametrize("case", ["moist_rf1", "moist_rf2", "dry"])
-def test_single_advection_operator_bit_identical(monkeypatch, case):
+def test_single_advection_operator_bit_identical(monkeypatch, case, blocks):
     if case == "dry":
         wl = configs.dry_bubble(nx=30, ny=26, nz=20, nsteps=2)
     else:
         wl = configs.moist_blob(nx=30, ny=26, nz=16, rain_fallout=1 if case == "moist_rf1" else 2)
-    ms = _pair(monkeypatch, wl)
+    ms = _pair(monkeypatch, wl, blocks)
     _perturb(ms, wl, 11)
     for op, fields in ADVECT_OPS.items():
         if op == "advect_micro" and not wl.microphysics_option:
@@ -71,8 +76,9 @@ def test_single_advection_operator_bit_identical(monkeypatch, case):
             np.testing.assert_array_equal(b, a, err_msg=f"{case} {op} field {abi.PROG_NAMES[f]}")
 
 
+@pytest.mark.parametrize("blocks", [3, 4])
 @pytest.mark.parametrize("case", ["moist_blob", "thunderstorm_small", "dry_bubble", "nz_not_multiple_of_4"])
-def test_steps_match_tile_kernel(monkeypatch, case):
+def test_steps_match_tile_kernel(monkeypatch, case, blocks):
     if case == "moist_blob":
         wl = configs.moist_blob(nx=30, ny=26, nz=16, nsteps=6)
     elif case == "thunderstorm_small":
@@ -81,7 +87,7 @@ def test_steps_match_tile_kernel(monkeypatch, case):
         wl = configs.dry_bubble(nx=34, ny=30, nz=20, nsteps=6)
     else:  # falls back to the tile kernel: both contexts run the same code
         wl = configs.moist_blob(nx=30, ny=26, nz=18, nsteps=6)
-    ms = _pair(monkeypatch, wl)
+    ms = _pair(monkeypatch, wl, blocks)
     for m in ms:
         m.step(wl.nsteps)
     nprog = 7 if wl.microphysics_option else 4
