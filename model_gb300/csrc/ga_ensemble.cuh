@@ -57,8 +57,8 @@ __global__ void __launch_bounds__(256) kb_advect(const KParams<T> *P, const KFie
 }
 
 // FP32 members with whole level quads: the four-level advection and post
-template <typename T, int TI, int TJ>
-__global__ void __launch_bounds__(AQ_THREADS, 3) kb_advect_quad(const KParams<T> *P, const KFields<T> *F,
+template <typename T, int TI, int TJ, int MB>
+__global__ void __launch_bounds__(AQ_THREADS, MB) kb_advect_quad(const KParams<T> *P, const KFields<T> *F,
                                                                const long *pre, int nmem, double step, int what)
 {
     static_assert(sizeof(T) == 4, "four-level kernels are FP32");
@@ -190,7 +190,7 @@ class Ensemble : public EnsembleBase {
     // four-level advection (tile adv_qi x adv_qj) while every basic state is
     // a function of height and adv_quad is set (autotuned)
     bool quad = false, adv_quad = true;
-    int adv_qi = 4, adv_qj = 8;
+    int adv_qi = 4, adv_qj = 8, adv_qb = 3;  // quad tile, blocks per SM of its register budget
     int sx_threads = 256;  // threads of a fused spectral-x block (autotuned)
     int nsm = 0;
     bool adv_quad_now = false;  // the choice build_prefixes made (prefixes and launches agree)
@@ -244,11 +244,16 @@ class Ensemble : public EnsembleBase {
         if constexpr (sizeof(T) == 4) {
             quad = true;
             for (auto *e : mem) quad = quad && e->NZ % 4 == 0;
-            cudaFuncSetAttribute(kb_advect_quad<T, 4, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
-            cudaFuncSetAttribute(kb_advect_quad<T, 4, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
-            cudaFuncSetAttribute(kb_advect_quad<T, 8, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
-            cudaFuncSetAttribute(kb_advect_quad<T, 2, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
-            cudaFuncSetAttribute(kb_advect_quad<T, 8, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+            cudaFuncSetAttribute(kb_advect_quad<T, 4, 4, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+            cudaFuncSetAttribute(kb_advect_quad<T, 4, 4, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+            cudaFuncSetAttribute(kb_advect_quad<T, 4, 8, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+            cudaFuncSetAttribute(kb_advect_quad<T, 4, 8, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+            cudaFuncSetAttribute(kb_advect_quad<T, 8, 4, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+            cudaFuncSetAttribute(kb_advect_quad<T, 8, 4, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+            cudaFuncSetAttribute(kb_advect_quad<T, 2, 8, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+            cudaFuncSetAttribute(kb_advect_quad<T, 2, 8, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+            cudaFuncSetAttribute(kb_advect_quad<T, 8, 8, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+            cudaFuncSetAttribute(kb_advect_quad<T, 8, 8, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
         }
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
         build_prefixes();
@@ -271,15 +276,28 @@ class Ensemble : public EnsembleBase {
         if (stream) cudaStreamDestroy(stream);
     }
 
+    // the batched four-level advection of tile TI x TJ in the chosen register budget
+    template <int TI, int TJ>
+    const void *quad_fn() const
+    {
+        if (adv_qb == 4) return (const void *)kb_advect_quad<T, TI, TJ, 4>;
+        return (const void *)kb_advect_quad<T, TI, TJ, 3>;
+    }
+    template <int TI, int TJ>
+    void launch_quad(dim3 g, size_t sm, const long *pr, const KFields<T> *F, double st, int what)
+    {
+        if (adv_qb == 4) kb_advect_quad<T, TI, TJ, 4><<<g, AQ_THREADS, sm, stream>>>(d_p, F, pr, nmem, st, what);
+        else kb_advect_quad<T, TI, TJ, 3><<<g, AQ_THREADS, sm, stream>>>(d_p, F, pr, nmem, st, what);
+    }
     const void *advect_fn() const
     {
         if constexpr (sizeof(T) == 4) {
             if (use_adv_quad()) {
-                if (adv_qi == 4 && adv_qj == 4) return (const void *)kb_advect_quad<T, 4, 4>;
-                if (adv_qi == 8 && adv_qj == 4) return (const void *)kb_advect_quad<T, 8, 4>;
-                if (adv_qi == 2) return (const void *)kb_advect_quad<T, 2, 8>;
-                if (adv_qi == 8) return (const void *)kb_advect_quad<T, 8, 8>;
-                return (const void *)kb_advect_quad<T, 4, 8>;
+                if (adv_qi == 4 && adv_qj == 4) return quad_fn<4, 4>();
+                if (adv_qi == 8 && adv_qj == 4) return quad_fn<8, 4>();
+                if (adv_qi == 2) return quad_fn<2, 8>();
+                if (adv_qi == 8) return quad_fn<8, 8>();
+                return quad_fn<4, 8>();
             }
         }
         if (adv_ti == 2) return (const void *)kb_advect<T, 2, 4>;
@@ -295,11 +313,11 @@ class Ensemble : public EnsembleBase {
         const long *pr = d_pre[EK_ADV];
         if constexpr (sizeof(T) == 4) {
             if (use_adv_quad()) {
-                if (adv_qi == 4 && adv_qj == 4) kb_advect_quad<T, 4, 4><<<g, AQ_THREADS, sm, stream>>>(d_p, F, pr, nmem, st, what);
-                else if (adv_qi == 8 && adv_qj == 4) kb_advect_quad<T, 8, 4><<<g, AQ_THREADS, sm, stream>>>(d_p, F, pr, nmem, st, what);
-                else if (adv_qi == 2) kb_advect_quad<T, 2, 8><<<g, AQ_THREADS, sm, stream>>>(d_p, F, pr, nmem, st, what);
-                else if (adv_qi == 8) kb_advect_quad<T, 8, 8><<<g, AQ_THREADS, sm, stream>>>(d_p, F, pr, nmem, st, what);
-                else kb_advect_quad<T, 4, 8><<<g, AQ_THREADS, sm, stream>>>(d_p, F, pr, nmem, st, what);
+                if (adv_qi == 4 && adv_qj == 4) launch_quad<4, 4>(g, sm, pr, F, st, what);
+                else if (adv_qi == 8 && adv_qj == 4) launch_quad<8, 4>(g, sm, pr, F, st, what);
+                else if (adv_qi == 2) launch_quad<2, 8>(g, sm, pr, F, st, what);
+                else if (adv_qi == 8) launch_quad<8, 8>(g, sm, pr, F, st, what);
+                else launch_quad<4, 8>(g, sm, pr, F, st, what);
                 return;
             }
         }
@@ -437,7 +455,7 @@ class Ensemble : public EnsembleBase {
         char line[160];
         {
             float best = 1e30f;
-            int bi = adv_ti, bj = adv_tj, qi = adv_qi, qj = adv_qj;
+            int bi = adv_ti, bj = adv_tj, qi = adv_qi, qj = adv_qj, qb = adv_qb;
             bool bq = false;
             adv_quad = false;
             for (auto &tl : Engine<T>::kAdvTiles) {
@@ -453,12 +471,15 @@ class Ensemble : public EnsembleBase {
             if (quad) {
                 adv_quad = true;
                 for (auto &tl : Engine<T>::kQuadTiles) {
-                    adv_qi = tl[0];
-                    adv_qj = tl[1];
-                    if (!quad_applies()) continue;
-                    build_prefixes();
-                    const float t = timeit([&] { launch_advect(F, 1. / 3., what); });
-                    if (t < best) { best = t; bq = true; qi = tl[0]; qj = tl[1]; }
+                    for (int mb = 3; mb <= 4; mb++) {
+                        adv_qi = tl[0];
+                        adv_qj = tl[1];
+                        adv_qb = mb;
+                        if (!quad_applies()) continue;
+                        build_prefixes();
+                        const float t = timeit([&] { launch_advect(F, 1. / 3., what); });
+                        if (t < best) { best = t; bq = true; qi = tl[0]; qj = tl[1]; qb = mb; }
+                    }
                 }
             }
             adv_ti = bi;
@@ -466,8 +487,11 @@ class Ensemble : public EnsembleBase {
             adv_quad = bq;
             adv_qi = qi;
             adv_qj = qj;
+            adv_qb = qb;
             build_prefixes();
-            if (bq) std::snprintf(line, sizeof line, "advect tile %dx%d, four levels per thread (%.3f ms); ", qi, qj, best);
+            if (bq)
+                std::snprintf(line, sizeof line, "advect tile %dx%d, four levels per thread, %d blocks/SM (%.3f ms); ", qi,
+                              qj, qb, best);
             else std::snprintf(line, sizeof line, "advect tile %dx%d (%.3f ms); ", bi, bj, best);
             info += line;
         }
