@@ -364,11 +364,33 @@ __global__ void __launch_bounds__(AJ_THREADS, 3)
     const int pi = i0 + li, pj = j0 + lj, pk0 = k0 + 4 * lq;
     if (pi >= p.nx || pj >= ny || pk0 >= nz) return;
     const int c = gix(ny, nz, pi, pj, pk0);
-    constexpr int NG = G == 0 ? 4 : 6;
     constexpr int GF[2][6] = {{FU, FV, FW, FTH, -1, -1}, {FU, FV, FW, FQV, FQC, FQR}};
+    // the fold and the gathered sums of field g from its loaded quads
+    auto finish = [&](int g, Q4 cur, const Q4 &m0, const Q4 &pv) {
+        const int f = GF[G][g];
+        const bool mine = G == 0 || f >= FQV;  // fields this group folds and replaces
+        if (mine) {
+            Q4 m = m0;
+            bool any = false;
+#pragma unroll
+            for (int e = 0; e < 4; e++) {
+                if (adv_cell(p, pi, pj, pk0 + e, f == FW ? 2 : 1)) {
+                    m.v[e] += pv.v[e];
+                    any = true;
+                }
+            }
+            if (any) stg4(A.M[f] + c, m);
+        }
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+            const bool cell = adv_cell(p, pi, pj, pk0 + e, f == FW ? 2 : 1);
+            if (mine && zero_cur && cell) cur.v[e] = acc[e][f];
+            else if (acc[e][f] != 0.f) cur.v[e] += acc[e][f];
+        }
+        stg4(A.cur[f] + c, cur);
+    };
     // buoyancy of w into theta (group 0) and the moisture loading (group 1)
-    {
-        const Q4 w4 = ldg4(A.P[FW], c);
+    auto buoyancy = [&](const Q4 &w4) {
         const float w5 = pk0 + 4 < nz ? A.P[FW][c + 4] : 0.f;
         const float wv[5] = {w4.v[0], w4.v[1], w4.v[2], w4.v[3], w5};
 #pragma unroll
@@ -387,32 +409,44 @@ __global__ void __launch_bounds__(AJ_THREADS, 3)
                 }
             }
         }
-    }
+    };
+    // every load of a batch of fields before its first store (a store would
+    // otherwise order the later loads after it): group 0 in one batch, group 1
+    // as u, v, w (sums only) and then qv, qc, qr
+    if (G == 0) {
+        Q4 cu[4], mm[4], pp[4];
 #pragma unroll
-    for (int g = 0; g < NG; g++) {
-        const int f = GF[G][g];
-        const bool mine = G == 0 || f >= FQV;  // fields this group folds and replaces
-        Q4 cur = ldg4(A.cur[f], c);
-        if (mine) {
-            Q4 mm = ldg4(A.M[f], c);
-            const Q4 pp = ldg4(A.P[f], c);
-            bool any = false;
+        for (int g = 0; g < 4; g++) {
+            const int f = GF[G][g];
+            cu[g] = ldg4(A.cur[f], c);
+            mm[g] = ldg4(A.M[f], c);
+            pp[g] = ldg4(A.P[f], c);
+        }
+        buoyancy(pp[2]);
 #pragma unroll
-            for (int e = 0; e < 4; e++) {
-                if (adv_cell(p, pi, pj, pk0 + e, f == FW ? 2 : 1)) {
-                    mm.v[e] += pp.v[e];
-                    any = true;
-                }
+        for (int g = 0; g < 4; g++) finish(g, cu[g], mm[g], pp[g]);
+    } else {
+        const Q4 z4{{0.f, 0.f, 0.f, 0.f}};
+        {
+            Q4 cu[3];
+#pragma unroll
+            for (int g = 0; g < 3; g++) cu[g] = ldg4(A.cur[GF[G][g]], c);
+            buoyancy(ldg4(A.P[FW], c));
+#pragma unroll
+            for (int g = 0; g < 3; g++) finish(g, cu[g], z4, z4);
+        }
+        {
+            Q4 cu[3], mm[3], pp[3];
+#pragma unroll
+            for (int g = 0; g < 3; g++) {
+                const int f = GF[G][3 + g];
+                cu[g] = ldg4(A.cur[f], c);
+                mm[g] = ldg4(A.M[f], c);
+                pp[g] = ldg4(A.P[f], c);
             }
-            if (any) stg4(A.M[f] + c, mm);
-        }
 #pragma unroll
-        for (int e = 0; e < 4; e++) {
-            const bool cell = adv_cell(p, pi, pj, pk0 + e, f == FW ? 2 : 1);
-            if (mine && zero_cur && cell) cur.v[e] = acc[e][f];
-            else if (acc[e][f] != 0.f) cur.v[e] += acc[e][f];
+            for (int g = 0; g < 3; g++) finish(3 + g, cu[g], mm[g], pp[g]);
         }
-        stg4(A.cur[f] + c, cur);
     }
     if (G == 0 && (pi == 0 || pi == p.nx - 1 || pj == 0 || pj == ny - 1)) {
 #pragma unroll
