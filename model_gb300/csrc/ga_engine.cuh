@@ -824,9 +824,13 @@ class Engine : public EngineBase {
                     cudaMemcpyAsync(rec + (size_t)(nprog * s + f) * N, buf[f][ci[f]], N * sizeof(T),
                                     cudaMemcpyDeviceToDevice, stream);
             qmask = mrec ? mrec + (size_t)s * N : nullptr;
-            advect(st, ADV_UV | ADV_WB | ADV_TH | (moist ? (ADV_Q | ADV_ZERO) : 0));
+            // the four-level advection launch also makes the mirror copies of
+            // the pressure solve (they touch no point the advection writes)
+            const bool fuse_mirror = !kp.periodic && adv_quad && quad_ok(adv_qi, adv_qj);
+            advect(st, ADV_UV | ADV_WB | ADV_TH | (moist ? (ADV_Q | ADV_ZERO) : 0) | (fuse_mirror ? ADV_MIRROR : 0));
             qmask = nullptr;
-            solve_pressure(st);
+            if (fuse_mirror) poisson(st);
+            else solve_pressure(st);
             int fl[7] = {0, 0, 0, 0, 0, 0, 0};
             fl[FU] = fl[FV] = fl[FW] = PF_PROJECT | PF_SPONGE | PF_VBC;
             fl[FTH] = PF_SPONGE | PF_VBC;

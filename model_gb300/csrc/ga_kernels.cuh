@@ -354,7 +354,10 @@ __device__ T s_tend(const KParams<T> &p, const KFields<T> &F, const T *s, const 
 // advect_microphysics_cell, optionally zero_moisture on the written points.
 // One thread per interior point [3,NX-3) x [3,NY-3) x [1,NZ-1).
 // ---------------------------------------------------------------------------
-enum { ADV_UV = 1, ADV_WB = 2, ADV_TH = 4, ADV_Q = 8, ADV_ZERO = 16 };
+// ADV_MIRROR (four-level kernel, non-periodic): the launch also makes the
+// lateral mirror copies of P u, v, w that precede the pressure solve; they read
+// and write only points the advection does not write
+enum { ADV_UV = 1, ADV_WB = 2, ADV_TH = 4, ADV_Q = 8, ADV_ZERO = 16, ADV_MIRROR = 32 };
 
 template <typename T>
 __global__ void __launch_bounds__(128) k_advect(KParams<T> p, KFields<T> F, T step, T sdtg, int what)

@@ -553,6 +553,12 @@ template <int TI, int TJ, int MB>
 __global__ void __launch_bounds__(AQ_THREADS, MB)
     k_advect_quad(KParams<float> p, KFields<float> F, float step, float sdtg, int what)
 {
+    if (what & ADV_MIRROR) {  // mirror copies (edge points from non-advected ones), grid-stride
+        const long nt = (long)gridDim.x * gridDim.y * AQ_THREADS;
+        const long ntot = 2L * (p.nx + p.ny - 2) * (p.nz - 2);
+        for (long t = ((long)blockIdx.y * gridDim.x + blockIdx.x) * AQ_THREADS + threadIdx.x; t < ntot; t += nt)
+            mirror_edges_body(p, F.P[FU], F.P[FV], F.P[FW], t);
+    }
     advect_quad_body<TI, TJ>(p, F, blockIdx.x, blockIdx.y, step, sdtg, what);
 }
 
