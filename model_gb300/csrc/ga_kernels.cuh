@@ -1257,6 +1257,38 @@ __device__ void pcr_column_f64(T2 *x, int nl, double hcol, double dx2, double si
     __syncwarp();
 }
 
+// x[r+1] = sum_j A[r][j] d[j] for the real (d = wk) and imaginary (d = wk + nl)
+// parts, A = Minv or (TRANS) its transpose, the last row zero when TRANS.  Four
+// lanes share an output (columns j = g, g+4, ...) and add their partial sums by
+// shuffles; only the block's full warps take part.
+template <bool TRANS, typename T2>
+__device__ __forceinline__ void mean_mode_products(T2 *x, int nl, const double *__restrict__ Minv, const double *wk)
+{
+    constexpr int GL = 4;
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x, nth = blockDim.x * blockDim.y;
+    const int nfull = nth & ~31, nout = 2 * nl;
+    if (tid >= nfull) return;
+    for (int base = 0; base < nout * GL; base += nfull) {
+        const int w = base + tid, o = w / GL, g = w % GL;
+        double s = 0.0;
+        int r = 0, part = 0;
+        if (o < nout) {
+            r = o % nl;
+            part = o / nl;
+            const double *d = wk + part * nl;
+            for (int j = g; j < nl; j += GL)
+                s += (TRANS ? Minv[(size_t)j * nl + r] : Minv[(size_t)r * nl + j]) * d[j];
+        }
+        s += __shfl_down_sync(0xffffffffu, s, 2, GL);
+        s += __shfl_down_sync(0xffffffffu, s, 1, GL);
+        if (o < nout && g == 0) {
+            if (TRANS && r == nl - 1) s = 0.0;
+            if (part == 0) x[r + 1].x = (decltype(x[0].x))s;
+            else x[r + 1].y = (decltype(x[0].y))s;
+        }
+    }
+}
+
 // The mean mode (p, q) = (0, 0) of an FP32 context in FP64: x = M'^-1 d with
 // the inverse of its gauge-pinned tridiagonal system (top row x = 0, as the
 // reduction above sets it) built once on the host; d = the column / size2d,
@@ -1272,14 +1304,7 @@ __device__ void mean_mode_solve(T2 *x, int nl, const double *__restrict__ Minv, 
         wk[nl + r] = g ? 0.0 : (double)x[r + 1].y / size2d;
     }
     __syncthreads();
-    for (int w = tid; w < 2 * nl; w += nth) {
-        const int r = w % nl, part = w / nl;
-        const double *row = Minv + (size_t)r * nl, *d = wk + part * nl;
-        double s = 0.0;
-        for (int j = 0; j < nl; j++) s += row[j] * d[j];
-        if (part == 0) x[r + 1].x = (decltype(x[0].x))s;
-        else x[r + 1].y = (decltype(x[0].y))s;
-    }
+    mean_mode_products<false>(x, nl, Minv, wk);
     __syncthreads();
 }
 
@@ -1295,15 +1320,7 @@ __device__ void mean_mode_solve_T(T2 *x, int nl, const double *__restrict__ Minv
         wk[nl + r] = (double)x[r + 1].y / size2d;
     }
     __syncthreads();
-    for (int w = tid; w < 2 * nl; w += nth) {
-        const int r = w % nl, part = w / nl;
-        const double *d = wk + part * nl;
-        double s = 0.0;
-        for (int j = 0; j < nl; j++) s += Minv[(size_t)j * nl + r] * d[j];
-        if (r == nl - 1) s = 0.0;
-        if (part == 0) x[r + 1].x = (decltype(x[0].x))s;
-        else x[r + 1].y = (decltype(x[0].y))s;
-    }
+    mean_mode_products<true>(x, nl, Minv, wk);
     __syncthreads();
 }
 
