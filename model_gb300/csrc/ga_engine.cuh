@@ -327,6 +327,12 @@ class Engine : public EngineBase {
         }
         adv_quad = adv_force != 1;
         if (const char *ev = std::getenv("GA_ADVECT_BLOCKS")) adv_qb = std::atoi(ev) == 4 ? 4 : 3;
+        if (const char *ev = std::getenv("GA_ADVECT_TILE")) {  // default four-level tile, "TIxTJ"
+            int a = 0, b = 0;
+            if (std::sscanf(ev, "%dx%d", &a, &b) == 2)
+                for (auto &tl : kQuadTiles)
+                    if (tl[0] == a && tl[1] == b) { adv_qi = a; adv_qj = b; }
+        }
         if (const char *ev = std::getenv("GA_POST")) post_quad = std::strcmp(ev, "column") != 0;
         post_quad = post_quad && sizeof(T) == 4 && NZ % 4 == 0;
         if constexpr (sizeof(T) == 4) {

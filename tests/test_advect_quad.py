@@ -28,16 +28,17 @@ def _built():
     build.build()
 
 
-def _pair(monkeypatch, wl, blocks=3):
-    """a per-level tile context and a four-level one whose registers are
-    sized for `blocks` blocks per SM"""
+def _pair(monkeypatch, wl, blocks=3, tile="4x8"):
+    """a per-level tile context and a four-level one (tile TIxTJ) whose
+    registers are sized for `blocks` blocks per SM"""
     ms = []
     for mode in ("tile", "quad"):
         monkeypatch.setenv("GA_ADVECT", mode)
         monkeypatch.setenv("GA_ADVECT_BLOCKS", str(blocks))
+        monkeypatch.setenv("GA_ADVECT_TILE", tile)
         ms.append(anelastic.Model(wl, abi.GA_PREC_F32))
-    monkeypatch.delenv("GA_ADVECT")
-    monkeypatch.delenv("GA_ADVECT_BLOCKS")
+    for v in ("GA_ADVECT", "GA_ADVECT_BLOCKS", "GA_ADVECT_TILE"):
+        monkeypatch.delenv(v)
     return ms
 
 
@@ -57,14 +58,15 @@ def _perturb(ms, wl, seed):
                 m.set(f, slot, x)
 
 
+@pytest.mark.parametrize("tile", ["4x8", "4x4", "8x4", "2x8", "8x8"])
 @pytest.mark.parametrize("blocks", [3, 4])
 @pytest.mark.parametrize("case", ["moist_rf1", "moist_rf2", "dry"])
-def test_single_advection_operator_bit_identical(monkeypatch, case, blocks):
+def test_single_advection_operator_bit_identical(monkeypatch, case, blocks, tile):
     if case == "dry":
         wl = configs.dry_bubble(nx=30, ny=26, nz=20, nsteps=2)
     else:
         wl = configs.moist_blob(nx=30, ny=26, nz=16, rain_fallout=1 if case == "moist_rf1" else 2)
-    ms = _pair(monkeypatch, wl, blocks)
+    ms = _pair(monkeypatch, wl, blocks, tile)
     _perturb(ms, wl, 11)
     for op, fields in ADVECT_OPS.items():
         if op == "advect_micro" and not wl.microphysics_option:
