@@ -106,6 +106,7 @@ class Engine : public EngineBase {
     // autotuner to one kernel
     int adv_quad = 1, adv_qi = 4, adv_qj = 8, adv_force = 0;
     int adv_qb = 3;  // blocks per SM the four-level kernel's registers are sized for (3 or 4)
+    int adv_rows = 0;  // four-level kernel: east and north faces by sliding rows (ADV_ROWS)
     // the four-level post-processing kernel (FP32, NZ % 4 == 0); GA_POST=column
     // keeps the per-level one
     bool post_quad = true;
@@ -333,6 +334,7 @@ class Engine : public EngineBase {
                 for (auto &tl : kQuadTiles)
                     if (tl[0] == a && tl[1] == b) { adv_qi = a; adv_qj = b; }
         }
+        if (const char *ev = std::getenv("GA_ADVECT_FACES")) adv_rows = !std::strcmp(ev, "rows");
         if (const char *ev = std::getenv("GA_POST")) post_quad = std::strcmp(ev, "column") != 0;
         post_quad = post_quad && sizeof(T) == 4 && NZ % 4 == 0;
         if constexpr (sizeof(T) == 4) {
@@ -574,11 +576,12 @@ class Engine : public EngineBase {
         ProfScope ps(this, PC_ADVECT, 1);
         if (adv_quad && quad_ok(adv_qi, adv_qj)) {
             const T st = (T)step, sg = (T)sdtg;
-            if (adv_qi == 4 && adv_qj == 4) launch_advect_quad<4, 4>(st, sg, what);
-            else if (adv_qi == 8 && adv_qj == 4) launch_advect_quad<8, 4>(st, sg, what);
-            else if (adv_qi == 2) launch_advect_quad<2, 8>(st, sg, what);
-            else if (adv_qi == 8) launch_advect_quad<8, 8>(st, sg, what);
-            else launch_advect_quad<4, 8>(st, sg, what);
+            const int wq = what | (adv_rows ? ADV_ROWS : 0);
+            if (adv_qi == 4 && adv_qj == 4) launch_advect_quad<4, 4>(st, sg, wq);
+            else if (adv_qi == 8 && adv_qj == 4) launch_advect_quad<8, 4>(st, sg, wq);
+            else if (adv_qi == 2) launch_advect_quad<2, 8>(st, sg, wq);
+            else if (adv_qi == 8) launch_advect_quad<8, 8>(st, sg, wq);
+            else launch_advect_quad<4, 8>(st, sg, wq);
         } else if (smem_adv <= 200 * 1024) {
             const T st = (T)step, sg = (T)sdtg;
             if (adv_ti == 2) launch_advect_tile<2, 4>(st, sg, what);
@@ -898,7 +901,7 @@ class Engine : public EngineBase {
         // advection tile
         {
             float best = 1e30f;
-            int bi = adv_ti, bj = adv_tj, bq = 0, qi = adv_qi, qj = adv_qj, qb = adv_qb;
+            int bi = adv_ti, bj = adv_tj, bq = 0, qi = adv_qi, qj = adv_qj, qb = adv_qb, br = adv_rows;
             if (adv_force != 2 || !quad_ok(adv_qi, adv_qj)) {
                 adv_quad = 0;
                 for (auto &tl : kAdvTiles) {
@@ -913,18 +916,19 @@ class Engine : public EngineBase {
                 adv_quad = 1;
                 for (auto &tl : kQuadTiles) {
                     if (!quad_ok(tl[0], tl[1])) continue;
-                    for (int mb = 3; mb <= 4; mb++) {
-                        adv_qi = tl[0]; adv_qj = tl[1]; adv_qb = mb;
-                        const float t = timeit([&] { advect(1. / 3., what); });
-                        if (t < best) { best = t; bq = 1; qi = tl[0]; qj = tl[1]; qb = mb; }
-                    }
+                    for (int mb = 3; mb <= 4; mb++)
+                        for (int rows = 0; rows <= 1; rows++) {
+                            adv_qi = tl[0]; adv_qj = tl[1]; adv_qb = mb; adv_rows = rows;
+                            const float t = timeit([&] { advect(1. / 3., what); });
+                            if (t < best) { best = t; bq = 1; qi = tl[0]; qj = tl[1]; qb = mb; br = rows; }
+                        }
                 }
             }
-            adv_ti = bi; adv_tj = bj; adv_quad = bq; adv_qi = qi; adv_qj = qj; adv_qb = qb;
+            adv_ti = bi; adv_tj = bj; adv_quad = bq; adv_qi = qi; adv_qj = qj; adv_qb = qb; adv_rows = br;
             smem_adv = advect_tile_smem(bi, bj, NZ, sizeof(T));
             if (bq)
-                std::snprintf(line, sizeof line, "advect tile %dx%d, four levels per thread, %d blocks/SM (%.4f ms); ",
-                              qi, qj, qb, best);
+                std::snprintf(line, sizeof line, "advect tile %dx%d, four levels per thread, %d blocks/SM%s (%.4f ms); ",
+                              qi, qj, qb, br ? ", face rows" : "", best);
             else std::snprintf(line, sizeof line, "advect tile %dx%d (%.4f ms); ", bi, bj, best);
             info += line;
         }

@@ -69,7 +69,9 @@ __global__ void __launch_bounds__(AQ_THREADS, MB) kb_advect_quad(const KParams<T
         const long lb = vb - pre[m];
         const int gx = (p.nx - 6 + TI - 1) / TI;
         const double sdtg = step * p.dt_d * 9.8 * 0.5;  // step*dt*grav*0.5, advection.cpp:330
-        advect_quad_body<TI, TJ>(p, F[m], (int)(lb % gx), (int)(lb / gx), (T)step, (T)sdtg, what);
+        // members' fields do not stay in L2, where the per-face form is the
+        // faster one; masking ADV_ROWS lets the compiler drop the row form
+        advect_quad_body<TI, TJ>(p, F[m], (int)(lb % gx), (int)(lb / gx), (T)step, (T)sdtg, what & ~ADV_ROWS);
         __syncthreads();
     }
 }

@@ -187,6 +187,138 @@ __device__ __forceinline__ Q4 aq_north(const KParams<float> &p, const KFields<fl
     return r;
 }
 
+// face columns per row segment of the row form
+constexpr int AQ_SEG = 3;
+
+// east faces (between i and i+1) of row j at levels k0..k0+3 for face
+// columns a = a0 .. min(a0+AQ_SEG, ti+1)-1, i = i0-1+a (u_east_ub, v_east_ub,
+// s_east_ub), into E + a * TJ * nz.  The six-point stencil slides along i, so
+// a segment loads each x column once; the table rows depend on k0 alone.
+template <int TI, int TJ, int FK>
+__device__ __forceinline__ void aq_east_row(const KParams<float> &p, const KFields<float> &F, const float *tab,
+                                            float *E, int i0, int j, int k0, int ti, int a0)
+{
+    const int nz = p.nz, sx = p.ny * nz, sy = nz;
+    const int c = gix(p.ny, nz, i0 - 1 + a0, j, k0);
+    const float *X = F.cur[aq_field(FK)], *U = F.cur[FU];
+    constexpr int BR = aq_brow(FK);
+    const Q4 z4{{0.f, 0.f, 0.f, 0.f}};
+    const Q4 ubar = lds4(tab + (FK <= 1 ? BT_UA : BT_UB) * nz + k0);
+    const Q4 c6 = FK == 0 ? lds4(tab + BT_C6_UB * nz + k0)
+                  : FK == 1 ? lds4(tab + BT_C6_VB * nz + k0)
+                  : BR >= 0 ? lds4(tab + (BT_C6_THB + BR) * nz + k0)
+                            : z4;
+    Q4 x[6];
+#pragma unroll
+    for (int m = 0; m < 5; m++) x[m] = ldg4(X, c + (m - 2) * sx);
+    Q4 u0 = FK == 0 ? ldg4(U, c) : z4;
+#pragma unroll
+    for (int s = 0; s < AQ_SEG; s++) {
+        const int a = a0 + s;
+        if (a > ti) break;
+        const int ca = c + s * sx;
+        x[5] = ldg4(X, ca + 3 * sx);
+        Q4 r;
+        if (FK == 0) {
+            const Q4 up = ldg4(U, ca + sx);
+#pragma unroll
+            for (int e = 0; e < 4; e++) {
+                const float ua = 0.5f * (up.v[e] + u0.v[e]);
+                const float ue = face5<float>(x[0].v[e], x[1].v[e], x[2].v[e], x[3].v[e], x[4].v[e], x[5].v[e],
+                                              sgn(ubar.v[e] + ua));
+                r.v[e] = ua * c6.v[e] + (ubar.v[e] + ua) * ue;
+            }
+            u0 = up;
+        } else if (FK == 1) {
+            const Q4 ua_ = ldg4(U, ca + sx), ub_ = ldg4(U, ca + sx - sy);
+#pragma unroll
+            for (int e = 0; e < 4; e++) {
+                const float ua = 0.5f * (ua_.v[e] + ub_.v[e]);
+                const float ve = face5<float>(x[0].v[e], x[1].v[e], x[2].v[e], x[3].v[e], x[4].v[e], x[5].v[e],
+                                              sgn(ubar.v[e] + ua));
+                r.v[e] = ua * c6.v[e] + (ubar.v[e] + ua) * ve;
+            }
+        } else {
+            const Q4 u1 = ldg4(U, ca + sx);
+#pragma unroll
+            for (int e = 0; e < 4; e++) {
+                const float ut = ubar.v[e] + u1.v[e];
+                const float se = face5<float>(x[0].v[e], x[1].v[e], x[2].v[e], x[3].v[e], x[4].v[e], x[5].v[e],
+                                              sgn(ut));
+                if (BR < 0) r.v[e] = ut * se;
+                else r.v[e] = u1.v[e] * c6.v[e] + ut * se;
+            }
+        }
+        sts4(E + a * TJ * nz, r);
+#pragma unroll
+        for (int m = 0; m < 5; m++) x[m] = x[m + 1];
+    }
+}
+
+// north faces (between j and j+1) of row i for face columns
+// b = b0 .. min(b0+AQ_SEG, tj+1)-1, j = j0-1+b (u_north_ub, v_north_ub,
+// s_north_ub), into N + b * nz
+template <int TI, int TJ, int FK>
+__device__ __forceinline__ void aq_north_row(const KParams<float> &p, const KFields<float> &F, const float *tab,
+                                             float *N, int i, int j0, int k0, int tj, int b0)
+{
+    const int nz = p.nz, sx = p.ny * nz, sy = nz;
+    const int c = gix(p.ny, nz, i, j0 - 1 + b0, k0);
+    const float *X = F.cur[aq_field(FK)], *V = F.cur[FV];
+    constexpr int BR = aq_brow(FK);
+    const Q4 z4{{0.f, 0.f, 0.f, 0.f}};
+    const Q4 vbar = lds4(tab + (FK <= 1 ? BT_VA : BT_VB) * nz + k0);
+    const Q4 c6 = FK == 0 ? lds4(tab + BT_C6_UB * nz + k0)
+                  : FK == 1 ? lds4(tab + BT_C6_VB * nz + k0)
+                  : BR >= 0 ? lds4(tab + (BT_C6_THB + BR) * nz + k0)
+                            : z4;
+    Q4 x[6];
+#pragma unroll
+    for (int m = 0; m < 5; m++) x[m] = ldg4(X, c + (m - 2) * sy);
+    Q4 v0 = FK == 1 ? ldg4(V, c) : z4;
+#pragma unroll
+    for (int s = 0; s < AQ_SEG; s++) {
+        const int b = b0 + s;
+        if (b > tj) break;
+        const int cb = c + s * sy;
+        x[5] = ldg4(X, cb + 3 * sy);
+        Q4 r;
+        if (FK == 0) {
+            const Q4 va_ = ldg4(V, cb + sy), vb_ = ldg4(V, cb - sx + sy);
+#pragma unroll
+            for (int e = 0; e < 4; e++) {
+                const float va = 0.5f * (va_.v[e] + vb_.v[e]);
+                const float un = face5<float>(x[0].v[e], x[1].v[e], x[2].v[e], x[3].v[e], x[4].v[e], x[5].v[e],
+                                              sgn(vbar.v[e] + va));
+                r.v[e] = va * c6.v[e] + (vbar.v[e] + va) * un;
+            }
+        } else if (FK == 1) {
+            const Q4 vp = ldg4(V, cb + sy);
+#pragma unroll
+            for (int e = 0; e < 4; e++) {
+                const float va = 0.5f * (vp.v[e] + v0.v[e]);
+                const float vn = face5<float>(x[0].v[e], x[1].v[e], x[2].v[e], x[3].v[e], x[4].v[e], x[5].v[e],
+                                              sgn(vbar.v[e] + va));
+                r.v[e] = va * c6.v[e] + (vbar.v[e] + va) * vn;
+            }
+            v0 = vp;
+        } else {
+            const Q4 v1 = ldg4(V, cb + sy);
+#pragma unroll
+            for (int e = 0; e < 4; e++) {
+                const float vt = vbar.v[e] + v1.v[e];
+                const float sn = face5<float>(x[0].v[e], x[1].v[e], x[2].v[e], x[3].v[e], x[4].v[e], x[5].v[e],
+                                              sgn(vt));
+                if (BR < 0) r.v[e] = vt * sn;
+                else r.v[e] = v1.v[e] * c6.v[e] + vt * sn;
+            }
+        }
+        sts4(N + b * nz, r);
+#pragma unroll
+        for (int m = 0; m < 5; m++) x[m] = x[m + 1];
+    }
+}
+
 // top face (between k and k+1) at k = k0..k0+3: u_top_ub, v_top_ub,
 // s_top_ub, r_top_ub; level NZ-1 is not a face of an advected cell (0)
 template <int FK>
@@ -283,14 +415,40 @@ __device__ __forceinline__ Q4 aq_top(const KParams<float> &p, const KFields<floa
     return r;
 }
 
-// the face columns of field FK into slot `sl` (E, N and T of the tile)
+// the face columns of field FK into slot `sl` (E, N and T of the tile).
+// rows: east and north faces by row segments of up to AQ_SEG face columns
+// whose stencil slides (fewer loads and less index arithmetic, but a
+// segment's loads one after another); otherwise one work item per face
+// column and quad.  In the row form one loop covers three kinds of work
+// item, each padded to whole warps: east segments (segment, b, quad), north
+// segments (segment, a, quad) and top faces (column, quad).  Both forms
+// evaluate the same expressions.
 template <int TI, int TJ, int FK>
 __device__ __forceinline__ void aq_faces(const KParams<float> &p, const KFields<float> &F, const float *tab,
-                                         float *sl, int i0, int j0, int ti, int tj)
+                                         float *sl, int i0, int j0, int ti, int tj, bool rows)
 {
     using G = AQGeom<TI, TJ>;
     const int nz = p.nz, NQ = nz >> 2;
     float *E = sl, *N = sl + G::CE * nz, *T = N + G::CN * nz;
+    if (rows) {
+        constexpr int SE = (TI + AQ_SEG) / AQ_SEG, SN = (TJ + AQ_SEG) / AQ_SEG;  // segments of TI+1, TJ+1
+        const int nE = (SE * TJ * NQ + 31) & ~31, nN = (SN * TI * NQ + 31) & ~31, nall = nE + nN + G::CT * NQ;
+        for (int w = threadIdx.x; w < nall; w += AQ_THREADS) {
+            if (w < nE) {
+                const int q = w % NQ, r = w / NQ, b = r % TJ, a0 = (r / TJ) * AQ_SEG;
+                if (b < tj && a0 <= ti)
+                    aq_east_row<TI, TJ, FK>(p, F, tab, E + b * nz + 4 * q, i0, j0 + b, 4 * q, ti, a0);
+            } else if (w < nE + nN) {
+                const int v = w - nE, q = v % NQ, r = v / NQ, a = r % TI, b0 = (r / TI) * AQ_SEG;
+                if (a < ti && b0 <= tj)
+                    aq_north_row<TI, TJ, FK>(p, F, tab, N + a * (TJ + 1) * nz + 4 * q, i0 + a, j0, 4 * q, tj, b0);
+            } else {
+                const int v = w - nE - nN, q = v % NQ, col = v / NQ, b = col % TJ, a = col / TJ;
+                if (a < ti && b < tj) sts4(T + col * nz + 4 * q, aq_top<FK>(p, F, tab, i0 + a, j0 + b, 4 * q));
+            }
+        }
+        return;
+    }
     for (int w = threadIdx.x; w < G::CE * NQ; w += AQ_THREADS) {
         const int q = w % NQ, col = w / NQ, b = col % TJ, a = col / TJ;
         if (a > ti || b >= tj) continue;
@@ -373,13 +531,14 @@ __device__ __forceinline__ void advect_quad_body(const KParams<float> &p, const 
     }
     const int i0 = 3 + bx * TI, j0 = 3 + by * TJ;
     const int ti = min(TI, p.nx - 3 - i0), tj = min(TJ, p.ny - 3 - j0);
+    const bool rows = (what & ADV_ROWS) != 0;
     __syncthreads();
 
     // ---- pass 1: u, v (and the buoyancy of w)
     if (what & (ADV_UV | ADV_WB)) {
         if (what & ADV_UV) {
-            aq_faces<TI, TJ, 0>(p, F, tab, s0, i0, j0, ti, tj);
-            aq_faces<TI, TJ, 1>(p, F, tab, s1, i0, j0, ti, tj);
+            aq_faces<TI, TJ, 0>(p, F, tab, s0, i0, j0, ti, tj, rows);
+            aq_faces<TI, TJ, 1>(p, F, tab, s1, i0, j0, ti, tj, rows);
         }
         __syncthreads();
         for (int w = threadIdx.x; w < G::CT * NQ; w += AQ_THREADS) {
@@ -441,8 +600,8 @@ __device__ __forceinline__ void advect_quad_body(const KParams<float> &p, const 
     // ---- pass 2: theta, qv (qv's clipping bit)
     const bool th_on = (what & ADV_TH) != 0, q_on = (what & ADV_Q) != 0;
     if (th_on || q_on) {
-        if (th_on) aq_faces<TI, TJ, 2>(p, F, tab, s0, i0, j0, ti, tj);
-        if (q_on) aq_faces<TI, TJ, 3>(p, F, tab, s1, i0, j0, ti, tj);
+        if (th_on) aq_faces<TI, TJ, 2>(p, F, tab, s0, i0, j0, ti, tj, rows);
+        if (q_on) aq_faces<TI, TJ, 3>(p, F, tab, s1, i0, j0, ti, tj, rows);
         __syncthreads();
         for (int w = threadIdx.x; w < G::CT * NQ; w += AQ_THREADS) {
             const int q = w % NQ, col = w / NQ, b = col % TJ, a = col / TJ;
@@ -500,8 +659,8 @@ __device__ __forceinline__ void advect_quad_body(const KParams<float> &p, const 
 
     // ---- pass 3: qc, qr (clipping bits 2 and 4, the rain's fall speed)
     if (q_on) {
-        aq_faces<TI, TJ, 4>(p, F, tab, s0, i0, j0, ti, tj);
-        aq_faces<TI, TJ, 5>(p, F, tab, s1, i0, j0, ti, tj);
+        aq_faces<TI, TJ, 4>(p, F, tab, s0, i0, j0, ti, tj, rows);
+        aq_faces<TI, TJ, 5>(p, F, tab, s1, i0, j0, ti, tj, rows);
         __syncthreads();
         for (int w = threadIdx.x; w < G::CT * NQ; w += AQ_THREADS) {
             const int q = w % NQ, col = w / NQ, b = col % TJ, a = col / TJ;

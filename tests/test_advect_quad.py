@@ -28,16 +28,18 @@ def _built():
     build.build()
 
 
-def _pair(monkeypatch, wl, blocks=3, tile="4x8"):
+def _pair(monkeypatch, wl, blocks=3, tile="4x8", faces="single"):
     """a per-level tile context and a four-level one (tile TIxTJ) whose
-    registers are sized for `blocks` blocks per SM"""
+    registers are sized for `blocks` blocks per SM; faces "rows" evaluates the
+    east and north faces by sliding rows"""
     ms = []
     for mode in ("tile", "quad"):
         monkeypatch.setenv("GA_ADVECT", mode)
         monkeypatch.setenv("GA_ADVECT_BLOCKS", str(blocks))
         monkeypatch.setenv("GA_ADVECT_TILE", tile)
+        monkeypatch.setenv("GA_ADVECT_FACES", faces)
         ms.append(anelastic.Model(wl, abi.GA_PREC_F32))
-    for v in ("GA_ADVECT", "GA_ADVECT_BLOCKS", "GA_ADVECT_TILE"):
+    for v in ("GA_ADVECT", "GA_ADVECT_BLOCKS", "GA_ADVECT_TILE", "GA_ADVECT_FACES"):
         monkeypatch.delenv(v)
     return ms
 
@@ -58,15 +60,16 @@ def _perturb(ms, wl, seed):
                 m.set(f, slot, x)
 
 
+@pytest.mark.parametrize("faces", ["single", "rows"])
 @pytest.mark.parametrize("tile", ["4x8", "4x4", "8x4", "2x8", "8x8"])
 @pytest.mark.parametrize("blocks", [3, 4])
 @pytest.mark.parametrize("case", ["moist_rf1", "moist_rf2", "dry"])
-def test_single_advection_operator_bit_identical(monkeypatch, case, blocks, tile):
+def test_single_advection_operator_bit_identical(monkeypatch, case, blocks, tile, faces):
     if case == "dry":
         wl = configs.dry_bubble(nx=30, ny=26, nz=20, nsteps=2)
     else:
         wl = configs.moist_blob(nx=30, ny=26, nz=16, rain_fallout=1 if case == "moist_rf1" else 2)
-    ms = _pair(monkeypatch, wl, blocks, tile)
+    ms = _pair(monkeypatch, wl, blocks, tile, faces)
     _perturb(ms, wl, 11)
     for op, fields in ADVECT_OPS.items():
         if op == "advect_micro" and not wl.microphysics_option:
@@ -78,9 +81,10 @@ def test_single_advection_operator_bit_identical(monkeypatch, case, blocks, tile
             np.testing.assert_array_equal(b, a, err_msg=f"{case} {op} field {abi.PROG_NAMES[f]}")
 
 
+@pytest.mark.parametrize("faces", ["single", "rows"])
 @pytest.mark.parametrize("blocks", [3, 4])
 @pytest.mark.parametrize("case", ["moist_blob", "thunderstorm_small", "dry_bubble", "nz_not_multiple_of_4"])
-def test_steps_match_tile_kernel(monkeypatch, case, blocks):
+def test_steps_match_tile_kernel(monkeypatch, case, blocks, faces):
     if case == "moist_blob":
         wl = configs.moist_blob(nx=30, ny=26, nz=16, nsteps=6)
     elif case == "thunderstorm_small":
@@ -89,7 +93,7 @@ def test_steps_match_tile_kernel(monkeypatch, case, blocks):
         wl = configs.dry_bubble(nx=34, ny=30, nz=20, nsteps=6)
     else:  # falls back to the tile kernel: both contexts run the same code
         wl = configs.moist_blob(nx=30, ny=26, nz=18, nsteps=6)
-    ms = _pair(monkeypatch, wl, blocks)
+    ms = _pair(monkeypatch, wl, blocks, faces=faces)
     for m in ms:
         m.step(wl.nsteps)
     nprog = 7 if wl.microphysics_option else 4
