@@ -51,7 +51,7 @@ PASSES_MOIST = {"advect": 22, "div_fft_y": 5, "fft_x": 4, "thomas": 4, "ifft_y_p
                 "kessler": 12}
 # DRAM bytes per launch (read + write) of the dominant kernel, from one ncu
 # capture of the bench command (cold cache): workload -> (kernel group, bytes, summary)
-TRAFFIC_NCU = {"thunderstorm": ("advect", 49.79e6, "profiles/forward_kernels_thunderstorm_128x128x48_fp32.md")}
+TRAFFIC_NCU = {"thunderstorm": ("advect", 50.01e6, "profiles/forward_kernels_thunderstorm_128x128x48_fp32.md")}
 # compulsory bytes per gridpoint-step of an ideally fused step (FP32 moist)
 STEP_BYTES_FP32_MOIST = 540.0
 
@@ -242,7 +242,9 @@ def e2e_jobs(model_cls, wl, prec, torch, jobs, job_steps, device):
             assert L.ga_get_field(m.h, f, 0, C.cast(host_out[f].data_ptr(), dp), n) == 0
         assert L.ga_get_field(m.h, abi.GA_PI, 0, C.cast(host_out[nprog].data_ptr(), dp), n) == 0
 
-    one_job()  # warm-up
+    one_job()  # warm-up; it leaves a real state for the autotuner
+    tuning = m.tune()  # once per context, as a user of ga_tune would
+    one_job()
     t0 = time.perf_counter()
     for _ in range(jobs):
         one_job()
@@ -253,7 +255,7 @@ def e2e_jobs(model_cls, wl, prec, torch, jobs, job_steps, device):
     return {"value": round(n * job_steps * jobs / el, 1), "unit": UNIT,
             "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
             "step": f"one {job_steps}-step run: upload initial state, integrate, download fields",
-            "jobs": jobs, "seconds_per_run": round(el / jobs, 4)}
+            "jobs": jobs, "seconds_per_run": round(el / jobs, 4), "tuning": tuning}
 
 
 def ensemble_bench(torch, device, steps, warmup, n_small=64, n_large=32):

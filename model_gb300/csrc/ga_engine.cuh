@@ -885,8 +885,20 @@ class Engine : public EngineBase {
         cudaEventCreate(&ea);
         cudaEventCreate(&eb);
         const long long l0 = launches;
+        // L2 is written over before each candidate's timed launches: a grid
+        // whose state fits in L2 is otherwise timed hot, which favours tiles
+        // with more halo re-reads than a step that starts from DRAM can afford
+        int l2 = 0;
+        cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, device);
+        const size_t flush_bytes = 2 * (size_t)std::max(l2, 0);
+        void *flush = nullptr;
+        if (flush_bytes && cudaMalloc(&flush, flush_bytes) != cudaSuccess) {
+            flush = nullptr;
+            cudaGetLastError();
+        }
         auto timeit = [&](auto fn) {
             fn();  // warm-up
+            if (flush) cudaMemsetAsync(flush, 0, flush_bytes, stream);
             cudaEventRecord(ea, stream);
             for (int r = 0; r < 3; r++) fn();
             cudaEventRecord(eb, stream);
@@ -1035,6 +1047,7 @@ class Engine : public EngineBase {
         const int rc = sync_status();
         cudaEventDestroy(ea);
         cudaEventDestroy(eb);
+        if (flush) cudaFree(flush);
         cudaFree(snap);
         launches = l0;
         drop_graphs();
