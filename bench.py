@@ -455,6 +455,7 @@ def run_ours(args):
     barrier(dist)
     sampler = ClockSampler(device)
     sampler.start()
+    time.sleep(0.3)  # nvidia-smi's first samples, before the timed region opens
     l0 = model.launch_count()
     torch.cuda.synchronize()
     barrier(dist)
@@ -547,7 +548,7 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="f32", choices=["f32", "f64"])
