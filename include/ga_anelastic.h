@@ -275,8 +275,11 @@ GA_API int ga_adjoint(ga_ctx *ctx, int nsteps, int checkpoint_every);
  * a CUDA graph.  Each member computes exactly what a standalone context with
  * its configuration computes.  Members share precision, device and
  * microphysics option; periodic members and semi-Lagrangian rain fallout are
- * not batched (GA_ERR_UNSUPPORTED).  Fields are set and read per member with
- * the same ids and slots as ga_set_field / ga_get_field.
+ * not batched (GA_ERR_UNSUPPORTED).  The x solve of the pressure equation is
+ * one fused kernel per y-wavenumber, or, when a member's levels do not fit in
+ * shared memory (or ga_ensemble_tune finds it faster), batched x FFTs, Thomas
+ * blocks and inverse x FFTs.  Fields are set and read per member with the
+ * same ids and slots as ga_set_field / ga_get_field.
  */
 typedef struct ga_ens ga_ens;
 GA_API int ga_ensemble_create(const ga_config *cfgs, const ga_columns *cols, int nmembers, ga_ens **out);

@@ -27,7 +27,7 @@ struct MemberAux {
     int KTy, psx;
 };
 
-enum { EK_ADV = 0, EK_MIRROR, EK_DIVY, EK_SX, EK_IFFTY, EK_POST, EK_KES, EK_COUNT };
+enum { EK_ADV = 0, EK_MIRROR, EK_DIVY, EK_SX, EK_IFFTY, EK_POST, EK_KES, EK_FX, EK_TH, EK_COUNT };
 
 __device__ __forceinline__ int find_member(const long *pre, int nmem, long vb)
 {
@@ -58,8 +58,10 @@ __global__ void __launch_bounds__(256) kb_advect(const KParams<T> *P, const KFie
 
 // FP32 members with whole level quads: the four-level advection and post
 template <typename T, int TI, int TJ, int MB>
-__global__ void __launch_bounds__(AQ_THREADS, MB) kb_advect_quad(const KParams<T> *P, const KFields<T> *F,
-                                                               const long *pre, int nmem, double step, int what)
+__global__ void __launch_bounds__(AQ_THREADS, MB) kb_advect_quad(const KParams<T> *__restrict__ P,
+                                                               const KFields<T> *__restrict__ F,
+                                                               const long *__restrict__ pre, int nmem, double step,
+                                                               int what)
 {
     static_assert(sizeof(T) == 4, "four-level kernels are FP32");
     const long total = pre[nmem];
@@ -69,8 +71,8 @@ __global__ void __launch_bounds__(AQ_THREADS, MB) kb_advect_quad(const KParams<T
         const long lb = vb - pre[m];
         const int gx = (p.nx - 6 + TI - 1) / TI;
         const double sdtg = step * p.dt_d * 9.8 * 0.5;  // step*dt*grav*0.5, advection.cpp:330
-        // members' fields do not stay in L2, where the per-face form is the
-        // faster one; masking ADV_ROWS lets the compiler drop the row form
+        // the row form spills in this kernel at either register budget;
+        // masking ADV_ROWS lets the compiler drop it
         advect_quad_body<TI, TJ>(p, F[m], (int)(lb % gx), (int)(lb / gx), (T)step, (T)sdtg, what & ~ADV_ROWS);
         __syncthreads();
     }
@@ -122,6 +124,33 @@ __global__ void kb_spectral_x(const KParams<T> *P, const MemberAux<T> *A, const 
         const int m = find_member(pre, nmem, vb);
         const MemberAux<T> &a = A[m];
         spectral_x_body(P[m], a.spec, a.plan_i, a.tw_i, a.psx, (int)(vb - pre[m]));
+        __syncthreads();
+    }
+}
+
+// the unfused x solve: x FFT per (y-wavenumber, level tile KT shared by every
+// member), then Thomas per TC columns, then the inverse x FFT
+template <typename T>
+__global__ void kb_fft_x(const KParams<T> *P, const MemberAux<T> *A, const long *pre, int nmem, int inv, int KT)
+{
+    const long total = pre[nmem];
+    for (long vb = blockIdx.x; vb < total; vb += gridDim.x) {
+        const int m = find_member(pre, nmem, vb);
+        const KParams<T> &p = P[m];
+        const MemberAux<T> &a = A[m];
+        const long lb = vb - pre[m];
+        const long nkt = (p.nz - 2 + KT - 1) / KT;  // level tiles of a wavenumber run next to each other
+        fft_x_body(p, a.spec, a.plan_i, a.tw_i, inv, KT, (int)(lb / nkt), (int)(lb % nkt));
+        __syncthreads();
+    }
+}
+template <typename T>
+__global__ void kb_thomas(const KParams<T> *P, const MemberAux<T> *A, const long *pre, int nmem, int TC)
+{
+    const long total = pre[nmem];
+    for (long vb = blockIdx.x; vb < total; vb += gridDim.x) {
+        const int m = find_member(pre, nmem, vb);
+        thomas_body(P[m], A[m].spec, TC, vb - pre[m]);
         __syncthreads();
     }
 }
@@ -194,6 +223,10 @@ class Ensemble : public EnsembleBase {
     bool quad = false, adv_quad = true;
     int adv_qi = 4, adv_qj = 8, adv_qb = 3;  // quad tile, blocks per SM of its register budget
     int sx_threads = 256;  // threads of a fused spectral-x block (autotuned)
+    // the x solve: fused kernel (0) or x FFT, Thomas, inverse x FFT (1), the
+    // level tile of the x FFTs and the columns of a Thomas block (autotuned)
+    int sx_unfused = 0, KTx = 8, TC = 64;
+    bool fused_ok = true;  // every member fits the fused x kernel
     int nsm = 0;
     bool adv_quad_now = false;  // the choice build_prefixes made (prefixes and launches agree)
     bool quad_applies() const
@@ -220,12 +253,13 @@ class Ensemble : public EnsembleBase {
                 delete e;
                 return;
             }
-            if (e->psx == 0 || e->smem_adv > 200 * 1024) {
+            if (e->smem_adv > 200 * 1024) {
                 *rc = GA_ERR_UNSUPPORTED;
                 set_error("ensemble: member too large for the batched kernels");
                 delete e;
                 return;
             }
+            fused_ok = fused_ok && e->psx > 0;  // every level of a wavenumber fits shared memory
             mem.push_back(e);
         }
         cudaMalloc(&d_p, sizeof(KParams<T>) * n);
@@ -243,6 +277,11 @@ class Ensemble : public EnsembleBase {
         cudaFuncSetAttribute(kb_div_fft_y<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
         cudaFuncSetAttribute(kb_spectral_x<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
         cudaFuncSetAttribute(kb_ifft_y_pi<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+        cudaFuncSetAttribute(kb_fft_x<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+        cudaFuncSetAttribute(kb_thomas<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+        if (const char *ev = std::getenv("GA_SPECTRAL_X")) sx_unfused = !std::strcmp(ev, "unfused");
+        if (!fused_ok) sx_unfused = 1;
+        while (KTx > 1 && !ktx_fits(KTx)) KTx >>= 1;
         if constexpr (sizeof(T) == 4) {
             quad = true;
             for (auto *e : mem) quad = quad && e->NZ % 4 == 0;
@@ -342,8 +381,24 @@ class Ensemble : public EnsembleBase {
     }
     void launch_sx()
     {
+        if (sx_unfused) {
+            const dim3 bx(KTx, std::max(1, 256 / KTx));
+            kb_fft_x<T><<<grid[EK_FX], bx, smem[EK_FX], stream>>>(d_p, d_aux, d_pre[EK_FX], nmem, 0, KTx);
+            kb_thomas<T><<<grid[EK_TH], 256, smem[EK_TH], stream>>>(d_p, d_aux, d_pre[EK_TH], nmem, TC);
+            kb_fft_x<T><<<grid[EK_FX], bx, smem[EK_FX], stream>>>(d_p, d_aux, d_pre[EK_FX], nmem, 1, KTx);
+            return;
+        }
         kb_spectral_x<T><<<grid[EK_SX], dim3(64, sx_threads / 64), smem[EK_SX], stream>>>(d_p, d_aux, d_pre[EK_SX],
                                                                                           nmem);
+    }
+    int sx_launches() const { return sx_unfused ? 3 : 1; }
+    // an x level tile every member's x FFT can hold in shared memory
+    bool ktx_fits(int kt) const
+    {
+        for (auto *e : mem)
+            if (kt > 2 * (e->NZ - 2) || 2 * (size_t)e->kp.ni * kt * sizeof(typename V2<T>::t) > 200 * 1024)
+                return false;
+        return true;
     }
 
     // virtual-block prefixes per kernel phase (for the current advection tile
@@ -383,6 +438,14 @@ class Ensemble : public EnsembleBase {
                     c = quad ? cdiv((long)e.NX * e.NY * (e.NZ / 4), PQ_THREADS) : cdiv((long)e.NX * e.NY, POST_COLS);
                     break;
                 case EK_KES: c = cdiv((long)(e.NX - 2) * (e.NY - 2) * (e.NZ - 2), 128); break;
+                case EK_FX:
+                    c = (long)e.kp.nj * cdiv(e.NZ - 2, KTx);
+                    sm = std::max(sm, 2 * (size_t)e.kp.ni * KTx * sizeof(typename V2<T>::t));
+                    break;
+                case EK_TH:
+                    c = cdiv((long)e.kp.ni * e.kp.nj, TC);
+                    sm = std::max(sm, (size_t)TC * (e.NZ | 1) * (sizeof(typename V2<T>::t) + sizeof(T)));
+                    break;
                 }
                 pre[m + 1] = pre[m] + c;
             }
@@ -406,6 +469,8 @@ class Ensemble : public EnsembleBase {
             if (quad) grid[EK_POST] = occ((const void *)kb_post_quad<T>, PQ_THREADS, 0);
         }
         grid[EK_KES] = occ((const void *)kb_kessler<T>, 128, 0);
+        grid[EK_FX] = occ((const void *)kb_fft_x<T>, KTx * std::max(1, 256 / KTx), smem[EK_FX]);
+        grid[EK_TH] = occ((const void *)kb_thomas<T>, 256, smem[EK_TH]);
         for (int k = 0; k < EK_COUNT; k++) grid[k] = (int)std::min<long>(grid[k], std::max(1L, total[k]));
     }
 
@@ -540,16 +605,37 @@ class Ensemble : public EnsembleBase {
                 refresh_tables();
                 build_prefixes();
             }
-            // the fused x kernel's block size
-            {
+            // the fused x kernel's block size, then the unfused x solve for
+            // each x level tile
+            const int keep_unfused = sx_unfused;
+            if (fused_ok) {
+                sx_unfused = 0;
                 const int keep = sx_threads;
                 sx_threads = 512;
                 const float t = timeit(chain);
                 if (t < best) best = t;
                 else sx_threads = keep;
             }
-            std::snprintf(line, sizeof line, "y level tile %d, x block %d threads (pressure solve %.3f ms)", bk,
-                          sx_threads, best);
+            sx_unfused = keep_unfused;
+            if (sx_unfused) best = timeit(chain);  // the default when GA_SPECTRAL_X=unfused
+            int bu = sx_unfused, bkx = KTx;
+            for (int kt = 1; kt <= 64; kt <<= 1) {
+                if (!ktx_fits(kt)) break;
+                sx_unfused = 1;
+                KTx = kt;
+                build_prefixes();
+                const float t = timeit(chain);
+                if (t < best) { best = t; bu = 1; bkx = kt; }
+            }
+            sx_unfused = bu;
+            KTx = bkx;
+            build_prefixes();
+            if (sx_unfused)
+                std::snprintf(line, sizeof line, "y level tile %d, x level tile %d (pressure solve %.3f ms)", bk, KTx,
+                              best);
+            else
+                std::snprintf(line, sizeof line, "y level tile %d, x block %d threads (pressure solve %.3f ms)", bk,
+                              sx_threads, best);
             info += line;
         }
         copy_all(false);
@@ -632,7 +718,7 @@ class Ensemble : public EnsembleBase {
                                                                                      nmem);
             const int fu = PF_PROJECT | PF_SPONGE | PF_VBC, ft = PF_SPONGE | PF_VBC, fq = PF_ZERO | PF_SPONGE | PF_VBC;
             launch_post(F, make_int4(fu, fu, fu, ft), make_int4(fq, fq, fq, 0), st);
-            launches += 6;
+            launches += 5 + sx_launches();
             if (s < 2) swap_all();
         }
         KFields<T> *F = d_f[rot];

@@ -1090,19 +1090,17 @@ __global__ void k_div_fft_y(KParams<T> p, KFields<T> F, typename V2<T>::t *spec,
     div_fft_y_body(p, F, spec, pj, tw, sdt, KT, blockIdx.y, blockIdx.x);
 }
 
-// FFT along x of the spectral buffer for one y-wavenumber q and a tile of
-// levels.  sign: forward (false) or inverse (true).
+// FFT along x of the spectral buffer for one y-wavenumber q and level tile
+// bx.  sign: forward (false) or inverse (true).  Block (KT, any).
 template <typename T>
-__global__ void k_fft_x(KParams<T> p, typename V2<T>::t *spec, FftPlan pi, const typename V2<T>::t *tw,
-                        int inv, int KT)
+__device__ void fft_x_body(const KParams<T> &p, typename V2<T>::t *spec, const FftPlan &pi,
+                           const typename V2<T>::t *tw, int inv, int KT, int q, int bx)
 {
     typedef typename V2<T>::t T2;
     extern __shared__ unsigned char smem_raw[];
     T2 *a = (T2 *)smem_raw;
     T2 *b = a + (long)p.ni * KT;
-    // the level tiles of a wavenumber run next to each other (shared rows)
-    const int q = blockIdx.y;
-    const int k0 = 1 + blockIdx.x * KT;
+    const int k0 = 1 + bx * KT;
     const int kt = min(KT, p.nz - 1 - k0);
     for (int i = threadIdx.y; i < p.ni; i += blockDim.y)
         for (int l = threadIdx.x; l < KT; l += blockDim.x)
@@ -1112,6 +1110,13 @@ __global__ void k_fft_x(KParams<T> p, typename V2<T>::t *spec, FftPlan pi, const
     for (int i = threadIdx.y; i < p.ni; i += blockDim.y)
         for (int l = threadIdx.x; l < kt; l += blockDim.x)
             spec[((long)i * p.nj + q) * p.nz + k0 + l] = r[i * KT + l];
+}
+// the level tiles of a wavenumber run next to each other (shared rows)
+template <typename T>
+__global__ void k_fft_x(KParams<T> p, typename V2<T>::t *spec, FftPlan pi, const typename V2<T>::t *tw,
+                        int inv, int KT)
+{
+    fft_x_body(p, spec, pi, tw, inv, KT, blockIdx.y, blockIdx.x);
 }
 
 // normalisation (pressure.cpp:827) + Thomas algorithm per horizontal
@@ -1334,8 +1339,9 @@ __device__ __forceinline__ bool low_mode(const KParams<T> &p, long col)
     return min(pp, p.ni - pp) < p.low_modes && min(qq, p.nj - qq) < p.low_modes;
 }
 
+// columns bx*TC .. of the spectral buffer
 template <typename T>
-__global__ void k_thomas(KParams<T> p, typename V2<T>::t *spec, int TC)
+__device__ void thomas_body(const KParams<T> &p, typename V2<T>::t *spec, int TC, long bx)
 {
     typedef typename V2<T>::t T2;
     extern __shared__ unsigned char smem_raw[];
@@ -1344,7 +1350,7 @@ __global__ void k_thomas(KParams<T> p, typename V2<T>::t *spec, int TC)
     T2 *xs = (T2 *)smem_raw;
     T *fs = (T *)(xs + (long)TC * cs);
     const long ncol = (long)p.ni * p.nj;
-    const long c0 = (long)blockIdx.x * TC;
+    const long c0 = bx * TC;
     const int nc = (int)min((long)TC, ncol - c0);
     T2 *g = spec + c0 * p.nz;
     for (int w = threadIdx.x; w < nc * p.nz; w += blockDim.x) cp_elem(xs + (w / p.nz) * cs + w % p.nz, g + w, true);
@@ -1380,6 +1386,11 @@ __global__ void k_thomas(KParams<T> p, typename V2<T>::t *spec, int TC)
     }
     __syncthreads();
     for (int w = threadIdx.x; w < nc * p.nz; w += blockDim.x) g[w] = xs[(w / p.nz) * cs + w % p.nz];
+}
+template <typename T>
+__global__ void k_thomas(KParams<T> p, typename V2<T>::t *spec, int TC)
+{
+    thomas_body(p, spec, TC, blockIdx.x);
 }
 
 template <typename T>

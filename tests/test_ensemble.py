@@ -9,14 +9,22 @@ from model_gb300 import abi, anelastic, configs
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("precision,tune", [(abi.GA_PREC_F64, False), (abi.GA_PREC_F32, False),
-                                            (abi.GA_PREC_F32, True)])
-def test_ensemble_members_equal_standalone_runs(precision, tune):
-    """tune: the autotuner runs mid-run; tiles change nothing bit for bit."""
+@pytest.mark.parametrize("precision,tune,x_solve", [(abi.GA_PREC_F64, False, "fused"),
+                                                    (abi.GA_PREC_F32, False, "fused"),
+                                                    (abi.GA_PREC_F32, True, "fused"),
+                                                    (abi.GA_PREC_F64, False, "unfused"),
+                                                    (abi.GA_PREC_F32, False, "unfused")])
+def test_ensemble_members_equal_standalone_runs(monkeypatch, precision, tune, x_solve):
+    """tune: the autotuner runs mid-run; tiles change nothing bit for bit.
+    x_solve "unfused": the ensemble's x solve as batched x FFTs and Thomas
+    blocks, against standalone contexts that use the fused x kernel."""
     members = [configs.moist_blob(nx=24, ny=22, nz=16, seed=3000),
                configs.moist_blob(nx=36, ny=30, nz=20, seed=3100, qc=2e-3),
                configs.moist_blob(nx=40, ny=24, nz=12, seed=3200, dt=3.0)]
+    if x_solve == "unfused":
+        monkeypatch.setenv("GA_SPECTRAL_X", "unfused")
     ens = anelastic.Ensemble(members, precision)
+    monkeypatch.delenv("GA_SPECTRAL_X", raising=False)
     for m, wl in enumerate(members):
         ens.load_member(m, wl.fields)
     nsteps = 5
@@ -38,6 +46,26 @@ def test_ensemble_members_equal_standalone_runs(precision, tune):
         solo.close()
     ens.close()
 
+
+
+def test_ensemble_member_too_tall_for_the_fused_x_kernel():
+    """a member whose levels of one y-wavenumber exceed shared memory (FP32:
+    200 x 70 spectral points) runs the batched unfused x solve; every member
+    still equals its standalone context bit for bit"""
+    members = [configs.moist_blob(nx=200, ny=20, nz=72, seed=3300),
+               configs.moist_blob(nx=36, ny=30, nz=20, seed=3100, qc=2e-3)]
+    ens = anelastic.Ensemble(members, abi.GA_PREC_F32)
+    for m, wl in enumerate(members):
+        ens.load_member(m, wl.fields)
+    ens.step(3)
+    for m, wl in enumerate(members):
+        solo = anelastic.Model(wl, abi.GA_PREC_F32)
+        solo.step(3)
+        for f in range(7):
+            np.testing.assert_array_equal(ens.get(m, f), solo.get(f), err_msg=f"member {m} f{f}")
+        np.testing.assert_array_equal(ens.get(m, abi.GA_PI), solo.get(abi.GA_PI))
+        solo.close()
+    ens.close()
 
 def test_ensemble_rejects_mixed_precision():
     a, b = configs.moist_blob(), configs.moist_blob(seed=9)
