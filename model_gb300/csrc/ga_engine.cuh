@@ -316,6 +316,7 @@ class Engine : public EngineBase {
             smem_sx = 2 * (size_t)ni * psx * sizeof(T2);
         }
         cudaFuncSetAttribute(k_spectral_x<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+        cudaFuncSetAttribute(k_spectral_x_1k<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
         smem_adv = advect_tile_smem(adv_ti, adv_tj, NZ, sizeof(T));
         cudaFuncSetAttribute(k_advect_tile<T, 4, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
         cudaFuncSetAttribute(k_advect_tile<T, 2, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
@@ -335,6 +336,8 @@ class Engine : public EngineBase {
                     if (tl[0] == a && tl[1] == b) { adv_qi = a; adv_qj = b; }
         }
         if (const char *ev = std::getenv("GA_ADVECT_FACES")) adv_rows = !std::strcmp(ev, "rows");
+        if (const char *ev = std::getenv("GA_SPECTRAL_X"))  // fused x block of 1024 threads by default
+            if (!std::strcmp(ev, "1024")) sx_threads = 1024;
         if (const char *ev = std::getenv("GA_POST")) post_quad = std::strcmp(ev, "column") != 0;
         post_quad = post_quad && sizeof(T) == 4 && NZ % 4 == 0;
         if constexpr (sizeof(T) == 4) {
@@ -631,6 +634,8 @@ class Engine : public EngineBase {
                     k_spectral_x_pair<T><<<2 * kp.nj, dim3(bh, std::max(1, sx_threads / bh)), smem_sxp, stream>>>(
                         kp, spec, plan_i, tw_i, sx_pair_layout(NZ));
                 }
+            } else if (sx_threads > 512) {
+                k_spectral_x_1k<T><<<kp.nj, dim3(bx, sx_threads / bx), smem_sx, stream>>>(kp, spec, plan_i, tw_i, psx);
             } else {
                 k_spectral_x<T><<<kp.nj, dim3(bx, std::max(1, sx_threads / bx)), smem_sx, stream>>>(kp, spec, plan_i,
                                                                                                    tw_i, psx);
@@ -996,9 +1001,12 @@ class Engine : public EngineBase {
                 int bt = keep;
                 bool bp = false;
                 sx_pair = false;
-                sx_threads = 512;
-                float t = timeit([&] { solve_pressure(1. / 3.); });
-                if (t < bx) { bx = t; bt = 512; }
+                for (int nt : {512, 1024}) {
+                    sx_threads = nt;
+                    const float t = timeit([&] { solve_pressure(1. / 3.); });
+                    if (t < bx) { bx = t; bt = nt; }
+                }
+                float t;
                 if (pair_ok()) {
                     sx_pair = true;
                     for (int nt : {256, 512}) {

@@ -1470,6 +1470,13 @@ __global__ void k_spectral_x(KParams<T> p, typename V2<T>::t *spec, FftPlan pi, 
 {
     spectral_x_body(p, spec, pi, tw, ps, blockIdx.x);
 }
+// the same with registers sized for blocks of up to 1024 threads
+template <typename T>
+__global__ void __launch_bounds__(1024) k_spectral_x_1k(KParams<T> p, typename V2<T>::t *spec, FftPlan pi,
+                                                        const typename V2<T>::t *tw, int ps)
+{
+    spectral_x_body(p, spec, pi, tw, ps, blockIdx.x);
+}
 
 // inverse FFT along y + PI = real part, with the level copies of
 // poisson_fft3d (pressure.cpp:878-892) and the lateral placement of

@@ -145,17 +145,19 @@ def test_post_quad_matches_column_kernel(monkeypatch, case):
             np.testing.assert_array_equal(b, a, err_msg=f"{case} field {f} slot {slot}")
 
 
+@pytest.mark.parametrize("form", ["pair", "1024"])
 @pytest.mark.parametrize("case", ["thunderstorm_small", "moist_blob_odd"])
-def test_spectral_x_pair_matches_single_cta(monkeypatch, case):
-    """the fused x kernel as CTA pairs (GA_SPECTRAL_X=pair) against one CTA
-    per y-wavenumber: whole steps bit for bit (an odd interior size splits
-    the lines and the columns unevenly)"""
+def test_spectral_x_pair_matches_single_cta(monkeypatch, case, form):
+    """the fused x kernel as CTA pairs (GA_SPECTRAL_X=pair) or as one block
+    of 1024 threads (GA_SPECTRAL_X=1024) against one 256-thread CTA per
+    y-wavenumber: whole steps bit for bit (an odd interior size splits the
+    lines and the columns unevenly)"""
     if case == "thunderstorm_small":
         wl = configs.thunderstorm(nx=44, ny=38, nsteps=4)
     else:
         wl = configs.moist_blob(nx=31, ny=27, nz=17, nsteps=4)
     ms = []
-    for mode in ("single", "pair"):
+    for mode in ("single", form):
         monkeypatch.setenv("GA_SPECTRAL_X", mode)
         ms.append(anelastic.Model(wl, abi.GA_PREC_F32))
     monkeypatch.delenv("GA_SPECTRAL_X")
