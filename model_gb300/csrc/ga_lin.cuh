@@ -268,9 +268,10 @@ struct Lin : LinBase {
         cudaStream_t s = e.stream;
         k_adj_fft_y_in<T><<<dim3(nkt_y, e.kp.ni), by_y, e.smem_y, s>>>(e.kp, lpi_f, e.spec, e.plan_j, e.tw_j, e.KTy);
         if (e.psx > 0) {  // x transforms and the solves fused, as in the forward step
-            const int nl = e.NZ - 2, bx = std::min(nl, 64);
-            k_spectral_x_adj<T><<<e.kp.nj, dim3(bx, std::max(1, e.sx_threads / bx)), e.smem_sx, s>>>(e.kp, e.spec, e.plan_i,
-                                                                                          e.tw_i, e.psx);
+            // the adjoint kernel's registers allow blocks of up to 512 threads
+            const int nl = e.NZ - 2, bx = std::min(nl, 64), nt = std::min(e.sx_threads, 512);
+            k_spectral_x_adj<T><<<e.kp.nj, dim3(bx, std::max(1, nt / bx)), e.smem_sx, s>>>(e.kp, e.spec, e.plan_i,
+                                                                                         e.tw_i, e.psx);
             e.launches += 1;
         } else {
             k_fft_x<T><<<dim3(nkt_x, e.kp.nj), by_x, e.smem_x, s>>>(e.kp, e.spec, e.plan_i, e.tw_i, 0, e.KTx);

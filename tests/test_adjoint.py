@@ -463,3 +463,24 @@ def test_gpu_adjoint_quad_kernel_matches_level_kernel(built, monkeypatch, case):
     monkeypatch.delenv("GA_ADJ")
     for k in outs[0]:
         np.testing.assert_array_equal(outs[1][k], outs[0][k], err_msg=str(k))
+
+
+
+@pytest.mark.gpu
+def test_gpu_adjoint_after_1024_thread_forward_x_solve(built, monkeypatch):
+    """a context whose fused forward x solve runs 1024-thread blocks
+    (GA_SPECTRAL_X=1024, an autotuner candidate) runs its adjoint x solve in
+    blocks the adjoint kernel's registers allow, with the same gradient bit
+    for bit"""
+    wl = small_vortex(nx=24, ny=20, nz=12)
+    st, y = trajectory_state(wl), random_dirs(wl, 22)
+    outs = []
+    for mode in ("single", "1024"):
+        monkeypatch.setenv("GA_SPECTRAL_X", mode)
+        m = _model(wl, st, abi.GA_PREC_F32)
+        m.lin_set_all(y)
+        m.adjoint(4, 2)
+        outs.append(m.lin_get_all())
+    monkeypatch.delenv("GA_SPECTRAL_X")
+    for k in outs[0]:
+        np.testing.assert_array_equal(outs[1][k], outs[0][k], err_msg=str(k))
