@@ -381,6 +381,11 @@ def adjoint_bench(torch, device, steps, every, moist=False, size=512):
                      "device_gb_in_use": round((total - free) / 1e9, 1),
                      "fwd_adj_ms_one_resident": round(t_adj1, 2),
                      "fwd_adj_over_fwd_one_resident": round(t_adj1 / t_fwd, 3)}
+        if moist and prec == abi.GA_PREC_F32:
+            # the forward against the HBM roofline by the 540 B/gridpoint-step model
+            peak, peak_kind = load_peaks()
+            out[name]["hbm_fraction_fwd"] = round(pts / (t_fwd * 1e-3) * STEP_BYTES_FP32_MOIST / 1e9 / peak, 4)
+            out[name]["hbm_peak"] = {"gbs": peak, "source": peak_kind}
         m.close()
     return out
 
