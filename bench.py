@@ -146,6 +146,14 @@ def allreduce_max(dist, x: float, device) -> float:
     return float(t.item())
 
 
+def replica_result(dist, ms_local: float, world: int, points: int, steps: int, device):
+    """Replicas: every rank integrates its own domain, so the job advanced
+    world x points x steps gridpoint-steps in the slowest rank's time.
+    Returns (max over ranks of the timed ms, whole-job gridpoint-steps/s)."""
+    ms = allreduce_max(dist, float(ms_local), device)
+    return ms, world * points * steps / (ms * 1e-3)
+
+
 # ---------------------------------------------------------------------------
 def time_steps(model, torch, steps, flush, profile=False):
     """Per-step CUDA-event times (ms) on the library's stream, with an L2
@@ -469,11 +477,10 @@ def run_ours(args):
     barrier(dist)
     clocks = sampler.stop()
     launches = model.launch_count() - l0
-    ms_total = allreduce_max(dist, float(sum(per)), f"cuda:{device}")
+    ms_total, value = replica_result(dist, float(sum(per)), world, wl.points, args.steps, f"cuda:{device}")
     rc = model.check_finite()
     if rc != 0:
         raise RuntimeError("non-finite state after the timed steps")
-    value = world * wl.points * args.steps / (ms_total * 1e-3)
 
     if rank != 0:
         if dist is not None:
