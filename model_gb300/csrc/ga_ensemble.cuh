@@ -605,31 +605,31 @@ class Ensemble : public EnsembleBase {
                 refresh_tables();
                 build_prefixes();
             }
-            // the fused x kernel's block size, then the unfused x solve for
-            // each x level tile
-            const int keep_unfused = sx_unfused;
+            // the x solve: the fused kernel's block sizes (when every member
+            // fits it), then the unfused solve for each x level tile
+            float bxs = 1e30f;
+            int bu = sx_unfused, bkx = KTx, bt = sx_threads;
             if (fused_ok) {
                 sx_unfused = 0;
-                const int keep = sx_threads;
-                sx_threads = 512;
-                const float t = timeit(chain);
-                if (t < best) best = t;
-                else sx_threads = keep;
+                for (int nt : {256, 512}) {
+                    sx_threads = nt;
+                    const float t = timeit(chain);
+                    if (t < bxs) { bxs = t; bu = 0; bt = nt; }
+                }
             }
-            sx_unfused = keep_unfused;
-            if (sx_unfused) best = timeit(chain);  // the default when GA_SPECTRAL_X=unfused
-            int bu = sx_unfused, bkx = KTx;
             for (int kt = 1; kt <= 64; kt <<= 1) {
                 if (!ktx_fits(kt)) break;
                 sx_unfused = 1;
                 KTx = kt;
                 build_prefixes();
                 const float t = timeit(chain);
-                if (t < best) { best = t; bu = 1; bkx = kt; }
+                if (t < bxs) { bxs = t; bu = 1; bkx = kt; }
             }
             sx_unfused = bu;
             KTx = bkx;
+            sx_threads = bt;
             build_prefixes();
+            best = bxs;
             if (sx_unfused)
                 std::snprintf(line, sizeof line, "y level tile %d, x level tile %d (pressure solve %.3f ms)", bk, KTx,
                               best);
