@@ -27,6 +27,7 @@ import json
 import os
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -79,7 +80,7 @@ class ClockSampler:
     def __init__(self, index: int):
         self.index = index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        self.path = os.path.join(tempfile.gettempdir(), f"ga_clocks_{os.getpid()}.csv")
 
     def start(self):
         try:
@@ -267,7 +268,7 @@ def e2e_jobs(model_cls, wl, prec, torch, jobs, job_steps, device):
 
 
 def ensemble_bench(torch, device, steps, warmup, n_small=64, n_large=32):
-    """Uneven ensemble (configs[3]): n_small members at 96x96x40 and n_large at
+    """Uneven ensemble: n_small members at 96x96x40 and n_large at
     160x160x48, FP32, Kessler, batched kernels + CUDA graph.  The state
     (about 8 GB) is far larger than L2, so no flush is needed."""
     from model_gb300 import abi, anelastic, configs

@@ -3,7 +3,7 @@
 The reference has no linearisation, so its checks are mathematical:
   - the TLM against central finite differences of the forward step;
   - the adjoint against the TLM by the dot-product test <L x, y> = <x, L^T y>
-    (north star: 1e-8 in FP64);
+    (to 1e-8 in FP64);
   - the GPU TLM / adjoint (gather form) against the oracle's (scatter form,
     oracle/ga_oracle_lin.c), whose forward step is pinned to the reference;
   - checkpointing changes nothing: the recomputed trajectory is bit-identical;

@@ -6,7 +6,7 @@ Tolerances (relative L2 over a whole field, FP64):
     (the FP64 kernels are compiled without FMA contraction and keep the
     reference's evaluation order);
   - operators with CUDA pow/exp (Kessler, fall speed) or the FFT: 1e-12;
-  - full steps: 1e-10 (the benchmark spec bound for the plain FP64 path).
+  - full steps: 1e-10 (the bound for the plain FP64 path).
 """
 import numpy as np
 import pytest
