@@ -218,13 +218,18 @@ GA_API void *ga_field_device_ptr(ga_ctx *ctx, int field, int slot);
 
 /*
  * Autotuner.  No counterpart in the reference.  ga_tune times the candidate
- * tile shapes and FFT plans of this context on its current state (advection
- * tile 4x4, 2x4, 4x2, 4x8, 8x4; the level tile of the y transforms; the
- * factor order of the x and y FFTs; the x level tile when the x transform is
- * not fused with the solve) and keeps the fastest.  The state is unchanged.
- * Every tile gives bit-identical results; the FFT factor orders round
- * differently (FP64: ~1e-15).  ga_tuning writes the current choice as text
- * (NUL-terminated, truncated to n bytes).
+ * kernels, tile shapes and FFT plans of this context on its current state and
+ * keeps the fastest: the advection kernel and tile (per-level tiles 4x4, 2x4,
+ * 4x2, 4x8, 8x4; in FP32 with NZ % 4 == 0 the four-level kernel with tiles
+ * 4x4, 4x8, 8x4, 2x8, 8x8, each at two register budgets, with east and north
+ * faces per work item or by sliding row segments); the level tile of the y
+ * transforms; the factor order of the x and y FFTs; the fused x solve's block
+ * (256, 512 or 1024 threads; FP32: also as CTA pairs) against the unfused x
+ * transforms and solve with each x level tile.  L2 is written over before each
+ * candidate's timed launches, as a step that starts from DRAM sees it.  The
+ * state is unchanged.  Every kernel and tile gives bit-identical results; the
+ * FFT factor orders round differently (FP64: ~1e-15).  ga_tuning writes the
+ * current choice as text (NUL-terminated, truncated to n bytes).
  */
 GA_API int ga_tune(ga_ctx *ctx);
 GA_API int ga_tuning(ga_ctx *ctx, char *buf, size_t n);
@@ -293,7 +298,8 @@ GA_API int ga_ensemble_synchronize(ga_ens *ens);
 GA_API void *ga_ensemble_stream(ga_ens *ens);
 GA_API long long ga_ensemble_launch_count(ga_ens *ens);
 GA_API int ga_ensemble_get_counters(ga_ens *ens, int member, long long *bigcounter, double *mtime);
-/* Autotuner of the batched step (advection tile, y level tile), as ga_tune. */
+/* Autotuner of the batched step (advection kernel and tile, y level tile, fused or
+ * unfused x solve), as ga_tune, over all members. */
 GA_API int ga_ensemble_tune(ga_ens *ens);
 GA_API int ga_ensemble_tuning(ga_ens *ens, char *buf, size_t n);
 
