@@ -37,7 +37,8 @@ sys.path.insert(0, ROOT)
 
 METRIC = "gridpoint-steps/s (fwd, fwd+adjoint) FP32 vs FP64 at stated err; %HBM peak"
 UNIT = "gridpoint-steps/s"
-WORKLOAD_DESC = "Kessler thunderstorm 128x128x48, dx=dy=1 km, dz=400 m, dt=4 s, 600-step run"
+WORKLOAD_DESC = ("Kessler thunderstorm 128x128x48, dx=dy=1 km, dz=400 m, dt=4 s; value: --steps steps from the "
+                 "initial state; e2e and accuracy: whole 600-step runs")
 DATA = "synthetic: seeded thunderstorm sounding (theta 300->343 K, RH 0.95->0.25, u 0->15 m/s) + 3 K warm bubble + U(+-0.05 K) noise"
 L2_FLUSH_BYTES = 256 << 20
 
@@ -50,9 +51,11 @@ PASSES_DRY = {"advect": 12, "div_fft_y": 5, "fft_x": 4, "thomas": 4, "ifft_y_pi"
               "kessler": 0}
 PASSES_MOIST = {"advect": 22, "div_fft_y": 5, "fft_x": 4, "thomas": 4, "ifft_y_pi": 3, "post": 16,
                 "kessler": 12}
-# DRAM bytes per launch (read + write) of the dominant kernel, from one ncu
-# capture of the bench command (cold cache): workload -> (kernel group, bytes, summary)
-TRAFFIC_NCU = {"thunderstorm": ("advect", 50.01e6, "profiles/forward_kernels_thunderstorm_128x128x48_fp32.md")}
+# DRAM bytes per launch (read + write) of the dominant kernel, copied from one
+# ncu capture of the bench command (cold cache) into this table; a run does not
+# measure it.  workload -> (kernel group, kernel, bytes, summary)
+TRAFFIC_NCU = {"thunderstorm": ("advect", "k_advect_quad<4,8,4>", 50.01e6,
+                                "profiles/forward_kernels_thunderstorm_128x128x48_fp32.md")}
 # compulsory bytes per gridpoint-step of an ideally fused step (FP32 moist)
 STEP_BYTES_FP32_MOIST = 540.0
 
@@ -206,7 +209,8 @@ def roofline(groups, wl, prec_bytes, peak_gbs, peak_kind, workload=None):
     table = {k: {"ms_per_launch": round(v["ms"] / v["launches"], 5), "share": round(v["ms"] / sum(
         x["ms"] for x in groups.values()), 4)} for k, v in groups.items()}
     tr = TRAFFIC_NCU.get(workload)
-    traffic, source = (tr[1], tr[2]) if tr and tr[0] == dom and prec_bytes == 4 else (None, None)
+    traffic, source = (tr[2], f"ncu capture of {tr[1]} summarised in {tr[3]}, copied into bench.py; "
+                       "not measured by this run") if tr and tr[0] == dom and prec_bytes == 4 else (None, None)
     out = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak_gbs, "unit": "GB/s",
            "frac": round(achieved / peak_gbs, 4), "peak_source": peak_kind,
            "algorithmic_bytes_per_launch": int(nbytes), "ms_per_launch": round(per_launch_ms, 5),

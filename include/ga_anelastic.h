@@ -306,25 +306,30 @@ GA_API int ga_ensemble_tuning(ga_ens *ens, char *buf, size_t n);
 /*
  * Pressure solve without device allocation.  No counterpart in the reference:
  * it is for callers that cannot allocate GPU memory themselves or through
- * this library (a host model that owns every byte of device memory in its own
- * pool, a plugin inside a process whose allocator forbids foreign cudaMalloc
- * calls, code running inside a stream capture where an allocation would break
- * the capture).
+ * this library: a host model that owns every byte of device memory in its
+ * own pool and hands none to third-party code, or a plugin inside a process
+ * whose allocator forbids foreign cudaMalloc calls.
  *
  * Runs solve_pressure (pressure.cpp:142-224) in FP64 on caller-owned device
  * arrays [NX][NY][NZ]: up, vp, wp (read, and their lateral boundary points
  * overwritten by the mirror or periodic copy, as the reference does) and pi
- * (written).  cols are host arrays as for ga_create.  The work is queued on
- * `stream` (a cudaStream_t, or NULL for the legacy default stream) on the
- * current CUDA device; the call returns without synchronizing.
+ * (written).  cols are host arrays as for ga_create; their mu, mw, rhou and
+ * rhow columns are read during the call and passed to the GPU by value, so
+ * the caller may free or change them as soon as the call returns.  The work
+ * is queued on `stream` (a cudaStream_t, or NULL for the legacy default
+ * stream) on the current CUDA device; the call returns without synchronizing.
  *
  * All scratch lives in one file-scope device array of GA_NOALLOC_SCRATCH_BYTES
  * that every GPU loading this library holds until the process exits.  The
- * first call on a device looks up that array's device address (once per
- * device); make that first call before any stream capture.  Grids whose
- * spectral buffer and tables exceed the array are rejected with GA_ERR_ARG
- * (for a non-periodic grid: 16*NX*NY*NZ + 8*NX*NY + 16*(NX+NY) bytes plus
- * small column tables, e.g. 128 x 128 x 96 fits).  Calls share the array:
+ * first call on a device looks up that array's device address and sets the
+ * kernels' shared-memory limits (once per device, with that device current).
+ * Grids are rejected with GA_ERR_ARG, before anything is queued, when their
+ * spectral buffer and tables exceed the array (for a non-periodic grid:
+ * 16*NX*NY*NZ + 8*NX*NY + 16*(NX+NY) bytes plus small column tables, e.g.
+ * 128 x 128 x 96 fits) or when a transform line is too long for the 200 KiB
+ * of shared memory per block (NY above about 6400, or a long NX whose levels
+ * also do not fit the unfused x transform).  Calls share the array and it
+ * keeps the last call's contents (each call writes every element it reads):
  * calls that overlap on the GPU race and must be ordered by the caller.
  * The function calls no cudaMalloc, cudaFree or other allocating routine.
  */

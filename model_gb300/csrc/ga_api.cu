@@ -401,11 +401,8 @@ int ga_solve_pressure_noalloc(const ga_config *cfg, const ga_columns *cols, doub
         return fail(GA_ERR_CONFIG, "ga_solve_pressure_noalloc: periodic domains need NX >= 13");
     if (!(cfg->dx > 0 && cfg->dy > 0 && cfg->dz > 0 && cfg->dt > 0) || !(step > 0))
         return fail(GA_ERR_CONFIG, "ga_solve_pressure_noalloc: dx, dy, dz, dt and step must be positive");
-    const size_t need = ga::noalloc_bytes_needed(cfg);
-    if (need > GA_NOALLOC_SCRATCH_BYTES)
-        return fail(GA_ERR_ARG, "ga_solve_pressure_noalloc: grid needs " + std::to_string(need) +
-                                    " bytes of scratch, more than the fixed " +
-                                    std::to_string((size_t)GA_NOALLOC_SCRATCH_BYTES) + " bytes");
+    std::string why;
+    if (ga::noalloc_check(cfg, &why) != GA_OK) return fail(GA_ERR_ARG, "ga_solve_pressure_noalloc: " + why);
     return ga::solve_pressure_noalloc(cfg, cols, up, vp, wp, pi, step, (cudaStream_t)stream);
 }
 

@@ -120,6 +120,9 @@ struct EnsembleBase {
 void set_error(const std::string &msg);
 
 size_t noalloc_bytes_needed(const ga_config *c);
+// GA_OK, or GA_ERR_ARG with the reason when the grid needs more scratch or
+// shared memory per block than the allocation-free solve has
+int noalloc_check(const ga_config *c, std::string *why);
 int solve_pressure_noalloc(const ga_config *c, const ga_columns *cols, double *up, double *vp, double *wp,
                            double *pi, double step, cudaStream_t stream);
 

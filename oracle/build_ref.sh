@@ -1,7 +1,8 @@
 #!/bin/bash
 # Builds the reference's serial step (PARALLEL 0) as a CPU oracle into
 # oracle/_ref/, from the reference's own sources where they lie.
-#   usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
+#   usage: oracle/build_ref.sh [REFERENCE_ROOT]
+#   (default: $GA_REFERENCE_ROOT, else /root/reference)
 # Only include/stdafx.h is copied into the build folder, with PARALLEL set to
 # 0 as the serial Makefile path expects; every other reference file is
 # compiled in place, unmodified.  main.cpp and files.cpp are replaced by
@@ -10,7 +11,7 @@
 # contraction, so x86 and Arm hosts compute the same values.
 # TEST INFRASTRUCTURE: the output is never shipped or called by the library.
 set -euo pipefail
-REF=${1:-/root/reference}
+REF=${1:-${GA_REFERENCE_ROOT:-/root/reference}}
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/_ref"
 if [ ! -f "$REF/source/pressure.cpp" ]; then

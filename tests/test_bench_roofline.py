@@ -25,8 +25,8 @@ def test_roofline_of_the_dominant_group():
     assert r["achieved"] == pytest.approx(nbytes / 0.05e-3 / 1e9, abs=0.1)
     assert r["frac"] == pytest.approx(r["achieved"] / 6757.2, abs=1e-4)
     assert sum(g["share"] for g in r["groups"].values()) == pytest.approx(1.0, abs=1e-3)
-    assert r["traffic"] == bench.TRAFFIC_NCU["thunderstorm"][1]
-    assert r["traffic_source"].startswith("profiles/")
+    assert r["traffic"] == bench.TRAFFIC_NCU["thunderstorm"][2]
+    assert "profiles/" in r["traffic_source"] and "not measured by this run" in r["traffic_source"]
 
 
 def test_roofline_traffic_only_where_it_was_captured():
