@@ -27,6 +27,13 @@ P0 = 100000.0
 GRAV = 9.8
 PRESSFC = 100200.0
 
+# theta anomalies (K) of the monsoon vortex, in the ratio of the reference's
+# example call (2.5, -2.05; data_initializer.cpp:809), scaled once (by 1.55105)
+# so that the maximum wind of the 192 x 128 x 32 state is 5.0 m/s, found 520 km
+# from the centre at 3.9 km
+VORTEX_TMAX = 3.8776
+VORTEX_TMIN = -3.1796
+
 _SM_GAMMA = np.uint64(0x9E3779B97F4A7C15)
 _SM_M1 = np.uint64(0xBF58476D1CE4E5B9)
 _SM_M2 = np.uint64(0x94D049BB133111EB)
@@ -278,20 +285,18 @@ def moist_blob(nx=24, ny=22, nz=16, dx=1000.0, dz=500.0, dt=4.0, nsteps=3, seed=
     return wl
 
 
-def monsoon_vortex(nx=192, ny=128, nz=32, dx=40000.0, dz=600.0, dt=120.0, nsteps=500, seed=1003,
-                   vort=1.0e-4, upper_shear=-2.0e-3, lower_shear=-1.0e-3, vmax=5.0, rmax=500000.0,
-                   zmax=4000.0, corner_lat=95.0, noise=0.0, moist=False, extra_basic=0.0) -> Workload:
-    """Sheared monsoon-depression state (dry): a zonal jet u(y, z) whose
-    relative vorticity peaks at `vort` (1/s) at the domain's centre latitude,
-    with vertical shear `lower_shear` below and `upper_shear` above the jet
-    level (1/s), theta in thermal-wind balance with it on the stable
-    sounding, and an axisymmetric vortex (max wind `vmax` at radius `rmax`,
-    peaking at height `zmax`).  Written from the description of the
-    reference's ITCZ-shear and vortex initialisers (data_initializer.cpp:
-    298-568, 760-1064); corner_lat places the domain over about 5-35 N.
+def jet_vortex(nx=192, ny=128, nz=32, dx=40000.0, dz=600.0, dt=120.0, nsteps=500, seed=1003,
+               vort=1.0e-4, upper_shear=-2.0e-3, lower_shear=-1.0e-3, vmax=5.0, rmax=500000.0,
+               zmax=4000.0, corner_lat=95.0, noise=0.0, moist=False, extra_basic=0.0) -> Workload:
+    """Analytic sheared jet with a vortex (small test cases of the general
+    basic-state path): a zonal jet u(y, z) whose relative vorticity peaks at
+    `vort` (1/s) at the domain's centre latitude, with vertical shear
+    `lower_shear` below and `upper_shear` above the jet level (1/s), theta in
+    thermal-wind balance with it on the stable sounding, and an axisymmetric
+    vortex (max wind `vmax` at radius `rmax`, peaking at height `zmax`).
     extra_basic > 0 adds smooth horizontally varying VBAR, WBAR and QBAR of
-    that relative size (test cases for the general basic-state path)."""
-    wl = Workload("monsoon_vortex", nx, ny, nz, dx, dx, dz, dt, nsteps, microphysics_option=1 if moist else 0,
+    that relative size.  The benchmark's monsoon state is monsoon_vortex."""
+    wl = Workload("jet_vortex", nx, ny, nz, dx, dx, dz, dt, nsteps, microphysics_option=1 if moist else 0,
                   corner_lat=corner_lat)
     theta = stable_sounding(nz, dz)
     qv = thunderstorm_sounding(nz, dz)[1] if moist else np.zeros(nz)
@@ -348,6 +353,41 @@ def monsoon_vortex(nx=192, ny=128, nz=32, dx=40000.0, dz=600.0, dt=120.0, nsteps
     return wl
 
 
+def monsoon_vortex(nx=192, ny=128, nz=32, dx=40000.0, dz=600.0, dt=120.0, nsteps=500, seed=1003,
+                   corner_lat=86.0, corner_lon=53.0, hor_shear=1.0e-4, vert_shear0=-2.0e-3,
+                   vert_shear1=-1.0e-3, vortex_lat=20.0, vortex_lon=88.0, r_end=2.0e6, zm=4000.0, zt=11000.0,
+                   tmax=VORTEX_TMAX, tmin=VORTEX_TMIN, noise=0.0) -> Workload:
+    """Sheared monsoon-depression state (dry): the reference's ITCZ-shear
+    basic state (initialize_basic_state_ITCZ_shear2(hor_shear, vert_shear0,
+    vert_shear1), data_initializer.cpp:298-568: vorticity strip at 18-21 N,
+    streamfunction inversion, vertical shear about a 4 km level, geostrophic
+    pressure and hydrostatic theta from the 20 N / 88 E column) and the
+    reference's axisymmetric vortex (initialize_vortex, :862-1064) at
+    (vortex_lat, vortex_lon) with radius r_end, its wind maximum at zm and
+    theta anomalies tmax (warm, above zm) and tmin (cold, below); restated in
+    model_gb300/monsoon.py.  corner_lat / corner_lon place the domain (the
+    reference's latoffset / lonoffset, initializer.cpp:181-182): with the
+    defaults 192 x 128 points of 40 km span 53.4-122.6 E and 3.1 S-42.7 N,
+    centred on the 20 N / 88 E column.  The default anomalies give a maximum
+    wind of 5 m/s at about 500 km from the centre, at 4 km."""
+    from model_gb300 import monsoon
+    wl = Workload("monsoon_vortex", nx, ny, nz, dx, dx, dz, dt, nsteps, microphysics_option=0,
+                  corner_lat=corner_lat)
+    st = monsoon.itcz_shear_state(nx, ny, nz, dx, dz, corner_lat, corner_lon, hor_shear, vert_shear0, vert_shear1)
+    f = wl.fields
+    f["tb_in"] = st["tb"].copy()
+    f["qb_in"] = st["qb"].copy()
+    for k in ("ubar", "vbar", "wbar", "thbar", "qbar", "pbar"):
+        f[k] = st[k]
+    _zero_perturbation(wl)
+    xpos = monsoon._nearest(st["lons"], vortex_lon)
+    ypos = monsoon._nearest(st["lats"], vortex_lat)
+    f["u"], f["v"], f["th"] = monsoon.vortex(st, nx, ny, nz, dx, dz, r_end, zm, zt, tmax, tmin, xpos, ypos)
+    if noise > 0:
+        _add_noise(wl, seed, noise)
+    return wl
+
+
 def ensemble_member(m: int, nx: int, ny: int, nz: int = 48, dz: float = 400.0, nsteps: int = 300,
                     base_seed: int = 1004) -> Workload:
     """Member m of the uneven ensemble: the thunderstorm sounding and bubble
@@ -372,6 +412,7 @@ WORKLOADS = {
     "squall_line": squall_line,
     "moist_blob": moist_blob,
     "monsoon_vortex": monsoon_vortex,
+    "jet_vortex": jet_vortex,
 }
 
 

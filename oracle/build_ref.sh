@@ -18,9 +18,14 @@ if [ ! -f "$REF/source/pressure.cpp" ]; then
     echo "reference sources not found under $REF" >&2
     exit 3
 fi
-mkdir -p "$OUT/include" "$OUT/obj"
+mkdir -p "$OUT/include" "$OUT/include_par" "$OUT/obj"
 sed 's/^#define PARALLEL 1/#define PARALLEL 0/' "$REF/include/stdafx.h" > "$OUT/include/stdafx.h"
 grep -q '^#define PARALLEL 0' "$OUT/include/stdafx.h"
+# the monsoon initialisers (data_initializer.cpp) fill the parallel build's
+# full-domain arrays; a second copy with ENERGY 1 selects that macro mapping
+# while keeping the serial index arithmetic (oracle/ref/itcz_harness.cpp)
+sed 's/^#define ENERGY 0/#define ENERGY 1/' "$OUT/include/stdafx.h" > "$OUT/include_par/stdafx.h"
+grep -q '^#define ENERGY 1' "$OUT/include_par/stdafx.h"
 CXXFLAGS="-O3 -ffp-contract=off -w -I$OUT/include -I$HERE/ref/shim -I$REF/include"
 SRCS="solver initializer data_initializer interpolate fluxes pressure advection turbulence damping
       boundaries util Heating kessler rutledge microphysics energy trajectory laplacian
@@ -30,9 +35,15 @@ for s in $SRCS; do
     g++ $CXXFLAGS -c "$REF/source/$s.cpp" -o "$OUT/obj/$s.o" & pids+=($!)
 done
 g++ $CXXFLAGS -c "$HERE/ref/ref_harness.cpp" -o "$OUT/obj/ref_harness.o" & pids+=($!)
+PARFLAGS="-O3 -ffp-contract=off -w -I$OUT/include_par -I$HERE/ref/shim -I$REF/include"
+mkdir -p "$OUT/obj_par"
+g++ $PARFLAGS -c "$REF/source/data_initializer.cpp" -o "$OUT/obj_par/data_initializer.o" & pids+=($!)
+g++ $CXXFLAGS -c "$HERE/ref/itcz_harness.cpp" -o "$OUT/obj_par/itcz_harness.o" & pids+=($!)
 g++ $CXXFLAGS -c "$HERE/ref/fftw_shim.cpp" -o "$OUT/obj/fftw_shim.o" & pids+=($!)
 g++ $CXXFLAGS -c "$HERE/ref/files_stub.cpp" -o "$OUT/obj/files_stub.o" & pids+=($!)
 gcc -O3 -ffp-contract=off -c "$HERE/ora_fft.c" -o "$OUT/obj/ora_fft.o" & pids+=($!)
 for p in "${pids[@]}"; do wait "$p"; done
 g++ -o "$OUT/ref_harness" "$OUT"/obj/*.o -lm
-echo "built $OUT/ref_harness"
+COMMON_OBJS=$(ls "$OUT"/obj/*.o | grep -v -e '/data_initializer.o$' -e '/ref_harness.o$')
+g++ -o "$OUT/itcz_harness" $COMMON_OBJS "$OUT"/obj_par/*.o -lm
+echo "built $OUT/ref_harness $OUT/itcz_harness"

@@ -34,7 +34,7 @@ RUN_CASES = {
     "moist_rf2": (lambda: configs.moist_blob(nx=14, ny=13, nz=10, rain_fallout=2), 4),
     "moist_periodic": (lambda: configs.moist_blob(nx=18, ny=13, nz=10, periodic=1), 3),
     # horizontally varying basic state (jet + balanced theta), moist: the general path
-    "jet": (lambda: configs.monsoon_vortex(nx=16, ny=14, nz=10, dx=20000.0, dz=800.0, dt=30.0, rmax=60000.0,
+    "jet": (lambda: configs.jet_vortex(nx=16, ny=14, nz=10, dx=20000.0, dz=800.0, dt=30.0, rmax=60000.0,
                                            vmax=8.0, moist=True, noise=0.3, extra_basic=1.0), 3),
 }
 
@@ -86,7 +86,7 @@ def _ops_state(wl, seed: int) -> dict:
 
 def make_ops():
     cases = {
-        "jet": configs.monsoon_vortex(nx=16, ny=14, nz=10, dx=20000.0, dz=800.0, dt=30.0, rmax=60000.0,
+        "jet": configs.jet_vortex(nx=16, ny=14, nz=10, dx=20000.0, dz=800.0, dt=30.0, rmax=60000.0,
                                       vmax=8.0, moist=True, noise=0.3, extra_basic=1.0),
         "moist": configs.moist_blob(nx=14, ny=13, nz=10),
         "moist_periodic_rf2": configs.moist_blob(nx=18, ny=13, nz=10, periodic=1, rain_fallout=2),

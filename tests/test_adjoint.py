@@ -33,7 +33,7 @@ def small_vortex(**kw):
     args = dict(nx=16, ny=14, nz=10, dx=20000.0, dz=800.0, dt=30.0, rmax=60000.0, vmax=8.0, noise=0.3,
                 extra_basic=1.0)
     args.update(kw)
-    return configs.monsoon_vortex(**args)
+    return configs.jet_vortex(**args)
 
 
 def trajectory_state(wl, seed=77):
