@@ -6,13 +6,17 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <memory>
+#include <tuple>
 #include <string>
 #include <vector>
 
 #include "ga_engine.h"
 #include "ga_kernels.cuh"
 #include "ga_quad.cuh"
+
+#include <cudaTypedefs.h>
 
 namespace ga {
 
@@ -107,6 +111,10 @@ class Engine : public EngineBase {
     int adv_quad = 1, adv_qi = 4, adv_qj = 8, adv_force = 0;
     int adv_qb = 3;  // blocks per SM the four-level kernel's registers are sized for (3 or 4)
     int adv_rows = 0;  // four-level kernel: east and north faces by sliding rows (ADV_ROWS)
+    // the four-level kernel with the current fields staged into shared memory
+    // by the tensor memory accelerator (k_advect_tma), and its candidate
+    int adv_tma = 0, adv_tmc = 0;
+    std::map<std::tuple<const void *, int, int, int>, CUtensorMap> tma_maps;  // per buffer and box
     // the four-level post-processing kernel (FP32, NZ % 4 == 0); GA_POST=column
     // keeps the per-level one
     bool post_quad = true;
@@ -166,7 +174,7 @@ class Engine : public EngineBase {
         for (int b = 0; b < 6; b++) bar[b] = dalloc<T>(N);
         vt = dalloc<T>(N);
         accrain = dalloc<double>((size_t)NX * NY);
-        d_err = dalloc<int>(1);
+        d_err = dalloc<int>(2);  // [0] Kessler, [1] staging (kErrStaging)
         const int periodic = c->periodic_ew_boundaries;
         const int ni = periodic ? NX - 6 : NX, nj = NY;
         spec = dalloc<T2>((size_t)ni * nj * NZ);
@@ -326,7 +334,13 @@ class Engine : public EngineBase {
         if (const char *ev = std::getenv("GA_ADVECT")) {
             if (!std::strcmp(ev, "tile")) adv_force = 1;
             else if (!std::strcmp(ev, "quad")) adv_force = 2;
+            else if (!std::strcmp(ev, "tma")) adv_force = 3;
         }
+        if (const char *ev = std::getenv("GA_ADVECT_TMA")) {  // default staged candidate 0..3
+            const int c = std::atoi(ev);
+            if (c >= 0 && c < 4) adv_tmc = c;
+        }
+        adv_tma = adv_force == 3;
         adv_quad = adv_force != 1;
         if (const char *ev = std::getenv("GA_ADVECT_BLOCKS")) adv_qb = std::atoi(ev) == 4 ? 4 : 3;
         if (const char *ev = std::getenv("GA_ADVECT_TILE")) {  // default four-level tile, "TIxTJ"
@@ -348,6 +362,7 @@ class Engine : public EngineBase {
         }
         if constexpr (sizeof(T) == 4) {
             for (auto &tl : kQuadTiles) quad_attr(tl[0], tl[1], optin);
+            tma_attr(optin);
         }
         cudaFuncSetAttribute(k_div_fft_y<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
         cudaFuncSetAttribute(k_ifft_y_pi<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
@@ -487,11 +502,12 @@ class Engine : public EngineBase {
             set_error(std::string("CUDA: ") + cudaGetErrorString(e));
             return GA_ERR_CUDA;
         }
-        return GA_OK;
+        return staging_status();
     }
 
     int launch_status()
     {
+        if (status != GA_OK) return status;
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) {
             set_error(std::string("CUDA launch: ") + cudaGetErrorString(e));
@@ -564,6 +580,111 @@ class Engine : public EngineBase {
         else if (ti == 2 && tj == 8) quad_attr_t<2, 8>(optin);
         else if (ti == 8 && tj == 8) quad_attr_t<8, 8>(optin);
     }
+    // the staged kernel's candidates: tile, level slab and the blocks per SM
+    // its registers are sized for (its shared memory admits as many, moist,
+    // for NZ up to 64)
+    struct TmaCand {
+        int ti, tj, kz, mb;
+    };
+    static constexpr TmaCand kTmaCands[4] = {{4, 4, 8, 4}, {4, 8, 8, 2}, {8, 8, 8, 2}, {4, 4, 16, 2}};
+
+    // cuTensorMapEncodeTiled from the driver, looked up once per process
+    static PFN_cuTensorMapEncodeTiled_v12000 tma_encoder()
+    {
+        static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+        static bool looked = false;
+        if (!looked) {
+            looked = true;
+            void *ptr = nullptr;
+            cudaDriverEntryPointQueryResult q;
+            if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &ptr, 12000, cudaEnableDefault, &q) ==
+                    cudaSuccess &&
+                q == cudaDriverEntryPointSuccess)
+                fn = (PFN_cuTensorMapEncodeTiled_v12000)ptr;
+        }
+        return fn;
+    }
+    // the tensor map of one [NX][NY][NZ] FP32 buffer with a box of bk x bj x bi
+    // points (k, j, i), cached per buffer and box
+    bool tma_map(const T *ptr, int bi, int bj, int bk, CUtensorMap *out)
+    {
+        const auto key = std::make_tuple((const void *)ptr, bi, bj, bk);
+        auto it = tma_maps.find(key);
+        if (it != tma_maps.end()) {
+            *out = it->second;
+            return true;
+        }
+        PFN_cuTensorMapEncodeTiled_v12000 enc = tma_encoder();
+        if (!enc) return false;
+        CUtensorMap m;
+        const cuuint64_t dims[3] = {(cuuint64_t)NZ, (cuuint64_t)NY, (cuuint64_t)NX};
+        const cuuint64_t strides[2] = {(cuuint64_t)NZ * sizeof(T), (cuuint64_t)NY * NZ * sizeof(T)};
+        const cuuint32_t box[3] = {(cuuint32_t)bk, (cuuint32_t)bj, (cuuint32_t)bi};
+        const cuuint32_t estr[3] = {1, 1, 1};
+        const CUresult r = enc(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, (void *)ptr, dims, strides, box, estr,
+                               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                               CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS) return false;
+        tma_maps[key] = m;
+        *out = m;
+        return true;
+    }
+    template <int TI, int TJ, int KZ, int MB>
+    void launch_advect_tma(T step, T sdtg, int what)
+    {
+        if constexpr (sizeof(T) == 4) {
+            using A = AQTma<TI, TJ, KZ>;
+            const int nf = kp.moist ? 7 : 4;
+            KFields<T> F = fields();
+            TmaMaps maps;
+            std::memset(&maps, 0, sizeof(maps));
+            for (int f = 0; f < nf; f++)
+                if (!tma_map(F.cur[f], A::BI, A::BJ, A::BK, &maps.m[f])) {
+                    status = GA_ERR_CUDA;
+                    set_error("advection: cuTensorMapEncodeTiled failed");
+                    return;
+                }
+            dim3 grid(cdiv(NX - 6, TI), cdiv(NY - 6, TJ), cdiv(NZ, KZ));
+            const size_t sm = advect_tma_smem(TI, TJ, KZ, NZ, nf);
+            k_advect_tma<TI, TJ, KZ, MB><<<grid, AQ_THREADS, sm, stream>>>(maps, kp, F, step, sdtg, what, d_err + 1);
+        }
+    }
+    void launch_advect_tma_cand(int c, T step, T sdtg, int what)
+    {
+        switch (c) {
+        case 0: launch_advect_tma<4, 4, 8, 4>(step, sdtg, what); break;
+        case 1: launch_advect_tma<4, 8, 8, 2>(step, sdtg, what); break;
+        case 2: launch_advect_tma<8, 8, 8, 2>(step, sdtg, what); break;
+        default: launch_advect_tma<4, 4, 16, 2>(step, sdtg, what); break;
+        }
+    }
+    static void tma_attr(int optin)
+    {
+        cudaFuncSetAttribute(k_advect_tma<4, 4, 8, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+        cudaFuncSetAttribute(k_advect_tma<4, 8, 8, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+        cudaFuncSetAttribute(k_advect_tma<8, 8, 8, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+        cudaFuncSetAttribute(k_advect_tma<4, 4, 16, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+    }
+    // the staged kernel applies where the four-level one does, with the
+    // driver's tensor-map encoder and the candidate's shared memory
+    bool tma_ok(int c) const
+    {
+        if (!(sizeof(T) == 4 && kp.ubase_adv && NZ % 4 == 0 && c >= 0 && c < 4 && tma_encoder())) return false;
+        const TmaCand &t = kTmaCands[c];
+        return advect_tma_smem(t.ti, t.tj, t.kz, NZ, kp.moist ? 7 : 4) <= 200 * 1024;
+    }
+    // the staging bit of the device error word (a bounded wait ran out)
+    int staging_status()
+    {
+        int e = 0;
+        cudaMemcpy(&e, d_err + 1, sizeof(int), cudaMemcpyDeviceToHost);
+        if (e & kErrStaging) {
+            set_error("advection: a shared-memory staging copy did not complete within its bound");
+            return GA_ERR_CUDA;
+        }
+        return GA_OK;
+    }
+
     // the paired x kernel applies: FP32, the fused path, its shared memory
     bool pair_ok() const { return sizeof(T) == 4 && psx > 0 && smem_sxp <= 200 * 1024; }
     // the four-level kernel applies: FP32, basic state a function of height,
@@ -577,7 +698,9 @@ class Engine : public EngineBase {
     {
         const double sdtg = step * cfg.dt * 9.8 * 0.5;  // step*dt*grav*0.5, advection.cpp:330
         ProfScope ps(this, PC_ADVECT, 1);
-        if (adv_quad && quad_ok(adv_qi, adv_qj)) {
+        if (adv_quad && adv_tma && tma_ok(adv_tmc)) {
+            launch_advect_tma_cand(adv_tmc, (T)step, (T)sdtg, what);
+        } else if (adv_quad && quad_ok(adv_qi, adv_qj)) {
             const T st = (T)step, sg = (T)sdtg;
             const int wq = what | (adv_rows ? ADV_ROWS : 0);
             if (adv_qi == 4 && adv_qj == 4) launch_advect_quad<4, 4>(st, sg, wq);
@@ -919,7 +1042,9 @@ class Engine : public EngineBase {
         {
             float best = 1e30f;
             int bi = adv_ti, bj = adv_tj, bq = 0, qi = adv_qi, qj = adv_qj, qb = adv_qb, br = adv_rows;
-            if (adv_force != 2 || !quad_ok(adv_qi, adv_qj)) {
+            int bt = 0, tc = adv_tmc;
+            adv_tma = 0;
+            if ((adv_force != 2 && adv_force != 3) || !quad_ok(adv_qi, adv_qj)) {
                 adv_quad = 0;
                 for (auto &tl : kAdvTiles) {
                     const size_t sm = advect_tile_smem(tl[0], tl[1], NZ, sizeof(T));
@@ -929,7 +1054,7 @@ class Engine : public EngineBase {
                     if (t < best) { best = t; bi = tl[0]; bj = tl[1]; }
                 }
             }
-            if (adv_force != 1) {
+            if (adv_force == 0 || adv_force == 2) {
                 adv_quad = 1;
                 for (auto &tl : kQuadTiles) {
                     if (!quad_ok(tl[0], tl[1])) continue;
@@ -937,13 +1062,30 @@ class Engine : public EngineBase {
                         for (int rows = 0; rows <= 1; rows++) {
                             adv_qi = tl[0]; adv_qj = tl[1]; adv_qb = mb; adv_rows = rows;
                             const float t = timeit([&] { advect(1. / 3., what); });
-                            if (t < best) { best = t; bq = 1; qi = tl[0]; qj = tl[1]; qb = mb; br = rows; }
+                            if (t < best) { best = t; bq = 1; qi = tl[0]; qj = tl[1]; qb = mb; br = rows; bt = 0; }
                         }
                 }
             }
+            if (adv_force == 0 || adv_force == 3) {
+                adv_quad = 1;
+                adv_tma = 1;
+                for (int c = 0; c < 4; c++) {
+                    if (!tma_ok(c)) continue;
+                    adv_tmc = c;
+                    const float t = timeit([&] { advect(1. / 3., what); });
+                    if (t < best) { best = t; bq = 1; bt = 1; tc = c; }
+                }
+                adv_tma = 0;
+            }
             adv_ti = bi; adv_tj = bj; adv_quad = bq; adv_qi = qi; adv_qj = qj; adv_qb = qb; adv_rows = br;
+            adv_tma = bt; adv_tmc = tc;
             smem_adv = advect_tile_smem(bi, bj, NZ, sizeof(T));
-            if (bq)
+            if (bt) {
+                const TmaCand &t = kTmaCands[tc];
+                std::snprintf(line, sizeof line,
+                              "advect tile %dx%d, %d-level slabs staged by TMA, %d blocks/SM (%.4f ms); ", t.ti, t.tj,
+                              t.kz, t.mb, best);
+            } else if (bq)
                 std::snprintf(line, sizeof line, "advect tile %dx%d, four levels per thread, %d blocks/SM%s (%.4f ms); ",
                               qi, qj, qb, br ? ", face rows" : "", best);
             else std::snprintf(line, sizeof line, "advect tile %dx%d (%.4f ms); ", bi, bj, best);

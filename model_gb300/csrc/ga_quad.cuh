@@ -18,6 +18,7 @@
 // ---------------------------------------------------------------------------
 #pragma once
 #include "ga_kernels.cuh"
+#include "ga_tma.cuh"
 
 #include <cooperative_groups.h>
 
@@ -91,20 +92,78 @@ __host__ __device__ constexpr int aq_field(int fk)
 // basic-state row of a scalar (brow of s_*_ub): 0 theta, 1 qv, -1 none
 __host__ __device__ constexpr int aq_brow(int fk) { return fk == 2 ? 0 : fk == 3 ? 1 : -1; }
 
+// Where the current fields are read from.  at(i, j, k0) is the index of a
+// column quad; ld4 / win read the quad or the 12-level window of field f at
+// column offset (di, dj) from it.
+//
+// GSrc: the fields in global memory, through the read-only path.
+struct GSrc {
+    const KFields<float> &F;
+    int ny, nz, sx, sy;
+    __device__ __forceinline__ GSrc(const KFields<float> &F_, int ny_, int nz_)
+        : F(F_), ny(ny_), nz(nz_), sx(ny_ * nz_), sy(nz_) {}
+    __device__ __forceinline__ int at(int i, int j, int k0) const { return gix(ny, nz, i, j, k0); }
+    __device__ __forceinline__ Q4 ld4(int f, int c, int di, int dj) const
+    {
+        return ldg4(F.cur[f], c + di * sx + dj * sy);
+    }
+    __device__ __forceinline__ Win win(int f, int c, int di, int dj, int k0) const
+    {
+        return ldwin(F.cur[f], c + di * sx + dj * sy, k0, nz);
+    }
+    // stored fall speed at level k0 + e of column (i, j)
+    __device__ __forceinline__ float vt(int i, int j, int k0, int c, int e) const { return F.vt[c + e]; }
+};
+
+// SSrc: halo boxes of the fields in shared memory, [i][j][k] with BJ x BK
+// floats per i, the box of field f at base + f * fs, origin (oi, oj, ok) in
+// global coordinates.  Points outside the field hold zeros, as the windows of
+// GSrc do.
+template <int BJ, int BK>
+struct SSrc {
+    const KFields<float> &F;
+    const float *base;
+    int fs, oi, oj, ok, ny, nz;
+    __device__ __forceinline__ int at(int i, int j, int k0) const { return ((i - oi) * BJ + (j - oj)) * BK + k0 - ok; }
+    __device__ __forceinline__ Q4 ld4(int f, int c, int di, int dj) const
+    {
+        return lds4(base + f * fs + c + (di * BJ + dj) * BK);
+    }
+    __device__ __forceinline__ Win win(int f, int c, int di, int dj, int k0) const
+    {
+        const float *a = base + f * fs + c + (di * BJ + dj) * BK;
+        // the top faces of the quad below a slab (only its last level is
+        // used) would read levels below the box: zeros, as below the column
+        const Q4 lo = k0 - 4 >= ok ? lds4(a - 4) : Q4{{0.f, 0.f, 0.f, 0.f}};
+        const Q4 mi = lds4(a), hi = lds4(a + 4);
+        Win w;
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+            w.v[e] = lo.v[e];
+            w.v[4 + e] = mi.v[e];
+            w.v[8 + e] = hi.v[e];
+        }
+        return w;
+    }
+    __device__ __forceinline__ float vt(int i, int j, int k0, int c, int e) const
+    {
+        return F.vt[gix(ny, nz, i, j, k0) + e];
+    }
+};
+
 // east face (between i and i+1) at levels k0..k0+3: u_east_ub, v_east_ub, s_east_ub
-template <int FK>
-__device__ __forceinline__ Q4 aq_east(const KParams<float> &p, const KFields<float> &F, const float *tab, int i,
-                                      int j, int k0)
+template <int FK, class S>
+__device__ __forceinline__ Q4 aq_east(const KParams<float> &p, const S &src, const float *tab, int i, int j, int k0)
 {
-    const int nz = p.nz, sx = p.ny * nz, sy = nz;
-    const int c = gix(p.ny, nz, i, j, k0);
-    const float *X = F.cur[aq_field(FK)], *U = F.cur[FU];
+    const int nz = p.nz;
+    const int c = src.at(i, j, k0);
+    constexpr int XF = aq_field(FK);
     Q4 x[6];
 #pragma unroll
-    for (int m = 0; m < 6; m++) x[m] = ldg4(X, c + (m - 2) * sx);
+    for (int m = 0; m < 6; m++) x[m] = src.ld4(XF, c, m - 2, 0);
     Q4 r;
     if (FK == 0) {
-        const Q4 up = ldg4(U, c + sx), u0 = ldg4(U, c), uba = lds4(tab + BT_UA * nz + k0),
+        const Q4 up = src.ld4(FU, c, 1, 0), u0 = src.ld4(FU, c, 0, 0), uba = lds4(tab + BT_UA * nz + k0),
                  c6 = lds4(tab + BT_C6_UB * nz + k0);
 #pragma unroll
         for (int e = 0; e < 4; e++) {
@@ -114,7 +173,7 @@ __device__ __forceinline__ Q4 aq_east(const KParams<float> &p, const KFields<flo
             r.v[e] = ua * c6.v[e] + (uba.v[e] + ua) * ue;
         }
     } else if (FK == 1) {
-        const Q4 ua_ = ldg4(U, c + sx), ub_ = ldg4(U, c + sx - sy), uba = lds4(tab + BT_UA * nz + k0),
+        const Q4 ua_ = src.ld4(FU, c, 1, 0), ub_ = src.ld4(FU, c, 1, -1), uba = lds4(tab + BT_UA * nz + k0),
                  c6 = lds4(tab + BT_C6_VB * nz + k0);
 #pragma unroll
         for (int e = 0; e < 4; e++) {
@@ -125,7 +184,7 @@ __device__ __forceinline__ Q4 aq_east(const KParams<float> &p, const KFields<flo
         }
     } else {
         constexpr int BR = aq_brow(FK);
-        const Q4 u1 = ldg4(U, c + sx), ub = lds4(tab + BT_UB * nz + k0);
+        const Q4 u1 = src.ld4(FU, c, 1, 0), ub = lds4(tab + BT_UB * nz + k0);
         const Q4 c6 = BR >= 0 ? lds4(tab + (BT_C6_THB + BR) * nz + k0) : Q4{{0.f, 0.f, 0.f, 0.f}};
 #pragma unroll
         for (int e = 0; e < 4; e++) {
@@ -140,19 +199,18 @@ __device__ __forceinline__ Q4 aq_east(const KParams<float> &p, const KFields<flo
 }
 
 // north face (between j and j+1): u_north_ub, v_north_ub, s_north_ub
-template <int FK>
-__device__ __forceinline__ Q4 aq_north(const KParams<float> &p, const KFields<float> &F, const float *tab, int i,
-                                       int j, int k0)
+template <int FK, class S>
+__device__ __forceinline__ Q4 aq_north(const KParams<float> &p, const S &src, const float *tab, int i, int j, int k0)
 {
-    const int nz = p.nz, sx = p.ny * nz, sy = nz;
-    const int c = gix(p.ny, nz, i, j, k0);
-    const float *X = F.cur[aq_field(FK)], *V = F.cur[FV];
+    const int nz = p.nz;
+    const int c = src.at(i, j, k0);
+    constexpr int XF = aq_field(FK);
     Q4 x[6];
 #pragma unroll
-    for (int m = 0; m < 6; m++) x[m] = ldg4(X, c + (m - 2) * sy);
+    for (int m = 0; m < 6; m++) x[m] = src.ld4(XF, c, 0, m - 2);
     Q4 r;
     if (FK == 0) {
-        const Q4 va_ = ldg4(V, c + sy), vb_ = ldg4(V, c - sx + sy), vba = lds4(tab + BT_VA * nz + k0),
+        const Q4 va_ = src.ld4(FV, c, 0, 1), vb_ = src.ld4(FV, c, -1, 1), vba = lds4(tab + BT_VA * nz + k0),
                  c6 = lds4(tab + BT_C6_UB * nz + k0);
 #pragma unroll
         for (int e = 0; e < 4; e++) {
@@ -162,7 +220,7 @@ __device__ __forceinline__ Q4 aq_north(const KParams<float> &p, const KFields<fl
             r.v[e] = va * c6.v[e] + (vba.v[e] + va) * un;
         }
     } else if (FK == 1) {
-        const Q4 vp = ldg4(V, c + sy), v0 = ldg4(V, c), vba = lds4(tab + BT_VA * nz + k0),
+        const Q4 vp = src.ld4(FV, c, 0, 1), v0 = src.ld4(FV, c, 0, 0), vba = lds4(tab + BT_VA * nz + k0),
                  c6 = lds4(tab + BT_C6_VB * nz + k0);
 #pragma unroll
         for (int e = 0; e < 4; e++) {
@@ -173,7 +231,7 @@ __device__ __forceinline__ Q4 aq_north(const KParams<float> &p, const KFields<fl
         }
     } else {
         constexpr int BR = aq_brow(FK);
-        const Q4 v1 = ldg4(V, c + sy), vb = lds4(tab + BT_VB * nz + k0);
+        const Q4 v1 = src.ld4(FV, c, 0, 1), vb = lds4(tab + BT_VB * nz + k0);
         const Q4 c6 = BR >= 0 ? lds4(tab + (BT_C6_THB + BR) * nz + k0) : Q4{{0.f, 0.f, 0.f, 0.f}};
 #pragma unroll
         for (int e = 0; e < 4; e++) {
@@ -321,18 +379,17 @@ __device__ __forceinline__ void aq_north_row(const KParams<float> &p, const KFie
 
 // top face (between k and k+1) at k = k0..k0+3: u_top_ub, v_top_ub,
 // s_top_ub, r_top_ub; level NZ-1 is not a face of an advected cell (0)
-template <int FK>
-__device__ __forceinline__ Q4 aq_top(const KParams<float> &p, const KFields<float> &F, const float *tab, int i,
-                                     int j, int k0)
+template <int FK, class S>
+__device__ __forceinline__ Q4 aq_top(const KParams<float> &p, const S &src, const float *tab, int i, int j, int k0)
 {
-    const int nz = p.nz, sx = p.ny * nz, sy = nz;
-    const int c = gix(p.ny, nz, i, j, k0);
-    const Win x = ldwin(F.cur[aq_field(FK)], c, k0, nz);
-    const Win w = ldwin(F.cur[FW], c, k0, nz);
+    const int nz = p.nz;
+    const int c = src.at(i, j, k0);
+    const Win x = src.win(aq_field(FK), c, 0, 0, k0);
+    const Win w = src.win(FW, c, 0, 0, k0);
     Q4 r;
     if (FK == 0 || FK == 1) {
         // the second w of the averaged advecting velocity: column i-1 (u) or j-1 (v)
-        const Win w2 = ldwin(F.cur[FW], c - (FK == 0 ? sx : sy), k0, nz);
+        const Win w2 = src.win(FW, c, FK == 0 ? -1 : 0, FK == 0 ? 0 : -1, k0);
         constexpr int C4 = FK == 0 ? BT_C4_UB : BT_C4_VB, H2 = FK == 0 ? BT_H2_UB : BT_H2_VB;
 #pragma unroll
         for (int e = 0; e < 4; e++) {
@@ -389,7 +446,7 @@ __device__ __forceinline__ Q4 aq_top(const KParams<float> &p, const KFields<floa
                     const int kk = k == 0 ? 1 : k;
                     v = fall_speed_point(p, x.at(kk - k0), kk);
                 } else {
-                    v = F.vt[c + e];
+                    v = src.vt(i, j, k0, c, e);
                 }
             }
             vt[e] = v;
@@ -416,21 +473,26 @@ __device__ __forceinline__ Q4 aq_top(const KParams<float> &p, const KFields<floa
 }
 
 // the face columns of field FK into slot `sl` (E, N and T of the tile).
-// rows: east and north faces by row segments of up to AQ_SEG face columns
-// whose stencil slides (fewer loads and less index arithmetic, but a
-// segment's loads one after another); otherwise one work item per face
-// column and quad.  In the row form one loop covers three kinds of work
-// item, each padded to whole warps: east segments (segment, b, quad), north
-// segments (segment, a, quad) and top faces (column, quad).  Both forms
-// evaluate the same expressions.
-template <int TI, int TJ, int FK>
-__device__ __forceinline__ void aq_faces(const KParams<float> &p, const KFields<float> &F, const float *tab,
-                                         float *sl, int i0, int j0, int ti, int tj, bool rows)
+// Level slab: cells ks..ke-1; the slot holds levels kb..ke-1 of every face
+// column at stride SK, where kb = ks, or ks - 4 when the slab starts above
+// the bottom (the divergence of level ks needs the top face of level ks - 1).
+// rows (global source, whole columns only): east and north faces by row
+// segments of up to AQ_SEG face columns whose stencil slides (fewer loads and
+// less index arithmetic, but a segment's loads one after another); otherwise
+// one work item per face column and quad.  In the row form one loop covers
+// three kinds of work item, each padded to whole warps: east segments
+// (segment, b, quad), north segments (segment, a, quad) and top faces
+// (column, quad).  Both forms evaluate the same expressions.
+template <int TI, int TJ, int FK, class S>
+__device__ __forceinline__ void aq_faces(const KParams<float> &p, const KFields<float> &F, const S &src,
+                                         const float *tab, float *sl, int i0, int j0, int ti, int tj, bool rows,
+                                         int ks, int ke, int kb, int SK)
 {
     using G = AQGeom<TI, TJ>;
-    const int nz = p.nz, NQ = nz >> 2;
-    float *E = sl, *N = sl + G::CE * nz, *T = N + G::CN * nz;
-    if (rows) {
+    float *E = sl, *N = sl + G::CE * SK, *T = N + G::CN * SK;
+    const int NQ = (ke - ks) >> 2, NQT = (ke - kb) >> 2;
+    if (rows) {  // GSrc, ks = kb = 0, ke = SK = nz
+        const int nz = p.nz;
         constexpr int SE = (TI + AQ_SEG) / AQ_SEG, SN = (TJ + AQ_SEG) / AQ_SEG;  // segments of TI+1, TJ+1
         const int nE = (SE * TJ * NQ + 31) & ~31, nN = (SN * TI * NQ + 31) & ~31, nall = nE + nN + G::CT * NQ;
         for (int w = threadIdx.x; w < nall; w += AQ_THREADS) {
@@ -444,7 +506,7 @@ __device__ __forceinline__ void aq_faces(const KParams<float> &p, const KFields<
                     aq_north_row<TI, TJ, FK>(p, F, tab, N + a * (TJ + 1) * nz + 4 * q, i0 + a, j0, 4 * q, tj, b0);
             } else {
                 const int v = w - nE - nN, q = v % NQ, col = v / NQ, b = col % TJ, a = col / TJ;
-                if (a < ti && b < tj) sts4(T + col * nz + 4 * q, aq_top<FK>(p, F, tab, i0 + a, j0 + b, 4 * q));
+                if (a < ti && b < tj) sts4(T + col * nz + 4 * q, aq_top<FK>(p, src, tab, i0 + a, j0 + b, 4 * q));
             }
         }
         return;
@@ -452,31 +514,36 @@ __device__ __forceinline__ void aq_faces(const KParams<float> &p, const KFields<
     for (int w = threadIdx.x; w < G::CE * NQ; w += AQ_THREADS) {
         const int q = w % NQ, col = w / NQ, b = col % TJ, a = col / TJ;
         if (a > ti || b >= tj) continue;
-        sts4(E + col * nz + 4 * q, aq_east<FK>(p, F, tab, i0 - 1 + a, j0 + b, 4 * q));
+        const int k0 = ks + 4 * q;
+        sts4(E + col * SK + k0 - kb, aq_east<FK>(p, src, tab, i0 - 1 + a, j0 + b, k0));
     }
     for (int w = threadIdx.x; w < G::CN * NQ; w += AQ_THREADS) {
         const int q = w % NQ, col = w / NQ, b = col % (TJ + 1), a = col / (TJ + 1);
         if (a >= ti || b > tj) continue;
-        sts4(N + col * nz + 4 * q, aq_north<FK>(p, F, tab, i0 + a, j0 - 1 + b, 4 * q));
+        const int k0 = ks + 4 * q;
+        sts4(N + col * SK + k0 - kb, aq_north<FK>(p, src, tab, i0 + a, j0 - 1 + b, k0));
     }
-    for (int w = threadIdx.x; w < G::CT * NQ; w += AQ_THREADS) {
-        const int q = w % NQ, col = w / NQ, b = col % TJ, a = col / TJ;
+    for (int w = threadIdx.x; w < G::CT * NQT; w += AQ_THREADS) {
+        const int q = w % NQT, col = w / NQT, b = col % TJ, a = col / TJ;
         if (a >= ti || b >= tj) continue;
-        sts4(T + col * nz + 4 * q, aq_top<FK>(p, F, tab, i0 + a, j0 + b, 4 * q));
+        const int k0 = kb + 4 * q;
+        sts4(T + col * SK + k0 - kb, aq_top<FK>(p, src, tab, i0 + a, j0 + b, k0));
     }
 }
 
 // flux divergence of the slot at the cell quad (tend of k_advect_tile)
 template <int TI, int TJ>
-__device__ __forceinline__ Q4 aq_div(const KParams<float> &p, const float *sl, const float *lv, int a, int b, int k0)
+__device__ __forceinline__ Q4 aq_div(const KParams<float> &p, const float *sl, const float *lv, int a, int b, int k0,
+                                     int kb, int SK)
 {
     using G = AQGeom<TI, TJ>;
     const int nz = p.nz;
-    const float *E = sl, *N = sl + G::CE * nz, *T = N + G::CN * nz;
+    const float *E = sl, *N = sl + G::CE * SK, *T = N + G::CN * SK;
     const float *s_mu = lv, *s_rhow = lv + nz, *s_odr = lv + 2 * nz;
-    const int oe = ((a + 1) * TJ + b) * nz + k0, ow = (a * TJ + b) * nz + k0;
-    const int on = (a * (TJ + 1) + b + 1) * nz + k0, os = (a * (TJ + 1) + b) * nz + k0;
-    const int ot = (a * TJ + b) * nz + k0;
+    const int kk = k0 - kb;
+    const int oe = ((a + 1) * TJ + b) * SK + kk, ow = (a * TJ + b) * SK + kk;
+    const int on = (a * (TJ + 1) + b + 1) * SK + kk, os = (a * (TJ + 1) + b) * SK + kk;
+    const int ot = (a * TJ + b) * SK + kk;
     const Q4 ee = lds4(E + oe), ew = lds4(E + ow), nn = lds4(N + on), ns = lds4(N + os), tt = lds4(T + ot);
     const float tb0 = k0 > 0 ? T[ot - 1] : 0.f;
     Q4 r;
@@ -506,56 +573,62 @@ __device__ __forceinline__ void aq_store(float *dst, int c, int k0, int nz, int 
     }
 }
 
-// one TI x TJ tile (bx, by); the batched ensemble kernel calls it per member
-template <int TI, int TJ>
-__device__ __forceinline__ void advect_quad_body(const KParams<float> &p, const KFields<float> &F, int bx, int by,
-                                                 float step, float sdtg, int what)
+// the level arrays and the basic-state table of a block, into shared memory
+__device__ __forceinline__ void aq_stage_tables(const KParams<float> &p, float *tab, float *lv)
 {
-    using G = AQGeom<TI, TJ>;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int nz = p.nz, NQ = nz >> 2, sx = p.ny * nz, sy = nz;
-    float *s0 = (float *)smem_raw, *s1 = s0 + G::CF * nz;
-    float *tab = s1 + G::CF * nz;
-    float *lv = tab + BT_COUNT * nz;
-    float *s_mu = lv, *s_rhow = lv + nz, *s_odr = lv + 2 * nz, *s_tb = lv + 3 * nz, *s_qb = lv + 4 * nz,
-          *s_tbv = lv + 5 * nz;
+    const int nz = p.nz;
     for (int e = threadIdx.x; e < BT_COUNT * nz; e += AQ_THREADS) tab[e] = p.btab[e];
     for (int k = threadIdx.x; k < nz; k += AQ_THREADS) {
-        s_mu[k] = p.mu[k];
-        s_rhow[k] = p.rhow[k];
-        s_odr[k] = p.one_d_rhou[k];
-        s_tb[k] = p.tb[k];
-        s_qb[k] = p.moist ? p.qb[k] : 0.f;
-        s_tbv[k] = p.tbv[k];
+        lv[k] = p.mu[k];
+        lv[nz + k] = p.rhow[k];
+        lv[2 * nz + k] = p.one_d_rhou[k];
+        lv[3 * nz + k] = p.tb[k];
+        lv[4 * nz + k] = p.moist ? p.qb[k] : 0.f;
+        lv[5 * nz + k] = p.tbv[k];
         lv[6 * nz + k] = p.rhou[k];
     }
-    const int i0 = 3 + bx * TI, j0 = 3 + by * TJ;
-    const int ti = min(TI, p.nx - 3 - i0), tj = min(TJ, p.ny - 3 - j0);
+}
+
+// the three passes over cells (i0..i0+ti-1, j0..j0+tj-1) and levels
+// ks..ke-1 with the current fields read from `src`; face slots s0, s1 with
+// levels kb..ke-1 at stride SK (see aq_faces); tables staged and synchronised
+template <int TI, int TJ, class S>
+__device__ __forceinline__ void advect_quad_cells(const KParams<float> &p, const KFields<float> &F, const S &src,
+                                                  float *s0, float *s1, const float *tab, const float *lv, int i0,
+                                                  int j0, int ti, int tj, int ks, int ke, int kb, int SK, float step,
+                                                  float sdtg, int what)
+{
+    using G = AQGeom<TI, TJ>;
+    const int nz = p.nz, NQ = (ke - ks) >> 2, sx = p.ny * nz, sy = nz;
+    const float *s_mu = lv, *s_rhow = lv + nz, *s_odr = lv + 2 * nz, *s_tb = lv + 3 * nz, *s_qb = lv + 4 * nz,
+                *s_tbv = lv + 5 * nz;
     const bool rows = (what & ADV_ROWS) != 0;
-    __syncthreads();
+    (void)sx;
+    (void)sy;
 
     // ---- pass 1: u, v (and the buoyancy of w)
     if (what & (ADV_UV | ADV_WB)) {
         if (what & ADV_UV) {
-            aq_faces<TI, TJ, 0>(p, F, tab, s0, i0, j0, ti, tj, rows);
-            aq_faces<TI, TJ, 1>(p, F, tab, s1, i0, j0, ti, tj, rows);
+            aq_faces<TI, TJ, 0>(p, F, src, tab, s0, i0, j0, ti, tj, rows, ks, ke, kb, SK);
+            aq_faces<TI, TJ, 1>(p, F, src, tab, s1, i0, j0, ti, tj, rows, ks, ke, kb, SK);
         }
         __syncthreads();
         for (int w = threadIdx.x; w < G::CT * NQ; w += AQ_THREADS) {
             const int q = w % NQ, col = w / NQ, b = col % TJ, a = col / TJ;
             if (a >= ti || b >= tj) continue;
-            const int i = i0 + a, j = j0 + b, k0 = 4 * q;
-            const int c = gix(p.ny, nz, i, j, k0);
+            const int i = i0 + a, j = j0 + b, k0 = ks + 4 * q;
+            const int c = gix(p.ny, nz, i, j, k0), cs = src.at(i, j, k0);
             // every load of the quad's u, v and w results before any store
             // (a store to P would otherwise order the later loads after it)
             Q4 ru, rv;
             if (what & ADV_UV) {
-                const float *U = F.cur[FU], *V = F.cur[FV];
                 const float fj = p.f[j];
-                const Q4 v0 = ldg4(V, c), v1 = ldg4(V, c + sy), v2 = ldg4(V, c - sx), v3 = ldg4(V, c - sx + sy);
-                const Q4 u0 = ldg4(U, c), u1 = ldg4(U, c + sx), u2 = ldg4(U, c - sy), u3 = ldg4(U, c + sx - sy);
+                const Q4 v0 = src.ld4(FV, cs, 0, 0), v1 = src.ld4(FV, cs, 0, 1), v2 = src.ld4(FV, cs, -1, 0),
+                         v3 = src.ld4(FV, cs, -1, 1);
+                const Q4 u0 = src.ld4(FU, cs, 0, 0), u1 = src.ld4(FU, cs, 1, 0), u2 = src.ld4(FU, cs, 0, -1),
+                         u3 = src.ld4(FU, cs, 1, -1);
                 const Q4 mu = ldg4(F.M[FU], c), mv = ldg4(F.M[FV], c);
-                const Q4 du = aq_div<TI, TJ>(p, s0, lv, a, b, k0), dv = aq_div<TI, TJ>(p, s1, lv, a, b, k0);
+                const Q4 du = aq_div<TI, TJ>(p, s0, lv, a, b, k0, kb, SK), dv = aq_div<TI, TJ>(p, s1, lv, a, b, k0, kb, SK);
 #pragma unroll
                 for (int e = 0; e < 4; e++) {
                     const float ov_u = 0.25f * (v0.v[e] + v1.v[e] + v2.v[e] + v3.v[e]);
@@ -569,12 +642,12 @@ __device__ __forceinline__ void advect_quad_body(const KParams<float> &p, const 
             Q4 rw;
             if (what & ADV_WB) {
                 // buoyancy at levels k0-1 .. k0+3 (b1 of level k is b0 of level k-1)
-                const Win th = ldwin(F.cur[FTH], c, k0, nz);
+                const Win th = src.win(FTH, cs, 0, 0, k0);
                 Win qv, qc, qr;
                 if (p.moist) {
-                    qv = ldwin(F.cur[FQV], c, k0, nz);
-                    qc = ldwin(F.cur[FQC], c, k0, nz);
-                    qr = ldwin(F.cur[FQR], c, k0, nz);
+                    qv = src.win(FQV, cs, 0, 0, k0);
+                    qc = src.win(FQC, cs, 0, 0, k0);
+                    qr = src.win(FQR, cs, 0, 0, k0);
                 }
                 float bb[5];
 #pragma unroll
@@ -600,15 +673,15 @@ __device__ __forceinline__ void advect_quad_body(const KParams<float> &p, const 
     // ---- pass 2: theta, qv (qv's clipping bit)
     const bool th_on = (what & ADV_TH) != 0, q_on = (what & ADV_Q) != 0;
     if (th_on || q_on) {
-        if (th_on) aq_faces<TI, TJ, 2>(p, F, tab, s0, i0, j0, ti, tj, rows);
-        if (q_on) aq_faces<TI, TJ, 3>(p, F, tab, s1, i0, j0, ti, tj, rows);
+        if (th_on) aq_faces<TI, TJ, 2>(p, F, src, tab, s0, i0, j0, ti, tj, rows, ks, ke, kb, SK);
+        if (q_on) aq_faces<TI, TJ, 3>(p, F, src, tab, s1, i0, j0, ti, tj, rows, ks, ke, kb, SK);
         __syncthreads();
         for (int w = threadIdx.x; w < G::CT * NQ; w += AQ_THREADS) {
             const int q = w % NQ, col = w / NQ, b = col % TJ, a = col / TJ;
             if (a >= ti || b >= tj) continue;
-            const int i = i0 + a, j = j0 + b, k0 = 4 * q;
-            const int c = gix(p.ny, nz, i, j, k0);
-            const Win wc = ldwin(F.cur[FW], c, k0, nz);
+            const int i = i0 + a, j = j0 + b, k0 = ks + 4 * q;
+            const int c = gix(p.ny, nz, i, j, k0), cs = src.at(i, j, k0);
+            const Win wc = src.win(FW, cs, 0, 0, k0);
             // both fields' start-of-step values before either store
             const Q4 z4{{0.f, 0.f, 0.f, 0.f}};
             const Q4 mq[2] = {th_on ? ldg4(F.M[FTH], c) : z4, q_on ? ldg4(F.M[FQV], c) : z4};
@@ -618,7 +691,7 @@ __device__ __forceinline__ void advect_quad_body(const KParams<float> &p, const 
             for (int fi = 0; fi < 2; fi++) {
                 if (fi == 0 ? !th_on : !q_on) continue;
                 const float *base = fi == 0 ? s_tb : s_qb;
-                const Q4 d = aq_div<TI, TJ>(p, fi == 0 ? s0 : s1, lv, a, b, k0);
+                const Q4 d = aq_div<TI, TJ>(p, fi == 0 ? s0 : s1, lv, a, b, k0, kb, SK);
                 const Q4 m = mq[fi];
                 Q4 r;
 #pragma unroll
@@ -659,16 +732,16 @@ __device__ __forceinline__ void advect_quad_body(const KParams<float> &p, const 
 
     // ---- pass 3: qc, qr (clipping bits 2 and 4, the rain's fall speed)
     if (q_on) {
-        aq_faces<TI, TJ, 4>(p, F, tab, s0, i0, j0, ti, tj, rows);
-        aq_faces<TI, TJ, 5>(p, F, tab, s1, i0, j0, ti, tj, rows);
+        aq_faces<TI, TJ, 4>(p, F, src, tab, s0, i0, j0, ti, tj, rows, ks, ke, kb, SK);
+        aq_faces<TI, TJ, 5>(p, F, src, tab, s1, i0, j0, ti, tj, rows, ks, ke, kb, SK);
         __syncthreads();
         for (int w = threadIdx.x; w < G::CT * NQ; w += AQ_THREADS) {
             const int q = w % NQ, col = w / NQ, b = col % TJ, a = col / TJ;
             if (a >= ti || b >= tj) continue;
-            const int i = i0 + a, j = j0 + b, k0 = 4 * q;
-            const int c = gix(p.ny, nz, i, j, k0);
-            const Q4 dc = aq_div<TI, TJ>(p, s0, lv, a, b, k0);
-            const Q4 dr = aq_div<TI, TJ>(p, s1, lv, a, b, k0);
+            const int i = i0 + a, j = j0 + b, k0 = ks + 4 * q;
+            const int c = gix(p.ny, nz, i, j, k0), cs = src.at(i, j, k0);
+            const Q4 dc = aq_div<TI, TJ>(p, s0, lv, a, b, k0, kb, SK);
+            const Q4 dr = aq_div<TI, TJ>(p, s1, lv, a, b, k0, kb, SK);
             const Q4 mc = ldg4(F.M[FQC], c), mr = ldg4(F.M[FQR], c);
             Q4 rc, rr;
             unsigned char bits[4] = {0, 0, 0, 0};
@@ -695,7 +768,7 @@ __device__ __forceinline__ void advect_quad_body(const KParams<float> &p, const 
             }
             if (p.rf == 1) {
                 // fall speed of the advected cells; level 0 repeats level 1
-                const Q4 qrc = ldg4(F.cur[FQR], c);
+                const Q4 qrc = src.ld4(FQR, cs, 0, 0);
 #pragma unroll
                 for (int e = 0; e < 4; e++) {
                     const int k = k0 + e;
@@ -705,6 +778,27 @@ __device__ __forceinline__ void advect_quad_body(const KParams<float> &p, const 
             }
         }
     }
+}
+
+
+// one TI x TJ tile (bx, by), every level, the fields read from global memory;
+// the batched ensemble kernel calls it per member
+template <int TI, int TJ>
+__device__ __forceinline__ void advect_quad_body(const KParams<float> &p, const KFields<float> &F, int bx, int by,
+                                                 float step, float sdtg, int what)
+{
+    using G = AQGeom<TI, TJ>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int nz = p.nz;
+    float *s0 = (float *)smem_raw, *s1 = s0 + G::CF * nz;
+    float *tab = s1 + G::CF * nz;
+    float *lv = tab + BT_COUNT * nz;
+    aq_stage_tables(p, tab, lv);
+    const int i0 = 3 + bx * TI, j0 = 3 + by * TJ;
+    const int ti = min(TI, p.nx - 3 - i0), tj = min(TJ, p.ny - 3 - j0);
+    __syncthreads();
+    const GSrc src(F, p.ny, nz);
+    advect_quad_cells<TI, TJ>(p, F, src, s0, s1, tab, lv, i0, j0, ti, tj, 0, nz, 0, nz, step, sdtg, what);
 }
 
 // MB: blocks per SM the registers are sized for (3: 80 registers, 4: 64)
@@ -719,6 +813,88 @@ __global__ void __launch_bounds__(AQ_THREADS, MB)
             mirror_edges_body(p, F.P[FU], F.P[FV], F.P[FW], t);
     }
     advect_quad_body<TI, TJ>(p, F, blockIdx.x, blockIdx.y, step, sdtg, what);
+}
+
+// ---------------------------------------------------------------------------
+// k_advect_tma: the same passes with every current field staged into shared
+// memory by the tensor memory accelerator.  A block owns TI x TJ columns and a
+// slab of KZ levels (ks .. ks+KZ-1, the last slab cut at NZ).  One elected
+// thread issues a 3-D tiled copy per field of the box i0-3 .. i0+TI+2,
+// j0-3 .. j0+TJ+2, ks-4 .. ks+KZ+3 (the widest stencil of a face, and the
+// 12-level windows of the top faces; points outside the field arrive as
+// zeros), all completing on one mbarrier; the face and cell arithmetic then
+// reads shared memory only, expression for expression the arithmetic of
+// k_advect_quad, so the results are bit-identical.  The start-of-step fields
+// (read once per point) and the stores stay in global memory.  A slab above
+// the bottom also evaluates the top faces of the quad below it (the
+// divergence of level ks needs the face at ks-1).
+// ---------------------------------------------------------------------------
+template <int TI, int TJ, int KZ>
+struct AQTma {
+    static constexpr int BI = TI + 6, BJ = TJ + 6, BK = KZ + 8;
+    static constexpr int BOX = BI * BJ * BK;          // floats per field box
+    static constexpr int BOXP = (BOX + 31) & ~31;     // boxes 128-byte aligned
+    static constexpr int SK = KZ + 4;                 // face-slot levels per column
+};
+
+// boxes of nf fields, two face slots, the basic-state table, the level
+// arrays, the barrier
+__host__ __device__ constexpr size_t advect_tma_smem(int ti, int tj, int kz, int nz, int nf)
+{
+    return ((size_t)nf * ((((ti + 6) * (tj + 6) * (kz + 8)) + 31) & ~31) +
+            2 * (size_t)((ti + 1) * tj + ti * (tj + 1) + ti * tj) * (kz + 4) + (size_t)BT_COUNT * nz +
+            (size_t)AQ_LV * nz) *
+               sizeof(float) +
+           16;
+}
+
+template <int TI, int TJ, int KZ, int MB>
+__global__ void __launch_bounds__(AQ_THREADS, MB)
+    k_advect_tma(const __grid_constant__ TmaMaps maps, KParams<float> p, KFields<float> F, float step, float sdtg,
+                 int what, int *err)
+{
+    using A = AQTma<TI, TJ, KZ>;
+    using G = AQGeom<TI, TJ>;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    const int nz = p.nz, nf = p.moist ? 7 : 4;
+    float *boxes = (float *)smem_raw;
+    float *s0 = boxes + nf * A::BOXP, *s1 = s0 + G::CF * A::SK;
+    float *tab = s1 + G::CF * A::SK;
+    float *lv = tab + BT_COUNT * nz;
+    uint64_t *bar = (uint64_t *)(lv + AQ_LV * nz);
+    if (what & ADV_MIRROR) {  // mirror copies (edge points from non-advected ones), grid-stride
+        const long nt = (long)gridDim.x * gridDim.y * gridDim.z * AQ_THREADS;
+        const long ntot = 2L * (p.nx + p.ny - 2) * (p.nz - 2);
+        const long b = ((long)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+        for (long t = b * AQ_THREADS + threadIdx.x; t < ntot; t += nt) mirror_edges_body(p, F.P[FU], F.P[FV], F.P[FW], t);
+    }
+    const int i0 = 3 + blockIdx.x * TI, j0 = 3 + blockIdx.y * TJ, ks = blockIdx.z * KZ;
+    const int ti = min(TI, p.nx - 3 - i0), tj = min(TJ, p.ny - 3 - j0);
+    const int ke = min(ks + KZ, nz), kb = ks > 0 ? ks - 4 : 0;
+    if (smem_addr(boxes) & 127u) {  // the copies need 128-byte aligned destinations
+        if (threadIdx.x == 0) atomicOr(err, kErrStaging);
+        return;
+    }
+    if (threadIdx.x == 0) {
+        mbar_init(bar, 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        mbar_arrive_expect_tx(bar, (uint32_t)(nf * A::BOX * sizeof(float)));
+        for (int f = 0; f < nf; f++) tma_load_3d(boxes + f * A::BOXP, &maps.m[f], ks - 4, j0 - 3, i0 - 3, bar);
+    }
+    aq_stage_tables(p, tab, lv);
+    // bounded wait; every thread leaves together if the copies did not land
+    const bool landed = __syncthreads_and(mbar_wait_bounded(bar, 0) ? 1 : 0);
+    if (!landed) {
+        if (threadIdx.x == 0) atomicOr(err, kErrStaging);
+        mbar_wait_bounded(bar, 0);  // the copies still in flight, bounded again
+        return;
+    }
+    const SSrc<A::BJ, A::BK> src{F, boxes, A::BOXP, i0 - 3, j0 - 3, ks - 4, p.ny, nz};
+    advect_quad_cells<TI, TJ>(p, F, src, s0, s1, tab, lv, i0, j0, ti, tj, ks, ke, kb, A::SK, step, sdtg,
+                              what & ~ADV_ROWS);
 }
 
 // ---------------------------------------------------------------------------

@@ -167,3 +167,71 @@ def test_spectral_x_pair_matches_single_cta(monkeypatch, case, form):
     for f in list(range(nprog)) + [abi.GA_PI]:
         a, b = (m.get(f) for m in ms)
         np.testing.assert_array_equal(b, a, err_msg=f"{case} field {f}")
+
+
+def _staged_pair(monkeypatch, wl, cand):
+    """a four-level context reading the fields from global memory and one
+    staging them into shared memory by the tensor memory accelerator
+    (candidate `cand` of the staged kernel: tile, level slab, blocks per SM)"""
+    ms = []
+    for mode in ("quad", "tma"):
+        monkeypatch.setenv("GA_ADVECT", mode)
+        monkeypatch.setenv("GA_ADVECT_TMA", str(cand))
+        ms.append(anelastic.Model(wl, abi.GA_PREC_F32))
+    monkeypatch.delenv("GA_ADVECT")
+    monkeypatch.delenv("GA_ADVECT_TMA")
+    return ms
+
+
+@pytest.mark.parametrize("cand", [0, 1, 2, 3])
+@pytest.mark.parametrize("case", ["moist_rf1", "moist_rf2", "dry", "tall_slabs"])
+def test_staged_advection_operator_bit_identical(monkeypatch, case, cand):
+    """k_advect_tma (halo boxes in shared memory) against k_advect_quad on
+    one advection operator: every forecast field bit for bit.  tall_slabs
+    has 20 levels, so the last 8- or 16-level slab is cut at NZ and the
+    slabs above the bottom need the top faces of the quad below them."""
+    if case == "dry":
+        wl = configs.dry_bubble(nx=30, ny=26, nz=20, nsteps=2)
+    elif case == "tall_slabs":
+        wl = configs.moist_blob(nx=27, ny=29, nz=20)
+    else:
+        wl = configs.moist_blob(nx=30, ny=26, nz=16, rain_fallout=1 if case == "moist_rf1" else 2)
+    ms = _staged_pair(monkeypatch, wl, cand)
+    _perturb(ms, wl, 13)
+    for op, fields in ADVECT_OPS.items():
+        if op == "advect_micro" and not wl.microphysics_option:
+            continue
+        for m in ms:
+            m.op(op, 0.5)
+        for f in fields:
+            a, b = (m.get(f, abi.GA_SLOT_P) for m in ms)
+            np.testing.assert_array_equal(b, a, err_msg=f"{case} cand {cand} {op} field {abi.PROG_NAMES[f]}")
+
+
+@pytest.mark.parametrize("cand", [0, 1, 2, 3])
+@pytest.mark.parametrize("case", ["thunderstorm_small", "dry_bubble"])
+def test_staged_advection_steps_bit_identical(monkeypatch, case, cand):
+    """whole steps (the mirror copies ride in the advection launch) with the
+    staged kernel against the four-level kernel: every field bit for bit"""
+    if case == "thunderstorm_small":
+        wl = configs.thunderstorm(nx=44, ny=38, nsteps=4)
+    else:
+        wl = configs.dry_bubble(nx=34, ny=30, nz=20, nsteps=4)
+    ms = _staged_pair(monkeypatch, wl, cand)
+    for m in ms:
+        m.step(wl.nsteps)
+    nprog = 7 if wl.microphysics_option else 4
+    for f in list(range(nprog)) + [abi.GA_PI]:
+        for slot in (abi.GA_SLOT_CUR, abi.GA_SLOT_M):
+            if f == abi.GA_PI and slot != abi.GA_SLOT_CUR:
+                continue
+            a, b = (m.get(f, slot) for m in ms)
+            np.testing.assert_array_equal(b, a, err_msg=f"{case} cand {cand} field {f} slot {slot}")
+
+
+def test_autotuner_races_the_staged_kernel(monkeypatch):
+    wl = configs.thunderstorm(nx=44, ny=38, nsteps=2)
+    monkeypatch.setenv("GA_ADVECT", "tma")
+    m = anelastic.Model(wl, abi.GA_PREC_F32)
+    info = m.tune()
+    assert "staged by TMA" in info, info
