@@ -202,6 +202,36 @@ GA_API int ga_op(ga_ctx *ctx, int op, double step);
 /* Number of completed steps (reference: bigcounter) and model time (mtime). */
 GA_API int ga_get_counters(ga_ctx *ctx, long long *bigcounter, double *mtime);
 
+/* FP64 domain budgets of one rotation slot (GA_SLOT_*), summed on the GPU in
+ * FP64 whatever the context's precision, over the physical cells
+ * i in [1, NX-1), j in [1, NY-1), k in [1, NZ-1) with the density-times-volume
+ * weight rhou[k] dx dy dz / mu[k]:
+ *   GA_BUDGET_THETA  sum of rho theta' dV      GA_BUDGET_WATER  QV + QC + QR
+ *   GA_BUDGET_QV / _QC / _QR  rho q dV        GA_BUDGET_KE     0.5 rho |u'|^2 dV
+ *   GA_BUDGET_RAIN   accumulated surface rain times dx dy (GA_ACCRAIN)
+ *   GA_BUDGET_MASS   sum of rho dV
+ * The flux form of the advection (advection.cpp:304-498) conserves the
+ * theta, moisture and water integrals up to the fluxes through the domain's
+ * boundary and the base-state terms; Kessler (kessler.cpp:25-213) conserves
+ * the total water of every point.  The blocks' partial sums are added in a
+ * fixed order, so repeated calls on the same state give the same bits.  The
+ * reference computes no budget on its step path (its energy diagnostics,
+ * energy.cpp, are out of this library's scope).  n must be >= GA_NBUDGET. */
+#define GA_BUDGET_THETA 0
+#define GA_BUDGET_QV    1
+#define GA_BUDGET_QC    2
+#define GA_BUDGET_QR    3
+#define GA_BUDGET_WATER 4
+#define GA_BUDGET_KE    5
+#define GA_BUDGET_RAIN  6
+#define GA_BUDGET_MASS  7
+#define GA_NBUDGET      8
+GA_API int ga_budget(ga_ctx *ctx, int slot, double *out, int n);
+
+/* Set the step counter and model time (a restart: bigcounter and mtime as
+ * ga_get_counters returned them when the state was saved). */
+GA_API int ga_set_counters(ga_ctx *ctx, long long bigcounter, double mtime);
+
 /* Scan the prognostic forecast buffers for NaN/Inf on the device.
  * Returns GA_OK or GA_ERR_NONFINITE.  The reference has no such check. */
 GA_API int ga_check_finite(ga_ctx *ctx);

@@ -52,6 +52,8 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     L.ga_synchronize.argtypes = [C.c_void_p]
     L.ga_op.argtypes = [C.c_void_p, C.c_int, C.c_double]
     L.ga_get_counters.argtypes = [C.c_void_p, C.POINTER(C.c_longlong), C.POINTER(C.c_double)]
+    L.ga_set_counters.argtypes = [C.c_void_p, C.c_longlong, C.c_double]
+    L.ga_budget.argtypes = [C.c_void_p, C.c_int, _DP, C.c_int]
     L.ga_check_finite.argtypes = [C.c_void_p]
     L.ga_launch_count.argtypes = [C.c_void_p]
     L.ga_launch_count.restype = C.c_longlong
@@ -240,6 +242,15 @@ class Model:
         bc, mt = C.c_longlong(), C.c_double()
         self._check(self.L.ga_get_counters(self.h, C.byref(bc), C.byref(mt)), "ga_get_counters")
         return bc.value, mt.value
+
+    def set_counters(self, bigcounter: int, mtime: float) -> None:
+        self._check(self.L.ga_set_counters(self.h, bigcounter, mtime), "ga_set_counters")
+
+    def budget(self, slot: int = abi.GA_SLOT_CUR) -> dict:
+        """FP64 domain budgets of one rotation slot (ga_budget), by name."""
+        out = (C.c_double * abi.GA_NBUDGET)()
+        self._check(self.L.ga_budget(self.h, slot, out, abi.GA_NBUDGET), "ga_budget")
+        return {n: out[b] for b, n in enumerate(abi.BUDGET_NAMES)}
 
     def check_finite(self) -> int:
         return self.L.ga_check_finite(self.h)

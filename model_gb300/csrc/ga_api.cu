@@ -210,6 +210,21 @@ int ga_get_counters(ga_ctx *ctx, long long *bigcounter, double *mtime)
     return GA_OK;
 }
 
+int ga_budget(ga_ctx *ctx, int slot, double *out, int n)
+{
+    if (!ctx || !out || n < GA_NBUDGET) return fail(GA_ERR_ARG, "ga_budget: bad arguments");
+    if (slot < 0 || slot > 2) return fail(GA_ERR_ARG, "ga_budget: bad slot");
+    return ctx->e->budget(slot, out);
+}
+
+int ga_set_counters(ga_ctx *ctx, long long bigcounter, double mtime)
+{
+    if (!ctx || bigcounter < 0) return fail(GA_ERR_ARG, "ga_set_counters: bad arguments");
+    ctx->e->bigcounter = bigcounter;
+    ctx->e->mtime = mtime;
+    return GA_OK;
+}
+
 int ga_check_finite(ga_ctx *ctx)
 {
     if (!ctx) return fail(GA_ERR_ARG, "ga_check_finite: null context");

@@ -114,6 +114,7 @@ class Engine : public EngineBase {
     // the four-level kernel with the current fields staged into shared memory
     // by the tensor memory accelerator (k_advect_tma), and its candidate
     int adv_tma = 0, adv_tmc = 0;
+    double *budget_w = nullptr, *budget_part = nullptr;  // FP64 budget weights and partial sums
     std::map<std::tuple<const void *, int, int, int>, CUtensorMap> tma_maps;  // per buffer and box
     // the four-level post-processing kernel (FP32, NZ % 4 == 0); GA_POST=column
     // keeps the per-level one
@@ -249,6 +250,12 @@ class Engine : public EngineBase {
         kp.acoef = col_T(ac.data(), NZ); kp.ccoef = col_T(cc.data(), NZ); kp.vcoef = col_T(vc.data(), NZ);
         kp.acoef_d = upload(ac); kp.ccoef_d = upload(cc); kp.vcoef_d = upload(vc);
         kp.rhou_d = upload(std::vector<double>(cols->rhou, cols->rhou + NZ));
+        {  // budget weights: density times cell volume, rhou[k] dx dy dz / mu[k]
+            std::vector<double> wk(NZ);
+            for (int k = 0; k < NZ; k++) wk[k] = cols->rhou[k] * dx * c->dy * c->dz / cols->mu[k];
+            budget_w = upload(wk);
+            budget_part = dalloc<double>((size_t)BUDGET_BLOCKS * GA_NB + GA_NB);
+        }
         kp.dx2 = dx * dx;
         kp.low_modes = sizeof(T) == 8 ? 0 : 1;  // FP32: the mean mode (0,0) solves in FP64
         if (const char *ev = std::getenv("GA_LOW_MODES"))  // FP32: |p|, |q| below this solve in FP64
@@ -1255,6 +1262,30 @@ class Engine : public EngineBase {
             if (rc) return rc;
         }
         return launch_status();
+    }
+
+    int budget(int slot, double *out) override
+    {
+        if (slot < 0 || slot > 2) return GA_ERR_ARG;
+        cudaSetDevice(device);
+        auto sl = [&](int f) -> const T * {
+            if (f >= nprog) return nullptr;
+            return buf[f][slot == GA_SLOT_CUR ? ci[f] : slot == GA_SLOT_P ? pi_[f] : mi[f]];
+        };
+        k_budget<T><<<BUDGET_BLOCKS, 256, 0, stream>>>(NX, NY, NZ, sl(FU), sl(FV), sl(FW), sl(FTH), sl(FQV), sl(FQC),
+                                                       sl(FQR), kp.moist ? accrain : nullptr, budget_w,
+                                                       cfg.dx * cfg.dy, budget_part);
+        k_budget_sum<<<1, 32, 0, stream>>>(budget_part, BUDGET_BLOCKS, budget_part + (size_t)BUDGET_BLOCKS * GA_NB);
+        launches += 2;
+        int rc = launch_status();
+        if (rc) return rc;
+        double h[GA_NB];
+        cudaMemcpyAsync(h, budget_part + (size_t)BUDGET_BLOCKS * GA_NB, sizeof h, cudaMemcpyDeviceToHost, stream);
+        rc = sync_status();
+        if (rc) return rc;
+        h[4] = h[1] + h[2] + h[3];
+        for (int b = 0; b < GA_NB; b++) out[b] = h[b];
+        return GA_OK;
     }
 
     int check_finite() override

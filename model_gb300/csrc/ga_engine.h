@@ -34,6 +34,7 @@ struct EngineBase {
     virtual int op(int op, double step) = 0;
     virtual int step(int nsteps) = 0;
     virtual int check_finite() = 0;
+    virtual int budget(int slot, double *out) = 0;  // GA_NBUDGET FP64 domain sums
     virtual void *field_ptr(int field, int slot) = 0;
     // tangent-linear model and adjoint (dry, non-periodic contexts)
     virtual int lin_set_field(int field, int slot, const double *host, size_t n) = 0;

@@ -2126,6 +2126,78 @@ __global__ void k_check_finite(const T *a, long n, int *flag)
         if (!isfinite(a[t])) { atomicExch(flag, 1); return; }
 }
 
+// ---------------------------------------------------------------------------
+// FP64 domain budgets of one rotation slot.  Over the physical cells
+// i in [1, NX-1), j in [1, NY-1), k in [1, NZ-1), with the weight
+// wk[k] = rhou[k] dx dy dz / mu[k] (density times cell volume), in FP64 for
+// either precision of the fields:
+//   0 theta', 1 qv, 2 qc, 3 qr (rho-weighted integrals; the flux form of
+//   the advection conserves them up to boundary fluxes), 5 the perturbation
+//   kinetic energy 0.5 rho (u^2 + v^2 + w^2) at cell points, 7 the mass;
+//   6 the accumulated surface rain times dx dy (columns i, j of the same
+//   range).  4 (total water, 1 + 2 + 3) is formed on the host.
+// Each block writes its GA_NB partial sums; k_budget_sum adds the blocks in
+// index order, so the result does not depend on the schedule.
+// ---------------------------------------------------------------------------
+constexpr int GA_NB = 8;
+constexpr int BUDGET_BLOCKS = 304;
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_budget(int nx, int ny, int nz, const T *u, const T *v, const T *w,
+                                                const T *th, const T *qv, const T *qc, const T *qr,
+                                                const double *accrain, const double *wk, double dxdy, double *part)
+{
+    double acc[GA_NB];
+#pragma unroll
+    for (int b = 0; b < GA_NB; b++) acc[b] = 0.0;
+    const long n = (long)nx * ny * nz, stride = (long)gridDim.x * blockDim.x;
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += stride) {
+        const int k = (int)(t % nz);
+        const long ij = t / nz;
+        const int j = (int)(ij % ny), i = (int)(ij / ny);
+        if (i < 1 || i >= nx - 1 || j < 1 || j >= ny - 1 || k < 1 || k >= nz - 1) continue;
+        const double wt = wk[k];
+        acc[0] += wt * (double)th[t];
+        if (qv) {
+            acc[1] += wt * (double)qv[t];
+            acc[2] += wt * (double)qc[t];
+            acc[3] += wt * (double)qr[t];
+        }
+        const double uu = u[t], vv = v[t], ww = w[t];
+        acc[5] += wt * 0.5 * (uu * uu + vv * vv + ww * ww);
+        acc[7] += wt;
+    }
+    if (accrain) {
+        for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < (long)nx * ny; t += stride) {
+            const int j = (int)(t % ny), i = (int)(t / ny);
+            if (i >= 1 && i < nx - 1 && j >= 1 && j < ny - 1) acc[6] += accrain[t] * dxdy;
+        }
+    }
+    __shared__ double red[8][GA_NB];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int b = 0; b < GA_NB; b++) {
+        double x = acc[b];
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        if (lane == 0) red[warp][b] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x < GA_NB) {
+        double x = 0.0;
+        for (int wi = 0; wi < (int)(blockDim.x >> 5); wi++) x += red[wi][threadIdx.x];
+        part[(long)blockIdx.x * GA_NB + threadIdx.x] = x;
+    }
+}
+
+static __global__ void k_budget_sum(const double *part, int nblocks, double *out)
+{
+    if (threadIdx.x < GA_NB) {
+        double x = 0.0;
+        for (int b = 0; b < nblocks; b++) x += part[(long)b * GA_NB + threadIdx.x];
+        out[threadIdx.x] = x;
+    }
+}
+
 template <typename T>
 __global__ void k_convert_in(T *dst, const double *src, long n)
 {
