@@ -430,9 +430,16 @@ def cpu_model() -> str:
     return f"nproc={os.cpu_count()}"
 
 
-def accuracy(model_cls, wl, torch, device, steps):
-    """FP32 against FP64 after `steps` steps: relative L2 per field."""
-    from model_gb300 import abi
+REFERENCE_DIGEST = os.path.join(ROOT, "tests", "golden", "long_{}.npz")
+
+
+def accuracy(model_cls, wl, torch, device, steps, workload="thunderstorm"):
+    """FP32 and FP64 after `steps` steps: relative L2 per field of FP32
+    against the GPU FP64 path (whole fields), and of both against the
+    reference's own serial FP64 build (the digest of its end state made by
+    tests/golden/make_long.py: the random-projection estimate of the whole
+    field's relative L2 error), where a digest of this run exists."""
+    from model_gb300 import abi, digest
     out = {}
     m64 = model_cls(wl, abi.GA_PREC_F64, device=device)
     m32 = model_cls(wl, abi.GA_PREC_F32, device=device)
@@ -441,14 +448,30 @@ def accuracy(model_cls, wl, torch, device, steps):
     t64 = time.perf_counter() - t0
     m32.step(steps)
     nprog = 7 if wl.microphysics_option else 4
+    ends = {"fp32": {}, "fp64": {}}
     for f in range(nprog):
         a, b = m32.get(f), m64.get(f)
         nb = np.linalg.norm(b)
         out[abi.PROG_NAMES[f]] = float(np.linalg.norm(a - b) / nb) if nb > 0 else float(np.linalg.norm(a))
+        ends["fp32"][abi.PROG_NAMES[f]], ends["fp64"][abi.PROG_NAMES[f]] = a, b
+    ends["fp32"]["pi"], ends["fp64"]["pi"] = m32.get(abi.GA_PI), m64.get(abi.GA_PI)
     m64.close()
     m32.close()
-    return {"steps": steps, "rel_l2_fp32_vs_fp64": {k: float(f"{v:.3e}") for k, v in out.items()},
-            "max": float(f"{max(out.values()):.3e}"), "fp64_wall_s": round(t64, 2)}
+    res = {"steps": steps, "rel_l2_fp32_vs_fp64": {k: float(f"{v:.3e}") for k, v in out.items()},
+           "max": float(f"{max(out.values()):.3e}"), "fp64_wall_s": round(t64, 2)}
+    path = REFERENCE_DIGEST.format(workload)
+    if os.path.exists(path):
+        with np.load(path) as z:
+            ref = {k: z[k] for k in z.files}
+        if int(ref["steps"]) == steps:
+            for prec in ("fp32", "fp64"):
+                cmp = digest.compare(ends[prec], ref)
+                est = {k: float(f"{v['proj']:.3e}") for k, v in cmp.items()}
+                res[f"rel_l2_{prec}_vs_reference"] = est
+                res[f"max_{prec}_vs_reference"] = max(est.values())
+            res["reference"] = ("the reference's serial FP64 build (PARALLEL 0) on the same initial state; "
+                                "relative L2 estimated from 64 random +-1 projections of each end-state field")
+    return res
 
 
 # ---------------------------------------------------------------------------
@@ -521,7 +544,7 @@ def run_ours(args):
         m64.close()
     model.close()
     if args.accuracy_steps > 0:
-        line["accuracy"] = accuracy(anelastic.Model, wl, torch, device, args.accuracy_steps)
+        line["accuracy"] = accuracy(anelastic.Model, wl, torch, device, args.accuracy_steps, args.workload)
     if args.e2e_jobs > 0:
         line["e2e"] = e2e_jobs(anelastic.Model, wl, prec, torch, args.e2e_jobs, args.e2e_steps, device)
     if args.ensemble_steps > 0:
