@@ -5,6 +5,8 @@ Three translation units compiled in parallel with nvcc, then linked:
   ga_f32.cu  FP32 engine
   ga_api.cu  the extern "C" boundary of include/ga_anelastic.h
   ga_noalloc.cu  FP64 pressure solve with file-scope scratch (no allocation)
+and the run driver model_gb300/ga_driver (csrc/ga_driver.cpp, host C++ on the
+C ABI, linked against the library).
 Objects go to model_gb300/_build/ (git-ignored).  A rebuild happens only
 when a source is newer than the library.
 """
@@ -21,6 +23,7 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libga_anelastic.so")
+DRIVER = os.path.join(PKG, "ga_driver")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # -ffp-contract=off for host code too: the host builds the sponge, Rayleigh and
 # spectral tables, and GCC on Arm would otherwise fuse their multiply-adds
@@ -48,10 +51,21 @@ def _sources():
 
 
 def up_to_date() -> bool:
-    if not os.path.exists(LIB):
+    if not os.path.exists(LIB) or not os.path.exists(DRIVER):
         return False
-    t = os.path.getmtime(LIB)
+    t = min(os.path.getmtime(LIB), os.path.getmtime(DRIVER))
     return all(os.path.getmtime(s) <= t for s in _sources())
+
+
+def build_driver() -> str:
+    """The C++ run driver on the C ABI (links the library by $ORIGIN)."""
+    cxx = shutil.which("g++") or "g++"
+    tmp = DRIVER + ".tmp"
+    cmd = [cxx, "-O2", "-std=c++17", "-I" + os.path.join(ROOT, "include"), os.path.join(CSRC, "ga_driver.cpp"),
+           "-L" + PKG, "-lga_anelastic", "-Wl,-rpath,$ORIGIN", "-o", tmp]
+    subprocess.run(cmd, check=True)
+    os.replace(tmp, DRIVER)
+    return DRIVER
 
 
 def build(force: bool = False, verbose: bool = False) -> str:
@@ -82,6 +96,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     cmd = [nv, *ARCH, "-shared", "-o", tmp, *objs]
     subprocess.run(cmd, check=True)
     os.replace(tmp, LIB)
+    build_driver()
     return LIB
 
 

@@ -851,7 +851,7 @@ class Engine : public EngineBase {
             k_fall_speed<T><<<cdiv(tv, 256), 256, 0, stream>>>(kp, F);
             const long ncol = (long)(NX - 2) * (NY - 2);
             k_ppm_prepare<T><<<cdiv(ncol, 64), 64, 0, stream>>>(kp, F, ppm_has, ppm_topq, ppm_topm);
-            k_ppm_carry<T><<<1, 1, 0, stream>>>(ncol, ppm_has, ppm_topq, ppm_topm, ppm_cin, ppm_carry);
+            k_ppm_carry<T><<<1, 32, 0, stream>>>(ncol, ppm_has, ppm_topq, ppm_topm, ppm_cin, ppm_carry);
             k_ppm_remap<T><<<cdiv(ncol, 64), 64, 0, stream>>>(kp, F, ppm_has, ppm_cin);
             k_fill<T><<<cdiv(N, 256), 256, 0, stream>>>(vt, N, T(0));
             launches += 5;

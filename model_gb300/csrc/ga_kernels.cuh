@@ -2029,19 +2029,46 @@ __global__ void k_ppm_prepare(KParams<T> p, KFields<T> F, unsigned char *has, T 
     }
 }
 
+// The edge value that the reference carries from one rainy column to the next
+// (microphysics.cpp:616-631): a sequential recurrence over the columns in
+// index order, c <- a + sgn(m) min(|2m|, |c - a|), so it stays one chain.
+// One warp walks it: the lanes load 32 columns at once (the next 32 are
+// loaded while the chain runs), and every lane evaluates the same chain from
+// shuffled values, so no step of it waits for memory.  Launch with 32 threads.
 template <typename T>
 __global__ void k_ppm_carry(long ncol, const unsigned char *has, const T *topq, const T *topm, T *carry_in,
                             T *carry)
 {
-    if (blockIdx.x || threadIdx.x) return;
+    if (blockIdx.x) return;
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
     T c = *carry;
-    for (long t = 0; t < ncol; t++) {
-        if (!has[t]) continue;
-        carry_in[t] = c;
-        T a = topq[t], m = topm[t];
-        c = a + sgn(m) * fmin(fabs(T(2.0) * m), fabs(c - a));
+    auto load = [&](long base, bool &h, T &a, T &m) {
+        const long t = base + lane;
+        h = t < ncol && has[t];
+        a = h ? topq[t] : T(0);
+        m = h ? topm[t] : T(0);
+    };
+    bool h;
+    T a, m;
+    load(0, h, a, m);
+    for (long base = 0; base < ncol; base += 32) {
+        bool hn = false;
+        T an = T(0), mn = T(0);
+        if (base + 32 < ncol) load(base + 32, hn, an, mn);
+        unsigned mask = __ballot_sync(full, h);
+        while (mask) {
+            const int l = __ffs(mask) - 1;
+            mask &= mask - 1;
+            const T al = __shfl_sync(full, a, l), ml = __shfl_sync(full, m, l);
+            if (lane == l) carry_in[base + l] = c;
+            c = al + sgn(ml) * fmin(fabs(T(2.0) * ml), fabs(c - al));
+        }
+        h = hn;
+        a = an;
+        m = mn;
     }
-    *carry = c;
+    if (lane == 0) *carry = c;
 }
 
 template <typename T>

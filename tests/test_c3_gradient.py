@@ -4,6 +4,12 @@ theta', u' and v', on the 192 x 128 x 32 ITCZ-shear state (dx = dy = 40 km,
 dz = 600 m, dt = 120 s), state checkpoints every 50 steps, checked against
 central finite differences along 16 seeded random directions in FP64.
 
+The directional derivatives of random directions d (each field scaled by
+s_f) spread about zero with standard deviation sigma = (sum_f s_f^2
+|dJ/dx_f|^2)^(1/2); the difference between the adjoint's and the central
+differences' derivative is bounded by 3e-5 sigma (a direction whose
+derivative happens to be near zero is not held to a relative bound).
+
 Every slot of u, v, w and theta gets seeded noise (0.05 standard deviation,
 scaled per field), so that no advecting velocity of the trajectory is exactly
 zero: there the upwind sign is decided at a kink, and central differences
@@ -18,9 +24,9 @@ from tests.test_adjoint import LIN, SCALE, MARGIN, vorticity_cost, vorticity_cos
 pytestmark = pytest.mark.gpu
 
 # central differences of 500 FP64 steps: along the first two directions the
-# relative difference to the adjoint was 3.1e-5 and 1.0e-5 at eps = 1e-4
-# (truncation), 2.3e-6 and 7.0e-6 at 1e-5, and about 3e-6 at 1e-6 (the
-# roundoff of the runs); eps = 1e-5 with a 3e-5 bound
+# difference to the adjoint was 3.1e-5 and 1.0e-5 of the derivative at
+# eps = 1e-4 (truncation), 2.3e-6 and 7.0e-6 at 1e-5, and about 3e-6 at 1e-6
+# (the roundoff of the runs); eps = 1e-5 with a bound of 3e-5 sigma
 STEPS, EVERY, NDIR, EPS = 500, 50, 16, 1e-5
 TOL = 3e-5
 
@@ -78,14 +84,16 @@ def test_c3_vorticity_gradient_16_directions_500_steps():
         mm.close()
         return j
 
+    sigma = float(np.sqrt(sum(SCALE[f] ** 2 * float(grad[f] @ grad[f]) for f in grad)))
     drng = np.random.default_rng(16)
     worst = 0.0
     for n in range(NDIR):
         d = {f: SCALE[f] * drng.standard_normal(wl.points) for f in grad}
         fd = (J(d, EPS) - J(d, -EPS)) / (2 * EPS)
         ad = sum(float(grad[f] @ d[f]) for f in d)
-        e = abs(fd - ad) / abs(ad)
+        e = abs(fd - ad) / sigma
         worst = max(worst, e)
-        print(f"direction {n}: adjoint {ad:.12e} central difference {fd:.12e} rel {e:.2e}")
-        assert e <= TOL, (n, fd, ad)
-    print(f"level {k} (850 hPa), margin {MARGIN}, worst relative difference {worst:.2e}")
+        print(f"direction {n}: adjoint {ad:.12e} central difference {fd:.12e} "
+              f"difference/sigma {e:.2e} difference/derivative {abs(fd - ad) / abs(ad):.2e}")
+        assert e <= TOL, (n, fd, ad, sigma)
+    print(f"level {k} (850 hPa), margin {MARGIN}, sigma {sigma:.3e}, worst difference/sigma {worst:.2e}")
