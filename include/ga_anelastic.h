@@ -99,7 +99,8 @@ extern "C" {
 #define GA_OP_RAYLEIGH         11  /* rayleigh_damping          damping.cpp:1148 */
 #define GA_OP_ADVANCE_INNER    12  /* advance_inner + microphysics_advance_inner solver.cpp:241, microphysics.cpp:642 */
 #define GA_OP_ADVANCE_OUTER    13  /* advance_outer + microphysics_advance       solver.cpp:254, microphysics.cpp:657 */
-#define GA_OP_COUNT            14
+#define GA_OP_EXPLICIT_DIFFUSION 14 /* apply_explicit_diffusion  damping.cpp:1125 (on the start-of-step slot) */
+#define GA_OP_COUNT            15
 
 /*
  * Runtime configuration: the subset of the reference's struct input_params
@@ -121,6 +122,13 @@ typedef struct ga_config {
     int    rayleigh_damping_z;      /* raydampheight: first damped level            */
     int    precision;               /* GA_PREC_F64 or GA_PREC_F32                   */
     int    device;                  /* CUDA device ordinal                           */
+    /* explicit diffusion of the start-of-step fields, once per step before the
+     * RK stages (apply_explicit_diffusion, damping.cpp:1125-1146, called at
+     * driver_serial.cpp:188); 0 (a zeroed struct) leaves it off */
+    int    use_explicit_diffusion;  /* USE_EXPLICIT_DIFFUSION                        */
+    int    diffusion_order;         /* DIFFUSION_ORDER: 2, 4 or 6                    */
+    double kdiffh, kdiffv;          /* horizontal / vertical coefficients (kmixh*,   */
+                                    /* kmixv*, damping.cpp:122-129)                  */
 } ga_config;
 
 /*

@@ -31,7 +31,7 @@ OPS = {
     "sign_cells": 0, "advect_uvw": 1, "solve_pressure": 2, "project": 3,
     "integrate_non_hydro": 4, "advect_theta": 5, "advect_micro": 6, "zero_moisture": 7,
     "bc": 8, "bc_micro": 9, "kessler": 10, "rayleigh": 11, "advance_inner": 12,
-    "advance_outer": 13,
+    "advance_outer": 13, "explicit_diffusion": 14,
 }
 
 # names used in bundles / fixtures
@@ -56,6 +56,8 @@ class GaConfig(C.Structure):
         ("boundary_width_north", C.c_int), ("boundary_width_south", C.c_int),
         ("boundary_width_east", C.c_int), ("boundary_width_west", C.c_int),
         ("rayleigh_damping_z", C.c_int), ("precision", C.c_int), ("device", C.c_int),
+        ("use_explicit_diffusion", C.c_int), ("diffusion_order", C.c_int),
+        ("kdiffh", C.c_double), ("kdiffv", C.c_double),
     ]
 
 

@@ -73,6 +73,11 @@ class Workload:
     rayleigh_damping_z: int = -1  # default NZ - 5
     height_lowest_level: float = -1.0  # default dz (uniform grid)
     corner_lat: float = 120.0
+    # explicit diffusion (apply_explicit_diffusion, damping.cpp:1125); off by default
+    use_explicit_diffusion: int = 0
+    diffusion_order: int = 4
+    kdiffh: float = 0.005
+    kdiffv: float = 0.005
     fields: dict = dataclasses.field(default_factory=dict)
 
     def __post_init__(self):
@@ -89,7 +94,8 @@ class Workload:
         keys = ("nx", "ny", "nz", "dx", "dy", "dz", "dt", "microphysics_option", "rain_fallout",
                 "periodic_ew_boundaries", "boundary_width_north", "boundary_width_south",
                 "boundary_width_east", "boundary_width_west", "rayleigh_damping_z",
-                "height_lowest_level", "corner_lat")
+                "height_lowest_level", "corner_lat", "use_explicit_diffusion", "diffusion_order", "kdiffh",
+                "kdiffv")
         return {k: getattr(self, k) for k in keys}
 
 

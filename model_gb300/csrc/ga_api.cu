@@ -130,6 +130,9 @@ int ga_create(const ga_config *cfg, const ga_columns *cols, ga_ctx **out)
         if (w < 0 || w > 64) return fail(GA_ERR_CONFIG, "ga_create: sponge widths must be in [0,64]");
     if (cfg->periodic_ew_boundaries && cfg->nx < 13)
         return fail(GA_ERR_CONFIG, "ga_create: periodic domains need NX >= 13");
+    if (cfg->use_explicit_diffusion && cfg->diffusion_order != 2 && cfg->diffusion_order != 4 &&
+        cfg->diffusion_order != 6)
+        return fail(GA_ERR_CONFIG, "ga_create: diffusion_order must be 2, 4 or 6");
     int rc = GA_OK;
     ga::EngineBase *e = nullptr;
     try {
@@ -318,6 +321,8 @@ int ga_ensemble_create(const ga_config *cfgs, const ga_columns *cols, int nmembe
             return fail(GA_ERR_CONFIG, "ga_ensemble_create: members must share precision, device and microphysics");
         if (c.periodic_ew_boundaries)
             return fail(GA_ERR_UNSUPPORTED, "ga_ensemble_create: periodic members are not batched");
+        if (c.use_explicit_diffusion)
+            return fail(GA_ERR_UNSUPPORTED, "ga_ensemble_create: explicit diffusion is not batched");
         if (c.microphysics_option == 1 && c.rain_fallout != 1)
             return fail(GA_ERR_UNSUPPORTED, "ga_ensemble_create: only Eulerian rain fallout is batched");
         if (c.nx < 12 || c.ny < 12 || c.nz < 6 || c.nz > 128 || !(c.dx > 0 && c.dy > 0 && c.dz > 0 && c.dt > 0))

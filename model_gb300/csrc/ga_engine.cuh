@@ -115,6 +115,65 @@ class Engine : public EngineBase {
     // by the tensor memory accelerator (k_advect_tma), and its candidate
     int adv_tma = 0, adv_tmc = 0;
     double *budget_w = nullptr, *budget_part = nullptr;  // FP64 budget weights and partial sums
+    T *diff_tend = nullptr;  // explicit diffusion: tendencies of every prognostic field
+    const T *diff_w = nullptr;  // and the vertical finite-difference weights, order+1 per level
+
+    // Fornberg's recurrence for finite-difference weights: c[i*(m+1)+d] is the
+    // weight of point x[i] in derivative d at z (util.cpp:199-247)
+    static void fornberg(double z, const double *x, int n, int m, double *c)
+    {
+        double c1 = 1.0, c4 = x[0] - z;
+        c[0] = 1.0;
+        for (int i = 1; i <= n; i++) {
+            const int mn = std::min(i, m);
+            double c2 = 1.0;
+            const double c5 = c4;
+            c4 = x[i] - z;
+            for (int j = 0; j <= i - 1; j++) {
+                const double c3 = x[i] - x[j];
+                c2 = c2 * c3;
+                if (j == i - 1) {
+                    for (int d = mn; d >= 1; d--)
+                        c[i * (m + 1) + d] =
+                            c1 * (d * c[(i - 1) * (m + 1) + d - 1] - c5 * c[(i - 1) * (m + 1) + d]) / c2;
+                    c[i * (m + 1)] = -c1 * c5 * c[(i - 1) * (m + 1)] / c2;
+                }
+                for (int d = mn; d >= 1; d--)
+                    c[j * (m + 1) + d] = (c4 * c[j * (m + 1) + d] - d * c[j * (m + 1) + d - 1]) / c3;
+                c[j * (m + 1)] = c4 * c[j * (m + 1)] / c3;
+            }
+            c1 = c2;
+        }
+    }
+    // the weights of init_diffusion_weights (damping.cpp:158-270) on heights h:
+    // the order's derivative at k in [order/2, NZ-order/2) from levels
+    // k-order/2 .. k+order/2 of the heights scaled by the local spacing; 4th-
+    // order rows at k = 2 and NZ-3 (order 6), 2nd-order rows at k = 1 and NZ-2
+    // (orders 4 and 6)
+    static std::vector<double> diffusion_weights(int order, const double *h, int nz)
+    {
+        std::vector<double> w((size_t)(order + 1) * nz, 0.0), hs(nz, 0.0), c(64);
+        for (int k = order / 2; k < nz - order / 2; k++) {
+            for (int n = 0; n < nz; n++) hs[n] = (h[n] - h[k]) / (h[k + 1] - h[k]);
+            std::fill(c.begin(), c.end(), 0.0);
+            fornberg(hs[k], hs.data() - order / 2 + k, order, order, c.data());
+            for (int j = 0; j <= order; j++) w[(size_t)(order + 1) * k + j] = c[(order + 1) * j + order];
+        }
+        const int rows[2][2] = {{2, nz - 3}, {1, nz - 2}};
+        for (int pass = 0; pass < 2; pass++) {
+            const int lower = pass == 0 ? 4 : 2;
+            if (order <= lower) continue;
+            for (int r = 0; r < 2; r++) {
+                const int k = rows[pass][r];
+                const int top = (pass == 0 && r == 0) ? nz - 1 : nz;  // damping.cpp:200 rescales to NZ-2
+                for (int n = 0; n < top; n++) hs[n] = (h[n] - h[k]) / (h[k + 1] - h[k]);
+                std::fill(c.begin(), c.end(), 0.0);
+                fornberg(hs[k], hs.data() - lower / 2 + k, lower, lower, c.data());
+                for (int j = 0; j <= lower; j++) w[(size_t)(order + 1) * k + j] = c[(lower + 1) * j + lower];
+            }
+        }
+        return w;
+    }
     std::map<std::tuple<const void *, int, int, int>, CUtensorMap> tma_maps;  // per buffer and box
     // the four-level post-processing kernel (FP32, NZ % 4 == 0); GA_POST=column
     // keeps the per-level one
@@ -255,6 +314,11 @@ class Engine : public EngineBase {
             for (int k = 0; k < NZ; k++) wk[k] = cols->rhou[k] * dx * c->dy * c->dz / cols->mu[k];
             budget_w = upload(wk);
             budget_part = dalloc<double>((size_t)BUDGET_BLOCKS * GA_NB + GA_NB);
+        }
+        if (c->use_explicit_diffusion) {
+            diff_tend = dalloc<T>((size_t)nprog * N);
+            const std::vector<double> w = diffusion_weights(c->diffusion_order, cols->zsu, NZ);
+            diff_w = col_T(w.data(), (int)w.size());
         }
         kp.dx2 = dx * dx;
         kp.low_modes = sizeof(T) == 8 ? 0 : 1;  // FP32: the mean mode (0,0) solves in FP64
@@ -701,6 +765,21 @@ class Engine : public EngineBase {
         return sizeof(T) == 4 && kp.ubase_adv && NZ % 4 == 0 && advect_quad_smem(ti, tj, NZ) <= 200 * 1024;
     }
 
+    // apply_explicit_diffusion (damping.cpp:1125-1146) on the start-of-step slot
+    void diffuse(double step)
+    {
+        const int order = cfg.diffusion_order;
+        if (!diff_tend || !diff_w || (order != 2 && order != 4 && order != 6)) return;
+        ProfScope ps(this, PC_DIFFUSION, 2);
+        const long tot = (long)(NX - 6) * (NY - 6) * (NZ - 2) * nprog;
+        const int nb = (int)std::min((tot + 255) / 256, 152L * 8);
+        KFields<T> F = fields();
+        k_diffuse_tend<T><<<nb, 256, 0, stream>>>(kp, F, diff_tend, nprog, order, (T)cfg.kdiffh, (T)cfg.kdiffv, diff_w,
+                                                  (T)step);
+        k_diffuse_add<T><<<nb, 256, 0, stream>>>(kp, F, diff_tend, nprog);
+        launches += 2;
+    }
+
     void advect(double step, int what)
     {
         const double sdtg = step * cfg.dt * 9.8 * 0.5;  // step*dt*grav*0.5, advection.cpp:330
@@ -914,6 +993,7 @@ class Engine : public EngineBase {
             }
             break;
         case GA_OP_KESSLER: kessler(); break;
+        case GA_OP_EXPLICIT_DIFFUSION: diffuse(step); break;
         case GA_OP_RAYLEIGH:
             fl[FU] = fl[FV] = fl[FW] = fl[FTH] = PF_RAYLEIGH;
             post(fl, 7, step, false);
@@ -961,6 +1041,7 @@ class Engine : public EngineBase {
     {
         static const double steps[3] = {1. / 3., 0.5, 1.0};
         const bool moist = kp.moist;
+        if (cfg.use_explicit_diffusion) diffuse(1.0);  // driver_serial.cpp:188, before the RK stages
         for (int s = 0; s < 3; s++) {
             const double st = steps[s];
             if (rec)

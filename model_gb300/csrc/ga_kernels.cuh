@@ -2154,6 +2154,95 @@ __global__ void k_check_finite(const T *a, long n, int *flag)
 }
 
 // ---------------------------------------------------------------------------
+// Explicit diffusion of the start-of-step fields (apply_explicit_diffusion,
+// damping.cpp:1125-1146, with diffusion_{2nd,4th,6th}_var, :769-940) over
+// i in [3, NX-3), j in [3, NY-3), k in [1, NZ-1).  k_diffuse_tend forms every
+// tendency from the old values (the reference's temp_var); k_diffuse_add then
+// adds them.  The vertical operator of the stretched-grid build weights the
+// column with the finite-difference weights `dw` (order+1 per level, built
+// on the host as init_diffusion_weights does, :158-270).
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ T dif2(const T *v, long c, long s) { return v[c + s] - T(2.0) * v[c] + v[c - s]; }
+template <typename T>
+__device__ __forceinline__ T dif4(const T *v, long c, long s)
+{
+    return v[c - 2 * s] - T(4.0) * v[c - s] + T(6.0) * v[c] - T(4.0) * v[c + s] + v[c + 2 * s];
+}
+template <typename T>
+__device__ __forceinline__ T dif6(const T *v, long c, long s)
+{
+    return v[c - 3 * s] - T(6.0) * v[c - 2 * s] + T(15.0) * v[c - s] - T(20.0) * v[c] + T(15.0) * v[c + s] -
+           T(6.0) * v[c + 2 * s] + v[c + 3 * s];
+}
+
+// weighted column sums (diffuse_k_2nd/4th/6th with weights, damping.cpp:556-715)
+template <typename T>
+__device__ __forceinline__ T wk2(const T *v, long c, const T *w) { return w[0] * v[c - 1] + w[1] * v[c] + w[2] * v[c + 1]; }
+template <typename T>
+__device__ __forceinline__ T wk4(const T *v, long c, const T *w)
+{
+    return w[0] * v[c - 2] + w[1] * v[c - 1] + w[2] * v[c] + w[3] * v[c + 1] + w[4] * v[c + 2];
+}
+template <typename T>
+__device__ __forceinline__ T wk6(const T *v, long c, const T *w)
+{
+    return w[0] * v[c - 3] + w[1] * v[c - 2] + w[2] * v[c - 1] + w[3] * v[c] + w[4] * v[c + 1] + w[5] * v[c + 2] +
+           w[6] * v[c + 3];
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_diffuse_tend(KParams<T> p, KFields<T> F, T *tend, int nf, int order, T kh,
+                                                      T kv, const T *dw, T step)
+{
+    const int ni = p.nx - 6, nj = p.ny - 6, nk = p.nz - 2;
+    const long per = (long)ni * nj * nk, tot = per * nf;
+    const long sx = (long)p.ny * p.nz, sy = p.nz;
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < tot; t += (long)gridDim.x * blockDim.x) {
+        const int f = (int)(t / per);
+        long r = t - f * per;
+        const int k = 1 + (int)(r % nk);
+        r /= nk;
+        const int j = 3 + (int)(r % nj), i = 3 + (int)(r / nj);
+        const long c = gix(p.ny, p.nz, i, j, k);
+        const T *v = F.M[f];
+        const int ind = order + 1, nz = p.nz;
+        T d;
+        if (order == 2) {
+            d = kh * dif2(v, c, sx) + kh * dif2(v, c, sy) + kv * wk2(v, c, dw + ind * k);
+        } else if (order == 4) {
+            if (k == 1 || k == nz - 2)  // both ends with row NZ-2, as damping.cpp:820 and :861 do
+                d = -kh * dif4(v, c, sx) - kh * dif4(v, c, sy) + kv * wk2(v, c, dw + ind * (nz - 2));
+            else
+                d = -kh * dif4(v, c, sx) - kh * dif4(v, c, sy) - kv * wk4(v, c, dw + ind * k);
+        } else {
+            T z;
+            if (k == 1 || k == nz - 2) z = kv * wk2(v, c, dw + ind * k);
+            else if (k == 2 || k == nz - 3) z = -kv * wk4(v, c, dw + ind * k);
+            else z = kv * wk6(v, c, dw + ind * k);
+            d = kh * dif6(v, c, sx) + kh * dif6(v, c, sy) + z;
+        }
+        tend[(long)f * p.n + c] = step * d;
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_diffuse_add(KParams<T> p, KFields<T> F, const T *tend, int nf)
+{
+    const int ni = p.nx - 6, nj = p.ny - 6, nk = p.nz - 2;
+    const long per = (long)ni * nj * nk, tot = per * nf;
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < tot; t += (long)gridDim.x * blockDim.x) {
+        const int f = (int)(t / per);
+        long r = t - f * per;
+        const int k = 1 + (int)(r % nk);
+        r /= nk;
+        const int j = 3 + (int)(r % nj), i = 3 + (int)(r / nj);
+        const long c = gix(p.ny, p.nz, i, j, k);
+        F.M[f][c] += tend[(long)f * p.n + c];
+    }
+}
+
+// ---------------------------------------------------------------------------
 // FP64 domain budgets of one rotation slot.  Over the physical cells
 // i in [1, NX-1), j in [1, NY-1), k in [1, NZ-1), with the weight
 // wk[k] = rhou[k] dx dy dz / mu[k] (density times cell volume), in FP64 for

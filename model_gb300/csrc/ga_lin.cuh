@@ -525,6 +525,10 @@ int Engine<T>::lin_supported() const
         set_error("tangent-linear / adjoint: non-periodic contexts, Eulerian rain fallout (rain_fallout 1) only");
         return GA_ERR_UNSUPPORTED;
     }
+    if (cfg.use_explicit_diffusion) {
+        set_error("tangent-linear / adjoint: explicit diffusion is not linearised");
+        return GA_ERR_UNSUPPORTED;
+    }
     return GA_OK;
 }
 

@@ -623,6 +623,136 @@ static void op_rayleigh(ora_state *S) /* damping.cpp:1148-1177 */
 }
 
 /* ------------------------------------------------------------------------
+ * Explicit diffusion: apply_explicit_diffusion (damping.cpp:1125-1146) with
+ * diffusion_{2nd,4th,6th}_var (:769-940) on the start-of-step fields, over
+ * i in [3, NX-3), j in [3, NY-3), k in [1, NZ-1).  Every tendency is formed
+ * from the old values before any is added.  The vertical operator of the
+ * stretched-grid build weights the column with the finite-difference weights
+ * of init_diffusion_weights (:158-270): Fornberg's recurrence (util.cpp:
+ * 199-247) on the heights scaled by the local spacing, the order's weights
+ * for k in [order/2, NZ-order/2), 4th-order rows at k = 2 and NZ-3 (order 6)
+ * and 2nd-order rows at k = 1 and NZ-2 (orders 4 and 6).
+ * ---------------------------------------------------------------------- */
+
+/* weights c[i*(m+1)+d] of derivative d at z from the points x[0..n] */
+static void fornberg(double z, const double *x, int n, int m, double *c)
+{
+    double c1 = 1.0, c4 = x[0] - z;
+    c[0] = 1.0;
+    for (int i = 1; i <= n; i++) {
+        const int mn = i < m ? i : m;
+        double c2 = 1.0;
+        const double c5 = c4;
+        c4 = x[i] - z;
+        for (int j = 0; j <= i - 1; j++) {
+            const double c3 = x[i] - x[j];
+            c2 = c2 * c3;
+            if (j == i - 1) {
+                for (int d = mn; d >= 1; d--)
+                    c[i * (m + 1) + d] = c1 * (d * c[(i - 1) * (m + 1) + d - 1] - c5 * c[(i - 1) * (m + 1) + d]) / c2;
+                c[i * (m + 1)] = -c1 * c5 * c[(i - 1) * (m + 1)] / c2;
+            }
+            for (int d = mn; d >= 1; d--)
+                c[j * (m + 1) + d] = (c4 * c[j * (m + 1) + d] - d * c[j * (m + 1) + d - 1]) / c3;
+            c[j * (m + 1)] = c4 * c[j * (m + 1)] / c3;
+        }
+        c1 = c2;
+    }
+}
+
+/* rows of order+1 weights per level: the order's derivative at level k from
+ * levels k-lo .. k-lo+n */
+static void diffusion_weights(int order, const double *h, int NZ, double *w)
+{
+    double hs[512], c[64];
+    memset(w, 0, sizeof(double) * (size_t)(order + 1) * NZ);
+    for (int n = 0; n < NZ; n++) hs[n] = 0.0;
+    for (int k = order / 2; k < NZ - order / 2; k++) {
+        for (int n = 0; n < NZ; n++) hs[n] = (h[n] - h[k]) / (h[k + 1] - h[k]);
+        memset(c, 0, sizeof c);
+        fornberg(hs[k], hs - order / 2 + k, order, order, c);
+        for (int j = 0; j <= order; j++) w[(order + 1) * k + j] = c[(order + 1) * j + order];
+    }
+    const int rows[2][2] = {{2, NZ - 3}, {1, NZ - 2}};
+    for (int pass = 0; pass < 2; pass++) {
+        const int lower = pass == 0 ? 4 : 2;
+        if (order <= lower) continue;
+        for (int r = 0; r < 2; r++) {
+            const int k = rows[pass][r];
+            /* the row at k = 2 rescales levels 0 .. NZ-2 only (damping.cpp:200) */
+            const int top = (pass == 0 && r == 0) ? NZ - 1 : NZ;
+            for (int n = 0; n < top; n++) hs[n] = (h[n] - h[k]) / (h[k + 1] - h[k]);
+            memset(c, 0, sizeof c);
+            fornberg(hs[k], hs - lower / 2 + k, lower, lower, c);
+            for (int j = 0; j <= lower; j++) w[(order + 1) * k + j] = c[(lower + 1) * j + lower];
+        }
+    }
+}
+
+static double d2(const double *v, long c, long s) { return v[c + s] - 2.0 * v[c] + v[c - s]; }
+static double d4(const double *v, long c, long s)
+{
+    return v[c - 2 * s] - 4.0 * v[c - s] + 6.0 * v[c] - 4.0 * v[c + s] + v[c + 2 * s];
+}
+static double d6(const double *v, long c, long s)
+{
+    return v[c - 3 * s] - 6.0 * v[c - 2 * s] + 15.0 * v[c - s] - 20.0 * v[c] + 15.0 * v[c + s] - 6.0 * v[c + 2 * s] +
+           v[c + 3 * s];
+}
+/* weighted column sums of the stretched-grid operators (diffuse_k_*, :556-715) */
+static double wk2(const double *v, long c, const double *w) { return w[0] * v[c - 1] + w[1] * v[c] + w[2] * v[c + 1]; }
+static double wk4(const double *v, long c, const double *w)
+{
+    return w[0] * v[c - 2] + w[1] * v[c - 1] + w[2] * v[c] + w[3] * v[c + 1] + w[4] * v[c + 2];
+}
+static double wk6(const double *v, long c, const double *w)
+{
+    return w[0] * v[c - 3] + w[1] * v[c - 2] + w[2] * v[c - 1] + w[3] * v[c] + w[4] * v[c + 1] + w[5] * v[c + 2] +
+           w[6] * v[c + 3];
+}
+
+static void op_explicit_diffusion(ora_state *S, double step)
+{
+    const int order = S->c.diffusion_order, nf = S->c.microphysics_option ? 7 : 4, NZ = S->NZ;
+    if (order != 2 && order != 4 && order != 6) return;
+    const double kh = S->c.kdiffh, kv = S->c.kdiffv;
+    const long sx = (long)S->NY * S->NZ, sy = S->NZ;
+    const int ind = order + 1;
+    double *w = (double *)calloc((size_t)ind * NZ, sizeof(double));
+    diffusion_weights(order, S->zsu, NZ, w);
+    double *tend = (double *)calloc((size_t)S->N, sizeof(double));
+    for (int f = 0; f < nf; f++) {
+        double *v = S->M[f];
+        for (int i = 3; i < S->NX - 3; i++)
+            for (int j = 3; j < S->NY - 3; j++)
+                for (int k = 1; k < NZ - 1; k++) {
+                    const long c = IX(i, j, k);
+                    double d;
+                    if (order == 2) {
+                        d = kh * d2(v, c, sx) + kh * d2(v, c, sy) + kv * wk2(v, c, w + ind * k);
+                    } else if (order == 4) {
+                        if (k == 1 || k == NZ - 2) /* both ends with row NZ-2 (damping.cpp:820, 861) */
+                            d = -kh * d4(v, c, sx) - kh * d4(v, c, sy) + kv * wk2(v, c, w + ind * (NZ - 2));
+                        else
+                            d = -kh * d4(v, c, sx) - kh * d4(v, c, sy) - kv * wk4(v, c, w + ind * k);
+                    } else {
+                        double z;
+                        if (k == 1 || k == NZ - 2) z = kv * wk2(v, c, w + ind * k);
+                        else if (k == 2 || k == NZ - 3) z = -kv * wk4(v, c, w + ind * k);
+                        else z = kv * wk6(v, c, w + ind * k);
+                        d = kh * d6(v, c, sx) + kh * d6(v, c, sy) + z;
+                    }
+                    tend[c] = step * d;
+                }
+        for (int i = 3; i < S->NX - 3; i++)
+            for (int j = 3; j < S->NY - 3; j++)
+                for (int k = 1; k < NZ - 1; k++) v[IX(i, j, k)] += tend[IX(i, j, k)];
+    }
+    free(tend);
+    free(w);
+}
+
+/* ------------------------------------------------------------------------
  * Kessler warm rain: run_kessler_microphysics (kessler.cpp:25-213).
  * ---------------------------------------------------------------------- */
 static void kessler_points(ora_state *S)
@@ -843,6 +973,7 @@ static void rk3_step(ora_state *S) /* driver_serial.cpp:178-286 */
 {
     static const double steps[3] = {1. / 3., 0.5, 1.0};
     const int micro = S->c.microphysics_option != 0;
+    if (S->c.use_explicit_diffusion) op_explicit_diffusion(S, 1.0);
     for (int s = 0; s < 3; s++) {
         integrate_non_hydro(S, steps[s]);
         op_advect_theta(S, steps[s]);
@@ -1122,6 +1253,7 @@ int ora_op(ora_state *S, int op, double step)
     case GA_OP_RAYLEIGH: op_rayleigh(S); return GA_OK;
     case GA_OP_ADVANCE_INNER: advance_inner(S); if (S->c.microphysics_option) micro_advance_inner(S); return GA_OK;
     case GA_OP_ADVANCE_OUTER: advance_outer(S); if (S->c.microphysics_option) micro_advance(S); return GA_OK;
+    case GA_OP_EXPLICIT_DIFFUSION: op_explicit_diffusion(S, step); return GA_OK;
     }
     return GA_ERR_ARG;
 }

@@ -132,6 +132,13 @@ int main(int argc, char **argv)
     inputs.boundary_width_south = (int)scal(in, "boundary_width_south");
     inputs.boundary_width_east = (int)scal(in, "boundary_width_east");
     inputs.boundary_width_west = (int)scal(in, "boundary_width_west");
+    /* explicit diffusion (optional records; off when absent) */
+    if (has(in, "use_explicit_diffusion")) {
+        inputs.use_explicit_diffusion = (int)scal(in, "use_explicit_diffusion");
+        inputs.diffusion_order = (int)scal(in, "diffusion_order");
+        inputs.kdiffh = scal(in, "kdiffh");
+        inputs.kdiffv = scal(in, "kdiffv");
+    }
     initialize_globals();
 
     const size_t N = (size_t)NX * NY * NZ;
@@ -178,6 +185,8 @@ int main(int argc, char **argv)
     if (USE_MICROPHYSICS) init_microphysics(NX, NY);
     initialize_pressure_solver();
     init_boundaries(iebuffer, iwbuffer, jnbuffer, jsbuffer, -1);
+    init_damping(NX, NY, NZ);                       /* driver_serial.cpp:72-74 */
+    init_diffusion_weights(DIFFUSION_ORDER, &ZU(0));
 
     if (mode == "run") {
         int nsteps = atoi(argv[4]);
@@ -201,6 +210,7 @@ int main(int argc, char **argv)
         else if (name == "bc_micro") apply_boundary_condition_microphysics(0);
         else if (name == "kessler") run_microphysics(1, NX - 1, 1, NY - 1);
         else if (name == "rayleigh") rayleigh_damping(1, NX - 1, 1, NY - 1, raydampheight);
+        else if (name == "explicit_diffusion") apply_explicit_diffusion(step, 3, NX - 3, 3, NY - 3);
         else { fprintf(stderr, "unknown op %s\n", name.c_str()); return 2; }
     } else {
         fprintf(stderr, "unknown mode\n");

@@ -23,6 +23,12 @@ def load(name: str) -> dict:
 def workload(d: dict) -> configs.Workload:
     kw = {k: int(d[k]) for k in _INT_KEYS}
     kw.update({k: float(d[k]) for k in _FLOAT_KEYS})
+    for k in ("use_explicit_diffusion", "diffusion_order"):  # optional: fixtures with diffusion
+        if k in d:
+            kw[k] = int(d[k])
+    for k in ("kdiffh", "kdiffv"):
+        if k in d:
+            kw[k] = float(d[k])
     wl = configs.Workload(name="golden", nsteps=int(d["nsteps"]), **kw)
     n3 = (wl.nx, wl.ny, wl.nz)
     for k in list(d):

@@ -27,6 +27,11 @@ from oracle import oracle as O  # noqa: E402
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 
+def _diffusing(wl, order, kdiffh):
+    wl.use_explicit_diffusion, wl.diffusion_order, wl.kdiffh = 1, order, kdiffh
+    return wl
+
+
 RUN_CASES = {
     "dry": (lambda: configs.dry_bubble(nx=16, ny=14, nz=10, dx=500.0, dz=400.0, amp=3.0,
                                        radius=2000.0, zc=1500.0, noise=0.2), 4),
@@ -34,12 +39,17 @@ RUN_CASES = {
     "moist_rf2": (lambda: configs.moist_blob(nx=14, ny=13, nz=10, rain_fallout=2), 4),
     "moist_periodic": (lambda: configs.moist_blob(nx=18, ny=13, nz=10, periodic=1), 3),
     # horizontally varying basic state (jet + balanced theta), moist: the general path
+    # explicit diffusion once per step (apply_explicit_diffusion), each order
+    "diffusion2_dry": (lambda: _diffusing(configs.dry_bubble(nx=16, ny=14, nz=10, dx=500.0, dz=400.0, amp=3.0,
+                                                             radius=2000.0, zc=1500.0, noise=0.2), 2, 0.02), 3),
+    "diffusion4_moist": (lambda: _diffusing(configs.moist_blob(nx=15, ny=14, nz=10), 4, 0.004), 3),
+    "diffusion6_moist": (lambda: _diffusing(configs.moist_blob(nx=16, ny=15, nz=12), 6, 0.002), 3),
     "jet": (lambda: configs.jet_vortex(nx=16, ny=14, nz=10, dx=20000.0, dz=800.0, dt=30.0, rmax=60000.0,
                                            vmax=8.0, moist=True, noise=0.3, extra_basic=1.0), 3),
 }
 
 OP_NAMES = ["advect_uvw", "solve_pressure", "integrate_non_hydro", "advect_theta",
-            "advect_micro", "zero_moisture", "bc", "bc_micro", "kessler", "rayleigh"]
+            "advect_micro", "zero_moisture", "bc", "bc_micro", "kessler", "rayleigh", "explicit_diffusion"]
 
 
 def _inputs(wl) -> dict:
@@ -92,6 +102,8 @@ def make_ops():
         "moist_periodic_rf2": configs.moist_blob(nx=18, ny=13, nz=10, periodic=1, rain_fallout=2),
     }
     for cname, wl in cases.items():
+        # the reference allocates the diffusion work array only with the flag on
+        _diffusing(wl, 4, 0.005)
         extra = _ops_state(wl, 5000)
         d = _inputs(wl)
         for k, v in extra.items():

@@ -334,6 +334,17 @@ def test_gpu_vorticity_gradient_matches_finite_differences(built):
 
 
 @pytest.mark.gpu
+def test_gpu_adjoint_rejects_explicit_diffusion(built):
+    from model_gb300 import anelastic
+    wl = configs.moist_blob(nx=20, ny=18, nz=12)
+    wl.use_explicit_diffusion, wl.diffusion_order = 1, 4
+    m = anelastic.Model(wl, abi.GA_PREC_F64)
+    with pytest.raises(anelastic.GaError):
+        m.lin_set(abi.GA_U, abi.GA_SLOT_CUR, np.zeros(wl.points))
+    assert "diffusion" in anelastic.last_error()
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("kw", [dict(rain_fallout=2), dict(periodic=1)])
 def test_gpu_adjoint_rejects_unsupported(built, kw):
     """Semi-Lagrangian rain fallout and periodic boundaries are not linearised."""

@@ -16,7 +16,7 @@ from tests import fixtures as fx
 
 pytestmark = pytest.mark.gpu
 
-EXACT_OPS = {"advect_uvw", "advect_theta", "zero_moisture", "bc", "bc_micro", "rayleigh"}
+EXACT_OPS = {"advect_uvw", "advect_theta", "zero_moisture", "bc", "bc_micro", "rayleigh", "explicit_diffusion"}
 
 
 @pytest.fixture(scope="module", autouse=True)
@@ -45,7 +45,8 @@ def test_full_steps_match_reference(name):
 
 @pytest.mark.parametrize("name", fx.ops_names())
 @pytest.mark.parametrize("op", ["advect_uvw", "solve_pressure", "integrate_non_hydro", "advect_theta",
-                                "advect_micro", "zero_moisture", "bc", "bc_micro", "kessler", "rayleigh"])
+                                "advect_micro", "zero_moisture", "bc", "bc_micro", "kessler", "rayleigh",
+                                "explicit_diffusion"])
 def test_single_operator_matches_reference(name, op):
     d = fx.load(name)
     wl = fx.workload(d)
@@ -117,6 +118,23 @@ def test_fp32_error_against_fp64():
     print("fp32 vs fp64 after 60 steps", {k: f"{v:.2e}" for k, v in errs.items()})
     for k in ("u", "v", "w", "th", "qv"):
         assert errs[k] <= 1e-4, (k, errs[k])
+
+
+@pytest.mark.parametrize("order", [2, 4, 6])
+def test_explicit_diffusion_thunderstorm_vs_oracle(order):
+    """full-size thunderstorm with explicit diffusion of each order: FP64
+    against the oracle after 6 steps, and FP32 against FP64"""
+    from model_gb300 import configs
+    wl = configs.thunderstorm()
+    wl.use_explicit_diffusion, wl.diffusion_order, wl.kdiffh, wl.kdiffv = 1, order, 0.004, 0.004
+    _oracle_compare(wl, 6, 1e-10)
+    a = anelastic.Model(wl, abi.GA_PREC_F32)
+    b = anelastic.Model(wl, abi.GA_PREC_F64)
+    a.step(6)
+    b.step(6)
+    for f in range(7):
+        e = fx.rel_l2(a.get(f), b.get(f))
+        assert e <= 1e-4, (abi.PROG_NAMES[f], e)
 
 
 def test_step_is_deterministic():
