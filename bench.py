@@ -310,6 +310,9 @@ def ensemble_bench(torch, device, steps, warmup, n_small=64, n_large=32):
            "setup_s": round(setup, 1), "precision": "fp32",
            "tuning": {"choice": tuning, "seconds": round(t_tune, 2)},
            "note": "one launch per kernel phase over all members; two-step CUDA graph"}
+    peak, peak_kind = load_peaks()
+    out["hbm_fraction"] = round(out["value"] * STEP_BYTES_FP32_MOIST / 1e9 / peak, 4)
+    out["hbm_peak"] = {"gbs": peak, "source": peak_kind, "bytes_per_gridpoint_step": STEP_BYTES_FP32_MOIST}
     ens.close()
     return out
 
