@@ -78,6 +78,19 @@ extern "C" {
 #define GA_NFIELDS 15
 /* 2-D field: accumulated rain accRain[NX][NY] (microphysics.h:25)           */
 #define GA_ACCRAIN 15
+/* turbulence diagnostics of a context with turbulence_option set, as of the
+ * last calculate_diff_tend (turbulence.cpp:23-31); read-only through
+ * ga_get_field (ga_set_field accepts them for operator tests)               */
+#define GA_KMIX    16  /* Kmix: vertical mixing coefficient (w levels)        */
+#define GA_KHMIX   17  /* KHmix: horizontal mixing coefficient                */
+#define GA_UFRIC   18  /* u_friction: stress divergence of u (m s^-2)        */
+#define GA_VFRIC   19  /* v_friction                                          */
+#define GA_WFRIC   20  /* w_friction                                          */
+#define GA_THDIFF  21  /* t_diffusion: flux divergence of theta (K s^-1)     */
+#define GA_QVDIFF  22  /* qv_diffusion (moist contexts)                       */
+#define GA_QCDIFF  23  /* qc_diffusion                                        */
+#define GA_QRDIFF  24  /* qr_diffusion                                        */
+#define GA_SATURATED 25 /* isSaturated of the last Kessler call, as 0 / 1     */
 
 /* rotation slots */
 #define GA_SLOT_CUR 0  /* us  : middle of the RK stage                        */
@@ -100,7 +113,8 @@ extern "C" {
 #define GA_OP_ADVANCE_INNER    12  /* advance_inner + microphysics_advance_inner solver.cpp:241, microphysics.cpp:642 */
 #define GA_OP_ADVANCE_OUTER    13  /* advance_outer + microphysics_advance       solver.cpp:254, microphysics.cpp:657 */
 #define GA_OP_EXPLICIT_DIFFUSION 14 /* apply_explicit_diffusion  damping.cpp:1125 (on the start-of-step slot) */
-#define GA_OP_COUNT            15
+#define GA_OP_TURBULENCE       15  /* calculate_diff_tend(1,NX-1,1,NY-1) turbulence.cpp:158 (needs turbulence_option) */
+#define GA_OP_COUNT            16
 
 /*
  * Runtime configuration: the subset of the reference's struct input_params
@@ -129,6 +143,16 @@ typedef struct ga_config {
     int    diffusion_order;         /* DIFFUSION_ORDER: 2, 4 or 6                    */
     double kdiffh, kdiffv;          /* horizontal / vertical coefficients (kmixh*,   */
                                     /* kmixv*, damping.cpp:122-129)                  */
+    /* turbulence: mixing coefficients and stress / scalar flux tendencies from
+     * the start-of-step fields once per step (calculate_diff_tend,
+     * turbulence.cpp:158-292, called at driver_serial.cpp:194), added in every
+     * RK stage (apply_velocity/scalar/moisture_diffusion, :233-290); flat ground
+     * and an all-ocean surface (the reference's land-sea mask without a file,
+     * :370-375) */
+    int    turbulence_option;       /* USE_TURBULENT_STRESS: 0 or 1                  */
+    int    use_surface_heat_flux;   /* SURFACE_HEAT_FLUX: surface heat and vapour    */
+                                    /* fluxes of a moist run                         */
+    double water_temp;              /* WATER_TEMP_C: sea-surface temperature (C)     */
 } ga_config;
 
 /*

@@ -24,6 +24,13 @@ GA_NPROG = 7
 GA_PI, GA_UBAR, GA_VBAR, GA_WBAR, GA_THBAR, GA_QBAR, GA_PBAR, GA_VT = range(7, 15)
 GA_NFIELDS = 15
 GA_ACCRAIN = 15
+# turbulence diagnostics (contexts with turbulence_option set)
+GA_KMIX, GA_KHMIX, GA_UFRIC, GA_VFRIC, GA_WFRIC, GA_THDIFF, GA_QVDIFF, GA_QCDIFF, GA_QRDIFF, GA_SATURATED = \
+    range(16, 26)
+# bundle names of the turbulence diagnostics (turbulence.cpp:23-31)
+TURB_NAMES = {"kmix": GA_KMIX, "khmix": GA_KHMIX, "u_friction": GA_UFRIC, "v_friction": GA_VFRIC,
+              "w_friction": GA_WFRIC, "t_diffusion": GA_THDIFF, "qv_diffusion": GA_QVDIFF,
+              "qc_diffusion": GA_QCDIFF, "qr_diffusion": GA_QRDIFF, "is_saturated": GA_SATURATED}
 
 GA_SLOT_CUR, GA_SLOT_P, GA_SLOT_M = 0, 1, 2
 
@@ -31,7 +38,7 @@ OPS = {
     "sign_cells": 0, "advect_uvw": 1, "solve_pressure": 2, "project": 3,
     "integrate_non_hydro": 4, "advect_theta": 5, "advect_micro": 6, "zero_moisture": 7,
     "bc": 8, "bc_micro": 9, "kessler": 10, "rayleigh": 11, "advance_inner": 12,
-    "advance_outer": 13, "explicit_diffusion": 14,
+    "advance_outer": 13, "explicit_diffusion": 14, "turbulence": 15,
 }
 
 # names used in bundles / fixtures
@@ -58,6 +65,7 @@ class GaConfig(C.Structure):
         ("rayleigh_damping_z", C.c_int), ("precision", C.c_int), ("device", C.c_int),
         ("use_explicit_diffusion", C.c_int), ("diffusion_order", C.c_int),
         ("kdiffh", C.c_double), ("kdiffv", C.c_double),
+        ("turbulence_option", C.c_int), ("use_surface_heat_flux", C.c_int), ("water_temp", C.c_double),
     ]
 
 

@@ -78,6 +78,10 @@ class Workload:
     diffusion_order: int = 4
     kdiffh: float = 0.005
     kdiffv: float = 0.005
+    # turbulence (calculate_diff_tend, turbulence.cpp:158); off by default
+    turbulence_option: int = 0
+    use_surface_heat_flux: int = 0
+    water_temp: float = 28.0
     fields: dict = dataclasses.field(default_factory=dict)
 
     def __post_init__(self):
@@ -95,7 +99,7 @@ class Workload:
                 "periodic_ew_boundaries", "boundary_width_north", "boundary_width_south",
                 "boundary_width_east", "boundary_width_west", "rayleigh_damping_z",
                 "height_lowest_level", "corner_lat", "use_explicit_diffusion", "diffusion_order", "kdiffh",
-                "kdiffv")
+                "kdiffv", "turbulence_option", "use_surface_heat_flux", "water_temp")
         return {k: getattr(self, k) for k in keys}
 
 

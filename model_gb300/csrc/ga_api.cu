@@ -133,6 +133,9 @@ int ga_create(const ga_config *cfg, const ga_columns *cols, ga_ctx **out)
     if (cfg->use_explicit_diffusion && cfg->diffusion_order != 2 && cfg->diffusion_order != 4 &&
         cfg->diffusion_order != 6)
         return fail(GA_ERR_CONFIG, "ga_create: diffusion_order must be 2, 4 or 6");
+    if (cfg->turbulence_option < 0 || cfg->turbulence_option > 1 || cfg->use_surface_heat_flux < 0 ||
+        cfg->use_surface_heat_flux > 1)
+        return fail(GA_ERR_CONFIG, "ga_create: turbulence_option and use_surface_heat_flux must be 0 or 1");
     int rc = GA_OK;
     ga::EngineBase *e = nullptr;
     try {
@@ -159,7 +162,7 @@ int ga_destroy(ga_ctx *ctx)
 int ga_set_field(ga_ctx *ctx, int field, int slot, const double *host, size_t n)
 {
     if (!ctx || !host) return fail(GA_ERR_ARG, "ga_set_field: null pointer");
-    if (field < 0 || field > GA_ACCRAIN || slot < 0 || slot > 2) return fail(GA_ERR_ARG, "ga_set_field: bad field or slot");
+    if (field < 0 || field > GA_SATURATED || slot < 0 || slot > 2) return fail(GA_ERR_ARG, "ga_set_field: bad field or slot");
     int rc = ctx->e->set_field(field, slot, host, n);
     if (rc == GA_ERR_ARG) set_error("ga_set_field: field not present in this context or wrong size");
     return rc;
@@ -168,7 +171,7 @@ int ga_set_field(ga_ctx *ctx, int field, int slot, const double *host, size_t n)
 int ga_get_field(ga_ctx *ctx, int field, int slot, double *host, size_t n)
 {
     if (!ctx || !host) return fail(GA_ERR_ARG, "ga_get_field: null pointer");
-    if (field < 0 || field > GA_ACCRAIN || slot < 0 || slot > 2) return fail(GA_ERR_ARG, "ga_get_field: bad field or slot");
+    if (field < 0 || field > GA_SATURATED || slot < 0 || slot > 2) return fail(GA_ERR_ARG, "ga_get_field: bad field or slot");
     int rc = ctx->e->get_field(field, slot, host, n);
     if (rc == GA_ERR_ARG) set_error("ga_get_field: field not present in this context or wrong size");
     return rc;
@@ -306,7 +309,7 @@ void *ga_stream(ga_ctx *ctx) { return ctx ? (void *)ctx->e->stream : nullptr; }
 
 void *ga_field_device_ptr(ga_ctx *ctx, int field, int slot)
 {
-    if (!ctx || field < 0 || field > GA_ACCRAIN || slot < 0 || slot > 2) return nullptr;
+    if (!ctx || field < 0 || field > GA_QRDIFF || slot < 0 || slot > 2) return nullptr;
     return ctx->e->field_ptr(field, slot);
 }
 
@@ -323,6 +326,8 @@ int ga_ensemble_create(const ga_config *cfgs, const ga_columns *cols, int nmembe
             return fail(GA_ERR_UNSUPPORTED, "ga_ensemble_create: periodic members are not batched");
         if (c.use_explicit_diffusion)
             return fail(GA_ERR_UNSUPPORTED, "ga_ensemble_create: explicit diffusion is not batched");
+        if (c.turbulence_option)
+            return fail(GA_ERR_UNSUPPORTED, "ga_ensemble_create: the turbulence scheme is not batched");
         if (c.microphysics_option == 1 && c.rain_fallout != 1)
             return fail(GA_ERR_UNSUPPORTED, "ga_ensemble_create: only Eulerian rain fallout is batched");
         if (c.nx < 12 || c.ny < 12 || c.nz < 6 || c.nz > 128 || !(c.dx > 0 && c.dy > 0 && c.dz > 0 && c.dt > 0))

@@ -15,6 +15,7 @@
 #include "ga_engine.h"
 #include "ga_kernels.cuh"
 #include "ga_quad.cuh"
+#include "ga_turb.cuh"
 
 #include <cudaTypedefs.h>
 
@@ -117,6 +118,10 @@ class Engine : public EngineBase {
     double *budget_w = nullptr, *budget_part = nullptr;  // FP64 budget weights and partial sums
     T *diff_tend = nullptr;  // explicit diffusion: tendencies of every prognostic field
     const T *diff_w = nullptr;  // and the vertical finite-difference weights, order+1 per level
+    // turbulence: coefficients, tendencies, tables (ga_turb.cuh); turb.kmix
+    // is null when the scheme is off.  turb_sat is Kessler's saturation record.
+    TurbArgs<T> turb{};
+    unsigned char *turb_sat = nullptr;
 
     // Fornberg's recurrence for finite-difference weights: c[i*(m+1)+d] is the
     // weight of point x[i] in derivative d at z (util.cpp:199-247)
@@ -315,6 +320,30 @@ class Engine : public EngineBase {
             budget_w = upload(wk);
             budget_part = dalloc<double>((size_t)BUDGET_BLOCKS * GA_NB + GA_NB);
         }
+        if (c->turbulence_option) {  // init_kmix (turbulence.cpp:85-151)
+            turb.kmix = dalloc<T>(N);
+            turb.khmix = dalloc<T>(N);
+            T *tt = dalloc<T>((size_t)nprog * N);
+            for (int f = 0; f < 7; f++) turb.tend[f] = f < nprog ? tt + (size_t)f * N : nullptr;
+            if (moist) turb_sat = dalloc<unsigned char>(N);
+            turb.sat = turb_sat;
+            std::vector<double> l2(NZ, 0.0), kv(NZ, 0.0);
+            for (int k = 1; k < NZ; k++) {
+                const double dzk = cols->zsu[k] - cols->zsu[k - 1];
+                l2[k] = dzk > 200.0 ? 200.0 * 200.0 : dzk * dzk;  // lv_max = 200 m
+                kv[k] = 0.15 * l2[k] / dt;                         // cmixv_max = 0.15
+            }
+            turb.l2 = col_T(l2.data(), NZ);
+            turb.kvmax = col_T(kv.data(), NZ);
+            turb.tbw = col_T(cols->tbw, NZ);
+            turb.kmixh_max = (T)(0.05 * dx * dx / dt);  // cmixh_max = 0.05
+            turb.lH = (T)(dx / 4.0);
+            const double wt = c->water_temp + 273.15;
+            turb.water_temp = (T)wt;
+            turb.es_water = (T)(611.2 * exp(17.67 * (wt - 273.15) / (wt - 29.65)));
+            turb.dp_to_surface = (T)(9.8 * cols->zsu[1] / (1004.0 * cols->tbv[1]));
+            turb.surface_flux = c->use_surface_heat_flux && moist;
+        }
         if (c->use_explicit_diffusion) {
             diff_tend = dalloc<T>((size_t)nprog * N);
             const std::vector<double> w = diffusion_weights(c->diffusion_order, cols->zsu, NZ);
@@ -476,6 +505,7 @@ class Engine : public EngineBase {
         F.vt = vt;
         F.accrain = accrain;
         F.qmask = qmask;
+        F.sat = turb_sat;
         return F;
     }
 
@@ -494,6 +524,10 @@ class Engine : public EngineBase {
         case GA_UBAR: case GA_VBAR: case GA_WBAR: case GA_THBAR: case GA_QBAR: case GA_PBAR:
             return bar[field - GA_UBAR];
         case GA_VT: return vt;
+        case GA_KMIX: return turb.kmix;
+        case GA_KHMIX: return turb.kmix ? turb.khmix : nullptr;
+        case GA_UFRIC: case GA_VFRIC: case GA_WFRIC: case GA_THDIFF: case GA_QVDIFF: case GA_QCDIFF: case GA_QRDIFF:
+            return turb.kmix ? turb.tend[field - GA_UFRIC] : nullptr;
         }
         return nullptr;
     }
@@ -511,10 +545,27 @@ class Engine : public EngineBase {
         return GA_OK;
     }
 
+    // the saturation record as 0 / 1 values
+    int sat_field(double *get, const double *set, size_t n)
+    {
+        if (!turb_sat || n != (size_t)N) return GA_ERR_ARG;
+        std::vector<unsigned char> h(N);
+        if (set) {
+            for (long x = 0; x < N; x++) h[x] = set[x] != 0;
+            cudaMemcpyAsync(turb_sat, h.data(), N, cudaMemcpyHostToDevice, stream);
+            return sync_status();
+        }
+        cudaMemcpyAsync(h.data(), turb_sat, N, cudaMemcpyDeviceToHost, stream);
+        const int rc = sync_status();
+        for (long x = 0; x < N; x++) get[x] = h[x];
+        return rc;
+    }
+
     int set_field(int field, int slot, const double *host, size_t n) override
     {
         if (!host) return GA_ERR_ARG;
         cudaSetDevice(device);
+        if (field == GA_SATURATED) return sat_field(nullptr, host, n);
         if (field == GA_ACCRAIN) {
             if (n != (size_t)NX * NY) return GA_ERR_ARG;
             cudaMemcpyAsync(accrain, host, n * sizeof(double), cudaMemcpyHostToDevice, stream);
@@ -547,6 +598,7 @@ class Engine : public EngineBase {
     {
         if (!host) return GA_ERR_ARG;
         cudaSetDevice(device);
+        if (field == GA_SATURATED) return sat_field(host, nullptr, n);
         if (field == GA_ACCRAIN) {
             if (n != (size_t)NX * NY) return GA_ERR_ARG;
             cudaMemcpyAsync(host, accrain, n * sizeof(double), cudaMemcpyDeviceToHost, stream);
@@ -780,6 +832,30 @@ class Engine : public EngineBase {
         launches += 2;
     }
 
+    // calculate_diff_tend (turbulence.cpp:158-188) from the start-of-step slot
+    void turbulence()
+    {
+        if (!turb.kmix) return;
+        ProfScope ps(this, PC_TURBULENCE, 2);
+        KFields<T> F = fields();
+        const int kx = (NZ + 31) / 32 * 32, cy = std::max(1, 256 / kx);
+        const long ncol = (long)(NX - 2) * (NY - 2);
+        const size_t sm = (size_t)cy * kx * (sizeof(T) + 1);
+        k_turb_kmix<T><<<cdiv(ncol, cy), dim3(kx, cy), sm, stream>>>(kp, F, turb);
+        const long tot = (long)(NX - 2) * (NY - 2) * (NZ - 2);
+        k_turb_tend<T><<<cdiv(tot, 256), 256, 0, stream>>>(kp, F, turb);
+        launches += 2;
+    }
+    // the tendencies' share of an RK stage (apply_*_diffusion, :233-290)
+    void turb_apply(int what, double step)
+    {
+        if (!turb.kmix) return;
+        ProfScope ps(this, PC_TURBULENCE, 1);
+        const long tot = (long)(NX - 2) * (NY - 2) * (NZ - 2);
+        k_turb_apply<T><<<cdiv(tot, 256), 256, 0, stream>>>(kp, fields(), turb, what, (T)(step * cfg.dt), (T)step);
+        launches++;
+    }
+
     void advect(double step, int what)
     {
         const double sdtg = step * cfg.dt * 9.8 * 0.5;  // step*dt*grav*0.5, advection.cpp:330
@@ -967,6 +1043,7 @@ class Engine : public EngineBase {
             break;
         case GA_OP_INTEGRATE_NON_HYDRO:
             advect(step, ADV_UV | ADV_WB);
+            turb_apply(TA_VEL, step);  // solver.cpp:103
             solve_pressure(step);
             fl[FU] = fl[FV] = fl[FW] = PF_PROJECT;
             post(fl, 7, step, false);
@@ -994,6 +1071,10 @@ class Engine : public EngineBase {
             break;
         case GA_OP_KESSLER: kessler(); break;
         case GA_OP_EXPLICIT_DIFFUSION: diffuse(step); break;
+        case GA_OP_TURBULENCE:
+            if (!turb.kmix) return GA_ERR_ARG;
+            turbulence();
+            break;
         case GA_OP_RAYLEIGH:
             fl[FU] = fl[FV] = fl[FW] = fl[FTH] = PF_RAYLEIGH;
             post(fl, 7, step, false);
@@ -1042,6 +1123,8 @@ class Engine : public EngineBase {
         static const double steps[3] = {1. / 3., 0.5, 1.0};
         const bool moist = kp.moist;
         if (cfg.use_explicit_diffusion) diffuse(1.0);  // driver_serial.cpp:188, before the RK stages
+        const bool turbulent = turb.kmix != nullptr;
+        if (turbulent) turbulence();  // driver_serial.cpp:194
         for (int s = 0; s < 3; s++) {
             const double st = steps[s];
             if (rec)
@@ -1052,7 +1135,13 @@ class Engine : public EngineBase {
             // the four-level advection launch also makes the mirror copies of
             // the pressure solve (they touch no point the advection writes)
             const bool fuse_mirror = !kp.periodic && adv_quad && quad_ok(adv_qi, adv_qj);
-            advect(st, ADV_UV | ADV_WB | ADV_TH | (moist ? (ADV_Q | ADV_ZERO) : 0) | (fuse_mirror ? ADV_MIRROR : 0));
+            // with turbulence the stage's tendencies come after the advection
+            // and before zero_moisture (driver_serial.cpp:205-230), which the
+            // post-processing pass then applies; they touch no point that the
+            // mirror copies read
+            const int zero = turbulent ? 0 : ADV_ZERO;
+            advect(st, ADV_UV | ADV_WB | ADV_TH | (moist ? (ADV_Q | zero) : 0) | (fuse_mirror ? ADV_MIRROR : 0));
+            if (turbulent) turb_apply(TA_VEL | TA_TH | TA_Q, st);
             qmask = nullptr;
             if (fuse_mirror) poisson(st);
             else solve_pressure(st);

@@ -11,9 +11,10 @@ namespace ga {
 
 // kernel groups timed by the optional event profiler
 enum ProfCat { PC_ADVECT = 0, PC_EDGES, PC_DIV_FFT_Y, PC_FFT_X, PC_THOMAS, PC_IFFT_Y_PI, PC_POST, PC_KESSLER,
-               PC_PPM, PC_COPY, PC_DIFFUSION, PC_COUNT };
+               PC_PPM, PC_COPY, PC_DIFFUSION, PC_TURBULENCE, PC_COUNT };
 static const char *const kProfNames[PC_COUNT] = {"advect", "edges", "div_fft_y", "fft_x", "thomas",
-                                                 "ifft_y_pi", "post", "kessler", "ppm", "copy", "diffusion"};
+                                                 "ifft_y_pi", "post", "kessler", "ppm", "copy", "diffusion",
+                                                 "turbulence"};
 
 // tangent-linear / adjoint state of an engine (ga_lin.cuh)
 struct LinBase {

@@ -77,6 +77,8 @@ struct KFields {
     // zero_moisture clipped (bit 0 qv, 1 qc, 2 qr) -- the branch record of
     // the linearisation
     unsigned char *qmask;
+    // optional: Kessler's saturation record for the turbulence scheme
+    unsigned char *sat;
 };
 
 enum { FU = 0, FV, FW, FTH, FQV, FQC, FQR };
@@ -1857,7 +1859,8 @@ struct KesPoint {
 // place from themselves and pi.  Returns true where the reference exits
 // (evaporation E > 100, kessler.cpp:83-88).
 template <typename S, typename T>
-__device__ __forceinline__ bool kessler_point(S &thp, S &qvp, S &qcp, S &qrp, const S &pi, const KesPoint<T> &c)
+__device__ __forceinline__ bool kessler_point(S &thp, S &qvp, S &qcp, S &qrp, const S &pi, const KesPoint<T> &c,
+                                              unsigned char *sat = nullptr)
 {
     const T cp = T(1004), p0 = T(100000), Lv = T(2.5e6);
     const T cpRd = T(1004.0 / 287.0);
@@ -1898,8 +1901,20 @@ __device__ __forceinline__ bool kessler_point(S &thp, S &qvp, S &qcp, S &qrp, co
     S tm = temperature - T(29.65);
     S phi = pd / (pd - esl) * qvsat * fcoef / (tm * tm);
     S C = zero;
-    if (val(vapor) > val(qvsat)) C = (vapor - qvsat) / (T(1.0) + phi);
-    else if (val(vapor) < val(qvsat) && val(qcp) > 0) C = kneg(kmin(qcp, (qvsat - vapor) / (T(1.0) + phi)));
+    // the saturation record of the turbulence scheme (isSaturated,
+    // kessler.cpp:137-163): saturated after condensation, after a partial
+    // evaporation of the cloud, or at exact saturation
+    unsigned char s_rec;
+    if (val(vapor) > val(qvsat)) {
+        C = (vapor - qvsat) / (T(1.0) + phi);
+        s_rec = 1;
+    } else if (val(vapor) < val(qvsat) && val(qcp) > 0) {
+        C = kneg(kmin(qcp, (qvsat - vapor) / (T(1.0) + phi)));
+        s_rec = -val(C) < val(qcp);
+    } else {
+        s_rec = val(vapor) == val(qvsat);
+    }
+    if (sat) *sat = s_rec;
     qcp = qcp + C;
     qvp = qvp - C;
     S dc = (Lv / (cp * pressure)) * C;
@@ -1934,7 +1949,8 @@ __device__ void kessler_body(const KParams<T> &p, const KFields<T> &F, int preci
     T *THP = F.P[FTH], *QVP = F.P[FQV], *QCP = F.P[FQC], *QRP = F.P[FQR];
     T thp = THP[ix], qvp = QVP[ix], qcp = QCP[ix], qrp = QRP[ix];
     const T piv = F.pi[ix];
-    if (kessler_point(thp, qvp, qcp, qrp, piv, kes_point(p, F, k, ix))) atomicExch(err, 1);
+    if (kessler_point(thp, qvp, qcp, qrp, piv, kes_point(p, F, k, ix), F.sat ? F.sat + ix : nullptr))
+        atomicExch(err, 1);
     THP[ix] = thp;
     QVP[ix] = qvp;
     QCP[ix] = qcp;

@@ -529,6 +529,10 @@ int Engine<T>::lin_supported() const
         set_error("tangent-linear / adjoint: explicit diffusion is not linearised");
         return GA_ERR_UNSUPPORTED;
     }
+    if (cfg.turbulence_option) {
+        set_error("tangent-linear / adjoint: the turbulence scheme is not linearised");
+        return GA_ERR_UNSUPPORTED;
+    }
     return GA_OK;
 }
 

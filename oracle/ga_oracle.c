@@ -63,6 +63,13 @@ struct ora_state {
     /* PPM remap scratch; qp_edges persists between calls as in the reference */
     double *qp_edges, *qn_edges, *mono;
     double *za, *qa, *qd, *ve;
+    /* turbulence (turbulence.cpp): mixing coefficients, the tendencies of
+     * the step (u, v, w friction; theta, qv, qc, qr diffusion), Kessler's
+     * saturation record, the vertical mixing-length tables */
+    double *kmix, *khmix, *ttend[7];
+    unsigned char *sat;
+    double *l2, *kvmax;
+    double kmixh_max, lH, water_temp, es_water;
     long long bigcounter;
     double mtime;
     int err;
@@ -753,6 +760,344 @@ static void op_explicit_diffusion(ora_state *S, double step)
 }
 
 /* ------------------------------------------------------------------------
+ * Turbulence (turbulence.cpp): once per step, from the start-of-step fields,
+ * the mixing coefficients (get_Kmix / get_Kmix_dry, :563-835) and the
+ * tendencies of the turbulent stress (turbulent_diffusion_velocity,
+ * :839-1022) and scalar fluxes (turbulent_diffusion_scalars / _theta,
+ * :1027-1276); in every RK stage they are added to the forecast fields
+ * (apply_*_diffusion, :233-290).  Flat ground (HTOPO = 0) and an all-ocean
+ * surface.  The reference's YZ-slab sweep keeps the previous slab's stresses
+ * as the "west" ones and carries each level's vertical flux to the next
+ * level; both are the stress or flux of the neighbouring point, evaluated
+ * here by the same expressions where they are used.
+ * ---------------------------------------------------------------------- */
+static const double tb_cs = 0.25, tb_one_d_Pr = 3.0, tb_lv_max = 200.0, tb_cmixh_max = 0.05,
+                    tb_cmixv_max = 0.15;
+
+static void turb_init(ora_state *S) /* init_kmix, turbulence.cpp:85-151 */
+{
+    const int NZ = S->NZ;
+    S->kmix = (double *)calloc((size_t)S->N, sizeof(double));
+    S->khmix = (double *)calloc((size_t)S->N, sizeof(double));
+    for (int t = 0; t < 7; t++) S->ttend[t] = (double *)calloc((size_t)S->N, sizeof(double));
+    S->sat = (unsigned char *)calloc((size_t)S->N, 1);
+    S->l2 = (double *)calloc(NZ, sizeof(double));
+    S->kvmax = (double *)calloc(NZ, sizeof(double));
+    S->kmixh_max = tb_cmixh_max * S->dx * S->dx / S->dt;
+    S->lH = S->dx / 4.0;
+    for (int k = 1; k < NZ; k++) {
+        const double dz = S->zsu[k] - S->zsu[k - 1];
+        S->l2[k] = dz > tb_lv_max ? tb_lv_max * tb_lv_max : dz * dz;
+        S->kvmax[k] = tb_cmixv_max * S->l2[k] / S->dt;
+    }
+    S->water_temp = S->c.water_temp + 273.15;
+    S->es_water = 611.2 * exp(17.67 * (S->water_temp - 273.15) / (S->water_temp - 29.65));
+}
+
+static void turb_kmix(ora_state *S)
+{
+    const int NX = S->NX, NY = S->NY, NZ = S->NZ, moist = S->c.microphysics_option != 0;
+    const long sx = (long)NY * NZ, sy = NZ;
+    const double *U = S->M[F_U], *V = S->M[F_V], *W = S->M[F_W], *TH = S->M[F_TH];
+    const double *UB = S->bar[0], *VB = S->bar[1], *WB = S->bar[2], *THB = S->bar[3], *QB = S->bar[4],
+                 *PB = S->bar[5];
+    const double odx = S->one_d_dx, ody = S->one_d_dy, cpRd = cp / Rd;
+    for (int i = 1; i < NX - 1; i++)
+        for (int j = 1; j < NY - 1; j++) {
+            S->kmix[IX(i, j, 1)] = 0;
+            S->kmix[IX(i, j, NZ - 1)] = 0;
+            for (int k = 2; k < NZ - 1; k++) {
+                const long c = IX(i, j, k);
+                const double odzw = S->one_d_dz * S->mw[k];
+                const double D11 = 0.50 *
+                                   (U[c + sx] + U[c + sx - 1] - U[c - sx] - U[c - sx - 1] + UB[c + sx] + UB[c + sx - 1] -
+                                    UB[c - sx] - UB[c - sx - 1]) *
+                                   odx;
+                const double D22 = 0.50 *
+                                   (V[c + sy] + V[c + sy - 1] - V[c - sy] - V[c - sy - 1] + VB[c + sy] + VB[c + sy - 1] -
+                                    VB[c - sy] - VB[c - sy - 1]) *
+                                   ody;
+                const double D33 = 1.0 * (W[c + 1] - W[c - 1] + WB[c + 1] - WB[c - 1]) * odzw;
+                const double D12 =
+                    0.5 * ((U[c + sy] + U[c + sy - 1] - U[c - sy] - U[c - sy - 1] + UB[c + sy] + UB[c + sy - 1] -
+                            UB[c - sy] - UB[c - sy - 1]) *
+                               ody +
+                           (V[c + sx] + V[c + sx - 1] - V[c - sx] - V[c - sx - 1] + VB[c + sx] + VB[c + sx - 1] -
+                            VB[c - sx] - VB[c - sx - 1]) *
+                               odx);
+                const double D13 = 0.5 * ((U[c] + U[c + sx] - U[c - 1] - U[c + sx - 1] + UB[c] + UB[c + sx] -
+                                           UB[c - 1] - UB[c + sx - 1]) *
+                                              odzw +
+                                          (W[c + sx] - W[c - sx] + WB[c + sx] - WB[c - sx]) * odx);
+                const double D23 = 0.5 * ((V[c] + V[c + sy] - V[c - 1] - V[c + sy - 1] + VB[c] + VB[c + sy] -
+                                           VB[c - 1] - VB[c + sy - 1]) *
+                                              odzw +
+                                          (W[c + sy] - W[c - sy] + WB[c + sy] - WB[c - sy]) * ody);
+                const double S2 = D11 * D11 + D22 * D22 + D33 * D33 + D12 * D12 + D13 * D13 + D23 * D23;
+                double bruntv;
+                if (!moist) {
+                    const double hi = (TH[c] + THB[c] + S->tb[k]) * (1 + 0.61 * S->qb[k]);
+                    const double lo = (TH[c - 1] + THB[c - 1] + S->tb[k - 1]) * (1 + 0.61 * S->qb[k - 1]);
+                    bruntv = 2.0 * grav / (S->tbv[k] + S->tbv[k - 1]) * (hi - lo) * odzw;
+                } else {
+                    const double *QV = S->M[F_QV], *QC = S->M[F_QC], *QR = S->M[F_QR], *PI = S->pi;
+                    if (!S->sat[c] || !S->sat[c - 1]) {
+                        const double hi = (TH[c] + THB[c] + S->tb[k]) * (1 + 0.61 * (QV[c] + QB[c] + S->qb[k]));
+                        const double lo =
+                            (TH[c - 1] + THB[c - 1] + S->tb[k - 1]) * (1 + 0.61 * (QV[c - 1] + QB[c - 1] + S->qb[k - 1]));
+                        bruntv = 2.0 * grav / (S->tbv[k] + S->tbv[k - 1]) * (hi - lo) * odzw;
+                    } else {
+                        double hi = TH[c] + THB[c] + S->tb[k];
+                        double lo = TH[c - 1] + THB[c - 1] + S->tb[k - 1];
+                        const double tH = hi * (PB[c] + PI[c] / (cp * S->tbv[k]));
+                        const double tL = lo * (PB[c - 1] + PI[c - 1] / (cp * S->tbv[k - 1]));
+                        const double temp = 0.5 * (tH + tL);
+                        const double dQL = QC[c] + QR[c] - QC[c - 1] - QR[c - 1] + QV[c] - QV[c - 1] + QB[c] - QB[c - 1] +
+                                           S->qb[k] - S->qb[k - 1];
+                        const double qv = 0.5 * (QV[c] + QV[c - 1] + QB[c] + QB[c - 1] + S->qb[k] + S->qb[k - 1]);
+                        const double pdH = p0 * pow(PB[c], cpRd) + PI[c] * S->rhou[k];
+                        const double pdL = p0 * pow(PB[c - 1], cpRd) + PI[c - 1] * S->rhou[k - 1];
+                        const double eH = 611.2 * exp(17.67 * (tH - 273.15) / (tH - 29.65));
+                        const double eL = 611.2 * exp(17.67 * (tL - 273.15) / (tL - 29.65));
+                        const double qsH = 0.62197 * eH / (pdH - eH);
+                        const double qsL = 0.62197 * eL / (pdL - eL);
+                        hi = hi * (1 + Lv * qsH / (cp * tH));
+                        lo = lo * (1 + Lv * qsL / (cp * tL));
+                        const double A = (grav / S->tbw[k]) * (1.0 + Lv * qv / (Rd * temp)) /
+                                         (1.0 + 0.622 * Lv * Lv * qv / (cp * Rd * temp * temp));
+                        bruntv = (A * (hi - lo) - grav * dQL) * odzw;
+                    }
+                }
+                if (S2 - tb_one_d_Pr * bruntv > 0) {
+                    const double cc = S->l2[k] * tb_cs * tb_cs;
+                    S->kmix[c] = cc * sqrt(S2 - tb_one_d_Pr * bruntv);
+                    S->khmix[c - 1] = 0.5 * (S->kmix[c - 1] / S->l2[k - 1] + S->kmix[c] / S->l2[k]) * S->lH * S->lH;
+                    if (S->kmix[c] > S->kvmax[k]) S->kmix[c] = S->kvmax[k];
+                    if (S->khmix[c - 1] > S->kmixh_max) S->khmix[c - 1] = S->kmixh_max;
+                } else {
+                    S->kmix[c] = 0;
+                    S->khmix[c - 1] = 0 + 0.5 * S->kmix[c - 1] / S->l2[k - 1] * S->lH * S->lH;
+                }
+            }
+        }
+}
+/* the deformation-rate components of turbulent_diffusion_velocity
+ * (turbulence.cpp:918-932) at a point of the start-of-step fields; the
+ * vertical ones are zero at level 0 (the reference never writes them there) */
+static double tau11(const ora_state *S, int i, int j, int k)
+{
+    const double *U = S->M[F_U];
+    return 2.0 * (U[IX(i + 1, j, k)] - U[IX(i, j, k)]) * S->one_d_dx;
+}
+static double tau22(const ora_state *S, int i, int j, int k)
+{
+    const double *V = S->M[F_V];
+    return 2.0 * (V[IX(i, j + 1, k)] - V[IX(i, j, k)]) * S->one_d_dy;
+}
+static double tau33(const ora_state *S, int i, int j, int k)
+{
+    const double *W = S->M[F_W];
+    if (k == 0) return 0;
+    return 2.0 * (W[IX(i, j, k + 1)] - W[IX(i, j, k)]) * (S->one_d_dz * S->mu[k]);
+}
+static double tau13(const ora_state *S, int i, int j, int k)
+{
+    const double *U = S->M[F_U], *W = S->M[F_W];
+    if (k == 0) return 0;
+    return (W[IX(i + 1, j, k + 1)] - W[IX(i, j, k + 1)]) * S->one_d_dx +
+           (U[IX(i + 1, j, k + 1)] - U[IX(i + 1, j, k)]) * (S->one_d_dz * S->mw[k + 1]);
+}
+static double tau23(const ora_state *S, int i, int j, int k)
+{
+    const double *V = S->M[F_V], *W = S->M[F_W];
+    if (k == 0) return 0;
+    return (W[IX(i, j + 1, k + 1)] - W[IX(i, j, k + 1)]) * S->one_d_dy +
+           (V[IX(i, j + 1, k + 1)] - V[IX(i, j + 1, k)]) * (S->one_d_dz * S->mw[k + 1]);
+}
+static double tau12(const ora_state *S, int i, int j, int k)
+{
+    const double *U = S->M[F_U], *V = S->M[F_V];
+    return (U[IX(i + 1, j + 1, k)] - U[IX(i + 1, j, k)]) * S->one_d_dy +
+           (V[IX(i + 1, j + 1, k)] - V[IX(i, j + 1, k)]) * S->one_d_dx;
+}
+
+/* wind speed of the full and of the basic-state wind at the lowest level */
+static void surface_wind(const ora_state *S, long c, double *ws, double *wsb)
+{
+    const double u = S->M[F_U][c], v = S->M[F_V][c], ub = S->bar[0][c], vb = S->bar[1][c];
+    *ws = sqrt((u + ub) * (u + ub) + (v + vb) * (v + vb));
+    *wsb = sqrt(ub * ub + vb * vb);
+}
+
+/* turbulent_diffusion_velocity (turbulence.cpp:839-1022): the ocean drag
+ * (:899-905) at the lowest level, the stress divergences above */
+static void turb_velocity(ora_state *S)
+{
+    const int NX = S->NX, NY = S->NY, NZ = S->NZ;
+    const double *KM = S->kmix, *KH = S->khmix, *U = S->M[F_U], *V = S->M[F_V];
+    const double *UB = S->bar[0], *VB = S->bar[1];
+    double *fu = S->ttend[0], *fv = S->ttend[1], *fw = S->ttend[2];
+    const double odx = S->one_d_dx, ody = S->one_d_dy;
+#define KMX(a, b, c) KM[IX(a, b, c)]
+#define KHX(a, b, c) KH[IX(a, b, c)]
+    for (int i = 1; i < NX - 1; i++)
+        for (int j = 1; j < NY - 1; j++) {
+            double ws, wsb;
+            const long c1 = IX(i, j, 1);
+            surface_wind(S, c1, &ws, &wsb);
+            const double drag = (1.1e-3 + 4.0e-5 * ws);
+            double tau_u_zl = drag * (ws * U[c1] + (ws - wsb) * UB[c1]);
+            double tau_v_zl = drag * (ws * V[c1] + (ws - wsb) * VB[c1]);
+            for (int k = 1; k < NZ - 1; k++) {
+                const double odz = S->one_d_dz * S->mu[k], odzw = S->one_d_dz * S->mw[k];
+                const double uK11H_h = KHX(i, j, k);
+                const double uK11H_l = KHX(i - 1, j, k);
+                const double uK12H_h = 0.25 * (KHX(i, j, k) + KHX(i - 1, j, k) + KHX(i - 1, j + 1, k) + KHX(i, j + 1, k));
+                const double uK12H_l = 0.25 * (KHX(i, j - 1, k) + KHX(i - 1, j - 1, k) + KHX(i - 1, j, k) + KHX(i, j, k));
+                const double uK13V_h = 0.50 * (KMX(i, j, k + 1) + KMX(i - 1, j, k + 1));
+                const double vK12H_h = 0.25 * (KHX(i, j - 1, k) + KHX(i, j, k) + KHX(i + 1, j - 1, k) + KHX(i + 1, j, k));
+                const double vK12H_l = uK12H_l;
+                const double vK22H_h = KHX(i, j, k);
+                const double vK22H_l = KHX(i, j - 1, k);
+                const double vK23V_h = 0.5 * (KMX(i, j, k + 1) + KMX(i, j - 1, k + 1));
+                const double wK13H_h = 0.25 * (KHX(i, j, k) + KHX(i, j, k - 1) + KHX(i + 1, j, k) + KHX(i + 1, j, k - 1));
+                const double wK13H_l = 0.25 * (KHX(i, j, k) + KHX(i, j, k - 1) + KHX(i - 1, j, k) + KHX(i - 1, j, k - 1));
+                const double wK23H_h = 0.25 * (KHX(i, j, k) + KHX(i, j, k - 1) + KHX(i, j + 1, k) + KHX(i, j + 1, k - 1));
+                const double wK23H_l = 0.25 * (KHX(i, j, k) + KHX(i, j, k - 1) + KHX(i, j - 1, k) + KHX(i, j - 1, k - 1));
+                const double wK33V_h = 0.50 * (KMX(i, j, k) + KMX(i, j, k + 1));
+                const double wK33V_l = 0.50 * (KMX(i, j, k) + KMX(i, j, k - 1));
+                const double t13w = tau13(S, i - 1, j, k), t23s = tau23(S, i, j - 1, k);
+                const long c = IX(i, j, k);
+                fu[c] = (uK11H_h * tau11(S, i, j, k) - uK11H_l * tau11(S, i - 1, j, k)) * odx +
+                        (uK12H_h * tau12(S, i - 1, j, k) - uK12H_l * tau12(S, i - 1, j - 1, k)) * ody +
+                        (uK13V_h * t13w - tau_u_zl) * odz;
+                fv[c] = (vK12H_h * tau12(S, i, j - 1, k) - vK12H_l * tau12(S, i - 1, j - 1, k)) * odx +
+                        (vK22H_h * tau22(S, i, j, k) - vK22H_l * tau22(S, i, j - 1, k)) * ody +
+                        (vK23V_h * t23s - tau_v_zl) * odz;
+                fw[c] = (wK13H_h * tau13(S, i, j, k - 1) - wK13H_l * tau13(S, i - 1, j, k - 1)) * odx +
+                        (wK23H_h * tau23(S, i, j, k - 1) - wK23H_l * tau23(S, i, j - 1, k - 1)) * ody +
+                        (wK33V_h * tau33(S, i, j, k) - wK33V_l * tau33(S, i, j, k - 1)) * odzw;
+                tau_u_zl = uK13V_h * t13w;
+                tau_v_zl = vK23V_h * t23s;
+            }
+        }
+#undef KMX
+#undef KHX
+}
+
+/* the scalar flux divergence of turbulent_diffusion_scalars / _theta
+ * (turbulence.cpp:1116-1173): horizontal fluxes with the Prandtl-scaled
+ * coefficients averaged to the faces, the vertical flux carried upward from
+ * the surface value tau_l */
+static double scalar_divergence(const ora_state *S, const double *q, int i, int j, int k, double tau_l,
+                                double *tau_h)
+{
+    const double *KM = S->kmix, *KH = S->khmix, P = tb_one_d_Pr;
+    const long c = IX(i, j, k), sx = (long)S->NY * S->NZ, sy = S->NZ;
+    const double odx = S->one_d_dx, ody = S->one_d_dy;
+    const double th = -P * KM[c + 1] * (q[c + 1] - q[c]) * (S->one_d_dz * S->mw[k + 1]);
+    double KHh = 0.5 * (P * KH[c + sy] + P * KH[c]);
+    double KLl = 0.5 * (P * KH[c] + P * KH[c - sy]);
+    const double t22h = -KHh * (q[c + sy] - q[c]) * ody;
+    const double t22l = -KLl * (q[c] - q[c - sy]) * ody;
+    KHh = 0.5 * (P * KH[c + sx] + P * KH[c]);
+    KLl = 0.5 * (P * KH[c] + P * KH[c - sx]);
+    const double t11h = -KHh * (q[c + sx] - q[c]) * odx;
+    const double t11l = -KLl * (q[c] - q[c - sx]) * odx;
+    *tau_h = th;
+    return -((t11h - t11l) * odx + (t22h - t22l) * ody + (th - tau_l) * (S->one_d_dz * S->mu[k]));
+}
+
+/* turbulent_diffusion_scalars (moist, turbulence.cpp:1027-1183) and
+ * turbulent_diffusion_theta (dry, :1190-1276); the ocean surface fluxes of
+ * heat and vapour (:1083-1104) when SURFACE_HEAT_FLUX is set */
+static void turb_scalars(ora_state *S)
+{
+    const int NX = S->NX, NY = S->NY, NZ = S->NZ, moist = S->c.microphysics_option != 0;
+    const double cpRd = cp / Rd;
+    const double dp_to_surface = grav * S->zsu[1] / (cp * S->tbv[1]);
+    for (int i = 1; i < NX - 1; i++)
+        for (int j = 1; j < NY - 1; j++) {
+            double tl[4] = {0, 0, 0, 0}; /* theta, qv, qc, qr */
+            const long c1 = IX(i, j, 1);
+            if (moist && S->c.use_surface_heat_flux) {
+                double ws, wsb;
+                surface_wind(S, c1, &ws, &wsb);
+                const double drag = (1.1e-3 + 4.0e-5 * ws) * 1.0 * 1.0;
+                const double PB = S->bar[5][c1], PI = S->pi[c1];
+                const double pressure = p0 * pow(PB + dp_to_surface, cpRd) + PI * S->rhou[1];
+                const double pisfc = PB + PI / (cp * S->tbv[1]) + dp_to_surface;
+                const double qvs = 0.62197 * S->es_water / (pressure - S->es_water);
+                const double tsb = (S->bar[3][c1] + S->tb[1]) * pisfc;
+                const double tsp = S->M[F_TH][c1] * pisfc;
+                tl[1] = drag * ((ws - wsb) * (qvs - S->bar[4][c1] - S->qb[1]) - ws * S->M[F_QV][c1]);
+                tl[0] = drag * ((ws - wsb) * (S->water_temp - tsb) - ws * tsp);
+            }
+            const int nf = moist ? 4 : 1;
+            for (int k = 1; k < NZ - 1; k++) {
+                const long c = IX(i, j, k);
+                for (int n = 0; n < nf; n++) {
+                    double th;
+                    S->ttend[3 + n][c] = scalar_divergence(S, S->M[F_TH + n], i, j, k, tl[n], &th);
+                    tl[n] = th;
+                }
+            }
+        }
+}
+
+/* calculate_diff_tend (turbulence.cpp:158-188) over i, j in [1, N-1) */
+static void op_turbulence(ora_state *S)
+{
+    turb_kmix(S);
+    turb_velocity(S);
+    turb_scalars(S);
+}
+
+/* apply_velocity_diffusion (turbulence.cpp:233-256) over i, j in [3, N-3):
+ * u and v from level 1, w from level 2 */
+static void turb_apply_velocity(ora_state *S, double step)
+{
+    const double deltaT = step * S->dt;
+    for (int i = 3; i < S->NX - 3; i++)
+        for (int j = 3; j < S->NY - 3; j++) {
+            long c = IX(i, j, 1);
+            S->P[F_U][c] += S->ttend[0][c] * deltaT;
+            S->P[F_V][c] += S->ttend[1][c] * deltaT;
+            for (int k = 2; k < S->NZ - 1; k++) {
+                c = IX(i, j, k);
+                S->P[F_U][c] += S->ttend[0][c] * deltaT;
+                S->P[F_V][c] += S->ttend[1][c] * deltaT;
+                S->P[F_W][c] += S->ttend[2][c] * deltaT;
+            }
+        }
+}
+
+/* apply_scalar_diffusion (:263-273) and apply_moisture_diffusion (:278-291)
+ * over i, j in [1, N-1) */
+static void turb_apply_theta(ora_state *S, double step)
+{
+    for (int i = 1; i < S->NX - 1; i++)
+        for (int j = 1; j < S->NY - 1; j++)
+            for (int k = 1; k < S->NZ - 1; k++) {
+                const long c = IX(i, j, k);
+                S->P[F_TH][c] += S->ttend[3][c] * step * S->dt;
+            }
+}
+
+static void turb_apply_moisture(ora_state *S, double step)
+{
+    const double deltaT = step * S->dt;
+    for (int i = 1; i < S->NX - 1; i++)
+        for (int j = 1; j < S->NY - 1; j++)
+            for (int k = 1; k < S->NZ - 1; k++) {
+                const long c = IX(i, j, k);
+                S->P[F_QV][c] += S->ttend[4][c] * deltaT;
+                S->P[F_QC][c] += S->ttend[5][c] * deltaT;
+                S->P[F_QR][c] += S->ttend[6][c] * deltaT;
+            }
+}
+
+/* ------------------------------------------------------------------------
  * Kessler warm rain: run_kessler_microphysics (kessler.cpp:25-213).
  * ---------------------------------------------------------------------- */
 static void kessler_points(ora_state *S)
@@ -806,8 +1151,15 @@ static void kessler_points(ora_state *S)
                 double tm = temperature - 29.65;
                 double phi = pd / (pd - esl) * qvsat * f / (tm * tm);
                 double C = 0.0;
-                if (vapor > qvsat) C = (vapor - qvsat) / (1.0 + phi);
-                else if (vapor < qvsat && QCP[ix] > 0) C = -fmin(QCP[ix], (qvsat - vapor) / (1.0 + phi));
+                if (vapor > qvsat) {
+                    C = (vapor - qvsat) / (1.0 + phi);
+                    if (S->sat) S->sat[ix] = 1;
+                } else if (vapor < qvsat && QCP[ix] > 0) {
+                    C = -fmin(QCP[ix], (qvsat - vapor) / (1.0 + phi));
+                    if (S->sat) S->sat[ix] = -C < QCP[ix];
+                } else if (S->sat) {
+                    S->sat[ix] = vapor == qvsat;  /* kessler.cpp:141-163 */
+                }
                 QCP[ix] += C;
                 QVP[ix] -= C;
                 double dc = (Lv / (cp * pressure)) * C;
@@ -965,6 +1317,7 @@ static void micro_advance(ora_state *S)
 static void integrate_non_hydro(ora_state *S, double step) /* solver.cpp:87-138 */
 {
     op_advect_uvw(S, step);
+    if (S->c.turbulence_option) turb_apply_velocity(S, step); /* solver.cpp:103 */
     op_solve_pressure(S, step);
     op_project(S, step);
 }
@@ -973,12 +1326,16 @@ static void rk3_step(ora_state *S) /* driver_serial.cpp:178-286 */
 {
     static const double steps[3] = {1. / 3., 0.5, 1.0};
     const int micro = S->c.microphysics_option != 0;
+    const int turb = S->c.turbulence_option != 0;
     if (S->c.use_explicit_diffusion) op_explicit_diffusion(S, 1.0);
+    if (turb) op_turbulence(S);
     for (int s = 0; s < 3; s++) {
         integrate_non_hydro(S, steps[s]);
         op_advect_theta(S, steps[s]);
+        if (turb) turb_apply_theta(S, steps[s]);
         if (micro) {
             op_advect_micro(S, steps[s]);
+            if (turb) turb_apply_moisture(S, steps[s]);
             op_zero_moisture(S);
         }
         op_bc(S);
@@ -1175,6 +1532,7 @@ ora_state *ora_create(const ga_config *cfg, const ga_columns *cols)
     S->qa = (double *)calloc(NZ, sizeof(double));
     S->qd = (double *)calloc(NZ, sizeof(double));
     S->ve = (double *)calloc(NZ, sizeof(double));
+    if (cfg->turbulence_option) turb_init(S);
     return S;
 }
 
@@ -1196,6 +1554,9 @@ void ora_destroy(ora_state *S)
     free(S->ray_u); free(S->ray_w);
     free(S->qp_edges); free(S->qn_edges); free(S->mono);
     free(S->za); free(S->qa); free(S->qd); free(S->ve);
+    free(S->kmix); free(S->khmix);
+    for (int t = 0; t < 7; t++) free(S->ttend[t]);
+    free(S->sat); free(S->l2); free(S->kvmax);
     free(S);
 }
 
@@ -1214,6 +1575,10 @@ static double *field_ptr(ora_state *S, int field, int slot, long *n)
         return S->bar[field - GA_UBAR];
     case GA_VT: return S->vt;
     case GA_ACCRAIN: *n = (long)S->NX * S->NY; return S->accrain;
+    case GA_KMIX: return S->kmix;
+    case GA_KHMIX: return S->khmix;
+    case GA_UFRIC: case GA_VFRIC: case GA_WFRIC: case GA_THDIFF: case GA_QVDIFF: case GA_QCDIFF: case GA_QRDIFF:
+        return S->ttend[field - GA_UFRIC];
     }
     return NULL;
 }
@@ -1221,6 +1586,11 @@ static double *field_ptr(ora_state *S, int field, int slot, long *n)
 int ora_set_field(ora_state *S, int field, int slot, const double *src, long n)
 {
     long nn;
+    if (field == GA_SATURATED) {
+        if (!S->sat || n != S->N) return GA_ERR_ARG;
+        for (long x = 0; x < n; x++) S->sat[x] = src[x] != 0;
+        return GA_OK;
+    }
     double *d = field_ptr(S, field, slot, &nn);
     if (!d || n != nn) return GA_ERR_ARG;
     memcpy(d, src, sizeof(double) * n);
@@ -1230,6 +1600,11 @@ int ora_set_field(ora_state *S, int field, int slot, const double *src, long n)
 int ora_get_field(ora_state *S, int field, int slot, double *dst, long n)
 {
     long nn;
+    if (field == GA_SATURATED) {
+        if (!S->sat || n != S->N) return GA_ERR_ARG;
+        for (long x = 0; x < n; x++) dst[x] = S->sat[x];
+        return GA_OK;
+    }
     double *d = field_ptr(S, field, slot, &nn);
     if (!d || n != nn) return GA_ERR_ARG;
     memcpy(dst, d, sizeof(double) * n);
@@ -1254,6 +1629,10 @@ int ora_op(ora_state *S, int op, double step)
     case GA_OP_ADVANCE_INNER: advance_inner(S); if (S->c.microphysics_option) micro_advance_inner(S); return GA_OK;
     case GA_OP_ADVANCE_OUTER: advance_outer(S); if (S->c.microphysics_option) micro_advance(S); return GA_OK;
     case GA_OP_EXPLICIT_DIFFUSION: op_explicit_diffusion(S, step); return GA_OK;
+    case GA_OP_TURBULENCE:
+        if (!S->kmix) return GA_ERR_ARG;
+        op_turbulence(S);
+        return GA_OK;
     }
     return GA_ERR_ARG;
 }

@@ -27,6 +27,7 @@
 #include "fluxes.h"
 #include "initializer.h"
 #include "pressure.h"
+#include "turbulence.h"
 
 #include <cstdint>
 #include <map>
@@ -34,6 +35,8 @@
 #include <vector>
 
 void s_integrate_rk3();
+extern double *Kmix, *KHmix;  /* turbulence.cpp: mixing coefficients */
+extern bool *isSaturated;     /* turbulence.cpp: Kessler saturation record */
 void zero_moisture(int il, int ih, int jl, int jh, int size);
 void column_average_density();
 
@@ -139,6 +142,11 @@ int main(int argc, char **argv)
         inputs.kdiffh = scal(in, "kdiffh");
         inputs.kdiffv = scal(in, "kdiffv");
     }
+    if (has(in, "turbulence_option")) {  /* turbulence (optional records) */
+        inputs.turbulence_option = (int)scal(in, "turbulence_option");
+        inputs.use_surface_heat_flux = (int)scal(in, "use_surface_heat_flux");
+        inputs.water_temp = scal(in, "water_temp");
+    }
     initialize_globals();
 
     const size_t N = (size_t)NX * NY * NZ;
@@ -182,7 +190,16 @@ int main(int argc, char **argv)
         load(in, "vt", vts, N);
     }
     /* rest of initialize_serial (driver_serial.cpp:44-76) */
+    if (USE_TURBULENT_STRESS) {
+        init_kmix(NX, NY, NZ, &ZU(0));
+        if (has(in, "is_saturated")) {  /* a saturation record for operator tests */
+            std::vector<double> sat(N);
+            load(in, "is_saturated", sat.data(), N);
+            for (size_t x = 0; x < N; x++) isSaturated[x] = sat[x] != 0;
+        }
+    }
     if (USE_MICROPHYSICS) init_microphysics(NX, NY);
+    initialize_landsea("");
     initialize_pressure_solver();
     init_boundaries(iebuffer, iwbuffer, jnbuffer, jsbuffer, -1);
     init_damping(NX, NY, NZ);                       /* driver_serial.cpp:72-74 */
@@ -211,6 +228,7 @@ int main(int argc, char **argv)
         else if (name == "kessler") run_microphysics(1, NX - 1, 1, NY - 1);
         else if (name == "rayleigh") rayleigh_damping(1, NX - 1, 1, NY - 1, raydampheight);
         else if (name == "explicit_diffusion") apply_explicit_diffusion(step, 3, NX - 3, 3, NY - 3);
+        else if (name == "turbulence") calculate_diff_tend(1, NX - 1, 1, NY - 1);  /* driver_serial.cpp:194 */
         else { fprintf(stderr, "unknown op %s\n", name.c_str()); return 2; }
     } else {
         fprintf(stderr, "unknown mode\n");
@@ -236,6 +254,18 @@ int main(int argc, char **argv)
     out["one_d_rhou"] = grab(one_d_rhou, NZ); out["one_d_rhow"] = grab(one_d_rhow, NZ);
     out["tb"] = grab(tb, NZ); out["tbv"] = grab(tbv, NZ); out["tbw"] = grab(tbw, NZ);
     out["qb"] = grab(qb, NZ); out["pib"] = grab(pib, NZ); out["f"] = grab(f, NY);
+    if (USE_TURBULENT_STRESS) {  /* the turbulence tendencies of the last calculate_diff_tend */
+        out["kmix"] = grab(Kmix, N); out["khmix"] = grab(KHmix, N);
+        out["u_friction"] = grab(u_friction, N); out["v_friction"] = grab(v_friction, N);
+        out["w_friction"] = grab(w_friction, N); out["t_diffusion"] = grab(t_diffusion, N);
+        if (USE_MICROPHYSICS) {
+            out["qv_diffusion"] = grab(qv_diffusion, N); out["qc_diffusion"] = grab(qc_diffusion, N);
+            out["qr_diffusion"] = grab(qr_diffusion, N);
+            std::vector<double> sat(N);
+            for (size_t x = 0; x < N; x++) sat[x] = isSaturated[x] ? 1.0 : 0.0;
+            out["is_saturated"] = sat;
+        }
+    }
     out["bigcounter"] = std::vector<double>(1, (double)bigcounter);
     out["mtime"] = std::vector<double>(1, mtime);
     write_bundle(argv[2], out);

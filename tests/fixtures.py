@@ -23,10 +23,11 @@ def load(name: str) -> dict:
 def workload(d: dict) -> configs.Workload:
     kw = {k: int(d[k]) for k in _INT_KEYS}
     kw.update({k: float(d[k]) for k in _FLOAT_KEYS})
-    for k in ("use_explicit_diffusion", "diffusion_order"):  # optional: fixtures with diffusion
+    for k in ("use_explicit_diffusion", "diffusion_order", "turbulence_option",
+              "use_surface_heat_flux"):  # optional: fixtures with diffusion or turbulence
         if k in d:
             kw[k] = int(d[k])
-    for k in ("kdiffh", "kdiffv"):
+    for k in ("kdiffh", "kdiffv", "water_temp"):
         if k in d:
             kw[k] = float(d[k])
     wl = configs.Workload(name="golden", nsteps=int(d["nsteps"]), **kw)
@@ -52,11 +53,16 @@ def ops_names():
     return sorted(f[:-4] for f in os.listdir(GOLDEN) if f.startswith("ops_") and f.endswith(".npz"))
 
 
+def turb_names():
+    return sorted(f[:-4] for f in os.listdir(GOLDEN) if f.startswith("turb_") and f.endswith(".npz"))
+
+
 def slot_extra(d: dict) -> dict:
     """Per-slot input arrays of an ops fixture (u_p, u_m, ..., pi, vt)."""
     out = {}
     for k in d:
-        if k.startswith("in_") and (k.endswith("_p") or k.endswith("_m") or k in ("in_pi", "in_vt")):
+        if k.startswith("in_") and (k.endswith("_p") or k.endswith("_m") or k in ("in_pi", "in_vt",
+                                                                                    "in_is_saturated")):
             out[k[3:]] = d[k]
     return out
 
@@ -68,6 +74,8 @@ for _f, _n in enumerate(abi.PROG_NAMES):
 FIELD_OF["pi"] = (abi.GA_PI, 0)
 FIELD_OF["vt"] = (abi.GA_VT, 0)
 FIELD_OF["accrain"] = (abi.GA_ACCRAIN, 0)
+for _n, _f in abi.TURB_NAMES.items():
+    FIELD_OF[_n] = (_f, 0)
 
 
 def rel_l2(a, b) -> float:

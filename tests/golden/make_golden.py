@@ -7,6 +7,8 @@ inputs and outputs as compressed .npz files:
   run_<case>.npz   full steps (s_integrate_rk3, driver_serial.cpp:178-286)
   ops_<case>.npz   single operators applied to one state whose three rotation
                    buffers all hold different data
+  turb_<case>.npz  the turbulence tendencies (calculate_diff_tend) of such a
+                   state, and Kessler's saturation record
 
 Usage (where the reference sources exist):  python tests/golden/make_golden.py
 The fixtures are then read by tests/test_golden_oracle.py (CPU) and
@@ -32,6 +34,16 @@ def _diffusing(wl, order, kdiffh):
     return wl
 
 
+def _turbulent(wl, surface_flux=0, water_temp=28.0):
+    wl.turbulence_option, wl.use_surface_heat_flux, wl.water_temp = 1, surface_flux, water_temp
+    return wl
+
+
+def _jet(moist):
+    return configs.jet_vortex(nx=16, ny=14, nz=10, dx=20000.0, dz=800.0, dt=30.0, rmax=60000.0, vmax=8.0,
+                              moist=moist, noise=0.3, extra_basic=1.0)
+
+
 RUN_CASES = {
     "dry": (lambda: configs.dry_bubble(nx=16, ny=14, nz=10, dx=500.0, dz=400.0, amp=3.0,
                                        radius=2000.0, zc=1500.0, noise=0.2), 4),
@@ -46,6 +58,13 @@ RUN_CASES = {
     "diffusion6_moist": (lambda: _diffusing(configs.moist_blob(nx=16, ny=15, nz=12), 6, 0.002), 3),
     "jet": (lambda: configs.jet_vortex(nx=16, ny=14, nz=10, dx=20000.0, dz=800.0, dt=30.0, rmax=60000.0,
                                            vmax=8.0, moist=True, noise=0.3, extra_basic=1.0), 3),
+    # turbulence (calculate_diff_tend once per step, applied in every RK stage)
+    "turbulence_dry": (lambda: _turbulent(configs.dry_bubble(nx=16, ny=14, nz=10, dx=500.0, dz=400.0, amp=3.0,
+                                                             radius=2000.0, zc=1500.0, noise=0.2)), 4),
+    "turbulence_jet_dry": (lambda: _turbulent(_jet(False)), 3),
+    "turbulence_moist": (lambda: _turbulent(configs.moist_blob(nx=15, ny=14, nz=10)), 4),
+    "turbulence_moist_sfc": (lambda: _turbulent(configs.moist_blob(nx=18, ny=14, nz=10, periodic=1), 1, 30.0), 4),
+    "turbulence_jet_sfc": (lambda: _turbulent(_jet(True), 1, 26.0), 3),
 }
 
 OP_NAMES = ["advect_uvw", "solve_pressure", "integrate_non_hydro", "advect_theta",
@@ -126,6 +145,49 @@ def make_ops():
         print("wrote", path, os.path.getsize(path))
 
 
+TURB_OPS = ["turbulence", "kessler"]
+
+
+def make_turb():
+    """turb_<case>.npz: calculate_diff_tend on a state whose rotation slots
+    differ, with a seeded saturation record (both Brunt-Vaisala branches of
+    get_Kmix), and Kessler's saturation record of the same state"""
+    cases = {
+        "moist": _turbulent(configs.moist_blob(nx=14, ny=13, nz=10)),
+        "moist_sfc": _turbulent(configs.moist_blob(nx=15, ny=13, nz=10), 1, 29.0),
+        "jet_dry": _turbulent(_jet(False)),
+        "jet_sfc": _turbulent(_jet(True), 1, 27.0),
+    }
+    for cname, wl in cases.items():
+        extra = _ops_state(wl, 7000)
+        if wl.microphysics_option:
+            extra["is_saturated"] = (configs.splitmix_uniform(7100, wl.points) < 0.5).astype(np.float64).reshape(
+                wl.nx, wl.ny, wl.nz)
+        else:
+            for q in ("qv", "qc", "qr"):
+                extra.pop(q + "_p"), extra.pop(q + "_m")
+        d = _inputs(wl)
+        for k, v in extra.items():
+            d["in_" + k] = v.ravel()
+        ops = TURB_OPS if wl.microphysics_option else TURB_OPS[:1]
+        for op in ops:
+            out = O.run_reference(wl, "op", op=op, step=1.0, extra=extra)
+            d[f"step_{op}"] = np.float64(1.0)
+            for k, v in out.items():
+                if k in abi.COLUMN_NAMES or k in ("f", "bigcounter", "mtime"):
+                    continue
+                if (op == "turbulence") != (k in abi.TURB_NAMES) or k == "is_saturated" and op == "turbulence":
+                    if not (op == "kessler" and k == "is_saturated"):
+                        continue
+                ref_in = extra.get(k, wl.fields.get(k))
+                if op != "turbulence" and ref_in is not None and np.array_equal(np.asarray(ref_in).ravel(), v):
+                    continue  # unchanged by this operator
+                d[f"{op}__{k}"] = v
+        path = os.path.join(HERE, f"turb_{cname}.npz")
+        np.savez_compressed(path, **d)
+        print("wrote", path, os.path.getsize(path))
+
+
 if __name__ == "__main__":
     if not O.reference_available():
         subprocess_rc = os.system(os.path.join(ROOT, "oracle", "build_ref.sh"))
@@ -133,3 +195,4 @@ if __name__ == "__main__":
             sys.exit("reference build failed")
     make_runs()
     make_ops()
+    make_turb()

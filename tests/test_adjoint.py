@@ -345,6 +345,17 @@ def test_gpu_adjoint_rejects_explicit_diffusion(built):
 
 
 @pytest.mark.gpu
+def test_gpu_adjoint_rejects_turbulence(built):
+    from model_gb300 import anelastic
+    wl = configs.moist_blob(nx=20, ny=18, nz=12)
+    wl.turbulence_option = 1
+    m = anelastic.Model(wl, abi.GA_PREC_F64)
+    with pytest.raises(anelastic.GaError):
+        m.adjoint(1, 1)
+    assert "turbulence" in anelastic.last_error()
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("kw", [dict(rain_fallout=2), dict(periodic=1)])
 def test_gpu_adjoint_rejects_unsupported(built, kw):
     """Semi-Lagrangian rain fallout and periodic boundaries are not linearised."""

@@ -36,6 +36,11 @@ def test_full_steps_bit_exact(name):
         np.testing.assert_array_equal(v, d["out_" + k], err_msg=f"{name}:{k}")
         checked += 1
     assert checked >= 13
+    if wl.turbulence_option:  # the tendencies of the last step's calculate_diff_tend
+        turb = [k for k in abi.TURB_NAMES if "out_" + k in d]
+        assert len(turb) >= 6
+        for k in turb:
+            np.testing.assert_array_equal(o.get(abi.TURB_NAMES[k]), d["out_" + k], err_msg=f"{name}:{k}")
 
 
 @pytest.mark.parametrize("name", fx.ops_names())
@@ -52,6 +57,29 @@ def test_single_operator_bit_exact(name, op):
     assert o.op(op, float(d[f"step_{op}"])) == 0
     outs = [k for k in d if k.startswith(op + "__")]
     assert outs, "fixture has no output for this operator"
+    for k in outs:
+        key = k.split("__", 1)[1]
+        f, slot = fx.FIELD_OF[key]
+        np.testing.assert_array_equal(o.get(f, slot), d[k], err_msg=f"{op}:{key}")
+
+
+@pytest.mark.parametrize("name", fx.turb_names())
+@pytest.mark.parametrize("op", ["turbulence", "kessler"])
+def test_turbulence_operator_bit_exact(name, op):
+    """calculate_diff_tend (mixing coefficients, stress and flux tendencies)
+    of a state with differing rotation slots and a seeded saturation record,
+    and the saturation record Kessler leaves"""
+    d = fx.load(name)
+    wl = fx.workload(d)
+    if op == "kessler" and not wl.microphysics_option:
+        pytest.skip("dry case")
+    o = O.Oracle(wl)
+    for k, v in fx.slot_extra(d).items():
+        f, slot = fx.FIELD_OF[k]
+        o.set(f, slot, v)
+    assert o.op(op, float(d[f"step_{op}"])) == 0
+    outs = [k for k in d if k.startswith(op + "__")]
+    assert len(outs) >= (6 if op == "turbulence" else 5)
     for k in outs:
         key = k.split("__", 1)[1]
         f, slot = fx.FIELD_OF[key]

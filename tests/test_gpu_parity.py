@@ -17,6 +17,7 @@ from tests import fixtures as fx
 pytestmark = pytest.mark.gpu
 
 EXACT_OPS = {"advect_uvw", "advect_theta", "zero_moisture", "bc", "bc_micro", "rayleigh", "explicit_diffusion"}
+# the turbulence scheme: operator fixtures turb_*.npz (test_turbulence_operator_matches_reference)
 
 
 @pytest.fixture(scope="module", autouse=True)
@@ -41,6 +42,16 @@ def test_full_steps_match_reference(name):
         assert e <= 1e-10, f"{name}:{k} rel L2 {e:.3e}"
     print(f"{name}: worst rel L2 {worst:.3e}")
     assert m.counters()[0] == wl.nsteps
+    if wl.turbulence_option:  # the last step's coefficients, tendencies and saturation record
+        for k, f in abi.TURB_NAMES.items():
+            if "out_" + k not in d:
+                continue
+            got = m.get(f)
+            if k == "is_saturated":
+                np.testing.assert_array_equal(got, d["out_" + k], err_msg=f"{name}:{k}")
+            else:
+                e = fx.rel_l2(got, d["out_" + k])
+                assert e <= 1e-10, f"{name}:{k} rel L2 {e:.3e}"
 
 
 @pytest.mark.parametrize("name", fx.ops_names())
@@ -64,6 +75,37 @@ def test_single_operator_matches_reference(name, op):
         f, slot = fx.FIELD_OF[key]
         got = m.get(f, slot)
         if op in EXACT_OPS:
+            np.testing.assert_array_equal(got, d[k], err_msg=f"{op}:{key}")
+        else:
+            e = fx.rel_l2(got, d[k])
+            assert e <= 1e-12, f"{op}:{key} rel L2 {e:.3e}"
+
+
+@pytest.mark.parametrize("name", fx.turb_names())
+@pytest.mark.parametrize("op", ["turbulence", "kessler"])
+def test_turbulence_operator_matches_reference(name, op):
+    """calculate_diff_tend on a state whose rotation slots differ, with a
+    seeded saturation record: bit exact for the dry scheme (no pow or exp),
+    1e-12 relative L2 where the saturated Brunt-Vaisala frequency or the
+    surface fluxes call pow and exp; Kessler's saturation record bit exact"""
+    d = fx.load(name)
+    wl = fx.workload(d)
+    if op == "kessler" and not wl.microphysics_option:
+        pytest.skip("dry case")
+    m = anelastic.Model(wl, abi.GA_PREC_F64)
+    for k, v in fx.slot_extra(d).items():
+        f, slot = fx.FIELD_OF[k]
+        if f < abi.GA_NPROG and f >= (7 if wl.microphysics_option else 4):
+            continue
+        m.set(f, slot, v)
+    m.op(op, float(d[f"step_{op}"]))
+    outs = [k for k in d if k.startswith(op + "__")]
+    assert len(outs) >= (6 if op == "turbulence" else 5)
+    for k in outs:
+        key = k.split("__", 1)[1]
+        f, slot = fx.FIELD_OF[key]
+        got = m.get(f, slot)
+        if not wl.microphysics_option or key == "is_saturated":
             np.testing.assert_array_equal(got, d[k], err_msg=f"{op}:{key}")
         else:
             e = fx.rel_l2(got, d[k])
@@ -135,6 +177,33 @@ def test_explicit_diffusion_thunderstorm_vs_oracle(order):
     for f in range(7):
         e = fx.rel_l2(a.get(f), b.get(f))
         assert e <= 1e-4, (abi.PROG_NAMES[f], e)
+
+
+@pytest.mark.parametrize("sfc", [0, 1])
+def test_turbulence_thunderstorm_vs_oracle(sfc):
+    """full-size thunderstorm with the turbulence scheme (and the ocean
+    surface fluxes): FP64 against the oracle after 6 steps, FP32 against
+    FP64"""
+    from model_gb300 import configs
+    wl = configs.thunderstorm()
+    wl.turbulence_option, wl.use_surface_heat_flux, wl.water_temp = 1, sfc, 29.0
+    _oracle_compare(wl, 6, 1e-10)
+    a = anelastic.Model(wl, abi.GA_PREC_F32)
+    b = anelastic.Model(wl, abi.GA_PREC_F64)
+    a.step(6)
+    b.step(6)
+    for f in range(7):
+        e = fx.rel_l2(a.get(f), b.get(f))
+        assert e <= 1e-4, (abi.PROG_NAMES[f], e)
+    assert fx.rel_l2(b.get(abi.GA_KMIX), a.get(abi.GA_KMIX)) <= 1e-3
+
+
+def test_turbulence_dry_jet_vs_oracle():
+    from model_gb300 import configs
+    wl = configs.jet_vortex(nx=64, ny=48, nz=24, dx=20000.0, dz=800.0, dt=30.0, rmax=200000.0, vmax=12.0,
+                            noise=0.3, extra_basic=1.0)
+    wl.turbulence_option = 1
+    _oracle_compare(wl, 10, 1e-10)
 
 
 def test_step_is_deterministic():
