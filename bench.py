@@ -406,6 +406,81 @@ def adjoint_bench(torch, device, steps, every, moist=False, size=512):
     return out
 
 
+# field passes per step of the optional physics (moist, FP32 fields): the
+# turbulence coefficients (14 fields in, 2 out), the tendencies (9 in, 7 out)
+# and three stage additions (14 in, 7 out each); explicit diffusion's
+# tendencies (7 in, 7 out) and their addition (14 in, 7 out)
+PHYSICS_PASSES = {"turbulence": 16 + 16 + 3 * 21, "diffusion": 14 + 21}
+
+
+def physics_bench(torch, device, steps, accuracy_steps):
+    """The C2 thunderstorm with the optional physics of the step switched on:
+    explicit diffusion (4th order), the turbulence scheme with ocean surface
+    fluxes, and both; FP32 tuned, per-group event times, the groups' HBM
+    fraction by their algorithmic passes, FP64 beside the combined case and
+    its FP32 error after accuracy_steps steps."""
+    from model_gb300 import abi, anelastic, configs
+    peak, peak_kind = load_peaks()
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{device}")
+    variants = {"none": {}, "explicit_diffusion": {"use_explicit_diffusion": 1, "diffusion_order": 4},
+                "turbulence": {"turbulence_option": 1, "use_surface_heat_flux": 1},
+                "both": {"use_explicit_diffusion": 1, "diffusion_order": 4, "turbulence_option": 1,
+                         "use_surface_heat_flux": 1}}
+    out = {"workload": "Kessler thunderstorm 128x128x48 with the optional physics", "steps": steps,
+           "kdiffh": 0.005, "kdiffv": 0.005, "water_temp_c": 28.0}
+    for name, kw in variants.items():
+        wl = configs.thunderstorm()
+        for k, v in kw.items():
+            setattr(wl, k, v)
+        m = anelastic.Model(wl, abi.GA_PREC_F32, device=device)
+        m.tune()
+        for _ in range(3):
+            m.step(1)
+        per = time_steps(m, torch, steps, flush)
+        ms = sum(per) / steps
+        groups = profile_groups(m, torch, min(steps, 10), flush)
+        nprof = min(steps, 10)
+        r = {"ms_per_step": round(ms, 4), "value": round(wl.points / (ms * 1e-3), 1), "unit": UNIT}
+        for g, passes in PHYSICS_PASSES.items():
+            if g in groups:
+                gms = groups[g]["ms"] / nprof
+                gbs = passes * wl.points * 4 / (gms * 1e-3) / 1e9
+                r[g] = {"ms_per_step": round(gms, 4), "launches_per_step": groups[g]["launches"] / nprof,
+                        "algorithmic_passes": passes, "achieved_gbs": round(gbs, 1),
+                        "hbm_frac": round(gbs / peak, 4)}
+        m.close()
+        out[name] = r
+    base = out["none"]["ms_per_step"]
+    for name in variants:
+        out[name]["over_none"] = round(out[name]["ms_per_step"] / base, 3)
+    wl = configs.thunderstorm()
+    for k, v in variants["both"].items():
+        setattr(wl, k, v)
+    m64 = anelastic.Model(wl, abi.GA_PREC_F64, device=device)
+    for _ in range(2):
+        m64.step(1)
+    per64 = time_steps(m64, torch, max(2, steps // 2), flush)
+    out["both"]["fp64_ms_per_step"] = round(sum(per64) / len(per64), 4)
+    out["both"]["fp32_over_fp64"] = round(out["both"]["fp64_ms_per_step"] / out["both"]["ms_per_step"], 2)
+    m64.close()
+    if accuracy_steps > 0:
+        a = anelastic.Model(wl, abi.GA_PREC_F32, device=device)
+        b = anelastic.Model(wl, abi.GA_PREC_F64, device=device)
+        a.step(accuracy_steps)
+        b.step(accuracy_steps)
+        errs = {}
+        for f in range(7):
+            x, y = a.get(f), b.get(f)
+            errs[abi.PROG_NAMES[f]] = float(np.linalg.norm(x - y) / max(np.linalg.norm(y), 1e-300))
+        out["both"]["accuracy"] = {"steps": accuracy_steps, "rel_l2_fp32_vs_fp64": {k: float(f"{v:.4g}") for k, v
+                                                                                   in errs.items()},
+                                   "max": float(f"{max(errs.values()):.4g}")}
+        a.close()
+        b.close()
+    out["hbm_peak"] = {"gbs": peak, "source": peak_kind}
+    return out
+
+
 def cpu_baseline(wl, steps):
     """The reference's CPU step (oracle restatement, 1 core) on a bounded
     sample of the same workload."""
@@ -557,6 +632,8 @@ def run_ours(args):
     if args.adjoint_moist_steps > 0:
         line["adjoint_moist"] = adjoint_bench(torch, device, args.adjoint_moist_steps, args.adjoint_moist_every,
                                               moist=True, size=args.adjoint_moist_size)
+    if args.physics_steps > 0:
+        line["physics"] = physics_bench(torch, device, args.physics_steps, args.physics_accuracy_steps)
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(wl, args.cpu_steps)
     print(json.dumps(line), flush=True)
@@ -608,6 +685,9 @@ def main():
     ap.add_argument("--adjoint-moist-steps", type=int, default=400)
     ap.add_argument("--adjoint-moist-every", type=int, default=40)
     ap.add_argument("--adjoint-moist-size", type=int, default=512, help="NX = NY of the moist adjoint case")
+    ap.add_argument("--physics-steps", type=int, default=20,
+                    help="timed steps of each optional-physics variant (0: skip)")
+    ap.add_argument("--physics-accuracy-steps", type=int, default=600)
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()

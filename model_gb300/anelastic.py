@@ -238,6 +238,12 @@ class Model:
     def rayleigh_damping(self):  # damping.cpp:1148
         self.op("rayleigh")
 
+    def apply_explicit_diffusion(self, step=1.0):  # damping.cpp:1125
+        self.op("explicit_diffusion", step)
+
+    def calculate_diff_tend(self):  # turbulence.cpp:158
+        self.op("turbulence")
+
     def counters(self):
         bc, mt = C.c_longlong(), C.c_double()
         self._check(self.L.ga_get_counters(self.h, C.byref(bc), C.byref(mt)), "ga_get_counters")

@@ -8,7 +8,8 @@
 // = 0, as initialize_from_output_serial leaves them), and advances the run
 // in chunks of `every` steps, writing after each chunk an exact restart file
 // of the whole state: all three rotation slots of every prognostic field, pi,
-// the fall speed, the accumulated rain and the counters, in FP64.  A run
+// the fall speed, the accumulated rain, Kessler's saturation record (with
+// the turbulence scheme) and the counters, in FP64.  A run
 // started from such a file continues bit for bit as if it had not stopped
 // (with rain_fallout 1; under rain_fallout 2 the edge value that the PPM
 // fallout carries from one rainy column to the next, microphysics.cpp:
@@ -25,7 +26,9 @@
 //                  [--precision f64|f32] [--device D]
 //   INPUT     settings (nx ny nz dx dy dz dt microphysics_option rain_fallout
 //             periodic_ew_boundaries boundary_width_{north,south,east,west}
-//             rayleigh_damping_z height_lowest_level corner_lat), the base
+//             rayleigh_damping_z height_lowest_level corner_lat; optional:
+//             use_explicit_diffusion diffusion_order kdiffh kdiffv
+//             turbulence_option use_surface_heat_flux water_temp), the base
 //             columns tb_in and qb_in, the basic state (ubar vbar wbar thbar
 //             qbar pbar) and the initial perturbation (u v w th [qv qc qr]
 //             [accrain])
@@ -104,6 +107,13 @@ struct Run {
         *v = it->second[0];
         return true;
     }
+    bool optional(const char *k, double *v) const
+    {
+        auto it = in.find(k);
+        if (it == in.end() || it->second.empty()) return false;
+        *v = it->second[0];
+        return true;
+    }
     const std::vector<double> *array(const Bundle &b, const std::string &k, size_t n) const
     {
         auto it = b.find(k);
@@ -133,6 +143,20 @@ struct Run {
         cfg.rayleigh_damping_z = (int)v[14];
         hll = v[15];
         corner_lat = v[16];
+        // optional physics switches (input_params: use_explicit_diffusion,
+        // diffusion_order, kdiffh, kdiffv, turbulence_option,
+        // use_surface_heat_flux, water_temp); absent means off
+        double o;
+        cfg.diffusion_order = 4;
+        cfg.kdiffh = cfg.kdiffv = 0.005;
+        cfg.water_temp = 28.0;
+        if (optional("use_explicit_diffusion", &o)) cfg.use_explicit_diffusion = (int)o;
+        if (optional("diffusion_order", &o)) cfg.diffusion_order = (int)o;
+        if (optional("kdiffh", &o)) cfg.kdiffh = o;
+        if (optional("kdiffv", &o)) cfg.kdiffv = o;
+        if (optional("turbulence_option", &o)) cfg.turbulence_option = (int)o;
+        if (optional("use_surface_heat_flux", &o)) cfg.use_surface_heat_flux = (int)o;
+        if (optional("water_temp", &o)) cfg.water_temp = o;
         cfg.precision = precision;
         cfg.device = device;
         n3 = (size_t)cfg.nx * cfg.ny * cfg.nz;
@@ -174,6 +198,11 @@ int save(ga_ctx *ctx, const Run &run, const std::string &path)
         rc = ga_get_field(ctx, GA_ACCRAIN, 0, acc.data(), run.n2);
         if (rc) return fail(rc, "ga_get_field(accrain)");
         out["accrain"] = acc;
+        if (run.cfg.turbulence_option) {  // Kessler's saturation record feeds the next step's mixing
+            rc = ga_get_field(ctx, GA_SATURATED, 0, buf.data(), run.n3);
+            if (rc) return fail(rc, "ga_get_field(is_saturated)");
+            out["is_saturated"] = buf;
+        }
     }
     long long bc = 0;
     double mt = 0;
@@ -279,6 +308,11 @@ int main(int argc, char **argv)
             if (!vt || !acc) { ga_destroy(ctx); return 2; }
             ga_set_field(ctx, GA_VT, 0, vt->data(), run.n3);
             ga_set_field(ctx, GA_ACCRAIN, 0, acc->data(), run.n2);
+            if (run.cfg.turbulence_option) {
+                const std::vector<double> *sat = run.array(st, "is_saturated", run.n3);
+                if (!sat) { ga_destroy(ctx); return 2; }
+                ga_set_field(ctx, GA_SATURATED, 0, sat->data(), run.n3);
+            }
         }
         const std::vector<double> *bc = run.array(st, "bigcounter", 1), *mt = run.array(st, "mtime", 1);
         if (!bc || !mt) { ga_destroy(ctx); return 2; }

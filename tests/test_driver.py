@@ -2,9 +2,12 @@
 
   - a moist run of 6 steps written every 3 steps, against the CPU oracle
     (1e-10 relative L2, the bound of the FP64 path);
+  - the optional physics settings (explicit diffusion, turbulence with
+    surface fluxes) against the oracle;
   - restart: 3 steps, then 3 more from the written state file, against the
     6-step run: every record of the state file (all rotation slots, pi, fall
-    speed, rain, counters) bit for bit, in FP64 and in FP32;
+    speed, rain, the saturation record, counters) bit for bit, in FP64 and
+    in FP32, with and without the turbulence scheme;
   - a missing input field is an error, reported before any context exists
     (runs without a GPU).
 """
@@ -57,10 +60,33 @@ def test_driver_run_matches_oracle(driver, tmp_path):
 
 
 @pytest.mark.gpu
+def test_driver_physics_switches_match_oracle(driver, tmp_path):
+    """explicit diffusion and the turbulence scheme with surface fluxes,
+    switched on through the input's optional settings"""
+    from oracle import oracle as O
+    from oracle.ga_bundle import read_bundle, write_bundle
+    wl = configs.moist_blob(nx=24, ny=22, nz=16, nsteps=4)
+    wl.use_explicit_diffusion, wl.diffusion_order, wl.kdiffh = 1, 6, 0.003
+    wl.turbulence_option, wl.use_surface_heat_flux, wl.water_temp = 1, 1, 27.0
+    inp = str(tmp_path / "in.bin")
+    write_bundle(inp, _bundle(wl))
+    _run(driver, inp, str(tmp_path / "run"), "--steps", "4")
+    st = read_bundle(str(tmp_path / "run_4.bin"))
+    o = O.Oracle(wl)
+    assert o.step(4) == 0
+    for f, name in enumerate(abi.PROG_NAMES):
+        e = fx.rel_l2(st[name], o.get(f))
+        assert e <= 1e-10, f"{name}: rel L2 {e:.3e}"
+    np.testing.assert_array_equal(st["is_saturated"], o.get(abi.GA_SATURATED))
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("precision", ["f64", "f32"])
-def test_driver_restart_is_exact(driver, tmp_path, precision):
+@pytest.mark.parametrize("turbulence", [0, 1])
+def test_driver_restart_is_exact(driver, tmp_path, precision, turbulence):
     from oracle.ga_bundle import read_bundle, write_bundle
     wl = configs.moist_blob(nx=24, ny=22, nz=16, nsteps=6)
+    wl.turbulence_option = turbulence
     inp = str(tmp_path / "in.bin")
     write_bundle(inp, _bundle(wl))
     _run(driver, inp, str(tmp_path / "full"), "--steps", "6", "--every", "3", "--precision", precision)
