@@ -104,7 +104,7 @@ extern "C" {
 #define GA_OP_PROJECT           3  /* gradient loop of integrate_non_hydro  solver.cpp:120-135 */
 #define GA_OP_INTEGRATE_NON_HYDRO 4 /* integrate_non_hydro      solver.cpp:87    */
 #define GA_OP_ADVECT_THETA      5  /* advect_theta              advection.cpp:349 */
-#define GA_OP_ADVECT_MICRO      6  /* advect_microphysics_cell  advection.cpp:451 */
+#define GA_OP_ADVECT_MICRO      6  /* advect_microphysics_cell  advection.cpp:451 (linear_model: advect_qv :577) */
 #define GA_OP_ZERO_MOISTURE     7  /* zero_moisture             microphysics.cpp:675 */
 #define GA_OP_BC                8  /* apply_boundary_condition  boundaries.cpp:119 */
 #define GA_OP_BC_MICRO          9  /* apply_boundary_condition_microphysics boundaries.cpp:200 */
@@ -153,6 +153,12 @@ typedef struct ga_config {
     int    use_surface_heat_flux;   /* SURFACE_HEAT_FLUX: surface heat and vapour    */
                                     /* fluxes of a moist run                         */
     double water_temp;              /* WATER_TEMP_C: sea-surface temperature (C)     */
+    /* the linearised model about the basic state (ISLINEAR: linear_integrate_rk3,
+     * driver_serial.cpp:83-171): perturbation faces advected by the basic-state
+     * velocity alone (fluxes.cpp:328-337, 594-650, 1204-1357), vapour advected
+     * without microphysics, explicit diffusion in every stage, the
+     * perturbation rescaled every 12 hours of model time */
+    int    linear_model;            /* 0 or 1                                        */
 } ga_config;
 
 /*

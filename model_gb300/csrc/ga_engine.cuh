@@ -122,6 +122,7 @@ class Engine : public EngineBase {
     // is null when the scheme is off.  turb_sat is Kessler's saturation record.
     TurbArgs<T> turb{};
     unsigned char *turb_sat = nullptr;
+    double *lin_vmax = nullptr;  // the linearised model's rescaling maximum
 
     // Fornberg's recurrence for finite-difference weights: c[i*(m+1)+d] is the
     // weight of point x[i] in derivative d at z (util.cpp:199-247)
@@ -319,6 +320,11 @@ class Engine : public EngineBase {
             for (int k = 0; k < NZ; k++) wk[k] = cols->rhou[k] * dx * c->dy * c->dz / cols->mu[k];
             budget_w = upload(wk);
             budget_part = dalloc<double>((size_t)BUDGET_BLOCKS * GA_NB + GA_NB);
+        }
+        if (c->linear_model) {  // linear_integrate_rk3: eager steps (a rescaling may fall on any step)
+            kp.linear = 1;
+            use_graphs = false;
+            lin_vmax = dalloc<double>(1);
         }
         if (c->turbulence_option) {  // init_kmix (turbulence.cpp:85-151)
             turb.kmix = dalloc<T>(N);
@@ -663,7 +669,7 @@ class Engine : public EngineBase {
             launches++;
         }
         kp.btab = btab;
-        kp.ubase_adv = adv;
+        kp.ubase_adv = adv && !cfg.linear_model;  // the tables hold the full-velocity faces only
         kp.ubase_kes = kes;
     }
 
@@ -1013,6 +1019,12 @@ class Engine : public EngineBase {
         }
     }
 
+    void swap_micro()  // microphysics_advance_inner (microphysics.cpp:642-653)
+    {
+        if (nprog == 7)
+            for (int f = 4; f < 7; f++) std::swap(ci[f], pi_[f]);
+    }
+
     void swap_inner(bool micro)
     {
         for (int f = 0; f < 4; f++) std::swap(ci[f], pi_[f]);
@@ -1050,7 +1062,7 @@ class Engine : public EngineBase {
             break;
         case GA_OP_ADVECT_THETA: advect(step, ADV_TH); break;
         case GA_OP_ADVECT_MICRO:
-            if (moist) advect(step, ADV_Q);
+            if (moist) advect(step, cfg.linear_model ? (ADV_Q | ADV_QVONLY) : ADV_Q);  // advect_qv when linear
             break;
         case GA_OP_ZERO_MOISTURE:
             if (moist) {
@@ -1165,6 +1177,53 @@ class Engine : public EngineBase {
         fl[FQV] = fl[FQC] = fl[FQR] = PF_SPONGE | PF_VBC | PF_WRITE_M;
         post(fl, 7, 1.0, true);
         swap_inner(true);
+        mtime += cfg.dt;
+        bigcounter++;
+    }
+
+    // one step of the linearised model: linear_integrate_rk3
+    // (driver_serial.cpp:83-171).  Within a stage the vapour is advected after
+    // the winds' rotation, so stages 1 and 2 advect it with the new winds;
+    // explicit diffusion acts on the start-of-step fields in every stage; no
+    // microphysics; the perturbation is rescaled every 12 hours.
+    void linear_step()
+    {
+        static const double steps[3] = {1. / 3., 0.5, 1.0};
+        const bool moist = kp.moist;
+        kp.stale_signs = 1;
+        for (int s = 0; s < 3; s++) {
+            const double st = steps[s];
+            advect(st, ADV_UV | ADV_WB | ADV_TH);
+            solve_pressure(st);
+            int fl[7] = {0, 0, 0, 0, 0, 0, 0};
+            fl[FU] = fl[FV] = fl[FW] = PF_PROJECT | PF_SPONGE | PF_VBC;
+            fl[FTH] = PF_SPONGE | PF_VBC;
+            post(fl, 7, st, true);
+            if (cfg.use_explicit_diffusion) diffuse(st);  // the start-of-step slot, driver_serial.cpp:102
+            if (s < 2) swap_inner(false);
+            if (moist) {
+                advect(st, ADV_Q | ADV_QVONLY);
+                int fq[7] = {0, 0, 0, 0, 0, 0, 0};
+                fq[FQV] = fq[FQC] = fq[FQR] = PF_SPONGE | PF_VBC;
+                post(fq, 7, st, true);
+                if (s < 2) swap_micro();
+            }
+        }
+        int fl[7] = {0, 0, 0, 0, 0, 0, 0};
+        fl[FU] = fl[FV] = fl[FW] = fl[FTH] = PF_SPONGE | PF_VBC | PF_RAYLEIGH | PF_WRITE_M;
+        fl[FQV] = fl[FQC] = fl[FQR] = PF_SPONGE | PF_VBC | PF_WRITE_M;
+        post(fl, 7, 1.0, true);
+        swap_inner(true);
+        kp.stale_signs = 0;
+        const long period = 12 * 60 * 60 / (int)cfg.dt;
+        if (period > 0 && bigcounter % period == 0 && bigcounter != 0) {
+            cudaMemsetAsync(lin_vmax, 0, sizeof(double), stream);
+            k_lin_vmax<T><<<152 * 4, 256, 0, stream>>>(buf[FV][pi_[FV]], kp.rhou, NZ, N, lin_vmax);
+            k_lin_rescale<T><<<152 * 4, 256, 0, stream>>>(buf[FU][ci[FU]], buf[FV][ci[FV]], buf[FW][ci[FW]],
+                                                          buf[FTH][ci[FTH]], buf[FU][mi[FU]], buf[FV][mi[FV]],
+                                                          buf[FW][mi[FW]], buf[FTH][mi[FTH]], N, lin_vmax);
+            launches += 2;
+        }
         mtime += cfg.dt;
         bigcounter++;
     }
@@ -1427,7 +1486,8 @@ class Engine : public EngineBase {
             }
         }
         for (; n < nsteps; n++) {
-            rk3_step();
+            if (cfg.linear_model) linear_step();
+            else rk3_step();
             int rc = launch_status();
             if (rc) return rc;
         }

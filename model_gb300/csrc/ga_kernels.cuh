@@ -54,6 +54,10 @@ struct KParams {
     int ubase_adv;  // UBAR, VBAR, WBAR, THBAR, QBAR depend on k only
     int ubase_kes;  // THBAR, QBAR, PBAR depend on k only
     const T *btab;
+    // the linearised model (ISLINEAR): perturbation faces advected by the
+    // basic-state velocity alone; stale_signs: its driver's theta and vapour
+    // faces take upwind signs of zero (the sign arrays it never computes)
+    int linear, stale_signs;
 };
 
 // rows of the basic-state table (each nz long), filled by k_base_tables
@@ -155,6 +159,16 @@ __device__ __forceinline__ T f2k(const T *a, const KParams<T> &p, int i, int j, 
     return T(0.5) * (LD(a, c + 1) + LD(a, c));
 }
 
+// the velocity advecting the perturbation at a face: basic state plus
+// perturbation, or the basic state alone in the linearised model (ISLINEAR,
+// fluxes.cpp:328-337, 366-374, 594-650, 1204-1357), for both the upwind sign
+// and the flux
+template <typename T>
+__device__ __forceinline__ T adv_vel(const KParams<T> &p, T basic, T pert)
+{
+    return p.linear ? basic : basic + pert;
+}
+
 // ---------------------------------------------------------------------------
 // momentum face fluxes: interpolate_velocity (fluxes.cpp:1384-1592),
 // advecting_velocity (:1109-1164), compute_fluxes (:582-627)
@@ -166,9 +180,10 @@ __device__ T u_east(const KParams<T> &p, const KFields<T> &F, int i, int j, int 
     const long c = gix(p.ny, p.nz, i, j, k), s = (long)p.ny * p.nz;
     T ua = T(0.5) * (LD(U, c + s) + LD(U, c));
     T uba = T(0.5) * (LD(UB, c + s) + LD(UB, c));
-    T ue = f5i(U, p, i, j, k, sgn(uba + ua));
+    const T at = adv_vel(p, uba, ua);
+    T ue = f5i(U, p, i, j, k, sgn(at));
     T ube = f5i(UB, p, i, j, k, sgn(ua));
-    return ua * ube + (uba + ua) * ue;
+    return ua * ube + at * ue;
 }
 template <typename T>
 __device__ T u_north(const KParams<T> &p, const KFields<T> &F, int i, int j, int k)
@@ -177,9 +192,10 @@ __device__ T u_north(const KParams<T> &p, const KFields<T> &F, int i, int j, int
     const long a = gix(p.ny, p.nz, i, j + 1, k), b = gix(p.ny, p.nz, i - 1, j + 1, k);
     T va = T(0.5) * (LD(V, a) + LD(V, b));
     T vba = T(0.5) * (LD(VB, a) + LD(VB, b));
-    T un = f5j(U, p, i, j, k, sgn(vba + va));
+    const T at = adv_vel(p, vba, va);
+    T un = f5j(U, p, i, j, k, sgn(at));
     T ubn = f5j(UB, p, i, j, k, sgn(va));
-    return va * ubn + (vba + va) * un;
+    return va * ubn + at * un;
 }
 template <typename T>
 __device__ T u_top(const KParams<T> &p, const KFields<T> &F, int i, int j, int k)
@@ -194,10 +210,10 @@ __device__ T u_top(const KParams<T> &p, const KFields<T> &F, int i, int j, int k
         ut = f2k(U, p, i, j, k);
         ubt = f2k(UB, p, i, j, k);
     } else {
-        ut = f3k(U, p, i, j, k, sgn(wba + wa));
+        ut = f3k(U, p, i, j, k, sgn(adv_vel(p, wba, wa)));
         ubt = f3k(UB, p, i, j, k, sgn(wa));
     }
-    return wa * ubt + (wba + wa) * ut;
+    return wa * ubt + adv_vel(p, wba, wa) * ut;
 }
 template <typename T>
 __device__ T v_east(const KParams<T> &p, const KFields<T> &F, int i, int j, int k)
@@ -206,9 +222,10 @@ __device__ T v_east(const KParams<T> &p, const KFields<T> &F, int i, int j, int 
     const long a = gix(p.ny, p.nz, i + 1, j, k), b = gix(p.ny, p.nz, i + 1, j - 1, k);
     T ua = T(0.5) * (LD(U, a) + LD(U, b));
     T uba = T(0.5) * (LD(UB, a) + LD(UB, b));
-    T ve = f5i(V, p, i, j, k, sgn(uba + ua));
+    const T at = adv_vel(p, uba, ua);
+    T ve = f5i(V, p, i, j, k, sgn(at));
     T vbe = f5i(VB, p, i, j, k, sgn(ua));
-    return ua * vbe + (uba + ua) * ve;
+    return ua * vbe + at * ve;
 }
 template <typename T>
 __device__ T v_north(const KParams<T> &p, const KFields<T> &F, int i, int j, int k)
@@ -217,9 +234,10 @@ __device__ T v_north(const KParams<T> &p, const KFields<T> &F, int i, int j, int
     const long c = gix(p.ny, p.nz, i, j, k);
     T va = T(0.5) * (LD(V, c + p.nz) + LD(V, c));
     T vba = T(0.5) * (LD(VB, c + p.nz) + LD(VB, c));
-    T vn = f5j(V, p, i, j, k, sgn(vba + va));
+    const T at = adv_vel(p, vba, va);
+    T vn = f5j(V, p, i, j, k, sgn(at));
     T vbn = f5j(VB, p, i, j, k, sgn(va));
-    return va * vbn + (vba + va) * vn;
+    return va * vbn + at * vn;
 }
 template <typename T>
 __device__ T v_top(const KParams<T> &p, const KFields<T> &F, int i, int j, int k)
@@ -234,10 +252,10 @@ __device__ T v_top(const KParams<T> &p, const KFields<T> &F, int i, int j, int k
         vt = f2k(V, p, i, j, k);
         vbt = f2k(VB, p, i, j, k);
     } else {
-        vt = f3k(V, p, i, j, k, sgn(wba + wa));
+        vt = f3k(V, p, i, j, k, sgn(adv_vel(p, wba, wa)));
         vbt = f3k(VB, p, i, j, k, sgn(wa));
     }
-    return wa * vbt + (wba + wa) * vt;
+    return wa * vbt + adv_vel(p, wba, wa) * vt;
 }
 
 // ---------------------------------------------------------------------------
@@ -250,10 +268,13 @@ __device__ T s_east(const KParams<T> &p, const KFields<T> &F, const T *s, const 
 {
     const long a = gix(p.ny, p.nz, i + 1, j, k);
     T u1 = LD(F.cur[FU], a);
-    T ut = LD(F.bar[0], a) + u1;
-    T se = f5i(s, p, i, j, k, sgn(ut));
+    T ut = sb ? adv_vel(p, LD(F.bar[0], a), u1) : LD(F.bar[0], a) + u1;
+    // the linearised driver's stale signs, except on the face east of column
+    // 2, which compute_west_scalar (fluxes.cpp:479-501) forms from the winds
+    const bool z = sb && p.stale_signs && i != 2;
+    T se = f5i(s, p, i, j, k, z ? T(0) : sgn(ut));
     if (!sb) return ut * se;
-    T be = f5i(sb, p, i, j, k, sgn(u1));
+    T be = f5i(sb, p, i, j, k, z ? T(0) : sgn(u1));
     return u1 * be + ut * se;
 }
 template <typename T>
@@ -261,10 +282,11 @@ __device__ T s_north(const KParams<T> &p, const KFields<T> &F, const T *s, const
 {
     const long a = gix(p.ny, p.nz, i, j + 1, k);
     T v1 = LD(F.cur[FV], a);
-    T vt = LD(F.bar[1], a) + v1;
-    T sn = f5j(s, p, i, j, k, sgn(vt));
+    T vt = sb ? adv_vel(p, LD(F.bar[1], a), v1) : LD(F.bar[1], a) + v1;
+    const bool z = sb && p.stale_signs;
+    T sn = f5j(s, p, i, j, k, z ? T(0) : sgn(vt));
     if (!sb) return vt * sn;
-    T bn = f5j(sb, p, i, j, k, sgn(v1));
+    T bn = f5j(sb, p, i, j, k, z ? T(0) : sgn(v1));
     return v1 * bn + vt * sn;
 }
 template <typename T>
@@ -273,14 +295,15 @@ __device__ T s_top(const KParams<T> &p, const KFields<T> &F, const T *s, const T
     if (k == 0) return T(0);
     const long a = gix(p.ny, p.nz, i, j, k + 1);
     T w1 = LD(F.cur[FW], a);
-    T wt = LD(F.bar[2], a) + w1;
+    T wt = sb ? adv_vel(p, LD(F.bar[2], a), w1) : LD(F.bar[2], a) + w1;
     T st, bt = T(0);
     if (k == 1 || k == p.nz - 2) {
         st = f2k(s, p, i, j, k);
         if (sb) bt = f2k(sb, p, i, j, k);
     } else {
-        st = f3k(s, p, i, j, k, sgn(wt));
-        if (sb) bt = f3k(sb, p, i, j, k, sgn(w1));
+        const bool z = sb && p.stale_signs;
+        st = f3k(s, p, i, j, k, z ? T(0) : sgn(wt));
+        if (sb) bt = f3k(sb, p, i, j, k, z ? T(0) : sgn(w1));
     }
     if (!sb) return wt * st;
     return w1 * bt + wt * st;
@@ -360,7 +383,8 @@ __device__ T s_tend(const KParams<T> &p, const KFields<T> &F, const T *s, const 
 // lateral mirror copies of P u, v, w that precede the pressure solve; they read
 // and write only points the advection does not write.  ADV_ROWS (four-level
 // kernel): east and north faces by sliding rows instead of one per work item
-enum { ADV_UV = 1, ADV_WB = 2, ADV_TH = 4, ADV_Q = 8, ADV_ZERO = 16, ADV_MIRROR = 32, ADV_ROWS = 64 };
+enum { ADV_UV = 1, ADV_WB = 2, ADV_TH = 4, ADV_Q = 8, ADV_ZERO = 16, ADV_MIRROR = 32, ADV_ROWS = 64,
+       ADV_QVONLY = 128 };  // with ADV_Q: the vapour alone (advect_qv, advection.cpp:577-601)
 
 template <typename T>
 __global__ void __launch_bounds__(128) k_advect(KParams<T> p, KFields<T> F, T step, T sdtg, int what)
@@ -407,7 +431,9 @@ __global__ void __launch_bounds__(128) k_advect(KParams<T> p, KFields<T> F, T st
     }
     if (what & ADV_TH)  // advection.cpp:366-370
         F.P[FTH][c] = LD(F.M[FTH], c) + step * s_tend(p, F, F.cur[FTH], F.bar[3], p.tb, i, j, k);
-    if (what & ADV_Q) {  // advection.cpp:466-497
+    if ((what & ADV_Q) && (what & ADV_QVONLY)) {  // advect_qv, advection.cpp:577-601
+        F.P[FQV][c] = LD(F.M[FQV], c) + step * s_tend(p, F, F.cur[FQV], F.bar[4], p.qb, i, j, k);
+    } else if (what & ADV_Q) {  // advection.cpp:466-497
         if (p.rf == 1) {
             const T *QR = F.cur[FQR];
             F.vt[c] = fall_speed_point(p, LD(QR, c), k);
@@ -801,7 +827,7 @@ __device__ void advect_tile_body(const KParams<T> &p, const KFields<T> &F, int b
             F.P[FTH][cix] = LD(F.M[FTH], cix) + step * t;
         }
         if (what & ADV_Q) {
-            if (p.rf == 1) {
+            if (p.rf == 1 && !(what & ADV_QVONLY)) {
                 const T *QR = F.cur[FQR];
                 F.vt[cix] = fall_speed_point(p, LD(QR, cix), k);
                 if (k == 1) F.vt[cix - 1] = fall_speed_point(p, LD(QR, cix), 1);
@@ -824,8 +850,10 @@ __device__ void advect_tile_body(const KParams<T> &p, const KFields<T> &F, int b
                 if (F.qmask) F.qmask[cix] = bits;
             }
             F.P[FQV][cix] = qv;
-            F.P[FQC][cix] = qc;
-            F.P[FQR][cix] = qr;
+            if (!(what & ADV_QVONLY)) {
+                F.P[FQC][cix] = qc;
+                F.P[FQR][cix] = qr;
+            }
         }
     }
 }
@@ -2344,3 +2372,47 @@ __global__ void k_convert_out(double *dst, const T *src, long n)
 }
 
 }  // namespace ga
+
+// ---------------------------------------------------------------------------
+// the linearised model's rescaling every 12 hours of model time
+// (driver_serial.cpp:160-166): find_max2 (util.cpp:818-829), the largest
+// positive rho-weighted value of v in the forecast slot, then rescale_pert2
+// (util.cpp:920-943), x <- (5 x) / max for the current and start-of-step u,
+// v, w and theta.  The maximum is order-independent, so blocks combine it
+// with an atomic maximum on the bit pattern of a non-negative double (whose
+// unsigned order is its numeric order); *out must start at 0.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(256) k_lin_vmax(const T *v, const T *rhou, int nz, long n, double *out)
+{
+    double m = 0.0;
+    for (long x = (long)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (long)gridDim.x * blockDim.x) {
+        const double r = (double)(v[x] * rhou[(int)(x % nz)]);
+        if (r > m) m = r;
+    }
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_down_sync(0xffffffffu, m, o));
+    __shared__ double wm[8];
+    if ((threadIdx.x & 31) == 0) wm[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < (int)(blockDim.x >> 5); w++) m = fmax(m, wm[w]);
+        atomicMax((unsigned long long *)out, (unsigned long long)__double_as_longlong(m));
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_lin_rescale(T *u, T *v, T *w, T *th, T *um, T *vm, T *wm, T *thm,
+                                                     long n, const double *vmax)
+{
+    const T mx = (T)*vmax, scale = T(5.0);
+    for (long x = (long)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (long)gridDim.x * blockDim.x) {
+        u[x] = scale * u[x] / mx;
+        v[x] = scale * v[x] / mx;
+        w[x] = scale * w[x] / mx;
+        th[x] = scale * th[x] / mx;
+        um[x] = scale * um[x] / mx;
+        vm[x] = scale * vm[x] / mx;
+        wm[x] = scale * wm[x] / mx;
+        thm[x] = scale * thm[x] / mx;
+    }
+}

@@ -26,6 +26,13 @@ grep -q '^#define PARALLEL 0' "$OUT/include/stdafx.h"
 # while keeping the serial index arithmetic (oracle/ref/itcz_harness.cpp)
 sed 's/^#define ENERGY 0/#define ENERGY 1/' "$OUT/include/stdafx.h" > "$OUT/include_par/stdafx.h"
 grep -q '^#define ENERGY 1' "$OUT/include_par/stdafx.h"
+# the linearised model (linear_integrate_rk3) is a compile-time switch of the
+# same sources: a third copy with ISLINEAR 1 (the first definition in the file,
+# the one the build's branch selects), built into ref_harness_lin
+mkdir -p "$OUT/include_lin" "$OUT/obj_lin"
+awk 'done == 0 && /^#define ISLINEAR 0/ {print "#define ISLINEAR 1"; done = 1; next} {print}' \
+    "$OUT/include/stdafx.h" > "$OUT/include_lin/stdafx.h"
+grep -q '^#define ISLINEAR 1' "$OUT/include_lin/stdafx.h"
 CXXFLAGS="-O3 -ffp-contract=off -w -I$OUT/include -I$HERE/ref/shim -I$REF/include"
 SRCS="solver initializer data_initializer interpolate fluxes pressure advection turbulence damping
       boundaries util Heating kessler rutledge microphysics energy trajectory laplacian
@@ -42,8 +49,15 @@ g++ $CXXFLAGS -c "$HERE/ref/itcz_harness.cpp" -o "$OUT/obj_par/itcz_harness.o" &
 g++ $CXXFLAGS -c "$HERE/ref/fftw_shim.cpp" -o "$OUT/obj/fftw_shim.o" & pids+=($!)
 g++ $CXXFLAGS -c "$HERE/ref/files_stub.cpp" -o "$OUT/obj/files_stub.o" & pids+=($!)
 gcc -O3 -ffp-contract=off -c "$HERE/ora_fft.c" -o "$OUT/obj/ora_fft.o" & pids+=($!)
+LINFLAGS="-O3 -ffp-contract=off -w -I$OUT/include_lin -I$HERE/ref/shim -I$REF/include"
+for s in $SRCS; do
+    g++ $LINFLAGS -c "$REF/source/$s.cpp" -o "$OUT/obj_lin/$s.o" & pids+=($!)
+done
+g++ $LINFLAGS -c "$HERE/ref/ref_harness.cpp" -o "$OUT/obj_lin/ref_harness.o" & pids+=($!)
 for p in "${pids[@]}"; do wait "$p"; done
 g++ -o "$OUT/ref_harness" "$OUT"/obj/*.o -lm
+g++ -o "$OUT/ref_harness_lin" "$OUT"/obj_lin/*.o "$OUT/obj/fftw_shim.o" "$OUT/obj/files_stub.o" \
+    "$OUT/obj/ora_fft.o" -lm
 COMMON_OBJS=$(ls "$OUT"/obj/*.o | grep -v -e '/data_initializer.o$' -e '/ref_harness.o$')
 g++ -o "$OUT/itcz_harness" $COMMON_OBJS "$OUT"/obj_par/*.o -lm
-echo "built $OUT/ref_harness $OUT/itcz_harness"
+echo "built $OUT/ref_harness $OUT/ref_harness_lin $OUT/itcz_harness"

@@ -70,6 +70,10 @@ struct ora_state {
     unsigned char *sat;
     double *l2, *kvmax;
     double kmixh_max, lH, water_temp, es_water;
+    /* the linearised driver never calls compute_sign_cells, so the scalar
+     * faces read sign arrays as allocation left them: zero (see
+     * linear_rk3_step) */
+    int stale_signs;
     long long bigcounter;
     double mtime;
     int err;
@@ -107,6 +111,15 @@ static inline double face3(double am1, double a0, double a1, double a2, double s
         a[IX(i, (j) + 2, k)], a[IX(i, (j) + 3, k)]
 #define SK(a, i, j, k) a[IX(i, j, (k)-1)], a[IX(i, j, k)], a[IX(i, j, (k) + 1)], a[IX(i, j, (k) + 2)]
 
+/* the velocity that advects the perturbation at a face: basic state plus
+ * perturbation, or in the linearised model (ISLINEAR, fluxes.cpp:328-337,
+ * 366-374, 594-624, 642-650, 1204-1357) the basic state alone, for both the
+ * upwind sign and the flux */
+static inline double adv_vel(const ora_state *S, double basic, double pert)
+{
+    return S->c.linear_model ? basic : basic + pert;
+}
+
 /* ------------------------------------------------------------------------
  * Momentum face fluxes: interpolate_velocity (fluxes.cpp:1384-1592),
  * advecting_velocity (:1109-1164), compute_fluxes (:582-627).
@@ -116,18 +129,20 @@ static double u_east(const ora_state *S, int i, int j, int k)
     const double *U = S->cur[F_U], *UB = S->bar[0];
     double ua = 0.5 * (U[IX(i + 1, j, k)] + U[IX(i, j, k)]);
     double uba = 0.5 * (UB[IX(i + 1, j, k)] + UB[IX(i, j, k)]);
-    double ue = face5(SI(U, i, j, k), sgn(uba + ua));
+    const double at = adv_vel(S, uba, ua);
+    double ue = face5(SI(U, i, j, k), sgn(at));
     double ube = face5(SI(UB, i, j, k), sgn(ua));
-    return ua * ube + (uba + ua) * ue;
+    return ua * ube + at * ue;
 }
 static double u_north(const ora_state *S, int i, int j, int k)
 {
     const double *U = S->cur[F_U], *UB = S->bar[0], *V = S->cur[F_V], *VB = S->bar[1];
     double va = 0.5 * (V[IX(i, j + 1, k)] + V[IX(i - 1, j + 1, k)]);
     double vba = 0.5 * (VB[IX(i, j + 1, k)] + VB[IX(i - 1, j + 1, k)]);
-    double un = face5(SJ(U, i, j, k), sgn(vba + va));
+    const double at = adv_vel(S, vba, va);
+    double un = face5(SJ(U, i, j, k), sgn(at));
     double ubn = face5(SJ(UB, i, j, k), sgn(va));
-    return va * ubn + (vba + va) * un;
+    return va * ubn + at * un;
 }
 static double u_top(const ora_state *S, int i, int j, int k)
 {
@@ -140,28 +155,30 @@ static double u_top(const ora_state *S, int i, int j, int k)
         ut = 0.5 * (U[IX(i, j, k + 1)] + U[IX(i, j, k)]);
         ubt = 0.5 * (UB[IX(i, j, k + 1)] + UB[IX(i, j, k)]);
     } else {
-        ut = face3(SK(U, i, j, k), sgn(wba + wa));
+        ut = face3(SK(U, i, j, k), sgn(adv_vel(S, wba, wa)));
         ubt = face3(SK(UB, i, j, k), sgn(wa));
     }
-    return wa * ubt + (wba + wa) * ut;
+    return wa * ubt + adv_vel(S, wba, wa) * ut;
 }
 static double v_east(const ora_state *S, int i, int j, int k)
 {
     const double *U = S->cur[F_U], *UB = S->bar[0], *V = S->cur[F_V], *VB = S->bar[1];
     double ua = 0.5 * (U[IX(i + 1, j, k)] + U[IX(i + 1, j - 1, k)]);
     double uba = 0.5 * (UB[IX(i + 1, j, k)] + UB[IX(i + 1, j - 1, k)]);
-    double ve = face5(SI(V, i, j, k), sgn(uba + ua));
+    const double at = adv_vel(S, uba, ua);
+    double ve = face5(SI(V, i, j, k), sgn(at));
     double vbe = face5(SI(VB, i, j, k), sgn(ua));
-    return ua * vbe + (uba + ua) * ve;
+    return ua * vbe + at * ve;
 }
 static double v_north(const ora_state *S, int i, int j, int k)
 {
     const double *V = S->cur[F_V], *VB = S->bar[1];
     double va = 0.5 * (V[IX(i, j + 1, k)] + V[IX(i, j, k)]);
     double vba = 0.5 * (VB[IX(i, j + 1, k)] + VB[IX(i, j, k)]);
-    double vn = face5(SJ(V, i, j, k), sgn(vba + va));
+    const double at = adv_vel(S, vba, va);
+    double vn = face5(SJ(V, i, j, k), sgn(at));
     double vbn = face5(SJ(VB, i, j, k), sgn(va));
-    return va * vbn + (vba + va) * vn;
+    return va * vbn + at * vn;
 }
 static double v_top(const ora_state *S, int i, int j, int k)
 {
@@ -174,10 +191,10 @@ static double v_top(const ora_state *S, int i, int j, int k)
         vt = 0.5 * (V[IX(i, j, k + 1)] + V[IX(i, j, k)]);
         vbt = 0.5 * (VB[IX(i, j, k + 1)] + VB[IX(i, j, k)]);
     } else {
-        vt = face3(SK(V, i, j, k), sgn(wba + wa));
+        vt = face3(SK(V, i, j, k), sgn(adv_vel(S, wba, wa)));
         vbt = face3(SK(VB, i, j, k), sgn(wa));
     }
-    return wa * vbt + (wba + wa) * vt;
+    return wa * vbt + adv_vel(S, wba, wa) * vt;
 }
 
 /* advect_uvw_velocity (advection.cpp:304-339) with u_tend_cell (:73-94) and
@@ -243,20 +260,24 @@ static double s_east(const ora_state *S, const double *s, const double *sb, int 
 {
     const double *U = S->cur[F_U], *UB = S->bar[0];
     double u1 = U[IX(i + 1, j, k)];
-    double ut = UB[IX(i + 1, j, k)] + u1;
-    double se = face5(SI(s, i, j, k), sgn(ut));
+    double ut = sb ? adv_vel(S, UB[IX(i + 1, j, k)], u1) : UB[IX(i + 1, j, k)] + u1;
+    /* the face east of column 2 comes from compute_west_scalar (fluxes.cpp:
+     * 479-501), whose signs are taken from the winds */
+    const int z = sb && S->stale_signs && i != 2;
+    double se = face5(SI(s, i, j, k), z ? 0.0 : sgn(ut));
     if (!sb) return ut * se;
-    double be = face5(SI(sb, i, j, k), sgn(u1));
+    double be = face5(SI(sb, i, j, k), z ? 0.0 : sgn(u1));
     return u1 * be + ut * se;
 }
 static double s_north(const ora_state *S, const double *s, const double *sb, int i, int j, int k)
 {
     const double *V = S->cur[F_V], *VB = S->bar[1];
     double v1 = V[IX(i, j + 1, k)];
-    double vt = VB[IX(i, j + 1, k)] + v1;
-    double sn = face5(SJ(s, i, j, k), sgn(vt));
+    double vt = sb ? adv_vel(S, VB[IX(i, j + 1, k)], v1) : VB[IX(i, j + 1, k)] + v1;
+    const int z = sb && S->stale_signs;
+    double sn = face5(SJ(s, i, j, k), z ? 0.0 : sgn(vt));
     if (!sb) return vt * sn;
-    double bn = face5(SJ(sb, i, j, k), sgn(v1));
+    double bn = face5(SJ(sb, i, j, k), z ? 0.0 : sgn(v1));
     return v1 * bn + vt * sn;
 }
 static double s_top(const ora_state *S, const double *s, const double *sb, int i, int j, int k)
@@ -264,14 +285,15 @@ static double s_top(const ora_state *S, const double *s, const double *sb, int i
     if (k == 0) return 0.0;
     const double *W = S->cur[F_W], *WB = S->bar[2];
     double w1 = W[IX(i, j, k + 1)];
-    double wt = WB[IX(i, j, k + 1)] + w1;
+    double wt = sb ? adv_vel(S, WB[IX(i, j, k + 1)], w1) : WB[IX(i, j, k + 1)] + w1;
     double st, bt = 0.0;
     if (k == 1 || k == S->NZ - 2) {
         st = 0.5 * (s[IX(i, j, k + 1)] + s[IX(i, j, k)]);
         if (sb) bt = 0.5 * (sb[IX(i, j, k + 1)] + sb[IX(i, j, k)]);
     } else {
-        st = face3(SK(s, i, j, k), sgn(wt));
-        if (sb) bt = face3(SK(sb, i, j, k), sgn(w1));
+        const int z = sb && S->stale_signs;
+        st = face3(SK(s, i, j, k), z ? 0.0 : sgn(wt));
+        if (sb) bt = face3(SK(sb, i, j, k), z ? 0.0 : sgn(w1));
     }
     if (!sb) return wt * st;
     return w1 * bt + wt * st;
@@ -325,6 +347,17 @@ static void op_advect_theta(ora_state *S, double step) /* advection.cpp:349-373 
                 S->P[F_TH][IX(i, j, k)] =
                     S->M[F_TH][IX(i, j, k)] +
                     step * s_tend(S, S->cur[F_TH], S->bar[3], S->tb, i, j, k);
+}
+
+/* advect_qv (advection.cpp:577-601): the vapour alone, the linearised
+ * model's moisture advection */
+static void op_advect_qv(ora_state *S, double step)
+{
+    for (int i = 3; i < S->NX - 3; i++)
+        for (int j = 3; j < S->NY - 3; j++)
+            for (int k = 1; k < S->NZ - 1; k++)
+                S->P[F_QV][IX(i, j, k)] =
+                    S->M[F_QV][IX(i, j, k)] + step * s_tend(S, S->cur[F_QV], S->bar[4], S->qb, i, j, k);
 }
 
 /* calculate_rain_fall_speed_kessler (kessler.cpp:222-252) over [il,ih)x[jl,jh) */
@@ -1357,6 +1390,63 @@ static void rk3_step(ora_state *S) /* driver_serial.cpp:178-286 */
     S->bigcounter++;
 }
 
+/* the linearised model's rescaling every 12 hours (driver_serial.cpp:160-
+ * 166): find_max2 (util.cpp:818-829) of the forecast slot of v weighted by
+ * rho, then rescale_pert2 (util.cpp:920-943) of the current and start-of-
+ * step u, v, w and theta (its vapour lines sit under a preprocessor test of a
+ * run-time variable and are compiled out) */
+static void linear_rescale(ora_state *S)
+{
+    const double *VP = S->P[F_V];
+    double mymax = 0;
+    for (int i = 0; i < S->NX; i++)
+        for (int j = 0; j < S->NY; j++)
+            for (int k = 0; k < S->NZ; k++)
+                if (VP[IX(i, j, k)] * S->rhou[k] > fabs(mymax)) mymax = fabs(VP[IX(i, j, k)] * S->rhou[k]);
+    const double scale = 5.0;
+    for (long x = 0; x < S->N; x++)
+        for (int f = F_U; f <= F_TH; f++) {
+            S->cur[f][x] = scale * S->cur[f][x] / mymax;
+            S->M[f][x] = scale * S->M[f][x] / mymax;
+        }
+}
+
+static void linear_rk3_step(ora_state *S) /* linear_integrate_rk3, driver_serial.cpp:83-171 */
+{
+    static const double steps[3] = {1. / 3., 0.5, 1.0};
+    const int micro = S->c.microphysics_option != 0;
+    /* unlike s_integrate_rk3 (driver_serial.cpp:202) this driver never calls
+     * compute_sign_cells (fluxes.cpp:316-341), and interpolate_scalar
+     * (fluxes.cpp:797-942) takes the theta and vapour faces' upwind signs from
+     * those arrays, which initialize_sign_cells (:273-277) left as allocated:
+     * zero, so those faces are the centred ones */
+    S->stale_signs = 1;
+    for (int s = 0; s < 3; s++) {
+        integrate_non_hydro(S, steps[s]);
+        op_advect_theta(S, steps[s]);
+        if (S->c.use_explicit_diffusion) op_explicit_diffusion(S, steps[s]);
+        op_bc(S);
+        if (s < 2) advance_inner(S);
+        if (micro) { /* after the winds' swap: stages 1 and 2 advect with the new winds */
+            op_advect_qv(S, steps[s]);
+            op_bc_micro(S);
+            if (s < 2) micro_advance_inner(S);
+        }
+    }
+    op_bc(S);
+    op_rayleigh(S);
+    advance_outer(S);
+    if (micro) {
+        op_bc_micro(S);
+        micro_advance(S);
+    }
+    S->stale_signs = 0;
+    const long period = 12 * 60 * 60 / (int)S->dt;
+    if (period > 0 && S->bigcounter % period == 0 && S->bigcounter != 0) linear_rescale(S);
+    S->mtime += S->dt;
+    S->bigcounter++;
+}
+
 /* ------------------------------------------------------------------------
  * Column builders: setup_vertical_height_levels (initializer.cpp:840-849),
  * stretched_grid (:1340-1385), initialize_vertical_basic_state2 (:858-928),
@@ -1620,7 +1710,10 @@ int ora_op(ora_state *S, int op, double step)
     case GA_OP_PROJECT: op_project(S, step); return GA_OK;
     case GA_OP_INTEGRATE_NON_HYDRO: integrate_non_hydro(S, step); return GA_OK;
     case GA_OP_ADVECT_THETA: op_advect_theta(S, step); return GA_OK;
-    case GA_OP_ADVECT_MICRO: op_advect_micro(S, step); return GA_OK;
+    case GA_OP_ADVECT_MICRO:
+        if (S->c.linear_model) op_advect_qv(S, step);
+        else op_advect_micro(S, step);
+        return GA_OK;
     case GA_OP_ZERO_MOISTURE: op_zero_moisture(S); return GA_OK;
     case GA_OP_BC: op_bc(S); return GA_OK;
     case GA_OP_BC_MICRO: op_bc_micro(S); return GA_OK;
@@ -1640,13 +1733,19 @@ int ora_op(ora_state *S, int op, double step)
 int ora_step(ora_state *S, int nsteps)
 {
     for (int n = 0; n < nsteps; n++) {
-        rk3_step(S);
+        if (S->c.linear_model) linear_rk3_step(S);
+        else rk3_step(S);
         if (S->err) return S->err;
     }
     return GA_OK;
 }
 
 long long ora_bigcounter(ora_state *S) { return S->bigcounter; }
+void ora_set_counters(ora_state *S, long long bigcounter, double mtime)
+{
+    S->bigcounter = bigcounter;
+    S->mtime = mtime;
+}
 int ora_error(ora_state *S) { return S->err; }
 
 /* Tangent-linear model and adjoint of the dry step (test infrastructure). */

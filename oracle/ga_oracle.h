@@ -29,6 +29,7 @@ int        ora_get_field(ora_state *s, int field, int slot, double *dst, long n)
 int        ora_op(ora_state *s, int op, double step);
 int        ora_step(ora_state *s, int nsteps);
 long long  ora_bigcounter(ora_state *s);
+void       ora_set_counters(ora_state *s, long long bigcounter, double mtime);
 /* Non-zero once Kessler met E>100, where the reference calls exit(0). */
 int        ora_error(ora_state *s);
 

@@ -24,6 +24,7 @@ from oracle.ga_bundle import read_bundle, write_bundle
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle.so")
 REF_HARNESS = os.path.join(HERE, "_ref", "ref_harness")
+REF_HARNESS_LIN = os.path.join(HERE, "_ref", "ref_harness_lin")  # the ISLINEAR build
 
 _lib = None
 _DP = C.POINTER(C.c_double)
@@ -50,6 +51,8 @@ def lib() -> C.CDLL:
         L.ora_step.argtypes = [C.c_void_p, C.c_int]
         L.ora_bigcounter.argtypes = [C.c_void_p]
         L.ora_bigcounter.restype = C.c_longlong
+        L.ora_set_counters.argtypes = [C.c_void_p, C.c_longlong, C.c_double]
+        L.ora_set_counters.restype = None
         L.ora_error.argtypes = [C.c_void_p]
         L.ora_lin_create.argtypes = [C.c_void_p]
         L.ora_lin_create.restype = C.c_void_p
@@ -137,6 +140,9 @@ class Oracle:
 
     def step(self, n: int = 1) -> int:
         return lib().ora_step(self.h, n)
+
+    def set_counters(self, bigcounter: int, mtime: float) -> None:
+        lib().ora_set_counters(self.h, bigcounter, mtime)
 
     def op(self, name: str, step: float = 1.0) -> int:
         return lib().ora_op(self.h, abi.OPS[name], step)
@@ -233,7 +239,7 @@ def run_reference(workload, mode: str = "run", nsteps: int = 1, op: str = "", st
     with tempfile.TemporaryDirectory() as td:
         fin, fout = os.path.join(td, "in.bin"), os.path.join(td, "out.bin")
         write_bundle(fin, workload_bundle(workload, extra))
-        args = [REF_HARNESS, fin, fout, mode]
+        args = [REF_HARNESS_LIN if getattr(workload, "linear_model", 0) else REF_HARNESS, fin, fout, mode]
         args += [str(nsteps)] if mode == "run" else [op, repr(step)]
         subprocess.run(args, check=True, stdout=subprocess.DEVNULL)
         return read_bundle(fout)

@@ -35,6 +35,8 @@
 #include <vector>
 
 void s_integrate_rk3();
+void linear_integrate_rk3();
+void advect_qv(double, int, int, int, int);
 extern double *Kmix, *KHmix;  /* turbulence.cpp: mixing coefficients */
 extern bool *isSaturated;     /* turbulence.cpp: Kessler saturation record */
 void zero_moisture(int il, int ih, int jl, int jh, int size);
@@ -205,10 +207,18 @@ int main(int argc, char **argv)
     init_damping(NX, NY, NZ);                       /* driver_serial.cpp:72-74 */
     init_diffusion_weights(DIFFUSION_ORDER, &ZU(0));
 
+    if (has(in, "bigcounter0")) {  /* a run that starts later in the model's life (restart counters) */
+        bigcounter = (int)scal(in, "bigcounter0");
+        mtime = scal(in, "mtime0");
+    }
     if (mode == "run") {
         int nsteps = atoi(argv[4]);
         for (int n = 0; n < nsteps; n++) {
+#if ISLINEAR
+            linear_integrate_rk3();  /* s_run_model, driver_serial.cpp:331 */
+#else
             s_integrate_rk3();
+#endif
             mtime += dt;
             bigcounter++;
         }
@@ -222,6 +232,7 @@ int main(int argc, char **argv)
         else if (name == "integrate_non_hydro") integrate_non_hydro(step, 0, NX, 0, NY);
         else if (name == "advect_theta") advect_theta(step, 3, NX - 3, 3, NY - 3);
         else if (name == "advect_micro") advect_microphysics_cell(step, 3, NX - 3, 3, NY - 3);
+        else if (name == "advect_qv") advect_qv(step, 3, NX - 3, 3, NY - 3);
         else if (name == "zero_moisture") zero_moisture(1, NX - 1, 1, NY - 1, (int)N);
         else if (name == "bc") apply_boundary_condition(0);
         else if (name == "bc_micro") apply_boundary_condition_microphysics(0);

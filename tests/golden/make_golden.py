@@ -9,6 +9,7 @@ inputs and outputs as compressed .npz files:
                    buffers all hold different data
   turb_<case>.npz  the turbulence tendencies (calculate_diff_tend) of such a
                    state, and Kessler's saturation record
+  linop_<case>.npz the linearised model's operators (the ISLINEAR build)
 
 Usage (where the reference sources exist):  python tests/golden/make_golden.py
 The fixtures are then read by tests/test_golden_oracle.py (CPU) and
@@ -39,6 +40,14 @@ def _turbulent(wl, surface_flux=0, water_temp=28.0):
     return wl
 
 
+def _linear(wl, bigcounter0=0):
+    wl.linear_model = 1
+    if bigcounter0:  # dt = 30 s: the rescaling falls on every 1440th step
+        wl.fields["bigcounter0"] = np.float64(bigcounter0)
+        wl.fields["mtime0"] = np.float64(bigcounter0 * wl.dt)
+    return wl
+
+
 def _jet(moist):
     return configs.jet_vortex(nx=16, ny=14, nz=10, dx=20000.0, dz=800.0, dt=30.0, rmax=60000.0, vmax=8.0,
                               moist=moist, noise=0.3, extra_basic=1.0)
@@ -65,6 +74,12 @@ RUN_CASES = {
     "turbulence_moist": (lambda: _turbulent(configs.moist_blob(nx=15, ny=14, nz=10)), 4),
     "turbulence_moist_sfc": (lambda: _turbulent(configs.moist_blob(nx=18, ny=14, nz=10, periodic=1), 1, 30.0), 4),
     "turbulence_jet_sfc": (lambda: _turbulent(_jet(True), 1, 26.0), 3),
+    # the linearised model (linear_integrate_rk3): dry and moist jets, with
+    # explicit diffusion in every stage, and across a 12-hour rescaling
+    "linear_dry": (lambda: _linear(_jet(False)), 4),
+    "linear_moist": (lambda: _linear(_jet(True)), 4),
+    "linear_diffusion": (lambda: _linear(_diffusing(_jet(True), 4, 0.004)), 3),
+    "linear_rescale": (lambda: _linear(_jet(False), bigcounter0=1438), 4),
 }
 
 OP_NAMES = ["advect_uvw", "solve_pressure", "integrate_non_hydro", "advect_theta",
@@ -188,6 +203,35 @@ def make_turb():
         print("wrote", path, os.path.getsize(path))
 
 
+LINEAR_OPS = {"advect_uvw": "advect_uvw", "advect_theta": "advect_theta", "advect_micro": "advect_qv",
+              "integrate_non_hydro": "integrate_non_hydro"}
+
+
+def make_linear_ops():
+    """linop_<case>.npz: the linearised operators (the ISLINEAR build) on a
+    state whose rotation slots differ; the moisture operator of the
+    linearised model is advect_qv"""
+    for cname, wl in {"jet": _linear(_jet(True))}.items():
+        extra = _ops_state(wl, 9000)
+        d = _inputs(wl)
+        for k, v in extra.items():
+            d["in_" + k] = v.ravel()
+        for op, ref_op in LINEAR_OPS.items():
+            st = 0.5
+            out = O.run_reference(wl, "op", op=ref_op, step=st, extra=extra)
+            d[f"step_{op}"] = np.float64(st)
+            for k, v in out.items():
+                if k in abi.COLUMN_NAMES or k in ("f", "bigcounter", "mtime"):
+                    continue
+                ref_in = extra.get(k, wl.fields.get(k))
+                if ref_in is not None and np.array_equal(np.asarray(ref_in).ravel(), v):
+                    continue
+                d[f"{op}__{k}"] = v
+        path = os.path.join(HERE, f"linop_{cname}.npz")
+        np.savez_compressed(path, **d)
+        print("wrote", path, os.path.getsize(path))
+
+
 if __name__ == "__main__":
     if not O.reference_available():
         subprocess_rc = os.system(os.path.join(ROOT, "oracle", "build_ref.sh"))
@@ -196,3 +240,4 @@ if __name__ == "__main__":
     make_runs()
     make_ops()
     make_turb()
+    make_linear_ops()
