@@ -159,6 +159,12 @@ typedef struct ga_config {
      * without microphysics, explicit diffusion in every stage, the
      * perturbation rescaled every 12 hours of model time */
     int    linear_model;            /* 0 or 1                                        */
+    /* the hydrostatic equation set (HYDROSTATIC: integrate_hydro, solver.cpp:
+     * 33-80): u and v advected, pressure from a lid-pressure Poisson solve and
+     * hydrostatic integration (pressure.cpp:229-298, 453-537), w diagnosed
+     * from continuity each stage (w_velocity_LH, solver.cpp:144-163);
+     * non-periodic domains */
+    int    hydrostatic;             /* 0 or 1                                        */
 } ga_config;
 
 /*

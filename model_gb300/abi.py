@@ -66,7 +66,7 @@ class GaConfig(C.Structure):
         ("use_explicit_diffusion", C.c_int), ("diffusion_order", C.c_int),
         ("kdiffh", C.c_double), ("kdiffv", C.c_double),
         ("turbulence_option", C.c_int), ("use_surface_heat_flux", C.c_int), ("water_temp", C.c_double),
-        ("linear_model", C.c_int),
+        ("linear_model", C.c_int), ("hydrostatic", C.c_int),
     ]
 
 

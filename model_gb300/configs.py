@@ -84,6 +84,8 @@ class Workload:
     water_temp: float = 28.0
     # the linearised model (linear_integrate_rk3, driver_serial.cpp:83); off by default
     linear_model: int = 0
+    # the hydrostatic equation set (integrate_hydro, solver.cpp:33); off by default
+    hydrostatic: int = 0
     fields: dict = dataclasses.field(default_factory=dict)
 
     def __post_init__(self):
@@ -101,7 +103,7 @@ class Workload:
                 "periodic_ew_boundaries", "boundary_width_north", "boundary_width_south",
                 "boundary_width_east", "boundary_width_west", "rayleigh_damping_z",
                 "height_lowest_level", "corner_lat", "use_explicit_diffusion", "diffusion_order", "kdiffh",
-                "kdiffv", "turbulence_option", "use_surface_heat_flux", "water_temp", "linear_model")
+                "kdiffv", "turbulence_option", "use_surface_heat_flux", "water_temp", "linear_model", "hydrostatic")
         return {k: getattr(self, k) for k in keys}
 
 

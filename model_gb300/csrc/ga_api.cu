@@ -136,8 +136,11 @@ int ga_create(const ga_config *cfg, const ga_columns *cols, ga_ctx **out)
     if (cfg->turbulence_option < 0 || cfg->turbulence_option > 1 || cfg->use_surface_heat_flux < 0 ||
         cfg->use_surface_heat_flux > 1)
         return fail(GA_ERR_CONFIG, "ga_create: turbulence_option and use_surface_heat_flux must be 0 or 1");
-    if (cfg->linear_model < 0 || cfg->linear_model > 1)
-        return fail(GA_ERR_CONFIG, "ga_create: linear_model must be 0 or 1");
+    if (cfg->linear_model < 0 || cfg->linear_model > 1 || cfg->hydrostatic < 0 || cfg->hydrostatic > 1)
+        return fail(GA_ERR_CONFIG, "ga_create: linear_model and hydrostatic must be 0 or 1");
+    if (cfg->hydrostatic && (cfg->periodic_ew_boundaries || cfg->turbulence_option || cfg->linear_model))
+        return fail(GA_ERR_UNSUPPORTED, "ga_create: the hydrostatic equation set is built for non-periodic "
+                                        "domains without the turbulence scheme or the linearised model");
     if (cfg->linear_model && cfg->turbulence_option)
         return fail(GA_ERR_UNSUPPORTED, "ga_create: the linearised model has no turbulence scheme "
                                         "(linear_integrate_rk3 never computes its tendencies)");
@@ -333,8 +336,8 @@ int ga_ensemble_create(const ga_config *cfgs, const ga_columns *cols, int nmembe
             return fail(GA_ERR_UNSUPPORTED, "ga_ensemble_create: explicit diffusion is not batched");
         if (c.turbulence_option)
             return fail(GA_ERR_UNSUPPORTED, "ga_ensemble_create: the turbulence scheme is not batched");
-        if (c.linear_model)
-            return fail(GA_ERR_UNSUPPORTED, "ga_ensemble_create: the linearised model is not batched");
+        if (c.linear_model || c.hydrostatic)
+            return fail(GA_ERR_UNSUPPORTED, "ga_ensemble_create: the linearised and hydrostatic sets are not batched");
         if (c.microphysics_option == 1 && c.rain_fallout != 1)
             return fail(GA_ERR_UNSUPPORTED, "ga_ensemble_create: only Eulerian rain fallout is batched");
         if (c.nx < 12 || c.ny < 12 || c.nz < 6 || c.nz > 128 || !(c.dx > 0 && c.dy > 0 && c.dz > 0 && c.dt > 0))

@@ -16,6 +16,7 @@
 #include "ga_kernels.cuh"
 #include "ga_quad.cuh"
 #include "ga_turb.cuh"
+#include "ga_hydro.cuh"
 
 #include <cudaTypedefs.h>
 
@@ -123,6 +124,8 @@ class Engine : public EngineBase {
     TurbArgs<T> turb{};
     unsigned char *turb_sat = nullptr;
     double *lin_vmax = nullptr;  // the linearised model's rescaling maximum
+    HydArgs<T> hyd{};            // the hydrostatic equation set (hyd.div null when off)
+    int hyd_L = 1;               // y-lines per block of its x transforms
 
     // Fornberg's recurrence for finite-difference weights: c[i*(m+1)+d] is the
     // weight of point x[i] in derivative d at z (util.cpp:199-247)
@@ -321,6 +324,37 @@ class Engine : public EngineBase {
             budget_w = upload(wk);
             budget_part = dalloc<double>((size_t)BUDGET_BLOCKS * GA_NB + GA_NB);
         }
+        if (c->hydrostatic) {  // init_fft2d (pressure.cpp:601-645), column_average_density
+            kp.hydrostatic = 1;
+            std::vector<double> du(NZ, 0.0), dw(NZ, 0.0);
+            for (int k = 0; k + 1 < NZ; k++) du[k] = cols->zsw[k + 1] - cols->zsw[k];
+            for (int k = 1; k < NZ; k++) dw[k] = cols->zsu[k] - cols->zsu[k - 1];
+            hyd.dzu = col_T(du.data(), NZ);
+            hyd.dzw = col_T(dw.data(), NZ);
+            double r = 0, zsum = 0;
+            for (int k = 1; k < NZ - 1; k++) {
+                r = r + cols->rhou[k] * cols->tbv[k] * du[k];
+                zsum += du[k];
+            }
+            hyd.rhoavg = (T)(r / zsum);
+            hyd.dz = (T)dz;
+            std::vector<double> ac(NY, 1. / (dy * dy)), cc(NY, 1. / (dy * dy)), bco((size_t)NX * NY);
+            ac[0] = 0;
+            cc[NY - 1] = 0;
+            for (int i = 0; i < NX; i++) {
+                const double kw = i < NX / 2 ? 2 * trigpi * (double)i / NX : 2 * trigpi * (double)(NX - i) / NX;
+                for (int j = 0; j < NY; j++)
+                    bco[(size_t)i * NY + j] = j == 0 ? -cols->rhow[2] / (dx * dx)
+                                                     : 2. * (cos(kw) - 1.) / (dx * dx) - cc[j] - ac[j];
+            }
+            hyd.bco = upload(bco);
+            hyd.ac = upload(ac);
+            hyd.cc = upload(cc);
+            hyd.pw = dalloc<double>((size_t)NX * 3 * (NY + 1));
+            hyd.div = dalloc<T>((size_t)NX * NY);
+            hyd.spec2 = dalloc<T2>((size_t)NX * NY);
+            hyd_L = (int)std::max<size_t>(1, std::min<size_t>(8, 49152 / (2 * (size_t)NX * sizeof(T2))));
+        }
         if (c->linear_model) {  // linear_integrate_rk3: eager steps (a rescaling may fall on any step)
             kp.linear = 1;
             use_graphs = false;
@@ -512,6 +546,7 @@ class Engine : public EngineBase {
         F.accrain = accrain;
         F.qmask = qmask;
         F.sat = turb_sat;
+        if (hyd.div) F.P[FW] = F.M[FW] = F.cur[FW];  // w lives in the current slot (boundaries.cpp:152-156)
         return F;
     }
 
@@ -838,6 +873,38 @@ class Engine : public EngineBase {
         launches += 2;
     }
 
+    // solve_pressure of the hydrostatic set (pressure.cpp:142-170, 229-298)
+    void hyd_solve(double step)
+    {
+        KFields<T> F = fields();
+        ProfScope ps(this, PC_THOMAS, 8);
+        const long e3 = 2L * (NX + NY - 2) * (NZ - 2);
+        k_mirror_edges<T><<<cdiv(e3, 256), 256, 0, stream>>>(kp, F.P[FU], F.P[FV], F.P[FV]);
+        const long ncol = (long)(NX - 2) * (NY - 2);
+        k_hyd_divavg<T><<<cdiv(ncol, 256), 256, 0, stream>>>(kp, F, hyd, (T)step);
+        k_hyd_mirror2d<T><<<cdiv(2L * (NX + NY - 2), 256), 256, 0, stream>>>(kp, hyd.div);
+        const size_t sm = 2 * (size_t)NX * hyd_L * sizeof(T2);
+        const dim3 fb(hyd_L, std::max(1, 256 / hyd_L));
+        k_hyd_fft<T><<<cdiv(NY, hyd_L), fb, sm, stream>>>(kp, hyd, plan_i, tw_i, 0, hyd_L);
+        k_hyd_thomas<T><<<cdiv(NX, 64), 64, 0, stream>>>(kp, hyd);
+        k_hyd_fft<T><<<cdiv(NY, hyd_L), fb, sm, stream>>>(kp, hyd, plan_i, tw_i, 1, hyd_L);
+        k_hyd_pi<T><<<cdiv(ncol, 128), 128, 0, stream>>>(kp, F, hyd);
+        k_mirror_edges<T><<<cdiv(e3, 256), 256, 0, stream>>>(kp, pi, pi, pi);
+        launches += 8;
+    }
+    void hyd_project(double step)
+    {
+        const long tot = (long)(NX - 2) * (NY - 2) * (NZ - 2);
+        k_hyd_project<T><<<cdiv(tot, 256), 256, 0, stream>>>(kp, fields(), (T)step);
+        launches++;
+    }
+    void hyd_w()
+    {
+        const long ncol = (long)(NX - 2) * (NY - 2);
+        k_hyd_w<T><<<cdiv(ncol, 128), 128, 0, stream>>>(kp, fields(), hyd);
+        launches++;
+    }
+
     // calculate_diff_tend (turbulence.cpp:158-188) from the start-of-step slot
     void turbulence()
     {
@@ -1027,7 +1094,8 @@ class Engine : public EngineBase {
 
     void swap_inner(bool micro)
     {
-        for (int f = 0; f < 4; f++) std::swap(ci[f], pi_[f]);
+        for (int f = 0; f < 4; f++)
+            if (f != FW || !hyd.div) std::swap(ci[f], pi_[f]);  // solver.cpp:240-248
         if (micro && nprog == 7)
             for (int f = 4; f < 7; f++) std::swap(ci[f], pi_[f]);
     }
@@ -1036,7 +1104,8 @@ class Engine : public EngineBase {
     {
         ProfScope ps(this, PC_COPY, 0);
         for (int f = f0; f < f1 && f < nprog; f++)
-            cudaMemcpyAsync(buf[f][mi[f]], buf[f][pi_[f]], N * sizeof(T), cudaMemcpyDeviceToDevice, stream);
+            if (f != FW || !hyd.div)
+                cudaMemcpyAsync(buf[f][mi[f]], buf[f][pi_[f]], N * sizeof(T), cudaMemcpyDeviceToDevice, stream);
     }
 
     int op(int o, double step) override
@@ -1047,13 +1116,26 @@ class Engine : public EngineBase {
         int fl[7] = {0, 0, 0, 0, 0, 0, 0};
         switch (o) {
         case GA_OP_SIGN_CELLS: break;
-        case GA_OP_ADVECT_UVW: advect(step, ADV_UV | ADV_WB); break;
-        case GA_OP_SOLVE_PRESSURE: solve_pressure(step); break;
+        case GA_OP_ADVECT_UVW: advect(step, hyd.div ? ADV_UV : ADV_UV | ADV_WB); break;  // advect_uv_velocity
+        case GA_OP_SOLVE_PRESSURE:
+            if (hyd.div) hyd_solve(step);
+            else solve_pressure(step);
+            break;
         case GA_OP_PROJECT:
+            if (hyd.div) {
+                hyd_project(step);
+                break;
+            }
             fl[FU] = fl[FV] = fl[FW] = PF_PROJECT;
             post(fl, 7, step, false);
             break;
         case GA_OP_INTEGRATE_NON_HYDRO:
+            if (hyd.div) {  // integrate_hydro (solver.cpp:33-80)
+                advect(step, ADV_UV);
+                hyd_solve(step);
+                hyd_project(step);
+                break;
+            }
             advect(step, ADV_UV | ADV_WB);
             turb_apply(TA_VEL, step);  // solver.cpp:103
             solve_pressure(step);
@@ -1144,6 +1226,19 @@ class Engine : public EngineBase {
                     cudaMemcpyAsync(rec + (size_t)(nprog * s + f) * N, buf[f][ci[f]], N * sizeof(T),
                                     cudaMemcpyDeviceToDevice, stream);
             qmask = mrec ? mrec + (size_t)s * N : nullptr;
+            if (hyd.div) {  // the hydrostatic set: driver_serial.cpp:208-239 with integrate_hydro
+                advect(st, ADV_UV | ADV_TH | (moist ? (ADV_Q | ADV_ZERO) : 0));
+                hyd_solve(st);
+                hyd_project(st);
+                hyd_w();
+                int fh[7] = {0, 0, 0, 0, 0, 0, 0};
+                fh[FU] = fh[FV] = fh[FW] = fh[FTH] = PF_SPONGE | PF_VBC;  // w: the current slot
+                fh[FQV] = fh[FQC] = fh[FQR] = PF_ZERO | PF_SPONGE | PF_VBC;
+                post(fh, 7, st, true);
+                qmask = nullptr;
+                if (s < 2) swap_inner(true);
+                continue;
+            }
             // the four-level advection launch also makes the mirror copies of
             // the pressure solve (they touch no point the advection writes)
             const bool fuse_mirror = !kp.periodic && adv_quad && quad_ok(adv_qi, adv_qj);

@@ -58,6 +58,9 @@ struct KParams {
     // basic-state velocity alone; stale_signs: its driver's theta and vapour
     // faces take upwind signs of zero (the sign arrays it never computes)
     int linear, stale_signs;
+    // the hydrostatic equation set: pi is the Exner perturbation itself
+    // (CONVERT_PRESSURE, kessler.cpp:7-11), w is diagnosed
+    int hydrostatic;
 };
 
 // rows of the basic-state table (each nz long), filled by k_base_tables
@@ -1881,6 +1884,7 @@ template <typename T> __device__ __forceinline__ T kneg(T a) { return -a; }
 template <typename T>
 struct KesPoint {
     T thbar, qbar, pbar, tb, qb, tbv, rhou, dt;
+    int hyd;  // hydrostatic set: pressure = pi + pbar
 };
 
 // run_kessler_microphysics at one point: (thp, qvp, qcp, qrp) updated in
@@ -1895,7 +1899,7 @@ __device__ __forceinline__ bool kessler_point(S &thp, S &qvp, S &qcp, S &qrp, co
     const T dt = c.dt, rhou = c.rhou;
     const S zero = thp - thp;  // 0 of the scalar type, derivative 0
     S theta = thp + c.thbar + c.tb;
-    S pressure = pi / (cp * c.tbv) + c.pbar;
+    S pressure = c.hyd ? pi + c.pbar : pi / (cp * c.tbv) + c.pbar;
     S vapor = qvp + c.qbar + c.qb;
     S temperature = theta * pressure;
     S pd = p0 * kpow(pressure, cpRd);
@@ -1962,6 +1966,7 @@ __device__ __forceinline__ KesPoint<T> kes_point(const KParams<T> &p, const KFie
     c.tbv = p.tbv[k];
     c.rhou = p.rhou[k];
     c.dt = p.dt;
+    c.hyd = p.hydrostatic;
     return c;
 }
 
@@ -2249,6 +2254,7 @@ __global__ void __launch_bounds__(256) k_diffuse_tend(KParams<T> p, KFields<T> F
         r /= nk;
         const int j = 3 + (int)(r % nj), i = 3 + (int)(r / nj);
         const long c = gix(p.ny, p.nz, i, j, k);
+        if (f == FW && p.hydrostatic) continue;  // damping.cpp:1052: no w when hydrostatic
         const T *v = F.M[f];
         const int ind = order + 1, nz = p.nz;
         T d;
@@ -2282,6 +2288,7 @@ __global__ void __launch_bounds__(256) k_diffuse_add(KParams<T> p, KFields<T> F,
         r /= nk;
         const int j = 3 + (int)(r % nj), i = 3 + (int)(r / nj);
         const long c = gix(p.ny, p.nz, i, j, k);
+        if (f == FW && p.hydrostatic) continue;
         F.M[f][c] += tend[(long)f * p.n + c];
     }
 }

@@ -533,8 +533,8 @@ int Engine<T>::lin_supported() const
         set_error("tangent-linear / adjoint: the turbulence scheme is not linearised");
         return GA_ERR_UNSUPPORTED;
     }
-    if (cfg.linear_model) {
-        set_error("tangent-linear / adjoint: contexts of the linearised model have none");
+    if (cfg.linear_model || cfg.hydrostatic) {
+        set_error("tangent-linear / adjoint: contexts of the linearised model or the hydrostatic set have none");
         return GA_ERR_UNSUPPORTED;
     }
     return GA_OK;

@@ -33,6 +33,11 @@ mkdir -p "$OUT/include_lin" "$OUT/obj_lin"
 awk 'done == 0 && /^#define ISLINEAR 0/ {print "#define ISLINEAR 1"; done = 1; next} {print}' \
     "$OUT/include/stdafx.h" > "$OUT/include_lin/stdafx.h"
 grep -q '^#define ISLINEAR 1' "$OUT/include_lin/stdafx.h"
+# the hydrostatic equation set likewise (HYDROSTATIC 1), built into ref_harness_hyd
+mkdir -p "$OUT/include_hyd" "$OUT/obj_hyd"
+awk 'done == 0 && /^#define HYDROSTATIC 0/ {print "#define HYDROSTATIC 1"; done = 1; next} {print}' \
+    "$OUT/include/stdafx.h" > "$OUT/include_hyd/stdafx.h"
+grep -q '^#define HYDROSTATIC 1' "$OUT/include_hyd/stdafx.h"
 CXXFLAGS="-O3 -ffp-contract=off -w -I$OUT/include -I$HERE/ref/shim -I$REF/include"
 SRCS="solver initializer data_initializer interpolate fluxes pressure advection turbulence damping
       boundaries util Heating kessler rutledge microphysics energy trajectory laplacian
@@ -54,10 +59,17 @@ for s in $SRCS; do
     g++ $LINFLAGS -c "$REF/source/$s.cpp" -o "$OUT/obj_lin/$s.o" & pids+=($!)
 done
 g++ $LINFLAGS -c "$HERE/ref/ref_harness.cpp" -o "$OUT/obj_lin/ref_harness.o" & pids+=($!)
+HYDFLAGS="-O3 -ffp-contract=off -w -I$OUT/include_hyd -I$HERE/ref/shim -I$REF/include"
+for s in $SRCS; do
+    g++ $HYDFLAGS -c "$REF/source/$s.cpp" -o "$OUT/obj_hyd/$s.o" & pids+=($!)
+done
+g++ $HYDFLAGS -c "$HERE/ref/ref_harness.cpp" -o "$OUT/obj_hyd/ref_harness.o" & pids+=($!)
 for p in "${pids[@]}"; do wait "$p"; done
 g++ -o "$OUT/ref_harness" "$OUT"/obj/*.o -lm
 g++ -o "$OUT/ref_harness_lin" "$OUT"/obj_lin/*.o "$OUT/obj/fftw_shim.o" "$OUT/obj/files_stub.o" \
     "$OUT/obj/ora_fft.o" -lm
+g++ -o "$OUT/ref_harness_hyd" "$OUT"/obj_hyd/*.o "$OUT/obj/fftw_shim.o" "$OUT/obj/files_stub.o" \
+    "$OUT/obj/ora_fft.o" -lm
 COMMON_OBJS=$(ls "$OUT"/obj/*.o | grep -v -e '/data_initializer.o$' -e '/ref_harness.o$')
 g++ -o "$OUT/itcz_harness" $COMMON_OBJS "$OUT"/obj_par/*.o -lm
-echo "built $OUT/ref_harness $OUT/ref_harness_lin $OUT/itcz_harness"
+echo "built $OUT/ref_harness $OUT/ref_harness_lin $OUT/ref_harness_hyd $OUT/itcz_harness"

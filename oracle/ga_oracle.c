@@ -74,6 +74,9 @@ struct ora_state {
      * faces read sign arrays as allocation left them: zero (see
      * linear_rk3_step) */
     int stale_signs;
+    /* hydrostatic equation set: the lid-pressure Poisson solve (init_fft2d,
+     * pressure.cpp:601-645), column-average density (initializer.cpp:1265) */
+    double *div2d, *rhoavg, *bco2, *ac2, *cc2, *p2, *q2, *io2d;
     long long bigcounter;
     double mtime;
     int err;
@@ -228,6 +231,7 @@ static void op_advect_uvw(ora_state *S, double step)
                             S->dt * S->f[j] * ov_v;
                 S->P[F_V][IX(i, j, k)] = S->M[F_V][IX(i, j, k)] + step * vt;
             }
+    if (S->c.hydrostatic) return; /* advect_uv_velocity (advection.cpp:269-293): no w */
     /* buoyancy: advection.cpp:329-337 with buoyancy_dry / buoyancy_warm_micro (:42-52) */
     const double *TH = S->cur[F_TH], *tbv = S->tbv;
     const int moist = S->c.microphysics_option != 0;
@@ -608,6 +612,11 @@ static void upper_lower_zero(ora_state *S, double *v)
         }
 }
 
+/* the array the boundary conditions and damping treat as w: the forecast,
+ * or under the hydrostatic equation set the diagnosed current w
+ * (boundaries.cpp:152-156, damping.cpp:1168-1172) */
+static double *w_bc(ora_state *S) { return S->c.hydrostatic ? S->cur[F_W] : S->P[F_W]; }
+
 static void op_bc(ora_state *S)
 {
     const int per = S->c.periodic_ew_boundaries;
@@ -618,8 +627,8 @@ static void op_bc(ora_state *S)
         upper_lower(S, S->P[F_U]);
         upper_lower(S, S->P[F_V]);
         upper_lower(S, S->P[F_TH]);
-        sponge(S, S->P[F_W], 0);
-        upper_lower_zero(S, S->P[F_W]);
+        sponge(S, w_bc(S), 0);
+        upper_lower_zero(S, w_bc(S));
     } else {
         sponge(S, S->P[F_U], 1);
         sponge(S, S->P[F_V], 1);
@@ -631,9 +640,9 @@ static void op_bc(ora_state *S)
         upper_lower(S, S->P[F_U]);
         upper_lower(S, S->P[F_V]);
         upper_lower(S, S->P[F_TH]);
-        sponge(S, S->P[F_W], 1);
-        periodic_ew(S, S->P[F_W]);
-        upper_lower_zero(S, S->P[F_W]);
+        sponge(S, w_bc(S), 1);
+        periodic_ew(S, w_bc(S));
+        upper_lower_zero(S, w_bc(S));
     }
 }
 
@@ -656,7 +665,7 @@ static void op_rayleigh(ora_state *S) /* damping.cpp:1148-1177 */
                 long ix = IX(i, j, k);
                 S->P[F_U][ix] -= cu * S->P[F_U][ix];
                 S->P[F_V][ix] -= cu * S->P[F_V][ix];
-                S->P[F_W][ix] -= cw * S->P[F_W][ix];
+                w_bc(S)[ix] -= cw * w_bc(S)[ix];
                 S->P[F_TH][ix] -= cu * S->P[F_TH][ix];
             }
     }
@@ -762,6 +771,7 @@ static void op_explicit_diffusion(ora_state *S, double step)
     diffusion_weights(order, S->zsu, NZ, w);
     double *tend = (double *)calloc((size_t)S->N, sizeof(double));
     for (int f = 0; f < nf; f++) {
+        if (f == F_W && S->c.hydrostatic) continue; /* damping.cpp:1052 */
         double *v = S->M[f];
         for (int i = 3; i < S->NX - 3; i++)
             for (int j = 3; j < S->NY - 3; j++)
@@ -1145,7 +1155,9 @@ static void kessler_points(ora_state *S)
                 long ix = IX(i, j, k);
                 const double rhou = S->rhou[k];
                 double theta = THP[ix] + THBAR[ix] + S->tb[k];
-                double pressure = PI[ix] / (cp * S->tbv[k]) + PBAR[ix];
+                /* CONVERT_PRESSURE (kessler.cpp:7-11): the hydrostatic set's pi is
+                 * already the Exner perturbation */
+                double pressure = (S->c.hydrostatic ? PI[ix] : PI[ix] / (cp * S->tbv[k])) + PBAR[ix];
                 double vapor = QVP[ix] + QBAR[ix] + S->qb[k];
                 double temperature = theta * pressure;
                 double pd = p0 * pow(pressure, cpRd);
@@ -1328,9 +1340,10 @@ static void swap_f(ora_state *S, int f)
     S->cur[f] = S->P[f];
     S->P[f] = t;
 }
-static void advance_inner(ora_state *S)
+static void advance_inner(ora_state *S) /* solver.cpp:240-248: w stays put when hydrostatic */
 {
-    for (int f = 0; f < 4; f++) swap_f(S, f);
+    for (int f = 0; f < 4; f++)
+        if (f != F_W || !S->c.hydrostatic) swap_f(S, f);
 }
 static void micro_advance_inner(ora_state *S)
 {
@@ -1338,13 +1351,181 @@ static void micro_advance_inner(ora_state *S)
 }
 static void advance_outer(ora_state *S)
 {
-    for (int f = 0; f < 4; f++) memcpy(S->M[f], S->P[f], sizeof(double) * S->N);
+    for (int f = 0; f < 4; f++)
+        if (f != F_W || !S->c.hydrostatic) memcpy(S->M[f], S->P[f], sizeof(double) * S->N);
     advance_inner(S);
 }
 static void micro_advance(ora_state *S)
 {
     for (int f = 4; f < 7; f++) memcpy(S->M[f], S->P[f], sizeof(double) * S->N);
     micro_advance_inner(S);
+}
+
+/* ------------------------------------------------------------------------
+ * Hydrostatic equation set (HYDROSTATIC): integrate_hydro (solver.cpp:33-80)
+ * with solve_hydrostatic_pressure (pressure.cpp:229-298), poisson_fft2d
+ * (:652-715), hydrostatic_pressure (:453-537) and w_velocity_LH
+ * (solver.cpp:144-163); non-periodic domains.
+ * ---------------------------------------------------------------------- */
+static double dzu(const ora_state *S, int k) { return S->zsw[k + 1] - S->zsw[k]; } /* DZU, model.h:205 */
+static double dzw(const ora_state *S, int k) { return S->zsu[k] - S->zsu[k - 1]; } /* DZW, model.h:206 */
+
+static void hyd_init(ora_state *S)
+{
+    const int NX = S->NX, NY = S->NY;
+    S->div2d = (double *)calloc((size_t)NX * NY, sizeof(double));
+    S->rhoavg = (double *)calloc((size_t)NX * NY, sizeof(double));
+    S->bco2 = (double *)calloc((size_t)NX * NY, sizeof(double));
+    S->ac2 = (double *)calloc(NY, sizeof(double));
+    S->cc2 = (double *)calloc(NY, sizeof(double));
+    S->p2 = (double *)calloc(NY + 1, sizeof(double));
+    S->q2 = (double *)calloc(NY + 1, sizeof(double));
+    S->io2d = (double *)calloc(2 * (size_t)NX * NY, sizeof(double));
+    for (long c = 0; c < (long)NX * NY; c++) { /* column_average_density, flat ground */
+        double r = 0, zsum = 0;
+        for (int k = 1; k < S->NZ - 1; k++) {
+            r = r + S->rhou[k] * S->tbv[k] * dzu(S, k);
+            zsum += dzu(S, k);
+        }
+        S->rhoavg[c] = r / zsum;
+    }
+    const double dx = S->dx, dy = S->dy;
+    for (int j = 0; j < NY; j++) S->ac2[j] = S->cc2[j] = 1. / (dy * dy);
+    S->ac2[0] = 0;
+    S->cc2[NY - 1] = 0;
+    for (int i = 0; i < NX; i++) {
+        const double kw = i < NX / 2 ? 2 * trigpi * (double)i / NX : 2 * trigpi * (double)(NX - i) / NX;
+        for (int j = 0; j < NY; j++) {
+            S->bco2[(long)i * NY + j] = 2. * (cos(kw) - 1.) / (dx * dx) - S->cc2[j] - S->ac2[j];
+            if (j == 0) S->bco2[(long)i * NY + j] = -S->rhow[2] / (dx * dx);
+        }
+    }
+}
+
+/* poisson_fft2d on div2d: FFT along i, scaled by 1/ni, a tridiagonal solve
+ * along j per wavenumber (its last row keeps the transformed value: the back
+ * substitution starts at nj-2), inverse FFT, real part */
+static void hyd_poisson2d(ora_state *S)
+{
+    const int ni = S->NX, nj = S->NY;
+    double *io = S->io2d;
+    for (long c = 0; c < (long)ni * nj; c++) {
+        io[2 * c] = S->div2d[c];
+        io[2 * c + 1] = 0;
+    }
+    for (int j = 0; j < nj; j++) ora_fft_1d(&S->fi, -1, io + 2 * j, nj, io + 2 * j, nj);
+    for (long c = 0; c < (long)ni * nj; c++) {
+        io[2 * c] = io[2 * c] / ni;
+        io[2 * c + 1] = io[2 * c + 1] / ni;
+    }
+    double *P = S->p2, *Q = S->q2;
+    for (int i = 0; i < ni; i++)
+        for (int part = 0; part < 2; part++) {
+            double *o = io + 2 * (long)i * nj + part;
+            for (int j = 0; j < nj; j++) {
+                const double denom = S->bco2[(long)i * nj + j] + S->ac2[j] * P[j];
+                P[j + 1] = -S->cc2[j] / denom;
+                Q[j + 1] = (o[2 * j] - S->ac2[j] * Q[j]) / denom;
+            }
+            for (int j = nj - 2; j >= 0; j--) o[2 * j] = P[j + 1] * o[2 * (j + 1)] + Q[j + 1];
+        }
+    for (int j = 0; j < nj; j++) ora_fft_1d(&S->fi, +1, io + 2 * j, nj, io + 2 * j, nj);
+    for (long c = 0; c < (long)ni * nj; c++) S->div2d[c] = io[2 * c];
+}
+
+static void op_solve_hydrostatic(ora_state *S, double step)
+{
+    const int NX = S->NX, NY = S->NY, NZ = S->NZ;
+    const double *UP = S->P[F_U], *VP = S->P[F_V], *TH = S->cur[F_TH];
+    double *PI = S->pi, *D = S->div2d;
+    mirror(S, S->P[F_U]);
+    mirror(S, S->P[F_V]);
+    for (int i = 1; i < NX - 1; i++) /* density-weighted column divergence */
+        for (int j = 1; j < NY - 1; j++) {
+            const long c = IX2(i, j);
+            double zsum = 0;
+            D[c] = 0;
+            for (int k = 1; k < NZ - 1; k++) {
+                D[c] += S->rhou[k] * dzu(S, k) *
+                        ((UP[IX(i + 1, j, k)] - UP[IX(i, j, k)]) * S->one_d_dx +
+                         (VP[IX(i, j + 1, k)] - VP[IX(i, j, k)]) * S->one_d_dy);
+                zsum += dzu(S, k);
+            }
+            D[c] /= (cp * zsum * step * S->dt);
+        }
+    for (int j = 0; j < NY; j++) { /* mirror_boundaries_2d (boundaries.cpp:331-345) */
+        D[IX2(0, j)] = D[IX2(1, j)];
+        D[IX2(NX - 1, j)] = D[IX2(NX - 2, j)];
+    }
+    for (int i = 0; i < NX; i++) {
+        D[IX2(i, 0)] = D[IX2(i, 1)];
+        D[IX2(i, NY - 1)] = D[IX2(i, NY - 2)];
+    }
+    hyd_poisson2d(S);
+    const int moist = S->c.microphysics_option != 0;
+    const double *QV = S->cur[F_QV], *QC = S->cur[F_QC], *QR = S->cur[F_QR], *tbv = S->tbv;
+    for (int i = 1; i < NX - 1; i++) /* hydrostatic_pressure(1,NX-1,1,NY-1) */
+        for (int j = 1; j < NY - 1; j++) {
+            long a = IX(i, j, NZ - 2);
+            PI[IX(i, j, NZ - 1)] = 0;
+            const double m0 = moist ? (1. + 0.61 * QV[a] - QC[a] - QR[a]) : 1;
+            PI[a] = -0.5 * (grav / cp) * ((TH[a] * m0) / (tbv[NZ - 2] * tbv[NZ - 2])) * dzw(S, NZ - 1);
+            for (int k = NZ - 3; k > 0; k--) {
+                const long u = IX(i, j, k + 1), d = IX(i, j, k);
+                const double mu_ = moist ? (1. + 0.61 * QV[u] - QC[u] - QR[u]) : 1;
+                const double md = moist ? (1. + 0.61 * QV[d] - QC[d] - QR[d]) : 1;
+                const double tup = (TH[u] * mu_) / (tbv[k + 1] * tbv[k + 1]);
+                const double tdn = (TH[d] * md) / (tbv[k] * tbv[k]);
+                PI[d] = PI[u] - 0.5 * (grav / cp) * (tup + tdn) * dzw(S, k + 1);
+            }
+            double zsum = 0;
+            PI[IX(i, j, 0)] = 0;
+            for (int k = 1; k < NZ - 1; k++) {
+                PI[IX(i, j, 0)] += S->rhou[k] * tbv[k] * PI[IX(i, j, k)] * dzu(S, k);
+                zsum += dzu(S, k);
+            }
+            PI[IX(i, j, 0)] /= zsum;
+        }
+    for (int i = 1; i < NX - 1; i++) /* lid pressure */
+        for (int j = 1; j < NY - 1; j++)
+            PI[IX(i, j, NZ - 1)] = (D[IX2(i, j)] - PI[IX(i, j, 0)]) / S->rhoavg[IX2(i, j)];
+    for (int i = 0; i < NX; i++)
+        for (int j = 0; j < NY; j++)
+            for (int k = 1; k < NZ - 1; k++) PI[IX(i, j, k)] += PI[IX(i, j, NZ - 1)];
+    mirror(S, PI);
+}
+
+/* w_velocity_LH (solver.cpp:144-163): w of the current slot from the
+ * anelastic continuity equation and the forecast u, v */
+static void hyd_w(ora_state *S)
+{
+    double *W = S->cur[F_W];
+    const double *UP = S->P[F_U], *VP = S->P[F_V];
+    for (int i = 1; i < S->NX - 1; i++)
+        for (int j = 1; j < S->NY - 1; j++) {
+            W[IX(i, j, 0)] = 0;
+            W[IX(i, j, 1)] = 0;
+            W[IX(i, j, S->NZ - 1)] = 0;
+            for (int k = 2; k < S->NZ - 1; k++)
+                W[IX(i, j, k)] = (S->rhow[k - 1] / S->rhow[k]) * W[IX(i, j, k - 1)] +
+                                 (S->rhou[k - 1] / S->rhow[k]) *
+                                     (-(UP[IX(i + 1, j, k - 1)] - UP[IX(i, j, k - 1)]) * S->one_d_dx -
+                                      (VP[IX(i, j + 1, k - 1)] - VP[IX(i, j, k - 1)]) * S->one_d_dy) *
+                                     S->dz / S->mu[k - 1];
+        }
+}
+
+static void integrate_hydro(ora_state *S, double step) /* solver.cpp:33-80 */
+{
+    op_advect_uvw(S, step); /* u and v only */
+    op_solve_hydrostatic(S, step);
+    for (int i = 1; i < S->NX - 1; i++)
+        for (int j = 1; j < S->NY - 1; j++)
+            for (int k = 1; k < S->NZ - 1; k++) {
+                const long c = IX(i, j, k);
+                S->P[F_U][c] -= step * (S->dtx * cp * S->tbv[k] * (S->pi[c] - S->pi[IX(i - 1, j, k)]));
+                S->P[F_V][c] -= step * (S->dty * cp * S->tbv[k] * (S->pi[c] - S->pi[IX(i, j - 1, k)]));
+            }
 }
 
 static void integrate_non_hydro(ora_state *S, double step) /* solver.cpp:87-138 */
@@ -1363,7 +1544,8 @@ static void rk3_step(ora_state *S) /* driver_serial.cpp:178-286 */
     if (S->c.use_explicit_diffusion) op_explicit_diffusion(S, 1.0);
     if (turb) op_turbulence(S);
     for (int s = 0; s < 3; s++) {
-        integrate_non_hydro(S, steps[s]);
+        if (S->c.hydrostatic) integrate_hydro(S, steps[s]);
+        else integrate_non_hydro(S, steps[s]);
         op_advect_theta(S, steps[s]);
         if (turb) turb_apply_theta(S, steps[s]);
         if (micro) {
@@ -1371,6 +1553,7 @@ static void rk3_step(ora_state *S) /* driver_serial.cpp:178-286 */
             if (turb) turb_apply_moisture(S, steps[s]);
             op_zero_moisture(S);
         }
+        if (S->c.hydrostatic) hyd_w(S); /* driver_serial.cpp:239 */
         op_bc(S);
         if (micro) {
             op_bc_micro(S);
@@ -1623,6 +1806,7 @@ ora_state *ora_create(const ga_config *cfg, const ga_columns *cols)
     S->qd = (double *)calloc(NZ, sizeof(double));
     S->ve = (double *)calloc(NZ, sizeof(double));
     if (cfg->turbulence_option) turb_init(S);
+    if (cfg->hydrostatic) hyd_init(S);
     return S;
 }
 
@@ -1647,6 +1831,8 @@ void ora_destroy(ora_state *S)
     free(S->kmix); free(S->khmix);
     for (int t = 0; t < 7; t++) free(S->ttend[t]);
     free(S->sat); free(S->l2); free(S->kvmax);
+    free(S->div2d); free(S->rhoavg); free(S->bco2); free(S->ac2); free(S->cc2); free(S->p2); free(S->q2);
+    free(S->io2d);
     free(S);
 }
 
@@ -1706,9 +1892,15 @@ int ora_op(ora_state *S, int op, double step)
     switch (op) {
     case GA_OP_SIGN_CELLS: return GA_OK;
     case GA_OP_ADVECT_UVW: op_advect_uvw(S, step); return GA_OK;
-    case GA_OP_SOLVE_PRESSURE: op_solve_pressure(S, step); return GA_OK;
+    case GA_OP_SOLVE_PRESSURE:
+        if (S->c.hydrostatic) op_solve_hydrostatic(S, step);
+        else op_solve_pressure(S, step);
+        return GA_OK;
     case GA_OP_PROJECT: op_project(S, step); return GA_OK;
-    case GA_OP_INTEGRATE_NON_HYDRO: integrate_non_hydro(S, step); return GA_OK;
+    case GA_OP_INTEGRATE_NON_HYDRO:
+        if (S->c.hydrostatic) integrate_hydro(S, step);
+        else integrate_non_hydro(S, step);
+        return GA_OK;
     case GA_OP_ADVECT_THETA: op_advect_theta(S, step); return GA_OK;
     case GA_OP_ADVECT_MICRO:
         if (S->c.linear_model) op_advect_qv(S, step);

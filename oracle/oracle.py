@@ -25,6 +25,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle.so")
 REF_HARNESS = os.path.join(HERE, "_ref", "ref_harness")
 REF_HARNESS_LIN = os.path.join(HERE, "_ref", "ref_harness_lin")  # the ISLINEAR build
+REF_HARNESS_HYD = os.path.join(HERE, "_ref", "ref_harness_hyd")  # the HYDROSTATIC build
 
 _lib = None
 _DP = C.POINTER(C.c_double)
@@ -239,7 +240,9 @@ def run_reference(workload, mode: str = "run", nsteps: int = 1, op: str = "", st
     with tempfile.TemporaryDirectory() as td:
         fin, fout = os.path.join(td, "in.bin"), os.path.join(td, "out.bin")
         write_bundle(fin, workload_bundle(workload, extra))
-        args = [REF_HARNESS_LIN if getattr(workload, "linear_model", 0) else REF_HARNESS, fin, fout, mode]
+        exe = REF_HARNESS_LIN if getattr(workload, "linear_model", 0) else \
+            REF_HARNESS_HYD if getattr(workload, "hydrostatic", 0) else REF_HARNESS
+        args = [exe, fin, fout, mode]
         args += [str(nsteps)] if mode == "run" else [op, repr(step)]
         subprocess.run(args, check=True, stdout=subprocess.DEVNULL)
         return read_bundle(fout)

@@ -37,6 +37,8 @@
 void s_integrate_rk3();
 void linear_integrate_rk3();
 void advect_qv(double, int, int, int, int);
+void advect_uv_velocity(double, int, int, int, int);
+void integrate_hydro(double, int, int, int, int, int);
 extern double *Kmix, *KHmix;  /* turbulence.cpp: mixing coefficients */
 extern bool *isSaturated;     /* turbulence.cpp: Kessler saturation record */
 void zero_moisture(int il, int ih, int jl, int jh, int size);
@@ -233,6 +235,8 @@ int main(int argc, char **argv)
         else if (name == "advect_theta") advect_theta(step, 3, NX - 3, 3, NY - 3);
         else if (name == "advect_micro") advect_microphysics_cell(step, 3, NX - 3, 3, NY - 3);
         else if (name == "advect_qv") advect_qv(step, 3, NX - 3, 3, NY - 3);
+        else if (name == "advect_uv") advect_uv_velocity(step, 3, NX - 3, 3, NY - 3);
+        else if (name == "integrate_hydro") integrate_hydro(step, 0, 0, NX, 0, NY);
         else if (name == "zero_moisture") zero_moisture(1, NX - 1, 1, NY - 1, (int)N);
         else if (name == "bc") apply_boundary_condition(0);
         else if (name == "bc_micro") apply_boundary_condition_microphysics(0);

@@ -24,7 +24,7 @@ def workload(d: dict) -> configs.Workload:
     kw = {k: int(d[k]) for k in _INT_KEYS}
     kw.update({k: float(d[k]) for k in _FLOAT_KEYS})
     for k in ("use_explicit_diffusion", "diffusion_order", "turbulence_option",
-              "use_surface_heat_flux", "linear_model"):  # optional: fixtures with these physics
+              "use_surface_heat_flux", "linear_model", "hydrostatic"):  # optional: fixtures with these physics
         if k in d:
             kw[k] = int(d[k])
     for k in ("kdiffh", "kdiffv", "water_temp"):
@@ -55,6 +55,10 @@ def ops_names():
 
 def linop_names():
     return sorted(f[:-4] for f in os.listdir(GOLDEN) if f.startswith("linop_") and f.endswith(".npz"))
+
+
+def hydop_names():
+    return sorted(f[:-4] for f in os.listdir(GOLDEN) if f.startswith("hydop_") and f.endswith(".npz"))
 
 
 def turb_names():

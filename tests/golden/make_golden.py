@@ -48,6 +48,11 @@ def _linear(wl, bigcounter0=0):
     return wl
 
 
+def _hydro(wl):
+    wl.hydrostatic = 1
+    return wl
+
+
 def _jet(moist):
     return configs.jet_vortex(nx=16, ny=14, nz=10, dx=20000.0, dz=800.0, dt=30.0, rmax=60000.0, vmax=8.0,
                               moist=moist, noise=0.3, extra_basic=1.0)
@@ -80,6 +85,12 @@ RUN_CASES = {
     "linear_moist": (lambda: _linear(_jet(True)), 4),
     "linear_diffusion": (lambda: _linear(_diffusing(_jet(True), 4, 0.004)), 3),
     "linear_rescale": (lambda: _linear(_jet(False), bigcounter0=1438), 4),
+    # the hydrostatic equation set (integrate_hydro, w diagnosed)
+    "hydro_dry": (lambda: _hydro(configs.dry_bubble(nx=16, ny=14, nz=10, dx=2000.0, dz=500.0, dt=4.0, amp=3.0,
+                                                    radius=6000.0, zc=1500.0, noise=0.2)), 4),
+    "hydro_moist": (lambda: _hydro(configs.moist_blob(nx=15, ny=14, nz=10, dx=2000.0)), 4),
+    "hydro_jet": (lambda: _hydro(_jet(True)), 3),
+    "hydro_diffusion": (lambda: _hydro(_diffusing(configs.moist_blob(nx=16, ny=14, nz=12, dx=2000.0), 4, 0.004)), 3),
 }
 
 OP_NAMES = ["advect_uvw", "solve_pressure", "integrate_non_hydro", "advect_theta",
@@ -203,6 +214,9 @@ def make_turb():
         print("wrote", path, os.path.getsize(path))
 
 
+HYDRO_OPS = {"advect_uvw": "advect_uv", "solve_pressure": "solve_pressure", "integrate_non_hydro": "integrate_hydro",
+             "kessler": "kessler", "bc": "bc", "rayleigh": "rayleigh"}
+
 LINEAR_OPS = {"advect_uvw": "advect_uvw", "advect_theta": "advect_theta", "advect_micro": "advect_qv",
               "integrate_non_hydro": "integrate_non_hydro"}
 
@@ -210,13 +224,19 @@ LINEAR_OPS = {"advect_uvw": "advect_uvw", "advect_theta": "advect_theta", "advec
 def make_linear_ops():
     """linop_<case>.npz: the linearised operators (the ISLINEAR build) on a
     state whose rotation slots differ; the moisture operator of the
-    linearised model is advect_qv"""
-    for cname, wl in {"jet": _linear(_jet(True))}.items():
+    linearised model is advect_qv.  hydop_<case>.npz: the operators of the
+    hydrostatic set (the HYDROSTATIC build)"""
+    _variant_ops("linop", {"jet": _linear(_jet(True))}, LINEAR_OPS)
+    _variant_ops("hydop", {"moist": _hydro(configs.moist_blob(nx=15, ny=14, nz=10, dx=2000.0))}, HYDRO_OPS)
+
+
+def _variant_ops(prefix, cases, ops):
+    for cname, wl in cases.items():
         extra = _ops_state(wl, 9000)
         d = _inputs(wl)
         for k, v in extra.items():
             d["in_" + k] = v.ravel()
-        for op, ref_op in LINEAR_OPS.items():
+        for op, ref_op in ops.items():
             st = 0.5
             out = O.run_reference(wl, "op", op=ref_op, step=st, extra=extra)
             d[f"step_{op}"] = np.float64(st)
@@ -227,7 +247,7 @@ def make_linear_ops():
                 if ref_in is not None and np.array_equal(np.asarray(ref_in).ravel(), v):
                     continue
                 d[f"{op}__{k}"] = v
-        path = os.path.join(HERE, f"linop_{cname}.npz")
+        path = os.path.join(HERE, f"{prefix}_{cname}.npz")
         np.savez_compressed(path, **d)
         print("wrote", path, os.path.getsize(path))
 

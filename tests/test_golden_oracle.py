@@ -107,3 +107,26 @@ def test_linear_operator_bit_exact(name, op):
         key = k.split("__", 1)[1]
         f, slot = fx.FIELD_OF[key]
         np.testing.assert_array_equal(o.get(f, slot), d[k], err_msg=f"{op}:{key}")
+
+
+@pytest.mark.parametrize("name", fx.hydop_names())
+@pytest.mark.parametrize("op", ["advect_uvw", "solve_pressure", "integrate_non_hydro", "kessler", "bc", "rayleigh"])
+def test_hydrostatic_operator_bit_exact(name, op):
+    """the operators of the hydrostatic set against the reference's
+    HYDROSTATIC build (advect_uvw is advect_uv_velocity, integrate_non_hydro
+    integrate_hydro; the boundary conditions and damping act on the current
+    w)"""
+    d = fx.load(name)
+    wl = fx.workload(d)
+    assert wl.hydrostatic
+    o = O.Oracle(wl)
+    for k, v in fx.slot_extra(d).items():
+        f, slot = fx.FIELD_OF[k]
+        o.set(f, slot, v)
+    assert o.op(op, float(d[f"step_{op}"])) == 0
+    outs = [k for k in d if k.startswith(op + "__")]
+    assert outs
+    for k in outs:
+        key = k.split("__", 1)[1]
+        f, slot = fx.FIELD_OF[key]
+        np.testing.assert_array_equal(o.get(f, slot), d[k], err_msg=f"{op}:{key}")
