@@ -481,6 +481,52 @@ def physics_bench(torch, device, steps, accuracy_steps):
     return out
 
 
+def variants_bench(torch, device, steps, accuracy_steps):
+    """The reference's other equation sets: the linearised model about the
+    C3 jet basic state (192x128x32, dt = 120 s) and the hydrostatic set on
+    the C2 thunderstorm at dx = 2 km; FP32 and FP64 ms/step (tuned FP32,
+    L2 written over between steps) and the FP32 error after accuracy_steps."""
+    from model_gb300 import abi, anelastic, configs
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{device}")
+    cases = {"linear_model": (lambda: configs.jet_vortex(noise=0.3, extra_basic=1.0), {"linear_model": 1},
+                              "linearised model about the 192x128x32 jet, dt=120 s"),
+             "hydrostatic": (lambda: configs.thunderstorm(dx=2000.0), {"hydrostatic": 1},
+                             "hydrostatic set, Kessler thunderstorm 128x128x48, dx=dy=2 km, dt=4 s")}
+    out = {"steps": steps}
+    for name, (mk, kw, desc) in cases.items():
+        wl = mk()
+        for k, v in kw.items():
+            setattr(wl, k, v)
+        r = {"workload": desc}
+        for prec, tag in ((abi.GA_PREC_F32, "fp32"), (abi.GA_PREC_F64, "fp64")):
+            m = anelastic.Model(wl, prec, device=device)
+            if prec == abi.GA_PREC_F32:
+                m.tune()
+            for _ in range(3):
+                m.step(1)
+            n = steps if prec == abi.GA_PREC_F32 else max(2, steps // 4)
+            per = time_steps(m, torch, n, flush)
+            ms = sum(per) / n
+            r[tag] = {"ms_per_step": round(ms, 4), "value": round(wl.points / (ms * 1e-3), 1), "unit": UNIT}
+            m.close()
+        r["fp32_over_fp64"] = round(r["fp64"]["ms_per_step"] / r["fp32"]["ms_per_step"], 2)
+        if accuracy_steps > 0:
+            a = anelastic.Model(wl, abi.GA_PREC_F32, device=device)
+            b = anelastic.Model(wl, abi.GA_PREC_F64, device=device)
+            a.step(accuracy_steps)
+            b.step(accuracy_steps)
+            nf = 7 if wl.microphysics_option else 4
+            errs = {abi.PROG_NAMES[f]: float(np.linalg.norm(a.get(f) - b.get(f)) /
+                                             max(np.linalg.norm(b.get(f)), 1e-300)) for f in range(nf)}
+            r["accuracy"] = {"steps": accuracy_steps,
+                             "rel_l2_fp32_vs_fp64": {k: float(f"{v:.4g}") for k, v in errs.items()},
+                             "max": float(f"{max(errs.values()):.4g}")}
+            a.close()
+            b.close()
+        out[name] = r
+    return out
+
+
 def cpu_baseline(wl, steps):
     """The reference's CPU step (oracle restatement, 1 core) on a bounded
     sample of the same workload."""
@@ -634,6 +680,8 @@ def run_ours(args):
                                               moist=True, size=args.adjoint_moist_size)
     if args.physics_steps > 0:
         line["physics"] = physics_bench(torch, device, args.physics_steps, args.physics_accuracy_steps)
+    if args.variant_steps > 0:
+        line["variants"] = variants_bench(torch, device, args.variant_steps, args.variant_accuracy_steps)
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(wl, args.cpu_steps)
     print(json.dumps(line), flush=True)
@@ -688,6 +736,9 @@ def main():
     ap.add_argument("--physics-steps", type=int, default=20,
                     help="timed steps of each optional-physics variant (0: skip)")
     ap.add_argument("--physics-accuracy-steps", type=int, default=600)
+    ap.add_argument("--variant-steps", type=int, default=20,
+                    help="timed steps of the linearised and hydrostatic sets (0: skip)")
+    ap.add_argument("--variant-accuracy-steps", type=int, default=100)
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()

@@ -338,19 +338,25 @@ class Engine : public EngineBase {
             }
             hyd.rhoavg = (T)(r / zsum);
             hyd.dz = (T)dz;
-            std::vector<double> ac(NY, 1. / (dy * dy)), cc(NY, 1. / (dy * dy)), bco((size_t)NX * NY);
+            std::vector<double> ac(NY, 1. / (dy * dy)), cc(NY, 1. / (dy * dy));
+            std::vector<double> pf((size_t)NX * (NY + 1), 0.0), rden((size_t)NX * NY);
             ac[0] = 0;
             cc[NY - 1] = 0;
             for (int i = 0; i < NX; i++) {
                 const double kw = i < NX / 2 ? 2 * trigpi * (double)i / NX : 2 * trigpi * (double)(NX - i) / NX;
-                for (int j = 0; j < NY; j++)
-                    bco[(size_t)i * NY + j] = j == 0 ? -cols->rhow[2] / (dx * dx)
-                                                     : 2. * (cos(kw) - 1.) / (dx * dx) - cc[j] - ac[j];
+                double *P = pf.data() + (size_t)i * (NY + 1);
+                for (int j = 0; j < NY; j++) {
+                    const double b = j == 0 ? -cols->rhow[2] / (dx * dx)
+                                            : 2. * (cos(kw) - 1.) / (dx * dx) - cc[j] - ac[j];
+                    const double denom = b + ac[j] * P[j];
+                    P[j + 1] = -cc[j] / denom;
+                    rden[(size_t)i * NY + j] = 1.0 / denom;
+                }
             }
-            hyd.bco = upload(bco);
+            hyd.pf = upload(pf);
+            hyd.rden = upload(rden);
             hyd.ac = upload(ac);
-            hyd.cc = upload(cc);
-            hyd.pw = dalloc<double>((size_t)NX * 3 * (NY + 1));
+            hyd.pw = dalloc<double>((size_t)NX * 2 * (NY + 1));
             hyd.div = dalloc<T>((size_t)NX * NY);
             hyd.spec2 = dalloc<T2>((size_t)NX * NY);
             hyd_L = (int)std::max<size_t>(1, std::min<size_t>(8, 49152 / (2 * (size_t)NX * sizeof(T2))));
@@ -881,14 +887,15 @@ class Engine : public EngineBase {
         const long e3 = 2L * (NX + NY - 2) * (NZ - 2);
         k_mirror_edges<T><<<cdiv(e3, 256), 256, 0, stream>>>(kp, F.P[FU], F.P[FV], F.P[FV]);
         const long ncol = (long)(NX - 2) * (NY - 2);
-        k_hyd_divavg<T><<<cdiv(ncol, 256), 256, 0, stream>>>(kp, F, hyd, (T)step);
+        const size_t hs = hyd_col_smem<T>(NZ);
+        k_hyd_divavg<T><<<cdiv(ncol, HC), HC_THREADS, hs, stream>>>(kp, F, hyd, (T)step);
         k_hyd_mirror2d<T><<<cdiv(2L * (NX + NY - 2), 256), 256, 0, stream>>>(kp, hyd.div);
         const size_t sm = 2 * (size_t)NX * hyd_L * sizeof(T2);
         const dim3 fb(hyd_L, std::max(1, 256 / hyd_L));
         k_hyd_fft<T><<<cdiv(NY, hyd_L), fb, sm, stream>>>(kp, hyd, plan_i, tw_i, 0, hyd_L);
         k_hyd_thomas<T><<<cdiv(NX, 64), 64, 0, stream>>>(kp, hyd);
         k_hyd_fft<T><<<cdiv(NY, hyd_L), fb, sm, stream>>>(kp, hyd, plan_i, tw_i, 1, hyd_L);
-        k_hyd_pi<T><<<cdiv(ncol, 128), 128, 0, stream>>>(kp, F, hyd);
+        k_hyd_pi<T><<<cdiv(ncol, HC), HC_THREADS, hs, stream>>>(kp, F, hyd);
         k_mirror_edges<T><<<cdiv(e3, 256), 256, 0, stream>>>(kp, pi, pi, pi);
         launches += 8;
     }
@@ -901,7 +908,7 @@ class Engine : public EngineBase {
     void hyd_w()
     {
         const long ncol = (long)(NX - 2) * (NY - 2);
-        k_hyd_w<T><<<cdiv(ncol, 128), 128, 0, stream>>>(kp, fields(), hyd);
+        k_hyd_w<T><<<cdiv(ncol, HC), HC_THREADS, hyd_col_smem<T>(NZ), stream>>>(kp, fields(), hyd);
         launches++;
     }
 

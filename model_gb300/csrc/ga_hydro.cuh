@@ -21,29 +21,57 @@ namespace ga {
 template <typename T>
 struct HydArgs {
     const T *dzu, *dzw;    // DZU(k) = zsw[k+1]-zsw[k], DZW(k) = zsu[k]-zsu[k-1] (model.h:205-206)
-    const double *bco;     // BCOEF(i, j) of init_fft2d (pressure.cpp:634-641), [nx][ny]
-    const double *ac, *cc; // acoef, ccoef [ny]
-    double *pw;            // tridiagonal work, [nx][ny+1] (P; real and imaginary Q follow)
+    // the tridiagonal system of init_fft2d (pressure.cpp:621-641) does not
+    // change during a run: its elimination factors P[j+1] = -ccoef[j]/denom
+    // and 1/denom, denom = BCOEF(i,j) + acoef[j] P[j], are formed once on the
+    // host (the reference's expressions, FP64), [nx][ny+1] and [nx][ny]
+    const double *pf, *rden;
+    const double *ac;      // acoef [ny]
+    double *pw;            // work of the back substitution, [nx][2 (ny+1)] (real and imaginary Q)
     T *div;                // div_avg, [nx][ny]
     typename V2<T>::t *spec2;  // transformed div_avg, [nx][ny]
     T rhoavg;              // column-average density (column_average_density, initializer.cpp:1265-1282)
     T dz;
 };
 
+// The column kernels below hold HC columns per block with their levels in
+// shared memory: the pointwise parts of each recurrence are formed by all
+// threads with loads coalesced along k, then one thread per column runs the
+// recurrence in the reference's order from shared memory.
+constexpr int HC = 16, HC_THREADS = 128;
+
+template <typename T>
+__host__ __device__ constexpr size_t hyd_col_smem(int nz)
+{
+    return 2 * (size_t)HC * nz * sizeof(T);
+}
+
 // density-weighted column divergence of the forecast u, v (pressure.cpp:248-261)
 template <typename T>
-__global__ void __launch_bounds__(256) k_hyd_divavg(KParams<T> p, KFields<T> F, HydArgs<T> h, T step)
+__global__ void __launch_bounds__(HC_THREADS) k_hyd_divavg(KParams<T> p, KFields<T> F, HydArgs<T> h, T step)
 {
-    const int nyi = p.ny - 2;
-    const long col = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (col >= (long)(p.nx - 2) * nyi) return;
-    const int i = 1 + (int)(col / nyi), j = 1 + (int)(col % nyi);
+    extern __shared__ unsigned char hyd_smem[];
+    T *term = (T *)hyd_smem;  // [HC][nz]
+    const int nyi = p.ny - 2, nz = p.nz;
+    const long ncol = (long)(p.nx - 2) * nyi, col0 = (long)blockIdx.x * HC;
     const T *UP = F.P[FU], *VP = F.P[FV];
-    const long sx = (long)p.ny * p.nz, sy = p.nz;
+    const long sx = (long)p.ny * nz, sy = nz;
+    for (int w = threadIdx.x; w < HC * nz; w += blockDim.x) {
+        const int cl = w / nz, k = w % nz;
+        const long col = col0 + cl;
+        if (col >= ncol || k < 1 || k >= nz - 1) continue;
+        const int i = 1 + (int)(col / nyi), j = 1 + (int)(col % nyi);
+        const long c = gix(p.ny, nz, i, j, k);
+        term[cl * nz + k] =
+            p.rhou[k] * h.dzu[k] * ((UP[c + sx] - UP[c]) * p.one_d_dx + (VP[c + sy] - VP[c]) * p.one_d_dy);
+    }
+    __syncthreads();
+    const long col = col0 + threadIdx.x;
+    if (threadIdx.x >= HC || col >= ncol) return;
+    const int i = 1 + (int)(col / nyi), j = 1 + (int)(col % nyi);
     T d = T(0), zsum = T(0);
-    for (int k = 1; k < p.nz - 1; k++) {
-        const long c = gix(p.ny, p.nz, i, j, k);
-        d += p.rhou[k] * h.dzu[k] * ((UP[c + sx] - UP[c]) * p.one_d_dx + (VP[c + sy] - VP[c]) * p.one_d_dy);
+    for (int k = 1; k < nz - 1; k++) {
+        d += term[threadIdx.x * nz + k];
         zsum += h.dzu[k];
     }
     d /= (T(1004) * zsum * step * p.dt);
@@ -113,7 +141,10 @@ __global__ void k_hyd_fft(KParams<T> p, HydArgs<T> h, FftPlan P, const typename 
 }
 
 // the tridiagonal solve along y of one x-wavenumber (pressure.cpp:675-700),
-// real and imaginary parts with the same P; in FP64
+// real and imaginary parts, in FP64 with the precomputed factors: each step
+// of the recurrence is a multiply-subtract and a multiply by 1/denom (the
+// reference divides by denom; the two differ by an ulp, well inside the
+// transform's own rounding)
 template <typename T>
 __global__ void k_hyd_thomas(KParams<T> p, HydArgs<T> h)
 {
@@ -121,19 +152,27 @@ __global__ void k_hyd_thomas(KParams<T> p, HydArgs<T> h)
     if (i >= p.nx) return;
     typedef typename V2<T>::t T2;
     const int nj = p.ny;
-    double *P = h.pw + (long)i * 3 * (nj + 1), *Qr = P + (nj + 1), *Qi = Qr + (nj + 1);
-    T2 *x = h.spec2 + (long)i * nj;
-    const double *B = h.bco + (long)i * nj;
-    P[0] = 0.0;
-    Qr[0] = 0.0;
-    Qi[0] = 0.0;
+    // distinct arrays: the loads of later rows may be issued before the
+    // stores of earlier ones
+    double *__restrict__ Qr = h.pw + (long)i * 2 * (nj + 1);
+    double *__restrict__ Qi = Qr + (nj + 1);
+    const double *__restrict__ P = h.pf + (long)i * (nj + 1);
+    const double *__restrict__ R = h.rden + (long)i * nj;
+    const double *__restrict__ ac = h.ac;
+    T2 *__restrict__ x = h.spec2 + (long)i * nj;
+    double qr = 0.0, qi = 0.0;
+    // unrolled so that the loads of a batch of rows are issued ahead of the
+    // dependent chain
+#pragma unroll 16
     for (int j = 0; j < nj; j++) {
-        const double denom = B[j] + h.ac[j] * P[j];
-        P[j + 1] = -h.cc[j] / denom;
-        Qr[j + 1] = ((double)x[j].x - h.ac[j] * Qr[j]) / denom;
-        Qi[j + 1] = ((double)x[j].y - h.ac[j] * Qi[j]) / denom;
+        const T2 v = x[j];
+        qr = ((double)v.x - ac[j] * qr) * R[j];
+        qi = ((double)v.y - ac[j] * qi) * R[j];
+        Qr[j + 1] = qr;
+        Qi[j + 1] = qi;
     }
     double xr = (double)x[nj - 1].x, xi = (double)x[nj - 1].y;
+#pragma unroll 16
     for (int j = nj - 2; j >= 0; j--) {
         xr = P[j + 1] * xr + Qr[j + 1];
         xi = P[j + 1] * xi + Qi[j + 1];
@@ -144,41 +183,57 @@ __global__ void k_hyd_thomas(KParams<T> p, HydArgs<T> h)
 
 // hydrostatic_pressure (pressure.cpp:453-537) from the current theta (and
 // moisture), its density-weighted column average into level 0, the lid
-// pressure (:285-286) into level NZ-1, and the total (:293-296); one thread
-// per interior column
+// pressure (:285-286) into level NZ-1, and the total (:293-296)
 template <typename T>
-__global__ void __launch_bounds__(128) k_hyd_pi(KParams<T> p, KFields<T> F, HydArgs<T> h)
+__global__ void __launch_bounds__(HC_THREADS) k_hyd_pi(KParams<T> p, KFields<T> F, HydArgs<T> h)
 {
+    extern __shared__ unsigned char hyd_smem[];
     const int nyi = p.ny - 2, nz = p.nz;
-    const long col = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (col >= (long)(p.nx - 2) * nyi) return;
-    const int i = 1 + (int)(col / nyi), j = 1 + (int)(col % nyi);
-    const long c0 = gix(p.ny, nz, i, j, 0);
+    T *g = (T *)hyd_smem;   // [HC][nz]: theta (times the water loading) / tbv^2
+    T *ps = g + HC * nz;    // [HC][nz]: the integral, then the total
+    const long ncol = (long)(p.nx - 2) * nyi, col0 = (long)blockIdx.x * HC;
     const T *TH = F.cur[FTH], *QV = F.cur[FQV], *QC = F.cur[FQC], *QR = F.cur[FQR];
     T *PI = F.pi;
+    for (int w = threadIdx.x; w < HC * nz; w += blockDim.x) {
+        const int cl = w / nz, k = w % nz;
+        const long col = col0 + cl;
+        if (col >= ncol || k < 1 || k >= nz - 1) continue;
+        const long c = gix(p.ny, nz, 1 + (int)(col / nyi), 1 + (int)(col % nyi), k);
+        const T fac = p.moist ? (T(1.) + T(0.61) * QV[c] - QC[c] - QR[c]) : T(1);
+        g[cl * nz + k] = (TH[c] * fac) / (p.tbv[k] * p.tbv[k]);
+    }
+    __syncthreads();
     const T gcp = T(9.8 / 1004.0);
-    auto fac = [&](int k) {
-        return p.moist ? (T(1.) + T(0.61) * QV[c0 + k] - QC[c0 + k] - QR[c0 + k]) : T(1);
-    };
-    PI[c0 + nz - 1] = T(0);
-    T up = -T(0.5) * gcp * ((TH[c0 + nz - 2] * fac(nz - 2)) / (p.tbv[nz - 2] * p.tbv[nz - 2])) * h.dzw[nz - 1];
-    PI[c0 + nz - 2] = up;
-    for (int k = nz - 3; k > 0; k--) {
-        const T tup = (TH[c0 + k + 1] * fac(k + 1)) / (p.tbv[k + 1] * p.tbv[k + 1]);
-        const T tdn = (TH[c0 + k] * fac(k)) / (p.tbv[k] * p.tbv[k]);
-        up = up - T(0.5) * gcp * (tup + tdn) * h.dzw[k + 1];
-        PI[c0 + k] = up;
+    const int cl = threadIdx.x;
+    const long col = col0 + cl;
+    if (cl < HC && col < ncol) {
+        const int i = 1 + (int)(col / nyi), j = 1 + (int)(col % nyi);
+        const T *gc = g + cl * nz;
+        T *pc = ps + cl * nz;
+        T up = -T(0.5) * gcp * gc[nz - 2] * h.dzw[nz - 1];
+        pc[nz - 2] = up;
+        for (int k = nz - 3; k > 0; k--) {
+            up = up - T(0.5) * gcp * (gc[k + 1] + gc[k]) * h.dzw[k + 1];
+            pc[k] = up;
+        }
+        T avg = T(0), zsum = T(0);
+        for (int k = 1; k < nz - 1; k++) {
+            avg += p.rhou[k] * p.tbv[k] * pc[k] * h.dzu[k];
+            zsum += h.dzu[k];
+        }
+        avg /= zsum;
+        pc[0] = avg;
+        pc[nz - 1] = (h.div[(long)i * p.ny + j] - avg) / h.rhoavg;
     }
-    T avg = T(0), zsum = T(0);
-    for (int k = 1; k < nz - 1; k++) {
-        avg += p.rhou[k] * p.tbv[k] * PI[c0 + k] * h.dzu[k];
-        zsum += h.dzu[k];
+    __syncthreads();
+    for (int w = threadIdx.x; w < HC * nz; w += blockDim.x) {
+        const int c2 = w / nz, k = w % nz;
+        const long cc = col0 + c2;
+        if (cc >= ncol) continue;
+        const long c = gix(p.ny, nz, 1 + (int)(cc / nyi), 1 + (int)(cc % nyi), k);
+        const T *pc = ps + c2 * nz;
+        PI[c] = (k == 0 || k == nz - 1) ? pc[k] : pc[k] + pc[nz - 1];
     }
-    avg /= zsum;
-    PI[c0] = avg;
-    const T lid = (h.div[(long)i * p.ny + j] - avg) / h.rhoavg;
-    PI[c0 + nz - 1] = lid;
-    for (int k = 1; k < nz - 1; k++) PI[c0 + k] += lid;
 }
 
 // the pressure-gradient force of integrate_hydro (solver.cpp:70-79) over
@@ -198,28 +253,45 @@ __global__ void __launch_bounds__(256) k_hyd_project(KParams<T> p, KFields<T> F,
     F.P[FV][c] = F.P[FV][c] - step * (p.dty * T(1004) * p.tbv[k] * (PI[c] - PI[c - sy]));
 }
 
-// w_velocity_LH (solver.cpp:144-163) into the current w, one thread per
-// interior column
+// w_velocity_LH (solver.cpp:144-163) into the current w
 template <typename T>
-__global__ void __launch_bounds__(128) k_hyd_w(KParams<T> p, KFields<T> F, HydArgs<T> h)
+__global__ void __launch_bounds__(HC_THREADS) k_hyd_w(KParams<T> p, KFields<T> F, HydArgs<T> h)
 {
+    extern __shared__ unsigned char hyd_smem[];
     const int nyi = p.ny - 2, nz = p.nz;
-    const long col = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (col >= (long)(p.nx - 2) * nyi) return;
-    const int i = 1 + (int)(col / nyi), j = 1 + (int)(col % nyi);
-    const long c0 = gix(p.ny, nz, i, j, 0), sx = (long)p.ny * nz, sy = nz;
+    T *dv = (T *)hyd_smem;  // [HC][nz]: the horizontal convergence of level k
+    T *ws = dv + HC * nz;   // [HC][nz]: w
+    const long ncol = (long)(p.nx - 2) * nyi, col0 = (long)blockIdx.x * HC;
     const T *UP = F.P[FU], *VP = F.P[FV];
+    const long sx = (long)p.ny * nz, sy = nz;
+    for (int w = threadIdx.x; w < HC * nz; w += blockDim.x) {
+        const int cl = w / nz, k = w % nz;
+        const long col = col0 + cl;
+        if (col >= ncol || k < 1 || k >= nz - 2) continue;
+        const long c = gix(p.ny, nz, 1 + (int)(col / nyi), 1 + (int)(col % nyi), k);
+        dv[cl * nz + k] = -(UP[c + sx] - UP[c]) * p.one_d_dx - (VP[c + sy] - VP[c]) * p.one_d_dy;
+    }
+    __syncthreads();
+    const int cl = threadIdx.x;
+    if (cl < HC && col0 + cl < ncol) {
+        T *wc = ws + cl * nz;
+        const T *dc = dv + cl * nz;
+        wc[0] = T(0);
+        wc[1] = T(0);
+        wc[nz - 1] = T(0);
+        T w = T(0);
+        for (int k = 2; k < nz - 1; k++) {
+            w = (p.rhow[k - 1] / p.rhow[k]) * w + (p.rhou[k - 1] / p.rhow[k]) * dc[k - 1] * h.dz / p.mu[k - 1];
+            wc[k] = w;
+        }
+    }
+    __syncthreads();
     T *W = F.cur[FW];
-    W[c0] = T(0);
-    W[c0 + 1] = T(0);
-    W[c0 + nz - 1] = T(0);
-    T w = T(0);
-    for (int k = 2; k < nz - 1; k++) {
-        const long c = c0 + k - 1;
-        w = (p.rhow[k - 1] / p.rhow[k]) * w +
-            (p.rhou[k - 1] / p.rhow[k]) * (-(UP[c + sx] - UP[c]) * p.one_d_dx - (VP[c + sy] - VP[c]) * p.one_d_dy) *
-                h.dz / p.mu[k - 1];
-        W[c0 + k] = w;
+    for (int w = threadIdx.x; w < HC * nz; w += blockDim.x) {
+        const int c2 = w / nz, k = w % nz;
+        const long cc = col0 + c2;
+        if (cc >= ncol) continue;
+        W[gix(p.ny, nz, 1 + (int)(cc / nyi), 1 + (int)(cc % nyi), k)] = ws[c2 * nz + k];
     }
 }
 
