@@ -187,6 +187,9 @@ class Engine : public EngineBase {
     // the four-level post-processing kernel (FP32, NZ % 4 == 0); GA_POST=column
     // keeps the per-level one
     bool post_quad = true;
+    // the step's last four-level pass also runs Kessler (rain_fallout 1);
+    // GA_KESSLER=separate keeps the separate kernel
+    bool kes_fused = true, post_kes = false;
     unsigned char *qmask = nullptr;         // clipping record of the next advection (linearisation)
     int plan_order_i = 0, plan_order_j = 0;
 
@@ -500,6 +503,7 @@ class Engine : public EngineBase {
             if (!std::strcmp(ev, "1024")) sx_threads = 1024;
         if (const char *ev = std::getenv("GA_POST")) post_quad = std::strcmp(ev, "column") != 0;
         post_quad = post_quad && sizeof(T) == 4 && NZ % 4 == 0;
+        if (const char *ev = std::getenv("GA_KESSLER")) kes_fused = std::strcmp(ev, "separate") != 0;
         if constexpr (sizeof(T) == 4) {
             smem_sxp = sx_pair_smem(kp.ni, NZ);
             cudaFuncSetAttribute(k_spectral_x_pair<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
@@ -1047,7 +1051,12 @@ class Engine : public EngineBase {
             if (post_quad) {
                 const long nq = NZ / 4;
                 auto go = [&](long ncols, int mode) {
-                    k_post_quad<T><<<cdiv(ncols * nq, PQ_THREADS), PQ_THREADS, 0, stream>>>(kp, F, a, b, (T)step, mode);
+                    if (post_kes)
+                        k_post_quad<T, true><<<cdiv(ncols * nq, PQ_THREADS), PQ_THREADS, 0, stream>>>(
+                            kp, F, a, b, (T)step, mode, d_err);
+                    else
+                        k_post_quad<T><<<cdiv(ncols * nq, PQ_THREADS), PQ_THREADS, 0, stream>>>(kp, F, a, b, (T)step,
+                                                                                            mode, d_err);
                     launches++;
                 };
                 if (pcopy && kp.periodic) {
@@ -1273,11 +1282,17 @@ class Engine : public EngineBase {
                                 cudaMemcpyDeviceToDevice, stream);
             cudaMemcpyAsync(rec + (size_t)(3 * nprog + 4) * N, pi, N * sizeof(T), cudaMemcpyDeviceToDevice, stream);
         }
-        if (moist) kessler();
+        // FP32, Eulerian rain, non-periodic: Kessler runs inside the last
+        // column pass (a periodic domain's copied columns take their own
+        // rain totals, so it keeps the separate kernel)
+        const bool fuse_kes = moist && kes_fused && post_quad && kp.rf == 1 && !kp.periodic;
+        if (moist && !fuse_kes) kessler();
         int fl[7] = {0, 0, 0, 0, 0, 0, 0};
         fl[FU] = fl[FV] = fl[FW] = fl[FTH] = PF_SPONGE | PF_VBC | PF_RAYLEIGH | PF_WRITE_M;
         fl[FQV] = fl[FQC] = fl[FQR] = PF_SPONGE | PF_VBC | PF_WRITE_M;
+        post_kes = fuse_kes;
         post(fl, 7, 1.0, true);
+        post_kes = false;
         swap_inner(true);
         mtime += cfg.dt;
         bigcounter++;

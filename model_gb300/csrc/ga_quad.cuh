@@ -905,10 +905,17 @@ __global__ void __launch_bounds__(AQ_THREADS, MB)
 // ---------------------------------------------------------------------------
 constexpr int PQ_THREADS = 256;
 
-// item w: column w / (NZ/4) of the enumeration `cols`, level quad w % (NZ/4)
-template <typename T>
+// item w: column w / (NZ/4) of the enumeration `cols`, level quad w % (NZ/4).
+// KES: the step's last pass with Kessler (run_kessler_microphysics,
+// kessler.cpp:25-213) and the Eulerian precipitation (precip_rate,
+// microphysics.cpp:143-160) applied to the loaded forecast values ahead of the
+// chain, as the reference applies them before its last boundary conditions;
+// err receives Kessler's E > 100 flag.  A periodic target pass evaluates the
+// source column's Kessler again (the same inputs, the same values) and leaves
+// the rain total to the source's own pass.
+template <typename T, bool KES = false>
 __device__ __forceinline__ void post_quad_body(const KParams<T> &p, const KFields<T> &F, int4 fl0, int4 fl1, T step,
-                                               int cols, long w)
+                                               int cols, long w, int *err = nullptr)
 {
     static_assert(sizeof(T) == 4, "four-level kernels are FP32");
     const int nz = p.nz, NQ = nz >> 2, sx = p.ny * nz, sy = nz;
@@ -948,6 +955,30 @@ __device__ __forceinline__ void post_quad_body(const KParams<T> &p, const KField
     Q4 inq[7];
 #pragma unroll
     for (int f = 0; f < 7; ++f) inq[f] = flv[f] ? ldg4(F.P[f], cs) : Q4{{0.f, 0.f, 0.f, 0.f}};
+    if constexpr (KES) {
+        if (col_in) {
+            const float qr0 = inq[FQR].v[0];  // level 0 before the chain (precip_rate reads it)
+            const Q4 pq = ldg4(F.pi, cs);
+#pragma unroll
+            for (int e = 0; e < 4; e++) {
+                const int k = k0 + e;
+                if (k < 1 || k >= nz - 1) continue;
+                float th = inq[FTH].v[e], qv = inq[FQV].v[e], qc = inq[FQC].v[e], qr = inq[FQR].v[e];
+                if (kessler_point(th, qv, qc, qr, pq.v[e], kes_point(p, F, k, (long)cs + e),
+                                  F.sat ? F.sat + cs + e : nullptr))
+                    atomicExch(err, 1);
+                inq[FTH].v[e] = th;
+                inq[FQV].v[e] = qv;
+                inq[FQC].v[e] = qc;
+                inq[FQR].v[e] = qr;
+            }
+            if (q == 0 && cols != COLS_TARGETS) {
+                const double inc = (double)(p.rhow[1] * 0.5f * (F.vt[cs] + F.vt[cs + 1]) * 0.5f *
+                                            (qr0 + inq[FQR].v[1]) * p.dt);
+                F.accrain[(long)si * p.ny + j] += inc;
+            }
+        }
+    }
     Q4 qb4{{0.f, 0.f, 0.f, 0.f}};
     if ((flv[FQV] & PF_ZERO) && col_in) qb4 = ldg4(F.bar[4], cs);
 #pragma unroll
@@ -1006,11 +1037,11 @@ __device__ __forceinline__ void post_quad_body(const KParams<T> &p, const KField
     }
 }
 
-template <typename T>
+template <typename T, bool KES = false>
 __global__ void __launch_bounds__(PQ_THREADS)
-    k_post_quad(KParams<T> p, KFields<T> F, int4 fl0, int4 fl1, T step, int cols)
+    k_post_quad(KParams<T> p, KFields<T> F, int4 fl0, int4 fl1, T step, int cols, int *err)
 {
-    post_quad_body(p, F, fl0, fl1, step, cols, (long)blockIdx.x * PQ_THREADS + threadIdx.x);
+    post_quad_body<T, KES>(p, F, fl0, fl1, step, cols, (long)blockIdx.x * PQ_THREADS + threadIdx.x, err);
 }
 
 // ---------------------------------------------------------------------------

@@ -145,6 +145,30 @@ def test_post_quad_matches_column_kernel(monkeypatch, case):
             np.testing.assert_array_equal(b, a, err_msg=f"{case} field {f} slot {slot}")
 
 
+@pytest.mark.parametrize("case", ["moist_blob", "turbulence", "hydrostatic"])
+def test_fused_kessler_matches_separate_kernel(monkeypatch, case):
+    """Kessler inside the step's last four-level pass against the separate
+    k_kessler (GA_KESSLER=separate): every field, pi, the rain total and the
+    turbulence scheme's saturation record bit for bit, on a raining blob"""
+    wl = configs.moist_blob(nx=36, ny=30, nz=16, nsteps=5)
+    if case == "turbulence":
+        wl.turbulence_option, wl.use_surface_heat_flux = 1, 1
+    elif case == "hydrostatic":
+        wl.hydrostatic, wl.dx, wl.dy = 1, 2000.0, 2000.0
+    ms = []
+    for mode in ("separate", "fused"):
+        monkeypatch.setenv("GA_KESSLER", mode)
+        ms.append(anelastic.Model(wl, abi.GA_PREC_F32))
+    monkeypatch.delenv("GA_KESSLER")
+    for m in ms:
+        m.step(wl.nsteps)
+    fields = list(range(7)) + [abi.GA_PI, abi.GA_ACCRAIN] + ([abi.GA_SATURATED] if wl.turbulence_option else [])
+    for f in fields:
+        a, b = (m.get(f) for m in ms)
+        np.testing.assert_array_equal(b, a, err_msg=f"{case} field {f}")
+    assert np.abs(ms[1].get(abi.GA_ACCRAIN)).max() > 0
+
+
 @pytest.mark.parametrize("form", ["pair", "1024"])
 @pytest.mark.parametrize("case", ["thunderstorm_small", "moist_blob_odd"])
 def test_spectral_x_pair_matches_single_cta(monkeypatch, case, form):
