@@ -71,7 +71,13 @@ def test_bad_config_rejected_before_device(lib):
     h = C.c_void_p()
     for change, code in [({"nx": 8}, abi.GA_ERR_CONFIG), ({"nz": 200}, abi.GA_ERR_CONFIG),
                          ({"microphysics_option": 2}, abi.GA_ERR_UNSUPPORTED),
-                         ({"dt": -1.0}, abi.GA_ERR_CONFIG), ({"rain_fallout": 3}, abi.GA_ERR_CONFIG)]:
+                         ({"dt": -1.0}, abi.GA_ERR_CONFIG), ({"rain_fallout": 3}, abi.GA_ERR_CONFIG),
+                         ({"use_explicit_diffusion": 1, "diffusion_order": 3}, abi.GA_ERR_CONFIG),
+                         ({"turbulence_option": 2}, abi.GA_ERR_CONFIG),
+                         ({"linear_model": 1, "turbulence_option": 1}, abi.GA_ERR_UNSUPPORTED),
+                         ({"hydrostatic": 1, "periodic_ew_boundaries": 1}, abi.GA_ERR_UNSUPPORTED),
+                         ({"hydrostatic": 1, "turbulence_option": 1}, abi.GA_ERR_UNSUPPORTED),
+                         ({"hydrostatic": 2}, abi.GA_ERR_CONFIG)]:
         s = wl.settings()
         s.update(change)
         cfg = abi.make_config(s)
