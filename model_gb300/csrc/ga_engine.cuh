@@ -370,6 +370,7 @@ class Engine : public EngineBase {
             lin_vmax = dalloc<double>(1);
         }
         if (c->turbulence_option) {  // init_kmix (turbulence.cpp:85-151)
+            cudaFuncSetAttribute(k_turb_tend_tile<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
             turb.kmix = dalloc<T>(N);
             turb.khmix = dalloc<T>(N);
             T *tt = dalloc<T>((size_t)nprog * N);
@@ -926,8 +927,14 @@ class Engine : public EngineBase {
         const long ncol = (long)(NX - 2) * (NY - 2);
         const size_t sm = (size_t)cy * kx * (sizeof(T) + 1);
         k_turb_kmix<T><<<cdiv(ncol, cy), dim3(kx, cy), sm, stream>>>(kp, F, turb);
-        const long tot = (long)(NX - 2) * (NY - 2) * (NZ - 2);
-        k_turb_tend<T><<<cdiv(tot, 256), 256, 0, stream>>>(kp, F, turb);
+        const size_t st = turb_tile_smem(NZ, sizeof(T));
+        if (st <= 200 * 1024) {
+            const dim3 g(cdiv(NX - 2, TT_TI), cdiv(NY - 2, TT_TJ));
+            k_turb_tend_tile<T><<<g, 256, st, stream>>>(kp, F, turb);
+        } else {
+            const long tot = (long)(NX - 2) * (NY - 2) * (NZ - 2);
+            k_turb_tend<T><<<cdiv(tot, 256), 256, 0, stream>>>(kp, F, turb);
+        }
         launches += 2;
     }
     // the tendencies' share of an RK stage (apply_*_diffusion, :233-290)

@@ -301,6 +301,118 @@ __global__ void __launch_bounds__(256) k_turb_tend(KParams<T> p, KFields<T> F, T
     for (int n = 0; n < nf; n++) a.tend[3 + n][c] = turb_scalar(p, a, F.M[FTH + n], c, k, sx, sy, tl[n]);
 }
 
+// The same tendencies by tiles: a block owns TI x TJ columns and every
+// level.  Phase 1 evaluates each deformation-rate component once on the
+// tile's columns and the column row and line west and south of them into
+// shared memory; phase 2 forms each point's stress divergence from those (the
+// pointwise kernel evaluates every component at each point that uses it,
+// about eighteen evaluations per point against six here) and its scalar flux
+// divergences as k_turb_tend does.  The arithmetic is k_turb_tend's.
+constexpr int TT_TI = 4, TT_TJ = 4;
+
+__host__ __device__ constexpr size_t turb_tile_smem(int nz, size_t tsize)
+{
+    return 6 * (size_t)(TT_TI + 1) * (TT_TJ + 1) * nz * tsize;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_turb_tend_tile(KParams<T> p, KFields<T> F, TurbArgs<T> a)
+{
+    extern __shared__ unsigned char tt_smem[];
+    constexpr int RA = TT_TI + 1, RB = TT_TJ + 1;
+    const int nz = p.nz;
+    T *S = (T *)tt_smem;  // [6][RA][RB][nz]: t11, t22, t33, t13, t23, t12
+    const long rs = (long)RA * RB * nz;
+    const int i0 = 1 + blockIdx.x * TT_TI, j0 = 1 + blockIdx.y * TT_TJ;
+    const int ti = min(TT_TI, p.nx - 1 - i0), tj = min(TT_TJ, p.ny - 1 - j0);
+    const long sx = (long)p.ny * nz, sy = nz;
+    const T odx = p.one_d_dx, ody = p.one_d_dy;
+    TurbTau<T> tau{F.M[FU], F.M[FV], F.M[FW], p.mu, p.mw, sx, sy, odx, ody, p.one_d_dz};
+    for (int w = threadIdx.x; w < RA * RB * (nz - 1); w += blockDim.x) {
+        const int k = w % (nz - 1), r = w / (nz - 1), bb = r % RB, aa = r / RB;
+        if (aa > ti || bb > tj) continue;
+        const long c = gix(p.ny, nz, i0 - 1 + aa, j0 - 1 + bb, k);
+        const long o = (long)r * nz + k;
+        S[o] = tau.t11(c);
+        S[rs + o] = tau.t22(c);
+        S[2 * rs + o] = tau.t33(c, k);
+        S[3 * rs + o] = tau.t13(c, k);
+        S[4 * rs + o] = tau.t23(c, k);
+        S[5 * rs + o] = tau.t12(c);
+    }
+    __syncthreads();
+    const T *S11 = S, *S22 = S + rs, *S33 = S + 2 * rs, *S13 = S + 3 * rs, *S23 = S + 4 * rs, *S12 = S + 5 * rs;
+    const T *KM = a.kmix, *KH = a.khmix;
+    for (int w = threadIdx.x; w < TT_TI * TT_TJ * (nz - 2); w += blockDim.x) {
+        const int k = 1 + w % (nz - 2), r = w / (nz - 2), b = r % TT_TJ, aa = r / TT_TJ;
+        if (aa >= ti || b >= tj) continue;
+        const int i = i0 + aa, j = j0 + b;
+        const long c = gix(p.ny, nz, i, j, k);
+        const long oc = (long)((aa + 1) * RB + b + 1) * nz, ow = (long)(aa * RB + b + 1) * nz;
+        const long os = (long)((aa + 1) * RB + b) * nz, osw = (long)(aa * RB + b) * nz;
+        const T odz = p.one_d_dz * p.mu[k], odzw = p.one_d_dz * p.mw[k];
+        const long c1 = c - (k - 1);
+        const T uK11H_h = KH[c];
+        const T uK11H_l = KH[c - sx];
+        const T uK12H_h = T(0.25) * (KH[c] + KH[c - sx] + KH[c - sx + sy] + KH[c + sy]);
+        const T uK12H_l = T(0.25) * (KH[c - sy] + KH[c - sx - sy] + KH[c - sx] + KH[c]);
+        const T uK13V_h = T(0.50) * (KM[c + 1] + KM[c - sx + 1]);
+        const T vK12H_h = T(0.25) * (KH[c - sy] + KH[c] + KH[c + sx - sy] + KH[c + sx]);
+        const T vK12H_l = uK12H_l;
+        const T vK22H_h = KH[c];
+        const T vK22H_l = KH[c - sy];
+        const T vK23V_h = T(0.5) * (KM[c + 1] + KM[c - sy + 1]);
+        const T wK13H_h = T(0.25) * (KH[c] + KH[c - 1] + KH[c + sx] + KH[c + sx - 1]);
+        const T wK13H_l = T(0.25) * (KH[c] + KH[c - 1] + KH[c - sx] + KH[c - sx - 1]);
+        const T wK23H_h = T(0.25) * (KH[c] + KH[c - 1] + KH[c + sy] + KH[c + sy - 1]);
+        const T wK23H_l = T(0.25) * (KH[c] + KH[c - 1] + KH[c - sy] + KH[c - sy - 1]);
+        const T wK33V_h = T(0.50) * (KM[c] + KM[c + 1]);
+        const T wK33V_l = T(0.50) * (KM[c] + KM[c - 1]);
+        T tau_u_zl, tau_v_zl;
+        if (k == 1) {  // ocean surface stress (:899-905)
+            const T u = F.M[FU][c1], v = F.M[FV][c1], ub = F.bar[0][c1], vb = F.bar[1][c1];
+            const T ws = sqrt((u + ub) * (u + ub) + (v + vb) * (v + vb));
+            const T wsb = sqrt(ub * ub + vb * vb);
+            const T drag = (T(1.1e-3) + T(4.0e-5) * ws);
+            tau_u_zl = drag * (ws * u + (ws - wsb) * ub);
+            tau_v_zl = drag * (ws * v + (ws - wsb) * vb);
+        } else {
+            tau_u_zl = (T(0.50) * (KM[c] + KM[c - sx])) * S13[ow + k - 1];
+            tau_v_zl = (T(0.5) * (KM[c] + KM[c - sy])) * S23[os + k - 1];
+        }
+        const T t13w = S13[ow + k], t23s = S23[os + k];
+        a.tend[0][c] = (uK11H_h * S11[oc + k] - uK11H_l * S11[ow + k]) * odx +
+                       (uK12H_h * S12[ow + k] - uK12H_l * S12[osw + k]) * ody + (uK13V_h * t13w - tau_u_zl) * odz;
+        a.tend[1][c] = (vK12H_h * S12[os + k] - vK12H_l * S12[osw + k]) * odx +
+                       (vK22H_h * S22[oc + k] - vK22H_l * S22[os + k]) * ody + (vK23V_h * t23s - tau_v_zl) * odz;
+        a.tend[2][c] = (wK13H_h * S13[oc + k - 1] - wK13H_l * S13[ow + k - 1]) * odx +
+                       (wK23H_h * S23[oc + k - 1] - wK23H_l * S23[os + k - 1]) * ody +
+                       (wK33V_h * S33[oc + k] - wK33V_l * S33[oc + k - 1]) * odzw;
+        const int nf = p.moist ? 4 : 1;
+        T tl[4] = {T(0), T(0), T(0), T(0)};
+        if (k == 1) {
+            if (p.moist && a.surface_flux) {  // ocean heat and vapour fluxes (:1083-1104)
+                typedef TurbC<T> C;
+                const T u = F.M[FU][c1], v = F.M[FV][c1], ub = F.bar[0][c1], vb = F.bar[1][c1];
+                const T ws = sqrt((u + ub) * (u + ub) + (v + vb) * (v + vb));
+                const T wsb = sqrt(ub * ub + vb * vb);
+                const T drag = (T(1.1e-3) + T(4.0e-5) * ws) * T(1.0) * T(1.0);
+                const T PB = F.bar[5][c1], PI = F.pi[c1];
+                const T pressure = C::p0 * kpow(PB + a.dp_to_surface, T(1004.0 / 287.0)) + PI * p.rhou[1];
+                const T pisfc = PB + PI / (C::cp * p.tbv[1]) + a.dp_to_surface;
+                const T qvs = T(0.62197) * a.es_water / (pressure - a.es_water);
+                const T tsb = (F.bar[3][c1] + p.tb[1]) * pisfc;
+                const T tsp = F.M[FTH][c1] * pisfc;
+                tl[1] = drag * ((ws - wsb) * (qvs - F.bar[4][c1] - p.qb[1]) - ws * F.M[FQV][c1]);
+                tl[0] = drag * ((ws - wsb) * (a.water_temp - tsb) - ws * tsp);
+            }
+        } else {
+            for (int n = 0; n < nf; n++) tl[n] = turb_flux_below(p, a, F.M[FTH + n], c, k);
+        }
+        for (int n = 0; n < nf; n++) a.tend[3 + n][c] = turb_scalar(p, a, F.M[FTH + n], c, k, sx, sy, tl[n]);
+    }
+}
+
 // ---------------------------------------------------------------------------
 // the tendencies added to the forecast fields in an RK stage: velocity
 // (apply_velocity_diffusion, :233-256, over [3,N-3): u and v from level 1, w
