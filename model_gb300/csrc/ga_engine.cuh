@@ -345,21 +345,22 @@ class Engine : public EngineBase {
             std::vector<double> pf((size_t)NX * (NY + 1), 0.0), rden((size_t)NX * NY);
             ac[0] = 0;
             cc[NY - 1] = 0;
-            for (int i = 0; i < NX; i++) {
+            for (int i = 0; i < NX; i++) {  // layouts [j][i]
                 const double kw = i < NX / 2 ? 2 * trigpi * (double)i / NX : 2 * trigpi * (double)(NX - i) / NX;
-                double *P = pf.data() + (size_t)i * (NY + 1);
+                double Pj = 0.0;
                 for (int j = 0; j < NY; j++) {
                     const double b = j == 0 ? -cols->rhow[2] / (dx * dx)
                                             : 2. * (cos(kw) - 1.) / (dx * dx) - cc[j] - ac[j];
-                    const double denom = b + ac[j] * P[j];
-                    P[j + 1] = -cc[j] / denom;
-                    rden[(size_t)i * NY + j] = 1.0 / denom;
+                    const double denom = b + ac[j] * Pj;
+                    Pj = -cc[j] / denom;
+                    pf[(size_t)(j + 1) * NX + i] = Pj;
+                    rden[(size_t)j * NX + i] = 1.0 / denom;
                 }
             }
-            hyd.pf = upload(pf);
-            hyd.rden = upload(rden);
-            hyd.ac = upload(ac);
-            hyd.pw = dalloc<double>((size_t)NX * 2 * (NY + 1));
+            hyd.pf = col_T(pf.data(), (int)pf.size());
+            hyd.rden = col_T(rden.data(), (int)rden.size());
+            hyd.ac = col_T(ac.data(), NY);
+            hyd.pw = dalloc<T>((size_t)NX * 2 * (NY + 1));
             hyd.div = dalloc<T>((size_t)NX * NY);
             hyd.spec2 = dalloc<T2>((size_t)NX * NY);
             hyd_L = (int)std::max<size_t>(1, std::min<size_t>(8, 49152 / (2 * (size_t)NX * sizeof(T2))));

@@ -12,7 +12,8 @@
 // x-wavenumber (whose back substitution leaves the last row at its
 // transformed value), and the inverse transform.  The transforms reuse the
 // shared-memory Stockham FFT of the 3-D solve (fft_smem), batched over a tile
-// of y-lines; the tridiagonal solves run in FP64.  Non-periodic domains.
+// of y-lines; the tridiagonal solves run in the context's precision with
+// elimination factors formed once on the host in FP64.  Non-periodic domains.
 #pragma once
 #include "ga_kernels.cuh"
 
@@ -24,12 +25,15 @@ struct HydArgs {
     // the tridiagonal system of init_fft2d (pressure.cpp:621-641) does not
     // change during a run: its elimination factors P[j+1] = -ccoef[j]/denom
     // and 1/denom, denom = BCOEF(i,j) + acoef[j] P[j], are formed once on the
-    // host (the reference's expressions, FP64), [nx][ny+1] and [nx][ny]
-    const double *pf, *rden;
-    const double *ac;      // acoef [ny]
-    double *pw;            // work of the back substitution, [nx][2 (ny+1)] (real and imaginary Q)
+    // host (the reference's expressions, FP64, stored in the context's
+    // precision: FP64 is scarce on this GPU, and the FP32 solve keeps the
+    // FP32 step's accuracy), [ny+1][nx] and [ny][nx] (x-wavenumber fastest:
+    // a warp of wavenumbers reads one row at a time)
+    const T *pf, *rden;
+    const T *ac;           // acoef [ny]
+    T *pw;                 // work of the back substitution, [2][ny+1][nx] (real and imaginary Q)
     T *div;                // div_avg, [nx][ny]
-    typename V2<T>::t *spec2;  // transformed div_avg, [nx][ny]
+    typename V2<T>::t *spec2;  // transformed div_avg, [ny][nx]
     T rhoavg;              // column-average density (column_average_density, initializer.cpp:1265-1282)
     T dz;
 };
@@ -112,7 +116,7 @@ __global__ void k_hyd_fft(KParams<T> p, HydArgs<T> h, FftPlan P, const typename 
             T2 v;
             if (l < lt) {
                 if (inv) {
-                    v = h.spec2[(long)i * p.ny + j0 + l];
+                    v = h.spec2[(long)(j0 + l) * p.nx + i];
                 } else {
                     v.x = h.div[(long)i * p.ny + j0 + l];
                     v.y = T(0);
@@ -135,13 +139,13 @@ __global__ void k_hyd_fft(KParams<T> p, HydArgs<T> h, FftPlan P, const typename 
                 T2 o;
                 o.x = v.x / n;
                 o.y = v.y / n;
-                h.spec2[(long)i * p.ny + j0 + l] = o;
+                h.spec2[(long)(j0 + l) * p.nx + i] = o;
             }
         }
 }
 
 // the tridiagonal solve along y of one x-wavenumber (pressure.cpp:675-700),
-// real and imaginary parts, in FP64 with the precomputed factors: each step
+// real and imaginary parts, with the precomputed factors: each step
 // of the recurrence is a multiply-subtract and a multiply by 1/denom (the
 // reference divides by denom; the two differ by an ulp, well inside the
 // transform's own rounding)
@@ -151,33 +155,34 @@ __global__ void k_hyd_thomas(KParams<T> p, HydArgs<T> h)
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.nx) return;
     typedef typename V2<T>::t T2;
-    const int nj = p.ny;
-    // distinct arrays: the loads of later rows may be issued before the
-    // stores of earlier ones
-    double *__restrict__ Qr = h.pw + (long)i * 2 * (nj + 1);
-    double *__restrict__ Qi = Qr + (nj + 1);
-    const double *__restrict__ P = h.pf + (long)i * (nj + 1);
-    const double *__restrict__ R = h.rden + (long)i * nj;
-    const double *__restrict__ ac = h.ac;
-    T2 *__restrict__ x = h.spec2 + (long)i * nj;
-    double qr = 0.0, qi = 0.0;
-    // unrolled so that the loads of a batch of rows are issued ahead of the
-    // dependent chain
-#pragma unroll 16
+    const int nj = p.ny, nx = p.nx;
+    // rows are [j][i]: each step of the recurrence is one coalesced row for
+    // the warp; distinct arrays, so the loads of later rows may be issued
+    // before the stores of earlier ones
+    T *__restrict__ Qr = h.pw + i;
+    T *__restrict__ Qi = h.pw + (long)(nj + 1) * nx + i;
+    const T *__restrict__ P = h.pf + i;
+    const T *__restrict__ R = h.rden + i;
+    const T *__restrict__ ac = h.ac;
+    T2 *__restrict__ x = h.spec2 + i;
+    T qr = T(0), qi = T(0);
+#pragma unroll 8
     for (int j = 0; j < nj; j++) {
-        const T2 v = x[j];
-        qr = ((double)v.x - ac[j] * qr) * R[j];
-        qi = ((double)v.y - ac[j] * qi) * R[j];
-        Qr[j + 1] = qr;
-        Qi[j + 1] = qi;
+        const T2 v = x[(long)j * nx];
+        const T r = R[(long)j * nx];
+        qr = (v.x - ac[j] * qr) * r;
+        qi = (v.y - ac[j] * qi) * r;
+        Qr[(long)(j + 1) * nx] = qr;
+        Qi[(long)(j + 1) * nx] = qi;
     }
-    double xr = (double)x[nj - 1].x, xi = (double)x[nj - 1].y;
-#pragma unroll 16
+    T xr = x[(long)(nj - 1) * nx].x, xi = x[(long)(nj - 1) * nx].y;
+#pragma unroll 8
     for (int j = nj - 2; j >= 0; j--) {
-        xr = P[j + 1] * xr + Qr[j + 1];
-        xi = P[j + 1] * xi + Qi[j + 1];
-        x[j].x = (T)xr;
-        x[j].y = (T)xi;
+        const T pj = P[(long)(j + 1) * nx];
+        xr = pj * xr + Qr[(long)(j + 1) * nx];
+        xi = pj * xi + Qi[(long)(j + 1) * nx];
+        x[(long)j * nx].x = xr;
+        x[(long)j * nx].y = xi;
     }
 }
 
