@@ -85,6 +85,13 @@ RUN_CASES = {
     "linear_moist": (lambda: _linear(_jet(True)), 4),
     "linear_diffusion": (lambda: _linear(_diffusing(_jet(True), 4, 0.004)), 3),
     "linear_rescale": (lambda: _linear(_jet(False), bigcounter0=1438), 4),
+    # edge sizes: the smallest grid the library takes (12x12x6), odd prime
+    # transform lengths (31, 29) with an odd level count, the smallest periodic
+    # domain (13: an x transform of 7), and the largest level count (128)
+    "edge_min": (lambda: configs.moist_blob(nx=12, ny=12, nz=6, dz=1500.0), 4),
+    "edge_prime": (lambda: configs.moist_blob(nx=31, ny=29, nz=7, dz=1200.0), 3),
+    "edge_periodic_min": (lambda: configs.moist_blob(nx=13, ny=12, nz=8, dz=1000.0, periodic=1), 3),
+    "edge_tall": (lambda: configs.moist_blob(nx=12, ny=13, nz=128, dz=100.0), 2),
     # the hydrostatic equation set (integrate_hydro, w diagnosed)
     "hydro_dry": (lambda: _hydro(configs.dry_bubble(nx=16, ny=14, nz=10, dx=2000.0, dz=500.0, dt=4.0, amp=3.0,
                                                     radius=6000.0, zc=1500.0, noise=0.2)), 4),

@@ -314,6 +314,23 @@ def test_linear_model_rejects_turbulence():
         anelastic.Model(wl, abi.GA_PREC_F64)
 
 
+@pytest.mark.parametrize("name", [n for n in fx.run_names() if n.startswith("run_edge_")])
+def test_edge_sizes_fp32_against_fp64(name):
+    """the edge-size golden cases (12x12x6, prime transform lengths with an
+    odd level count, the smallest periodic domain, 128 levels) in FP32 (the
+    per-level column kernels where NZ is not a multiple of 4, the four-level
+    ones where it is) against FP64"""
+    d = fx.load(name)
+    wl = fx.workload(d)
+    a = anelastic.Model(wl, abi.GA_PREC_F32, columns=fx.columns(d))
+    b = anelastic.Model(wl, abi.GA_PREC_F64, columns=fx.columns(d))
+    a.step(wl.nsteps)
+    b.step(wl.nsteps)
+    for f in range(7):
+        e = fx.rel_l2(a.get(f), b.get(f))
+        assert e <= 1e-4, (name, abi.PROG_NAMES[f], e)
+
+
 def test_step_is_deterministic():
     from model_gb300 import configs
     wl = configs.moist_blob(nx=40, ny=36, nz=20, nsteps=5)
