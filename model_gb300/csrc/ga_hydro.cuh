@@ -165,24 +165,51 @@ __global__ void k_hyd_thomas(KParams<T> p, HydArgs<T> h)
     const T *__restrict__ R = h.rden + i;
     const T *__restrict__ ac = h.ac;
     T2 *__restrict__ x = h.spec2 + i;
+    // each chunk's rows are loaded before its steps run, so a chunk waits on
+    // memory once rather than once per step
+    constexpr int CH = 16;
     T qr = T(0), qi = T(0);
-#pragma unroll 8
-    for (int j = 0; j < nj; j++) {
-        const T2 v = x[(long)j * nx];
-        const T r = R[(long)j * nx];
-        qr = (v.x - ac[j] * qr) * r;
-        qi = (v.y - ac[j] * qi) * r;
-        Qr[(long)(j + 1) * nx] = qr;
-        Qi[(long)(j + 1) * nx] = qi;
+    for (int j0 = 0; j0 < nj; j0 += CH) {
+        T2 v[CH];
+        T r[CH], av[CH];
+#pragma unroll
+        for (int t = 0; t < CH; t++) {
+            const int j = min(j0 + t, nj - 1);
+            v[t] = x[(long)j * nx];
+            r[t] = R[(long)j * nx];
+            av[t] = ac[j];
+        }
+#pragma unroll
+        for (int t = 0; t < CH; t++) {
+            const int j = j0 + t;
+            if (j < nj) {
+                qr = (v[t].x - av[t] * qr) * r[t];
+                qi = (v[t].y - av[t] * qi) * r[t];
+                Qr[(long)(j + 1) * nx] = qr;
+                Qi[(long)(j + 1) * nx] = qi;
+            }
+        }
     }
     T xr = x[(long)(nj - 1) * nx].x, xi = x[(long)(nj - 1) * nx].y;
-#pragma unroll 8
-    for (int j = nj - 2; j >= 0; j--) {
-        const T pj = P[(long)(j + 1) * nx];
-        xr = pj * xr + Qr[(long)(j + 1) * nx];
-        xi = pj * xi + Qi[(long)(j + 1) * nx];
-        x[(long)j * nx].x = xr;
-        x[(long)j * nx].y = xi;
+    for (int j1 = nj - 2; j1 >= 0; j1 -= CH) {
+        T pj[CH], qrj[CH], qij[CH];
+#pragma unroll
+        for (int t = 0; t < CH; t++) {
+            const int j = max(j1 - t, 0);
+            pj[t] = P[(long)(j + 1) * nx];
+            qrj[t] = Qr[(long)(j + 1) * nx];
+            qij[t] = Qi[(long)(j + 1) * nx];
+        }
+#pragma unroll
+        for (int t = 0; t < CH; t++) {
+            const int j = j1 - t;
+            if (j >= 0) {
+                xr = pj[t] * xr + qrj[t];
+                xi = pj[t] * xi + qij[t];
+                x[(long)j * nx].x = xr;
+                x[(long)j * nx].y = xi;
+            }
+        }
     }
 }
 
