@@ -408,9 +408,9 @@ def adjoint_bench(torch, device, steps, every, moist=False, size=512):
 
 # field passes per step of the optional physics (moist, FP32 fields): the
 # turbulence coefficients (14 fields in, 2 out), the tendencies (9 in, 7 out)
-# and three stage additions (14 in, 7 out each); explicit diffusion's
-# tendencies (7 in, 7 out) and their addition (14 in, 7 out)
-PHYSICS_PASSES = {"turbulence": 16 + 16 + 3 * 21, "diffusion": 14 + 21}
+# and three stage additions (14 in, 7 out each); explicit diffusion's one
+# pass (7 in, 7 out)
+PHYSICS_PASSES = {"turbulence": 16 + 16 + 3 * 21, "diffusion": 14}
 
 
 def physics_bench(torch, device, steps, accuracy_steps):

@@ -117,7 +117,8 @@ class Engine : public EngineBase {
     // by the tensor memory accelerator (k_advect_tma), and its candidate
     int adv_tma = 0, adv_tmc = 0;
     double *budget_w = nullptr, *budget_part = nullptr;  // FP64 budget weights and partial sums
-    T *diff_tend = nullptr;  // explicit diffusion: tendencies of every prognostic field
+    T *diff_tend = nullptr;  // explicit diffusion: a second buffer for every prognostic field
+    T *diff_buf[7] = {};     // (the one each field's diffused start-of-step values go to)
     const T *diff_w = nullptr;  // and the vertical finite-difference weights, order+1 per level
     // turbulence: coefficients, tendencies, tables (ga_turb.cuh); turb.kmix
     // is null when the scheme is off.  turb_sat is Kessler's saturation record.
@@ -397,6 +398,7 @@ class Engine : public EngineBase {
         }
         if (c->use_explicit_diffusion) {
             diff_tend = dalloc<T>((size_t)nprog * N);
+            for (int f = 0; f < nprog; f++) diff_buf[f] = diff_tend + (size_t)f * N;
             const std::vector<double> w = diffusion_weights(c->diffusion_order, cols->zsu, NZ);
             diff_w = col_T(w.data(), (int)w.size());
         }
@@ -875,14 +877,19 @@ class Engine : public EngineBase {
     {
         const int order = cfg.diffusion_order;
         if (!diff_tend || !diff_w || (order != 2 && order != 4 && order != 6)) return;
-        ProfScope ps(this, PC_DIFFUSION, 2);
-        const long tot = (long)(NX - 6) * (NY - 6) * (NZ - 2) * nprog;
-        const int nb = (int)std::min((tot + 255) / 256, 152L * 8);
+        ProfScope ps(this, PC_DIFFUSION, 1);
+        const long tot = N * nprog;
+        const int nb = (int)std::min((tot + 255) / 256, 152L * 16);
         KFields<T> F = fields();
-        k_diffuse_tend<T><<<nb, 256, 0, stream>>>(kp, F, diff_tend, nprog, order, (T)cfg.kdiffh, (T)cfg.kdiffv, diff_w,
+        DiffOut<T> o;
+        for (int f = 0; f < 7; f++) o.out[f] = (f < nprog && !(f == FW && hyd.div)) ? diff_buf[f] : nullptr;
+        k_diffuse_into<T><<<nb, 256, 0, stream>>>(kp, F, o, nprog, order, (T)cfg.kdiffh, (T)cfg.kdiffv, diff_w,
                                                   (T)step);
-        k_diffuse_add<T><<<nb, 256, 0, stream>>>(kp, F, diff_tend, nprog);
-        launches += 2;
+        // the diffused copy becomes the start-of-step slot; two steps swap
+        // back, so a captured two-step graph leaves the pointers as it found them
+        for (int f = 0; f < nprog; f++)
+            if (o.out[f]) std::swap(buf[f][mi[f]], diff_buf[f]);
+        launches += 1;
     }
 
     // solve_pressure of the hydrostatic set (pressure.cpp:142-170, 229-298)
@@ -1204,6 +1211,9 @@ class Engine : public EngineBase {
             break;
         default: return GA_ERR_ARG;
         }
+        // a captured two-step graph pairs the rotation parity with the
+        // diffusion buffers' parity; a single operator may break the pairing
+        if (diff_tend) drop_graphs();
         int rc = launch_status();
         if (rc) return rc;
         rc = sync_status();

@@ -2276,6 +2276,51 @@ __global__ void __launch_bounds__(256) k_diffuse_tend(KParams<T> p, KFields<T> F
     }
 }
 
+// the diffused fields written whole into a second buffer per field (the
+// interior points M + step d, every other point copied), which then takes the
+// start-of-step slot's place: one pass instead of the tendency buffer and its
+// addition (every tendency is still formed from the old values)
+template <typename T>
+struct DiffOut {
+    T *out[7];
+};
+template <typename T>
+__global__ void __launch_bounds__(256) k_diffuse_into(KParams<T> p, KFields<T> F, DiffOut<T> o, int nf, int order,
+                                                      T kh, T kv, const T *dw, T step)
+{
+    const long per = p.n, tot = per * nf;
+    const long sx = (long)p.ny * p.nz, sy = p.nz;
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < tot; t += (long)gridDim.x * blockDim.x) {
+        const int f = (int)(t / per);
+        const long c = t - f * per;
+        T *out = o.out[f];
+        if (!out) continue;  // a field left alone (w of the hydrostatic set)
+        const T *v = F.M[f];
+        const int k = (int)(c % p.nz), j = (int)((c / p.nz) % p.ny), i = (int)(c / sx);
+        if (i < 3 || i >= p.nx - 3 || j < 3 || j >= p.ny - 3 || k < 1 || k >= p.nz - 1) {
+            out[c] = v[c];
+            continue;
+        }
+        const int ind = order + 1, nz = p.nz;
+        T d;
+        if (order == 2) {
+            d = kh * dif2(v, c, sx) + kh * dif2(v, c, sy) + kv * wk2(v, c, dw + ind * k);
+        } else if (order == 4) {
+            if (k == 1 || k == nz - 2)  // both ends with row NZ-2, as damping.cpp:820 and :861 do
+                d = -kh * dif4(v, c, sx) - kh * dif4(v, c, sy) + kv * wk2(v, c, dw + ind * (nz - 2));
+            else
+                d = -kh * dif4(v, c, sx) - kh * dif4(v, c, sy) - kv * wk4(v, c, dw + ind * k);
+        } else {
+            T z;
+            if (k == 1 || k == nz - 2) z = kv * wk2(v, c, dw + ind * k);
+            else if (k == 2 || k == nz - 3) z = -kv * wk4(v, c, dw + ind * k);
+            else z = kv * wk6(v, c, dw + ind * k);
+            d = kh * dif6(v, c, sx) + kh * dif6(v, c, sy) + z;
+        }
+        out[c] = v[c] + step * d;
+    }
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256) k_diffuse_add(KParams<T> p, KFields<T> F, const T *tend, int nf)
 {
