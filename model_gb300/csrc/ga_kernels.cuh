@@ -2205,9 +2205,10 @@ __global__ void k_check_finite(const T *a, long n, int *flag)
 // ---------------------------------------------------------------------------
 // Explicit diffusion of the start-of-step fields (apply_explicit_diffusion,
 // damping.cpp:1125-1146, with diffusion_{2nd,4th,6th}_var, :769-940) over
-// i in [3, NX-3), j in [3, NY-3), k in [1, NZ-1).  k_diffuse_tend forms every
-// tendency from the old values (the reference's temp_var); k_diffuse_add then
-// adds them.  The vertical operator of the stretched-grid build weights the
+// i in [3, NX-3), j in [3, NY-3), k in [1, NZ-1).  Every point's diffusion
+// is formed from the old values (the reference's temp_var) and written into a
+// second buffer (k_diffuse_into).  The vertical operator of the stretched-grid
+// build weights the
 // column with the finite-difference weights `dw` (order+1 per level, built
 // on the host as init_diffusion_weights does, :158-270).
 // ---------------------------------------------------------------------------
@@ -2238,42 +2239,6 @@ __device__ __forceinline__ T wk6(const T *v, long c, const T *w)
 {
     return w[0] * v[c - 3] + w[1] * v[c - 2] + w[2] * v[c - 1] + w[3] * v[c] + w[4] * v[c + 1] + w[5] * v[c + 2] +
            w[6] * v[c + 3];
-}
-
-template <typename T>
-__global__ void __launch_bounds__(256) k_diffuse_tend(KParams<T> p, KFields<T> F, T *tend, int nf, int order, T kh,
-                                                      T kv, const T *dw, T step)
-{
-    const int ni = p.nx - 6, nj = p.ny - 6, nk = p.nz - 2;
-    const long per = (long)ni * nj * nk, tot = per * nf;
-    const long sx = (long)p.ny * p.nz, sy = p.nz;
-    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < tot; t += (long)gridDim.x * blockDim.x) {
-        const int f = (int)(t / per);
-        long r = t - f * per;
-        const int k = 1 + (int)(r % nk);
-        r /= nk;
-        const int j = 3 + (int)(r % nj), i = 3 + (int)(r / nj);
-        const long c = gix(p.ny, p.nz, i, j, k);
-        if (f == FW && p.hydrostatic) continue;  // damping.cpp:1052: no w when hydrostatic
-        const T *v = F.M[f];
-        const int ind = order + 1, nz = p.nz;
-        T d;
-        if (order == 2) {
-            d = kh * dif2(v, c, sx) + kh * dif2(v, c, sy) + kv * wk2(v, c, dw + ind * k);
-        } else if (order == 4) {
-            if (k == 1 || k == nz - 2)  // both ends with row NZ-2, as damping.cpp:820 and :861 do
-                d = -kh * dif4(v, c, sx) - kh * dif4(v, c, sy) + kv * wk2(v, c, dw + ind * (nz - 2));
-            else
-                d = -kh * dif4(v, c, sx) - kh * dif4(v, c, sy) - kv * wk4(v, c, dw + ind * k);
-        } else {
-            T z;
-            if (k == 1 || k == nz - 2) z = kv * wk2(v, c, dw + ind * k);
-            else if (k == 2 || k == nz - 3) z = -kv * wk4(v, c, dw + ind * k);
-            else z = kv * wk6(v, c, dw + ind * k);
-            d = kh * dif6(v, c, sx) + kh * dif6(v, c, sy) + z;
-        }
-        tend[(long)f * p.n + c] = step * d;
-    }
 }
 
 // the diffused fields written whole into a second buffer per field (the
@@ -2318,23 +2283,6 @@ __global__ void __launch_bounds__(256) k_diffuse_into(KParams<T> p, KFields<T> F
             d = kh * dif6(v, c, sx) + kh * dif6(v, c, sy) + z;
         }
         out[c] = v[c] + step * d;
-    }
-}
-
-template <typename T>
-__global__ void __launch_bounds__(256) k_diffuse_add(KParams<T> p, KFields<T> F, const T *tend, int nf)
-{
-    const int ni = p.nx - 6, nj = p.ny - 6, nk = p.nz - 2;
-    const long per = (long)ni * nj * nk, tot = per * nf;
-    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < tot; t += (long)gridDim.x * blockDim.x) {
-        const int f = (int)(t / per);
-        long r = t - f * per;
-        const int k = 1 + (int)(r % nk);
-        r /= nk;
-        const int j = 3 + (int)(r % nj), i = 3 + (int)(r / nj);
-        const long c = gix(p.ny, p.nz, i, j, k);
-        if (f == FW && p.hydrostatic) continue;
-        F.M[f][c] += tend[(long)f * p.n + c];
     }
 }
 
