@@ -331,6 +331,29 @@ def test_edge_sizes_fp32_against_fp64(name):
         assert e <= 1e-4, (name, abi.PROG_NAMES[f], e)
 
 
+@pytest.mark.parametrize("seed", range(48))
+def test_random_configuration_vs_oracle(seed):
+    """the GPU's FP64 step against the oracle on the seeded random
+    configurations of tests/test_oracle_random.py (grids with prime
+    transform lengths and odd level counts, sponge widths, periodic domains,
+    rain fallout, explicit diffusion, turbulence, the linearised and
+    hydrostatic sets), whose oracle runs equal the reference build's bit for
+    bit: every prognostic field and pi within 1e-10"""
+    from oracle import oracle as O
+    from tests.test_oracle_random import _case
+    wl, nsteps = _case(7000 + seed)
+    cols = anelastic.build_columns(wl)
+    m = anelastic.Model(wl, abi.GA_PREC_F64, columns=cols)
+    m.step(nsteps)
+    o = O.Oracle(wl, cols)
+    assert o.step(nsteps) == 0
+    nprog = 7 if wl.microphysics_option else 4
+    for f in list(range(nprog)) + [abi.GA_PI]:
+        for slot in ((abi.GA_SLOT_CUR, abi.GA_SLOT_P, abi.GA_SLOT_M) if f < nprog else (0,)):
+            e = fx.rel_l2(m.get(f, slot), o.get(f, slot))
+            assert e <= 1e-10, (seed, f, slot, e)
+
+
 def test_step_is_deterministic():
     from model_gb300 import configs
     wl = configs.moist_blob(nx=40, ny=36, nz=20, nsteps=5)
