@@ -354,6 +354,26 @@ def test_random_configuration_vs_oracle(seed):
             assert e <= 1e-10, (seed, f, slot, e)
 
 
+@pytest.mark.parametrize("seed", range(48))
+def test_random_configuration_fp32(seed):
+    """FP32 (the four-level kernels where NZ is a multiple of 4 and the basic
+    state a function of height, the per-level ones elsewhere) against FP64 on
+    the seeded random configurations, within 1e-3 relative L2 after their 2-3
+    steps (the jets' small w sets the bound)"""
+    from tests.test_oracle_random import _case
+    wl, nsteps = _case(7000 + seed)
+    cols = anelastic.build_columns(wl)
+    a = anelastic.Model(wl, abi.GA_PREC_F32, columns=cols)
+    b = anelastic.Model(wl, abi.GA_PREC_F64, columns=cols)
+    a.step(nsteps)
+    b.step(nsteps)
+    for f in range(7 if wl.microphysics_option else 4):
+        x, y = a.get(f), b.get(f)
+        assert np.isfinite(x).all(), (seed, f)
+        e = fx.rel_l2(x, y)
+        assert e <= 1e-3, (seed, abi.PROG_NAMES[f], e)
+
+
 def test_step_is_deterministic():
     from model_gb300 import configs
     wl = configs.moist_blob(nx=40, ny=36, nz=20, nsteps=5)
