@@ -48,8 +48,10 @@ extern "C" {
 #define GA_ERR_NOMEM       -3   /* device allocation failed                   */
 #define GA_ERR_CONFIG      -4   /* configuration rejected (grid too small...) */
 #define GA_ERR_NONFINITE   -5   /* NaN/Inf found by ga_check_finite           */
-#define GA_ERR_KESSLER     -6   /* evaporation E>100, where the reference
-                                   calls exit(0) (kessler.cpp:83-88)          */
+#define GA_ERR_KESSLER     -6   /* microphysics instability where the
+                                   reference calls exit(0): evaporation E>100
+                                   (kessler.cpp:83-88, rutledge.cpp:252-258)
+                                   or snow melting |psmlt|>100 (:370-376)     */
 #define GA_ERR_UNSUPPORTED -7   /* option not built in this library           */
 
 /* ---- precision of a context ------------------------------------------- */
@@ -90,7 +92,19 @@ extern "C" {
 #define GA_QVDIFF  22  /* qv_diffusion (moist contexts)                       */
 #define GA_QCDIFF  23  /* qc_diffusion                                        */
 #define GA_QRDIFF  24  /* qr_diffusion                                        */
-#define GA_SATURATED 25 /* isSaturated of the last Kessler call, as 0 / 1     */
+#define GA_SATURATED 25 /* isSaturated of the last microphysics call, as 0 / 1 */
+/* ice microphysics (microphysics_option 2: run_rutledge_microphysics,
+ * rutledge.cpp:150-452; arrays of microphysics.h:18-24)                     */
+#define GA_QS      26  /* qss/qsps/qsms: snow, three rotation slots           */
+#define GA_QI      27  /* qis/qips/qims: cloud ice, three rotation slots      */
+#define GA_VTS     28  /* sts: snow fall speed                                */
+#define GA_VTI     29  /* its: cloud-ice fall speed; state: the Eulerian
+                        * update keeps it where it is not recomputed
+                        * (rutledge.cpp:580-600)                              */
+#define GA_ACCSNOW 30  /* accSnow[NX][NY]: accumulated snow (2-D)             */
+#define GA_N0S     31  /* N0S: the snow intercept that the last microphysics
+                        * pass left (one value; the snow fall speed reads it,
+                        * rutledge.cpp:197-205, 503-520)                      */
 
 /* rotation slots */
 #define GA_SLOT_CUR 0  /* us  : middle of the RK stage                        */
@@ -108,13 +122,14 @@ extern "C" {
 #define GA_OP_ZERO_MOISTURE     7  /* zero_moisture             microphysics.cpp:675 */
 #define GA_OP_BC                8  /* apply_boundary_condition  boundaries.cpp:119 */
 #define GA_OP_BC_MICRO          9  /* apply_boundary_condition_microphysics boundaries.cpp:200 */
-#define GA_OP_KESSLER          10  /* run_microphysics -> run_kessler_microphysics microphysics.cpp:97, kessler.cpp:25 */
+#define GA_OP_KESSLER          10  /* run_microphysics microphysics.cpp:97: run_kessler_microphysics kessler.cpp:25, or run_rutledge_microphysics rutledge.cpp:150 */
 #define GA_OP_RAYLEIGH         11  /* rayleigh_damping          damping.cpp:1148 */
 #define GA_OP_ADVANCE_INNER    12  /* advance_inner + microphysics_advance_inner solver.cpp:241, microphysics.cpp:642 */
 #define GA_OP_ADVANCE_OUTER    13  /* advance_outer + microphysics_advance       solver.cpp:254, microphysics.cpp:657 */
 #define GA_OP_EXPLICIT_DIFFUSION 14 /* apply_explicit_diffusion  damping.cpp:1125 (on the start-of-step slot) */
 #define GA_OP_TURBULENCE       15  /* calculate_diff_tend(1,NX-1,1,NY-1) turbulence.cpp:158 (needs turbulence_option) */
-#define GA_OP_COUNT            16
+#define GA_OP_ADVECT_ICE       16  /* advect_ice_cell           advection.cpp:508 (microphysics_option 2) */
+#define GA_OP_COUNT            17
 
 /*
  * Runtime configuration: the subset of the reference's struct input_params
@@ -126,7 +141,7 @@ extern "C" {
 typedef struct ga_config {
     int    nx, ny, nz;              /* NX, NY, NZ                                   */
     double dx, dy, dz, dt;          /* grid spacing (m) and time step (s)           */
-    int    microphysics_option;     /* 0 none, 1 Kessler (2 = ice: unsupported)     */
+    int    microphysics_option;     /* 0 none, 1 Kessler, 2 Rutledge-Hobbs ice      */
     int    rain_fallout;            /* 1 Eulerian, 2 semi-Lagrangian (PPM)          */
     int    periodic_ew_boundaries;  /* 0 sponge on all sides, 1 periodic east-west  */
     int    boundary_width_north;    /* jnbuffer  (boundaries.cpp:23-26)             */

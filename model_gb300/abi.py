@@ -32,13 +32,20 @@ TURB_NAMES = {"kmix": GA_KMIX, "khmix": GA_KHMIX, "u_friction": GA_UFRIC, "v_fri
               "w_friction": GA_WFRIC, "t_diffusion": GA_THDIFF, "qv_diffusion": GA_QVDIFF,
               "qc_diffusion": GA_QCDIFF, "qr_diffusion": GA_QRDIFF, "is_saturated": GA_SATURATED}
 
+# ice microphysics (microphysics_option 2): snow and cloud ice with three
+# rotation slots each, their fall speeds, accumulated snow, the snow intercept
+GA_QS, GA_QI, GA_VTS, GA_VTI, GA_ACCSNOW, GA_N0S = range(26, 32)
+# bundle names of the ice fields (microphysics.h:18-25, rutledge.cpp:90)
+ICE_PROG = {"qs": GA_QS, "qi": GA_QI}
+ICE_NAMES = {"sts": GA_VTS, "its": GA_VTI, "accsnow": GA_ACCSNOW, "n0s": GA_N0S}
+
 GA_SLOT_CUR, GA_SLOT_P, GA_SLOT_M = 0, 1, 2
 
 OPS = {
     "sign_cells": 0, "advect_uvw": 1, "solve_pressure": 2, "project": 3,
     "integrate_non_hydro": 4, "advect_theta": 5, "advect_micro": 6, "zero_moisture": 7,
     "bc": 8, "bc_micro": 9, "kessler": 10, "rayleigh": 11, "advance_inner": 12,
-    "advance_outer": 13, "explicit_diffusion": 14, "turbulence": 15,
+    "advance_outer": 13, "explicit_diffusion": 14, "turbulence": 15, "advect_ice": 16,
 }
 
 # names used in bundles / fixtures

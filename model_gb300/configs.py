@@ -191,7 +191,7 @@ def _basic_state(wl: Workload, theta_col, qv_col, u_col):
 
 def _zero_perturbation(wl: Workload):
     n3 = (wl.nx, wl.ny, wl.nz)
-    for k in ("u", "v", "w", "th", "qv", "qc", "qr"):
+    for k in ("u", "v", "w", "th", "qv", "qc", "qr") + (("qs", "qi") if wl.microphysics_option == 2 else ()):
         wl.fields[k] = np.zeros(n3)
 
 
@@ -226,12 +226,13 @@ def dry_bubble(nx=64, ny=64, nz=40, dx=500.0, dz=250.0, dt=2.0, nsteps=100, seed
 
 def thunderstorm(nx=128, ny=128, nz=48, dx=1000.0, dz=400.0, dt=4.0, nsteps=600, seed=1002,
                  amp=3.0, rh=10000.0, rz=1500.0, zc=1500.0, noise=0.05, u_top=15.0,
-                 shear_depth=6000.0, rain_fallout=1, name="thunderstorm") -> Workload:
-    """Kessler moist thunderstorm: thunderstorm_sounding basic state; theta'
-    = amp * (1 + cos(pi r))/2 for r <= 1 with r the distance from (domain
-    centre, zc) scaled by rh horizontally and rz vertically (shape of
-    sample_initializations.py:349-362), plus U(+-noise)."""
-    wl = Workload(name, nx, ny, nz, dx, dx, dz, dt, nsteps, microphysics_option=1,
+                 shear_depth=6000.0, rain_fallout=1, name="thunderstorm", microphysics_option=1) -> Workload:
+    """Moist thunderstorm (Kessler; microphysics_option 2 for the ice scheme
+    of the reference's own thunderstorm inputs): thunderstorm_sounding basic
+    state; theta' = amp * (1 + cos(pi r))/2 for r <= 1 with r the distance
+    from (domain centre, zc) scaled by rh horizontally and rz vertically
+    (shape of sample_initializations.py:349-362), plus U(+-noise)."""
+    wl = Workload(name, nx, ny, nz, dx, dx, dz, dt, nsteps, microphysics_option=microphysics_option,
                   rain_fallout=rain_fallout)
     th, qv, u = thunderstorm_sounding(nz, dz, u_top, shear_depth)
     _basic_state(wl, th, qv, u)
@@ -296,6 +297,43 @@ def moist_blob(nx=24, ny=22, nz=16, dx=1000.0, dz=500.0, dt=4.0, nsteps=3, seed=
     f["qv"] += 1.0e-3 * blob
     f["qc"] += qc * blob * (1.0 + 0.5 * rnd[4])
     f["qr"] += qr * blob * (1.0 + 0.5 * rnd[5])
+    return wl
+
+
+def ice_cloud(nx=24, ny=22, nz=20, dx=1000.0, dz=600.0, dt=4.0, nsteps=3, seed=2101, rain_fallout=1,
+              periodic=0, qc=1.0e-3, qr=1.0e-3, qi=4.0e-4, qs=1.0e-3, zc=5000.0) -> Workload:
+    """Small ice-microphysics case (microphysics_option 2) that reaches the
+    warm, mixed-phase and ice-only branches from the first step: a cloudy,
+    supersaturated blob centred at zc in the thunderstorm sounding (0 C near
+    4 km, -30 C near 8.5 km), 5 km deep in half-width, carrying cloud water,
+    rain, cloud ice and snow, with seeded noise on all perturbation fields.
+    Outside the blob snow is exactly zero, as the snow intercept's update
+    distinguishes."""
+    wl = Workload("ice_cloud", nx, ny, nz, dx, dx, dz, dt, nsteps, microphysics_option=2,
+                  rain_fallout=rain_fallout, periodic_ew_boundaries=periodic,
+                  boundary_width_north=3, boundary_width_south=3, boundary_width_east=3,
+                  boundary_width_west=3)
+    th, qv, u = thunderstorm_sounding(nz, dz, 12.0, 4000.0)
+    _basic_state(wl, th, qv, u)
+    _zero_perturbation(wl)
+    x, y, z = _grid_xyz(nx, ny, nz, dx, dx, dz)
+    xc, yc = 0.5 * nx * dx, 0.5 * ny * dx
+    r = np.sqrt(((x[:, None, None] - xc) / (0.3 * nx * dx)) ** 2
+                + ((y[None, :, None] - yc) / (0.3 * ny * dx)) ** 2
+                + ((z[None, None, :] - zc) / 5000.0) ** 2)
+    blob = np.where(r <= 1.0, 0.5 * (1.0 + np.cos(math.pi * r)), 0.0)
+    f = wl.fields
+    n3 = (nx, ny, nz)
+    rnd = [2.0 * splitmix_uniform(seed + s, wl.points).reshape(n3) - 1.0 for s in range(8)]
+    f["th"] += 2.0 * blob + 0.3 * rnd[0]
+    f["u"] += 2.0 * rnd[1]
+    f["v"] += 2.0 * rnd[2]
+    f["w"] += 0.5 * rnd[3] * blob
+    f["qv"] += 1.0e-3 * blob
+    f["qc"] += qc * blob * (1.0 + 0.5 * rnd[4])
+    f["qr"] += qr * blob * (1.0 + 0.5 * rnd[5])
+    f["qi"] = qi * blob * (1.0 + 0.5 * rnd[6])
+    f["qs"] = qs * blob * (1.0 + 0.5 * rnd[7])
     return wl
 
 
@@ -425,6 +463,7 @@ WORKLOADS = {
     "thunderstorm": thunderstorm,
     "squall_line": squall_line,
     "moist_blob": moist_blob,
+    "ice_cloud": ice_cloud,
     "monsoon_vortex": monsoon_vortex,
     "jet_vortex": jet_vortex,
 }

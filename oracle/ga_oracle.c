@@ -35,7 +35,8 @@ static const double two15ths = 2.0 / 15.0;
 static const double one60ths = 1.0 / 60.0;
 static const double minvar = 1.0e-12; /* kessler.cpp:5 */
 
-enum { F_U, F_V, F_W, F_TH, F_QV, F_QC, F_QR };
+/* prognostic fields; snow and cloud ice follow the seven of GA_U..GA_QR */
+enum { F_U, F_V, F_W, F_TH, F_QV, F_QC, F_QR, F_QS, F_QI, ORA_NF };
 
 struct ora_state {
     ga_config c;
@@ -44,9 +45,14 @@ struct ora_state {
     double dx, dy, dz, dt, dtx, dty, dtz, one_d_dx, one_d_dy, one_d_dz;
     double *zu, *zw, *zsu, *zsw, *mu, *mw, *rhou, *rhow, *one_d_rhou, *one_d_rhow;
     double *tb, *tbv, *tbw, *qb, *pib, *f;
-    double *buf[GA_NPROG][3];
-    double *cur[GA_NPROG], *P[GA_NPROG], *M[GA_NPROG];
+    double *buf[ORA_NF][3];
+    double *cur[ORA_NF], *P[ORA_NF], *M[ORA_NF];
     double *pi, *bar[6], *vt, *accrain;
+    /* ice microphysics (microphysics_option 2): snow and ice fall speeds,
+     * accumulated snow, and the snow intercept N0S, a file-scope variable of
+     * rutledge.cpp:90 that each snowy point of a microphysics pass rewrites */
+    int ice;
+    double *sts, *its, *accsnow, n0s;
     /* pressure solver */
     int ni, nj, nk, ioff;
     double *hcoef;  /* (cos kx + cos ly) - 2, per (p,q) */
@@ -232,7 +238,8 @@ static void op_advect_uvw(ora_state *S, double step)
                 S->P[F_V][IX(i, j, k)] = S->M[F_V][IX(i, j, k)] + step * vt;
             }
     if (S->c.hydrostatic) return; /* advect_uv_velocity (advection.cpp:269-293): no w */
-    /* buoyancy: advection.cpp:329-337 with buoyancy_dry / buoyancy_warm_micro (:42-52) */
+    /* buoyancy: advection.cpp:329-337 with buoyancy_dry / buoyancy_warm_micro /
+     * buoyancy_cold_micro (:42-58) */
     const double *TH = S->cur[F_TH], *tbv = S->tbv;
     const int moist = S->c.microphysics_option != 0;
     for (int i = 3; i < NX - 3; i++)
@@ -248,6 +255,11 @@ static void op_advect_uvw(ora_state *S, double step)
                          QR[IX(i, j, k)];
                     b1 = TH[IX(i, j, k - 1)] / tbv[k - 1] + 0.61 * QV[IX(i, j, k - 1)] -
                          QC[IX(i, j, k - 1)] - QR[IX(i, j, k - 1)];
+                    if (S->ice) {
+                        const double *QI = S->cur[F_QI], *QS = S->cur[F_QS];
+                        b0 = b0 - QI[IX(i, j, k)] - QS[IX(i, j, k)];
+                        b1 = b1 - QI[IX(i, j, k - 1)] - QS[IX(i, j, k - 1)];
+                    }
                 }
                 S->P[F_W][IX(i, j, k)] = S->M[F_W][IX(i, j, k)] + step * S->dt * grav * 0.5 * (b0 + b1);
             }
@@ -302,11 +314,13 @@ static double s_top(const ora_state *S, const double *s, const double *sb, int i
     if (!sb) return wt * st;
     return w1 * bt + wt * st;
 }
-/* rain: interpolate_scalar_with_fallspeed (fluxes.cpp:953-1032) and the qr
- * fluxes of compute_fluxes_moisture (:719-784), incl. the bottom outflow */
-static double r_top(const ora_state *S, const double *s, int i, int j, int k)
+/* a field with a fall speed: interpolate_scalar_with_fallspeed
+ * (fluxes.cpp:953-1032) with the qr fluxes of compute_fluxes_moisture
+ * (:719-784) or compute_fluxes_scalar_with_fallspeed (:699-716), incl. the
+ * bottom outflow */
+static double r_top(const ora_state *S, const double *s, const double *VT, int i, int j, int k)
 {
-    const double *W = S->cur[F_W], *WB = S->bar[2], *VT = S->vt;
+    const double *W = S->cur[F_W], *WB = S->bar[2];
     if (k == 0) {
         double s0 = 0.5 * (s[IX(i, j, 0)] + s[IX(i, j, 1)]);
         return -0.5 * (VT[IX(i, j, 1)] + VT[IX(i, j, 0)]) * s0;
@@ -382,10 +396,83 @@ static void fall_speed(ora_state *S, const double *qr, int il, int ih, int jl, i
         for (int j = jl; j < jh; j++) vt[IX(i, j, 0)] = vt[IX(i, j, 1)];
 }
 
+/* ------------------------------------------------------------------------
+ * Ice microphysics constants (rutledge.cpp:13-147) and fall speeds
+ * (calculate_snow/rain/ice_fall_speed_rutledge, :503-600).
+ * ---------------------------------------------------------------------- */
+static const double Ls = 2.85e6, Lf = 3.50e5;          /* model.h:256-257 */
+static const double rut_tmin = -30 + 273.15, rut_tmax = 0 + 273.15;
+static const double rut_minvar = 1.0e-10;             /* minvar_snow/cice/rain/cwat */
+static const double N0r = 8e6, ERC = 1, M0 = 1e-12, Rstar = 8.314e3, Mw = 18.016, Ka = 2.43e-2,
+                    chi = 2.26e-5, dimax = 500.0e-6, app = 1.139, bexp = 0.11, rhoS = 200, ESC = 1.0,
+                    mu_s = 1.718e-5, ap_lin = 3.0e3;
+static double rut_rfall(void) { return 2115.0 * pow(0.01, 0.2) * 17.83786; } /* rutledge.cpp:140 */
+/* CONVERT_PRESSURE + PBAR (rutledge.cpp:20-24) */
+static double rut_pressure(const ora_state *S, long ix, int k)
+{
+    return (S->c.hydrostatic ? S->pi[ix] : S->pi[ix] / (cp * S->tbv[k])) + S->bar[5][ix];
+}
+static void rut_rain_fall(ora_state *S, double *vtr, const double *qr, int il, int ih, int jl, int jh)
+{
+    const double cpRd = cp / Rd, rfall = rut_rfall();
+    for (int i = il; i < ih; i++)
+        for (int j = jl; j < jh; j++)
+            for (int k = 1; k < S->NZ - 1; k++) {
+                const long ix = IX(i, j, k);
+                if (qr[ix] > rut_minvar) {
+                    double pd = p0 * pow(rut_pressure(S, ix, k), cpRd);
+                    double lambdaR = sqrt(sqrt((trigpi * 1000 * N0r) / (S->rhou[k] * qr[ix])));
+                    vtr[ix] = rfall / (6.0 * pow(lambdaR, 0.8)) * pow(p0 / pd, 0.4);
+                } else
+                    vtr[ix] = 0;
+            }
+    for (int i = il; i < ih; i++)
+        for (int j = jl; j < jh; j++) vtr[IX(i, j, 0)] = vtr[IX(i, j, 1)];
+}
+static void rut_snow_fall(ora_state *S, double *vts, const double *qs, int il, int ih, int jl, int jh)
+{
+    const double cpRd = cp / Rd;
+    for (int i = il; i < ih; i++)
+        for (int j = jl; j < jh; j++)
+            for (int k = 1; k < S->NZ - 1; k++) {
+                const long ix = IX(i, j, k);
+                if (qs[ix] > rut_minvar) {
+                    double pd = p0 * pow(rut_pressure(S, ix, k), cpRd);
+                    double lambdaS = pow((trigpi * rhoS * S->n0s) / (S->rhou[k] * qs[ix]), 0.25);
+                    vts[ix] = app * 1.15 * pow(lambdaS, -bexp) * pow(p0 / pd, 0.4);
+                } else
+                    vts[ix] = 0;
+            }
+    for (int i = il; i < ih; i++)
+        for (int j = jl; j < jh; j++) vts[IX(i, j, 0)] = vts[IX(i, j, 1)];
+}
+/* the ice fall speed is written only where its input exceeds the threshold
+ * and keeps its value elsewhere */
+static void rut_ice_fall(ora_state *S, double *vti, const double *qi, int il, int ih, int jl, int jh)
+{
+    for (int i = il; i < ih; i++)
+        for (int j = jl; j < jh; j++)
+            for (int k = 1; k < S->NZ - 1; k++) {
+                const long ix = IX(i, j, k);
+                if (qi[ix] > rut_minvar) {
+                    double nc = fmin(fmax(5.38e7 * pow(S->rhou[k] * qi[ix], 0.75), 1.0e3), 1.0e6);
+                    double MI = S->rhou[k] * fmax(qi[ix], 0) / nc;
+                    double Dl = fmax(fmin(11.9 * sqrt(MI), dimax), 1.0e-25);
+                    vti[ix] = 1.49e4 * pow(Dl, 1.31);
+                }
+            }
+    for (int i = il; i < ih; i++)
+        for (int j = jl; j < jh; j++) vti[IX(i, j, 0)] = vti[IX(i, j, 1)];
+}
+
 static void op_advect_micro(ora_state *S, double step) /* advection.cpp:451-498 */
 {
     const int NX = S->NX, NY = S->NY, NZ = S->NZ;
-    if (S->c.rain_fallout == 1) fall_speed(S, S->cur[F_QR], 3, NX - 3, 3, NY - 3);
+    /* calculate_eulerian_fall_speed_rain (microphysics.cpp:169-179) */
+    if (S->c.rain_fallout == 1) {
+        if (S->ice) rut_rain_fall(S, S->vt, S->cur[F_QR], 3, NX - 3, 3, NY - 3);
+        else fall_speed(S, S->cur[F_QR], 3, NX - 3, 3, NY - 3);
+    }
     const double *rhow = S->rhow, *one_d_rhou = S->one_d_rhou;
     const double *QC = S->cur[F_QC], *QR = S->cur[F_QR];
     for (int i = 3; i < NX - 3; i++)
@@ -398,10 +485,42 @@ static void op_advect_micro(ora_state *S, double step) /* advection.cpp:451-498 
                 double DTZ = S->dtz * S->mu[k];
                 double tr = -S->dtx * (s_east(S, QR, NULL, i, j, k) - s_east(S, QR, NULL, i - 1, j, k)) -
                             S->dty * (s_north(S, QR, NULL, i, j, k) - s_north(S, QR, NULL, i, j - 1, k)) -
-                            DTZ * (rhow[k + 1] * r_top(S, QR, i, j, k) - rhow[k] * r_top(S, QR, i, j, k - 1)) *
+                            DTZ * (rhow[k + 1] * r_top(S, QR, S->vt, i, j, k) - rhow[k] * r_top(S, QR, S->vt, i, j, k - 1)) *
                                 one_d_rhou[k];
                 S->P[F_QR][ix] = S->M[F_QR][ix] + step * tr;
             }
+}
+
+/* advect_ice_cell (advection.cpp:508-567): snow, then cloud ice, each with
+ * its fall speed; the Eulerian fall speeds first (calculate_eulerian_fall_
+ * speed_snow_ice, microphysics.cpp:188-199), whose ice argument is the
+ * pressure field (advection.cpp:514) */
+static void op_advect_ice(ora_state *S, double step)
+{
+    if (!S->ice) return;
+    const int NX = S->NX, NY = S->NY, NZ = S->NZ;
+    if (S->c.rain_fallout == 1) {
+        rut_ice_fall(S, S->its, S->pi, 3, NX - 3, 3, NY - 3);
+        rut_snow_fall(S, S->sts, S->cur[F_QS], 3, NX - 3, 3, NY - 3);
+    }
+    const double *rhow = S->rhow, *one_d_rhou = S->one_d_rhou;
+    const int fld[2] = {F_QS, F_QI};
+    const double *fall[2] = {S->sts, S->its};
+    for (int n = 0; n < 2; n++) {
+        const double *q = S->cur[fld[n]];
+        for (int i = 3; i < NX - 3; i++)
+            for (int j = 3; j < NY - 3; j++)
+                for (int k = 1; k < NZ - 1; k++) {
+                    const long ix = IX(i, j, k);
+                    double DTZ = S->dtz * S->mu[k];
+                    double t = -S->dtx * (s_east(S, q, NULL, i, j, k) - s_east(S, q, NULL, i - 1, j, k)) -
+                               S->dty * (s_north(S, q, NULL, i, j, k) - s_north(S, q, NULL, i, j - 1, k)) -
+                               DTZ * (rhow[k + 1] * r_top(S, q, fall[n], i, j, k) -
+                                      rhow[k] * r_top(S, q, fall[n], i, j, k - 1)) *
+                                   one_d_rhou[k];
+                    S->P[fld[n]][ix] = S->M[fld[n]][ix] + step * t;
+                }
+    }
 }
 
 static void op_zero_moisture(ora_state *S) /* microphysics.cpp:675-700 */
@@ -411,6 +530,11 @@ static void op_zero_moisture(ora_state *S) /* microphysics.cpp:675-700 */
         if (qc[n] < 0) qc[n] = 0;
     for (long n = 0; n < S->N; n++)
         if (qr[n] < 0) qr[n] = 0;
+    if (S->ice)
+        for (long n = 0; n < S->N; n++) {
+            if (S->P[F_QI][n] < 0) S->P[F_QI][n] = 0;
+            if (S->P[F_QS][n] < 0) S->P[F_QS][n] = 0;
+        }
     for (int i = 1; i < S->NX - 1; i++)
         for (int j = 1; j < S->NY - 1; j++)
             for (int k = 1; k < S->NZ - 1; k++) {
@@ -649,11 +773,11 @@ static void op_bc(ora_state *S)
 static void op_bc_micro(ora_state *S)
 {
     const int per = S->c.periodic_ew_boundaries;
-    const int f3[3] = {F_QV, F_QC, F_QR};
-    for (int n = 0; n < 3; n++) sponge(S, S->P[f3[n]], per);
+    const int f5[5] = {F_QV, F_QC, F_QR, F_QI, F_QS}, nf = S->ice ? 5 : 3;
+    for (int n = 0; n < nf; n++) sponge(S, S->P[f5[n]], per);
     if (per)
-        for (int n = 0; n < 3; n++) periodic_ew(S, S->P[f3[n]]);
-    for (int n = 0; n < 3; n++) upper_lower(S, S->P[f3[n]]);
+        for (int n = 0; n < nf; n++) periodic_ew(S, S->P[f5[n]]);
+    for (int n = 0; n < nf; n++) upper_lower(S, S->P[f5[n]]);
 }
 
 static void op_rayleigh(ora_state *S) /* damping.cpp:1148-1177 */
@@ -762,7 +886,8 @@ static double wk6(const double *v, long c, const double *w)
 
 static void op_explicit_diffusion(ora_state *S, double step)
 {
-    const int order = S->c.diffusion_order, nf = S->c.microphysics_option ? 7 : 4, NZ = S->NZ;
+    const int order = S->c.diffusion_order, NZ = S->NZ;
+    const int nf = S->ice ? ORA_NF : S->c.microphysics_option ? 7 : 4; /* damping.cpp:1016-1021 */
     if (order != 2 && order != 4 && order != 6) return;
     const double kh = S->c.kdiffh, kv = S->c.kdiffv;
     const long sx = (long)S->NY * S->NZ, sy = S->NZ;
@@ -1284,11 +1409,10 @@ static double ppm_remap(ora_state *S, const double *zin, const double *zout, con
         }
     return rainfall;
 }
-static void fallout(ora_state *S)
+static void fallout(ora_state *S, double *var, const double *vel, double *acc)
 {
     const int NZ = S->NZ;
-    double *var = S->P[F_QR];
-    const double *vel = S->vt, *ZW = S->zsw;
+    const double *ZW = S->zsw;
     const double DeCFL0 = 0.05, dt = S->dt;
     double *ZA = S->za, *QA = S->qa, *QD = S->qd, *Ve = S->ve;
     for (int k = 0; k < NZ; k++) { ZA[k] = ZW[k]; Ve[k] = 0; QD[k] = 0; QA[k] = 0; }
@@ -1308,7 +1432,7 @@ static void fallout(ora_state *S)
             for (int k = 0; k < NZ - 1; k++) ZA[k] = ZW[k] - dt * Ve[k];
             for (int k = 0; k < NZ - 1; k++)
                 QA[k] = S->rhou[k] * var[IX(i, j, k)] * (ZW[k + 1] - ZW[k]) / (ZA[k + 1] - ZA[k]);
-            S->accrain[IX2(i, j)] += ppm_remap(S, ZA, ZW, QA, QD, NZ);
+            acc[IX2(i, j)] += ppm_remap(S, ZA, ZW, QA, QD, NZ);
             for (int k = 0; k < NZ; k++) var[IX(i, j, k)] = QD[k] * S->one_d_rhou[k];
         }
 }
@@ -1319,7 +1443,7 @@ static void op_kessler(ora_state *S) /* run_microphysics(1,NX-1,1,NY-1) */
     kessler_points(S);
     if (S->c.rain_fallout == 2) {
         fall_speed(S, S->P[F_QR], 1, S->NX - 1, 1, S->NY - 1);
-        fallout(S);
+        fallout(S, S->P[F_QR], S->vt, S->accrain);
         memset(S->vt, 0, sizeof(double) * S->N);
     } else {
         /* precip_rate (microphysics.cpp:143-160) */
@@ -1329,6 +1453,249 @@ static void op_kessler(ora_state *S) /* run_microphysics(1,NX-1,1,NY-1) */
                                          (S->vt[IX(i, j, 0)] + S->vt[IX(i, j, 1)]) * 0.5 *
                                          (S->P[F_QR][IX(i, j, 0)] + S->P[F_QR][IX(i, j, 1)]) * S->dt;
     }
+}
+
+/* ------------------------------------------------------------------------
+ * Ice microphysics: run_rutledge_microphysics (rutledge.cpp:150-452), the
+ * point processes of Rutledge and Hobbs (1983) with the changes of Hong et
+ * al. (2004), then saturation_adjustment (:700-820) with get_qvsat (:611-693),
+ * zero_moisture, and the rain, ice and snow fallout.
+ * ---------------------------------------------------------------------- */
+#define RUT_ESL(t) (611.2 * exp(17.67 * ((t) - 273.15) / ((t) - 29.65)))      /* SAT_VAP_WAT */
+#define RUT_ESI(t) (611.2 * exp(21.8745584 * ((t) - 273.15) / ((t) - 7.66))) /* SAT_VAP_ICE */
+#define RUT_QSAT(e, p) (0.62197 * (e) / ((p) - (e)))                         /* SAT_MIX_RATIO */
+#define RUT_ALPHA(x) (1.0 + ((x) - 273.15) / (rut_tmax - rut_tmin))
+
+static void rutledge_points(ora_state *S)
+{
+    const double cpRd = cp / Rd, dt = S->dt;
+    const double a0 = -0.267, a1 = 5.15e3, a2 = -1.0225e6, a3 = 7.55e7; /* rain fall-speed polynomial */
+    double *THP = S->P[F_TH], *QVP = S->P[F_QV], *QCP = S->P[F_QC], *QRP = S->P[F_QR];
+    double *QIP = S->P[F_QI], *QSP = S->P[F_QS];
+    const double *THBAR = S->bar[3], *QBAR = S->bar[4];
+    for (int i = 1; i < S->NX - 1; i++)
+        for (int j = 1; j < S->NY - 1; j++)
+            for (int k = 1; k < S->NZ - 1; k++) {
+                const long ix = IX(i, j, k);
+                const double rhou = S->rhou[k], odr = S->one_d_rhou[k];
+                double theta = THP[ix] + THBAR[ix] + S->tb[k];
+                double pressure = rut_pressure(S, ix, k);
+                double vapor = QVP[ix] + QBAR[ix] + S->qb[k];
+                double temperature = theta * pressure;
+                double pd = p0 * pow(pressure, cpRd);
+                double esl = RUT_ESL(temperature), esi = RUT_ESI(temperature);
+                double qvl_sat = RUT_QSAT(esl, pd), qvi_sat = RUT_QSAT(esi, pd);
+                double pcond = 0, lambdaS, lambdaR, var, Ap, Bp, App = 0, Bpp = 0;
+                if (QSP[ix] != 0) {
+                    S->n0s = fmin(2.0e6 * exp(0.12 * (273.16 - temperature)), 2.0e8);
+                    lambdaS = sqrt(sqrt((trigpi * rhoS * S->n0s) / (rhou * QSP[ix])));
+                } else
+                    lambdaS = 0;
+                const double N0S = S->n0s;
+                /* rain: autoconversion, accretion, evaporation, freezing */
+                double A = 0, B = 0, E = 0, prfrz = 0;
+                if (QCP[ix] > 1.0e-3) A = 0.001 * (QCP[ix] - 1.0e-3) * dt;
+                if (QRP[ix] > rut_minvar) {
+                    lambdaR = pow((trigpi * 1000 * N0r) / (rhou * QRP[ix]), 0.25);
+                    B = 0.25 * trigpi * QCP[ix] * ERC * N0r * pow(p0 / pd, 0.4) * 2 / pow(lambdaR, 3) *
+                        (a0 + a1 * 3 / lambdaR + a2 * 12 / (lambdaR * lambdaR) +
+                         a3 * 60 / (lambdaR * lambdaR * lambdaR)) *
+                        dt;
+                    Ap = (Lv / (Ka * temperature)) * ((Lv * Mw) / (Rstar * temperature) - 1);
+                    Bp = Rstar * temperature / (chi * Mw * esl);
+                    var = 0.78 / (lambdaR * lambdaR) +
+                          0.31 * sqrt(ap_lin * rhou / mu_s) / (lambdaR * lambdaR * lambdaR) * 2.0 * pow((p0 / pd), 0.2);
+                    E = var * 2 * trigpi * N0r * (vapor / qvl_sat - 1.0) / (Ap + Bp) * dt * odr;
+                    if (temperature < 273.16) {
+                        prfrz = 20 * trigpi * trigpi * 100.0 * N0r * (1000.0 / rhou) *
+                                exp(0.66 * (273.16 - temperature) - 1) /
+                                (lambdaR * lambdaR * lambdaR * lambdaR * lambdaR * lambdaR * lambdaR);
+                        prfrz = fmin(prfrz * odr * dt, QRP[ix]);
+                    }
+                    if (E > 100) S->err = GA_ERR_KESSLER;
+                }
+                /* cloud ice: initiation, deposition, autoconversion to snow,
+                 * collection by snow, melting */
+                double pint = 0, pdepi = 0, pconv = 0, psaci = 0, psmlti = 0;
+                if (temperature < 273.16) {
+                    double nc0 = 1.0e3 * exp(0.1 * (273.16 - temperature));
+                    double nc = fmin(fmax(5.38e7 * pow(rhou * QIP[ix], 0.75), 1.0e3), 1.0e6);
+                    if (qvi_sat < vapor) pint = fmin(M0 * nc0 / rhou, vapor - qvi_sat);
+                    if (QIP[ix] > rut_minvar || QSP[ix] > rut_minvar) {
+                        App = (Lv / (Ka * temperature)) * ((Ls * Mw) / (Rstar * temperature) - 1);
+                        Bpp = Rstar * temperature / (chi * Mw * esi);
+                        double MI = rhou * QIP[ix] / nc;
+                        double Dl = 11.3 * sqrt(MI);
+                        pdepi = (4 * Dl * (vapor / qvi_sat - 1) * nc) / (App + Bpp) * odr * dt;
+                    }
+                    if (QIP[ix] > rut_minvar) {
+                        double qimax;
+                        if (temperature > 233.16 && pd > 30000) qimax = 8.0e-5 * odr;
+                        else qimax = 0.18e-3;
+                        if (QIP[ix] > qimax) pconv = QIP[ix] - qimax;
+                    }
+                    if (QIP[ix] > rut_minvar && lambdaS > 1e-15) {
+                        double ESI = exp(0.05 * (temperature - 273.16));
+                        psaci = (trigpi * app * QIP[ix] * ESI * N0S) / 4 * pow(p0 / pd, 0.4) * 2.22 /
+                                pow(lambdaS, 3.11) * dt;
+                    }
+                } else
+                    psmlti = QIP[ix];
+                /* snow: melting, deposition, evaporation of melting snow */
+                double psmlt = 0, psdep = 0, pmltev = 0;
+                if (QSP[ix] > rut_minvar && lambdaS > 1e-15) {
+                    var = 0.65 / (lambdaS * lambdaS) +
+                          0.44 * sqrt(app * rhou / mu_s) * pow(p0 / pd, 0.2) * 1.383 / pow(lambdaS, 2.555);
+                    if (temperature > 273.16) {
+                        psmlt = -(2 * trigpi * N0S / Lf) * Ka * (temperature - 273.16) * var;
+                        psmlt = dt * psmlt * odr;
+                    }
+                    if (temperature < 273.16) {
+                        psdep = 4 * (vapor / qvi_sat - 1) * N0S / (App + Bpp) * var;
+                        psdep = dt * psdep * odr;
+                    }
+                    if (temperature >= 273.16) {
+                        Ap = (Lv / (Ka * temperature)) * ((Lv * Mw) / (Rstar * temperature) - 1);
+                        Bp = Rstar * temperature / (chi * Mw * esl);
+                        pmltev = 4 * (vapor / qvl_sat - 1) * N0S / (Ap + Bp) * var;
+                        pmltev = dt * pmltev * odr;
+                    }
+                    if (fabs(psmlt) > 100) S->err = GA_ERR_KESSLER;
+                }
+                /* cloud water collected by snow, frozen below tmin */
+                double psacw_cold = 0, psacw_warm = 0;
+                if (QCP[ix] > rut_minvar && lambdaS > 1e-15) {
+                    double psacw = (trigpi * app * QCP[ix] * ESC * N0S) / 4 * pow(p0 / pd, 0.4) * 2.22 /
+                                   pow(lambdaS, 3.11) * dt;
+                    if (temperature < 273.16) psacw_cold = psacw;
+                    else psacw_warm = psacw;
+                }
+                double pcfrz = 0;
+                if (temperature < rut_tmin) pcfrz = QCP[ix];
+                double pint_p_pdepi = fmin(pint + pdepi, vapor);
+                pint_p_pdepi = -fmin(-pint_p_pdepi, QIP[ix]);
+                QVP[ix] += -(pcond + E + psdep + pmltev + pint_p_pdepi);
+                QCP[ix] += pcond + psmlti - A - B - psacw_warm - psacw_cold - pcfrz;
+                QIP[ix] += pint_p_pdepi - psmlti - psaci - pconv + pcfrz;
+                QRP[ix] += E + A + B - psmlt + psacw_warm - prfrz;
+                QSP[ix] += psdep + pmltev + psaci + psmlt + psacw_cold + pconv + prfrz;
+                double diabatic = Lv / (cp * S->pib[k]) * (pcond + E + pmltev) +
+                                  Ls / (cp * S->pib[k]) * (pint_p_pdepi + psdep) +
+                                  Lf / (cp * S->pib[k]) * (psmlt + psmlti + psacw_cold + pcfrz + prfrz);
+                THP[ix] += diabatic;
+            }
+}
+
+/* get_qvsat (rutledge.cpp:611-693): saturation mixing ratio over water, ice
+ * or the temperature-weighted mix, and the latent-heating correction terms;
+ * pow(x,2) is folded to x*x by the reference's compiler */
+static double rut_qvsat(double T, double pd, double *phi, double *phil, double *phii)
+{
+    double qvsat;
+    if (T > rut_tmax) {
+        double esl = RUT_ESL(T);
+        qvsat = RUT_QSAT(esl, pd);
+        double f = 17.67 * (273.15 - 29.65) * Lv / cp, tm = T - 29.65;
+        *phi = *phil = *phii = pd / (pd - esl) * qvsat * f / (tm * tm);
+    } else if (T < rut_tmin) {
+        double esl = RUT_ESI(T);
+        qvsat = RUT_QSAT(esl, pd);
+        double f = 21.8745584 * (273.15 - 7.66) * Ls / cp, tm = T - 7.66;
+        *phi = *phil = *phii = pd / (pd - esl) * qvsat * f / (tm * tm);
+    } else {
+        double esl = RUT_ESL(T), esi = RUT_ESI(T);
+        double qvl_sat = RUT_QSAT(esl, pd), qvi_sat = RUT_QSAT(esi, pd);
+        double fl = 17.67 * (273.15 - 29.65) * Lv / cp, fi = 21.8745584 * (273.15 - 7.66) * Ls / cp;
+        double tl = T - 29.65, ti = T - 7.66;
+        *phil = pd / (pd - esl) * qvl_sat * fl / (tl * tl);
+        *phii = pd / (pd - esi) * qvi_sat * fi / (ti * ti);
+        qvsat = RUT_ALPHA(T) * qvl_sat + (1.0 - RUT_ALPHA(T)) * qvi_sat;
+        *phi = RUT_ALPHA(T) * *phil + (1.0 - RUT_ALPHA(T)) * *phii;
+    }
+    return qvsat;
+}
+
+static void rut_saturation_adjustment(ora_state *S)
+{
+    const double cpRd = cp / Rd;
+    double *THP = S->P[F_TH], *QVP = S->P[F_QV], *QCP = S->P[F_QC], *QIP = S->P[F_QI];
+    for (int i = 1; i < S->NX - 1; i++)
+        for (int j = 1; j < S->NY - 1; j++)
+            for (int k = 1; k < S->NZ - 1; k++) {
+                const long ix = IX(i, j, k);
+                double theta = THP[ix] + S->bar[3][ix] + S->tb[k];
+                double pressure = rut_pressure(S, ix, k);
+                double vapor = QVP[ix] + S->bar[4][ix] + S->qb[k];
+                double T = theta * pressure;
+                double pd = p0 * pow(pressure, cpRd);
+                double phi, phil, phii;
+                double qvsat = rut_qvsat(T, pd, &phi, &phil, &phii);
+                double Cl = 0, Ci = 0;
+                if (vapor > qvsat) {
+                    if (T > rut_tmax) Cl = (vapor - qvsat) / (1.0 + phi);
+                    else if (T < rut_tmin) Ci = (vapor - qvsat) / (1.0 + phi);
+                    else {
+                        Cl = RUT_ALPHA(T) * (vapor - qvsat) / (1.0 + phi);
+                        Ci = (1.0 - RUT_ALPHA(T)) * (vapor - qvsat) / (1.0 + phi);
+                    }
+                    if (S->sat) S->sat[ix] = 1;
+                } else if (vapor < qvsat && (QCP[ix] + QIP[ix]) > 0) {
+                    if (T > rut_tmax) Cl = -fmin(QCP[ix], (qvsat - vapor) / (1.0 + phi));
+                    else if (T < rut_tmin) Ci = -fmin(QIP[ix], (qvsat - vapor) / (1.0 + phi));
+                    else {
+                        Cl = -fmin(QCP[ix], (qvsat - vapor) / (1.0 + phil));
+                        if (Cl + QCP[ix] <= 0) Ci = -fmin(QIP[ix], (qvsat - vapor + Cl) / (1.0 + phii));
+                    }
+                    if (S->sat) S->sat[ix] = -(Ci + Cl) < QCP[ix] + QIP[ix];
+                } else if (S->sat) {
+                    S->sat[ix] = vapor == qvsat;
+                }
+                QIP[ix] += Ci;
+                QCP[ix] += Cl;
+                QVP[ix] -= (Ci + Cl);
+                double diabatic = (Lv / (cp * S->pib[k])) * Cl + (Ls / (cp * S->pib[k])) * Ci;
+                THP[ix] += diabatic;
+            }
+}
+
+static void op_rutledge(ora_state *S)
+{
+    const int NX = S->NX, NY = S->NY;
+    rutledge_points(S);
+    rut_saturation_adjustment(S);
+    op_zero_moisture(S);
+    if (S->c.rain_fallout == 2) {
+        rut_snow_fall(S, S->sts, S->P[F_QS], 1, NX - 1, 1, NY - 1);
+        rut_ice_fall(S, S->its, S->P[F_QI], 1, NX - 1, 1, NY - 1);
+        rut_rain_fall(S, S->vt, S->P[F_QR], 1, NX - 1, 1, NY - 1);
+        fallout(S, S->P[F_QR], S->vt, S->accrain);
+        fallout(S, S->P[F_QI], S->its, S->accsnow);
+        fallout(S, S->P[F_QS], S->sts, S->accsnow);
+        memset(S->vt, 0, sizeof(double) * S->N);
+        memset(S->sts, 0, sizeof(double) * S->N);
+        memset(S->its, 0, sizeof(double) * S->N);
+    } else {
+        /* precip_rate (microphysics.cpp:143-160) of rain, of rain at the snow
+         * fall speed, and of ice at the snow fall speed (rutledge.cpp:486-489) */
+        for (int i = 1; i < NX - 1; i++)
+            for (int j = 1; j < NY - 1; j++) {
+                const double r = S->rhow[1];
+                const double *qr = S->P[F_QR], *qi = S->P[F_QI];
+                S->accrain[IX2(i, j)] += r * 0.5 * (S->vt[IX(i, j, 0)] + S->vt[IX(i, j, 1)]) * 0.5 *
+                                         (qr[IX(i, j, 0)] + qr[IX(i, j, 1)]) * S->dt;
+                S->accsnow[IX2(i, j)] += r * 0.5 * (S->sts[IX(i, j, 0)] + S->sts[IX(i, j, 1)]) * 0.5 *
+                                         (qr[IX(i, j, 0)] + qr[IX(i, j, 1)]) * S->dt;
+                S->accsnow[IX2(i, j)] += r * 0.5 * (S->sts[IX(i, j, 0)] + S->sts[IX(i, j, 1)]) * 0.5 *
+                                         (qi[IX(i, j, 0)] + qi[IX(i, j, 1)]) * S->dt;
+            }
+    }
+}
+
+/* run_microphysics (microphysics.cpp:97-131) over (1,NX-1,1,NY-1) */
+static void op_microphysics(ora_state *S)
+{
+    if (S->ice) op_rutledge(S);
+    else op_kessler(S);
 }
 
 /* ------------------------------------------------------------------------
@@ -1347,7 +1714,8 @@ static void advance_inner(ora_state *S) /* solver.cpp:240-248: w stays put when 
 }
 static void micro_advance_inner(ora_state *S)
 {
-    for (int f = 4; f < 7; f++) swap_f(S, f);
+    const int nf = S->ice ? ORA_NF : 7;
+    for (int f = 4; f < nf; f++) swap_f(S, f);
 }
 static void advance_outer(ora_state *S)
 {
@@ -1357,7 +1725,8 @@ static void advance_outer(ora_state *S)
 }
 static void micro_advance(ora_state *S)
 {
-    for (int f = 4; f < 7; f++) memcpy(S->M[f], S->P[f], sizeof(double) * S->N);
+    const int nf = S->ice ? ORA_NF : 7;
+    for (int f = 4; f < nf; f++) memcpy(S->M[f], S->P[f], sizeof(double) * S->N);
     micro_advance_inner(S);
 }
 
@@ -1550,6 +1919,7 @@ static void rk3_step(ora_state *S) /* driver_serial.cpp:178-286 */
         if (turb) turb_apply_theta(S, steps[s]);
         if (micro) {
             op_advect_micro(S, steps[s]);
+            if (S->ice) op_advect_ice(S, steps[s]); /* driver_serial.cpp:229 */
             if (turb) turb_apply_moisture(S, steps[s]);
             op_zero_moisture(S);
         }
@@ -1562,7 +1932,7 @@ static void rk3_step(ora_state *S) /* driver_serial.cpp:178-286 */
         if (s < 2) advance_inner(S);
     }
     if (micro) {
-        op_kessler(S);
+        op_microphysics(S);
         op_bc_micro(S);
         micro_advance(S);
     }
@@ -1733,7 +2103,7 @@ ora_state *ora_create(const ga_config *cfg, const ga_columns *cols)
     S->tb = dup_col(cols->tb, NZ); S->tbv = dup_col(cols->tbv, NZ); S->tbw = dup_col(cols->tbw, NZ);
     S->qb = dup_col(cols->qb, NZ); S->pib = dup_col(cols->pib, NZ);
     S->f = dup_col(cols->f, NY);
-    for (int f = 0; f < GA_NPROG; f++) {
+    for (int f = 0; f < ORA_NF; f++) {
         for (int s = 0; s < 3; s++) S->buf[f][s] = (double *)calloc((size_t)S->N, sizeof(double));
         S->cur[f] = S->buf[f][0];
         S->P[f] = S->buf[f][1];
@@ -1743,6 +2113,11 @@ ora_state *ora_create(const ga_config *cfg, const ga_columns *cols)
     for (int b = 0; b < 6; b++) S->bar[b] = (double *)calloc((size_t)S->N, sizeof(double));
     S->vt = (double *)calloc((size_t)S->N, sizeof(double));
     S->accrain = (double *)calloc((size_t)NX * NY, sizeof(double));
+    S->ice = cfg->microphysics_option == 2;
+    S->sts = (double *)calloc((size_t)S->N, sizeof(double));
+    S->its = (double *)calloc((size_t)S->N, sizeof(double));
+    S->accsnow = (double *)calloc((size_t)NX * NY, sizeof(double));
+    S->n0s = 8e6; /* rutledge.cpp:90 */
     /* pressure solver set-up: initialize_pressure_solver (pressure.cpp:99-134) */
     S->ni = cfg->periodic_ew_boundaries ? NX - 6 : NX;
     S->nj = NY;
@@ -1816,8 +2191,9 @@ void ora_destroy(ora_state *S)
     double *cols[] = {S->zu, S->zw, S->zsu, S->zsw, S->mu, S->mw, S->rhou, S->rhow, S->one_d_rhou,
                       S->one_d_rhow, S->tb, S->tbv, S->tbw, S->qb, S->pib, S->f};
     for (unsigned n = 0; n < sizeof(cols) / sizeof(cols[0]); n++) free(cols[n]);
-    for (int f = 0; f < GA_NPROG; f++)
+    for (int f = 0; f < ORA_NF; f++)
         for (int s = 0; s < 3; s++) free(S->buf[f][s]);
+    free(S->sts); free(S->its); free(S->accsnow);
     free(S->pi);
     for (int b = 0; b < 6; b++) free(S->bar[b]);
     free(S->vt); free(S->accrain);
@@ -1855,6 +2231,20 @@ static double *field_ptr(ora_state *S, int field, int slot, long *n)
     case GA_KHMIX: return S->khmix;
     case GA_UFRIC: case GA_VFRIC: case GA_WFRIC: case GA_THDIFF: case GA_QVDIFF: case GA_QCDIFF: case GA_QRDIFF:
         return S->ttend[field - GA_UFRIC];
+    }
+    if (!S->ice) return NULL;
+    switch (field) {
+    case GA_QS: case GA_QI: {
+        const int f = field == GA_QS ? F_QS : F_QI;
+        if (slot == GA_SLOT_CUR) return S->cur[f];
+        if (slot == GA_SLOT_P) return S->P[f];
+        if (slot == GA_SLOT_M) return S->M[f];
+        return NULL;
+    }
+    case GA_VTS: return S->sts;
+    case GA_VTI: return S->its;
+    case GA_ACCSNOW: *n = (long)S->NX * S->NY; return S->accsnow;
+    case GA_N0S: *n = 1; return &S->n0s;
     }
     return NULL;
 }
@@ -1909,7 +2299,11 @@ int ora_op(ora_state *S, int op, double step)
     case GA_OP_ZERO_MOISTURE: op_zero_moisture(S); return GA_OK;
     case GA_OP_BC: op_bc(S); return GA_OK;
     case GA_OP_BC_MICRO: op_bc_micro(S); return GA_OK;
-    case GA_OP_KESSLER: op_kessler(S); return S->err;
+    case GA_OP_KESSLER: op_microphysics(S); return S->err;
+    case GA_OP_ADVECT_ICE:
+        if (!S->ice) return GA_ERR_ARG;
+        op_advect_ice(S, step);
+        return GA_OK;
     case GA_OP_RAYLEIGH: op_rayleigh(S); return GA_OK;
     case GA_OP_ADVANCE_INNER: advance_inner(S); if (S->c.microphysics_option) micro_advance_inner(S); return GA_OK;
     case GA_OP_ADVANCE_OUTER: advance_outer(S); if (S->c.microphysics_option) micro_advance(S); return GA_OK;

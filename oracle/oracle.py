@@ -119,7 +119,8 @@ class Oracle:
             raise RuntimeError(f"ora_set_field({field},{slot}) -> {rc}")
 
     def get(self, field: int, slot: int = 0) -> np.ndarray:
-        n = self.wl.nx * self.wl.ny if field == abi.GA_ACCRAIN else self.n3
+        n = self.wl.nx * self.wl.ny if field in (abi.GA_ACCRAIN, abi.GA_ACCSNOW) else \
+            1 if field == abi.GA_N0S else self.n3
         a = np.zeros(n)
         rc = lib().ora_get_field(self.h, field, slot, _ptr(a), n)
         if rc != 0:
@@ -138,6 +139,12 @@ class Oracle:
             self.set(f, abi.GA_SLOT_M, arr)
         if "accrain" in fields:
             self.set(abi.GA_ACCRAIN, 0, fields["accrain"])
+        if self.wl.microphysics_option == 2:
+            for name, fid in abi.ICE_PROG.items():
+                self.set(fid, abi.GA_SLOT_CUR, fields[name])
+                self.set(fid, abi.GA_SLOT_M, fields[name])
+            if "accsnow" in fields:
+                self.set(abi.GA_ACCSNOW, 0, fields["accsnow"])
 
     def step(self, n: int = 1) -> int:
         return lib().ora_step(self.h, n)
@@ -157,6 +164,12 @@ class Oracle:
         out["pi"] = self.get(abi.GA_PI)
         out["vt"] = self.get(abi.GA_VT)
         out["accrain"] = self.get(abi.GA_ACCRAIN)
+        if self.wl.microphysics_option == 2:
+            for name, fid in abi.ICE_PROG.items():
+                for slot, suf in abi.SLOT_SUFFIX.items():
+                    out[name + suf] = self.get(fid, slot)
+            for name, fid in abi.ICE_NAMES.items():
+                out[name] = self.get(fid)
         return out
 
 

@@ -42,6 +42,7 @@ void integrate_hydro(double, int, int, int, int, int);
 extern double *Kmix, *KHmix;  /* turbulence.cpp: mixing coefficients */
 extern bool *isSaturated;     /* turbulence.cpp: Kessler saturation record */
 void zero_moisture(int il, int ih, int jl, int jh, int size);
+extern double N0S;            /* rutledge.cpp: snow intercept of the last snowy point */
 void column_average_density();
 
 /* globals normally defined by files.cpp */
@@ -182,8 +183,14 @@ int main(int argc, char **argv)
         load(in, "qr", qrs, N);
         load(in, "accrain", accRain, (size_t)NX * NY);
     }
+    if (USE_ICE) {
+        load(in, "qs", qss, N);
+        load(in, "qi", qis, N);
+        load(in, "accsnow", accSnow, (size_t)NX * NY);
+    }
     memcpy(ums, us, N * 8); memcpy(vms, vs, N * 8); memcpy(wms, ws, N * 8); memcpy(thms, ths, N * 8);
     if (USE_MICROPHYSICS) { memcpy(qvms, qvs, N * 8); memcpy(qcms, qcs, N * 8); memcpy(qrms, qrs, N * 8); }
+    if (USE_ICE) { memcpy(qsms, qss, N * 8); memcpy(qims, qis, N * 8); }
     /* explicit slot overrides (per-operator tests set all three buffers) */
     load(in, "u_p", ups, N); load(in, "v_p", vps, N); load(in, "w_p", wps, N); load(in, "th_p", thps, N);
     load(in, "u_m", ums, N); load(in, "v_m", vms, N); load(in, "w_m", wms, N); load(in, "th_m", thms, N);
@@ -192,6 +199,12 @@ int main(int argc, char **argv)
         load(in, "qv_p", qvps, N); load(in, "qc_p", qcps, N); load(in, "qr_p", qrps, N);
         load(in, "qv_m", qvms, N); load(in, "qc_m", qcms, N); load(in, "qr_m", qrms, N);
         load(in, "vt", vts, N);
+    }
+    if (USE_ICE) {
+        load(in, "qs_p", qsps, N); load(in, "qi_p", qips, N);
+        load(in, "qs_m", qsms, N); load(in, "qi_m", qims, N);
+        load(in, "sts", sts, N); load(in, "its", its, N);
+        if (has(in, "n0s")) N0S = scal(in, "n0s");
     }
     /* rest of initialize_serial (driver_serial.cpp:44-76) */
     if (USE_TURBULENT_STRESS) {
@@ -244,6 +257,7 @@ int main(int argc, char **argv)
         else if (name == "rayleigh") rayleigh_damping(1, NX - 1, 1, NY - 1, raydampheight);
         else if (name == "explicit_diffusion") apply_explicit_diffusion(step, 3, NX - 3, 3, NY - 3);
         else if (name == "turbulence") calculate_diff_tend(1, NX - 1, 1, NY - 1);  /* driver_serial.cpp:194 */
+        else if (name == "advect_ice") advect_ice_cell(step, 3, NX - 3, 3, NY - 3);  /* driver_serial.cpp:229 */
         else { fprintf(stderr, "unknown op %s\n", name.c_str()); return 2; }
     } else {
         fprintf(stderr, "unknown mode\n");
@@ -262,6 +276,13 @@ int main(int argc, char **argv)
         out["qr"] = grab(qrs, N); out["qr_p"] = grab(qrps, N); out["qr_m"] = grab(qrms, N);
         out["vt"] = grab(vts, N);
         out["accrain"] = grab(accRain, (size_t)NX * NY);
+    }
+    if (USE_ICE) {
+        out["qs"] = grab(qss, N); out["qs_p"] = grab(qsps, N); out["qs_m"] = grab(qsms, N);
+        out["qi"] = grab(qis, N); out["qi_p"] = grab(qips, N); out["qi_m"] = grab(qims, N);
+        out["sts"] = grab(sts, N); out["its"] = grab(its, N);
+        out["accsnow"] = grab(accSnow, (size_t)NX * NY);
+        out["n0s"] = std::vector<double>(1, N0S);
     }
     out["zu"] = grab(zu, NZ); out["zw"] = grab(zw, NZ); out["zsu"] = grab(zsu, NZ); out["zsw"] = grab(zsw, NZ);
     out["mu"] = grab(mu, NZ); out["mw"] = grab(mw, NZ);

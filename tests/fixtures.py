@@ -57,6 +57,10 @@ def linop_names():
     return sorted(f[:-4] for f in os.listdir(GOLDEN) if f.startswith("linop_") and f.endswith(".npz"))
 
 
+def iceop_names():
+    return sorted(f[:-4] for f in os.listdir(GOLDEN) if f.startswith("iceop_") and f.endswith(".npz"))
+
+
 def hydop_names():
     return sorted(f[:-4] for f in os.listdir(GOLDEN) if f.startswith("hydop_") and f.endswith(".npz"))
 
@@ -69,8 +73,8 @@ def slot_extra(d: dict) -> dict:
     """Per-slot input arrays of an ops fixture (u_p, u_m, ..., pi, vt)."""
     out = {}
     for k in d:
-        if k.startswith("in_") and (k.endswith("_p") or k.endswith("_m") or k in ("in_pi", "in_vt",
-                                                                                    "in_is_saturated")):
+        if k.startswith("in_") and (k.endswith("_p") or k.endswith("_m") or k in (
+                "in_pi", "in_vt", "in_is_saturated", "in_sts", "in_its", "in_n0s")):
             out[k[3:]] = d[k]
     return out
 
@@ -83,6 +87,11 @@ FIELD_OF["pi"] = (abi.GA_PI, 0)
 FIELD_OF["vt"] = (abi.GA_VT, 0)
 FIELD_OF["accrain"] = (abi.GA_ACCRAIN, 0)
 for _n, _f in abi.TURB_NAMES.items():
+    FIELD_OF[_n] = (_f, 0)
+for _n, _f in abi.ICE_PROG.items():
+    for _slot, _suf in abi.SLOT_SUFFIX.items():
+        FIELD_OF[_n + _suf] = (_f, _slot)
+for _n, _f in abi.ICE_NAMES.items():
     FIELD_OF[_n] = (_f, 0)
 
 

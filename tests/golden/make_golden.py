@@ -10,6 +10,7 @@ inputs and outputs as compressed .npz files:
   turb_<case>.npz  the turbulence tendencies (calculate_diff_tend) of such a
                    state, and Kessler's saturation record
   linop_<case>.npz the linearised model's operators (the ISLINEAR build)
+  iceop_<case>.npz the operators of the ice microphysics (microphysics_option 2)
 
 Usage (where the reference sources exist):  python tests/golden/make_golden.py
 The fixtures are then read by tests/test_golden_oracle.py (CPU) and
@@ -51,6 +52,10 @@ def _linear(wl, bigcounter0=0):
 def _hydro(wl):
     wl.hydrostatic = 1
     return wl
+
+
+def _ice(nx=15, ny=14, nz=16, **kw):
+    return configs.ice_cloud(nx=nx, ny=ny, nz=nz, dz=750.0, **kw)
 
 
 def _jet(moist):
@@ -98,6 +103,14 @@ RUN_CASES = {
     "hydro_moist": (lambda: _hydro(configs.moist_blob(nx=15, ny=14, nz=10, dx=2000.0)), 4),
     "hydro_jet": (lambda: _hydro(_jet(True)), 3),
     "hydro_diffusion": (lambda: _hydro(_diffusing(configs.moist_blob(nx=16, ny=14, nz=12, dx=2000.0), 4, 0.004)), 3),
+    # ice microphysics (run_rutledge_microphysics): Eulerian and semi-
+    # Lagrangian fallout, periodic, with turbulence and ocean fluxes, with
+    # explicit diffusion; 16 levels of 750 m reach the ice-only temperatures
+    "ice": (lambda: _ice(), 3),
+    "ice_rf2": (lambda: _ice(rain_fallout=2), 3),
+    "ice_periodic": (lambda: _ice(nx=18, periodic=1), 3),
+    "ice_turbulence": (lambda: _turbulent(_ice(nx=16), 1, 29.0), 3),
+    "ice_diffusion": (lambda: _diffusing(_ice(nx=16, ny=15), 4, 0.004), 3),
 }
 
 OP_NAMES = ["advect_uvw", "solve_pressure", "integrate_non_hydro", "advect_theta",
@@ -140,6 +153,17 @@ def _ops_state(wl, seed: int) -> dict:
             if name in ("qc", "qr"):
                 v = np.abs(v) if suf == "_m" else v  # P may hold negatives for zero_moisture
             extra[name + suf] = v
+    if wl.microphysics_option == 2:  # snow and ice: every slot non-negative
+        for name in ("qs", "qi"):
+            for suf in ("_p", "_m"):
+                r = 2.0 * configs.splitmix_uniform(s, wl.points).reshape(n3) - 1.0
+                s += 1
+                extra[name + suf] = np.abs(wl.fields[name] + 4e-4 * r)
+        extra["sts"] = np.zeros(n3)
+        # a fall speed that the Eulerian ice update keeps where pi is small
+        extra["its"] = 0.3 * configs.splitmix_uniform(s, wl.points).reshape(n3)
+        s += 1
+        extra["n0s"] = np.array([5.0e7])
     r = 2.0 * configs.splitmix_uniform(s, wl.points).reshape(n3) - 1.0
     extra["pi"] = 20.0 * r
     extra["vt"] = np.zeros(n3)
@@ -228,6 +252,30 @@ LINEAR_OPS = {"advect_uvw": "advect_uvw", "advect_theta": "advect_theta", "advec
               "integrate_non_hydro": "integrate_non_hydro"}
 
 
+ICE_OPS = {"advect_uvw": "advect_uvw", "advect_micro": "advect_micro", "advect_ice": "advect_ice",
+           "kessler": "kessler", "bc_micro": "bc_micro", "zero_moisture": "zero_moisture",
+           "explicit_diffusion": "explicit_diffusion"}
+
+
+def make_ice_ops():
+    """iceop_<case>.npz: the operators of the ice scheme on a state whose
+    rotation slots differ (run_microphysics is run_rutledge_microphysics);
+    the periodic case with turbulence also records saturation_adjustment's
+    saturation record.  A third case puts negative snow and ice into the
+    forecast slot for zero_moisture and the boundary conditions (the
+    microphysics would take roots of them)."""
+    cases = {"cloud": _diffusing(_ice(), 4, 0.005),
+             "periodic_sat": _turbulent(_diffusing(_ice(nx=18, periodic=1, rain_fallout=2), 6, 0.003), 1, 28.0)}
+    _variant_ops("iceop", cases, ICE_OPS, step=1.0 / 3.0)
+    wl = _diffusing(_ice(nx=16, ny=13), 2, 0.01)
+    neg = _ops_state(wl, 9500)
+    for name in ("qs_p", "qi_p"):
+        r = 2.0 * configs.splitmix_uniform(9600 + len(name), wl.points).reshape(wl.nx, wl.ny, wl.nz) - 1.0
+        neg[name] = neg[name] + 3e-4 * r
+    _variant_ops("iceop", {"negative": wl}, {"zero_moisture": "zero_moisture", "bc_micro": "bc_micro"},
+                 extra=neg)
+
+
 def make_linear_ops():
     """linop_<case>.npz: the linearised operators (the ISLINEAR build) on a
     state whose rotation slots differ; the moisture operator of the
@@ -237,19 +285,25 @@ def make_linear_ops():
     _variant_ops("hydop", {"moist": _hydro(configs.moist_blob(nx=15, ny=14, nz=10, dx=2000.0))}, HYDRO_OPS)
 
 
-def _variant_ops(prefix, cases, ops):
+def _variant_ops(prefix, cases, ops, step=0.5, extra=None):
     for cname, wl in cases.items():
-        extra = _ops_state(wl, 9000)
+        if extra is None or len(cases) > 1:
+            extra = _ops_state(wl, 9000)
+        if wl.turbulence_option and wl.microphysics_option:
+            extra["is_saturated"] = (configs.splitmix_uniform(9900, wl.points) < 0.5).astype(np.float64).reshape(
+                wl.nx, wl.ny, wl.nz)
         d = _inputs(wl)
         for k, v in extra.items():
             d["in_" + k] = v.ravel()
         for op, ref_op in ops.items():
-            st = 0.5
+            st = step
             out = O.run_reference(wl, "op", op=ref_op, step=st, extra=extra)
             d[f"step_{op}"] = np.float64(st)
             for k, v in out.items():
                 if k in abi.COLUMN_NAMES or k in ("f", "bigcounter", "mtime"):
                     continue
+                if k in abi.TURB_NAMES and k != "is_saturated":
+                    continue  # the turbulence tendencies: calculate_diff_tend only
                 ref_in = extra.get(k, wl.fields.get(k))
                 if ref_in is not None and np.array_equal(np.asarray(ref_in).ravel(), v):
                     continue
@@ -268,3 +322,4 @@ if __name__ == "__main__":
     make_ops()
     make_turb()
     make_linear_ops()
+    make_ice_ops()

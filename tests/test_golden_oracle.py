@@ -130,3 +130,30 @@ def test_hydrostatic_operator_bit_exact(name, op):
         key = k.split("__", 1)[1]
         f, slot = fx.FIELD_OF[key]
         np.testing.assert_array_equal(o.get(f, slot), d[k], err_msg=f"{op}:{key}")
+
+
+@pytest.mark.parametrize("name", fx.iceop_names())
+@pytest.mark.parametrize("op", ["advect_uvw", "advect_micro", "advect_ice", "kessler", "bc_micro", "zero_moisture",
+                                "explicit_diffusion"])
+def test_ice_operator_bit_exact(name, op):
+    """the operators of the ice scheme (microphysics_option 2) against the
+    reference build: the buoyancy with snow and ice, the Rutledge rain fall
+    speed, advect_ice_cell, run_rutledge_microphysics (with semi-Lagrangian
+    fallout and the saturation record in the periodic case), the boundary
+    conditions, zero_moisture and explicit diffusion of snow and ice"""
+    d = fx.load(name)
+    if f"step_{op}" not in d:
+        pytest.skip("operator not in this fixture")
+    wl = fx.workload(d)
+    assert wl.microphysics_option == 2
+    o = O.Oracle(wl)
+    for k, v in fx.slot_extra(d).items():
+        f, slot = fx.FIELD_OF[k]
+        o.set(f, slot, v)
+    assert o.op(op, float(d[f"step_{op}"])) == 0
+    outs = [k for k in d if k.startswith(op + "__")]
+    assert outs
+    for k in outs:
+        key = k.split("__", 1)[1]
+        f, slot = fx.FIELD_OF[key]
+        np.testing.assert_array_equal(o.get(f, slot), d[k], err_msg=f"{op}:{key}")
