@@ -163,7 +163,8 @@ class Model:
         self._check(self.L.ga_set_field(self.h, field, slot, _ptr(a), a.size), "ga_set_field")
 
     def get(self, field: int, slot: int = 0) -> np.ndarray:
-        n = self.wl.nx * self.wl.ny if field == abi.GA_ACCRAIN else self.n3
+        n = self.wl.nx * self.wl.ny if field in (abi.GA_ACCRAIN, abi.GA_ACCSNOW) else \
+            1 if field == abi.GA_N0S else self.n3
         a = np.zeros(n)
         self._check(self.L.ga_get_field(self.h, field, slot, _ptr(a), n), "ga_get_field")
         return a
@@ -180,6 +181,12 @@ class Model:
             self.set(f, abi.GA_SLOT_M, arr)
         if "accrain" in fields:
             self.set(abi.GA_ACCRAIN, 0, fields["accrain"])
+        if self.wl.microphysics_option == 2:  # snow and cloud ice (initializer.cpp:1920-1926)
+            for name, fid in abi.ICE_PROG.items():
+                self.set(fid, abi.GA_SLOT_CUR, fields[name])
+                self.set(fid, abi.GA_SLOT_M, fields[name])
+            if "accsnow" in fields:
+                self.set(abi.GA_ACCSNOW, 0, fields["accsnow"])
 
     def state(self) -> dict:
         out = {}
@@ -191,6 +198,12 @@ class Model:
         if self.wl.microphysics_option:
             out["vt"] = self.get(abi.GA_VT)
             out["accrain"] = self.get(abi.GA_ACCRAIN)
+        if self.wl.microphysics_option == 2:
+            for name, fid in abi.ICE_PROG.items():
+                for slot, suf in abi.SLOT_SUFFIX.items():
+                    out[name + suf] = self.get(fid, slot)
+            for name, fid in abi.ICE_NAMES.items():
+                out[name] = self.get(fid)
         return out
 
     # ---- stepping -------------------------------------------------------
@@ -232,8 +245,11 @@ class Model:
     def apply_boundary_condition_microphysics(self):  # boundaries.cpp:200
         self.op("bc_micro")
 
-    def run_microphysics(self):  # microphysics.cpp:97
+    def run_microphysics(self):  # microphysics.cpp:97 (Kessler or the ice scheme)
         self.op("kessler")
+
+    def advect_ice_cell(self, step):  # advection.cpp:508
+        self.op("advect_ice", step)
 
     def rayleigh_damping(self):  # damping.cpp:1148
         self.op("rayleigh")

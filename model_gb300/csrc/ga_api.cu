@@ -116,12 +116,13 @@ int ga_create(const ga_config *cfg, const ga_columns *cols, ga_ctx **out)
     if (cfg->nz < 6 || cfg->nz > 128) return fail(GA_ERR_CONFIG, "ga_create: NZ must be in [6,128]");
     if (!(cfg->dx > 0 && cfg->dy > 0 && cfg->dz > 0 && cfg->dt > 0))
         return fail(GA_ERR_CONFIG, "ga_create: dx, dy, dz, dt must be positive");
-    if (cfg->microphysics_option == 2)
-        return fail(GA_ERR_UNSUPPORTED, "ga_create: microphysics_option 2 (ice) is not built");
-    if (cfg->microphysics_option < 0 || cfg->microphysics_option > 1)
-        return fail(GA_ERR_CONFIG, "ga_create: microphysics_option must be 0 or 1");
-    if (cfg->microphysics_option == 1 && cfg->rain_fallout != 1 && cfg->rain_fallout != 2)
+    if (cfg->microphysics_option < 0 || cfg->microphysics_option > 2)
+        return fail(GA_ERR_CONFIG, "ga_create: microphysics_option must be 0, 1 or 2");
+    if (cfg->microphysics_option >= 1 && cfg->rain_fallout != 1 && cfg->rain_fallout != 2)
         return fail(GA_ERR_CONFIG, "ga_create: rain_fallout must be 1 or 2");
+    if (cfg->microphysics_option == 2 && (cfg->hydrostatic == 1 || cfg->linear_model == 1))
+        return fail(GA_ERR_UNSUPPORTED, "ga_create: the ice scheme is built for the nonlinear non-hydrostatic "
+                                        "equation set");
     if (cfg->precision != GA_PREC_F64 && cfg->precision != GA_PREC_F32)
         return fail(GA_ERR_CONFIG, "ga_create: unknown precision");
     const int widths[] = {cfg->boundary_width_north, cfg->boundary_width_south, cfg->boundary_width_east,
@@ -170,7 +171,7 @@ int ga_destroy(ga_ctx *ctx)
 int ga_set_field(ga_ctx *ctx, int field, int slot, const double *host, size_t n)
 {
     if (!ctx || !host) return fail(GA_ERR_ARG, "ga_set_field: null pointer");
-    if (field < 0 || field > GA_SATURATED || slot < 0 || slot > 2) return fail(GA_ERR_ARG, "ga_set_field: bad field or slot");
+    if (field < 0 || field > GA_N0S || slot < 0 || slot > 2) return fail(GA_ERR_ARG, "ga_set_field: bad field or slot");
     int rc = ctx->e->set_field(field, slot, host, n);
     if (rc == GA_ERR_ARG) set_error("ga_set_field: field not present in this context or wrong size");
     return rc;
@@ -179,7 +180,7 @@ int ga_set_field(ga_ctx *ctx, int field, int slot, const double *host, size_t n)
 int ga_get_field(ga_ctx *ctx, int field, int slot, double *host, size_t n)
 {
     if (!ctx || !host) return fail(GA_ERR_ARG, "ga_get_field: null pointer");
-    if (field < 0 || field > GA_SATURATED || slot < 0 || slot > 2) return fail(GA_ERR_ARG, "ga_get_field: bad field or slot");
+    if (field < 0 || field > GA_N0S || slot < 0 || slot > 2) return fail(GA_ERR_ARG, "ga_get_field: bad field or slot");
     int rc = ctx->e->get_field(field, slot, host, n);
     if (rc == GA_ERR_ARG) set_error("ga_get_field: field not present in this context or wrong size");
     return rc;
@@ -317,7 +318,8 @@ void *ga_stream(ga_ctx *ctx) { return ctx ? (void *)ctx->e->stream : nullptr; }
 
 void *ga_field_device_ptr(ga_ctx *ctx, int field, int slot)
 {
-    if (!ctx || field < 0 || field > GA_QRDIFF || slot < 0 || slot > 2) return nullptr;
+    if (!ctx || slot < 0 || slot > 2) return nullptr;
+    if ((field < 0 || field > GA_QRDIFF) && (field < GA_QS || field > GA_N0S)) return nullptr;
     return ctx->e->field_ptr(field, slot);
 }
 

@@ -17,6 +17,7 @@
 #include "ga_quad.cuh"
 #include "ga_turb.cuh"
 #include "ga_hydro.cuh"
+#include "ga_ice.cuh"
 
 #include <cudaTypedefs.h>
 
@@ -76,11 +77,16 @@ class Engine : public EngineBase {
     ga_config cfg;
     int NX, NY, NZ;
     long N;
-    int nprog;
-    T *buf[7][3] = {};
-    int ci[7], pi_[7], mi[7];  // rotation: which buffer is current / forecast / start-of-step
+    int nprog;  // 4 dry, 7 with Kessler, 9 with the ice scheme (snow FQS, ice FQI)
+    T *buf[9][3] = {};
+    int ci[9], pi_[9], mi[9];  // rotation: which buffer is current / forecast / start-of-step
     T *pi = nullptr, *bar[6] = {}, *vt = nullptr;
     double *accrain = nullptr;
+    // ice scheme (ga_ice.cuh): snow and ice fall speeds, accumulated snow, the
+    // snow intercept (one value) and its per-point record of the last pass
+    T *sts = nullptr, *its = nullptr, *n0s = nullptr, *n0s_pt = nullptr;
+    double *accsnow = nullptr;
+    int *n0s_idx = nullptr;
     T2 *spec = nullptr;
     T2 *tw_i = nullptr, *tw_j = nullptr;
     FftPlan plan_i, plan_j;
@@ -118,7 +124,7 @@ class Engine : public EngineBase {
     int adv_tma = 0, adv_tmc = 0;
     double *budget_w = nullptr, *budget_part = nullptr;  // FP64 budget weights and partial sums
     T *diff_tend = nullptr;  // explicit diffusion: a second buffer for every prognostic field
-    T *diff_buf[7] = {};     // (the one each field's diffused start-of-step values go to)
+    T *diff_buf[9] = {};     // (the one each field's diffused start-of-step values go to)
     const T *diff_w = nullptr;  // and the vertical finite-difference weights, order+1 per level
     // turbulence: coefficients, tendencies, tables (ga_turb.cuh); turb.kmix
     // is null when the scheme is off.  turb_sat is Kessler's saturation record.
@@ -236,9 +242,10 @@ class Engine : public EngineBase {
         device = c->device;
         if (cudaSetDevice(device) != cudaSuccess) { status = GA_ERR_CUDA; return; }
         if (cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking) != cudaSuccess) { status = GA_ERR_CUDA; return; }
-        const bool moist = c->microphysics_option == 1;
-        nprog = moist ? 7 : 4;
-        for (int f = 0; f < 7; f++) {
+        const bool moist = c->microphysics_option >= 1;
+        const bool ice = c->microphysics_option == 2;
+        nprog = ice ? 9 : moist ? 7 : 4;
+        for (int f = 0; f < 9; f++) {
             const int nb = f < nprog ? 3 : 0;
             for (int s = 0; s < nb; s++) buf[f][s] = dalloc<T>(N);
             ci[f] = 0; pi_[f] = 1; mi[f] = 2;
@@ -267,6 +274,19 @@ class Engine : public EngineBase {
         kp.tb = col_T(cols->tb, NZ); kp.tbv = col_T(cols->tbv, NZ); kp.qb = col_T(cols->qb, NZ);
         kp.f = col_T(cols->f, NY); kp.zsw = col_T(cols->zsw, NZ);
         kp.rhou1 = (T)cols->rhou[1];
+        if (ice) {  // the ice scheme's state (initializer.cpp:457-466, rutledge.cpp:90)
+            kp.ice = 1;
+            kp.rfall = (T)(2115.0 * std::pow(0.01, 0.2) * 17.83786);  // rutledge.cpp:140
+            kp.pib = col_T(cols->pib, NZ);
+            sts = dalloc<T>(N);
+            its = dalloc<T>(N);
+            accsnow = dalloc<double>((size_t)NX * NY);
+            n0s = upload(std::vector<T>(1, (T)8e6));
+            n0s_pt = dalloc<T>(N);
+            n0s_idx = dalloc<int>(1);
+            if (n0s_idx) cudaMemset(n0s_idx, 0xff, sizeof(int));  // -1: no snowy point recorded
+            adv_force = 1;  // the per-level tile kernel (snow and ice buoyancy, stored fall speeds)
+        }
 
         // ---- Rayleigh coefficients (damping.cpp:1150-1162) ----
         const double trigpi = 3.14159265358979324;
@@ -375,8 +395,9 @@ class Engine : public EngineBase {
             cudaFuncSetAttribute(k_turb_tend_tile<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
             turb.kmix = dalloc<T>(N);
             turb.khmix = dalloc<T>(N);
-            T *tt = dalloc<T>((size_t)nprog * N);
-            for (int f = 0; f < 7; f++) turb.tend[f] = f < nprog ? tt + (size_t)f * N : nullptr;
+            const int nt = std::min(nprog, 7);  // no tendencies of snow or ice (turbulence.cpp:233-290)
+            T *tt = dalloc<T>((size_t)nt * N);
+            for (int f = 0; f < 7; f++) turb.tend[f] = f < nt ? tt + (size_t)f * N : nullptr;
             if (moist) turb_sat = dalloc<unsigned char>(N);
             turb.sat = turb_sat;
             std::vector<double> l2(NZ, 0.0), kv(NZ, 0.0);
@@ -484,7 +505,7 @@ class Engine : public EngineBase {
         cudaFuncSetAttribute(k_advect_tile<T, 4, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
         cudaFuncSetAttribute(k_advect_tile<T, 4, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
         cudaFuncSetAttribute(k_advect_tile<T, 8, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
-        if (const char *ev = std::getenv("GA_ADVECT")) {
+        if (const char *ev = std::getenv("GA_ADVECT"); ev && !ice) {
             if (!std::strcmp(ev, "tile")) adv_force = 1;
             else if (!std::strcmp(ev, "quad")) adv_force = 2;
             else if (!std::strcmp(ev, "tma")) adv_force = 3;
@@ -549,7 +570,7 @@ class Engine : public EngineBase {
     {
         KFields<T> F;
         std::memset(&F, 0, sizeof(F));
-        for (int f = 0; f < 7; f++) {
+        for (int f = 0; f < 9; f++) {
             F.cur[f] = buf[f][ci[f]];
             F.P[f] = buf[f][pi_[f]];
             F.M[f] = buf[f][mi[f]];
@@ -558,6 +579,12 @@ class Engine : public EngineBase {
         F.pi = pi;
         F.vt = vt;
         F.accrain = accrain;
+        F.sts = sts;
+        F.its = its;
+        F.accsnow = accsnow;
+        F.n0s = n0s;
+        F.n0s_pt = n0s_pt;
+        F.n0s_idx = n0s_idx;
         F.qmask = qmask;
         F.sat = turb_sat;
         if (hyd.div) F.P[FW] = F.M[FW] = F.cur[FW];  // w lives in the current slot (boundaries.cpp:152-156)
@@ -583,6 +610,17 @@ class Engine : public EngineBase {
         case GA_KHMIX: return turb.kmix ? turb.khmix : nullptr;
         case GA_UFRIC: case GA_VFRIC: case GA_WFRIC: case GA_THDIFF: case GA_QVDIFF: case GA_QCDIFF: case GA_QRDIFF:
             return turb.kmix ? turb.tend[field - GA_UFRIC] : nullptr;
+        case GA_QS: case GA_QI: {
+            if (!kp.ice) return nullptr;
+            const int f = field == GA_QS ? FQS : FQI;
+            if (slot == GA_SLOT_CUR) return buf[f][ci[f]];
+            if (slot == GA_SLOT_P) return buf[f][pi_[f]];
+            if (slot == GA_SLOT_M) return buf[f][mi[f]];
+            return nullptr;
+        }
+        case GA_VTS: return sts;
+        case GA_VTI: return its;
+        case GA_N0S: *n = 1; return n0s;
         }
         return nullptr;
     }
@@ -590,6 +628,7 @@ class Engine : public EngineBase {
     void *field_ptr(int field, int slot) override
     {
         if (field == GA_ACCRAIN) return accrain;
+        if (field == GA_ACCSNOW) return accsnow;
         long n;
         return host_field(field, slot, &n);
     }
@@ -621,9 +660,16 @@ class Engine : public EngineBase {
         if (!host) return GA_ERR_ARG;
         cudaSetDevice(device);
         if (field == GA_SATURATED) return sat_field(nullptr, host, n);
-        if (field == GA_ACCRAIN) {
+        if (field == GA_ACCRAIN || (field == GA_ACCSNOW && accsnow)) {
             if (n != (size_t)NX * NY) return GA_ERR_ARG;
-            cudaMemcpyAsync(accrain, host, n * sizeof(double), cudaMemcpyHostToDevice, stream);
+            cudaMemcpyAsync(field == GA_ACCRAIN ? accrain : accsnow, host, n * sizeof(double),
+                            cudaMemcpyHostToDevice, stream);
+            return sync_status();
+        }
+        if (field == GA_N0S && n0s) {
+            if (n != 1) return GA_ERR_ARG;
+            const T v = (T)host[0];
+            cudaMemcpyAsync(n0s, &v, sizeof(T), cudaMemcpyHostToDevice, stream);
             return sync_status();
         }
         long nn;
@@ -654,10 +700,19 @@ class Engine : public EngineBase {
         if (!host) return GA_ERR_ARG;
         cudaSetDevice(device);
         if (field == GA_SATURATED) return sat_field(host, nullptr, n);
-        if (field == GA_ACCRAIN) {
+        if (field == GA_ACCRAIN || (field == GA_ACCSNOW && accsnow)) {
             if (n != (size_t)NX * NY) return GA_ERR_ARG;
-            cudaMemcpyAsync(host, accrain, n * sizeof(double), cudaMemcpyDeviceToHost, stream);
+            cudaMemcpyAsync(host, field == GA_ACCRAIN ? accrain : accsnow, n * sizeof(double),
+                            cudaMemcpyDeviceToHost, stream);
             return sync_status();
+        }
+        if (field == GA_N0S && n0s) {
+            if (n != 1) return GA_ERR_ARG;
+            T v = T(0);
+            cudaMemcpyAsync(&v, n0s, sizeof(T), cudaMemcpyDeviceToHost, stream);
+            const int rc = sync_status();
+            host[0] = (double)v;
+            return rc;
         }
         long nn;
         T *d = host_field(field, slot, &nn);
@@ -882,7 +937,7 @@ class Engine : public EngineBase {
         const int nb = (int)std::min((tot + 255) / 256, 152L * 16);
         KFields<T> F = fields();
         DiffOut<T> o;
-        for (int f = 0; f < 7; f++) o.out[f] = (f < nprog && !(f == FW && hyd.div)) ? diff_buf[f] : nullptr;
+        for (int f = 0; f < 9; f++) o.out[f] = (f < nprog && !(f == FW && hyd.div)) ? diff_buf[f] : nullptr;
         k_diffuse_into<T><<<nb, 256, 0, stream>>>(kp, F, o, nprog, order, (T)cfg.kdiffh, (T)cfg.kdiffv, diff_w,
                                                   (T)step);
         // the diffused copy becomes the start-of-step slot; two steps swap
@@ -1054,12 +1109,33 @@ class Engine : public EngineBase {
         poisson(step);
     }
 
-    // per-field flags for k_post; pcopy selects the periodic two-pass form
+    // per-field flags for k_post (nfields up to 9: snow and ice last); pcopy
+    // selects the periodic two-pass form.  Snow and ice take a second pass of
+    // the same kernel, in the slots of cloud water and rain, whose clipping,
+    // sponge and top/bottom conditions they share (microphysics.cpp:675-700,
+    // boundaries.cpp:200-284).
     void post(const int *flags, int nfields, double step, bool pcopy)
     {
-        KFields<T> F = fields();
         int fl[8] = {0, 0, 0, 0, 0, 0, 0, 0};
         for (int f = 0; f < nfields && f < 7; f++) fl[f] = f < nprog ? flags[f] : 0;
+        post_pass(fields(), fl, step, pcopy);
+        if (nprog == 9 && nfields == 9 && (flags[FQS] | flags[FQI])) {
+            KFields<T> F = fields();
+            F.cur[FQC] = F.cur[FQS]; F.P[FQC] = F.P[FQS]; F.M[FQC] = F.M[FQS];
+            F.cur[FQR] = F.cur[FQI]; F.P[FQR] = F.P[FQI]; F.M[FQR] = F.M[FQI];
+            int fi[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+            fi[FQC] = flags[FQS] & (PF_ZERO | PF_SPONGE | PF_VBC | PF_WRITE_M);
+            fi[FQR] = flags[FQI] & (PF_ZERO | PF_SPONGE | PF_VBC | PF_WRITE_M);
+            const bool kes = post_kes;
+            post_kes = false;
+            post_pass(F, fi, step, pcopy);
+            post_kes = kes;
+        }
+    }
+
+    void post_pass(const KFields<T> &F, const int *fl, double step, bool pcopy)
+    {
+        if (!(fl[0] | fl[1] | fl[2] | fl[3] | fl[4] | fl[5] | fl[6])) return;
         int4 a = make_int4(fl[0], fl[1], fl[2], fl[3]), b = make_int4(fl[4], fl[5], fl[6], fl[7]);
         ProfScope ps(this, PC_POST, (pcopy && kp.periodic) ? 2 : 1);
         if constexpr (sizeof(T) == 4) {
@@ -1117,18 +1193,98 @@ class Engine : public EngineBase {
         }
     }
 
+    // Rutledge fall speeds of the Eulerian advection (advect_microphysics_cell's
+    // rain, advect_ice_cell's snow and ice) over the advected columns
+    void ice_fall_euler(int what)
+    {
+        KFields<T> F = fields();
+        const long tot = (long)(NX - 6) * (NY - 6) * (NZ - 2);
+        k_ice_fall<T><<<cdiv(tot, 256), 256, 0, stream>>>(kp, F, 3, NX - 3, 3, NY - 3, what, 0);
+        launches++;
+    }
+
+    void advect_ice(double step)  // advect_ice_cell (advection.cpp:508-567)
+    {
+        KFields<T> F = fields();
+        ProfScope ps(this, PC_ADVECT, 1);
+        const long tot = (long)(NX - 6) * (NY - 6) * (NZ - 2);
+        k_advect_ice<T><<<cdiv(tot, 128), 128, 0, stream>>>(kp, F, (T)step);
+        launches++;
+    }
+
+    // semi-Lagrangian PPM fallout of one hydrometeor (hydrometeor_fallout,
+    // microphysics.cpp:210-292) with its fall speed into its accumulator; the
+    // edge value the reference carries between columns runs on through the
+    // calls in their order
+    void ppm_fallout(KFields<T> F, T *var, T *fall, double *acc)
+    {
+        F.P[FQR] = var;
+        F.vt = fall;
+        F.accrain = acc;
+        const long ncol = (long)(NX - 2) * (NY - 2);
+        k_ppm_prepare<T><<<cdiv(ncol, 64), 64, 0, stream>>>(kp, F, ppm_has, ppm_topq, ppm_topm);
+        k_ppm_carry<T><<<1, 32, 0, stream>>>(ncol, ppm_has, ppm_topq, ppm_topm, ppm_cin, ppm_carry);
+        k_ppm_remap<T><<<cdiv(ncol, 64), 64, 0, stream>>>(kp, F, ppm_has, ppm_cin);
+        launches += 3;
+    }
+
+    // run_rutledge_microphysics (rutledge.cpp:150-501).  exact: zero_moisture
+    // of the points outside the interior and the precipitation as passes of
+    // their own, for a forecast state that no stage has clipped (the single
+    // operator); in the step every such point is already clipped and the
+    // level-1 threads add the precipitation
+    void rutledge(bool exact)
+    {
+        KFields<T> F = fields();
+        const long tot = (long)(NX - 2) * (NY - 2) * (NZ - 2);
+        const bool rf1 = kp.rf != 2;
+        {
+            ProfScope ps(this, PC_KESSLER, 2);
+            k_rutledge<T><<<cdiv(tot, 128), 128, 0, stream>>>(kp, F, rf1 && !exact, d_err);
+            k_ice_n0s<T><<<1, 32, 0, stream>>>(F);
+            launches += 2;
+        }
+        if (exact) {
+            int fz[9] = {};
+            fz[FQV] = fz[FQC] = fz[FQR] = fz[FQS] = fz[FQI] = PF_ZERO;
+            post(fz, 9, 1.0, false);
+            if (rf1) {
+                const long ncol = (long)(NX - 2) * (NY - 2);
+                k_ice_precip<T><<<cdiv(ncol, 128), 128, 0, stream>>>(kp, F);
+                launches++;
+            }
+        }
+        if (!rf1) {
+            ProfScope ps(this, PC_PPM, 13);
+            k_ice_fall<T><<<cdiv(tot, 256), 256, 0, stream>>>(kp, F, 1, NX - 1, 1, NY - 1,
+                                                              IF_RAIN | IF_SNOW | IF_ICE, 1);
+            ppm_fallout(F, F.P[FQR], vt, accrain);
+            ppm_fallout(F, F.P[FQI], its, accsnow);
+            ppm_fallout(F, F.P[FQS], sts, accsnow);
+            k_fill<T><<<cdiv(N, 256), 256, 0, stream>>>(vt, N, T(0));
+            k_fill<T><<<cdiv(N, 256), 256, 0, stream>>>(sts, N, T(0));
+            k_fill<T><<<cdiv(N, 256), 256, 0, stream>>>(its, N, T(0));
+            launches += 4;
+        }
+    }
+
+    void microphysics(bool exact)  // run_microphysics (microphysics.cpp:97-131)
+    {
+        if (kp.ice) rutledge(exact);
+        else kessler();
+    }
+
     void swap_micro()  // microphysics_advance_inner (microphysics.cpp:642-653)
     {
-        if (nprog == 7)
-            for (int f = 4; f < 7; f++) std::swap(ci[f], pi_[f]);
+        for (int f = 4; f < nprog; f++) std::swap(ci[f], pi_[f]);
     }
 
     void swap_inner(bool micro)
     {
         for (int f = 0; f < 4; f++)
             if (f != FW || !hyd.div) std::swap(ci[f], pi_[f]);  // solver.cpp:240-248
-        if (micro && nprog == 7)
-            for (int f = 4; f < 7; f++) std::swap(ci[f], pi_[f]);
+        if (micro)
+            for (int f = 4; f < nprog; f++) std::swap(ci[f], pi_[f]);
     }
 
     void copy_m_from_p(int f0, int f1)
@@ -1144,7 +1300,7 @@ class Engine : public EngineBase {
         cudaSetDevice(device);
         refresh_base();
         const bool moist = kp.moist;
-        int fl[7] = {0, 0, 0, 0, 0, 0, 0};
+        int fl[9] = {};
         switch (o) {
         case GA_OP_SIGN_CELLS: break;
         case GA_OP_ADVECT_UVW: advect(step, hyd.div ? ADV_UV : ADV_UV | ADV_WB); break;  // advect_uv_velocity
@@ -1158,7 +1314,7 @@ class Engine : public EngineBase {
                 break;
             }
             fl[FU] = fl[FV] = fl[FW] = PF_PROJECT;
-            post(fl, 7, step, false);
+            post(fl, 9, step, false);
             break;
         case GA_OP_INTEGRATE_NON_HYDRO:
             if (hyd.div) {  // integrate_hydro (solver.cpp:33-80)
@@ -1171,30 +1327,37 @@ class Engine : public EngineBase {
             turb_apply(TA_VEL, step);  // solver.cpp:103
             solve_pressure(step);
             fl[FU] = fl[FV] = fl[FW] = PF_PROJECT;
-            post(fl, 7, step, false);
+            post(fl, 9, step, false);
             break;
         case GA_OP_ADVECT_THETA: advect(step, ADV_TH); break;
         case GA_OP_ADVECT_MICRO:
-            if (moist) advect(step, cfg.linear_model ? (ADV_Q | ADV_QVONLY) : ADV_Q);  // advect_qv when linear
+            if (!moist) break;
+            if (kp.ice && kp.rf == 1) ice_fall_euler(IF_RAIN);  // advection.cpp:456-457
+            advect(step, cfg.linear_model ? (ADV_Q | ADV_QVONLY) : ADV_Q);  // advect_qv when linear
+            break;
+        case GA_OP_ADVECT_ICE:
+            if (!kp.ice) return GA_ERR_ARG;
+            if (kp.rf == 1) ice_fall_euler(IF_SNOW | IF_ICE);  // advection.cpp:513-514
+            advect_ice(step);
             break;
         case GA_OP_ZERO_MOISTURE:
             if (moist) {
-                fl[FQV] = fl[FQC] = fl[FQR] = PF_ZERO;
-                post(fl, 7, step, false);
+                fl[FQV] = fl[FQC] = fl[FQR] = fl[FQS] = fl[FQI] = PF_ZERO;
+                post(fl, 9, step, false);
             }
             break;
         case GA_OP_BC:
             fl[FU] = fl[FV] = fl[FW] = fl[FTH] = PF_SPONGE | PF_VBC;
             if (kp.periodic) periodic_pi();
-            post(fl, 7, step, true);
+            post(fl, 9, step, true);
             break;
         case GA_OP_BC_MICRO:
             if (moist) {
-                fl[FQV] = fl[FQC] = fl[FQR] = PF_SPONGE | PF_VBC;
-                post(fl, 7, step, true);
+                fl[FQV] = fl[FQC] = fl[FQR] = fl[FQS] = fl[FQI] = PF_SPONGE | PF_VBC;
+                post(fl, 9, step, true);
             }
             break;
-        case GA_OP_KESSLER: kessler(); break;
+        case GA_OP_KESSLER: microphysics(true); break;
         case GA_OP_EXPLICIT_DIFFUSION: diffuse(step); break;
         case GA_OP_TURBULENCE:
             if (!turb.kmix) return GA_ERR_ARG;
@@ -1202,11 +1365,11 @@ class Engine : public EngineBase {
             break;
         case GA_OP_RAYLEIGH:
             fl[FU] = fl[FV] = fl[FW] = fl[FTH] = PF_RAYLEIGH;
-            post(fl, 7, step, false);
+            post(fl, 9, step, false);
             break;
         case GA_OP_ADVANCE_INNER: swap_inner(true); break;
         case GA_OP_ADVANCE_OUTER:
-            copy_m_from_p(0, 7);
+            copy_m_from_p(0, 9);
             swap_inner(true);
             break;
         default: return GA_ERR_ARG;
@@ -1234,7 +1397,9 @@ class Engine : public EngineBase {
         int e = 0;
         cudaMemcpy(&e, d_err, sizeof(int), cudaMemcpyDeviceToHost);
         if (e) {
-            set_error("Kessler evaporation E>100 (the reference exits here, kessler.cpp:83-88)");
+            set_error(kp.ice ? "ice microphysics: rain evaporation E>100 or snow melting |psmlt|>100 (the reference "
+                               "exits here, rutledge.cpp:252-258, 370-376)"
+                             : "Kessler evaporation E>100 (the reference exits here, kessler.cpp:83-88)");
             return GA_ERR_KESSLER;
         }
         return GA_OK;
@@ -1265,11 +1430,29 @@ class Engine : public EngineBase {
                 hyd_solve(st);
                 hyd_project(st);
                 hyd_w();
-                int fh[7] = {0, 0, 0, 0, 0, 0, 0};
+                int fh[9] = {};
                 fh[FU] = fh[FV] = fh[FW] = fh[FTH] = PF_SPONGE | PF_VBC;  // w: the current slot
                 fh[FQV] = fh[FQC] = fh[FQR] = PF_ZERO | PF_SPONGE | PF_VBC;
-                post(fh, 7, st, true);
+                post(fh, 9, st, true);
                 qmask = nullptr;
+                if (s < 2) swap_inner(true);
+                continue;
+            }
+            if (kp.ice) {  // driver_serial.cpp:198-247 with advect_ice_cell
+                // the Rutledge fall speeds read the pressure of this stage's
+                // solve, so the moisture advection follows it
+                advect(st, ADV_UV | ADV_WB | ADV_TH);
+                if (turbulent) turb_apply(TA_VEL | TA_TH, st);
+                solve_pressure(st);
+                if (kp.rf == 1) ice_fall_euler(IF_RAIN | IF_SNOW | IF_ICE);
+                advect(st, ADV_Q | (turbulent ? 0 : ADV_ZERO));
+                advect_ice(st);
+                if (turbulent) turb_apply(TA_Q, st);
+                int fl[9] = {};
+                fl[FU] = fl[FV] = fl[FW] = PF_PROJECT | PF_SPONGE | PF_VBC;
+                fl[FTH] = PF_SPONGE | PF_VBC;
+                fl[FQV] = fl[FQC] = fl[FQR] = fl[FQS] = fl[FQI] = PF_ZERO | PF_SPONGE | PF_VBC;
+                post(fl, 9, st, true);
                 if (s < 2) swap_inner(true);
                 continue;
             }
@@ -1286,11 +1469,11 @@ class Engine : public EngineBase {
             qmask = nullptr;
             if (fuse_mirror) poisson(st);
             else solve_pressure(st);
-            int fl[7] = {0, 0, 0, 0, 0, 0, 0};
+            int fl[9] = {};
             fl[FU] = fl[FV] = fl[FW] = PF_PROJECT | PF_SPONGE | PF_VBC;
             fl[FTH] = PF_SPONGE | PF_VBC;
             fl[FQV] = fl[FQC] = fl[FQR] = PF_ZERO | PF_SPONGE | PF_VBC;
-            post(fl, 7, st, true);
+            post(fl, 9, st, true);
             if (s < 2) swap_inner(true);
         }
         if (moist && rec) {
@@ -1303,13 +1486,13 @@ class Engine : public EngineBase {
         // FP32, Eulerian rain, non-periodic: Kessler runs inside the last
         // column pass (a periodic domain's copied columns take their own
         // rain totals, so it keeps the separate kernel)
-        const bool fuse_kes = moist && kes_fused && post_quad && kp.rf == 1 && !kp.periodic;
-        if (moist && !fuse_kes) kessler();
-        int fl[7] = {0, 0, 0, 0, 0, 0, 0};
+        const bool fuse_kes = moist && !kp.ice && kes_fused && post_quad && kp.rf == 1 && !kp.periodic;
+        if (moist && !fuse_kes) microphysics(false);
+        int fl[9] = {};
         fl[FU] = fl[FV] = fl[FW] = fl[FTH] = PF_SPONGE | PF_VBC | PF_RAYLEIGH | PF_WRITE_M;
-        fl[FQV] = fl[FQC] = fl[FQR] = PF_SPONGE | PF_VBC | PF_WRITE_M;
+        fl[FQV] = fl[FQC] = fl[FQR] = fl[FQS] = fl[FQI] = PF_SPONGE | PF_VBC | PF_WRITE_M;
         post_kes = fuse_kes;
-        post(fl, 7, 1.0, true);
+        post(fl, 9, 1.0, true);
         post_kes = false;
         swap_inner(true);
         mtime += cfg.dt;
@@ -1330,24 +1513,24 @@ class Engine : public EngineBase {
             const double st = steps[s];
             advect(st, ADV_UV | ADV_WB | ADV_TH);
             solve_pressure(st);
-            int fl[7] = {0, 0, 0, 0, 0, 0, 0};
+            int fl[9] = {};
             fl[FU] = fl[FV] = fl[FW] = PF_PROJECT | PF_SPONGE | PF_VBC;
             fl[FTH] = PF_SPONGE | PF_VBC;
-            post(fl, 7, st, true);
+            post(fl, 9, st, true);
             if (cfg.use_explicit_diffusion) diffuse(st);  // the start-of-step slot, driver_serial.cpp:102
             if (s < 2) swap_inner(false);
             if (moist) {
                 advect(st, ADV_Q | ADV_QVONLY);
-                int fq[7] = {0, 0, 0, 0, 0, 0, 0};
+                int fq[9] = {};
                 fq[FQV] = fq[FQC] = fq[FQR] = PF_SPONGE | PF_VBC;
-                post(fq, 7, st, true);
+                post(fq, 9, st, true);
                 if (s < 2) swap_micro();
             }
         }
-        int fl[7] = {0, 0, 0, 0, 0, 0, 0};
+        int fl[9] = {};
         fl[FU] = fl[FV] = fl[FW] = fl[FTH] = PF_SPONGE | PF_VBC | PF_RAYLEIGH | PF_WRITE_M;
         fl[FQV] = fl[FQC] = fl[FQR] = PF_SPONGE | PF_VBC | PF_WRITE_M;
-        post(fl, 7, 1.0, true);
+        post(fl, 9, 1.0, true);
         swap_inner(true);
         kp.stale_signs = 0;
         const long period = 12 * 60 * 60 / (int)cfg.dt;

@@ -61,6 +61,12 @@ struct KParams {
     // the hydrostatic equation set: pi is the Exner perturbation itself
     // (CONVERT_PRESSURE, kessler.cpp:7-11), w is diagnosed
     int hydrostatic;
+    // ice microphysics (microphysics_option 2): snow and cloud ice, the
+    // Rutledge fall speeds stored by their own kernel; rfall is the rain
+    // fall-speed constant of rutledge.cpp:140
+    int ice;
+    T rfall;
+    const T *pib;  // Exner function of the base state [nz] (the ice scheme's latent heating)
 };
 
 // rows of the basic-state table (each nz long), filled by k_base_tables
@@ -76,10 +82,17 @@ enum {
 
 template <typename T>
 struct KFields {
-    T *cur[7], *P[7], *M[7];
+    T *cur[9], *P[9], *M[9];  // u v w th qv qc qr, and snow, ice with the ice scheme
     const T *bar[6];
     T *pi, *vt;
     double *accrain;
+    // ice scheme: snow and ice fall speeds, accumulated snow, the snow
+    // intercept carried between microphysics passes (one value), each snowy
+    // point's intercept of the last pass and the largest snowy point index
+    T *sts, *its;
+    double *accsnow;
+    T *n0s, *n0s_pt;
+    int *n0s_idx;
     // optional: per point of the advected cells, which moisture fields
     // zero_moisture clipped (bit 0 qv, 1 qc, 2 qr) -- the branch record of
     // the linearisation
@@ -88,7 +101,7 @@ struct KFields {
     unsigned char *sat;
 };
 
-enum { FU = 0, FV, FW, FTH, FQV, FQC, FQR };
+enum { FU = 0, FV, FW, FTH, FQV, FQC, FQR, FQS, FQI };
 
 // grids are limited to fewer than 2^31 points (checked by the engine)
 __host__ __device__ __forceinline__ int gix(int ny, int nz, int i, int j, int k)
@@ -326,11 +339,13 @@ __device__ __forceinline__ T fall_speed_point(const KParams<T> &p, T qr, int k)
 }
 
 // fall speed seen by the rain flux of an advected column: recomputed from the
-// current rain (Eulerian fallout, advection.cpp:456-457) or the stored field
+// current rain (Eulerian Kessler fallout, advection.cpp:456-457) or the stored
+// field (semi-Lagrangian fallout; the ice scheme, whose rain fall speed reads
+// the pressure solved in the same stage)
 template <typename T>
 __device__ __forceinline__ T vt_at(const KParams<T> &p, const KFields<T> &F, int i, int j, int k)
 {
-    if (p.rf == 1 && k < p.nz - 1) {
+    if (p.rf == 1 && !p.ice && k < p.nz - 1) {
         int kk = k == 0 ? 1 : k;
         return fall_speed_point(p, LD(F.cur[FQR], gix(p.ny, p.nz, i, j, kk)), kk);
     }
@@ -429,6 +444,11 @@ __global__ void __launch_bounds__(128) k_advect(KParams<T> p, KFields<T> F, T st
             const T *QV = F.cur[FQV], *QC = F.cur[FQC], *QR = F.cur[FQR];
             b0 = LD(TH, c) / p.tbv[k] + T(0.61) * LD(QV, c) - LD(QC, c) - LD(QR, c);
             b1 = LD(TH, c - 1) / p.tbv[k - 1] + T(0.61) * LD(QV, c - 1) - LD(QC, c - 1) - LD(QR, c - 1);
+            if (p.ice) {  // buoyancy_cold_micro (advection.cpp:56-58)
+                const T *QI = F.cur[FQI], *QS = F.cur[FQS];
+                b0 = b0 - LD(QI, c) - LD(QS, c);
+                b1 = b1 - LD(QI, c - 1) - LD(QS, c - 1);
+            }
         }
         F.P[FW][c] = LD(F.M[FW], c) + sdtg * (b0 + b1);
     }
@@ -437,7 +457,7 @@ __global__ void __launch_bounds__(128) k_advect(KParams<T> p, KFields<T> F, T st
     if ((what & ADV_Q) && (what & ADV_QVONLY)) {  // advect_qv, advection.cpp:577-601
         F.P[FQV][c] = LD(F.M[FQV], c) + step * s_tend(p, F, F.cur[FQV], F.bar[4], p.qb, i, j, k);
     } else if (what & ADV_Q) {  // advection.cpp:466-497
-        if (p.rf == 1) {
+        if (p.rf == 1 && !p.ice) {
             const T *QR = F.cur[FQR];
             F.vt[c] = fall_speed_point(p, LD(QR, c), k);
             if (k == 1) F.vt[c - 1] = fall_speed_point(p, LD(QR, c), 1);
@@ -812,6 +832,11 @@ __device__ void advect_tile_body(const KParams<T> &p, const KFields<T> &F, int b
                 const T *QV = F.cur[FQV], *QC = F.cur[FQC], *QR = F.cur[FQR];
                 b0 = LD(TH, cix) / p.tbv[k] + T(0.61) * LD(QV, cix) - LD(QC, cix) - LD(QR, cix);
                 b1 = LD(TH, cix - 1) / p.tbv[k - 1] + T(0.61) * LD(QV, cix - 1) - LD(QC, cix - 1) - LD(QR, cix - 1);
+                if (p.ice) {  // buoyancy_cold_micro (advection.cpp:56-58)
+                    const T *QI = F.cur[FQI], *QS = F.cur[FQS];
+                    b0 = b0 - LD(QI, cix) - LD(QS, cix);
+                    b1 = b1 - LD(QI, cix - 1) - LD(QS, cix - 1);
+                }
             }
             F.P[FW][cix] = LD(F.M[FW], cix) + sdtg * (b0 + b1);
         }
@@ -830,7 +855,7 @@ __device__ void advect_tile_body(const KParams<T> &p, const KFields<T> &F, int b
             F.P[FTH][cix] = LD(F.M[FTH], cix) + step * t;
         }
         if (what & ADV_Q) {
-            if (p.rf == 1 && !(what & ADV_QVONLY)) {
+            if (p.rf == 1 && !p.ice && !(what & ADV_QVONLY)) {
                 const T *QR = F.cur[FQR];
                 F.vt[cix] = fall_speed_point(p, LD(QR, cix), k);
                 if (k == 1) F.vt[cix - 1] = fall_speed_point(p, LD(QR, cix), 1);
@@ -2247,7 +2272,7 @@ __device__ __forceinline__ T wk6(const T *v, long c, const T *w)
 // addition (every tendency is still formed from the old values)
 template <typename T>
 struct DiffOut {
-    T *out[7];
+    T *out[9];
 };
 template <typename T>
 __global__ void __launch_bounds__(256) k_diffuse_into(KParams<T> p, KFields<T> F, DiffOut<T> o, int nf, int order,

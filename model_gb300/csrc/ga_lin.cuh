@@ -533,6 +533,10 @@ int Engine<T>::lin_supported() const
         set_error("tangent-linear / adjoint: the turbulence scheme is not linearised");
         return GA_ERR_UNSUPPORTED;
     }
+    if (kp.ice) {
+        set_error("tangent-linear / adjoint: the ice scheme is not linearised");
+        return GA_ERR_UNSUPPORTED;
+    }
     if (cfg.linear_model || cfg.hydrostatic) {
         set_error("tangent-linear / adjoint: contexts of the linearised model or the hydrostatic set have none");
         return GA_ERR_UNSUPPORTED;

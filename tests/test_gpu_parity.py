@@ -198,7 +198,8 @@ def _oracle_compare(wl, nsteps, tol, counters=None):
     assert o.step(nsteps) == 0
     worst = {}
     nprog = 7 if wl.microphysics_option else 4
-    for f in list(range(nprog)) + [abi.GA_PI]:
+    extra = [abi.GA_QS, abi.GA_QI, abi.GA_VTI] if wl.microphysics_option == 2 else []
+    for f in list(range(nprog)) + [abi.GA_PI] + extra:
         worst[f] = fx.rel_l2(m.get(f), o.get(f))
     print(wl.name, nsteps, {k: f"{v:.2e}" for k, v in worst.items()})
     for f, e in worst.items():
@@ -409,3 +410,81 @@ def test_autotuner_keeps_state_and_results(_built):
     sa, sb = a.state(), b.state()
     for k in sa:
         assert fx.rel_l2(sb[k], sa[k]) <= 1e-12, k
+
+
+ICE_EXACT = {"advect_uvw", "bc_micro", "zero_moisture", "explicit_diffusion"}
+
+
+@pytest.mark.parametrize("name", fx.iceop_names())
+@pytest.mark.parametrize("op", ["advect_uvw", "advect_micro", "advect_ice", "kessler", "bc_micro", "zero_moisture",
+                                "explicit_diffusion"])
+def test_ice_operator_matches_reference(name, op):
+    """the ice scheme's operators against the reference build: bit exact
+    where no pow or exp enters (the buoyancy with snow and ice, boundary
+    conditions, clipping, diffusion), 1e-12 relative L2 for the fall speeds,
+    the advection with them and run_rutledge_microphysics; its saturation
+    record and the snow intercept's source point exact"""
+    d = fx.load(name)
+    if f"step_{op}" not in d:
+        pytest.skip("operator not in this fixture")
+    wl = fx.workload(d)
+    m = anelastic.Model(wl, abi.GA_PREC_F64)
+    for k, v in fx.slot_extra(d).items():
+        f, slot = fx.FIELD_OF[k]
+        m.set(f, slot, v)
+    m.op(op, float(d[f"step_{op}"]))
+    outs = [k for k in d if k.startswith(op + "__")]
+    assert outs
+    for k in outs:
+        key = k.split("__", 1)[1]
+        f, slot = fx.FIELD_OF[key]
+        got = m.get(f, slot)
+        if op in ICE_EXACT or key == "is_saturated":
+            np.testing.assert_array_equal(got, d[k], err_msg=f"{name} {op}:{key}")
+        else:
+            e = fx.rel_l2(got, d[k])
+            assert e <= 1e-12, f"{name} {op}:{key} rel L2 {e:.3e}"
+
+
+@pytest.mark.parametrize("rf", [1, 2])
+def test_ice_cloud_thunderstorm_size_vs_oracle(rf):
+    """the ice scheme at the thunderstorm grid (128x128x48, 400 m levels): a
+    12 km deep cloud of water, rain, ice and snow, 4 steps, every prognostic
+    field, pi and the ice fall speed within 1e-10 of the oracle; then FP32
+    against FP64"""
+    from model_gb300 import configs
+    wl = configs.ice_cloud(nx=128, ny=128, nz=48, dz=400.0, rain_fallout=rf)
+    _oracle_compare(wl, 4, 1e-10)
+    a = anelastic.Model(wl, abi.GA_PREC_F32)
+    b = anelastic.Model(wl, abi.GA_PREC_F64)
+    a.step(4)
+    b.step(4)
+    for f in list(range(7)) + [abi.GA_QS, abi.GA_QI]:
+        x = a.get(f)
+        assert np.isfinite(x).all(), f
+        e = fx.rel_l2(x, b.get(f))
+        print("fp32", f, f"{e:.2e}")
+        assert e <= 1e-3, (f, e)
+
+
+@pytest.mark.parametrize("seed", range(16))
+def test_random_ice_configuration_vs_oracle(seed):
+    """the GPU's FP64 step with the ice scheme against the oracle on the
+    seeded configurations of tests/test_oracle_random.py (whose oracle runs
+    equal the reference build's bit for bit): every prognostic field in
+    every slot, pi, the ice fall speed and the snow intercept within 1e-10"""
+    from oracle import oracle as O
+    from tests.test_oracle_random import _ice_case
+    wl, nsteps = _ice_case(8000 + seed)
+    cols = anelastic.build_columns(wl)
+    m = anelastic.Model(wl, abi.GA_PREC_F64, columns=cols)
+    m.step(nsteps)
+    o = O.Oracle(wl, cols)
+    assert o.step(nsteps) == 0
+    for f in list(range(7)) + [abi.GA_QS, abi.GA_QI]:
+        for slot in (abi.GA_SLOT_CUR, abi.GA_SLOT_P, abi.GA_SLOT_M):
+            e = fx.rel_l2(m.get(f, slot), o.get(f, slot))
+            assert e <= 1e-10, (seed, f, slot, e)
+    for f in (abi.GA_PI, abi.GA_VTI, abi.GA_VTS, abi.GA_VT, abi.GA_ACCRAIN, abi.GA_ACCSNOW, abi.GA_N0S):
+        e = fx.rel_l2(m.get(f), o.get(f))
+        assert e <= 1e-10, (seed, f, e)

@@ -79,3 +79,56 @@ def test_random_configuration_bit_exact(seed):
         for k, f in abi.TURB_NAMES.items():
             if k in ref:
                 np.testing.assert_array_equal(o.get(f), ref[k], err_msg=f"seed {seed}: {k}")
+
+
+NICE = 16
+
+
+def _ice_case(seed: int):
+    """a seeded ice-scheme configuration: grid, sponge widths, periodic east-
+    west, fallout, explicit diffusion, turbulence with or without the ocean
+    fluxes, the blob's height and its snow and ice"""
+    rng = np.random.default_rng(seed)
+    nx = int(rng.choice([13, 15, 16, 19, 24]))
+    ny = int(rng.choice([12, 14, 17]))
+    nz = int(rng.choice([8, 12, 16, 20]))
+    rf = int(rng.integers(1, 3))
+    periodic = int(rng.integers(0, 2))
+    wl = configs.ice_cloud(nx=nx, ny=ny, nz=nz, dz=12000.0 / nz, rain_fallout=rf, periodic=periodic,
+                           zc=float(rng.uniform(3000.0, 8000.0)), qi=float(rng.uniform(1e-4, 8e-4)),
+                           qs=float(rng.uniform(2e-4, 2e-3)), seed=3000 + seed)
+    for side in ("north", "south", "east", "west"):
+        setattr(wl, "boundary_width_" + side, int(rng.integers(0, 4)))
+    wl.rayleigh_damping_z = int(rng.integers(max(1, nz - 5), nz - 1))
+    if rng.random() < 0.4:
+        wl.use_explicit_diffusion, wl.diffusion_order = 1, int(rng.choice([2, 4, 6]))
+        wl.kdiffh = wl.kdiffv = float(rng.uniform(0.001, 0.01))
+    if rng.random() < 0.4:
+        wl.turbulence_option = 1
+        wl.use_surface_heat_flux = int(rng.integers(0, 2))
+        wl.water_temp = float(rng.uniform(24.0, 30.0))
+    return wl, int(rng.integers(2, 4))
+
+
+@pytest.mark.parametrize("seed", range(NICE))
+def test_random_ice_configuration_bit_exact(seed):
+    """the ice scheme on seeded configurations: every field of the dump,
+    the snow intercept and (with turbulence) the saturation record"""
+    wl, nsteps = _ice_case(8000 + seed)
+    ref = O.run_reference(wl, "run", nsteps)
+    cols = {k: ref[k] for k in abi.COLUMN_NAMES}
+    cols["f"] = ref["f"]
+    o = O.Oracle(wl, cols)
+    assert o.step(nsteps) == 0
+    st = o.state()
+    checked = 0
+    for k, v in st.items():
+        if k in ref:
+            np.testing.assert_array_equal(v, ref[k], err_msg=f"seed {seed}: {k}")
+            assert np.isfinite(v).all(), (seed, k)
+            checked += 1
+    assert checked >= 24
+    if wl.turbulence_option:
+        for k, f in abi.TURB_NAMES.items():
+            if k in ref:
+                np.testing.assert_array_equal(o.get(f), ref[k], err_msg=f"seed {seed}: {k}")
