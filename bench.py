@@ -482,16 +482,21 @@ def physics_bench(torch, device, steps, accuracy_steps):
 
 
 def variants_bench(torch, device, steps, accuracy_steps):
-    """The reference's other equation sets: the linearised model about the
-    C3 jet basic state (192x128x32, dt = 120 s) and the hydrostatic set on
-    the C2 thunderstorm at dx = 2 km; FP32 and FP64 ms/step (tuned FP32,
-    L2 written over between steps) and the FP32 error after accuracy_steps."""
+    """The reference's other equation sets and its ice scheme: the
+    linearised model about the C3 jet basic state (192x128x32, dt = 120 s),
+    the hydrostatic set on the C2 thunderstorm at dx = 2 km, and the ice
+    microphysics on a cloud at the C2 grid; FP32 and FP64 ms/step (tuned
+    FP32, L2 written over between steps) and the FP32 error after
+    accuracy_steps."""
     from model_gb300 import abi, anelastic, configs
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{device}")
     cases = {"linear_model": (lambda: configs.jet_vortex(noise=0.3, extra_basic=1.0), {"linear_model": 1},
                               "linearised model about the 192x128x32 jet, dt=120 s"),
              "hydrostatic": (lambda: configs.thunderstorm(dx=2000.0), {"hydrostatic": 1},
-                             "hydrostatic set, Kessler thunderstorm 128x128x48, dx=dy=2 km, dt=4 s")}
+                             "hydrostatic set, Kessler thunderstorm 128x128x48, dx=dy=2 km, dt=4 s"),
+             "ice": (lambda: configs.ice_cloud(nx=128, ny=128, nz=48, dz=400.0), {},
+                     "ice microphysics (microphysics_option 2), a 10 km deep cloud of water, rain, ice and "
+                     "snow on the thunderstorm grid 128x128x48, dx=dy=1 km, dt=4 s")}
     out = {"steps": steps}
     for name, (mk, kw, desc) in cases.items():
         wl = mk()
@@ -516,8 +521,11 @@ def variants_bench(torch, device, steps, accuracy_steps):
             a.step(accuracy_steps)
             b.step(accuracy_steps)
             nf = 7 if wl.microphysics_option else 4
-            errs = {abi.PROG_NAMES[f]: float(np.linalg.norm(a.get(f) - b.get(f)) /
-                                             max(np.linalg.norm(b.get(f)), 1e-300)) for f in range(nf)}
+            fids = {abi.PROG_NAMES[f]: f for f in range(nf)}
+            if wl.microphysics_option == 2:
+                fids.update(abi.ICE_PROG)
+            errs = {name: float(np.linalg.norm(a.get(f) - b.get(f)) / max(np.linalg.norm(b.get(f)), 1e-300))
+                    for name, f in fids.items()}
             r["accuracy"] = {"steps": accuracy_steps,
                              "rel_l2_fp32_vs_fp64": {k: float(f"{v:.4g}") for k, v in errs.items()},
                              "max": float(f"{max(errs.values()):.4g}")}

@@ -167,6 +167,18 @@ struct Run {
 };
 
 const char *kProg[7] = {"u", "v", "w", "th", "qv", "qc", "qr"};
+
+// the prognostic fields of a configuration: (field id, bundle name)
+std::vector<std::pair<int, std::string>> prog_fields(const Run &run)
+{
+    std::vector<std::pair<int, std::string>> v;
+    for (int f = 0; f < run.nprog; f++) v.emplace_back(f, kProg[f]);
+    if (run.cfg.microphysics_option == 2) {  // snow and cloud ice (microphysics.h:21-22)
+        v.emplace_back(GA_QS, "qs");
+        v.emplace_back(GA_QI, "qi");
+    }
+    return v;
+}
 const char *kBar[6] = {"ubar", "vbar", "wbar", "thbar", "qbar", "pbar"};
 const char *kSlotSuffix[3] = {"", "_p", "_m"};
 
@@ -181,11 +193,11 @@ int save(ga_ctx *ctx, const Run &run, const std::string &path)
 {
     Bundle out;
     std::vector<double> buf(run.n3);
-    for (int f = 0; f < run.nprog; f++)
+    for (const auto &pf : prog_fields(run))
         for (int s = 0; s < 3; s++) {
-            int rc = ga_get_field(ctx, f, s, buf.data(), run.n3);
+            int rc = ga_get_field(ctx, pf.first, s, buf.data(), run.n3);
             if (rc) return fail(rc, "ga_get_field");
-            out[std::string(kProg[f]) + kSlotSuffix[s]] = buf;
+            out[pf.second + kSlotSuffix[s]] = buf;
         }
     int rc = ga_get_field(ctx, GA_PI, 0, buf.data(), run.n3);
     if (rc) return fail(rc, "ga_get_field(pi)");
@@ -198,11 +210,27 @@ int save(ga_ctx *ctx, const Run &run, const std::string &path)
         rc = ga_get_field(ctx, GA_ACCRAIN, 0, acc.data(), run.n2);
         if (rc) return fail(rc, "ga_get_field(accrain)");
         out["accrain"] = acc;
-        if (run.cfg.turbulence_option) {  // Kessler's saturation record feeds the next step's mixing
+        if (run.cfg.turbulence_option) {  // the saturation record feeds the next step's mixing
             rc = ga_get_field(ctx, GA_SATURATED, 0, buf.data(), run.n3);
             if (rc) return fail(rc, "ga_get_field(is_saturated)");
             out["is_saturated"] = buf;
         }
+    }
+    if (run.cfg.microphysics_option == 2) {  // the ice scheme's carried state
+        const int f3[2] = {GA_VTS, GA_VTI};
+        const char *n3[2] = {"sts", "its"};
+        for (int a = 0; a < 2; a++) {
+            rc = ga_get_field(ctx, f3[a], 0, buf.data(), run.n3);
+            if (rc) return fail(rc, "ga_get_field(ice fall speed)");
+            out[n3[a]] = buf;
+        }
+        std::vector<double> acc(run.n2), n0s(1);
+        rc = ga_get_field(ctx, GA_ACCSNOW, 0, acc.data(), run.n2);
+        if (rc) return fail(rc, "ga_get_field(accsnow)");
+        out["accsnow"] = acc;
+        rc = ga_get_field(ctx, GA_N0S, 0, n0s.data(), 1);
+        if (rc) return fail(rc, "ga_get_field(n0s)");
+        out["n0s"] = n0s;
     }
     long long bc = 0;
     double mt = 0;
@@ -270,9 +298,9 @@ int main(int argc, char **argv)
             return 2;
         }
     if (!restart)
-        for (int fi = 0; fi < run.nprog; fi++)
-            if (!run.array(run.in, kProg[fi], run.n3)) {
-                std::fprintf(stderr, "ga_driver: input lacks %s\n", kProg[fi]);
+        for (const auto &pf : prog_fields(run))
+            if (!run.array(run.in, pf.second, run.n3)) {
+                std::fprintf(stderr, "ga_driver: input lacks %s\n", pf.second.c_str());
                 return 2;
             }
     ga_ctx *ctx = nullptr;
@@ -292,11 +320,11 @@ int main(int argc, char **argv)
             ga_destroy(ctx);
             return 2;
         }
-        for (int fi = 0; fi < run.nprog; fi++)
+        for (const auto &pf : prog_fields(run))
             for (int s = 0; s < 3; s++) {
-                const std::vector<double> *a = run.array(st, std::string(kProg[fi]) + kSlotSuffix[s], run.n3);
+                const std::vector<double> *a = run.array(st, pf.second + kSlotSuffix[s], run.n3);
                 if (!a) { ga_destroy(ctx); return 2; }
-                rc = ga_set_field(ctx, fi, s, a->data(), run.n3);
+                rc = ga_set_field(ctx, pf.first, s, a->data(), run.n3);
                 if (rc) { ga_destroy(ctx); return fail(rc, "ga_set_field(restart)"); }
             }
         const std::vector<double> *pi = run.array(st, "pi", run.n3);
@@ -314,23 +342,40 @@ int main(int argc, char **argv)
                 ga_set_field(ctx, GA_SATURATED, 0, sat->data(), run.n3);
             }
         }
+        if (run.cfg.microphysics_option == 2) {
+            const std::vector<double> *sts = run.array(st, "sts", run.n3), *its = run.array(st, "its", run.n3);
+            const std::vector<double> *acc = run.array(st, "accsnow", run.n2), *n0s = run.array(st, "n0s", 1);
+            if (!sts || !its || !acc || !n0s) { ga_destroy(ctx); return 2; }
+            ga_set_field(ctx, GA_VTS, 0, sts->data(), run.n3);
+            ga_set_field(ctx, GA_VTI, 0, its->data(), run.n3);
+            ga_set_field(ctx, GA_ACCSNOW, 0, acc->data(), run.n2);
+            ga_set_field(ctx, GA_N0S, 0, n0s->data(), 1);
+        }
         const std::vector<double> *bc = run.array(st, "bigcounter", 1), *mt = run.array(st, "mtime", 1);
         if (!bc || !mt) { ga_destroy(ctx); return 2; }
         ga_set_counters(ctx, (long long)(*bc)[0], (*mt)[0]);
     } else {
         // initialize_from_output_serial: current = start of step = the perturbation
         const std::vector<double> zero(run.n3, 0.0);
-        for (int fi = 0; fi < run.nprog; fi++) {
-            const std::vector<double> *a = run.array(run.in, kProg[fi], run.n3);
-            if (!a) { std::fprintf(stderr, "ga_driver: input lacks %s\n", kProg[fi]); ga_destroy(ctx); return 2; }
-            ga_set_field(ctx, fi, GA_SLOT_CUR, a->data(), run.n3);
-            ga_set_field(ctx, fi, GA_SLOT_M, a->data(), run.n3);
-            rc = ga_set_field(ctx, fi, GA_SLOT_P, zero.data(), run.n3);
+        for (const auto &pf : prog_fields(run)) {
+            const std::vector<double> *a = run.array(run.in, pf.second, run.n3);
+            if (!a) {
+                std::fprintf(stderr, "ga_driver: input lacks %s\n", pf.second.c_str());
+                ga_destroy(ctx);
+                return 2;
+            }
+            ga_set_field(ctx, pf.first, GA_SLOT_CUR, a->data(), run.n3);
+            ga_set_field(ctx, pf.first, GA_SLOT_M, a->data(), run.n3);
+            rc = ga_set_field(ctx, pf.first, GA_SLOT_P, zero.data(), run.n3);
             if (rc) { ga_destroy(ctx); return fail(rc, "ga_set_field(initial state)"); }
         }
         if (run.cfg.microphysics_option) {
             const std::vector<double> *acc = run.array(run.in, "accrain", run.n2);
             if (acc) ga_set_field(ctx, GA_ACCRAIN, 0, acc->data(), run.n2);
+        }
+        if (run.cfg.microphysics_option == 2) {
+            const std::vector<double> *acc = run.array(run.in, "accsnow", run.n2);
+            if (acc) ga_set_field(ctx, GA_ACCSNOW, 0, acc->data(), run.n2);
         }
     }
 

@@ -8,6 +8,8 @@
     6-step run: every record of the state file (all rotation slots, pi, fall
     speed, rain, the saturation record, counters) bit for bit, in FP64 and
     in FP32, with and without the turbulence scheme;
+  - the ice scheme: a run against the oracle (snow, ice, their fall speeds,
+    snow accumulation and the snow intercept) and its restart;
   - a missing input field is an error, reported before any context exists
     (runs without a GPU).
 """
@@ -81,11 +83,36 @@ def test_driver_physics_switches_match_oracle(driver, tmp_path):
 
 
 @pytest.mark.gpu
+def test_driver_ice_run_matches_oracle(driver, tmp_path):
+    """the ice scheme through the driver: every prognostic field including
+    snow and ice, the ice fall speed, the accumulations and the snow
+    intercept against the oracle after 6 steps written every 3"""
+    from oracle import oracle as O
+    from oracle.ga_bundle import read_bundle, write_bundle
+    wl = configs.ice_cloud(nx=24, ny=22, nz=20, nsteps=6)
+    inp = str(tmp_path / "in.bin")
+    write_bundle(inp, _bundle(wl))
+    _run(driver, inp, str(tmp_path / "run"), "--steps", "6", "--every", "3")
+    st = read_bundle(str(tmp_path / "run_6.bin"))
+    o = O.Oracle(wl)
+    assert o.step(6) == 0
+    ref = o.state()
+    for k in ("u", "v", "w", "th", "qv", "qc", "qr", "qs", "qi", "qs_m", "qi_m", "pi", "its", "accrain",
+              "accsnow", "n0s"):
+        e = fx.rel_l2(st[k], ref[k])
+        assert e <= 1e-10, f"{k}: rel L2 {e:.3e}"
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("precision", ["f64", "f32"])
 @pytest.mark.parametrize("turbulence", [0, 1])
-def test_driver_restart_is_exact(driver, tmp_path, precision, turbulence):
+@pytest.mark.parametrize("scheme", ["kessler", "ice"])
+def test_driver_restart_is_exact(driver, tmp_path, precision, turbulence, scheme):
     from oracle.ga_bundle import read_bundle, write_bundle
-    wl = configs.moist_blob(nx=24, ny=22, nz=16, nsteps=6)
+    if scheme == "ice":
+        wl = configs.ice_cloud(nx=24, ny=22, nz=20, nsteps=6)
+    else:
+        wl = configs.moist_blob(nx=24, ny=22, nz=16, nsteps=6)
     wl.turbulence_option = turbulence
     inp = str(tmp_path / "in.bin")
     write_bundle(inp, _bundle(wl))
@@ -108,3 +135,8 @@ def test_driver_rejects_missing_input(driver, tmp_path):
     write_bundle(inp, b)
     r = subprocess.run([driver, inp, str(tmp_path / "x"), "--steps", "2"], capture_output=True, text=True)
     assert r.returncode != 0 and "qc" in r.stderr
+    b = _bundle(configs.ice_cloud(nx=24, ny=22, nz=12, nsteps=2))
+    del b["qs"]
+    write_bundle(inp, b)
+    r = subprocess.run([driver, inp, str(tmp_path / "x"), "--steps", "2"], capture_output=True, text=True)
+    assert r.returncode != 0 and "qs" in r.stderr
