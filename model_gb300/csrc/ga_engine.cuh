@@ -285,7 +285,6 @@ class Engine : public EngineBase {
             n0s_pt = dalloc<T>(N);
             n0s_idx = dalloc<int>(1);
             if (n0s_idx) cudaMemset(n0s_idx, 0xff, sizeof(int));  // -1: no snowy point recorded
-            adv_force = 1;  // the per-level tile kernel (snow and ice buoyancy, stored fall speeds)
         }
 
         // ---- Rayleigh coefficients (damping.cpp:1150-1162) ----
@@ -505,7 +504,7 @@ class Engine : public EngineBase {
         cudaFuncSetAttribute(k_advect_tile<T, 4, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
         cudaFuncSetAttribute(k_advect_tile<T, 4, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
         cudaFuncSetAttribute(k_advect_tile<T, 8, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
-        if (const char *ev = std::getenv("GA_ADVECT"); ev && !ice) {
+        if (const char *ev = std::getenv("GA_ADVECT")) {
             if (!std::strcmp(ev, "tile")) adv_force = 1;
             else if (!std::strcmp(ev, "quad")) adv_force = 2;
             else if (!std::strcmp(ev, "tma")) adv_force = 3;
@@ -902,7 +901,9 @@ class Engine : public EngineBase {
     // driver's tensor-map encoder and the candidate's shared memory
     bool tma_ok(int c) const
     {
-        if (!(sizeof(T) == 4 && kp.ubase_adv && NZ % 4 == 0 && c >= 0 && c < 4 && tma_encoder())) return false;
+        // the staged boxes hold the seven fields of the Kessler step, not snow and ice
+        if (!(sizeof(T) == 4 && kp.ubase_adv && NZ % 4 == 0 && c >= 0 && c < 4 && !kp.ice && tma_encoder()))
+            return false;
         const TmaCand &t = kTmaCands[c];
         return advect_tma_smem(t.ti, t.tj, t.kz, NZ, kp.moist ? 7 : 4) <= 200 * 1024;
     }
@@ -1440,13 +1441,22 @@ class Engine : public EngineBase {
             }
             if (kp.ice) {  // driver_serial.cpp:198-247 with advect_ice_cell
                 // the Rutledge fall speeds read the pressure of this stage's
-                // solve, so the moisture advection follows it
-                advect(st, ADV_UV | ADV_WB | ADV_TH);
+                // solve, so the moisture advection follows it; the four-level
+                // kernel (FP32) advects snow and ice in the same launch
+                const bool quad = adv_quad && quad_ok(adv_qi, adv_qj) && !(adv_tma && tma_ok(adv_tmc));
+                const bool fuse = !kp.periodic && quad;
+                advect(st, ADV_UV | ADV_WB | ADV_TH | (fuse ? ADV_MIRROR : 0));
                 if (turbulent) turb_apply(TA_VEL | TA_TH, st);
-                solve_pressure(st);
+                if (fuse) poisson(st);
+                else solve_pressure(st);
                 if (kp.rf == 1) ice_fall_euler(IF_RAIN | IF_SNOW | IF_ICE);
-                advect(st, ADV_Q | (turbulent ? 0 : ADV_ZERO));
-                advect_ice(st);
+                const int zero = turbulent ? 0 : ADV_ZERO;
+                if (quad) {
+                    advect(st, ADV_Q | ADV_ICE | zero);
+                } else {
+                    advect(st, ADV_Q | zero);
+                    advect_ice(st);
+                }
                 if (turbulent) turb_apply(TA_Q, st);
                 int fl[9] = {};
                 fl[FU] = fl[FV] = fl[FW] = PF_PROJECT | PF_SPONGE | PF_VBC;

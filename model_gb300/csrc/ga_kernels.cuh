@@ -401,8 +401,10 @@ __device__ T s_tend(const KParams<T> &p, const KFields<T> &F, const T *s, const 
 // lateral mirror copies of P u, v, w that precede the pressure solve; they read
 // and write only points the advection does not write.  ADV_ROWS (four-level
 // kernel): east and north faces by sliding rows instead of one per work item
+// ADV_QVONLY (with ADV_Q): the vapour alone (advect_qv, advection.cpp:577-601).
+// ADV_ICE (four-level kernel, ice scheme): snow and cloud ice too
 enum { ADV_UV = 1, ADV_WB = 2, ADV_TH = 4, ADV_Q = 8, ADV_ZERO = 16, ADV_MIRROR = 32, ADV_ROWS = 64,
-       ADV_QVONLY = 128 };  // with ADV_Q: the vapour alone (advect_qv, advection.cpp:577-601)
+       ADV_QVONLY = 128, ADV_ICE = 256 };
 
 template <typename T>
 __global__ void __launch_bounds__(128) k_advect(KParams<T> p, KFields<T> F, T step, T sdtg, int what)

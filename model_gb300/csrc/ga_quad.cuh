@@ -84,10 +84,12 @@ __device__ __forceinline__ Win ldwin(const float *a, int c, int k0, int nz)
     return w;
 }
 
-// field kinds of the passes: 0 u, 1 v, 2 theta, 3 qv, 4 qc, 5 qr
+// field kinds of the passes: 0 u, 1 v, 2 theta, 3 qv, 4 qc, 5 qr, and with
+// the ice scheme 6 snow, 7 cloud ice (5-7 fall with their fall speeds)
 __host__ __device__ constexpr int aq_field(int fk)
 {
-    return fk == 0 ? FU : fk == 1 ? FV : fk == 2 ? FTH : fk == 3 ? FQV : fk == 4 ? FQC : FQR;
+    return fk == 0 ? FU : fk == 1 ? FV : fk == 2 ? FTH : fk == 3 ? FQV : fk == 4 ? FQC : fk == 5 ? FQR
+           : fk == 6 ? FQS : FQI;
 }
 // basic-state row of a scalar (brow of s_*_ub): 0 theta, 1 qv, -1 none
 __host__ __device__ constexpr int aq_brow(int fk) { return fk == 2 ? 0 : fk == 3 ? 1 : -1; }
@@ -111,8 +113,8 @@ struct GSrc {
     {
         return ldwin(F.cur[f], c + di * sx + dj * sy, k0, nz);
     }
-    // stored fall speed at level k0 + e of column (i, j)
-    __device__ __forceinline__ float vt(int i, int j, int k0, int c, int e) const { return F.vt[c + e]; }
+    // stored fall speed (array a) at level k0 + e of column (i, j)
+    __device__ __forceinline__ float vt(const float *a, int i, int j, int k0, int c, int e) const { return a[c + e]; }
 };
 
 // SSrc: halo boxes of the fields in shared memory, [i][j][k] with BJ x BK
@@ -145,9 +147,9 @@ struct SSrc {
         }
         return w;
     }
-    __device__ __forceinline__ float vt(int i, int j, int k0, int c, int e) const
+    __device__ __forceinline__ float vt(const float *a, int i, int j, int k0, int c, int e) const
     {
-        return F.vt[gix(ny, nz, i, j, k0) + e];
+        return a[gix(ny, nz, i, j, k0) + e];
     }
 };
 
@@ -410,7 +412,7 @@ __device__ __forceinline__ Q4 aq_top(const KParams<float> &p, const S &src, cons
             }
             r.v[e] = f;
         }
-    } else if (FK != 5) {
+    } else if (FK < 5) {
         constexpr int BR = aq_brow(FK);
 #pragma unroll
         for (int e = 0; e < 4; e++) {
@@ -435,18 +437,20 @@ __device__ __forceinline__ Q4 aq_top(const KParams<float> &p, const S &src, cons
             r.v[e] = f;
         }
     } else {
-        // rain: the fall speed at levels k0..k0+4 (vt_at)
+        // rain, snow, ice: the fall speed at levels k0..k0+4 (vt_at; the
+        // ice scheme's speeds are stored by their own kernel)
+        const float *fa = FK == 5 ? src.F.vt : FK == 6 ? src.F.sts : src.F.its;
         float vt[5];
 #pragma unroll
         for (int e = 0; e < 5; e++) {
             const int k = k0 + e;
             float v = 0.f;
             if (k < nz) {
-                if (p.rf == 1 && k < nz - 1) {
+                if (FK == 5 && p.rf == 1 && !p.ice && k < nz - 1) {
                     const int kk = k == 0 ? 1 : k;
                     v = fall_speed_point(p, x.at(kk - k0), kk);
                 } else {
-                    v = src.vt(i, j, k0, c, e);
+                    v = src.vt(fa, i, j, k0, c, e);
                 }
             }
             vt[e] = v;
@@ -657,6 +661,14 @@ __device__ __forceinline__ void advect_quad_cells(const KParams<float> &p, const
                     if (!p.moist) bb[e] = th.at(e - 1) / s_tbv[kc];
                     else bb[e] = th.at(e - 1) / s_tbv[kc] + 0.61f * qv.at(e - 1) - qc.at(e - 1) - qr.at(e - 1);
                 }
+                if (p.ice) {  // buoyancy_cold_micro (advection.cpp:56-58): less ice, then snow
+                    const Win qi = src.win(FQI, cs, 0, 0, k0);
+#pragma unroll
+                    for (int e = 0; e < 5; e++) bb[e] = bb[e] - qi.at(e - 1);
+                    const Win qs = src.win(FQS, cs, 0, 0, k0);
+#pragma unroll
+                    for (int e = 0; e < 5; e++) bb[e] = bb[e] - qs.at(e - 1);
+                }
                 const Q4 m = ldg4(F.M[FW], c);
 #pragma unroll
                 for (int e = 0; e < 4; e++) rw.v[e] = m.v[e] + sdtg * (bb[e + 1] + bb[e]);
@@ -766,7 +778,7 @@ __device__ __forceinline__ void advect_quad_cells(const KParams<float> &p, const
                     if (k >= 1 && k <= nz - 2) qm[e] |= bits[e];
                 }
             }
-            if (p.rf == 1) {
+            if (p.rf == 1 && !p.ice) {
                 // fall speed of the advected cells; level 0 repeats level 1
                 const Q4 qrc = src.ld4(FQR, cs, 0, 0);
 #pragma unroll
@@ -776,6 +788,38 @@ __device__ __forceinline__ void advect_quad_cells(const KParams<float> &p, const
                     if (k == 1) F.vt[c + e - 1] = fall_speed_point(p, qrc.v[e], 1);
                 }
             }
+        }
+    }
+
+    // ---- pass 4 (ice scheme): snow and cloud ice with their fall speeds
+    // (advect_ice_cell, advection.cpp:508-567), clipped with the moisture
+    if (what & ADV_ICE) {
+        __syncthreads();
+        aq_faces<TI, TJ, 6>(p, F, src, tab, s0, i0, j0, ti, tj, rows, ks, ke, kb, SK);
+        aq_faces<TI, TJ, 7>(p, F, src, tab, s1, i0, j0, ti, tj, rows, ks, ke, kb, SK);
+        __syncthreads();
+        for (int w = threadIdx.x; w < G::CT * NQ; w += AQ_THREADS) {
+            const int q = w % NQ, col = w / NQ, b = col % TJ, a = col / TJ;
+            if (a >= ti || b >= tj) continue;
+            const int i = i0 + a, j = j0 + b, k0 = ks + 4 * q;
+            const int c = gix(p.ny, nz, i, j, k0);
+            const Q4 ds = aq_div<TI, TJ>(p, s0, lv, a, b, k0, kb, SK);
+            const Q4 di = aq_div<TI, TJ>(p, s1, lv, a, b, k0, kb, SK);
+            const Q4 ms = ldg4(F.M[FQS], c), mi = ldg4(F.M[FQI], c);
+            Q4 rs, ri;
+#pragma unroll
+            for (int e = 0; e < 4; e++) {
+                float qs = ms.v[e] + step * ds.v[e];
+                float qi = mi.v[e] + step * di.v[e];
+                if (what & ADV_ZERO) {
+                    if (qs < 0) qs = 0;
+                    if (qi < 0) qi = 0;
+                }
+                rs.v[e] = qs;
+                ri.v[e] = qi;
+            }
+            aq_store(F.P[FQS], c, k0, nz, 1, rs);
+            aq_store(F.P[FQI], c, k0, nz, 1, ri);
         }
     }
 }

@@ -259,3 +259,24 @@ def test_autotuner_races_the_staged_kernel(monkeypatch):
     m = anelastic.Model(wl, abi.GA_PREC_F32)
     info = m.tune()
     assert "staged by TMA" in info, info
+
+
+@pytest.mark.parametrize("faces", ["single", "rows"])
+@pytest.mark.parametrize("rf", [1, 2])
+def test_ice_step_four_level_matches_tile(monkeypatch, faces, rf):
+    """the ice scheme's FP32 step with the four-level kernel (ice buoyancy,
+    the stored Rutledge rain fall speed, the snow and ice pass) against the
+    per-level kernels (k_advect_tile and k_advect_ice): every prognostic
+    field, snow and ice within 1e-5 relative L2 after 4 steps.  The two
+    snow and ice advections contract their multiply-adds differently, and
+    the microphysics' thresholds let last-bit differences grow: cloud ice
+    differs by 1.1e-6 with semi-Lagrangian fallout."""
+    wl = configs.ice_cloud(nx=40, ny=36, nz=32, dz=375.0, rain_fallout=rf)
+    ms = _pair(monkeypatch, wl, tile="4x8", faces=faces)
+    for m in ms:
+        m.step(4)
+    for f in list(range(7)) + [abi.GA_QS, abi.GA_QI]:
+        a, b = ms[0].get(f), ms[1].get(f)
+        assert np.isfinite(b).all(), f
+        e = fx.rel_l2(b, a)
+        assert e <= 1e-5, (f, e)
