@@ -6,6 +6,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <map>
 #include <memory>
 #include <tuple>
@@ -132,6 +133,31 @@ class Engine : public EngineBase {
     unsigned char *turb_sat = nullptr;
     double *lin_vmax = nullptr;  // the linearised model's rescaling maximum
     HydArgs<T> hyd{};            // the hydrostatic equation set (hyd.div null when off)
+    // a second stream for the theta and moisture advection, which needs
+    // nothing of the stage's pressure solve and runs beside it (forked from
+    // and joined back into `stream`; captured into the same graph).  On when
+    // the x solve (one block per y-wavenumber) leaves SMs idle; GA_OVERLAP=0
+    // or =1 overrides
+    cudaStream_t stream2 = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    bool overlap = true;
+    std::function<void()> mid_solve;  // queued by poisson() after its first launch
+    // launches inside run on the second stream (the launch helpers use `stream`)
+    struct OnSide {
+        Engine *e;
+        explicit OnSide(Engine *x) : e(x) { std::swap(e->stream, e->stream2); }
+        ~OnSide() { std::swap(e->stream, e->stream2); }
+    };
+    void fork()
+    {
+        cudaEventRecord(ev_fork, stream);
+        cudaStreamWaitEvent(stream2, ev_fork, 0);
+    }
+    void join()
+    {
+        cudaEventRecord(ev_join, stream2);
+        cudaStreamWaitEvent(stream, ev_join, 0);
+    }
     int hyd_L = 1;               // y-lines per block of its x transforms
 
     // Fornberg's recurrence for finite-difference weights: c[i*(m+1)+d] is the
@@ -242,6 +268,22 @@ class Engine : public EngineBase {
         device = c->device;
         if (cudaSetDevice(device) != cudaSuccess) { status = GA_ERR_CUDA; return; }
         if (cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking) != cudaSuccess) { status = GA_ERR_CUDA; return; }
+        // the second stream at the lowest priority: the solve's blocks, on the
+        // step's critical path, are dispatched first as SMs free up
+        int prio_lo = 0, prio_hi = 0;
+        cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
+        if (cudaStreamCreateWithPriority(&stream2, cudaStreamNonBlocking, prio_lo) != cudaSuccess ||
+            cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming) != cudaSuccess) {
+            status = GA_ERR_CUDA;
+            return;
+        }
+        {
+            int nsm = 0;
+            cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
+            overlap = c->ny <= nsm;  // kp.nj = NY blocks in the x solve
+            if (const char *ev = std::getenv("GA_OVERLAP")) overlap = std::strcmp(ev, "0") != 0;
+        }
         const bool moist = c->microphysics_option >= 1;
         const bool ice = c->microphysics_option == 2;
         nprog = ice ? 9 : moist ? 7 : 4;
@@ -562,6 +604,10 @@ class Engine : public EngineBase {
             if (g) cudaGraphExecDestroy(g);
         for (void *p : allocs) cudaFree(p);
         if (staging) cudaFree(staging);
+        if (stream2) cudaStreamSynchronize(stream2);
+        if (ev_fork) cudaEventDestroy(ev_fork);
+        if (ev_join) cudaEventDestroy(ev_join);
+        if (stream2) cudaStreamDestroy(stream2);
         if (stream) cudaStreamDestroy(stream);
     }
 
@@ -1063,6 +1109,11 @@ class Engine : public EngineBase {
             ProfScope ps(this, PC_DIV_FFT_Y, 1);
             k_div_fft_y<T><<<dim3(nkt_y, kp.ni), by_y, smem_y, stream>>>(kp, F, spec, plan_j, tw_j, sdt, KTy);
         }
+        if (mid_solve) {  // work queued beside the rest of the solve (the x solve leaves SMs idle)
+            auto fn = std::move(mid_solve);
+            mid_solve = nullptr;
+            fn();
+        }
         if (psx > 0) {
             ProfScope ps(this, PC_THOMAS, 1);
             const int nl = NZ - 2, bx = std::min(nl, 64);
@@ -1445,8 +1496,16 @@ class Engine : public EngineBase {
                 // kernel (FP32) advects snow and ice in the same launch
                 const bool quad = adv_quad && quad_ok(adv_qi, adv_qj) && !(adv_tma && tma_ok(adv_tmc));
                 const bool fuse = !kp.periodic && quad;
-                advect(st, ADV_UV | ADV_WB | ADV_TH | (fuse ? ADV_MIRROR : 0));
-                if (turbulent) turb_apply(TA_VEL | TA_TH, st);
+                const bool side = overlap && !prof;  // theta beside the solve
+                advect(st, ADV_UV | ADV_WB | (side ? 0 : ADV_TH) | (fuse ? ADV_MIRROR : 0));
+                if (turbulent) turb_apply(side ? TA_VEL : TA_VEL | TA_TH, st);
+                if (side)
+                    mid_solve = [this, st, turbulent] {
+                        fork();
+                        OnSide os(this);
+                        advect(st, ADV_TH);
+                        if (turbulent) turb_apply(TA_TH, st);
+                    };
                 if (fuse) poisson(st);
                 else solve_pressure(st);
                 if (kp.rf == 1) ice_fall_euler(IF_RAIN | IF_SNOW | IF_ICE);
@@ -1458,6 +1517,7 @@ class Engine : public EngineBase {
                     advect_ice(st);
                 }
                 if (turbulent) turb_apply(TA_Q, st);
+                if (side) join();
                 int fl[9] = {};
                 fl[FU] = fl[FV] = fl[FW] = PF_PROJECT | PF_SPONGE | PF_VBC;
                 fl[FTH] = PF_SPONGE | PF_VBC;
@@ -1474,11 +1534,32 @@ class Engine : public EngineBase {
             // post-processing pass then applies; they touch no point that the
             // mirror copies read
             const int zero = turbulent ? 0 : ADV_ZERO;
-            advect(st, ADV_UV | ADV_WB | ADV_TH | (moist ? (ADV_Q | zero) : 0) | (fuse_mirror ? ADV_MIRROR : 0));
-            if (turbulent) turb_apply(TA_VEL | TA_TH | TA_Q, st);
-            qmask = nullptr;
-            if (fuse_mirror) poisson(st);
-            else solve_pressure(st);
+            const int scal = ADV_TH | (moist ? (ADV_Q | zero) : 0);
+            if (overlap && !prof) {
+                // theta and moisture beside the pressure solve: they read the
+                // current and start-of-step fields, which the solve leaves alone
+                advect(st, ADV_UV | ADV_WB | (fuse_mirror ? ADV_MIRROR : 0));
+                if (turbulent) turb_apply(TA_VEL, st);
+                unsigned char *qm = qmask;
+                mid_solve = [this, st, scal, turbulent, qm] {
+                    fork();
+                    OnSide os(this);
+                    qmask = qm;
+                    advect(st, scal);
+                    qmask = nullptr;
+                    if (turbulent) turb_apply(TA_TH | TA_Q, st);
+                };
+                qmask = nullptr;
+                if (fuse_mirror) poisson(st);
+                else solve_pressure(st);
+                join();
+            } else {
+                advect(st, ADV_UV | ADV_WB | scal | (fuse_mirror ? ADV_MIRROR : 0));
+                if (turbulent) turb_apply(TA_VEL | TA_TH | TA_Q, st);
+                qmask = nullptr;
+                if (fuse_mirror) poisson(st);
+                else solve_pressure(st);
+            }
             int fl[9] = {};
             fl[FU] = fl[FV] = fl[FW] = PF_PROJECT | PF_SPONGE | PF_VBC;
             fl[FTH] = PF_SPONGE | PF_VBC;
