@@ -1478,9 +1478,19 @@ class Engine : public EngineBase {
                                     cudaMemcpyDeviceToDevice, stream);
             qmask = mrec ? mrec + (size_t)s * N : nullptr;
             if (hyd.div) {  // the hydrostatic set: driver_serial.cpp:208-239 with integrate_hydro
-                advect(st, ADV_UV | ADV_TH | (moist ? (ADV_Q | ADV_ZERO) : 0));
+                // theta and moisture beside the lid-pressure solve; joined
+                // before w_velocity_LH rewrites the current w they read
+                const int scal = ADV_TH | (moist ? (ADV_Q | ADV_ZERO) : 0);
+                const bool side = overlap && !prof;
+                advect(st, ADV_UV | (side ? 0 : scal));
+                if (side) {
+                    fork();
+                    OnSide os(this);
+                    advect(st, scal);
+                }
                 hyd_solve(st);
                 hyd_project(st);
+                if (side) join();
                 hyd_w();
                 int fh[9] = {};
                 fh[FU] = fh[FV] = fh[FW] = fh[FTH] = PF_SPONGE | PF_VBC;  // w: the current slot
@@ -1602,8 +1612,16 @@ class Engine : public EngineBase {
         kp.stale_signs = 1;
         for (int s = 0; s < 3; s++) {
             const double st = steps[s];
-            advect(st, ADV_UV | ADV_WB | ADV_TH);
+            const bool side = overlap && !prof;  // theta beside the pressure solve
+            advect(st, ADV_UV | ADV_WB | (side ? 0 : ADV_TH));
+            if (side)
+                mid_solve = [this, st] {
+                    fork();
+                    OnSide os(this);
+                    advect(st, ADV_TH);
+                };
             solve_pressure(st);
+            if (side) join();
             int fl[9] = {};
             fl[FU] = fl[FV] = fl[FW] = PF_PROJECT | PF_SPONGE | PF_VBC;
             fl[FTH] = PF_SPONGE | PF_VBC;
