@@ -266,16 +266,20 @@ GA_API int ga_get_counters(ga_ctx *ctx, long long *bigcounter, double *mtime);
  * i in [1, NX-1), j in [1, NY-1), k in [1, NZ-1) with the density-times-volume
  * weight rhou[k] dx dy dz / mu[k]:
  *   GA_BUDGET_THETA  sum of rho theta' dV      GA_BUDGET_WATER  QV + QC + QR
- *   GA_BUDGET_QV / _QC / _QR  rho q dV        GA_BUDGET_KE     0.5 rho |u'|^2 dV
+ *   GA_BUDGET_QV / _QC / _QR  rho q dV          (+ QI + QS with the ice scheme)
+ *   GA_BUDGET_KE     0.5 rho |u'|^2 dV
  *   GA_BUDGET_RAIN   accumulated surface rain times dx dy (GA_ACCRAIN)
  *   GA_BUDGET_MASS   sum of rho dV
+ *   GA_BUDGET_QI / _QS  rho q dV of cloud ice and snow, GA_BUDGET_SNOW the
+ *   accumulated snow times dx dy (GA_ACCSNOW); 0 without the ice scheme
  * The flux form of the advection (advection.cpp:304-498) conserves the
  * theta, moisture and water integrals up to the fluxes through the domain's
  * boundary and the base-state terms; Kessler (kessler.cpp:25-213) conserves
  * the total water of every point.  The blocks' partial sums are added in a
  * fixed order, so repeated calls on the same state give the same bits.  The
  * reference computes no budget on its step path (its energy diagnostics,
- * energy.cpp, are out of this library's scope).  n must be >= GA_NBUDGET. */
+ * energy.cpp, are out of this library's scope).  n must be at least 8 (the
+ * entries up to GA_BUDGET_MASS); min(n, GA_NBUDGET) entries are written. */
 #define GA_BUDGET_THETA 0
 #define GA_BUDGET_QV    1
 #define GA_BUDGET_QC    2
@@ -284,7 +288,10 @@ GA_API int ga_get_counters(ga_ctx *ctx, long long *bigcounter, double *mtime);
 #define GA_BUDGET_KE    5
 #define GA_BUDGET_RAIN  6
 #define GA_BUDGET_MASS  7
-#define GA_NBUDGET      8
+#define GA_BUDGET_QI    8
+#define GA_BUDGET_QS    9
+#define GA_BUDGET_SNOW  10
+#define GA_NBUDGET      11
 GA_API int ga_budget(ga_ctx *ctx, int slot, double *out, int n);
 
 /* Set the step counter and model time (a restart: bigcounter and mtime as

@@ -53,7 +53,7 @@ PROG_NAMES = ["u", "v", "w", "th", "qv", "qc", "qr"]
 BAR_NAMES = ["ubar", "vbar", "wbar", "thbar", "qbar", "pbar"]
 SLOT_SUFFIX = {GA_SLOT_CUR: "", GA_SLOT_P: "_p", GA_SLOT_M: "_m"}
 # ga_budget entries (GA_BUDGET_*)
-BUDGET_NAMES = ["theta", "qv", "qc", "qr", "water", "ke", "rain", "mass"]
+BUDGET_NAMES = ["theta", "qv", "qc", "qr", "water", "ke", "rain", "mass", "qi", "qs", "snow"]
 GA_NBUDGET = len(BUDGET_NAMES)
 COLUMN_NAMES = ["zu", "zw", "zsu", "zsw", "mu", "mw", "rhou", "rhow", "one_d_rhou",
                 "one_d_rhow", "tb", "tbv", "tbw", "qb", "pib"]

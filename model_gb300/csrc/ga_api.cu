@@ -227,9 +227,12 @@ int ga_get_counters(ga_ctx *ctx, long long *bigcounter, double *mtime)
 
 int ga_budget(ga_ctx *ctx, int slot, double *out, int n)
 {
-    if (!ctx || !out || n < GA_NBUDGET) return fail(GA_ERR_ARG, "ga_budget: bad arguments");
+    if (!ctx || !out || n < GA_BUDGET_MASS + 1) return fail(GA_ERR_ARG, "ga_budget: bad arguments");
     if (slot < 0 || slot > 2) return fail(GA_ERR_ARG, "ga_budget: bad slot");
-    return ctx->e->budget(slot, out);
+    double all[GA_NBUDGET];
+    const int rc = ctx->e->budget(slot, all);
+    for (int b = 0; b < n && b < GA_NBUDGET; b++) out[b] = all[b];
+    return rc;
 }
 
 int ga_set_counters(ga_ctx *ctx, long long bigcounter, double mtime)

@@ -1930,8 +1930,8 @@ class Engine : public EngineBase {
             return buf[f][slot == GA_SLOT_CUR ? ci[f] : slot == GA_SLOT_P ? pi_[f] : mi[f]];
         };
         k_budget<T><<<BUDGET_BLOCKS, 256, 0, stream>>>(NX, NY, NZ, sl(FU), sl(FV), sl(FW), sl(FTH), sl(FQV), sl(FQC),
-                                                       sl(FQR), kp.moist ? accrain : nullptr, budget_w,
-                                                       cfg.dx * cfg.dy, budget_part);
+                                                       sl(FQR), sl(FQI), sl(FQS), kp.moist ? accrain : nullptr,
+                                                       accsnow, budget_w, cfg.dx * cfg.dy, budget_part);
         k_budget_sum<<<1, 32, 0, stream>>>(budget_part, BUDGET_BLOCKS, budget_part + (size_t)BUDGET_BLOCKS * GA_NB);
         launches += 2;
         int rc = launch_status();
@@ -1940,7 +1940,7 @@ class Engine : public EngineBase {
         cudaMemcpyAsync(h, budget_part + (size_t)BUDGET_BLOCKS * GA_NB, sizeof h, cudaMemcpyDeviceToHost, stream);
         rc = sync_status();
         if (rc) return rc;
-        h[4] = h[1] + h[2] + h[3];
+        h[4] = h[1] + h[2] + h[3] + h[8] + h[9];  // total water (ice and snow 0 without the ice scheme)
         for (int b = 0; b < GA_NB; b++) out[b] = h[b];
         return GA_OK;
     }

@@ -2326,13 +2326,14 @@ __global__ void __launch_bounds__(256) k_diffuse_into(KParams<T> p, KFields<T> F
 // Each block writes its GA_NB partial sums; k_budget_sum adds the blocks in
 // index order, so the result does not depend on the schedule.
 // ---------------------------------------------------------------------------
-constexpr int GA_NB = 8;
+constexpr int GA_NB = 11;  // GA_NBUDGET
 constexpr int BUDGET_BLOCKS = 304;
 
 template <typename T>
 __global__ void __launch_bounds__(256) k_budget(int nx, int ny, int nz, const T *u, const T *v, const T *w,
                                                 const T *th, const T *qv, const T *qc, const T *qr,
-                                                const double *accrain, const double *wk, double dxdy, double *part)
+                                                const T *qi, const T *qs, const double *accrain,
+                                                const double *accsnow, const double *wk, double dxdy, double *part)
 {
     double acc[GA_NB];
 #pragma unroll
@@ -2350,6 +2351,10 @@ __global__ void __launch_bounds__(256) k_budget(int nx, int ny, int nz, const T 
             acc[2] += wt * (double)qc[t];
             acc[3] += wt * (double)qr[t];
         }
+        if (qi) {  // the ice scheme's cloud ice and snow
+            acc[8] += wt * (double)qi[t];
+            acc[9] += wt * (double)qs[t];
+        }
         const double uu = u[t], vv = v[t], ww = w[t];
         acc[5] += wt * 0.5 * (uu * uu + vv * vv + ww * ww);
         acc[7] += wt;
@@ -2357,7 +2362,10 @@ __global__ void __launch_bounds__(256) k_budget(int nx, int ny, int nz, const T 
     if (accrain) {
         for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < (long)nx * ny; t += stride) {
             const int j = (int)(t % ny), i = (int)(t / ny);
-            if (i >= 1 && i < nx - 1 && j >= 1 && j < ny - 1) acc[6] += accrain[t] * dxdy;
+            if (i >= 1 && i < nx - 1 && j >= 1 && j < ny - 1) {
+                acc[6] += accrain[t] * dxdy;
+                if (accsnow) acc[10] += accsnow[t] * dxdy;
+            }
         }
     }
     __shared__ double red[8][GA_NB];

@@ -34,20 +34,22 @@ def _weights(wl, cols):
     return np.asarray(cols["rhou"]) * wl.dx * wl.dy * wl.dz / np.asarray(cols["mu"])
 
 
-def _np_budget(wl, cols, fields, accrain=None):
+def _np_budget(wl, cols, fields, accrain=None, accsnow=None):
     """The same sums in numpy (FP64)."""
     wk = _weights(wl, cols)
     sl = (slice(1, wl.nx - 1), slice(1, wl.ny - 1), slice(1, wl.nz - 1))
     g = lambda a: np.asarray(a, dtype=np.float64).reshape(wl.nx, wl.ny, wl.nz)[sl]  # noqa: E731
     w = wk[1:-1][None, None, :]
     out = {"theta": float(np.sum(w * g(fields["th"])))}
-    for q in ("qv", "qc", "qr"):
+    for q in ("qv", "qc", "qr", "qi", "qs"):
         out[q] = float(np.sum(w * g(fields[q]))) if q in fields else 0.0
-    out["water"] = out["qv"] + out["qc"] + out["qr"]
+    out["water"] = out["qv"] + out["qc"] + out["qr"] + out["qi"] + out["qs"]
     out["ke"] = float(np.sum(w * 0.5 * (g(fields["u"]) ** 2 + g(fields["v"]) ** 2 + g(fields["w"]) ** 2)))
     out["rain"] = 0.0 if accrain is None else float(
         np.sum(np.asarray(accrain).reshape(wl.nx, wl.ny)[1:-1, 1:-1]) * wl.dx * wl.dy)
     out["mass"] = float(np.sum(w * np.ones_like(g(fields["th"]))))
+    out["snow"] = 0.0 if accsnow is None else float(
+        np.sum(np.asarray(accsnow).reshape(wl.nx, wl.ny)[1:-1, 1:-1]) * wl.dx * wl.dy)
     return out
 
 
@@ -71,6 +73,38 @@ def test_fp64_budgets_match_oracle_state():
     ref = _np_budget(wl, cols, fields, o.get(abi.GA_ACCRAIN))
     _close(got, ref, 1e-12, "fp64 vs oracle")
     assert got["rain"] > 0 and got["qr"] > 0
+
+
+@pytest.mark.parametrize("prec", [abi.GA_PREC_F64, abi.GA_PREC_F32])
+def test_ice_budgets_match_state(prec):
+    """the ice scheme's budgets: cloud ice, snow, accumulated snow, and the
+    total water with them, against numpy sums of the oracle's state (FP64)
+    or of the context's own fields (FP32, accumulated in FP64); a caller
+    passing the first 8 entries gets them"""
+    import ctypes as C
+    from oracle import oracle as O
+    wl = configs.ice_cloud(nx=30, ny=26, nz=16, dz=750.0, nsteps=4)
+    cols = anelastic.build_columns(wl)
+    m = anelastic.Model(wl, prec, columns=cols)
+    m.step(wl.nsteps)
+    got = m.budget(abi.GA_SLOT_CUR)
+    names = list(abi.PROG_NAMES) + ["qs", "qi"]
+    fids = list(range(7)) + [abi.GA_QS, abi.GA_QI]
+    if prec == abi.GA_PREC_F64:
+        o = O.Oracle(wl, cols)
+        assert o.step(wl.nsteps) == 0
+        fields = {n: o.get(f) for f, n in zip(fids, names)}
+        ref = _np_budget(wl, cols, fields, o.get(abi.GA_ACCRAIN), o.get(abi.GA_ACCSNOW))
+        _close(got, ref, 1e-12, "ice fp64 vs oracle")
+    else:
+        fields = {n: m.get(f) for f, n in zip(fids, names)}
+        ref = _np_budget(wl, cols, fields, m.get(abi.GA_ACCRAIN), m.get(abi.GA_ACCSNOW))
+        _close(got, ref, 1e-13, "ice fp32")
+    assert got["qi"] > 0 and got["qs"] > 0 and got["snow"] > 0
+    assert got["water"] == got["qv"] + got["qc"] + got["qr"] + got["qi"] + got["qs"]
+    short = (C.c_double * 8)()
+    assert m.L.ga_budget(m.h, abi.GA_SLOT_CUR, short, 8) == 0
+    assert list(short) == [got[n] for n in abi.BUDGET_NAMES[:8]]
 
 
 def test_fp32_budgets_accumulate_in_fp64():
