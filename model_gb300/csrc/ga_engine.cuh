@@ -1483,18 +1483,25 @@ class Engine : public EngineBase {
                 const int scal = ADV_TH | (moist ? (ADV_Q | ADV_ZERO) : 0);
                 const bool side = overlap && !prof;
                 advect(st, ADV_UV | (side ? 0 : scal));
-                if (side) {
+                if (side) {  // with their column pass
                     fork();
                     OnSide os(this);
                     advect(st, scal);
+                    int fs[9] = {};
+                    fs[FTH] = PF_SPONGE | PF_VBC;
+                    if (moist) fs[FQV] = fs[FQC] = fs[FQR] = PF_ZERO | PF_SPONGE | PF_VBC;
+                    post(fs, 9, st, true);
                 }
                 hyd_solve(st);
                 hyd_project(st);
                 if (side) join();
                 hyd_w();
                 int fh[9] = {};
-                fh[FU] = fh[FV] = fh[FW] = fh[FTH] = PF_SPONGE | PF_VBC;  // w: the current slot
-                fh[FQV] = fh[FQC] = fh[FQR] = PF_ZERO | PF_SPONGE | PF_VBC;
+                fh[FU] = fh[FV] = fh[FW] = PF_SPONGE | PF_VBC;  // w: the current slot
+                if (!side) {
+                    fh[FTH] = PF_SPONGE | PF_VBC;
+                    fh[FQV] = fh[FQC] = fh[FQR] = PF_ZERO | PF_SPONGE | PF_VBC;
+                }
                 post(fh, 9, st, true);
                 qmask = nullptr;
                 if (s < 2) swap_inner(true);
@@ -1515,6 +1522,9 @@ class Engine : public EngineBase {
                         OnSide os(this);
                         advect(st, ADV_TH);
                         if (turbulent) turb_apply(TA_TH, st);
+                        int fs[9] = {};
+                        fs[FTH] = PF_SPONGE | PF_VBC;
+                        post(fs, 9, st, true);
                     };
                 if (fuse) poisson(st);
                 else solve_pressure(st);
@@ -1527,12 +1537,12 @@ class Engine : public EngineBase {
                     advect_ice(st);
                 }
                 if (turbulent) turb_apply(TA_Q, st);
-                if (side) join();
                 int fl[9] = {};
                 fl[FU] = fl[FV] = fl[FW] = PF_PROJECT | PF_SPONGE | PF_VBC;
-                fl[FTH] = PF_SPONGE | PF_VBC;
+                if (!side) fl[FTH] = PF_SPONGE | PF_VBC;
                 fl[FQV] = fl[FQC] = fl[FQR] = fl[FQS] = fl[FQI] = PF_ZERO | PF_SPONGE | PF_VBC;
                 post(fl, 9, st, true);
+                if (side) join();
                 if (s < 2) swap_inner(true);
                 continue;
             }
@@ -1551,17 +1561,26 @@ class Engine : public EngineBase {
                 advect(st, ADV_UV | ADV_WB | (fuse_mirror ? ADV_MIRROR : 0));
                 if (turbulent) turb_apply(TA_VEL, st);
                 unsigned char *qm = qmask;
-                mid_solve = [this, st, scal, turbulent, qm] {
+                // their column pass (sponge, top/bottom, clipping) follows on
+                // the same stream; the main stream's pass projects u, v, w
+                mid_solve = [this, st, scal, turbulent, qm, moist] {
                     fork();
                     OnSide os(this);
                     qmask = qm;
                     advect(st, scal);
                     qmask = nullptr;
                     if (turbulent) turb_apply(TA_TH | TA_Q, st);
+                    int fs[9] = {};
+                    fs[FTH] = PF_SPONGE | PF_VBC;
+                    if (moist) fs[FQV] = fs[FQC] = fs[FQR] = PF_ZERO | PF_SPONGE | PF_VBC;
+                    post(fs, 9, st, true);
                 };
                 qmask = nullptr;
                 if (fuse_mirror) poisson(st);
                 else solve_pressure(st);
+                int fl[9] = {};
+                fl[FU] = fl[FV] = fl[FW] = PF_PROJECT | PF_SPONGE | PF_VBC;
+                post(fl, 9, st, true);
                 join();
             } else {
                 advect(st, ADV_UV | ADV_WB | scal | (fuse_mirror ? ADV_MIRROR : 0));
@@ -1569,12 +1588,12 @@ class Engine : public EngineBase {
                 qmask = nullptr;
                 if (fuse_mirror) poisson(st);
                 else solve_pressure(st);
+                int fl[9] = {};
+                fl[FU] = fl[FV] = fl[FW] = PF_PROJECT | PF_SPONGE | PF_VBC;
+                fl[FTH] = PF_SPONGE | PF_VBC;
+                fl[FQV] = fl[FQC] = fl[FQR] = PF_ZERO | PF_SPONGE | PF_VBC;
+                post(fl, 9, st, true);
             }
-            int fl[9] = {};
-            fl[FU] = fl[FV] = fl[FW] = PF_PROJECT | PF_SPONGE | PF_VBC;
-            fl[FTH] = PF_SPONGE | PF_VBC;
-            fl[FQV] = fl[FQC] = fl[FQR] = PF_ZERO | PF_SPONGE | PF_VBC;
-            post(fl, 9, st, true);
             if (s < 2) swap_inner(true);
         }
         if (moist && rec) {
