@@ -141,12 +141,27 @@ class Engine : public EngineBase {
     cudaStream_t stream2 = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     bool overlap = true;
+    // the adjoint's recorded steps copy each stage's start fields to the tape
+    // on the second stream, beside the stage that only reads them
+    bool overlap_rec = true;
     std::function<void()> mid_solve;  // queued by poisson() after its first launch
     // launches inside run on the second stream (the launch helpers use `stream`)
     struct OnSide {
         Engine *e;
         explicit OnSide(Engine *x) : e(x) { std::swap(e->stream, e->stream2); }
         ~OnSide() { std::swap(e->stream, e->stream2); }
+    };
+    struct OnSideIf {
+        Engine *e;
+        bool on;
+        OnSideIf(Engine *x, bool o) : e(x), on(o)
+        {
+            if (on) std::swap(e->stream, e->stream2);
+        }
+        ~OnSideIf()
+        {
+            if (on) std::swap(e->stream, e->stream2);
+        }
     };
     void fork()
     {
@@ -282,7 +297,7 @@ class Engine : public EngineBase {
             int nsm = 0;
             cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
             overlap = c->ny <= nsm;  // kp.nj = NY blocks in the x solve
-            if (const char *ev = std::getenv("GA_OVERLAP")) overlap = std::strcmp(ev, "0") != 0;
+            if (const char *ev = std::getenv("GA_OVERLAP")) overlap_rec = overlap = std::strcmp(ev, "0") != 0;
         }
         const bool moist = c->microphysics_option >= 1;
         const bool ice = c->microphysics_option == 2;
@@ -1472,10 +1487,17 @@ class Engine : public EngineBase {
         if (turbulent) turbulence();  // driver_serial.cpp:194
         for (int s = 0; s < 3; s++) {
             const double st = steps[s];
-            if (rec)
+            // the stage-start fields to the tape: the stage reads them and
+            // writes only the forecast slots, so the copies may run beside it
+            // until the stage's end (the next stage writes these buffers)
+            const bool rec_side = rec && overlap_rec && !prof && !hyd.div && !kp.ice;
+            if (rec) {
+                if (rec_side) fork();
+                OnSideIf os(this, rec_side);
                 for (int f = 0; f < nprog; f++)
                     cudaMemcpyAsync(rec + (size_t)(nprog * s + f) * N, buf[f][ci[f]], N * sizeof(T),
                                     cudaMemcpyDeviceToDevice, stream);
+            }
             qmask = mrec ? mrec + (size_t)s * N : nullptr;
             if (hyd.div) {  // the hydrostatic set: driver_serial.cpp:208-239 with integrate_hydro
                 // theta and moisture beside the lid-pressure solve; joined
@@ -1593,6 +1615,7 @@ class Engine : public EngineBase {
                 fl[FTH] = PF_SPONGE | PF_VBC;
                 fl[FQV] = fl[FQC] = fl[FQR] = PF_ZERO | PF_SPONGE | PF_VBC;
                 post(fl, 9, st, true);
+                if (rec_side) join();
             }
             if (s < 2) swap_inner(true);
         }
