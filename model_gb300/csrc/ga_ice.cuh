@@ -44,26 +44,34 @@ __device__ __forceinline__ T ice_pressure(const KParams<T> &p, const KFields<T> 
     return (p.hydrostatic ? pv : pv / (T(RutC::cp) * p.tbv[k])) + F.bar[5][c];
 }
 
+// the pressure factor (p0/pd)^0.4 of the rain and snow fall speeds, pd the
+// dimensional pressure p0 pressure^(cp/Rd); both speeds evaluate the same
+// expression of the same pressure (rutledge.cpp:512-517, 539-545), so one
+// evaluation serves both
+template <typename T>
+__device__ __forceinline__ T rut_p04(T pressure)
+{
+    const T pd = T(RutC::p0) * pow(pressure, T(RutC::cp / RutC::Rd));
+    return pow(T(RutC::p0) / pd, T(0.4));
+}
 // calculate_rain_fall_speed_rutledge at one point (rutledge.cpp:530-555)
 template <typename T>
-__device__ __forceinline__ T rut_rain_speed(const KParams<T> &p, T qr, T pressure, int k)
+__device__ __forceinline__ T rut_rain_speed(const KParams<T> &p, T qr, T p04, int k)
 {
     if (qr > T(RutC::minvar)) {
-        const T pd = T(RutC::p0) * pow(pressure, T(RutC::cp / RutC::Rd));
         const T lambdaR = sqrt(sqrt((T(RutC::trigpi) * T(1000) * T(RutC::N0r)) / (p.rhou[k] * qr)));
-        return p.rfall / (T(6.0) * pow(lambdaR, T(0.8))) * pow(T(RutC::p0) / pd, T(0.4));
+        return p.rfall / (T(6.0) * pow(lambdaR, T(0.8))) * p04;
     }
     return T(0);
 }
 // calculate_snow_fall_speed_rutledge at one point (:503-520), with the
 // intercept the last microphysics pass left
 template <typename T>
-__device__ __forceinline__ T rut_snow_speed(const KParams<T> &p, T qs, T pressure, T n0s, int k)
+__device__ __forceinline__ T rut_snow_speed(const KParams<T> &p, T qs, T p04, T n0s, int k)
 {
     if (qs > T(RutC::minvar)) {
-        const T pd = T(RutC::p0) * pow(pressure, T(RutC::cp / RutC::Rd));
         const T lambdaS = pow((T(RutC::trigpi) * T(RutC::rhoS) * n0s) / (p.rhou[k] * qs), T(0.25));
-        return T(RutC::app) * T(1.15) * pow(lambdaS, -T(RutC::bexp)) * pow(T(RutC::p0) / pd, T(0.4));
+        return T(RutC::app) * T(1.15) * pow(lambdaS, -T(RutC::bexp)) * p04;
     }
     return T(0);
 }
@@ -102,15 +110,17 @@ __global__ void k_ice_fall(KParams<T> p, KFields<T> F, int i0, int i1, int j0, i
     const int j = j0 + (int)((t / nzi) % nj);
     const int i = i0 + (int)(t / ((long)nzi * nj));
     const long c = gix(p.ny, p.nz, i, j, k);
-    T pressure = T(0);
-    if (what & (IF_RAIN | IF_SNOW)) pressure = ice_pressure(p, F, c, k);
+    const T qr = (what & IF_RAIN) ? (from_p ? F.P[FQR] : F.cur[FQR])[c] : T(0);
+    const T qs = (what & IF_SNOW) ? (from_p ? F.P[FQS] : F.cur[FQS])[c] : T(0);
+    // the pressure factor only where a rain or snow speed needs it
+    const T p04 = (qr > T(RutC::minvar) || qs > T(RutC::minvar)) ? rut_p04(ice_pressure(p, F, c, k)) : T(0);
     if (what & IF_RAIN) {
-        const T v = rut_rain_speed(p, (from_p ? F.P[FQR] : F.cur[FQR])[c], pressure, k);
+        const T v = rut_rain_speed(p, qr, p04, k);
         F.vt[c] = v;
         if (k == 1) F.vt[c - 1] = v;
     }
     if (what & IF_SNOW) {
-        const T v = rut_snow_speed(p, (from_p ? F.P[FQS] : F.cur[FQS])[c], pressure, *F.n0s, k);
+        const T v = rut_snow_speed(p, qs, p04, *F.n0s, k);
         F.sts[c] = v;
         if (k == 1) F.sts[c - 1] = v;
     }
