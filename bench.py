@@ -708,12 +708,13 @@ def _ref_init(barrier):
     _REF_BARRIER = barrier
 
 
-def _ref_replica(steps: int):
+def _ref_replica(job):
     """one replica of the reference's serial step: build the state, wait
     for every replica, then time the steps"""
     from model_gb300 import configs
     from oracle import oracle as O
-    wl = configs.thunderstorm()
+    steps, kw = job
+    wl = configs.thunderstorm(**kw)
     o = O.Oracle(wl)
     o.step(1)  # warm-up
     _REF_BARRIER.wait()
@@ -722,27 +723,28 @@ def _ref_replica(steps: int):
     return time.perf_counter() - t0, rc
 
 
-def cpu_all_cores(steps: int):
-    """the reference's CPU step on every host core: one replica per core in
-    spawned processes, all stepping at once; aggregate gridpoint-steps/s =
-    replicas x points x steps / the slowest replica's time"""
+def cpu_all_cores(steps: int, ncores: int = 0, **kw):
+    """the reference's CPU step on every host core (or ncores): one replica
+    per core in spawned processes, all stepping at once; aggregate
+    gridpoint-steps/s = replicas x points x steps / the slowest replica's
+    time.  kw: thunderstorm settings (the full workload by default)"""
     import multiprocessing as mp
     from model_gb300 import configs
     from oracle import oracle as O
     O.build()
-    n = os.cpu_count() or 1
+    n = ncores or os.cpu_count() or 1
     ctx = mp.get_context("spawn")
     barrier = ctx.Barrier(n)
     with ctx.Pool(n, initializer=_ref_init, initargs=(barrier,)) as pool:
-        res = pool.map(_ref_replica, [steps] * n)
+        res = pool.map(_ref_replica, [(steps, kw)] * n)
     assert all(rc == 0 for _, rc in res)
     slow = max(el for el, _ in res)
-    wl = configs.thunderstorm()
+    wl = configs.thunderstorm(**kw)
     return {"value": round(n * wl.points * steps / slow, 1), "unit": UNIT, "cores": n, "kind": "port",
             "sample": f"{n} replicas (one per host core) of {steps} steps of the {wl.nx}x{wl.ny}x{wl.nz} "
                       f"workload after one warm-up step, stepping at once ({slow:.1f} s for the slowest; "
                       f"{wl.points * steps / slow:.0f} gridpoint-steps/s per core)",
-            "cpu": cpu_model()}
+            "slowest_replica_s": slow, "cpu": cpu_model()}
 
 
 def run_reference(args):

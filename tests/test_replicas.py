@@ -72,3 +72,17 @@ def test_reference_arm_prints_on_rank_zero_only():
                        capture_output=True, text=True, timeout=120)
     assert p.returncode == 0, p.stderr[-2000:]
     assert p.stdout.strip() == ""
+
+
+def test_reference_arm_aggregates_replicas_on_host_cores():
+    """the reference arm's all-core timing: spawned replicas of the serial
+    step (here 2 on a small thunderstorm), each warmed up and stepping behind
+    one barrier; the value is replicas x points x steps over the slowest"""
+    if ROOT not in sys.path:
+        sys.path.insert(0, ROOT)
+    import bench  # spawned workers import it by name
+    out = bench.cpu_all_cores(2, ncores=2, nx=20, ny=18, nz=12)
+    assert out["cores"] == 2 and out["kind"] == "port"
+    slow = out["slowest_replica_s"]
+    assert slow > 0
+    assert abs(out["value"] - 2 * 20 * 18 * 12 * 2 / slow) <= 1e-6 * out["value"]
