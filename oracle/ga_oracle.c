@@ -1802,6 +1802,16 @@ static void hyd_poisson2d(ora_state *S)
     for (long c = 0; c < (long)ni * nj; c++) S->div2d[c] = io[2 * c];
 }
 
+/* the moisture factor of hydrostatic_pressure (pressure.cpp:457-490): 1 dry;
+ * 1 + 0.61 qv - qc - qr with Kessler; less snow and ice with the ice scheme */
+static double hyd_moist(const ora_state *S, long a)
+{
+    if (!S->c.microphysics_option) return 1;
+    double m = 1. + 0.61 * S->cur[F_QV][a] - S->cur[F_QC][a] - S->cur[F_QR][a];
+    if (S->ice) m = m - S->cur[F_QS][a] - S->cur[F_QI][a];
+    return m;
+}
+
 static void op_solve_hydrostatic(ora_state *S, double step)
 {
     const int NX = S->NX, NY = S->NY, NZ = S->NZ;
@@ -1831,18 +1841,17 @@ static void op_solve_hydrostatic(ora_state *S, double step)
         D[IX2(i, NY - 1)] = D[IX2(i, NY - 2)];
     }
     hyd_poisson2d(S);
-    const int moist = S->c.microphysics_option != 0;
-    const double *QV = S->cur[F_QV], *QC = S->cur[F_QC], *QR = S->cur[F_QR], *tbv = S->tbv;
+    const double *tbv = S->tbv;
     for (int i = 1; i < NX - 1; i++) /* hydrostatic_pressure(1,NX-1,1,NY-1) */
         for (int j = 1; j < NY - 1; j++) {
             long a = IX(i, j, NZ - 2);
             PI[IX(i, j, NZ - 1)] = 0;
-            const double m0 = moist ? (1. + 0.61 * QV[a] - QC[a] - QR[a]) : 1;
+            const double m0 = hyd_moist(S, a);
             PI[a] = -0.5 * (grav / cp) * ((TH[a] * m0) / (tbv[NZ - 2] * tbv[NZ - 2])) * dzw(S, NZ - 1);
             for (int k = NZ - 3; k > 0; k--) {
                 const long u = IX(i, j, k + 1), d = IX(i, j, k);
-                const double mu_ = moist ? (1. + 0.61 * QV[u] - QC[u] - QR[u]) : 1;
-                const double md = moist ? (1. + 0.61 * QV[d] - QC[d] - QR[d]) : 1;
+                const double mu_ = hyd_moist(S, u);
+                const double md = hyd_moist(S, d);
                 const double tup = (TH[u] * mu_) / (tbv[k + 1] * tbv[k + 1]);
                 const double tdn = (TH[d] * md) / (tbv[k] * tbv[k]);
                 PI[d] = PI[u] - 0.5 * (grav / cp) * (tup + tdn) * dzw(S, k + 1);

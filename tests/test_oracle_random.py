@@ -132,3 +132,26 @@ def test_random_ice_configuration_bit_exact(seed):
         for k, f in abi.TURB_NAMES.items():
             if k in ref:
                 np.testing.assert_array_equal(o.get(f), ref[k], err_msg=f"seed {seed}: {k}")
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_random_hydrostatic_ice_bit_exact(seed):
+    """the ice scheme in the hydrostatic set (the oracle only; the library
+    builds the ice scheme for the non-hydrostatic step): the hydrostatic
+    pressure's buoyancy less snow and ice (pressure.cpp:459-475) and the ice
+    scheme's Exner pressure, against the reference's HYDROSTATIC build"""
+    wl, nsteps = _ice_case(8100 + seed)
+    wl.hydrostatic, wl.periodic_ew_boundaries, wl.turbulence_option = 1, 0, 0
+    wl.dx = wl.dy = 2000.0
+    ref = O.run_reference(wl, "run", nsteps)
+    cols = {k: ref[k] for k in abi.COLUMN_NAMES}
+    cols["f"] = ref["f"]
+    o = O.Oracle(wl, cols)
+    assert o.step(nsteps) == 0
+    checked = 0
+    for k, v in o.state().items():
+        if k in ref:
+            np.testing.assert_array_equal(v, ref[k], err_msg=f"seed {seed}: {k}")
+            assert np.isfinite(v).all(), (seed, k)
+            checked += 1
+    assert checked >= 24
