@@ -120,9 +120,9 @@ int ga_create(const ga_config *cfg, const ga_columns *cols, ga_ctx **out)
         return fail(GA_ERR_CONFIG, "ga_create: microphysics_option must be 0, 1 or 2");
     if (cfg->microphysics_option >= 1 && cfg->rain_fallout != 1 && cfg->rain_fallout != 2)
         return fail(GA_ERR_CONFIG, "ga_create: rain_fallout must be 1 or 2");
-    if (cfg->microphysics_option == 2 && (cfg->hydrostatic == 1 || cfg->linear_model == 1))
-        return fail(GA_ERR_UNSUPPORTED, "ga_create: the ice scheme is built for the nonlinear non-hydrostatic "
-                                        "equation set");
+    if (cfg->microphysics_option == 2 && cfg->linear_model == 1)
+        return fail(GA_ERR_UNSUPPORTED, "ga_create: the linearised model has no ice scheme (linear_integrate_rk3 "
+                                        "advects the vapour alone)");
     if (cfg->precision != GA_PREC_F64 && cfg->precision != GA_PREC_F32)
         return fail(GA_ERR_CONFIG, "ga_create: unknown precision");
     const int widths[] = {cfg->boundary_width_north, cfg->boundary_width_south, cfg->boundary_width_east,

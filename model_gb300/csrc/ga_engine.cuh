@@ -1502,7 +1502,10 @@ class Engine : public EngineBase {
             if (hyd.div) {  // the hydrostatic set: driver_serial.cpp:208-239 with integrate_hydro
                 // theta and moisture beside the lid-pressure solve; joined
                 // before w_velocity_LH rewrites the current w they read
-                const int scal = ADV_TH | (moist ? (ADV_Q | ADV_ZERO) : 0);
+                // with the ice scheme the moisture follows the solve (the
+                // Rutledge fall speeds read the solved Exner perturbation)
+                const bool ice = kp.ice;
+                const int scal = ADV_TH | (moist && !ice ? (ADV_Q | ADV_ZERO) : 0);
                 const bool side = overlap && !prof;
                 advect(st, ADV_UV | (side ? 0 : scal));
                 if (side) {  // with their column pass
@@ -1511,19 +1514,28 @@ class Engine : public EngineBase {
                     advect(st, scal);
                     int fs[9] = {};
                     fs[FTH] = PF_SPONGE | PF_VBC;
-                    if (moist) fs[FQV] = fs[FQC] = fs[FQR] = PF_ZERO | PF_SPONGE | PF_VBC;
+                    if (moist && !ice) fs[FQV] = fs[FQC] = fs[FQR] = PF_ZERO | PF_SPONGE | PF_VBC;
                     post(fs, 9, st, true);
                 }
                 hyd_solve(st);
                 hyd_project(st);
+                if (ice) {
+                    const bool quad = adv_quad && quad_ok(adv_qi, adv_qj) && !(adv_tma && tma_ok(adv_tmc));
+                    if (kp.rf == 1) ice_fall_euler(IF_RAIN | IF_SNOW | IF_ICE);
+                    if (quad) {
+                        advect(st, ADV_Q | ADV_ICE | ADV_ZERO);
+                    } else {
+                        advect(st, ADV_Q | ADV_ZERO);
+                        advect_ice(st);
+                    }
+                }
                 if (side) join();
                 hyd_w();
                 int fh[9] = {};
                 fh[FU] = fh[FV] = fh[FW] = PF_SPONGE | PF_VBC;  // w: the current slot
-                if (!side) {
-                    fh[FTH] = PF_SPONGE | PF_VBC;
-                    fh[FQV] = fh[FQC] = fh[FQR] = PF_ZERO | PF_SPONGE | PF_VBC;
-                }
+                if (!side) fh[FTH] = PF_SPONGE | PF_VBC;
+                if (!side || ice) fh[FQV] = fh[FQC] = fh[FQR] = PF_ZERO | PF_SPONGE | PF_VBC;
+                if (ice) fh[FQS] = fh[FQI] = PF_ZERO | PF_SPONGE | PF_VBC;
                 post(fh, 9, st, true);
                 qmask = nullptr;
                 if (s < 2) swap_inner(true);

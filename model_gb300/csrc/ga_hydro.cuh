@@ -231,7 +231,8 @@ __global__ void __launch_bounds__(HC_THREADS) k_hyd_pi(KParams<T> p, KFields<T> 
         const long col = col0 + cl;
         if (col >= ncol || k < 1 || k >= nz - 1) continue;
         const long c = gix(p.ny, nz, 1 + (int)(col / nyi), 1 + (int)(col % nyi), k);
-        const T fac = p.moist ? (T(1.) + T(0.61) * QV[c] - QC[c] - QR[c]) : T(1);
+        T fac = p.moist ? (T(1.) + T(0.61) * QV[c] - QC[c] - QR[c]) : T(1);
+        if (p.ice) fac = fac - F.cur[FQS][c] - F.cur[FQI][c];  // pressure.cpp:459-475
         g[cl * nz + k] = (TH[c] * fac) / (p.tbv[k] * p.tbv[k]);
     }
     __syncthreads();

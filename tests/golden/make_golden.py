@@ -111,6 +111,7 @@ RUN_CASES = {
     "ice_periodic": (lambda: _ice(nx=18, periodic=1), 3),
     "ice_turbulence": (lambda: _turbulent(_ice(nx=16), 1, 29.0), 3),
     "ice_diffusion": (lambda: _diffusing(_ice(nx=16, ny=15), 4, 0.004), 3),
+    "hydro_ice": (lambda: _hydro(_ice(dx=2000.0)), 3),
 }
 
 OP_NAMES = ["advect_uvw", "solve_pressure", "integrate_non_hydro", "advect_theta",

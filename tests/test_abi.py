@@ -71,7 +71,6 @@ def test_bad_config_rejected_before_device(lib):
     h = C.c_void_p()
     for change, code in [({"nx": 8}, abi.GA_ERR_CONFIG), ({"nz": 200}, abi.GA_ERR_CONFIG),
                          ({"microphysics_option": 3}, abi.GA_ERR_CONFIG),
-                         ({"microphysics_option": 2, "hydrostatic": 1}, abi.GA_ERR_UNSUPPORTED),
                          ({"microphysics_option": 2, "linear_model": 1}, abi.GA_ERR_UNSUPPORTED),
                          ({"dt": -1.0}, abi.GA_ERR_CONFIG), ({"rain_fallout": 3}, abi.GA_ERR_CONFIG),
                          ({"use_explicit_diffusion": 1, "diffusion_order": 3}, abi.GA_ERR_CONFIG),
